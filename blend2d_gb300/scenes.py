@@ -1,0 +1,503 @@
+"""Seeded synthetic render workloads serialized as blgpu command streams.
+
+The stream format is defined in include/blgpu_stream.h; every record mirrors one call of the
+reference's BLContext API (blend2d/core/context.h), so the same bytes can be replayed into the
+reference library, into the CPU oracle and into the GPU backend.
+
+The workload shapes restate the benchmark configurations this backend is measured on:
+  * ``polygons``  - 512x512 canvas, 2,000 ten-vertex polygons in 64x64 boxes, solid colours;
+  * ``curves``    - 1920x1080 canvas, 20,000 closed cubic paths with linear/radial/conic gradients;
+  * ``patterns``  - 4096x4096 canvas, 50,000 affine-transformed pattern quads (NN/BI, SrcCopy/SrcOver);
+  * ``batch``     - many independent canvases of uneven sizes (see ``batch_canvases``);
+plus ``random_mix`` - small scenes in the style of the reference's differential context tester
+(blend2d-testing/tests/bl_test_context_utilities.h:508-1223): rects, polygons, quad/cubic paths,
+all fill styles, both comp-ops, fill alpha and transforms.
+
+Randomness comes from numpy's PCG64, which is platform independent, so a (kind, seed) pair
+always serializes to the same bytes.
+"""
+
+from __future__ import annotations
+
+import math
+import struct
+
+import numpy as np
+
+MAGIC = 0x53443242
+VERSION = 1
+
+OP_END = 0
+OP_SET_COMP_OP = 1
+OP_SET_FILL_RULE = 2
+OP_SET_GLOBAL_ALPHA = 3
+OP_SET_FILL_ALPHA = 4
+OP_SET_HINT = 5
+OP_SET_TRANSFORM = 6
+OP_RESET_TRANSFORM = 7
+OP_STYLE_RGBA32 = 8
+OP_STYLE_GRADIENT = 9
+OP_STYLE_PATTERN = 10
+OP_CLEAR_ALL = 11
+OP_FILL_ALL = 12
+OP_FILL_RECT_I = 13
+OP_FILL_RECT_D = 14
+OP_FILL_BOX_D = 15
+OP_FILL_POLYGON_D = 16
+OP_FILL_PATH_D = 17
+OP_SAVE = 18
+OP_RESTORE = 19
+
+SRC_OVER, SRC_COPY = 0, 1
+NON_ZERO, EVEN_ODD = 0, 1
+LINEAR, RADIAL, CONIC = 0, 1, 2
+PAD, REPEAT, REFLECT = 0, 1, 2
+HINT_GRADIENT_QUALITY, HINT_PATTERN_QUALITY = 1, 2
+NEAREST, BILINEAR = 0, 1
+P_MOVE, P_ON, P_QUAD, P_CONIC, P_CUBIC, P_CLOSE = 0, 1, 2, 3, 4, 5
+
+
+def rgba64_from_rgba32(c: int) -> int:
+    """BLRgba64 from BLRgba32: every 8-bit channel c becomes c * 0x101 (rgba.h)."""
+    a, r, g, b = (c >> 24) & 255, (c >> 16) & 255, (c >> 8) & 255, c & 255
+    return ((a * 257) << 48) | ((r * 257) << 32) | ((g * 257) << 16) | (b * 257)
+
+
+class StreamWriter:
+    """Builds one command stream (one canvas, one frame)."""
+
+    def __init__(self, width: int, height: int):
+        self.width = int(width)
+        self.height = int(height)
+        self.images: list[np.ndarray] = []
+        self.parts: list[bytes] = []
+        self.fill_count = 0
+
+    # -- images ---------------------------------------------------------------------------------
+    def add_image(self, pixels: np.ndarray) -> int:
+        assert pixels.dtype == np.uint32 and pixels.ndim == 2
+        self.images.append(np.ascontiguousarray(pixels))
+        return len(self.images) - 1
+
+    # -- records --------------------------------------------------------------------------------
+    def _rec(self, op: int, payload: bytes = b"") -> None:
+        pad = (-len(payload)) % 8
+        self.parts.append(struct.pack("<II", op, len(payload) + pad) + payload + b"\0" * pad)
+
+    def comp_op(self, op: int):
+        self._rec(OP_SET_COMP_OP, struct.pack("<II", op, 0))
+
+    def fill_rule(self, rule: int):
+        self._rec(OP_SET_FILL_RULE, struct.pack("<II", rule, 0))
+
+    def global_alpha(self, a: float):
+        self._rec(OP_SET_GLOBAL_ALPHA, struct.pack("<d", a))
+
+    def fill_alpha(self, a: float):
+        self._rec(OP_SET_FILL_ALPHA, struct.pack("<d", a))
+
+    def hint(self, hint: int, value: int):
+        self._rec(OP_SET_HINT, struct.pack("<II", hint, value))
+
+    def transform(self, m):
+        self._rec(OP_SET_TRANSFORM, struct.pack("<6d", *m))
+
+    def reset_transform(self):
+        self._rec(OP_RESET_TRANSFORM)
+
+    def solid(self, argb32: int):
+        self._rec(OP_STYLE_RGBA32, struct.pack("<II", int(argb32) & 0xFFFFFFFF, 0))
+
+    def gradient(self, gtype: int, values, extend: int, stops, transform=None):
+        vals = list(values) + [0.0] * (6 - len(values))
+        tr = list(transform) if transform is not None else [1.0, 0.0, 0.0, 1.0, 0.0, 0.0]
+        payload = struct.pack("<IIII6d6d", gtype, extend, len(stops), 1 if transform is not None else 0, *vals, *tr)
+        for off, argb in stops:
+            payload += struct.pack("<dQ", float(off), rgba64_from_rgba32(int(argb)))
+        self._rec(OP_STYLE_GRADIENT, payload)
+
+    def pattern(self, image_index: int, extend: int = PAD, area=None, transform=None):
+        ar = list(area) if area is not None else [0, 0, 0, 0]
+        tr = list(transform) if transform is not None else [1.0, 0.0, 0.0, 1.0, 0.0, 0.0]
+        self._rec(OP_STYLE_PATTERN, struct.pack("<II4iII6d", image_index, extend, *ar,
+                                                1 if transform is not None else 0, 0, *tr))
+
+    def clear_all(self):
+        self._rec(OP_CLEAR_ALL)
+        self.fill_count += 1
+
+    def fill_all(self):
+        self._rec(OP_FILL_ALL)
+        self.fill_count += 1
+
+    def fill_rect_i(self, x, y, w, h):
+        self._rec(OP_FILL_RECT_I, struct.pack("<4i", int(x), int(y), int(w), int(h)))
+        self.fill_count += 1
+
+    def fill_rect_d(self, x, y, w, h):
+        self._rec(OP_FILL_RECT_D, struct.pack("<4d", x, y, w, h))
+        self.fill_count += 1
+
+    def fill_box_d(self, x0, y0, x1, y1):
+        self._rec(OP_FILL_BOX_D, struct.pack("<4d", x0, y0, x1, y1))
+        self.fill_count += 1
+
+    def fill_polygon(self, xy: np.ndarray):
+        xy = np.ascontiguousarray(xy, dtype="<f8").reshape(-1, 2)
+        self._rec(OP_FILL_POLYGON_D, struct.pack("<II", xy.shape[0], 0) + xy.tobytes())
+        self.fill_count += 1
+
+    def fill_path(self, cmds, xy: np.ndarray):
+        cmds = bytes(bytearray(cmds))
+        xy = np.ascontiguousarray(xy, dtype="<f8").reshape(-1, 2)
+        assert len(cmds) == xy.shape[0]
+        pad = (-len(cmds)) % 8
+        self._rec(OP_FILL_PATH_D, struct.pack("<II", len(cmds), 0) + cmds + b"\0" * pad + xy.tobytes())
+        self.fill_count += 1
+
+    def save(self):
+        self._rec(OP_SAVE)
+
+    def restore(self):
+        self._rec(OP_RESTORE)
+
+    # -- output ---------------------------------------------------------------------------------
+    def to_bytes(self) -> bytes:
+        out = [struct.pack("<6I", MAGIC, VERSION, self.width, self.height, len(self.images), 0)]
+        for img in self.images:
+            h, w = img.shape
+            raw = img.astype("<u4").tobytes()
+            out.append(struct.pack("<II", w, h) + raw + b"\0" * ((-len(raw)) % 8))
+        out.extend(self.parts)
+        out.append(struct.pack("<II", OP_END, 0))
+        return b"".join(out)
+
+
+# ------------------------------------------------------------------------------------------------
+# Random helpers
+# ------------------------------------------------------------------------------------------------
+
+def _log_uniform(rng, lo, hi, size=None):
+    return np.exp(rng.uniform(math.log(lo), math.log(hi), size))
+
+
+def _random_stops(rng, n):
+    offs = np.sort(rng.uniform(0.0, 1.0, n))
+    cols = rng.integers(0, 2**32, n, dtype=np.uint64)
+    return [(float(o), int(c)) for o, c in zip(offs, cols)]
+
+
+def premultiplied_noise(rng, w, h) -> np.ndarray:
+    """Uniform random premultiplied PRGB32 pixels: a ~ U8, each colour channel ~ U[0, a]."""
+    a = rng.integers(0, 256, (h, w), dtype=np.uint32)
+    ch = [(rng.random((h, w)) * (a + 1)).astype(np.uint32).clip(0, 255) for _ in range(3)]
+    ch = [np.minimum(c, a) for c in ch]
+    return (a << 24) | (ch[0] << 16) | (ch[1] << 8) | ch[2]
+
+
+def _cubic_path(rng, x0, y0, side, nseg):
+    """Closed path of `nseg` cubic segments with control points uniform in the bbox."""
+    pts = rng.uniform(0.0, side, (3 * nseg, 2)) + np.array([x0, y0])
+    start = pts[-1].copy()
+    cmds = [P_MOVE]
+    xy = [start]
+    for i in range(nseg):
+        c = pts[3 * i: 3 * i + 3]
+        if i == nseg - 1:
+            c = c.copy()
+            c[2] = start
+        cmds += [P_CUBIC, P_CUBIC, P_CUBIC]
+        xy += [c[0], c[1], c[2]]
+    cmds.append(P_CLOSE)
+    xy.append(start)
+    return cmds, np.array(xy)
+
+
+def _gradient_style(rng, sw: StreamWriter, x0, y0, side, kind=None):
+    kind = int(rng.integers(0, 3)) if kind is None else kind
+    stops = _random_stops(rng, int(rng.integers(2, 9)))
+    extend = int(rng.integers(0, 3))
+    if kind == LINEAR:
+        p = rng.uniform(0, side, 4) + np.array([x0, y0, x0, y0])
+        sw.gradient(LINEAR, p.tolist(), extend, stops)
+    elif kind == RADIAL:
+        c = rng.uniform(0, side, 2) + np.array([x0, y0])
+        f = rng.uniform(0, side, 2) + np.array([x0, y0])
+        sw.gradient(RADIAL, [c[0], c[1], f[0], f[1], side * 0.5, 0.0], extend, stops)
+    else:
+        c = rng.uniform(0, side, 2) + np.array([x0, y0])
+        sw.gradient(CONIC, [c[0], c[1], float(rng.uniform(0, 2 * math.pi)), 1.0], extend, stops)
+
+
+# ------------------------------------------------------------------------------------------------
+# Benchmark workloads
+# ------------------------------------------------------------------------------------------------
+
+def polygons(seed: int = 1, width: int = 512, height: int = 512, count: int = 2000, box: float = 64.0) -> StreamWriter:
+    """Opaque-black canvas, `count` random 10-vertex polygons in box x box squares, solid
+    random ARGB32 colours (premultiplied by the context), NonZero, SrcOver, identity transform."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sw = StreamWriter(width, height)
+    sw.solid(0xFF000000)
+    sw.fill_all()
+    sw.fill_rule(NON_ZERO)
+    sw.comp_op(SRC_OVER)
+    org = rng.uniform(0.0, 1.0, (count, 2)) * np.array([width - box, height - box])
+    verts = rng.uniform(0.0, box, (count, 10, 2)) + org[:, None, :]
+    cols = rng.integers(0, 2**32, count, dtype=np.uint64)
+    for i in range(count):
+        sw.solid(int(cols[i]))
+        sw.fill_polygon(verts[i])
+    return sw
+
+
+def curves(seed: int = 2, width: int = 1920, height: int = 1080, count: int = 20000) -> StreamWriter:
+    """Closed cubic paths (4-12 segments, bbox side log-uniform 8-256 px, partly outside the
+    canvas), NonZero/EvenOdd 50/50, linear/radial/conic gradients with 2-8 stops and
+    pad/repeat/reflect extend, SrcOver."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sw = StreamWriter(width, height)
+    sw.solid(0xFF000000)
+    sw.fill_all()
+    sw.comp_op(SRC_OVER)
+    for i in range(count):
+        side = float(_log_uniform(rng, 8.0, 256.0))
+        x0 = float(rng.uniform(-side * 0.5, width - side * 0.5))
+        y0 = float(rng.uniform(-side * 0.5, height - side * 0.5))
+        nseg = int(rng.integers(4, 13))
+        cmds, xy = _cubic_path(rng, x0, y0, side, nseg)
+        sw.fill_rule(int(rng.integers(0, 2)))
+        _gradient_style(rng, sw, x0, y0, side, kind=i % 3)
+        sw.fill_path(cmds, xy)
+    return sw
+
+
+def patterns(seed: int = 3, width: int = 4096, height: int = 4096, count: int = 50000,
+             image_size: int = 256, image_count: int = 8) -> StreamWriter:
+    """Affine pattern quads: image rect mapped by translate * rotate * scale about the image
+    centre, filled as a 4-point polygon with BLPattern(image, PAD, T); NN/BI and SrcCopy/SrcOver
+    50/50."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sw = StreamWriter(width, height)
+    for _ in range(image_count):
+        sw.add_image(premultiplied_noise(rng, image_size, image_size))
+    sw.solid(0xFF000000)
+    sw.fill_all()
+    sw.fill_rule(NON_ZERO)
+    half = image_size * 0.5
+    corners = np.array([[0, 0], [image_size, 0], [image_size, image_size], [0, image_size]], dtype=np.float64)
+    for _ in range(count):
+        tx, ty = rng.uniform(0, width), rng.uniform(0, height)
+        ang = rng.uniform(0, 2 * math.pi)
+        s = float(_log_uniform(rng, 0.25, 4.0))
+        c, sn = math.cos(ang) * s, math.sin(ang) * s
+        # T = translate(tx, ty) * rotate(ang) * scale(s) * translate(-half, -half), row-vector form.
+        m = [c, sn, -sn, c, tx - (c * half - sn * half), ty - (sn * half + c * half)]
+        quad = np.stack([corners[:, 0] * m[0] + corners[:, 1] * m[2] + m[4],
+                         corners[:, 0] * m[1] + corners[:, 1] * m[3] + m[5]], axis=1)
+        sw.hint(HINT_PATTERN_QUALITY, int(rng.integers(0, 2)))
+        sw.comp_op(int(rng.integers(0, 2)))
+        sw.pattern(int(rng.integers(0, image_count)), PAD, transform=m)
+        sw.fill_polygon(quad)
+    return sw
+
+
+def batch_canvases(seed: int = 4, count: int = 4096, min_side: int = 32, max_side: int = 2048,
+                   min_paths: int = 10, max_paths: int = 5000, scale: float = 1.0):
+    """Independent canvases for the batched renderer: width and height log-uniform in
+    [min_side, max_side], log-uniform path counts, each path of the polygon or cubic kind with a
+    mixed style (solid or gradient) and comp-op. `scale` shrinks path counts for quick runs."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for _ in range(count):
+        w = int(_log_uniform(rng, min_side, max_side))
+        h = int(_log_uniform(rng, min_side, max_side))
+        n = max(1, int(_log_uniform(rng, min_paths, max_paths) * scale))
+        sw = StreamWriter(w, h)
+        sw.solid(0xFF000000)
+        sw.fill_all()
+        for _ in range(n):
+            side = float(min(_log_uniform(rng, 8.0, 256.0), max(w, h)))
+            x0 = float(rng.uniform(-side * 0.25, max(w - side * 0.75, 1.0)))
+            y0 = float(rng.uniform(-side * 0.25, max(h - side * 0.75, 1.0)))
+            sw.comp_op(int(rng.integers(0, 2)))
+            sw.fill_rule(int(rng.integers(0, 2)))
+            if rng.integers(0, 2) == 0:
+                sw.solid(int(rng.integers(0, 2**32, dtype=np.uint64)))
+                sw.fill_polygon(rng.uniform(0, side, (10, 2)) + np.array([x0, y0]))
+            else:
+                _gradient_style(rng, sw, x0, y0, side)
+                cmds, xy = _cubic_path(rng, x0, y0, side, int(rng.integers(4, 13)))
+                sw.fill_path(cmds, xy)
+        out.append(sw)
+    return out
+
+
+# ------------------------------------------------------------------------------------------------
+# Differential-test scenes
+# ------------------------------------------------------------------------------------------------
+
+def random_mix(seed: int, width: int = 257, height: int = 257, count: int = 200,
+               styles=("solid", "linear", "radial", "conic", "pattern_nn", "pattern_bi"),
+               commands=("rect_i", "rect_d", "box_d", "polygon", "path_quad", "path_cubic"),
+               transforms: bool = True, alphas: bool = True) -> StreamWriter:
+    """Mixed commands/styles/comp-ops over a canvas slightly larger than the shapes' range
+    (coordinates span -30 .. size+30 like the reference tester, so clipping is exercised)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sw = StreamWriter(width, height)
+    for _ in range(3):
+        sw.add_image(premultiplied_noise(rng, int(rng.integers(5, 80)), int(rng.integers(5, 80))))
+    sw.clear_all()
+    lo_x, hi_x, lo_y, hi_y = -30.0, width + 30.0, -30.0, height + 30.0
+
+    def pt(n):
+        return np.stack([rng.uniform(lo_x, hi_x, n), rng.uniform(lo_y, hi_y, n)], axis=1)
+
+    for i in range(count):
+        sw.comp_op(int(rng.integers(0, 2)))
+        sw.fill_rule(int(rng.integers(0, 2)))
+        if alphas:
+            r = rng.integers(0, 4)
+            sw.fill_alpha(1.0 if r < 2 else (0.0 if r == 2 else float(rng.uniform())))
+        if transforms and rng.integers(0, 4) == 0:
+            a = rng.uniform(-0.5, 0.5)
+            s = rng.uniform(0.7, 1.3)
+            cx, cy = width * 0.5, height * 0.5
+            c, sn = math.cos(a) * s, math.sin(a) * s
+            sw.transform([c, sn, -sn, c, cx - (c * cx - sn * cy), cy - (sn * cx + c * cy)])
+        elif transforms:
+            sw.reset_transform()
+
+        style = styles[int(rng.integers(0, len(styles)))]
+        if style == "solid":
+            sw.solid(int(rng.integers(0, 2**32, dtype=np.uint64)))
+        elif style in ("linear", "radial", "conic"):
+            side = float(rng.uniform(20, max(width, height)))
+            x0, y0 = float(rng.uniform(lo_x, max(lo_x, hi_x - side))), float(rng.uniform(lo_y, max(lo_y, hi_y - side)))
+            _gradient_style(rng, sw, x0, y0, side, kind={"linear": LINEAR, "radial": RADIAL, "conic": CONIC}[style])
+        else:
+            sw.hint(HINT_PATTERN_QUALITY, NEAREST if style == "pattern_nn" else BILINEAR)
+            idx = int(rng.integers(0, len(sw.images)))
+            ang = rng.uniform(0, 2 * math.pi) if rng.integers(0, 2) else 0.0
+            s = float(_log_uniform(rng, 0.3, 3.0))
+            c, sn = math.cos(ang) * s, math.sin(ang) * s
+            tx, ty = rng.uniform(lo_x, hi_x), rng.uniform(lo_y, hi_y)
+            sw.pattern(idx, int(rng.integers(0, 3)), transform=[c, sn, -sn, c, tx, ty])
+
+        cmd = commands[int(rng.integers(0, len(commands)))]
+        if cmd == "rect_i":
+            x, y = rng.integers(-30, width + 30), rng.integers(-30, height + 30)
+            sw.fill_rect_i(x, y, rng.integers(1, width // 2), rng.integers(1, height // 2))
+        elif cmd == "rect_d":
+            x, y = rng.uniform(lo_x, hi_x), rng.uniform(lo_y, hi_y)
+            sw.fill_rect_d(x, y, rng.uniform(0.5, width * 0.5), rng.uniform(0.5, height * 0.5))
+        elif cmd == "box_d":
+            a, b = pt(2)
+            sw.fill_box_d(min(a[0], b[0]), min(a[1], b[1]), max(a[0], b[0]), max(a[1], b[1]))
+        elif cmd == "polygon":
+            sw.fill_polygon(pt(int(rng.integers(3, 11))))
+        elif cmd == "path_quad":
+            n = int(rng.integers(1, 6))
+            p = pt(2 * n + 1)
+            sw.fill_path([P_MOVE] + [P_QUAD, P_QUAD] * n, p)
+        else:
+            n = int(rng.integers(1, 5))
+            p = pt(3 * n + 1)
+            sw.fill_path([P_MOVE] + [P_CUBIC, P_CUBIC, P_CUBIC] * n + [P_CLOSE], np.vstack([p, p[:1]]))
+    return sw
+
+
+WORKLOADS = {
+    "polygons": polygons,
+    "curves": curves,
+    "patterns": patterns,
+}
+
+
+def edge_cases(seed: int = 7, width: int = 131, height: int = 97) -> StreamWriter:
+    """Degenerate and boundary inputs the reference tolerates: empty and zero-area shapes,
+    horizontal-only polygons, single points, shapes far outside the canvas, coordinates at the
+    canvas border, huge coordinates that need clipping, NaN vertices (rejected as invalid
+    geometry), zero alpha, fully transparent colours (DstCopy NOP), opaque colours (SrcOver ->
+    SrcCopy), collinear curves, cusps, zero-length gradients and out-of-range stop offsets."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sw = StreamWriter(width, height)
+    sw.add_image(premultiplied_noise(rng, 1, 1))
+    sw.add_image(premultiplied_noise(rng, 7, 3))
+    sw.solid(0xFF204060)
+    sw.fill_all()
+    W, H = float(width), float(height)
+    polys = [
+        np.array([[10, 10], [10, 10], [10, 10]]),                      # single point
+        np.array([[5, 20], [60, 20], [30, 20]]),                        # horizontal only
+        np.array([[0, 0], [W, 0], [W, H], [0, H]]),                     # exactly the canvas
+        np.array([[-1e6, -1e6], [1e6, -1e6], [1e6, 1e6]]),              # huge, clipped
+        np.array([[-50, 10], [-10, 80], [-30, 40]]),                    # left of the canvas
+        np.array([[W + 5, 10], [W + 50, 80], [W + 9, 40]]),             # right of the canvas
+        np.array([[10, -80], [60, -5], [30, -40]]),                     # above
+        np.array([[10, H + 3], [60, H + 90], [30, H + 40]]),            # below
+        np.array([[-20, -20], [W + 20, 30], [40, H + 20]]),             # crosses every edge
+        np.array([[0.5, 0.5], [0.75, 0.5], [0.75, 0.75]]),              # sub-pixel
+        np.array([[W - 0.25, 3], [W + 0.25, 30], [W - 0.1, 60]]),       # at the right border
+        np.array([[1, 1], [40, 40], [80, 80], [120, 120]]),             # collinear
+        np.array([[10, 10], [np.nan, 20], [30, 40]]),                   # NaN vertex
+        np.array([[30, 5], [31, 90], [32, 5], [33, 90], [34, 5]]),      # thin spikes
+    ]
+    for i, pts in enumerate(polys):
+        sw.fill_rule(i & 1)
+        sw.comp_op(SRC_OVER if i % 3 else SRC_COPY)
+        sw.solid(int(rng.integers(0, 2**32, dtype=np.uint64)))
+        sw.fill_polygon(pts.astype(np.float64))
+    # zero-alpha / transparent / opaque colours
+    sw.comp_op(SRC_OVER)
+    sw.solid(0x00000000); sw.fill_rect_d(5, 5, 50, 50)
+    sw.solid(0x00FFFFFF); sw.fill_rect_d(5, 5, 50, 50)
+    sw.solid(0xFF00FF00); sw.fill_rect_d(6.3, 7.7, 20.2, 0.4)
+    sw.fill_alpha(0.0); sw.fill_rect_i(0, 0, width, height); sw.fill_alpha(1.0)
+    sw.global_alpha(0.5); sw.solid(0x80FF0000); sw.fill_box_d(-3.5, -2.25, 40.125, 30.75); sw.global_alpha(1.0)
+    # rect edge cases
+    sw.comp_op(SRC_COPY)
+    sw.solid(0xC0112233)
+    sw.fill_rect_i(-10, -10, 5, 5)      # fully outside
+    sw.fill_rect_i(10, 10, 0, 8)        # zero width
+    sw.fill_rect_i(10, 10, -4, 8)       # negative width
+    sw.fill_rect_d(20.5, 30.5, 1e-3, 1e-3)
+    sw.fill_rect_d(W - 1.5, H - 1.5, 10, 10)
+    sw.fill_box_d(70.1, 10.9, 71.0, 60.2)   # one pixel wide, fractional
+    sw.fill_box_d(40.0, 60.0, 90.0, 61.0)   # aligned, one row
+    # curves: cusp, collinear, all-equal, huge, crossing
+    sw.comp_op(SRC_OVER)
+    curves_list = [
+        ([P_MOVE, P_CUBIC, P_CUBIC, P_CUBIC], [[10, 50], [90, 10], [10, 10], [90, 50]]),
+        ([P_MOVE, P_CUBIC, P_CUBIC, P_CUBIC], [[10, 60], [40, 60], [70, 60], [100, 60]]),
+        ([P_MOVE, P_CUBIC, P_CUBIC, P_CUBIC], [[20, 20], [20, 20], [20, 20], [20, 20]]),
+        ([P_MOVE, P_CUBIC, P_CUBIC, P_CUBIC], [[-500, -500], [5000, 100], [-3000, 900], [600, -200]]),
+        ([P_MOVE, P_QUAD, P_QUAD, P_QUAD, P_QUAD], [[0, 96], [65, -40], [130, 96], [65, 200], [0, 96]]),
+        ([P_MOVE, P_ON, P_ON, P_CLOSE, P_MOVE, P_ON, P_ON, P_CLOSE], [[5, 5], [60, 30], [20, 80], [0, 0], [70, 5], [125, 30], [85, 80], [0, 0]]),
+    ]
+    for i, (cmds, xy) in enumerate(curves_list):
+        sw.fill_rule(i & 1)
+        _gradient_style(rng, sw, 0.0, 0.0, 120.0, kind=i % 3)
+        sw.fill_path(cmds, np.array(xy, dtype=np.float64))
+    # degenerate gradients
+    sw.gradient(LINEAR, [30, 30, 30, 30], PAD, [(0.0, 0xFF0000FF), (1.0, 0xFFFF0000)])           # zero length
+    sw.fill_rect_d(0, 0, 60, 40)
+    sw.gradient(RADIAL, [50, 50, 50, 50, 0.0, 0.0], REFLECT, [(0.0, 0xFF00FF00), (1.0, 0x8000FFFF)])  # zero radius
+    sw.fill_rect_d(30, 30, 60, 40)
+    sw.gradient(LINEAR, [0, 0, 100, 0], REPEAT, [(0.5, 0xFF00FF00)])                              # single stop
+    sw.fill_rect_d(10, 60, 100, 20)
+    sw.gradient(LINEAR, [0, 0, 100, 0], PAD, [(0.0, 0x00000000), (1.0, 0x00000000)])              # all transparent
+    sw.fill_rect_d(10, 60, 100, 20)
+    sw.gradient(CONIC, [60, 45, 0.0, 1.0], PAD, [(0.0, 0xFF0000FF), (0.5, 0xFFFFFFFF), (0.5, 0xFF000000), (1.0, 0xFF00FF00)])
+    sw.fill_rect_d(20, 10, 90, 80)
+    # tiny patterns (1x1 and 7x3) with every extend mode and translation-only transforms
+    for ext in (PAD, REPEAT, REFLECT):
+        for q in (NEAREST, BILINEAR):
+            sw.hint(HINT_PATTERN_QUALITY, q)
+            sw.pattern(1, ext, transform=[1, 0, 0, 1, 3.0 * ext + 0.5 * q, 2.25 * q])
+            sw.fill_rect_d(4 + 40 * ext, 4 + 40 * q, 37.5, 33.25)
+    sw.pattern(0, REPEAT)
+    sw.fill_rect_i(100, 70, 20, 20)
+    sw.pattern(1, REFLECT, area=[2, 1, 4, 2])
+    sw.fill_rect_i(60, 70, 30, 20)
+    return sw

@@ -1,0 +1,751 @@
+/*
+ * b2d_oracle.c - oracle (test infrastructure): command-stream replay with the reference's
+ * synchronous rendering-context front end, restated from:
+ *   state & alpha        blend2d/raster/rastercontext.cpp:1919-2027, :4380-4415
+ *   transforms           blend2d/raster/rastercontext.cpp:740-800, blend2d/core/matrix.cpp:292-324
+ *   style resolution     blend2d/raster/rastercontext.cpp:363-494, :572-695, :1231-1453
+ *   comp-op simplify     blend2d/core/compopsimplifyimpl_p.h:86-162
+ *   fetch-data setup     blend2d/pipeline/pipedefs.cpp:17-699
+ *   gradient info/stops  blend2d/core/gradient.cpp:58-173, :202-287
+ *   fill dispatch        blend2d/raster/rastercontext.cpp:2633-2990, :3317-3500
+ *   band height          blend2d/raster/rastercontext.cpp:4154-4193
+ */
+#include "b2d_oracle_p.h"
+#include "blgpu_stream.h"
+
+/* ============================================================================================
+ * Fetch-data setup
+ * ============================================================================================ */
+
+static void o_init_pattern_simple(OStyle* st, uint32_t extend, int tx, int ty, int fractional, int base_is_fxfy) {
+  uint32_t ex = extend, ey = extend;   /* simple extend modes only */
+  int rx = 0, ry = 0;
+  if (st->src_w <= 1) ex = 0;
+  if (st->src_h <= 1) ey = 0;
+  if (ex >= 1) {
+    int is_reflect = ex == 2;
+    rx = st->src_w << is_reflect;
+    if ((unsigned)tx >= (unsigned)rx) tx %= rx;
+    if (tx < 0) tx += rx;
+    if (fractional) ex = 1;
+  }
+  st->vx_stride0 = st->src_stride;
+  st->vx_stride1 = 0;
+  st->vx_ystop0 = st->src_h;
+  st->vx_ystop1 = 0;
+  st->vx_y_rewind = 0;
+  st->vx_ptr_rewind = (ey != 1 ? 0 : (intptr_t)(st->src_h - 1)) * st->src_stride;
+  if (ey >= 1) {
+    ry = st->src_h << (ey == 2);
+    if ((unsigned)ty >= (unsigned)ry) ty %= ry;
+    if (ty < 0) ty += ry;
+    st->vx_stride1 = (ey == 1) ? st->src_stride : -st->src_stride;
+    st->vx_ystop1 = st->src_h;
+    st->vx_y_rewind = (uintptr_t)st->src_h;
+  }
+  st->pat_tx = tx; st->pat_ty = ty; st->pat_rx = rx; st->pat_ry = ry;
+  if (base_is_fxfy) st->fetch_type = ex == 0 ? O_FT_PAT_FXFY_PAD : O_FT_PAT_FXFY_ROR;
+  else st->fetch_type = ex == 0 ? O_FT_PAT_ALIGNED_PAD : (ex == 1 ? O_FT_PAT_ALIGNED_REPEAT : O_FT_PAT_ALIGNED_ROR);
+}
+
+static void o_init_pattern_fx_fy(OStyle* st, uint32_t extend, uint32_t quality, int64_t tx64, int64_t ty64) {
+  int fxfy = 0;
+  uint32_t wx = (uint32_t)(tx64 & 0xFF), wy = (uint32_t)(ty64 & 0xFF);
+  int tx = -(int)(tx64 >> 8), ty = -(int)(ty64 >> 8);
+  int fractional = (wx | wy) != 0;
+  if (fractional) {
+    if (quality == 0) {
+      tx -= (wx >= 128);
+      ty -= (wy >= 128);
+      fractional = 0;
+    }
+    else {
+      st->pat_wa = ((wy) * (wx)) >> 8;
+      st->pat_wb = ((wy) * (256 - wx) + 255) >> 8;
+      st->pat_wc = ((256 - wy) * (wx)) >> 8;
+      st->pat_wd = ((256 - wy) * (256 - wx) + 255) >> 8;
+      tx--;
+      ty--;
+      fxfy = 1;
+    }
+  }
+  o_init_pattern_simple(st, extend, tx, ty, fractional, fxfy);
+}
+
+static int o_is_near(double x, double y) { return fabs(x - y) <= 1e-14; }
+
+/* init_pattern_affine (pipedefs.cpp:162-381). Returns 0 when the pattern is a NOP. */
+static int o_init_pattern_affine(OStyle* st, uint32_t extend, uint32_t quality, const OMat* transform) {
+  OMat inv;
+  if (!o_mat_invert(&inv, transform)) return 0;
+  int tw = st->src_w, th = st->src_h;
+  if (tw == 0) return 0;
+
+  double xx = inv.m00, xy = inv.m01, yx = inv.m10, yy = inv.m11;
+  if (o_is_near(xx, 1.0) & (fabs(xy) <= 1e-14) & (fabs(yx) <= 1e-14) & o_is_near(yy, 1.0)) {
+    int64_t tx64 = o_floor_to_int64(-inv.m20 * 256.0);
+    int64_t ty64 = o_floor_to_int64(-inv.m21 * 256.0);
+    o_init_pattern_fx_fy(st, extend, quality, tx64, ty64);
+    return 1;
+  }
+
+  st->fetch_type = quality == 0 ? O_FT_PAT_AFFINE_NN : O_FT_PAT_AFFINE_BI;
+  uint32_t ex = extend, ey = extend;
+  double tx = inv.m20, ty = inv.m21;
+  tx += 0.5 * (xx + yx);
+  ty += 0.5 * (xy + yy);
+  double fp_scale = 4294967296.0;
+  int ox = INT32_MAX, oy = INT32_MAX, rx = 0, ry = 0;
+
+  st->af_minx = 0; st->af_miny = 0;
+  st->af_maxx = tw - 1; st->af_maxy = th - 1;
+  st->af_corx = tw - 1; st->af_cory = th - 1;
+
+  if (ex != 0) {
+    st->af_minx = INT32_MIN;
+    if (ex == 1) st->af_corx = 0;
+    ox = tw;
+    if (ex == 2) tw *= 2;
+    if (xx < 0.0) {
+      xx = -xx; yx = -yx; tx = (double)tw - tx;
+      if (ex == 1) { ox = 0; st->af_corx = st->af_maxx; st->af_maxx = -1; }
+    }
+    ox--;
+  }
+  if (ey != 0) {
+    st->af_miny = INT32_MIN;
+    if (ey == 1) st->af_cory = 0;
+    oy = th;
+    if (ey == 2) th *= 2;
+    if (xy < 0.0) {
+      xy = -xy; yy = -yy; ty = (double)th - ty;
+      if (ey == 1) { oy = 0; st->af_cory = st->af_maxy; st->af_maxy = -1; }
+    }
+    oy--;
+  }
+  if (quality != 0) { tx -= 0.5; ty -= 0.5; }
+
+  double tw_d = (double)tw, th_d = (double)th;
+  if (ex == 0) tw_d = 2147483647.0;
+  else { tx = fmod(tx, tw_d); rx = tw; if (xx >= tw_d) xx = fmod(xx, tw_d); }
+  if (ey == 0) th_d = 2147483647.0;
+  else { ty = fmod(ty, th_d); ry = th; if (xy >= th_d) xy = fmod(xy, th_d); }
+
+  xx *= fp_scale; xy *= fp_scale; yx *= fp_scale; yy *= fp_scale; tx *= fp_scale; ty *= fp_scale;
+
+  double all_min = o_min(o_min(yy, yx), o_min(xy, xx));
+  double all_max = o_max(o_max(xx, xy), o_max(yx, yy));
+  all_min = o_min(all_min, o_min(ty, tx));
+  all_max = o_max(o_max(tx, ty), all_max);
+  if (all_min >= (double)(INT64_MIN + 1) && all_max <= (double)INT64_MAX) {
+    st->af_xx = (uint64_t)o_floor_to_int64(xx); st->af_xy = (uint64_t)o_floor_to_int64(xy);
+    st->af_yx = (uint64_t)o_floor_to_int64(yx); st->af_yy = (uint64_t)o_floor_to_int64(yy);
+    st->af_tx = (uint64_t)o_floor_to_int64(tx); st->af_ty = (uint64_t)o_floor_to_int64(ty);
+  }
+  else {
+    st->af_xx = st->af_xy = st->af_yx = st->af_yy = st->af_tx = st->af_ty = 0;
+  }
+  st->af_rx = rx; st->af_ry = ry;
+  st->af_ox = ox; st->af_oy = oy;
+  st->af_tw = (int32_t)tw_d; st->af_th = (int32_t)th_d;
+  return 1;
+}
+
+typedef struct { double offset; uint64_t rgba; } OGStop;
+
+static int o_init_gradient(OStyle* st, uint32_t type, uint32_t extend, const double* v, const OMat* transform) {
+  OMat inv;
+  uint32_t lut_size = st->lut_size;
+  if (type == 0) {   /* linear (pipedefs.cpp:386-434) */
+    if (!o_mat_invert(&inv, transform)) return 0;
+    uint32_t maxi = extend == 2 ? lut_size * 2u - 1u : lut_size - 1u;
+    uint32_t rori = extend == 2 ? maxi : 0u;
+    double ax = v[2] - v[0], ay = v[3] - v[1];
+    double dist = ax * ax + ay * ay;
+    OPt m = o_mat_map(transform, v[0], v[1]);
+    double ox = 0.5 - m.x, oy = 0.5 - m.y;
+    double dt = ax * inv.m00 + ay * inv.m01;
+    double dy = ax * inv.m10 + ay * inv.m11;
+    double scale = (double)(int64_t)((uint64_t)lut_size << 32) / dist;
+    double offset = ox * dt + oy * dy;
+    dt *= scale; dy *= scale; offset *= scale;
+    st->lin_dy = (uint64_t)o_floor_to_int64(dy);
+    st->lin_dt = (uint64_t)o_floor_to_int64(dt);
+    st->lin_pt0 = (uint64_t)o_floor_to_int64(offset);
+    st->maxi = maxi; st->rori = rori;
+    st->fetch_type = extend != 0 ? O_FT_LINEAR_ROR : O_FT_LINEAR_PAD;
+    return 1;
+  }
+  if (type == 1) {   /* radial (pipedefs.cpp:480-576) */
+    if (!o_mat_invert(&inv, transform)) return 0;
+    uint32_t maxi = extend == 2 ? lut_size * 2u - 1u : lut_size - 1u;
+    uint32_t rori = extend == 2 ? maxi : 0u;
+    st->maxi = maxi; st->rori = rori;
+    OPt cp = { v[0], v[1] }, fp = { v[2], v[3] };
+    double cr = v[4], fr = v[5];
+    OPt dp = { cp.x - fp.x, cp.y - fp.y };
+    double dr = cr - fr;
+    double sq_dx_plus_dy = dp.x * dp.x + dp.y * dp.y;
+    double dx_plus_dy = sqrt(sq_dx_plus_dy);
+    double dist_from_border = fabs(dx_plus_dy - dr);
+    const double dist_limit = 0.5;
+    if (dist_from_border < dist_limit) {
+      OPt dp0 = { (dp.x * (dr - dist_limit)) / dx_plus_dy, (dp.y * (dr - dist_limit)) / dx_plus_dy };
+      OPt dp1 = { (dp.x * (dr + dist_limit)) / dx_plus_dy, (dp.y * (dr + dist_limit)) / dx_plus_dy };
+      double d0 = fabs(dp0.x * dp0.x + dp0.y * dp0.y - sq_dx_plus_dy);
+      double d1 = fabs(dp1.x * dp1.x + dp1.y * dp1.y - sq_dx_plus_dy);
+      dp = (d0 < d1) ? dp0 : dp1;
+      fp.x = cp.x - dp.x; fp.y = cp.y - dp.y;
+      sq_dx_plus_dy = dp.x * dp.x + dp.y * dp.y;
+    }
+    double a = dr * dr - sq_dx_plus_dy;
+    double sq_fr = fr * fr;
+    double scale = (double)lut_size;
+    double xx = inv.m00, xy = inv.m01, yx = inv.m10, yy = inv.m11;
+    OPt tp = { inv.m20 + (xx + xy) * 0.5 - fp.x, inv.m21 + (yx + yy) * 0.5 - fp.y };
+    st->rad_tx = tp.x; st->rad_ty = tp.y; st->rad_yx = yx; st->rad_yy = yy;
+    double a_mul_4 = a * 4.0;
+    double inv2a = (scale * 0.5) / a;
+    double sq_inv2a = inv2a * inv2a;
+    st->rad_amul4 = a_mul_4; st->rad_inv2a = inv2a; st->rad_sq_inv2a = sq_inv2a; st->rad_sq_fr = sq_fr;
+    double sq_xx_plus_sq_yx = xx * xx + xy * xy;
+    double b0 = 2.0 * (dr * fr + tp.x * dp.x + tp.y * dp.y);
+    double bx = 2.0 * (dp.x * xx + dp.y * xy);
+    double by = 2.0 * (dp.x * yx + dp.y * yy);
+    st->rad_b0 = -b0; st->rad_by = -by;
+    double bx_mul_2 = bx * 2.0;
+    double sq_bx = bx * bx;
+    double dd0 = sq_bx + bx_mul_2 * b0 + a_mul_4 * (sq_xx_plus_sq_yx + 2.0 * (tp.x * xx + tp.y * xy));
+    double ddy = bx_mul_2 * by + a_mul_4 * (2.0 * (xx * yx + yy * xy));
+    double ddd_half = (sq_bx + a_mul_4 * sq_xx_plus_sq_yx);
+    double ddd_half_inv = ddd_half * sq_inv2a;
+    st->rad_dd0 = dd0 - ddd_half;
+    st->rad_ddy = ddy;
+    st->rad_bd = (float)(-bx * inv2a);
+    st->rad_ddd = (float)ddd_half_inv;
+    st->fetch_type = extend != 0 ? O_FT_RADIAL_ROR : O_FT_RADIAL_PAD;
+    return 1;
+  }
+  /* conic (pipedefs.cpp:614-671) */
+  {
+    static const double q256[4] = { 4.071421038552e+1, -1.311160794048e+1, 6.017670215625, -1.623253505085 };
+    const double kPI_MUL_2 = 6.28318530717958647692;
+    double angle = v[2], repeat = v[3];
+    OPt c = o_mat_map(transform, v[0], v[1]);
+    c.x = 0.5 - c.x; c.y = 0.5 - c.y;
+    OPt vv = { 1.0 * transform->m00 + 0.0 * transform->m10, 1.0 * transform->m01 + 0.0 * transform->m11 };
+    double matrix_angle = atan2(vv.y, vv.x);
+    /* updated_transform = transform.rotate(-matrix_angle, c) (matrix.cpp:292-324) */
+    OMat u = *transform;
+    {
+      double ang = -matrix_angle;
+      double as = sin(ang), ac = cos(ang);
+      double t00 = as * u.m10 + ac * u.m00;
+      double t01 = as * u.m11 + ac * u.m01;
+      double t10 = ac * u.m10 - as * u.m00;
+      double t11 = ac * u.m11 - as * u.m01;
+      double px = c.x, py = c.y;
+      double ttx = px - ac * px + as * py;
+      double tty = py - as * px - ac * py;
+      double t20 = ttx * u.m00 + tty * u.m10 + u.m20;
+      double t21 = ttx * u.m01 + tty * u.m11 + u.m21;
+      u.m20 = t20; u.m21 = t21;
+      u.m00 = t00; u.m01 = t01; u.m10 = t10; u.m11 = t11;
+    }
+    angle += matrix_angle;
+    double fr = angle / -kPI_MUL_2;
+    double off = fr - floor(fr);
+    if (off != 0.0) off = -1.0 + off;
+    if (!o_mat_invert(&inv, &u)) return 0;
+    st->con_tx = c.x * inv.m00 + c.y * inv.m10;
+    st->con_ty = c.x * inv.m01 + c.y * inv.m11;
+    st->con_yx = inv.m10;
+    st->con_yy = inv.m11;
+    double lutSizeD = (double)(int)lut_size;
+    double repeated = lutSizeD * repeat;
+    double qScale = repeated / 256.0;
+    for (int k = 0; k < 4; k++) st->con_q[k] = (float)(q256[k] * qScale);
+    st->con_n1 = (float)repeated;
+    st->con_n2 = (float)(repeated * 0.5);
+    st->con_n4 = (float)(repeated * 0.25);
+    st->con_offset = (float)(off * repeated - 0.5);
+    st->con_xx = (float)inv.m00;
+    st->con_maxi = INT32_MAX;
+    st->con_rori = (int32_t)(lut_size - 1u);
+    st->fetch_type = O_FT_CONIC;
+    return 1;
+  }
+}
+
+/* Gradient stop analysis & normalization (gradient.cpp:58-173). Returns the kept count or -1. */
+static int o_normalize_stops(OGStop* dst, const BLGpuStreamGradientStop* src, int n) {
+  uint32_t result = 0, was_same = 0;
+  double prev = -1.0;
+  for (int i = 0; i < n; i++) {
+    double offset = src[i].offset;
+    if (!((offset >= 0.0) & (offset <= 1.0))) return -1;
+    uint32_t is_same = (offset == prev);
+    result |= (offset < prev);
+    result |= is_same & was_same;
+    was_same = is_same;
+    prev = offset;
+  }
+  if (result == 0 || n == 0) {
+    for (int i = 0; i < n; i++) { dst[i].offset = src[i].offset; dst[i].rgba = src[i].rgba64; }
+    return n;
+  }
+  /* stable sort by offset, then drop the middle of 3+ equal offsets */
+  int* idx = (int*)malloc(sizeof(int) * (size_t)n);
+  for (int i = 0; i < n; i++) idx[i] = i;
+  for (int i = 1; i < n; i++) {
+    int v = idx[i], j = i;
+    while (j > 0 && (src[idx[j - 1]].offset > src[v].offset)) { idx[j] = idx[j - 1]; j--; }
+    idx[j] = v;
+  }
+  int j = 0;
+  double prev1 = -1.0, prev2 = -1.0;
+  for (int i = 0; i < n - 1; i++) {
+    double offset = src[idx[i]].offset;
+    uint64_t rgba = src[idx[i]].rgba64;
+    j -= (int)((prev1 == prev2) & (prev2 == offset));
+    dst[j].offset = offset;
+    dst[j].rgba = rgba;
+    j++;
+    prev1 = prev2;
+    prev2 = offset;
+  }
+  free(idx);
+  return j;
+}
+
+/* ============================================================================================
+ * Context
+ * ============================================================================================ */
+
+typedef struct {
+  int comp_op, fill_rule;
+  double global_alpha, fill_alpha;
+  uint32_t global_alpha_i, fill_alpha_i;
+  uint32_t gradient_quality, pattern_quality;
+  OMat user, final_t, final_fixed;
+  int final_type, final_fixed_type;
+  int integral_translation, tx_i, ty_i;
+  OStyle style;
+} OState;
+
+typedef struct {
+  int w, h;
+  uint32_t* pixels;
+  uint32_t lut_variant;
+  OState s;
+  OState* stack; int nstack, cap_stack;
+  OEdgeStorage storage;
+  OEdgeBuilder eb;
+  OFillCtx fc;
+  const uint32_t** images; const int* iw; const int* ih;
+  B2DOracleStats* stats;
+} OCtx;
+
+static void on_transform_changed(OCtx* c) {   /* rastercontext.cpp:741-800 */
+  OState* s = &c->s;
+  OMat id = { 1, 0, 0, 1, 0, 0 };
+  o_mat_multiply(&s->final_t, &s->user, &id);
+  s->final_fixed = s->final_t;
+  s->final_fixed.m00 *= 256.0; s->final_fixed.m01 *= 256.0;
+  s->final_fixed.m10 *= 256.0; s->final_fixed.m11 *= 256.0;
+  s->final_fixed.m20 *= 256.0; s->final_fixed.m21 *= 256.0;
+  s->final_type = o_mat_type(&s->final_t);
+  s->final_fixed_type = s->final_type > O_TT_SCALE ? s->final_type : O_TT_SCALE;
+  s->integral_translation = 0;
+  if (s->final_type <= O_TT_TRANSLATE) {
+    double mn = floor((double)(INT32_MIN + 1) * 256.0);
+    double mx = floor((double)(INT32_MAX - 1 - (c->w > c->h ? c->w : c->h)) * 256.0);
+    const OMat* ft = &s->final_fixed;
+    if (ft->m20 >= mn && ft->m20 <= mx && ft->m21 >= mn && ft->m21 <= mx) {
+      int64_t tx64 = o_floor_to_int64(ft->m20), ty64 = o_floor_to_int64(ft->m21);
+      if (((tx64 | ty64) & 0xFF) == 0) {
+        s->tx_i = (int)(tx64 >> 8);
+        s->ty_i = (int)(ty64 >> 8);
+        s->integral_translation = 1;
+      }
+    }
+  }
+}
+
+static void set_style_solid(OCtx* c, uint32_t rgba32) {
+  OStyle* st = &c->s.style;
+  st->nop = 0;
+  st->fetch_type = O_FT_SOLID;
+  st->solid = o_premultiply(rgba32);
+  st->format = rgba32 == 0 ? O_FMT_ZERO32 : (rgba32 >= 0xFF000000u ? O_FMT_FRGB32 : O_FMT_PRGB32);
+}
+
+static void set_style_gradient(OCtx* c, const uint8_t* p) {
+  BLGpuStreamGradient g;
+  memcpy(&g, p, sizeof(g));
+  OStyle* st = &c->s.style;
+  memset(st, 0, sizeof(*st));
+  BLGpuStreamGradientStop* raw = (BLGpuStreamGradientStop*)malloc(sizeof(BLGpuStreamGradientStop) * (g.stop_count + 1));
+  memcpy(raw, p + sizeof(g), sizeof(BLGpuStreamGradientStop) * g.stop_count);
+  OGStop* stops = (OGStop*)malloc(sizeof(OGStop) * (g.stop_count + 1));
+  int n = o_normalize_stops(stops, raw, (int)g.stop_count);
+  if (n < 0) n = 0;   /* assign_stops failed: the gradient keeps no stops */
+
+  /* transform = gradient.transform x final_transform when the gradient has one */
+  OMat tf = c->s.final_t;
+  if (g.has_transform) {
+    OMat gm = { g.transform[0], g.transform[1], g.transform[2], g.transform[3], g.transform[4], g.transform[5] };
+    if (o_mat_type(&gm) != O_TT_IDENTITY) o_mat_multiply(&tf, &gm, &c->s.final_t);
+  }
+
+  if (n == 0) { st->nop = 1; goto done; }
+
+  /* ensure_info (gradient.cpp:202-287) */
+  {
+    uint32_t flags = 0;
+    uint64_t prev = stops[0].rgba & 0xFF00FF00FF00FF00ull;
+    if (prev < 0xFF00000000000000ull) flags |= 1;
+    if (prev > 0x00FFFFFFFFFFFFFFull) flags |= 2;
+    for (int i = 1; i < n; i++) {
+      uint64_t v = stops[i].rgba & 0xFF00FF00FF00FF00ull;
+      if (v == prev) continue;
+      flags |= 4;
+      if (v < 0xFF00000000000000ull) flags |= 1;
+      if (v > 0x00FFFFFFFFFFFFFFull) flags |= 2;
+      prev = v;
+    }
+    if (!(flags & 2)) flags &= ~4u;
+    uint32_t lut_size;
+    if (!(flags & 4)) lut_size = 256;
+    else if (n == 1) lut_size = 256;
+    else if (n == 2) lut_size = (stops[1].offset - stops[0].offset >= 0.998) ? 256 : 512;
+    else if (n == 3) lut_size = (stops[0].offset <= 0.002 && stops[1].offset == 0.5 && stops[2].offset >= 0.998) ? 512 : 1024;
+    else lut_size = 1024;
+    st->format = (flags & 1) ? O_FMT_PRGB32 : O_FMT_FRGB32;
+    if (!(flags & 4)) {
+      uint64_t v = stops[n - 1].rgba;
+      uint32_t c32 = (uint32_t)(((v >> 56) & 0xFF) << 24 | ((v >> 40) & 0xFF) << 16 | ((v >> 24) & 0xFF) << 8 | ((v >> 8) & 0xFF));
+      st->fetch_type = O_FT_SOLID;
+      st->solid = o_premultiply(c32);
+      goto done;
+    }
+    st->lut_size = lut_size;
+    b2d_oracle_build_lut(st->lut, lut_size, stops, (size_t)n, c->lut_variant);
+    if (!o_init_gradient(st, g.type, g.extend_mode, g.values, &tf)) st->nop = 1;
+  }
+done:
+  free(raw);
+  free(stops);
+}
+
+static void set_style_pattern(OCtx* c, const uint8_t* p) {
+  BLGpuStreamPattern pt;
+  memcpy(&pt, p, sizeof(pt));
+  OStyle* st = &c->s.style;
+  memset(st, 0, sizeof(*st));
+  int iw = c->iw[pt.image_index], ih = c->ih[pt.image_index];
+  int ax = 0, ay = 0, aw = iw, ah = ih;
+  if (pt.area[2] > 0) { ax = pt.area[0]; ay = pt.area[1]; aw = pt.area[2]; ah = pt.area[3]; }
+  st->format = O_FMT_PRGB32;
+  if (!aw || !ah) { st->nop = 1; return; }
+  st->src = c->images[pt.image_index] + (intptr_t)ay * iw + ax;
+  st->src_w = aw; st->src_h = ah; st->src_stride = iw;
+
+  OMat tf = c->s.final_t;
+  if (pt.has_transform) {
+    OMat pm = { pt.transform[0], pt.transform[1], pt.transform[2], pt.transform[3], pt.transform[4], pt.transform[5] };
+    if (o_mat_type(&pm) != O_TT_IDENTITY) o_mat_multiply(&tf, &pm, &c->s.final_t);
+  }
+  if (!o_init_pattern_affine(st, pt.extend_mode, c->s.pattern_quality, &tf)) st->nop = 1;
+}
+
+/* Resolve the fill: returns 0 for NOP, else sets comp-op (0/1) and alpha. */
+static int resolve_fill(OCtx* c, int* comp_op, uint32_t* alpha) {
+  OState* s = &c->s;
+  if (s->global_alpha_i == 0 || s->fill_alpha_i == 0 || s->style.nop) return 0;
+  int op = s->comp_op;
+  if (op == 0) {   /* SrcOver simplification for a PRGB32 destination */
+    if (s->style.format == O_FMT_ZERO32) return 0;        /* DstCopy */
+    if (s->style.format == O_FMT_FRGB32) op = 1;          /* SrcCopy */
+  }
+  *comp_op = op;
+  *alpha = s->fill_alpha_i;
+  return 1;
+}
+
+static void fill_box_a(OCtx* c, int x0, int y0, int x1, int y1) {
+  if (c->stats) c->stats->fill_calls++;
+  o_fill_box_a(&c->fc, x0, y0, x1, y1);
+}
+
+static void fill_clipped_box_f(OCtx* c, int x0, int y0, int x1, int y1) {
+  if (((x0 | y0 | x1 | y1) & 0xFF) == 0) { fill_box_a(c, x0 >> 8, y0 >> 8, x1 >> 8, y1 >> 8); return; }
+  if (c->stats) c->stats->fill_calls++;
+  o_fill_box_u(&c->fc, x0, y0, x1, y1);
+}
+
+static void fill_edges(OCtx* c, uint32_t fill_rule) {
+  if (c->storage.nedges == 0 || c->storage.bbox_y0 >= c->storage.bbox_y1) return;
+  if (c->stats) { c->stats->fill_calls++; c->stats->edge_points += c->storage.npts; }
+  o_fill_analytic(&c->fc, &c->storage, fill_rule);
+}
+
+static void fill_polygon(OCtx* c, const double* xy, size_t n, uint32_t rule, const OMat* m, int ttype) {
+  o_storage_clear(&c->storage);
+  o_eb_begin(&c->eb);
+  if (o_eb_add_poly(&c->eb, xy, n, m, ttype) == 0) {
+    o_eb_done(&c->eb);
+    fill_edges(c, rule);
+  }
+}
+
+static void fill_box_d(OCtx* c, double bx0, double by0, double bx1, double by1) {
+  OState* s = &c->s;
+  const OMat* t = &s->final_fixed;
+  if (s->final_fixed_type <= O_TT_SWAP) {
+    double x0 = bx0 * t->m00 + by0 * t->m10 + t->m20;
+    double y0 = bx0 * t->m01 + by0 * t->m11 + t->m21;
+    double x1 = bx1 * t->m00 + by1 * t->m10 + t->m20;
+    double y1 = bx1 * t->m01 + by1 * t->m11 + t->m21;
+    double mx0 = o_min(x0, x1), my0 = o_min(y0, y1), mx1 = o_max(x0, x1), my1 = o_max(y0, y1);
+    /* Geometry::intersect with the fixed clip box */
+    double cx1 = (double)c->w * 256.0, cy1 = (double)c->h * 256.0;
+    double ix0 = o_max(mx0, 0.0), iy0 = o_max(my0, 0.0), ix1 = o_min(mx1, cx1), iy1 = o_min(my1, cy1);
+    if (!((ix0 < ix1) & (iy0 < iy1))) return;
+    int ux0 = o_trunc_to_int(ix0), uy0 = o_trunc_to_int(iy0), ux1 = o_trunc_to_int(ix1), uy1 = o_trunc_to_int(iy1);
+    if (ux0 >= ux1 || uy0 >= uy1) return;
+    fill_clipped_box_f(c, ux0, uy0, ux1, uy1);
+  }
+  else {
+    double poly[8] = { bx0, by0, bx1, by0, bx1, by1, bx0, by1 };
+    fill_polygon(c, poly, 4, 1 /* EVEN_ODD */, t, s->final_fixed_type);
+  }
+}
+
+static int replay(OCtx* c, const uint8_t* base, size_t size, size_t off) {
+  while (off + 8 <= size) {
+    uint32_t op, len;
+    memcpy(&op, base + off, 4);
+    memcpy(&len, base + off + 4, 4);
+    const uint8_t* p = base + off + 8;
+    if (off + 8 + len > size) return -1;
+    off += 8 + (size_t)len;
+    if (op == BLGPU_OP_END) break;
+    OState* s = &c->s;
+    int cop; uint32_t alpha;
+
+    switch (op) {
+      case BLGPU_OP_SET_COMP_OP: { uint32_t v; memcpy(&v, p, 4); s->comp_op = (int)v; break; }
+      case BLGPU_OP_SET_FILL_RULE: { uint32_t v; memcpy(&v, p, 4); s->fill_rule = (int)v; break; }
+      case BLGPU_OP_SET_GLOBAL_ALPHA: {
+        double a; memcpy(&a, p, 8);
+        if (isnan(a)) break;
+        a = o_clamp(a, 0.0, 1.0);
+        double ia = a * 255.0;
+        s->global_alpha = a;
+        s->global_alpha_i = (uint32_t)o_round_to_int(ia);
+        s->fill_alpha_i = (uint32_t)o_round_to_int(ia * s->fill_alpha);
+        break;
+      }
+      case BLGPU_OP_SET_FILL_ALPHA: {
+        double a; memcpy(&a, p, 8);
+        if (isnan(a)) break;
+        a = o_clamp(a, 0.0, 1.0);
+        s->fill_alpha = a;
+        s->fill_alpha_i = (uint32_t)o_round_to_int(s->global_alpha * 255.0 * a);
+        break;
+      }
+      case BLGPU_OP_SET_HINT: {
+        uint32_t h, v; memcpy(&h, p, 4); memcpy(&v, p + 4, 4);
+        if (h == BLGPU_HINT_GRADIENT_QUALITY) s->gradient_quality = v;
+        else if (h == BLGPU_HINT_PATTERN_QUALITY) s->pattern_quality = v;
+        break;
+      }
+      case BLGPU_OP_SET_TRANSFORM: {
+        double m[6]; memcpy(m, p, sizeof(m));
+        s->user.m00 = m[0]; s->user.m01 = m[1]; s->user.m10 = m[2]; s->user.m11 = m[3]; s->user.m20 = m[4]; s->user.m21 = m[5];
+        on_transform_changed(c);
+        break;
+      }
+      case BLGPU_OP_RESET_TRANSFORM: {
+        OMat id = { 1, 0, 0, 1, 0, 0 };
+        s->user = id;
+        on_transform_changed(c);
+        break;
+      }
+      case BLGPU_OP_STYLE_RGBA32: { uint32_t v; memcpy(&v, p, 4); set_style_solid(c, v); break; }
+      case BLGPU_OP_STYLE_GRADIENT: set_style_gradient(c, p); break;
+      case BLGPU_OP_STYLE_PATTERN: set_style_pattern(c, p); break;
+
+      case BLGPU_OP_CLEAR_ALL: {
+        OStyle clear_style;
+        memset(&clear_style, 0, sizeof(clear_style));
+        clear_style.fetch_type = O_FT_SOLID;
+        c->fc.style = &clear_style;
+        c->fc.comp_op = 1;
+        c->fc.alpha = 255;
+        fill_box_a(c, 0, 0, c->w, c->h);
+        break;
+      }
+      case BLGPU_OP_FILL_ALL:
+        if (!resolve_fill(c, &cop, &alpha)) break;
+        c->fc.style = &s->style; c->fc.comp_op = cop; c->fc.alpha = alpha;
+        fill_box_a(c, 0, 0, c->w, c->h);
+        break;
+
+      case BLGPU_OP_FILL_RECT_I: {
+        int32_t r[4]; memcpy(r, p, sizeof(r));
+        if (!resolve_fill(c, &cop, &alpha)) break;
+        c->fc.style = &s->style; c->fc.comp_op = cop; c->fc.alpha = alpha;
+        if (!s->integral_translation) {
+          if ((r[2] <= 0) | (r[3] <= 0)) break;
+          fill_box_d(c, (double)r[0], (double)r[1], (double)r[0] + (double)r[2], (double)r[1] + (double)r[3]);
+        }
+        else {
+          int64_t x0 = (int64_t)r[0] + s->tx_i, y0 = (int64_t)r[1] + s->ty_i;
+          int64_t x1 = (int64_t)r[2] + x0, y1 = (int64_t)r[3] + y0;
+          x0 = x0 < 0 ? 0 : x0; y0 = y0 < 0 ? 0 : y0;
+          x1 = x1 > c->w ? c->w : x1; y1 = y1 > c->h ? c->h : y1;
+          if ((x0 >= x1) | (y0 >= y1)) break;
+          fill_box_a(c, (int)x0, (int)y0, (int)x1, (int)y1);
+        }
+        break;
+      }
+      case BLGPU_OP_FILL_RECT_D: {
+        double r[4]; memcpy(r, p, sizeof(r));
+        if (!resolve_fill(c, &cop, &alpha)) break;
+        c->fc.style = &s->style; c->fc.comp_op = cop; c->fc.alpha = alpha;
+        fill_box_d(c, r[0], r[1], r[0] + r[2], r[1] + r[3]);
+        break;
+      }
+      case BLGPU_OP_FILL_BOX_D: {
+        double b[4]; memcpy(b, p, sizeof(b));
+        if (!resolve_fill(c, &cop, &alpha)) break;
+        c->fc.style = &s->style; c->fc.comp_op = cop; c->fc.alpha = alpha;
+        fill_box_d(c, b[0], b[1], b[2], b[3]);
+        break;
+      }
+      case BLGPU_OP_FILL_POLYGON_D: {
+        uint32_t n; memcpy(&n, p, 4);
+        if (c->stats) c->stats->input_vertices += n;
+        if (!resolve_fill(c, &cop, &alpha)) break;
+        if (n < 3) break;
+        c->fc.style = &s->style; c->fc.comp_op = cop; c->fc.alpha = alpha;
+        double* xy = (double*)malloc(sizeof(double) * 2 * n);
+        memcpy(xy, p + 8, sizeof(double) * 2 * n);
+        fill_polygon(c, xy, n, (uint32_t)s->fill_rule, &s->final_fixed, s->final_fixed_type);
+        free(xy);
+        break;
+      }
+      case BLGPU_OP_FILL_PATH_D: {
+        uint32_t n; memcpy(&n, p, 4);
+        if (c->stats) c->stats->input_vertices += n;
+        if (!resolve_fill(c, &cop, &alpha)) break;
+        if (n == 0) break;
+        c->fc.style = &s->style; c->fc.comp_op = cop; c->fc.alpha = alpha;
+        const uint8_t* cmd = p + 8;
+        double* xy = (double*)malloc(sizeof(double) * 2 * n);
+        memcpy(xy, cmd + ((n + 7u) & ~7u), sizeof(double) * 2 * n);
+        o_storage_clear(&c->storage);
+        o_eb_begin(&c->eb);
+        if (o_eb_add_path(&c->eb, cmd, xy, n, &s->final_fixed, s->final_fixed_type) == 0) {
+          o_eb_done(&c->eb);
+          fill_edges(c, (uint32_t)s->fill_rule);
+        }
+        free(xy);
+        break;
+      }
+      case BLGPU_OP_SAVE:
+        if (c->nstack == c->cap_stack) {
+          c->cap_stack = c->cap_stack ? c->cap_stack * 2 : 8;
+          c->stack = (OState*)realloc(c->stack, sizeof(OState) * (size_t)c->cap_stack);
+        }
+        c->stack[c->nstack++] = *s;
+        break;
+      case BLGPU_OP_RESTORE:
+        if (c->nstack) *s = c->stack[--c->nstack];
+        break;
+      default:
+        return -2;
+    }
+  }
+  return 0;
+}
+
+static int default_band_height(int w) {   /* calculate_band_height, thread_count = 0 */
+  int bh = 64;
+  size_t pixel_count = (size_t)(unsigned)w * (size_t)bh;
+  do {
+    if (pixel_count * 4u <= 1024u * 256u) break;
+    bh >>= 1;
+    pixel_count >>= 1;
+  } while (bh > 8);
+  return bh;
+}
+
+int b2d_oracle_render(const uint8_t* stream, size_t size, uint32_t* out, const B2DOracleOptions* opt, B2DOracleStats* stats) {
+  if (size < sizeof(BLGpuStreamHeader)) return -1;
+  BLGpuStreamHeader hdr;
+  memcpy(&hdr, stream, sizeof(hdr));
+  if (hdr.magic != BLGPU_STREAM_MAGIC || hdr.version != BLGPU_STREAM_VERSION) return -1;
+
+  OCtx c;
+  memset(&c, 0, sizeof(c));
+  c.w = (int)hdr.width;
+  c.h = (int)hdr.height;
+  c.pixels = out;
+  c.lut_variant = opt ? opt->lut_variant : B2D_ORACLE_LUT_SSE2;
+  c.stats = stats;
+  if (stats) memset(stats, 0, sizeof(*stats));
+  memset(out, 0, (size_t)c.w * (size_t)c.h * 4u);
+
+  size_t off = sizeof(hdr);
+  const uint32_t** images = (const uint32_t**)calloc(hdr.image_count + 1, sizeof(void*));
+  int* iw = (int*)calloc(hdr.image_count + 1, sizeof(int));
+  int* ih = (int*)calloc(hdr.image_count + 1, sizeof(int));
+  uint32_t** owned = (uint32_t**)calloc(hdr.image_count + 1, sizeof(void*));
+  for (uint32_t i = 0; i < hdr.image_count; i++) {
+    BLGpuStreamImage im;
+    memcpy(&im, stream + off, sizeof(im));
+    off += sizeof(im);
+    size_t n = (size_t)im.width * im.height;
+    owned[i] = (uint32_t*)malloc(n * 4u + 4u);
+    memcpy(owned[i], stream + off, n * 4u);
+    images[i] = owned[i];
+    iw[i] = (int)im.width; ih[i] = (int)im.height;
+    off += (n * 4u + 7u) & ~(size_t)7;
+  }
+  c.images = images; c.iw = iw; c.ih = ih;
+
+  /* default state (rastercontext.cpp:4380-4415) */
+  c.s.comp_op = 0; c.s.fill_rule = 0;
+  c.s.global_alpha = 1.0; c.s.fill_alpha = 1.0; c.s.global_alpha_i = 255; c.s.fill_alpha_i = 255;
+  c.s.gradient_quality = 0; c.s.pattern_quality = 1;
+  OMat id = { 1, 0, 0, 1, 0, 0 };
+  c.s.user = id;
+  on_transform_changed(&c);
+  set_style_solid(&c, 0xFF000000u);
+
+  int bh = (opt && opt->band_height) ? (int)opt->band_height : default_band_height(c.w);
+  o_storage_init(&c.storage, c.w, c.h, bh);
+  double tol = 0.20 * 256.0;
+  o_eb_init(&c.eb, &c.storage, c.w, c.h, tol * tol);
+
+  size_t required_width = (((size_t)c.w + 1u + 4u) + 3u) & ~(size_t)3u;
+  c.fc.dst = out; c.fc.width = c.w; c.fc.height = c.h; c.fc.stride = c.w;
+  c.fc.cell_stride = required_width;
+  c.fc.bit_stride = ((required_width / 4u) + 63u) / 64u;
+  c.fc.cells = (uint32_t*)calloc((size_t)bh * c.fc.cell_stride, 4);
+  c.fc.bits = (uint64_t*)calloc((size_t)bh * c.fc.bit_stride, 8);
+  c.fc.stats = stats;
+
+  int rc = replay(&c, stream, size, off);
+
+  free(c.fc.cells); free(c.fc.bits);
+  o_eb_free(&c.eb);
+  o_storage_free(&c.storage);
+  free(c.stack);
+  for (uint32_t i = 0; i < hdr.image_count; i++) free(owned[i]);
+  free(owned); free(images); free(iw); free(ih);
+  return rc;
+}

@@ -1,0 +1,228 @@
+// ref_replay.cpp - replays a blgpu command stream (include/blgpu_stream.h) into the reference
+// Blend2D BLContext and writes the resulting PRGB32 pixels.
+//
+// Test infrastructure: built by oracle/ref.mk against the reference sources (never shipped).
+// Every record maps 1:1 onto the reference C++ API (blend2d/core/context.h:2155-2700).
+//
+//   b2d_replay_<variant> <stream.bin> <out.raw|-> [--threads N] [--frames K]
+//
+// With --frames K the stream is rendered K+1 times (one warm-up) and the median wall time of
+// `begin -> all calls -> end()` is printed as JSON on stdout.
+
+#include <blend2d/blend2d.h>
+#include <blgpu_stream.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+static std::vector<uint8_t> read_file(const char* path) {
+  std::vector<uint8_t> buf;
+  FILE* f = fopen(path, "rb");
+  if (!f) { fprintf(stderr, "cannot open %s\n", path); exit(2); }
+  fseek(f, 0, SEEK_END);
+  long n = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  buf.resize(size_t(n));
+  if (n && fread(buf.data(), 1, size_t(n), f) != size_t(n)) { fprintf(stderr, "short read\n"); exit(2); }
+  fclose(f);
+  return buf;
+}
+
+struct Stream {
+  const uint8_t* base = nullptr;
+  size_t size = 0;
+  BLGpuStreamHeader hdr {};
+  std::vector<BLImage> images;
+  size_t records_offset = 0;
+};
+
+static void parse_header(Stream& s) {
+  memcpy(&s.hdr, s.base, sizeof(s.hdr));
+  if (s.hdr.magic != BLGPU_STREAM_MAGIC || s.hdr.version != BLGPU_STREAM_VERSION) {
+    fprintf(stderr, "bad stream header\n");
+    exit(2);
+  }
+  size_t off = sizeof(BLGpuStreamHeader);
+  for (uint32_t i = 0; i < s.hdr.image_count; i++) {
+    BLGpuStreamImage ih;
+    memcpy(&ih, s.base + off, sizeof(ih));
+    off += sizeof(ih);
+    BLImage img(int(ih.width), int(ih.height), BL_FORMAT_PRGB32);
+    BLImageData d;
+    img.make_mutable(&d);
+    for (uint32_t y = 0; y < ih.height; y++)
+      memcpy(static_cast<uint8_t*>(d.pixel_data) + intptr_t(y) * d.stride, s.base + off + size_t(y) * ih.width * 4u, size_t(ih.width) * 4u);
+    off += (size_t(ih.width) * ih.height * 4u + 7u) & ~size_t(7);
+    s.images.push_back(img);
+  }
+  s.records_offset = off;
+}
+
+template<typename T>
+static T rd(const uint8_t* p) { T v; memcpy(&v, p, sizeof(T)); return v; }
+
+static void replay(const Stream& s, BLImage& img, uint32_t threads) {
+  BLImageData d;
+  img.make_mutable(&d);
+  for (int y = 0; y < d.size.h; y++)
+    memset(static_cast<uint8_t*>(d.pixel_data) + intptr_t(y) * d.stride, 0, size_t(d.size.w) * 4u);
+
+  BLContextCreateInfo cci {};
+  cci.thread_count = threads;
+  BLContext ctx(img, cci);
+
+  std::vector<BLPoint> pts;
+  size_t off = s.records_offset;
+  while (off + 8 <= s.size) {
+    uint32_t op = rd<uint32_t>(s.base + off);
+    uint32_t len = rd<uint32_t>(s.base + off + 4);
+    const uint8_t* p = s.base + off + 8;
+    off += 8 + len;
+    if (op == BLGPU_OP_END)
+      break;
+
+    switch (op) {
+      case BLGPU_OP_SET_COMP_OP: ctx.set_comp_op(BLCompOp(rd<uint32_t>(p))); break;
+      case BLGPU_OP_SET_FILL_RULE: ctx.set_fill_rule(BLFillRule(rd<uint32_t>(p))); break;
+      case BLGPU_OP_SET_GLOBAL_ALPHA: ctx.set_global_alpha(rd<double>(p)); break;
+      case BLGPU_OP_SET_FILL_ALPHA: ctx.set_fill_alpha(rd<double>(p)); break;
+      case BLGPU_OP_SET_HINT: ctx.set_hint(BLContextHint(rd<uint32_t>(p)), rd<uint32_t>(p + 4)); break;
+      case BLGPU_OP_SET_TRANSFORM: {
+        double m[6];
+        memcpy(m, p, sizeof(m));
+        ctx.set_transform(BLMatrix2D(m[0], m[1], m[2], m[3], m[4], m[5]));
+        break;
+      }
+      case BLGPU_OP_RESET_TRANSFORM: ctx.reset_transform(); break;
+      case BLGPU_OP_STYLE_RGBA32: ctx.set_fill_style(BLRgba32(rd<uint32_t>(p))); break;
+      case BLGPU_OP_STYLE_GRADIENT: {
+        BLGpuStreamGradient g = rd<BLGpuStreamGradient>(p);
+        std::vector<BLGradientStop> stops(g.stop_count);
+        for (uint32_t i = 0; i < g.stop_count; i++) {
+          BLGpuStreamGradientStop st = rd<BLGpuStreamGradientStop>(p + sizeof(g) + i * sizeof(st));
+          stops[i] = BLGradientStop(st.offset, BLRgba64(st.rgba64));
+        }
+        BLGradient grad;
+        if (g.type == BLGPU_GRADIENT_LINEAR)
+          grad.create(BLLinearGradientValues(g.values[0], g.values[1], g.values[2], g.values[3]), BLExtendMode(g.extend_mode));
+        else if (g.type == BLGPU_GRADIENT_RADIAL)
+          grad.create(BLRadialGradientValues(g.values[0], g.values[1], g.values[2], g.values[3], g.values[4], g.values[5]), BLExtendMode(g.extend_mode));
+        else
+          grad.create(BLConicGradientValues(g.values[0], g.values[1], g.values[2], g.values[3]), BLExtendMode(g.extend_mode));
+        grad.assign_stops(stops.data(), stops.size());
+        if (g.has_transform)
+          grad.set_transform(BLMatrix2D(g.transform[0], g.transform[1], g.transform[2], g.transform[3], g.transform[4], g.transform[5]));
+        ctx.set_fill_style(grad);
+        break;
+      }
+      case BLGPU_OP_STYLE_PATTERN: {
+        BLGpuStreamPattern pt = rd<BLGpuStreamPattern>(p);
+        const BLImage& src = s.images[pt.image_index];
+        BLPattern pat;
+        if (pt.area[2] > 0)
+          pat.create(src, BLRectI(pt.area[0], pt.area[1], pt.area[2], pt.area[3]), BLExtendMode(pt.extend_mode));
+        else
+          pat.create(src, BLExtendMode(pt.extend_mode));
+        if (pt.has_transform)
+          pat.set_transform(BLMatrix2D(pt.transform[0], pt.transform[1], pt.transform[2], pt.transform[3], pt.transform[4], pt.transform[5]));
+        ctx.set_fill_style(pat);
+        break;
+      }
+      case BLGPU_OP_CLEAR_ALL: ctx.clear_all(); break;
+      case BLGPU_OP_FILL_ALL: ctx.fill_all(); break;
+      case BLGPU_OP_FILL_RECT_I: {
+        int32_t r[4];
+        memcpy(r, p, sizeof(r));
+        ctx.fill_rect(BLRectI(r[0], r[1], r[2], r[3]));
+        break;
+      }
+      case BLGPU_OP_FILL_RECT_D: {
+        double r[4];
+        memcpy(r, p, sizeof(r));
+        ctx.fill_rect(BLRect(r[0], r[1], r[2], r[3]));
+        break;
+      }
+      case BLGPU_OP_FILL_BOX_D: {
+        double b[4];
+        memcpy(b, p, sizeof(b));
+        ctx.fill_box(BLBox(b[0], b[1], b[2], b[3]));
+        break;
+      }
+      case BLGPU_OP_FILL_POLYGON_D: {
+        uint32_t n = rd<uint32_t>(p);
+        pts.resize(n);
+        memcpy(pts.data(), p + 8, size_t(n) * sizeof(BLPoint));
+        ctx.fill_polygon(pts.data(), n);
+        break;
+      }
+      case BLGPU_OP_FILL_PATH_D: {
+        uint32_t n = rd<uint32_t>(p);
+        const uint8_t* cmds = p + 8;
+        const uint8_t* xy = cmds + ((n + 7u) & ~7u);
+        BLPath path;
+        uint8_t* cmd_out;
+        BLPoint* vtx_out;
+        path.modify_op(BL_MODIFY_OP_ASSIGN_GROW, n, &cmd_out, &vtx_out);
+        memcpy(cmd_out, cmds, n);
+        memcpy(vtx_out, xy, size_t(n) * sizeof(BLPoint));
+        ctx.fill_path(path);
+        break;
+      }
+      case BLGPU_OP_SAVE: ctx.save(); break;
+      case BLGPU_OP_RESTORE: ctx.restore(); break;
+      default:
+        fprintf(stderr, "unknown op %u\n", op);
+        exit(2);
+    }
+  }
+  ctx.end();
+}
+
+int main(int argc, char** argv) {
+  if (argc < 3) {
+    fprintf(stderr, "usage: %s stream.bin out.raw|- [--threads N] [--frames K]\n", argv[0]);
+    return 2;
+  }
+  uint32_t threads = 0;
+  int frames = 0;
+  for (int i = 3; i + 1 < argc; i += 2) {
+    if (!strcmp(argv[i], "--threads")) threads = uint32_t(atoi(argv[i + 1]));
+    else if (!strcmp(argv[i], "--frames")) frames = atoi(argv[i + 1]);
+  }
+
+  std::vector<uint8_t> buf = read_file(argv[1]);
+  Stream s;
+  s.base = buf.data();
+  s.size = buf.size();
+  parse_header(s);
+
+  BLImage img(int(s.hdr.width), int(s.hdr.height), BL_FORMAT_PRGB32);
+  replay(s, img, threads);
+
+  if (frames > 0) {
+    std::vector<double> ms;
+    for (int f = 0; f < frames; f++) {
+      auto t0 = std::chrono::steady_clock::now();
+      replay(s, img, threads);
+      auto t1 = std::chrono::steady_clock::now();
+      ms.push_back(std::chrono::duration<double, std::milli>(t1 - t0).count());
+    }
+    std::sort(ms.begin(), ms.end());
+    printf("{\"frames\": %d, \"threads\": %u, \"median_ms\": %.4f, \"min_ms\": %.4f}\n", frames, threads, ms[ms.size() / 2], ms[0]);
+  }
+
+  if (strcmp(argv[2], "-") != 0) {
+    BLImageData d;
+    img.get_data(&d);
+    FILE* f = fopen(argv[2], "wb");
+    for (int y = 0; y < d.size.h; y++)
+      fwrite(static_cast<const uint8_t*>(d.pixel_data) + intptr_t(y) * d.stride, 1, size_t(d.size.w) * 4u, f);
+    fclose(f);
+  }
+  return 0;
+}
