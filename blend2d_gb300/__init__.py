@@ -1,0 +1,322 @@
+"""blend2d_gb300 - a GB300 (sm_103a) raster backend for Blend2D's fill pipeline.
+
+The product is `_build/libblgpu.so` (C ABI declared in include/blgpu.h). This module is a thin
+ctypes mirror of that ABI with the reference's vocabulary (BLContext-like calls, BLResult codes).
+There is no CPU fallback: if the library is missing, importing the bindings raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import struct
+import threading
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_build", "libblgpu.so")
+
+# BLResult codes (blend2d/core/api.h)
+SUCCESS = 0
+ERROR_OUT_OF_MEMORY = 0x00010000
+ERROR_INVALID_VALUE = 0x00010001
+ERROR_INVALID_STATE = 0x00010002
+ERROR_NOT_IMPLEMENTED = 0x00010007
+ERROR_NO_STATES_TO_RESTORE = 0x00010038
+ERROR_DEVICE = 0x00011000
+
+FORMAT_PRGB32 = 1
+IMAGE_DEVICE_MEMORY = 1
+FLUSH_SYNC = 0x80000000
+LUT_SSE2, LUT_AVX2, LUT_SCALAR = 0, 1, 2
+
+COMP_OP_SRC_OVER, COMP_OP_SRC_COPY = 0, 1
+FILL_RULE_NON_ZERO, FILL_RULE_EVEN_ODD = 0, 1
+HINT_RENDERING_QUALITY, HINT_GRADIENT_QUALITY, HINT_PATTERN_QUALITY = 0, 1, 2
+GRADIENT_LINEAR, GRADIENT_RADIAL, GRADIENT_CONIC = 0, 1, 2
+EXTEND_PAD, EXTEND_REPEAT, EXTEND_REFLECT = 0, 1, 2
+PATH_MOVE, PATH_ON, PATH_QUAD, PATH_CONIC, PATH_CUBIC, PATH_CLOSE = 0, 1, 2, 3, 4, 5
+
+
+class BLGpuError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        super().__init__(f"{what} failed with BLResult 0x{code:08x}")
+        self.code = code
+
+
+class RuntimeCreateInfo(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("lut_variant", ctypes.c_uint32), ("cuda_stream", ctypes.c_void_p),
+                ("reserved", ctypes.c_uint32 * 4)]
+
+
+class Image(ctypes.Structure):
+    _fields_ = [("pixel_data", ctypes.c_void_p), ("stride", ctypes.c_ssize_t), ("width", ctypes.c_int32),
+                ("height", ctypes.c_int32), ("format", ctypes.c_uint32), ("flags", ctypes.c_uint32)]
+
+
+class GradientStop(ctypes.Structure):
+    _fields_ = [("offset", ctypes.c_double), ("rgba64", ctypes.c_uint64)]
+
+
+class Gradient(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_uint32), ("extend_mode", ctypes.c_uint32), ("values", ctypes.c_double * 6),
+                ("stops", ctypes.POINTER(GradientStop)), ("stop_count", ctypes.c_size_t),
+                ("transform", ctypes.POINTER(ctypes.c_double))]
+
+
+class Pattern(ctypes.Structure):
+    _fields_ = [("image", ctypes.POINTER(Image)), ("area", ctypes.c_int32 * 4), ("extend_mode", ctypes.c_uint32),
+                ("transform", ctypes.POINTER(ctypes.c_double))]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("frames", ctypes.c_uint64), ("fill_commands", ctypes.c_uint64), ("segments", ctypes.c_uint64),
+                ("tiles", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("last_gpu_ms", ctypes.c_double),
+                ("last_fine_ms", ctypes.c_double)]
+
+
+_P = ctypes.c_void_p
+_U32 = ctypes.c_uint32
+_D = ctypes.c_double
+_SIGNATURES = {
+    "blgpu_runtime_create": [ctypes.POINTER(_P), ctypes.POINTER(RuntimeCreateInfo)],
+    "blgpu_runtime_destroy": [_P],
+    "blgpu_runtime_get_stats": [_P, ctypes.POINTER(Stats)],
+    "blgpu_runtime_replay": [_P, ctypes.c_int],
+    "blgpu_runtime_synchronize": [_P],
+    "blgpu_context_create": [ctypes.POINTER(_P), _P],
+    "blgpu_context_destroy": [_P],
+    "blgpu_context_begin": [_P, ctypes.POINTER(Image)],
+    "blgpu_context_end": [_P],
+    "blgpu_context_flush": [_P, _U32],
+    "blgpu_context_save": [_P],
+    "blgpu_context_restore": [_P],
+    "blgpu_context_set_comp_op": [_P, _U32],
+    "blgpu_context_set_fill_rule": [_P, _U32],
+    "blgpu_context_set_global_alpha": [_P, _D],
+    "blgpu_context_set_fill_alpha": [_P, _D],
+    "blgpu_context_set_hint": [_P, _U32, _U32],
+    "blgpu_context_set_transform": [_P, ctypes.POINTER(ctypes.c_double)],
+    "blgpu_context_reset_transform": [_P],
+    "blgpu_context_set_fill_style_rgba32": [_P, _U32],
+    "blgpu_context_set_fill_style_gradient": [_P, ctypes.POINTER(Gradient)],
+    "blgpu_context_set_fill_style_pattern": [_P, ctypes.POINTER(Pattern)],
+    "blgpu_context_clear_all": [_P],
+    "blgpu_context_fill_all": [_P],
+    "blgpu_context_fill_rect_i": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32],
+    "blgpu_context_fill_rect_d": [_P, _D, _D, _D, _D],
+    "blgpu_context_fill_box_d": [_P, _D, _D, _D, _D],
+    "blgpu_context_fill_polygon_d": [_P, _P, ctypes.c_size_t],
+    "blgpu_context_fill_path_d": [_P, _P, _P, ctypes.c_size_t],
+    "blgpu_context_submit_stream": [_P, ctypes.c_char_p, ctypes.c_size_t],
+    "blgpu_render_batch": [_P, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(Image),
+                           _U32],
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Loads libblgpu.so (raises if it has not been built: there is no fallback path)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(path):
+                raise RuntimeError(f"{path} is missing: build it with `python -m blend2d_gb300.build`")
+            lib = ctypes.CDLL(path)
+            for name, args in _SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.argtypes = args
+                fn.restype = ctypes.c_uint32
+            _lib = lib
+        return _lib
+
+
+def _check(code: int, what: str):
+    if code != SUCCESS:
+        raise BLGpuError(code, what)
+
+
+def _mat(m):
+    if m is None:
+        return None
+    arr = (ctypes.c_double * 6)(*[float(v) for v in m])
+    return arr
+
+
+def make_image(target) -> tuple[Image, object]:
+    """BLGpuImage for a (h, w) uint32 numpy array (host) or torch tensor (host or CUDA)."""
+    if isinstance(target, np.ndarray):
+        if target.dtype != np.uint32 or target.ndim != 2 or not target.flags["C_CONTIGUOUS"]:
+            raise ValueError("target must be a C-contiguous (h, w) uint32 array")
+        h, w = target.shape
+        return Image(target.ctypes.data, w * 4, w, h, FORMAT_PRGB32, 0), target
+    import torch  # device images come from torch tensors
+    if not isinstance(target, torch.Tensor) or target.dim() != 2 or target.element_size() != 4:
+        raise ValueError("target must be a 2-D 32-bit tensor")
+    if not target.is_contiguous():
+        raise ValueError("target tensor must be contiguous")
+    h, w = target.shape
+    flags = IMAGE_DEVICE_MEMORY if target.is_cuda else 0
+    return Image(target.data_ptr(), w * 4, w, h, FORMAT_PRGB32, flags), target
+
+
+class Runtime:
+    """One device, one stream, the device memory of the pipeline (BLGpuRuntime)."""
+
+    def __init__(self, device: int = 0, lut_variant: int = LUT_SSE2, cuda_stream: int | None = None):
+        self._lib = load_library()
+        info = RuntimeCreateInfo(device, lut_variant, cuda_stream or None)
+        h = _P()
+        _check(self._lib.blgpu_runtime_create(ctypes.byref(h), ctypes.byref(info)), "blgpu_runtime_create")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self._lib.blgpu_runtime_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def stats(self) -> Stats:
+        s = Stats()
+        _check(self._lib.blgpu_runtime_get_stats(self.handle, ctypes.byref(s)), "blgpu_runtime_get_stats")
+        return s
+
+    def replay(self, use_graph: bool = True):
+        _check(self._lib.blgpu_runtime_replay(self.handle, int(use_graph)), "blgpu_runtime_replay")
+
+    def synchronize(self):
+        _check(self._lib.blgpu_runtime_synchronize(self.handle), "blgpu_runtime_synchronize")
+
+    def render_batch(self, streams: list[bytes], targets: list) -> None:
+        """Renders each stream into its target (numpy or torch image) in one device pipeline."""
+        n = len(streams)
+        imgs = (Image * n)()
+        keep = []
+        for i, t in enumerate(targets):
+            imgs[i], k = make_image(t)
+            keep.append(k)
+        ptrs = (ctypes.c_char_p * n)(*streams)
+        sizes = (ctypes.c_size_t * n)(*[len(s) for s in streams])
+        _check(self._lib.blgpu_render_batch(self.handle, ptrs, sizes, imgs, n), "blgpu_render_batch")
+
+
+class Context:
+    """Rendering context bound to one PRGB32 image (BLContext, synchronous mode)."""
+
+    def __init__(self, runtime: Runtime, target=None):
+        self.rt = runtime
+        self._lib = runtime._lib
+        h = _P()
+        _check(self._lib.blgpu_context_create(ctypes.byref(h), runtime.handle), "blgpu_context_create")
+        self.handle = h
+        self._keep = []
+        if target is not None:
+            self.begin(target)
+
+    def _call(self, name, *args):
+        _check(getattr(self._lib, name)(self.handle, *args), name)
+
+    def begin(self, target):
+        img, keep = make_image(target)
+        self._img = img
+        self._keep = [keep]
+        self._call("blgpu_context_begin", ctypes.byref(img))
+
+    def end(self):
+        self._call("blgpu_context_end")
+        self._keep = []
+
+    def flush(self, flags: int = FLUSH_SYNC):
+        self._call("blgpu_context_flush", flags)
+        self._keep = self._keep[:1]
+
+    def close(self):
+        if self.handle:
+            self._lib.blgpu_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def save(self): self._call("blgpu_context_save")
+    def restore(self): self._call("blgpu_context_restore")
+    def set_comp_op(self, op): self._call("blgpu_context_set_comp_op", op)
+    def set_fill_rule(self, rule): self._call("blgpu_context_set_fill_rule", rule)
+    def set_global_alpha(self, a): self._call("blgpu_context_set_global_alpha", a)
+    def set_fill_alpha(self, a): self._call("blgpu_context_set_fill_alpha", a)
+    def set_hint(self, hint, value): self._call("blgpu_context_set_hint", hint, value)
+    def set_transform(self, m): self._call("blgpu_context_set_transform", _mat(m))
+    def reset_transform(self): self._call("blgpu_context_reset_transform")
+    def set_fill_style_rgba32(self, argb32): self._call("blgpu_context_set_fill_style_rgba32", argb32 & 0xFFFFFFFF)
+
+    def set_fill_style_gradient(self, type, values, stops, extend_mode=EXTEND_PAD, transform=None):
+        """stops: iterable of (offset, rgba64)."""
+        st = (GradientStop * max(len(stops), 1))(*[GradientStop(float(o), int(c)) for o, c in stops])
+        vals = list(values) + [0.0] * (6 - len(values))
+        m = _mat(transform)
+        g = Gradient(type, extend_mode, (ctypes.c_double * 6)(*vals), st, len(stops),
+                     ctypes.cast(m, ctypes.POINTER(ctypes.c_double)) if m is not None else None)
+        self._call("blgpu_context_set_fill_style_gradient", ctypes.byref(g))
+
+    def set_fill_style_pattern(self, image, area=(0, 0, 0, 0), extend_mode=EXTEND_REPEAT, transform=None):
+        img, keep = make_image(image)
+        self._keep.append((img, keep))
+        m = _mat(transform)
+        p = Pattern(ctypes.pointer(img), (ctypes.c_int32 * 4)(*area), extend_mode,
+                    ctypes.cast(m, ctypes.POINTER(ctypes.c_double)) if m is not None else None)
+        self._call("blgpu_context_set_fill_style_pattern", ctypes.byref(p))
+
+    def clear_all(self): self._call("blgpu_context_clear_all")
+    def fill_all(self): self._call("blgpu_context_fill_all")
+    def fill_rect_i(self, x, y, w, h): self._call("blgpu_context_fill_rect_i", x, y, w, h)
+    def fill_rect_d(self, x, y, w, h): self._call("blgpu_context_fill_rect_d", x, y, w, h)
+    def fill_box_d(self, x0, y0, x1, y1): self._call("blgpu_context_fill_box_d", x0, y0, x1, y1)
+
+    def fill_polygon_d(self, xy):
+        a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
+        self._call("blgpu_context_fill_polygon_d", a.ctypes.data, a.shape[0])
+
+    def fill_path_d(self, cmds, xy):
+        c = np.ascontiguousarray(cmds, dtype=np.uint8)
+        a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
+        if c.shape[0] != a.shape[0]:
+            raise ValueError("one command per vertex")
+        self._call("blgpu_context_fill_path_d", c.ctypes.data, a.ctypes.data, a.shape[0])
+
+    def submit_stream(self, stream: bytes):
+        self._call("blgpu_context_submit_stream", stream, len(stream))
+
+
+def stream_size(stream: bytes) -> tuple[int, int]:
+    w, h = struct.unpack_from("<II", stream, 8)
+    return w, h
+
+
+def render_stream(runtime: Runtime, stream: bytes, target=None):
+    """Renders a command stream into `target` (default: a new zeroed host image); returns it."""
+    if target is None:
+        w, h = stream_size(stream)
+        target = np.zeros((h, w), dtype=np.uint32)
+    ctx = Context(runtime, target)
+    try:
+        ctx.submit_stream(stream)
+        ctx.end()
+    finally:
+        ctx.close()
+    return target

@@ -1,0 +1,182 @@
+// blgpu_internal.h - data layout shared by the host front end and the sm_103a kernels.
+//
+// A *frame* is everything recorded between two flushes of one or more canvases: fill commands in
+// painter's order, their styles (fetch parameters prepared on the host with the reference's
+// formulas), input geometry in double precision, transforms, gradient LUT requests and pattern
+// images. The device pipeline turns it into pixels:
+//
+//   K0 lut_build    - gradient LUTs (one thread per entry, reference builder semantics)
+//   K1 edge_build   - FP64 edge building per analytic command (count pass + emit pass) producing
+//                     24.8 fixed-point segments, exactly the reference's EdgeBuilder output
+//   K2 binning      - per command tile ranges, per (command, tile row) segment lists, per tile row
+//                     command lists in painter's order
+//   K3 fine         - persistent tile kernel: tile pixels stay in registers while every command
+//                     touching the tile is rasterized into shared-memory cells, swept and composited
+//
+// Everything here is POD so a frame can be uploaded with one copy.
+#pragma once
+
+#include <stdint.h>
+
+namespace blgpu {
+
+constexpr int kTileW = 32;          // tile width in pixels
+constexpr int kTileH = 32;          // tile height in pixels (also the rasterizer band)
+constexpr int kTileShift = 5;
+constexpr int kFineThreads = 256;   // 4 pixels per thread, 8 threads per tile row
+
+enum FillKind : uint32_t {
+  kFillAnalytic = 0,   // edges -> analytic coverage (FillAnalytic_Base)
+  kFillBoxA = 1,       // pixel-aligned box (FillBoxA_Base)
+  kFillBoxU = 2        // 24.8 box with fractional borders (FillData::init_box_u_8bpc_24x8)
+};
+
+enum GeomKind : uint32_t { kGeomPolygon = 0, kGeomPath = 1 };
+
+enum FetchKind : uint32_t {
+  kFetchSolid = 0,
+  kFetchLinearPad, kFetchLinearRoR,
+  kFetchRadialPad, kFetchRadialRoR,
+  kFetchConic,
+  kFetchPatAlignedPad, kFetchPatAlignedRepeat, kFetchPatAlignedRoR,
+  kFetchPatFxFyPad, kFetchPatFxFyRoR,
+  kFetchPatAffineNN, kFetchPatAffineBI
+};
+
+enum LutVariant : uint32_t { kLutSSE2 = 0, kLutAVX2 = 1, kLutScalar = 2 };
+
+// Fetch parameters of one style, set up on the host exactly like the reference's
+// Pipeline::FetchUtils (blend2d/pipeline/pipedefs.cpp).
+struct alignas(16) DevStyle {
+  uint32_t fetch;          // FetchKind
+  uint32_t solid;          // premultiplied PRGB32 (kFetchSolid)
+  uint32_t lut_offset;     // first entry in the LUT pool
+  uint32_t lut_size;
+  uint32_t maxi, rori;
+  int32_t con_maxi, con_rori;
+  // linear (32.32 fixed point)
+  uint64_t lin_pt0, lin_dt, lin_dy;
+  // radial
+  double rad_tx, rad_ty, rad_yx, rad_yy, rad_b0, rad_by, rad_dd0, rad_ddy;
+  double rad_inv2a, rad_amul4, rad_sq_inv2a, rad_sq_fr;
+  float rad_bd, rad_ddd;
+  // conic
+  float con_q[4];
+  float con_n1, con_n2, con_n4, con_offset, con_xx;
+  float pad0;
+  double con_tx, con_ty, con_yx, con_yy;
+  // pattern source (area origin inside the image pool)
+  uint64_t src_offset;     // in pixels
+  int32_t src_w, src_h, src_stride, pad1;
+  // pattern aligned / fx-fy
+  int32_t pat_tx, pat_ty, pat_rx, pat_ry;
+  uint32_t pat_wa, pat_wb, pat_wc, pat_wd;
+  uint32_t ext_y;          // vertical extend: 0 pad, 1 repeat, 2 reflect
+  uint32_t pad2[3];
+  // pattern affine (32.32 fixed point)
+  uint64_t af_xx, af_xy, af_yx, af_yy, af_tx, af_ty;
+  int32_t af_ox, af_oy, af_rx, af_ry;
+  int32_t af_minx, af_miny, af_maxx, af_maxy;
+  int32_t af_corx, af_cory, af_tw, af_th;
+};
+
+struct alignas(16) DevXform {
+  double m[6];             // m00 m01 m10 m11 m20 m21 (final transform x 256)
+  uint32_t affine;         // 1 = EdgeTransformAffine, 0 = EdgeTransformScale
+  uint32_t pad[3];
+};
+
+struct alignas(16) DevCmd {
+  uint32_t kind;           // FillKind
+  uint32_t canvas;         // canvas index
+  uint32_t style;          // DevStyle index
+  uint32_t flags;          // bit0 SrcCopy, bit1 EvenOdd
+  uint32_t alpha;          // 0..255
+  uint32_t geom;           // GeomKind
+  uint32_t geom_first;     // first vertex
+  uint32_t geom_count;     // vertex count
+  uint32_t xform;          // DevXform index
+  int32_t fetch_y0;        // box fills: first row the reference's fetcher is initialized at
+  int32_t box[4];          // BoxA: pixels; BoxU: 24.8; analytic: pixel bbox written by K1
+  uint32_t seg_first;      // K1 output
+  uint32_t seg_count;
+  uint32_t status;         // 0 ok, 1 invalid geometry (NaN), 2 nothing to render
+  uint32_t pad;
+};
+
+struct alignas(16) DevCanvas {
+  uint32_t* pixels;        // device pointer to the canvas's first pixel
+  int32_t w, h, stride;    // stride in pixels
+  int32_t band_height;     // reference band height (conic fetch start rows)
+  int32_t tiles_x, tiles_y;
+  uint32_t tile_base;      // first global tile index
+  uint32_t row_base;       // first global tile-row index
+  uint32_t cmd_first, cmd_count;
+  uint32_t pad[2];
+};
+
+struct alignas(16) DevLutJob {
+  uint32_t style;          // DevStyle index (receives the LUT)
+  uint32_t stop_first;     // first stop in the stop pool
+  uint32_t stop_count;
+  uint32_t lut_offset;
+  uint32_t lut_size;
+  uint32_t variant;        // LutVariant
+  uint32_t pad[2];
+};
+
+struct DevStop {
+  double offset;
+  uint64_t rgba64;
+};
+
+struct DevSeg {            // one non-horizontal 24.8 segment, y0 < y1
+  int32_t x0, y0, x1, y1;
+};
+
+// Device-side view of a frame (pointers into one device arena).
+struct FrameView {
+  const DevCmd* cmds;
+  DevCmd* cmds_rw;
+  const DevStyle* styles;
+  const DevXform* xforms;
+  const DevCanvas* canvases;
+  const double* verts;         // xy pairs
+  const uint8_t* path_cmds;    // one command byte per vertex
+  const DevLutJob* lut_jobs;
+  const DevStop* stops;
+  uint32_t* luts;
+  const uint32_t* images;
+  uint32_t* pixels;
+  // K1
+  uint32_t* seg_counts;        // [num_cmds]
+  uint32_t* seg_rows;          // [num_cmds] tile rows spanned, summed over the command's segments
+  DevSeg* segs;
+  uint32_t* seg_meta;          // cmd << 1 | sign
+  // K2
+  uint32_t* cmd_tile_x;        // tx0 | tx1 << 16 (0xFFFFFFFF = nothing)
+  uint32_t* cmd_tile_y;        // ty0 | ty1 << 16
+  uint32_t* cmdrow_base;       // [num_cmds + 1]: first (cmd,row) slot
+  uint32_t* cmdrow_counts;     // [num_cmdrows + 1]
+  uint32_t* cmdrow_offsets;    // exclusive scan of counts
+  uint32_t* cmdrow_cursor;
+  uint32_t* seglist;           // segment indices grouped by (cmd,row)
+  uint32_t* row_counts;        // [num_rows + 1]
+  uint32_t* row_offsets;
+  uint32_t* row_cmds;          // command indices grouped by tile row, painter's order
+  uint32_t* tile_order;        // tile processing order for the persistent fine kernel
+  uint32_t* tile_canvas;       // canvas index per global tile
+  uint32_t* work_counter;
+  uint32_t* totals;            // [4] segments, seglist bound, (cmd,row) slots, row entries
+  uint32_t* error_flags;
+  uint32_t num_cmds;
+  uint32_t num_canvases;
+  uint32_t num_tiles;
+  uint32_t num_rows;
+  uint32_t num_lut_jobs;
+  uint32_t num_segs;
+  uint32_t num_cmdrows;
+  uint32_t num_seglist;
+};
+
+}  // namespace blgpu

@@ -1,0 +1,753 @@
+// context.cpp - the rendering-context front end and the C ABI (include/blgpu.h).
+//
+// BLGpuContext keeps the reference's synchronous context state (comp-op, fill rule, alphas,
+// hints, user/final transforms, fill style, save/restore stack) and turns every fill call into a
+// device command exactly where the reference would dispatch a fill to its pipeline:
+//   state & alpha      blend2d/raster/rastercontext.cpp:1805-1833, :1920-2056, :4380-4415
+//   transforms         blend2d/raster/rastercontext.cpp:740-800
+//   style resolution   blend2d/raster/rastercontext.cpp:363-494, :572-695, :1231-1453
+//   comp-op simplify   blend2d/core/compopsimplifyimpl_p.h:86-162
+//   fill dispatch      blend2d/raster/rastercontext.cpp:2633-2990, :3317-3500
+// Commands accumulate in a frame; flush(SYNC) / end() runs the frame's device pipeline.
+#include <math.h>
+#include <string.h>
+
+#include <deque>
+#include <new>
+#include <vector>
+
+#include "blgpu.h"
+#include "blgpu_stream.h"
+#include "frontend.h"
+#include "runtime.h"
+
+using namespace blgpu;
+
+struct BLGpuRuntime {
+  Runtime rt;
+};
+
+namespace {
+
+constexpr uint32_t kCompOpSrcOver = 0;
+constexpr uint32_t kCompOpSrcCopy = 1;
+constexpr uint32_t kCompOpMaxValue = 28;        // BL_COMP_OP_MAX_VALUE
+constexpr uint32_t kFillRuleMaxValue = 1;       // BL_FILL_RULE_MAX_VALUE
+constexpr uint32_t kHintRenderingQuality = 0;   // BL_CONTEXT_HINT_*
+constexpr uint32_t kHintGradientQuality = 1;
+constexpr uint32_t kHintPatternQuality = 2;
+constexpr uint32_t kGradientQualityDither = 2;
+constexpr uint32_t kPatternQualityMaxValue = 1;
+
+// A fill style as the context holds it: resolved fetch data plus what a frame must provide.
+struct CtxStyle {
+  HostStyle hs;
+  bool has_image = false;
+  BLGpuImage image{};
+  uint64_t frame_gen = 0;       // frame generation the style was registered in
+  uint32_t frame_index = 0;
+};
+
+struct State {
+  uint32_t comp_op = kCompOpSrcOver;
+  uint32_t fill_rule = 0;
+  double global_alpha = 1.0, fill_alpha = 1.0;
+  uint32_t global_alpha_i = 255, fill_alpha_i = 255;
+  uint32_t gradient_quality = 0, pattern_quality = 1;
+  Mat user{1, 0, 0, 1, 0, 0};
+  Mat final_t{1, 0, 0, 1, 0, 0};
+  Mat final_fixed{256, 0, 0, 256, 0, 0};
+  int final_type = kTTIdentity, final_fixed_type = kTTScale;
+  bool integral_translation = true;
+  int tx_i = 0, ty_i = 0;
+  CtxStyle style;
+  uint64_t xform_gen = 0;       // frame generation of xform_index
+  uint32_t xform_index = 0;
+};
+
+}  // namespace
+
+struct BLGpuContext {
+  BLGpuRuntime* rt = nullptr;
+  Frame own_frame;
+  Frame* frame = &own_frame;
+  bool bound = false;
+  BLGpuImage target{};
+  uint32_t canvas = 0;
+  int w = 0, h = 0;
+  State s;
+  std::vector<State> stack;
+  uint64_t clear_style_gen = 0;
+  uint32_t clear_style_index = 0;
+  std::deque<std::vector<uint32_t>> stream_images;   // pattern pixels copied out of submitted streams
+
+  void reset_state() {
+    s = State{};
+    stack.clear();
+    on_transform_changed();
+    style_solid(s.style.hs, 0xFF000000u);
+  }
+
+  // rastercontext.cpp:741-800
+  void on_transform_changed() {
+    Mat id{1, 0, 0, 1, 0, 0};
+    mat_multiply(s.final_t, s.user, id);
+    s.final_fixed = s.final_t;
+    s.final_fixed.m00 *= 256.0; s.final_fixed.m01 *= 256.0;
+    s.final_fixed.m10 *= 256.0; s.final_fixed.m11 *= 256.0;
+    s.final_fixed.m20 *= 256.0; s.final_fixed.m21 *= 256.0;
+    s.final_type = mat_type(s.final_t);
+    s.final_fixed_type = s.final_type > kTTScale ? s.final_type : int(kTTScale);
+    s.integral_translation = false;
+    s.xform_gen = 0;
+    if (s.final_type <= kTTTranslate) {
+      double mn = floor(double(INT32_MIN + 1) * 256.0);
+      double mx = floor(double(INT32_MAX - 1 - (w > h ? w : h)) * 256.0);
+      const Mat& ft = s.final_fixed;
+      if (ft.m20 >= mn && ft.m20 <= mx && ft.m21 >= mn && ft.m21 <= mx) {
+        int64_t tx64 = floor_to_int64(ft.m20), ty64 = floor_to_int64(ft.m21);
+        if (((tx64 | ty64) & 0xFF) == 0) {
+          s.tx_i = int(tx64 >> 8);
+          s.ty_i = int(ty64 >> 8);
+          s.integral_translation = true;
+        }
+      }
+    }
+  }
+
+  // --- frame registration ---------------------------------------------------------------
+
+  uint32_t register_style(CtxStyle& cs) {
+    if (cs.frame_gen == frame->generation) return cs.frame_index;
+    DevStyle d = cs.hs.dev;
+    if (d.lut_size) {
+      DevLutJob job{};
+      job.style = uint32_t(frame->styles.size());
+      job.stop_first = uint32_t(frame->stops.size());
+      job.stop_count = uint32_t(cs.hs.stops.size());
+      job.lut_offset = frame->lut_words;
+      job.lut_size = d.lut_size;
+      job.variant = rt->rt.lut_variant;
+      frame->stops.insert(frame->stops.end(), cs.hs.stops.begin(), cs.hs.stops.end());
+      frame->lut_jobs.push_back(job);
+      d.lut_offset = frame->lut_words;
+      frame->lut_words += d.lut_size;
+    }
+    if (cs.has_image) d.src_offset += frame->add_image(cs.image);
+    frame->styles.push_back(d);
+    cs.frame_gen = frame->generation;
+    cs.frame_index = uint32_t(frame->styles.size() - 1);
+    return cs.frame_index;
+  }
+
+  uint32_t register_clear_style() {
+    if (clear_style_gen == frame->generation) return clear_style_index;
+    DevStyle d{};
+    d.fetch = kFetchSolid;
+    d.solid = 0;
+    frame->styles.push_back(d);
+    clear_style_gen = frame->generation;
+    clear_style_index = uint32_t(frame->styles.size() - 1);
+    return clear_style_index;
+  }
+
+  uint32_t register_xform() {
+    if (s.xform_gen == frame->generation) return s.xform_index;
+    DevXform x{};
+    x.m[0] = s.final_fixed.m00; x.m[1] = s.final_fixed.m01;
+    x.m[2] = s.final_fixed.m10; x.m[3] = s.final_fixed.m11;
+    x.m[4] = s.final_fixed.m20; x.m[5] = s.final_fixed.m21;
+    x.affine = s.final_fixed_type > kTTScale ? 1u : 0u;
+    frame->xforms.push_back(x);
+    s.xform_gen = frame->generation;
+    s.xform_index = uint32_t(frame->xforms.size() - 1);
+    return s.xform_index;
+  }
+
+  DevCmd& push_cmd(uint32_t kind, uint32_t style, bool src_copy, uint32_t alpha) {
+    DevCmd c{};
+    c.kind = kind;
+    c.canvas = canvas;
+    c.style = style;
+    c.flags = src_copy ? 1u : 0u;
+    c.alpha = alpha;
+    frame->cmds.push_back(c);
+    frame->canvases[canvas].cmd_count++;
+    return frame->cmds.back();
+  }
+
+  // --- fill resolution --------------------------------------------------------------------
+
+  struct Fill { uint32_t style; bool src_copy; uint32_t alpha; };
+
+  // Returns false for a NOP fill (no alpha, no style, or a comp-op that simplifies to DstCopy).
+  bool resolve_fill(Fill& f) {
+    if (s.global_alpha_i == 0 || s.fill_alpha_i == 0 || s.style.hs.nop) return false;
+    uint32_t op = s.comp_op;
+    if (op == kCompOpSrcOver) {
+      if (s.style.hs.format == kFmtZERO32) return false;
+      if (s.style.hs.format == kFmtFRGB32) op = kCompOpSrcCopy;
+    }
+    f.src_copy = op == kCompOpSrcCopy;
+    f.alpha = s.fill_alpha_i;
+    f.style = register_style(s.style);
+    return true;
+  }
+
+  void fill_box_a(const Fill& f, int x0, int y0, int x1, int y1) {
+    DevCmd& c = push_cmd(kFillBoxA, f.style, f.src_copy, f.alpha);
+    c.box[0] = x0; c.box[1] = y0; c.box[2] = x1; c.box[3] = y1;
+    c.fetch_y0 = y0;
+  }
+
+  // FillData::init_box_u_8bpc_24x8 (pipedefs_p.h:644-815): the fetcher starts at the first row
+  // whose mask is not zero.
+  void fill_clipped_box_f(const Fill& f, int x0, int y0, int x1, int y1) {
+    if (((x0 | y0 | x1 | y1) & 0xFF) == 0) { fill_box_a(f, x0 >> 8, y0 >> 8, x1 >> 8, y1 >> 8); return; }
+    uint32_t alpha = f.alpha;
+    uint32_t ax0 = uint32_t(x0) >> 8, ay0 = uint32_t(y0) >> 8;
+    uint32_t ax1 = uint32_t(x1 + 0xFF) >> 8, ay1 = uint32_t(y1 + 0xFF) >> 8;
+    uint32_t fx0 = uint32_t(x0) & 0xFFu, fy0 = uint32_t(y0) & 0xFFu;
+    uint32_t fx1 = (uint32_t(x1 - 1) & 0xFFu) + 1u, fy1 = (uint32_t(y1 - 1) & 0xFFu) + 1u;
+    uint32_t w = ax1 - ax0, h = ay1 - ay0;
+    fy0 = (h == 1 ? fy1 : 256u) - fy0;
+    uint32_t fy0_a = fy0 * alpha, fy1_a = fy1 * alpha;
+    uint32_t m_first, m_mid, m_last;
+    if (w == 1) {
+      uint32_t fw = fx1 - fx0;
+      m_first = (fw * fy0_a) >> 16; m_mid = (fw * alpha) >> 8; m_last = (fw * fy1_a) >> 16;
+    }
+    else {
+      m_first = fy0_a >> 8; m_mid = alpha; m_last = fy1_a >> 8;
+    }
+    uint32_t row_y0 = ay0, row_y1 = ay1;
+    if (h == 1) {
+      if (!m_first) return;
+    }
+    else {
+      if (!m_first) row_y0++;
+      if (!m_last) row_y1--;
+      if (!(row_y0 < row_y1) || (w == 1 && m_mid == 0)) return;
+    }
+    DevCmd& c = push_cmd(kFillBoxU, f.style, f.src_copy, f.alpha);
+    c.box[0] = x0; c.box[1] = y0; c.box[2] = x1; c.box[3] = y1;
+    c.fetch_y0 = int32_t(row_y0);
+  }
+
+  void fill_analytic(const Fill& f, const double* xy, const uint8_t* cmds, size_t n, uint32_t fill_rule,
+                     uint32_t xform) {
+    DevCmd& c = push_cmd(kFillAnalytic, f.style, f.src_copy, f.alpha);
+    c.flags |= fill_rule == 1 ? 2u : 0u;
+    c.geom = cmds ? kGeomPath : kGeomPolygon;
+    c.geom_first = uint32_t(frame->verts.size() / 2);
+    c.geom_count = uint32_t(n);
+    c.xform = xform;
+    frame->verts.insert(frame->verts.end(), xy, xy + 2 * n);
+    if (cmds) frame->path_cmds.insert(frame->path_cmds.end(), cmds, cmds + n);
+    else frame->path_cmds.resize(frame->path_cmds.size() + n, uint8_t(0));
+  }
+
+  void fill_box_d(const Fill& f, double bx0, double by0, double bx1, double by1) {
+    const Mat& t = s.final_fixed;
+    if (s.final_fixed_type <= kTTSwap) {
+      double x0 = bx0 * t.m00 + by0 * t.m10 + t.m20;
+      double y0 = bx0 * t.m01 + by0 * t.m11 + t.m21;
+      double x1 = bx1 * t.m00 + by1 * t.m10 + t.m20;
+      double y1 = bx1 * t.m01 + by1 * t.m11 + t.m21;
+      auto dmin = [](double a, double b) { return b < a ? b : a; };
+      auto dmax = [](double a, double b) { return a < b ? b : a; };
+      double mx0 = dmin(x0, x1), my0 = dmin(y0, y1), mx1 = dmax(x0, x1), my1 = dmax(y0, y1);
+      double cx1 = double(w) * 256.0, cy1 = double(h) * 256.0;
+      double ix0 = dmax(mx0, 0.0), iy0 = dmax(my0, 0.0), ix1 = dmin(mx1, cx1), iy1 = dmin(my1, cy1);
+      if (!((ix0 < ix1) & (iy0 < iy1))) return;
+      int ux0 = trunc_to_int(ix0), uy0 = trunc_to_int(iy0), ux1 = trunc_to_int(ix1), uy1 = trunc_to_int(iy1);
+      if (ux0 >= ux1 || uy0 >= uy1) return;
+      fill_clipped_box_f(f, ux0, uy0, ux1, uy1);
+    }
+    else {
+      double poly[8] = {bx0, by0, bx1, by0, bx1, by1, bx0, by1};
+      fill_analytic(f, poly, nullptr, 4, 1, register_xform());
+    }
+  }
+
+  // --- API ---------------------------------------------------------------------------------
+
+  BLGpuResult begin(const BLGpuImage* image) {
+    if (!image || image->format != BLGPU_FORMAT_PRGB32 || image->width <= 0 || image->height <= 0 ||
+        image->width > 65535 || image->height > 65535 || !image->pixel_data ||
+        image->stride < intptr_t(image->width) * 4)
+      return BLGPU_ERROR_INVALID_VALUE;
+    if (bound) { BLGpuResult r = end(); if (r) return r; }
+    target = *image;
+    w = image->width;
+    h = image->height;
+    bound = true;
+    frame->clear();
+    stream_images.clear();
+    canvas = frame->add_canvas(target, true);
+    reset_state();
+    return BLGPU_SUCCESS;
+  }
+
+  // Runs the recorded frame (canvas content uploaded unless the first command overwrites it).
+  BLGpuResult flush_frame() {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    BLGpuResult r = BLGPU_SUCCESS;
+    if (!frame->cmds.empty()) {
+      mark_uploads(*frame);
+      r = rt->rt.run(*frame);
+    }
+    frame->clear();
+    stream_images.clear();
+    canvas = frame->add_canvas(target, true);
+    return r;
+  }
+
+  static void mark_uploads(Frame& fr) {
+    for (size_t i = 0; i < fr.canvases.size(); i++) {
+      const DevCanvas& cv = fr.canvases[i];
+      if (!cv.cmd_count) continue;
+      const DevCmd& c = fr.cmds[cv.cmd_first];
+      bool overwrites = c.kind == kFillBoxA && (c.flags & 1u) && c.alpha == 255 && c.box[0] == 0 && c.box[1] == 0 &&
+                        c.box[2] == cv.w && c.box[3] == cv.h;
+      fr.targets[i].upload = !overwrites;
+    }
+  }
+
+  BLGpuResult end() {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    BLGpuResult r = flush_frame();
+    frame->clear();
+    bound = false;
+    return r;
+  }
+
+  BLGpuResult set_comp_op(uint32_t op) {
+    if (op > kCompOpMaxValue) return BLGPU_ERROR_INVALID_VALUE;
+    if (op > kCompOpSrcCopy) return BLGPU_ERROR_NOT_IMPLEMENTED;
+    s.comp_op = op;
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult set_fill_rule(uint32_t rule) {
+    if (rule > kFillRuleMaxValue) return BLGPU_ERROR_INVALID_VALUE;
+    s.fill_rule = rule;
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult set_global_alpha(double a) {   // rastercontext.cpp:2000-2028
+    if (isnan(a)) return BLGPU_ERROR_INVALID_VALUE;
+    a = a < 0.0 ? 0.0 : (a > 1.0 ? 1.0 : a);
+    double ia = a * 255.0;
+    s.global_alpha = a;
+    s.global_alpha_i = uint32_t(round_to_int(ia));
+    s.fill_alpha_i = uint32_t(round_to_int(ia * s.fill_alpha));
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult set_fill_alpha(double a) {     // rastercontext.cpp:1920-1945
+    if (isnan(a)) return BLGPU_ERROR_INVALID_VALUE;
+    a = a < 0.0 ? 0.0 : (a > 1.0 ? 1.0 : a);
+    s.fill_alpha = a;
+    s.fill_alpha_i = uint32_t(round_to_int(s.global_alpha * 255.0 * a));
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult set_hint(uint32_t hint, uint32_t value) {   // rastercontext.cpp:1805-1832
+    switch (hint) {
+      case kHintRenderingQuality:
+        return value > 0 ? BLGPU_ERROR_INVALID_VALUE : BLGPU_SUCCESS;
+      case kHintGradientQuality:
+        if (value > kGradientQualityDither) return BLGPU_ERROR_INVALID_VALUE;
+        if (value == kGradientQualityDither) return BLGPU_ERROR_NOT_IMPLEMENTED;
+        s.gradient_quality = value;
+        return BLGPU_SUCCESS;
+      case kHintPatternQuality:
+        if (value > kPatternQualityMaxValue) return BLGPU_ERROR_INVALID_VALUE;
+        s.pattern_quality = value;
+        return BLGPU_SUCCESS;
+      default:
+        return BLGPU_ERROR_INVALID_VALUE;
+    }
+  }
+
+  BLGpuResult set_transform(const double* m) {
+    if (!m) return BLGPU_ERROR_INVALID_VALUE;
+    s.user = Mat{m[0], m[1], m[2], m[3], m[4], m[5]};
+    on_transform_changed();
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult reset_transform() {
+    s.user = Mat{1, 0, 0, 1, 0, 0};
+    on_transform_changed();
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult set_style_rgba32(uint32_t c) {
+    s.style = CtxStyle{};
+    style_solid(s.style.hs, c);
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult set_style_gradient(const BLGpuGradient* g) {
+    if (!g || g->type > 2 || g->extend_mode > 2 || (g->stop_count && !g->stops)) return BLGPU_ERROR_INVALID_VALUE;
+    GradientDesc d;
+    d.type = g->type;
+    d.extend = g->extend_mode;
+    memcpy(d.values, g->values, sizeof(d.values));
+    d.stops = reinterpret_cast<const DevStop*>(g->stops);
+    d.stop_count = g->stop_count;
+    d.transform = g->transform;
+    s.style = CtxStyle{};
+    style_gradient(s.style.hs, d, s.final_t);
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult set_style_pattern(const BLGpuPattern* p) {
+    if (!p || !p->image) return BLGPU_ERROR_INVALID_VALUE;
+    const BLGpuImage& im = *p->image;
+    if (im.format != BLGPU_FORMAT_PRGB32 || im.width < 0 || im.height < 0 || (im.width && !im.pixel_data) ||
+        im.stride < intptr_t(im.width) * 4)
+      return BLGPU_ERROR_INVALID_VALUE;
+    if (p->extend_mode > 8) return BLGPU_ERROR_INVALID_VALUE;
+    if (p->extend_mode > 2) return BLGPU_ERROR_NOT_IMPLEMENTED;   // complex (per-axis) extend modes
+    if (p->area[2] > 0) {
+      int64_t x = p->area[0], y = p->area[1], aw = p->area[2], ah = p->area[3];
+      if (x < 0 || y < 0 || ah < 0 || x + aw > im.width || y + ah > im.height) return BLGPU_ERROR_INVALID_VALUE;
+    }
+    PatternDesc d;
+    d.image = 0;
+    d.img_w = im.width;
+    d.img_h = im.height;
+    memcpy(d.area, p->area, sizeof(d.area));
+    d.extend = p->extend_mode;
+    d.transform = p->transform;
+    s.style = CtxStyle{};
+    style_pattern(s.style.hs, d, s.pattern_quality, s.final_t);
+    if (!s.style.hs.nop) {
+      s.style.has_image = true;
+      s.style.image = im;
+    }
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult clear_all() {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    Fill f{register_clear_style(), true, 255};
+    fill_box_a(f, 0, 0, w, h);
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult fill_all() {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    Fill f;
+    if (!resolve_fill(f)) return BLGPU_SUCCESS;
+    fill_box_a(f, 0, 0, w, h);
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult fill_rect_i(int32_t x, int32_t y, int32_t rw, int32_t rh) {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    Fill f;
+    if (!resolve_fill(f)) return BLGPU_SUCCESS;
+    if (!s.integral_translation) {
+      if ((rw <= 0) | (rh <= 0)) return BLGPU_SUCCESS;
+      fill_box_d(f, double(x), double(y), double(x) + double(rw), double(y) + double(rh));
+      return BLGPU_SUCCESS;
+    }
+    int64_t x0 = int64_t(x) + s.tx_i, y0 = int64_t(y) + s.ty_i;
+    int64_t x1 = int64_t(rw) + x0, y1 = int64_t(rh) + y0;
+    x0 = x0 < 0 ? 0 : x0; y0 = y0 < 0 ? 0 : y0;
+    x1 = x1 > w ? w : x1; y1 = y1 > h ? h : y1;
+    if ((x0 >= x1) | (y0 >= y1)) return BLGPU_SUCCESS;
+    fill_box_a(f, int(x0), int(y0), int(x1), int(y1));
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult fill_box(double x0, double y0, double x1, double y1) {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    Fill f;
+    if (!resolve_fill(f)) return BLGPU_SUCCESS;
+    fill_box_d(f, x0, y0, x1, y1);
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult fill_polygon(const double* xy, size_t n) {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    if (n && !xy) return BLGPU_ERROR_INVALID_VALUE;
+    if (n > 0x3FFFFFFFu) return BLGPU_ERROR_INVALID_VALUE;
+    Fill f;
+    if (!resolve_fill(f)) return BLGPU_SUCCESS;
+    if (n < 3) return BLGPU_SUCCESS;
+    fill_analytic(f, xy, nullptr, n, s.fill_rule, register_xform());
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult fill_path(const uint8_t* cmds, const double* xy, size_t n) {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    if (n && (!xy || !cmds)) return BLGPU_ERROR_INVALID_VALUE;
+    if (n > 0x3FFFFFFFu) return BLGPU_ERROR_INVALID_VALUE;
+    Fill f;
+    if (!resolve_fill(f)) return BLGPU_SUCCESS;
+    if (n == 0) return BLGPU_SUCCESS;
+    fill_analytic(f, xy, cmds, n, s.fill_rule, register_xform());
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult save() { stack.push_back(s); return BLGPU_SUCCESS; }
+  BLGpuResult restore() {
+    if (stack.empty()) return BLGPU_ERROR_NO_STATES_TO_RESTORE;
+    s = stack.back();
+    stack.pop_back();
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult submit_stream(const uint8_t* base, size_t size);
+};
+
+// Stream replay: the same record semantics as the context calls above.
+BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
+  if (!bound) return BLGPU_ERROR_INVALID_STATE;
+  if (!base || size < sizeof(BLGpuStreamHeader)) return BLGPU_ERROR_INVALID_VALUE;
+  BLGpuStreamHeader hdr;
+  memcpy(&hdr, base, sizeof(hdr));
+  if (hdr.magic != BLGPU_STREAM_MAGIC || hdr.version != BLGPU_STREAM_VERSION) return BLGPU_ERROR_INVALID_VALUE;
+  if (int(hdr.width) != w || int(hdr.height) != h) return BLGPU_ERROR_INVALID_VALUE;
+  size_t off = sizeof(hdr);
+  std::vector<BLGpuImage> images(hdr.image_count);
+  for (uint32_t i = 0; i < hdr.image_count; i++) {
+    BLGpuStreamImage im;
+    if (off + sizeof(im) > size) return BLGPU_ERROR_INVALID_VALUE;
+    memcpy(&im, base + off, sizeof(im));
+    off += sizeof(im);
+    size_t n = size_t(im.width) * im.height;
+    if (im.width > 65535 || im.height > 65535 || off + n * 4u > size) return BLGPU_ERROR_INVALID_VALUE;
+    stream_images.emplace_back(n ? n : 1);
+    memcpy(stream_images.back().data(), base + off, n * 4u);
+    images[i] = BLGpuImage{stream_images.back().data(), intptr_t(im.width) * 4, int32_t(im.width), int32_t(im.height),
+                           BLGPU_FORMAT_PRGB32, 0};
+    off += (n * 4u + 7u) & ~size_t(7);
+  }
+  while (off + 8 <= size) {
+    uint32_t op, len;
+    memcpy(&op, base + off, 4);
+    memcpy(&len, base + off + 4, 4);
+    const uint8_t* p = base + off + 8;
+    if (off + 8 + size_t(len) > size) return BLGPU_ERROR_INVALID_VALUE;
+    off += 8 + size_t(len);
+    if (op == BLGPU_OP_END) break;
+    auto need = [&](size_t bytes) { return size_t(len) >= bytes; };
+    BLGpuResult r = BLGPU_SUCCESS;
+    switch (op) {
+      case BLGPU_OP_SET_COMP_OP: { if (!need(4)) return BLGPU_ERROR_INVALID_VALUE; uint32_t v; memcpy(&v, p, 4); r = set_comp_op(v); break; }
+      case BLGPU_OP_SET_FILL_RULE: { if (!need(4)) return BLGPU_ERROR_INVALID_VALUE; uint32_t v; memcpy(&v, p, 4); r = set_fill_rule(v); break; }
+      case BLGPU_OP_SET_GLOBAL_ALPHA: { if (!need(8)) return BLGPU_ERROR_INVALID_VALUE; double a; memcpy(&a, p, 8); set_global_alpha(a); break; }
+      case BLGPU_OP_SET_FILL_ALPHA: { if (!need(8)) return BLGPU_ERROR_INVALID_VALUE; double a; memcpy(&a, p, 8); set_fill_alpha(a); break; }
+      case BLGPU_OP_SET_HINT: {
+        if (!need(8)) return BLGPU_ERROR_INVALID_VALUE;
+        uint32_t hh, v; memcpy(&hh, p, 4); memcpy(&v, p + 4, 4);
+        r = set_hint(hh, v);
+        break;
+      }
+      case BLGPU_OP_SET_TRANSFORM: { if (!need(48)) return BLGPU_ERROR_INVALID_VALUE; double m[6]; memcpy(m, p, 48); set_transform(m); break; }
+      case BLGPU_OP_RESET_TRANSFORM: reset_transform(); break;
+      case BLGPU_OP_STYLE_RGBA32: { if (!need(4)) return BLGPU_ERROR_INVALID_VALUE; uint32_t v; memcpy(&v, p, 4); set_style_rgba32(v); break; }
+      case BLGPU_OP_STYLE_GRADIENT: {
+        BLGpuStreamGradient g;
+        if (!need(sizeof(g))) return BLGPU_ERROR_INVALID_VALUE;
+        memcpy(&g, p, sizeof(g));
+        if (!need(sizeof(g) + size_t(g.stop_count) * sizeof(BLGpuStreamGradientStop))) return BLGPU_ERROR_INVALID_VALUE;
+        std::vector<BLGpuGradientStop> stops(g.stop_count);
+        if (g.stop_count) memcpy(stops.data(), p + sizeof(g), sizeof(BLGpuGradientStop) * g.stop_count);
+        BLGpuGradient gg;
+        gg.type = g.type;
+        gg.extend_mode = g.extend_mode;
+        memcpy(gg.values, g.values, sizeof(gg.values));
+        gg.stops = stops.data();
+        gg.stop_count = g.stop_count;
+        gg.transform = g.has_transform ? g.transform : nullptr;
+        r = set_style_gradient(&gg);
+        break;
+      }
+      case BLGPU_OP_STYLE_PATTERN: {
+        BLGpuStreamPattern pt;
+        if (!need(sizeof(pt))) return BLGPU_ERROR_INVALID_VALUE;
+        memcpy(&pt, p, sizeof(pt));
+        if (pt.image_index >= hdr.image_count) return BLGPU_ERROR_INVALID_VALUE;
+        BLGpuPattern pp;
+        pp.image = &images[pt.image_index];
+        memcpy(pp.area, pt.area, sizeof(pp.area));
+        pp.extend_mode = pt.extend_mode;
+        pp.transform = pt.has_transform ? pt.transform : nullptr;
+        r = set_style_pattern(&pp);
+        break;
+      }
+      case BLGPU_OP_CLEAR_ALL: r = clear_all(); break;
+      case BLGPU_OP_FILL_ALL: r = fill_all(); break;
+      case BLGPU_OP_FILL_RECT_I: {
+        if (!need(16)) return BLGPU_ERROR_INVALID_VALUE;
+        int32_t q[4]; memcpy(q, p, 16);
+        r = fill_rect_i(q[0], q[1], q[2], q[3]);
+        break;
+      }
+      case BLGPU_OP_FILL_RECT_D: {
+        if (!need(32)) return BLGPU_ERROR_INVALID_VALUE;
+        double q[4]; memcpy(q, p, 32);
+        r = fill_box(q[0], q[1], q[0] + q[2], q[1] + q[3]);
+        break;
+      }
+      case BLGPU_OP_FILL_BOX_D: {
+        if (!need(32)) return BLGPU_ERROR_INVALID_VALUE;
+        double q[4]; memcpy(q, p, 32);
+        r = fill_box(q[0], q[1], q[2], q[3]);
+        break;
+      }
+      case BLGPU_OP_FILL_POLYGON_D: {
+        if (!need(8)) return BLGPU_ERROR_INVALID_VALUE;
+        uint32_t n; memcpy(&n, p, 4);
+        if (!need(8 + size_t(n) * 16)) return BLGPU_ERROR_INVALID_VALUE;
+        std::vector<double> xy(size_t(n) * 2);
+        if (n) memcpy(xy.data(), p + 8, size_t(n) * 16);
+        r = fill_polygon(xy.data(), n);
+        break;
+      }
+      case BLGPU_OP_FILL_PATH_D: {
+        if (!need(8)) return BLGPU_ERROR_INVALID_VALUE;
+        uint32_t n; memcpy(&n, p, 4);
+        size_t cmd_bytes = (size_t(n) + 7u) & ~size_t(7);
+        if (!need(8 + cmd_bytes + size_t(n) * 16)) return BLGPU_ERROR_INVALID_VALUE;
+        std::vector<double> xy(size_t(n) * 2);
+        if (n) memcpy(xy.data(), p + 8 + cmd_bytes, size_t(n) * 16);
+        r = fill_path(p + 8, xy.data(), n);
+        break;
+      }
+      case BLGPU_OP_SAVE: save(); break;
+      case BLGPU_OP_RESTORE: restore(); break;
+      default: return BLGPU_ERROR_INVALID_VALUE;
+    }
+    if (r) return r;
+  }
+  return BLGPU_SUCCESS;
+}
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+
+#define BLGPU_API extern "C" __attribute__((visibility("default")))
+
+BLGPU_API BLGpuResult blgpu_runtime_create(BLGpuRuntime** out, const BLGpuRuntimeCreateInfo* info) {
+  if (!out) return BLGPU_ERROR_INVALID_VALUE;
+  *out = nullptr;
+  BLGpuRuntime* r = new (std::nothrow) BLGpuRuntime();
+  if (!r) return BLGPU_ERROR_OUT_OF_MEMORY;
+  BLGpuResult res = r->rt.init(info);
+  if (res) { r->rt.destroy(); delete r; return res; }
+  *out = r;
+  return BLGPU_SUCCESS;
+}
+
+BLGPU_API BLGpuResult blgpu_runtime_destroy(BLGpuRuntime* rt) {
+  if (!rt) return BLGPU_ERROR_INVALID_VALUE;
+  rt->rt.destroy();
+  delete rt;
+  return BLGPU_SUCCESS;
+}
+
+BLGPU_API BLGpuResult blgpu_runtime_get_stats(const BLGpuRuntime* rt, BLGpuStats* out) {
+  if (!rt || !out) return BLGPU_ERROR_INVALID_VALUE;
+  *out = rt->rt.stats;
+  return BLGPU_SUCCESS;
+}
+
+BLGPU_API BLGpuResult blgpu_runtime_replay(BLGpuRuntime* rt, int use_graph) {
+  if (!rt) return BLGPU_ERROR_INVALID_VALUE;
+  return rt->rt.replay(use_graph != 0);
+}
+
+BLGPU_API BLGpuResult blgpu_runtime_synchronize(BLGpuRuntime* rt) {
+  if (!rt) return BLGPU_ERROR_INVALID_VALUE;
+  return rt->rt.synchronize();
+}
+
+BLGPU_API BLGpuResult blgpu_context_create(BLGpuContext** out, BLGpuRuntime* rt) {
+  if (!out || !rt) return BLGPU_ERROR_INVALID_VALUE;
+  BLGpuContext* c = new (std::nothrow) BLGpuContext();
+  if (!c) return BLGPU_ERROR_OUT_OF_MEMORY;
+  c->rt = rt;
+  c->reset_state();
+  *out = c;
+  return BLGPU_SUCCESS;
+}
+
+BLGPU_API BLGpuResult blgpu_context_destroy(BLGpuContext* ctx) {
+  if (!ctx) return BLGPU_ERROR_INVALID_VALUE;
+  BLGpuResult r = ctx->bound ? ctx->end() : BLGPU_SUCCESS;
+  delete ctx;
+  return r;
+}
+
+#define CTX_CALL(expr) do { if (!ctx) return BLGPU_ERROR_INVALID_VALUE; return ctx->expr; } while (0)
+
+BLGPU_API BLGpuResult blgpu_context_begin(BLGpuContext* ctx, const BLGpuImage* image) { CTX_CALL(begin(image)); }
+BLGPU_API BLGpuResult blgpu_context_end(BLGpuContext* ctx) { CTX_CALL(end()); }
+BLGPU_API BLGpuResult blgpu_context_flush(BLGpuContext* ctx, uint32_t flags) {
+  if (!ctx) return BLGPU_ERROR_INVALID_VALUE;
+  if (!ctx->bound) return BLGPU_ERROR_INVALID_STATE;
+  if (!(flags & BLGPU_FLUSH_SYNC)) return BLGPU_SUCCESS;
+  return ctx->flush_frame();
+}
+BLGPU_API BLGpuResult blgpu_context_save(BLGpuContext* ctx) { CTX_CALL(save()); }
+BLGPU_API BLGpuResult blgpu_context_restore(BLGpuContext* ctx) { CTX_CALL(restore()); }
+BLGPU_API BLGpuResult blgpu_context_set_comp_op(BLGpuContext* ctx, uint32_t v) { CTX_CALL(set_comp_op(v)); }
+BLGPU_API BLGpuResult blgpu_context_set_fill_rule(BLGpuContext* ctx, uint32_t v) { CTX_CALL(set_fill_rule(v)); }
+BLGPU_API BLGpuResult blgpu_context_set_global_alpha(BLGpuContext* ctx, double a) { CTX_CALL(set_global_alpha(a)); }
+BLGPU_API BLGpuResult blgpu_context_set_fill_alpha(BLGpuContext* ctx, double a) { CTX_CALL(set_fill_alpha(a)); }
+BLGPU_API BLGpuResult blgpu_context_set_hint(BLGpuContext* ctx, uint32_t hint, uint32_t v) { CTX_CALL(set_hint(hint, v)); }
+BLGPU_API BLGpuResult blgpu_context_set_transform(BLGpuContext* ctx, const double m[6]) { CTX_CALL(set_transform(m)); }
+BLGPU_API BLGpuResult blgpu_context_reset_transform(BLGpuContext* ctx) { CTX_CALL(reset_transform()); }
+BLGPU_API BLGpuResult blgpu_context_set_fill_style_rgba32(BLGpuContext* ctx, uint32_t c) { CTX_CALL(set_style_rgba32(c)); }
+BLGPU_API BLGpuResult blgpu_context_set_fill_style_gradient(BLGpuContext* ctx, const BLGpuGradient* g) { CTX_CALL(set_style_gradient(g)); }
+BLGPU_API BLGpuResult blgpu_context_set_fill_style_pattern(BLGpuContext* ctx, const BLGpuPattern* p) { CTX_CALL(set_style_pattern(p)); }
+BLGPU_API BLGpuResult blgpu_context_clear_all(BLGpuContext* ctx) { CTX_CALL(clear_all()); }
+BLGPU_API BLGpuResult blgpu_context_fill_all(BLGpuContext* ctx) { CTX_CALL(fill_all()); }
+BLGPU_API BLGpuResult blgpu_context_fill_rect_i(BLGpuContext* ctx, int32_t x, int32_t y, int32_t w, int32_t h) { CTX_CALL(fill_rect_i(x, y, w, h)); }
+BLGPU_API BLGpuResult blgpu_context_fill_rect_d(BLGpuContext* ctx, double x, double y, double w, double h) { CTX_CALL(fill_box(x, y, x + w, y + h)); }
+BLGPU_API BLGpuResult blgpu_context_fill_box_d(BLGpuContext* ctx, double x0, double y0, double x1, double y1) { CTX_CALL(fill_box(x0, y0, x1, y1)); }
+BLGPU_API BLGpuResult blgpu_context_fill_polygon_d(BLGpuContext* ctx, const double* xy, size_t n) { CTX_CALL(fill_polygon(xy, n)); }
+BLGPU_API BLGpuResult blgpu_context_fill_path_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n) { CTX_CALL(fill_path(cmds, xy, n)); }
+BLGPU_API BLGpuResult blgpu_context_submit_stream(BLGpuContext* ctx, const void* stream, size_t size) {
+  CTX_CALL(submit_stream(static_cast<const uint8_t*>(stream), size));
+}
+
+// Batched rendering: every stream gets its own canvas in one shared frame, so one device
+// pipeline (one persistent fine launch) renders all of them.
+BLGPU_API BLGpuResult blgpu_render_batch(BLGpuRuntime* rt, const void* const* streams, const size_t* sizes,
+                                         const BLGpuImage* images, uint32_t count) {
+  if (!rt || (count && (!streams || !sizes || !images))) return BLGPU_ERROR_INVALID_VALUE;
+  if (!count) return BLGPU_SUCCESS;
+  Frame frame;
+  std::vector<BLGpuContext> ctxs(count);
+  for (uint32_t i = 0; i < count; i++) {
+    BLGpuContext& c = ctxs[i];
+    const BLGpuImage& im = images[i];
+    if (im.format != BLGPU_FORMAT_PRGB32 || im.width <= 0 || im.height <= 0 || im.width > 65535 ||
+        im.height > 65535 || !im.pixel_data || im.stride < intptr_t(im.width) * 4)
+      return BLGPU_ERROR_INVALID_VALUE;
+    c.rt = rt;
+    c.frame = &frame;
+    c.target = im;
+    c.w = im.width;
+    c.h = im.height;
+    c.bound = true;
+    c.canvas = frame.add_canvas(im, true);
+    c.reset_state();
+    BLGpuResult r = c.submit_stream(static_cast<const uint8_t*>(streams[i]), sizes[i]);
+    if (r) return r;
+    c.bound = false;
+  }
+  if (frame.cmds.empty()) return BLGPU_SUCCESS;
+  BLGpuContext::mark_uploads(frame);
+  return rt->rt.run(frame);
+}

@@ -1,0 +1,937 @@
+// edge_build.cuh - FP64 edge building on the device (kernel K1).
+//
+// One thread builds the edges of one analytic fill command: transform, clip against the canvas
+// (24.8 fixed-point clip box), split curves into monotonic pieces, flatten them by midpoint
+// subdivision and truncate to 24.8 integers - the same arithmetic, in the same order, as the
+// reference's EdgeBuilder<int> (blend2d/raster/edgebuilder_p.h:776-2629) and the Bezier splitters
+// it calls (blend2d/geometry/bezier_p.h:366-395, :834-920; blend2d/support/math_p.h:574-592).
+//
+// The reference links polylines into per-band lists; the rasterized result depends only on the
+// multiset of non-horizontal segments (cell sums are commutative), so here every polyline point
+// appended after the first emits the segment joining it to its predecessor. The translation unit
+// is compiled with -fmad=false so every a*b+c stays unfused like the reference's SSE2 build.
+#pragma once
+
+#include "blgpu_internal.h"
+
+namespace blgpu {
+namespace eb {
+
+struct Pt { double x, y; };
+
+__device__ __forceinline__ double dmin(double a, double b) { return b < a ? b : a; }
+__device__ __forceinline__ double dmax(double a, double b) { return a < b ? b : a; }
+__device__ __forceinline__ double dclamp(double a, double lo, double hi) { return dmin(hi, dmax(lo, a)); }
+
+// x86 cvttsd2si: truncation, INT_MIN for NaN / out-of-range (the reference is an x86-64 build).
+__device__ __forceinline__ int trunc_i(double x) {
+  if (!(x > -2147483649.0 && x < 2147483648.0)) return INT32_MIN;
+  return __double2int_rz(x);
+}
+
+// Segment sink: counts (out == nullptr) or writes segments and tracks the pixel bbox.
+struct Sink {
+  DevSeg* out;
+  uint32_t* meta;
+  uint32_t cmd;
+  uint32_t n;
+  uint32_t rows;        // sum over segments of the tile rows each one spans (seglist size)
+  int ymin, ymax, xmin, xmax;
+
+  __device__ __forceinline__ void emit(int x0, int y0, int x1, int y1, uint32_t sign) {
+    if (y0 == y1) return;
+    if (out) {
+      out[n] = DevSeg{x0, y0, x1, y1};
+      meta[n] = (cmd << 1) | sign;
+    }
+    n++;
+    rows += (uint32_t((y1 - 1) >> 8) >> kTileShift) - (uint32_t(y0 >> 8) >> kTileShift) + 1u;
+    ymin = min(ymin, y0);
+    ymax = max(ymax, y1);
+    xmin = min(xmin, min(x0, x1));
+    xmax = max(xmax, max(x0, x1));
+  }
+};
+
+enum { CF_X0 = 1, CF_Y0 = 2, CF_X1 = 4, CF_Y1 = 8 };
+
+struct Builder {
+  Sink sink;
+  double cx0, cy0, cx1, cy1;
+  int icx0, icx1;
+  double tol_sq;
+  double acc_x0_y0, acc_x0_y1, acc_x1_y0, acc_x1_y1;
+  // open polyline
+  int px, py;
+  uint32_t psign;
+  bool pasc;
+
+  __device__ __forceinline__ uint32_t fx0(Pt p) const { return uint32_t(!(p.x >= cx0)) << 0; }
+  __device__ __forceinline__ uint32_t fx1(Pt p) const { return uint32_t(!(p.x <= cx1)) << 2; }
+  __device__ __forceinline__ uint32_t fy0(Pt p) const { return uint32_t(!(p.y >= cy0)) << 1; }
+  __device__ __forceinline__ uint32_t fy1(Pt p) const { return uint32_t(!(p.y <= cy1)) << 3; }
+  __device__ __forceinline__ uint32_t fx(Pt p) const { return fx0(p) | fx1(p); }
+  __device__ __forceinline__ uint32_t fy(Pt p) const { return fy0(p) | fy1(p); }
+  __device__ __forceinline__ uint32_t fxy(Pt p) const { return fx(p) | fy(p); }
+
+  // polylines: descending ones run top-down, ascending ones are collected bottom-up.
+  __device__ __forceinline__ void desc_open(int x, int y, uint32_t sign) { px = x; py = y; psign = sign; pasc = false; }
+  __device__ __forceinline__ void asc_open(int x, int y) { px = x; py = y; psign = 1; pasc = true; }
+  __device__ __forceinline__ void add(int x, int y) {
+    if (pasc) sink.emit(x, y, px, py, 1u);
+    else sink.emit(px, py, x, y, psign);
+    px = x; py = y;
+  }
+
+  __device__ void add_line_segment(double x0, double y0, double x1, double y1) {
+    int a = trunc_i(x0), b = trunc_i(y0), c = trunc_i(x1), d = trunc_i(y1);
+    if (b == d) return;
+    if (b < d) sink.emit(a, b, c, d, 0u);
+    else sink.emit(c, d, a, b, 1u);
+  }
+
+  __device__ void emit_left() {
+    int a = trunc_i(acc_x0_y0), b = trunc_i(acc_x0_y1);
+    if (a == b) return;
+    sink.emit(icx0, min(a, b), icx0, max(a, b), uint32_t(a > b));
+  }
+  __device__ void emit_right() {
+    int a = trunc_i(acc_x1_y0), b = trunc_i(acc_x1_y1);
+    if (a == b) return;
+    sink.emit(icx1, min(a, b), icx1, max(a, b), uint32_t(a > b));
+  }
+  __device__ void acc_left(double y0, double y1) {
+    if (acc_x0_y1 == y0) { acc_x0_y1 = y1; return; }
+    emit_left();
+    acc_x0_y0 = y0; acc_x0_y1 = y1;
+  }
+  __device__ void acc_right(double y0, double y1) {
+    if (acc_x1_y1 == y0) { acc_x1_y1 = y1; return; }
+    emit_right();
+    acc_x1_y0 = y0; acc_x1_y1 = y1;
+  }
+  __device__ __forceinline__ void acc_left_s(double y0, double y1, uint32_t s) { if (s) acc_left(y1, y0); else acc_left(y0, y1); }
+  __device__ __forceinline__ void acc_right_s(double y0, double y1, uint32_t s) { if (s) acc_right(y1, y0); else acc_right(y0, y1); }
+  __device__ void done() { emit_left(); emit_right(); }
+};
+
+// Vertex source (EdgeSourcePoly / EdgeSourcePath, edgebuilder_p.h:102-270).
+struct Src {
+  const double* xy;
+  const uint8_t* cmd;   // nullptr for polygons
+  int i, n;
+  bool affine;
+  double m00, m01, m10, m11, m20, m21;
+
+  __device__ __forceinline__ Pt tf(int k) const {
+    double x = xy[2 * k], y = xy[2 * k + 1];
+    if (affine) return Pt{x * m00 + y * m10 + m20, x * m01 + y * m11 + m21};
+    return Pt{x * m00 + m20, y * m11 + m21};
+  }
+  __device__ bool begin(Pt& p) {
+    if (!cmd) {
+      if (i == n) return false;
+      p = tf(i); i++;
+      return true;
+    }
+    for (;;) {
+      if (i == n) return false;
+      uint8_t c = cmd[i]; i++;
+      if (c != 0) continue;
+      p = tf(i - 1);
+      return true;
+    }
+  }
+  __device__ __forceinline__ bool is_close() const { return cmd && i != n && cmd[i] == 5; }
+  __device__ __forceinline__ bool is_line() const { return cmd ? (i != n && cmd[i] == 1) : (i != n); }
+  __device__ __forceinline__ bool is_quad() const { return cmd && i <= n - 2 && cmd[i] == 2; }
+  __device__ __forceinline__ bool is_conic() const { return cmd && i < n - 2 && cmd[i] == 3; }
+  __device__ __forceinline__ bool is_cubic() const { return cmd && i < n - 2 && cmd[i] == 4; }
+  __device__ __forceinline__ bool next_line(Pt& p) { if (!is_line()) return false; p = tf(i); i++; return true; }
+};
+
+// ---------------------------------------------------------------------------------------------
+// line_to (edgebuilder_p.h:1123-1607)
+// ---------------------------------------------------------------------------------------------
+
+__device__ int line_to(Builder& eb, Src& src, Pt& A, uint32_t& AF, Pt b) {
+  Pt p, d;
+  uint32_t b_flags = 0;
+  int x0, y0, x1, y1;
+  double borY0 = 0.0, borY1;
+
+  do {
+    if (!AF) {
+      b_flags = eb.fxy(b);
+      if (!b_flags) {
+        x0 = trunc_i(A.x); y0 = trunc_i(A.y); x1 = trunc_i(b.x); y1 = trunc_i(b.y);
+        for (;;) {
+          if (y0 < y1) {
+DescBegin:
+            eb.desc_open(x0, y0, 0u);
+            eb.add(x1, y1);
+            for (;;) {
+DescLoopA:
+              if (!src.next_line(A)) { A = b; return 0; }
+              b_flags = eb.fxy(A);
+              if (b_flags) { Pt t = A; A = b; b = t; goto BeforeClipEnd; }
+              x0 = trunc_i(A.x); y0 = trunc_i(A.y);
+              if (y0 < y1) { eb.asc_open(x1, y1); eb.add(x0, y0); goto AscLoopB; }
+              eb.add(x0, y0);
+DescLoopB:
+              if (!src.next_line(b)) return 0;
+              b_flags = eb.fxy(b);
+              if (b_flags) goto BeforeClipEnd;
+              x1 = trunc_i(b.x); y1 = trunc_i(b.y);
+              if (y1 < y0) { eb.asc_open(x0, y0); eb.add(x1, y1); goto AscLoopA; }
+              eb.add(x1, y1);
+            }
+          }
+          else if (y0 > y1) {
+AscBegin:
+            eb.asc_open(x0, y0);
+            eb.add(x1, y1);
+            for (;;) {
+AscLoopA:
+              if (!src.next_line(A)) { A = b; return 0; }
+              b_flags = eb.fxy(A);
+              if (b_flags) { Pt t = A; A = b; b = t; goto BeforeClipEnd; }
+              x0 = trunc_i(A.x); y0 = trunc_i(A.y);
+              if (y0 > y1) { eb.desc_open(x1, y1, 0u); eb.add(x0, y0); goto DescLoopB; }
+              eb.add(x0, y0);
+AscLoopB:
+              if (!src.next_line(b)) return 0;
+              b_flags = eb.fxy(b);
+              if (b_flags) goto BeforeClipEnd;
+              x1 = trunc_i(b.x); y1 = trunc_i(b.y);
+              if (y1 > y0) { eb.desc_open(x0, y0, 0u); eb.add(x1, y1); goto DescLoopA; }
+              eb.add(x1, y1);
+            }
+          }
+          else {
+            A = b;
+            if (!src.next_line(b)) return 0;
+            b_flags = eb.fxy(b);
+            if (b_flags) break;
+            x0 = x1; y0 = y1;
+            x1 = trunc_i(b.x); y1 = trunc_i(b.y);
+          }
+        }
+      }
+BeforeClipEnd:
+      p = A;
+      d = Pt{b.x - A.x, b.y - A.y};
+    }
+    else {
+RestartClip:
+      if (AF & CF_Y0) {
+        for (;;) {
+          if (eb.cy0 < b.y) break;
+          A = b;
+          if (!src.next_line(b)) { AF = eb.fx(A) | eb.fy0(A); return 0; }
+        }
+        AF = eb.fx(A) | eb.fy0(A);
+        b_flags = eb.fx(b) | eb.fy1(b);
+        borY0 = eb.cy0;
+        uint32_t common = AF & b_flags;
+        if (common) {
+          borY1 = dmin(eb.cy1, b.y);
+          if (common & CF_X0) eb.acc_left(borY0, borY1); else eb.acc_right(borY0, borY1);
+          A = b; AF = b_flags;
+          continue;
+        }
+      }
+      else if (AF & CF_Y1) {
+        for (;;) {
+          if (eb.cy1 > b.y) break;
+          A = b;
+          if (!src.next_line(b)) { AF = eb.fx(A) | eb.fy1(A); return 0; }
+        }
+        AF = eb.fx(A) | eb.fy1(A);
+        b_flags = eb.fx(b) | eb.fy0(b);
+        borY0 = eb.cy1;
+        uint32_t common = AF & b_flags;
+        if (common) {
+          borY1 = dmax(eb.cy0, b.y);
+          if (common & CF_X0) eb.acc_left(borY0, borY1); else eb.acc_right(borY0, borY1);
+          A = b; AF = b_flags;
+          continue;
+        }
+      }
+      else if (AF & CF_X0) {
+        borY0 = dclamp(A.y, eb.cy0, eb.cy1);
+        for (;;) {
+          if (eb.cx0 < b.x) break;
+          A = b;
+          if (!src.next_line(b)) {
+            AF = eb.fy(A) | eb.fx0(A);
+            borY1 = dclamp(A.y, eb.cy0, eb.cy1);
+            if (borY0 != borY1) eb.acc_left(borY0, borY1);
+            return 0;
+          }
+        }
+        borY1 = dclamp(A.y, eb.cy0, eb.cy1);
+        if (borY0 != borY1) eb.acc_left(borY0, borY1);
+        AF = eb.fx0(A) | eb.fy(A);
+        b_flags = eb.fx1(b) | eb.fy(b);
+        if (AF & b_flags) goto RestartClip;
+        borY0 = borY1;
+      }
+      else {
+        borY0 = dclamp(A.y, eb.cy0, eb.cy1);
+        for (;;) {
+          if (eb.cx1 > b.x) break;
+          A = b;
+          if (!src.next_line(b)) {
+            AF = eb.fy(A) | eb.fx1(A);
+            borY1 = dclamp(A.y, eb.cy0, eb.cy1);
+            if (borY0 != borY1) eb.acc_right(borY0, borY1);
+            return 0;
+          }
+        }
+        borY1 = dclamp(A.y, eb.cy0, eb.cy1);
+        if (borY0 != borY1) eb.acc_right(borY0, borY1);
+        AF = eb.fx1(A) | eb.fy(A);
+        b_flags = eb.fx0(b) | eb.fy(b);
+        if (AF & b_flags) goto RestartClip;
+        borY0 = borY1;
+      }
+
+      d = Pt{b.x - A.x, b.y - A.y};
+      p = Pt{eb.cx1, eb.cy1};
+      switch (AF) {
+        case 0: p = A; break;
+        case CF_X0 | CF_Y0: p.x = eb.cx0; /* fallthrough */
+        case CF_X1 | CF_Y0:
+          p.y = A.y + (p.x - A.x) * d.y / d.x;
+          AF = eb.fy(p);
+          if (p.y >= eb.cy0) break;
+          /* fallthrough */
+        case CF_Y0:
+          p.y = eb.cy0;
+          p.x = A.x + (p.y - A.y) * d.x / d.y;
+          AF = eb.fx(p);
+          break;
+        case CF_X0 | CF_Y1: p.x = eb.cx0; /* fallthrough */
+        case CF_X1 | CF_Y1:
+          p.y = A.y + (p.x - A.x) * d.y / d.x;
+          AF = eb.fy(p);
+          if (p.y <= eb.cy1) break;
+          /* fallthrough */
+        case CF_Y1:
+          p.y = eb.cy1;
+          p.x = A.x + (p.y - A.y) * d.x / d.y;
+          AF = eb.fx(p);
+          break;
+        case CF_X0: p.x = eb.cx0; /* fallthrough */
+        case CF_X1:
+          p.y = A.y + (p.x - A.x) * d.y / d.x;
+          AF = eb.fy(p);
+          break;
+        default:
+          return 1;   // NaN: BL_ERROR_INVALID_GEOMETRY
+      }
+
+      if (AF) {
+        borY1 = dclamp(b.y, eb.cy0, eb.cy1);
+        if (p.x <= eb.cx0) eb.acc_left(borY0, borY1);
+        else if (p.x >= eb.cx1) eb.acc_right(borY0, borY1);
+        A = b; AF = b_flags;
+        continue;
+      }
+
+      borY1 = dclamp(p.y, eb.cy0, eb.cy1);
+      if (borY0 != borY1) {
+        if (p.x <= eb.cx0) eb.acc_left(borY0, borY1);
+        else eb.acc_right(borY0, borY1);
+      }
+
+      if (!b_flags) {
+        A = b;
+        AF = 0;
+        x0 = trunc_i(p.x); y0 = trunc_i(p.y); x1 = trunc_i(b.x); y1 = trunc_i(b.y);
+        if (y0 == y1) continue;
+        if (y0 < y1) goto DescBegin;
+        else goto AscBegin;
+      }
+    }
+
+    {
+      Pt q{eb.cx1, eb.cy1};
+      switch (b_flags) {
+        case CF_X0 | CF_Y0: q.x = eb.cx0; /* fallthrough */
+        case CF_X1 | CF_Y0:
+          q.y = A.y + (q.x - A.x) * d.y / d.x;
+          if (q.y >= eb.cy0) break;
+          /* fallthrough */
+        case CF_Y0:
+          q.y = eb.cy0;
+          q.x = A.x + (q.y - A.y) * d.x / d.y;
+          break;
+        case CF_X0 | CF_Y1: q.x = eb.cx0; /* fallthrough */
+        case CF_X1 | CF_Y1:
+          q.y = A.y + (q.x - A.x) * d.y / d.x;
+          if (q.y <= eb.cy1) break;
+          /* fallthrough */
+        case CF_Y1:
+          q.y = eb.cy1;
+          q.x = A.x + (q.y - A.y) * d.x / d.y;
+          break;
+        case CF_X0: q.x = eb.cx0; /* fallthrough */
+        case CF_X1:
+          q.y = A.y + (q.x - A.x) * d.y / d.x;
+          break;
+        default:
+          return 1;
+      }
+      eb.add_line_segment(p.x, p.y, q.x, q.y);
+      double cby = dclamp(b.y, eb.cy0, eb.cy1);
+      if (q.y != cby) {
+        if (q.x == eb.cx0) eb.acc_left(q.y, cby);
+        else eb.acc_right(q.y, cby);
+      }
+    }
+
+    A = b;
+    AF = b_flags;
+  } while (src.next_line(b));
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Curve splitting (bezier_p.h) and monotonic flattening (edgebuilder_p.h:426-768, :2029-2445)
+// ---------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ double cross(Pt a, Pt b) { return a.x * b.y - a.y * b.x; }
+__device__ __forceinline__ double mag_sq(Pt v) { return v.x * v.x + v.y * v.y; }
+
+__device__ int quad_roots(double* dst, double a, double b, double c, double t_min, double t_max) {
+  double d = dmax(b * b - 4.0 * a * c, 0.0);
+  double s = sqrt(d);
+  double q = -0.5 * (b + copysign(s, b));
+  double t0 = q / a;
+  double t1 = c / q;
+  double x0 = dmin(t0, t1);
+  double x1 = dmax(t1, t0);
+  dst[0] = x0;
+  int n = int((x0 >= t_min) & (x0 <= t_max));
+  dst[n] = x1;
+  n += int((x1 > x0) & (x1 >= t_min) & (x1 <= t_max));
+  return n;
+}
+
+__device__ int split_quad(Pt* c) {
+  Pt c0 = c[0], c1 = c[1], c2 = c[2];
+  double ex = (c0.x - c1.x) / (c0.x - c1.x * 2.0 + c2.x);
+  double ey = (c0.y - c1.y) / (c0.y - c1.y * 2.0 + c2.y);
+  double t0 = dmin(ex, ey), t1 = dmax(ex, ey);
+  double ts[3];
+  int n = 0;
+  ts[n] = t0; n += int((t0 > 0.0) & (t0 < 1.0));
+  ts[n] = t1; n += int((t1 > dmax(t0, 0.0)) & (t1 < 1.0));
+  if (!n) return 0;
+  ts[n++] = 1.0;
+  Pt v1{c1.x - c0.x, c1.y - c0.y}, v2{c2.x - c1.x, c2.y - c1.y};
+  Pt qa{v2.x - v1.x, v2.y - v1.y}, qb{v1.x + v1.x, v1.y + v1.y}, qc = c0;
+  Pt last = c2;
+  double t_cut = 0.0;
+  Pt* out = c;
+  int i = 0;
+  do {
+    double t = ts[i];
+    double dt = (t - t_cut) * 0.5;
+    Pt cp{(qa.x * (t * 2.0) + qb.x) * dt, (qa.y * (t * 2.0) + qb.y) * dt};
+    Pt tp{(qa.x * t + qb.x) * t + qc.x, (qa.y * t + qb.y) * t + qc.y};
+    if (++i == n) tp = last;
+    out[1] = Pt{tp.x - cp.x, tp.y - cp.y};
+    out[2] = tp;
+    out += 2;
+    t_cut = t;
+  } while (i != n);
+  return int(out - c);
+}
+
+__device__ int split_cubic(Pt* c) {
+  Pt c0 = c[0], c1 = c[1], c2 = c[2], c3 = c[3];
+  Pt v1{c1.x - c0.x, c1.y - c0.y}, v2{c2.x - c1.x, c2.y - c1.y}, v3{c3.x - c2.x, c3.y - c2.y};
+  Pt ca{v3.x - v2.x - v2.x + v1.x, v3.y - v2.y - v2.y + v1.y};
+  Pt cb{3.0 * (v2.x - v1.x), 3.0 * (v2.y - v1.y)};
+  Pt cc{3.0 * v1.x, 3.0 * v1.y};
+  Pt cd = c0;
+  double ts[8];
+  int n = 0;
+  double q0 = cross(cb, ca), q1 = cross(cc, ca), q2 = cross(cc, cb);
+  double t_cusp = (q1 / q0) * -0.5;
+  ts[n] = t_cusp; n += int((t_cusp > 0.0) & (t_cusp < 1.0));
+  const double kAfter0 = 1e-40, kBefore1 = 0.999999999999999889;
+  n += quad_roots(ts + n, q0 * 6.0, q1 * 6.0, q2 * 2.0, kAfter0, kBefore1);
+  Pt da{3.0 * (v3.x - v2.x - v2.x + v1.x), 3.0 * (v3.y - v2.y - v2.y + v1.y)};
+  Pt db{6.0 * (v2.x - v1.x), 6.0 * (v2.y - v1.y)};
+  Pt dc{3.0 * v1.x, 3.0 * v1.y};
+  n += quad_roots(ts + n, da.x, db.x, dc.x, kAfter0, kBefore1);
+  n += quad_roots(ts + n, da.y, db.y, dc.y, kAfter0, kBefore1);
+  if (!n) return 0;
+  for (int i = 1; i < n; i++) {
+    double v = ts[i];
+    int j = i;
+    while (j > 0 && v < ts[j - 1]) { ts[j] = ts[j - 1]; j--; }
+    ts[j] = v;
+  }
+  ts[n++] = 1.0;
+  Pt last = c3;
+  Pt* out = c;
+  int i = 0;
+  double t_cut = 0.0;
+  do {
+    double t = ts[i++];
+    if (t == t_cut) continue;
+    const double k1Div3 = 1.0 / 3.0;
+    double dt = (t - t_cut) * k1Div3;
+    Pt tp{((ca.x * t + cb.x) * t + cc.x) * t + cd.x, ((ca.y * t + cb.y) * t + cc.y) * t + cd.y};
+    if (i == n) tp = last;
+    Pt cp1{((ca.x * (t_cut * 3.0) + cb.x * 2.0) * t_cut + cc.x) * dt, ((ca.y * (t_cut * 3.0) + cb.y * 2.0) * t_cut + cc.y) * dt};
+    Pt cp2{((ca.x * (t * 3.0) + cb.x * 2.0) * t + cc.x) * dt, ((ca.y * (t * 3.0) + cb.y * 2.0) * t + cc.y) * dt};
+    out[1] = Pt{out[0].x + cp1.x, out[0].y + cp1.y};
+    out[2] = Pt{tp.x - cp2.x, tp.y - cp2.y};
+    out[3] = tp;
+    out += 3;
+    t_cut = t;
+  } while (i != n);
+  return int(out - c);
+}
+
+struct Step { double value, limit; Pt p01, p12, p23, p012, p123, p0123; };
+
+__device__ __forceinline__ Pt mid(Pt a, Pt b) { return Pt{(a.x + b.x) * 0.5, (a.y + b.y) * 0.5}; }
+
+// Monotonic curve with an explicit subdivision stack (FlattenMonoQuad / FlattenMonoCubic).
+template<int DEG>
+struct Mono {
+  double tol_sq;
+  Pt p[DEG + 1];
+  Pt stack[32 * (DEG + 1)];
+  int sp;
+
+  __device__ __forceinline__ void begin(const Pt* src, uint32_t sign) {
+    sp = 0;
+#pragma unroll
+    for (int i = 0; i <= DEG; i++) p[i] = sign ? src[DEG - i] : src[i];
+  }
+  __device__ __forceinline__ Pt first() const { return p[0]; }
+  __device__ __forceinline__ Pt last() const { return p[DEG]; }
+  __device__ __forceinline__ bool can_pop() const { return sp != 0; }
+  __device__ __forceinline__ bool can_push() const { return sp != 32 * (DEG + 1); }
+  __device__ __forceinline__ bool ltr() const { return p[0].x < p[DEG].x; }
+  __device__ void bound_ltr() {
+#pragma unroll
+    for (int i = 1; i < DEG; i++) { p[i].x = dclamp(p[i].x, p[0].x, p[DEG].x); p[i].y = dclamp(p[i].y, p[0].y, p[DEG].y); }
+  }
+  __device__ void bound_rtl() {
+#pragma unroll
+    for (int i = 1; i < DEG; i++) { p[i].x = dclamp(p[i].x, p[DEG].x, p[0].x); p[i].y = dclamp(p[i].y, p[0].y, p[DEG].y); }
+  }
+  __device__ bool is_flat(Step& s) const {
+    if (DEG == 2) {
+      Pt v1{p[1].x - p[0].x, p[1].y - p[0].y}, v2{p[2].x - p[0].x, p[2].y - p[0].y};
+      double d = cross(v2, v1);
+      double len_sq = mag_sq(v2);
+      s.value = d * d;
+      s.limit = tol_sq * len_sq;
+    }
+    else {
+      Pt v{p[DEG].x - p[0].x, p[DEG].y - p[0].y};
+      Pt a{p[1].x - p[0].x, p[1].y - p[0].y}, b{p[2].x - p[0].x, p[2].y - p[0].y};
+      double c1 = cross(v, a), c2 = cross(v, b);
+      double d1 = c1 * c1, d2 = c2 * c2;
+      double len_sq = mag_sq(v);
+      s.value = dmax(d1, d2);
+      s.limit = tol_sq * len_sq;
+    }
+    return s.value <= s.limit;
+  }
+  __device__ void split(Step& s) const {
+    if (DEG == 2) {
+      s.p01 = mid(p[0], p[1]); s.p12 = mid(p[1], p[2]); s.p012 = mid(s.p01, s.p12);
+    }
+    else {
+      s.p01 = mid(p[0], p[1]); s.p12 = mid(p[1], p[2]); s.p23 = mid(p[2], p[DEG]);
+      s.p012 = mid(s.p01, s.p12); s.p123 = mid(s.p12, s.p23); s.p0123 = mid(s.p012, s.p123);
+    }
+  }
+  __device__ __forceinline__ Pt step_mid(const Step& s) const { return DEG == 2 ? s.p012 : s.p0123; }
+  __device__ void push(const Step& s) {
+    if (DEG == 2) {
+      stack[sp] = s.p012; stack[sp + 1] = s.p12; stack[sp + 2] = p[2];
+      sp += 3;
+      p[1] = s.p01; p[2] = s.p012;
+    }
+    else {
+      stack[sp] = s.p0123; stack[sp + 1] = s.p123; stack[sp + 2] = s.p23; stack[sp + 3] = p[DEG];
+      sp += 4;
+      p[1] = s.p01; p[2] = s.p012; p[DEG] = s.p0123;
+    }
+  }
+  __device__ void discard_and_advance(const Step& s) {
+    if (DEG == 2) { p[0] = s.p012; p[1] = s.p12; }
+    else { p[0] = s.p0123; p[1] = s.p123; p[2] = s.p23; }
+  }
+  __device__ void pop() {
+    sp -= DEG + 1;
+#pragma unroll
+    for (int i = 0; i <= DEG; i++) p[i] = stack[sp + i];
+  }
+};
+
+__device__ __forceinline__ double dx_div_dy(Pt a, Pt b) { return (b.x - a.x) / (b.y - a.y); }
+__device__ __forceinline__ double dy_div_dx(Pt a, Pt b) { return (b.y - a.y) / (b.x - a.x); }
+
+template<int DEG>
+__device__ void flatten_safe(Builder& eb, Mono<DEG>& mc, const Pt* src, uint32_t sign) {
+  mc.begin(src, sign);
+  if (mc.ltr()) mc.bound_ltr(); else mc.bound_rtl();
+  eb.desc_open(trunc_i(mc.first().x), trunc_i(mc.first().y), sign);
+  for (;;) {
+    Step step;
+    if (!mc.is_flat(step)) {
+      if (mc.can_push()) { mc.split(step); mc.push(step); continue; }
+    }
+    eb.add(trunc_i(mc.last().x), trunc_i(mc.last().y));
+    if (!mc.can_pop()) break;
+    mc.pop();
+  }
+}
+
+template<int DEG>
+__device__ void flatten_unsafe(Builder& eb, Mono<DEG>& mc, const Pt* src, uint32_t sign) {
+  mc.begin(src, sign);
+  double y_start = mc.first().y;
+  double y_end = dmin(mc.last().y, eb.cy1);
+  if ((y_start >= y_end) | (y_end <= eb.cy0)) return;
+
+  const double kDeltaLimit = 0.00390625;
+  double x_delta = fabs(mc.first().x - mc.last().x);
+  uint32_t out = 0;
+  Step step;
+
+  if (x_delta <= kDeltaLimit) {
+    y_start = dmax(y_start, eb.cy0);
+    double x_min = dmin(mc.first().x, mc.last().x);
+    double x_max = dmax(mc.first().x, mc.last().x);
+    if (x_max <= eb.cx0) eb.acc_left_s(y_start, y_end, sign);
+    else if (x_min >= eb.cx1) eb.acc_right_s(y_start, y_end, sign);
+    else {
+      eb.desc_open(trunc_i(mc.first().x), trunc_i(y_start), sign);
+      eb.add(trunc_i(mc.last().x), trunc_i(y_end));
+    }
+    return;
+  }
+  else if (mc.ltr()) {
+    mc.bound_ltr();
+    if (y_start < eb.cy0) {
+      y_start = eb.cy0;
+      for (;;) {
+        out = (mc.first().x >= eb.cx1);
+        if (out) break;
+        if (!mc.is_flat(step)) {
+          mc.split(step);
+          if (mc.step_mid(step).y <= eb.cy0) { mc.discard_and_advance(step); continue; }
+          if (mc.can_push()) { mc.push(step); continue; }
+        }
+        if (mc.last().y > eb.cy0) {
+          out = mc.last().x < eb.cx0;
+          if (out) goto LTR_BeforeX0_Pop;
+          double xc = mc.first().x + (eb.cy0 - mc.first().y) * dx_div_dy(mc.first(), mc.last());
+          if (xc <= eb.cx0) goto LTR_BeforeX0_Clip;
+          out = (xc >= eb.cx1);
+          if (out) break;
+          eb.desc_open(trunc_i(xc), trunc_i(eb.cy0), sign);
+          goto LTR_AddLine;
+        }
+        if (!mc.can_pop()) break;
+        mc.pop();
+      }
+      out <<= 2;
+    }
+    else if (y_start < eb.cy1) {
+      if (mc.first().x < eb.cx0) {
+        for (;;) {
+          out = (mc.first().y >= eb.cy1);
+          if (out) break;
+          if (!mc.is_flat(step)) {
+            mc.split(step);
+            if (mc.step_mid(step).x <= eb.cx0) { mc.discard_and_advance(step); continue; }
+            if (mc.can_push()) { mc.push(step); continue; }
+          }
+          if (mc.last().x > eb.cx0) {
+LTR_BeforeX0_Clip:
+            {
+              double yc = mc.first().y + (eb.cx0 - mc.first().x) * dy_div_dx(mc.first(), mc.last());
+              out = (yc >= y_end);
+              if (out) break;
+              if (y_start < yc) eb.acc_left_s(y_start, yc, sign);
+              eb.desc_open(trunc_i(eb.cx0), trunc_i(yc), sign);
+              goto LTR_AddLine;
+            }
+          }
+          out = (mc.last().y >= y_end);
+          if (out) break;
+LTR_BeforeX0_Pop:
+          if (!mc.can_pop()) break;
+          mc.pop();
+        }
+      }
+      else if (mc.first().x < eb.cx1) {
+        eb.desc_open(trunc_i(mc.first().x), trunc_i(mc.first().y), sign);
+        for (;;) {
+          if (!mc.is_flat(step)) {
+            mc.split(step);
+            if (mc.can_push()) { mc.push(step); continue; }
+          }
+LTR_AddLine:
+          out = mc.last().x > eb.cx1;
+          if (out) {
+            double yc = mc.first().y + (eb.cx1 - mc.first().x) * dy_div_dx(mc.first(), mc.last());
+            if (yc <= y_end) {
+              y_start = yc;
+              eb.add(trunc_i(eb.cx1), trunc_i(yc));
+              break;
+            }
+          }
+          out = mc.last().y >= eb.cy1;
+          if (out) {
+            double xc = dmin(mc.first().x + (eb.cy1 - mc.first().y) * dx_div_dy(mc.first(), mc.last()), eb.cx1);
+            eb.add(trunc_i(xc), trunc_i(eb.cy1));
+            out = 0;
+            break;
+          }
+          eb.add(trunc_i(mc.last().x), trunc_i(mc.last().y));
+          if (!mc.can_pop()) break;
+          mc.pop();
+        }
+        out <<= 2;
+      }
+      else {
+        out = CF_X1;
+      }
+    }
+  }
+  else {
+    mc.bound_rtl();
+    if (y_start < eb.cy0) {
+      y_start = eb.cy0;
+      for (;;) {
+        out = (mc.first().x <= eb.cx0);
+        if (out) break;
+        if (!mc.is_flat(step)) {
+          mc.split(step);
+          if (mc.step_mid(step).y <= eb.cy0) { mc.discard_and_advance(step); continue; }
+          if (mc.can_push()) { mc.push(step); continue; }
+        }
+        if (mc.last().y > eb.cy0) {
+          out = mc.last().x > eb.cx1;
+          if (out) goto RTL_AfterX1_Pop;
+          double xc = mc.first().x + (eb.cy0 - mc.first().y) * dx_div_dy(mc.first(), mc.last());
+          if (xc >= eb.cx1) goto RTL_AfterX1_Clip;
+          out = (xc <= eb.cx0);
+          if (out) break;
+          eb.desc_open(trunc_i(xc), trunc_i(eb.cy0), sign);
+          goto RTL_AddLine;
+        }
+        if (!mc.can_pop()) break;
+        mc.pop();
+      }
+    }
+    else if (y_start < eb.cy1) {
+      if (mc.first().x > eb.cx1) {
+        for (;;) {
+          out = (mc.first().y >= eb.cy1);
+          if (out) break;
+          if (!mc.is_flat(step)) {
+            mc.split(step);
+            if (mc.step_mid(step).x >= eb.cx1) { mc.discard_and_advance(step); continue; }
+            if (mc.can_push()) { mc.push(step); continue; }
+          }
+          if (mc.last().x < eb.cx1) {
+RTL_AfterX1_Clip:
+            {
+              double yc = mc.first().y + (eb.cx1 - mc.first().x) * dy_div_dx(mc.first(), mc.last());
+              out = (yc >= y_end);
+              if (out) break;
+              if (y_start < yc) eb.acc_right_s(y_start, yc, sign);
+              eb.desc_open(trunc_i(eb.cx1), trunc_i(yc), sign);
+              goto RTL_AddLine;
+            }
+          }
+          out = (mc.last().y >= y_end);
+          if (out) break;
+RTL_AfterX1_Pop:
+          if (!mc.can_pop()) break;
+          mc.pop();
+        }
+        out <<= 2;
+      }
+      else if (mc.first().x > eb.cx0) {
+        eb.desc_open(trunc_i(mc.first().x), trunc_i(mc.first().y), sign);
+        for (;;) {
+          if (!mc.is_flat(step)) {
+            mc.split(step);
+            if (mc.can_push()) { mc.push(step); continue; }
+          }
+RTL_AddLine:
+          out = mc.last().x < eb.cx0;
+          if (out) {
+            double yc = mc.first().y + (eb.cx0 - mc.first().x) * dy_div_dx(mc.first(), mc.last());
+            if (yc <= y_end) {
+              y_start = yc;
+              eb.add(trunc_i(eb.cx0), trunc_i(yc));
+              break;
+            }
+          }
+          out = mc.last().y >= eb.cy1;
+          if (out) {
+            double xc = dmax(mc.first().x + (eb.cy1 - mc.first().y) * dx_div_dy(mc.first(), mc.last()), eb.cx0);
+            eb.add(trunc_i(xc), trunc_i(eb.cy1));
+            out = 0;
+            break;
+          }
+          eb.add(trunc_i(mc.last().x), trunc_i(mc.last().y));
+          if (!mc.can_pop()) break;
+          mc.pop();
+        }
+      }
+      else {
+        out = CF_X0;
+      }
+    }
+  }
+
+  if (out && y_start < y_end) {
+    if (out & CF_X0) eb.acc_left_s(y_start, y_end, sign);
+    else eb.acc_right_s(y_start, y_end, sign);
+  }
+}
+
+// quad_to / cubic_to / conic_to (edgebuilder_p.h:1618-2022); DEG 2 with `conic` reads the conic
+// record layout (control point, weight slot, end point) but flattens like a quad, as the
+// reference does.
+template<int DEG>
+__device__ void curve_to(Builder& eb, Src& src, Pt& p0, uint32_t& p0_flags, bool conic) {
+  Pt spline[DEG == 3 ? 25 : 7];
+  auto next = [&](void) {
+    if (DEG == 3) { spline[1] = src.tf(src.i); spline[2] = src.tf(src.i + 1); spline[3] = src.tf(src.i + 2); src.i += 3; }
+    else if (conic) { spline[1] = src.tf(src.i); spline[2] = src.tf(src.i + 2); src.i += 2; }
+    else { spline[1] = src.tf(src.i); spline[2] = src.tf(src.i + 1); src.i += 2; }
+  };
+  auto has_next = [&](void) -> bool {
+    return DEG == 3 ? src.is_cubic() : (conic ? src.is_conic() : src.is_quad());
+  };
+  next();
+  Mono<DEG> mc;
+  mc.tol_sq = eb.tol_sq;
+
+  for (;;) {
+    uint32_t fl[DEG + 1];
+    uint32_t common = p0_flags;
+#pragma unroll
+    for (int i = 1; i <= DEG; i++) { fl[i] = eb.fxy(spline[i]); common &= fl[i]; }
+
+    if (common) {
+      bool end = false;
+      if (common & CF_Y0) {
+        for (;;) {
+          p0 = spline[DEG];
+          end = !has_next();
+          if (end) break;
+          next();
+          bool all = true;
+#pragma unroll
+          for (int i = 1; i <= DEG; i++) all &= (spline[i].y <= eb.cy0);
+          if (!all) break;
+        }
+      }
+      else if (common & CF_Y1) {
+        for (;;) {
+          p0 = spline[DEG];
+          end = !has_next();
+          if (end) break;
+          next();
+          bool all = true;
+#pragma unroll
+          for (int i = 1; i <= DEG; i++) all &= (spline[i].y >= eb.cy1);
+          if (!all) break;
+        }
+      }
+      else {
+        double y0 = dclamp(p0.y, eb.cy0, eb.cy1);
+        bool left = (common & CF_X0) != 0;
+        for (;;) {
+          p0 = spline[DEG];
+          end = !has_next();
+          if (end) break;
+          next();
+          bool all = true;
+#pragma unroll
+          for (int i = 1; i <= DEG; i++) all &= left ? (spline[i].x <= eb.cx0) : (spline[i].x >= eb.cx1);
+          if (!all) break;
+        }
+        double y1 = dclamp(p0.y, eb.cy0, eb.cy1);
+        if (left) eb.acc_left(y0, y1); else eb.acc_right(y0, y1);
+      }
+      p0_flags = eb.fxy(p0);
+      if (end) return;
+      continue;
+    }
+
+    spline[0] = p0;
+    int nout = DEG == 3 ? split_cubic(spline) : split_quad(spline);
+    if (nout == 0) nout = DEG;
+
+    uint32_t any = p0_flags;
+#pragma unroll
+    for (int i = 1; i <= DEG; i++) any |= fl[i];
+
+    for (int k = 0; k < nout; k += DEG) {
+      const Pt* sp = spline + k;
+      uint32_t sign = sp[0].y > sp[DEG].y;
+      if (any) flatten_unsafe<DEG>(eb, mc, sp, sign);
+      else flatten_safe<DEG>(eb, mc, sp, sign);
+    }
+    p0 = spline[nout];
+    if (any) p0_flags = fl[DEG];
+
+    if (!has_next()) return;
+    next();
+  }
+}
+
+// add_from_source (edgebuilder_p.h:1032-1070) for a closed fill. Returns 0 or 1 (invalid).
+__device__ int build(Builder& eb, Src& src) {
+  Pt a;
+  uint32_t a_flags;
+  while (src.begin(a)) {
+    Pt start = a, b;
+    bool done = false;
+    a_flags = eb.fxy(a);
+    for (;;) {
+      if (src.is_line()) {
+        b = src.tf(src.i); src.i++;
+LineTo:
+        if (line_to(eb, src, a, a_flags, b)) return 1;
+        if (done) break;
+      }
+      else if (src.is_quad()) curve_to<2>(eb, src, a, a_flags, false);
+      else if (src.is_cubic()) curve_to<3>(eb, src, a, a_flags, false);
+      else if (src.is_conic()) curve_to<2>(eb, src, a, a_flags, true);
+      else {
+        b = start;
+        done = true;
+        goto LineTo;
+      }
+    }
+  }
+  eb.done();
+  return 0;
+}
+
+}  // namespace eb
+}  // namespace blgpu

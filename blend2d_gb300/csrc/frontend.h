@@ -1,0 +1,62 @@
+// frontend.h - host-side rendering-context front end (the part of BLRasterContextImpl that stays
+// on the CPU in the reference too): state, transforms, style resolution and fetch-data setup.
+//
+// Every formula follows the reference (file:line at each function in frontend.cpp) and runs in
+// IEEE double with no FMA contraction (-ffp-contract=off), so the fetch parameters the kernels
+// consume are bit-identical to the ones the reference pipeline consumes.
+#pragma once
+
+#include <stdint.h>
+
+#include <vector>
+
+#include "blgpu_internal.h"
+
+namespace blgpu {
+
+struct Mat { double m00, m01, m10, m11, m20, m21; };
+
+enum TransformType : int { kTTIdentity = 0, kTTTranslate, kTTScale, kTTSwap, kTTAffine, kTTInvalid };
+enum SrcFormat : int { kFmtPRGB32 = 0, kFmtFRGB32 = 1, kFmtZERO32 = 2 };
+
+int trunc_to_int(double x);
+int64_t floor_to_int64(double x);
+int round_to_int(double x);
+void mat_multiply(Mat& dst, const Mat& a, const Mat& b);
+bool mat_invert(Mat& dst, const Mat& src);
+int mat_type(const Mat& m);
+uint32_t premultiply(uint32_t argb32);
+
+// A resolved fill style: fetch parameters plus what the frame must provide (LUT, image).
+struct HostStyle {
+  bool nop = true;                  // NoFillStyle
+  int format = kFmtPRGB32;          // source format for comp-op simplification
+  DevStyle dev{};
+  std::vector<DevStop> stops;       // gradient stops (LUT to build) when dev.lut_size != 0
+  int image = -1;                   // frame image index for patterns
+};
+
+struct GradientDesc {
+  uint32_t type, extend;
+  double values[6];
+  const DevStop* stops;
+  size_t stop_count;
+  const double* transform;
+};
+
+// Pattern source as seen by the front end: the image is already registered in the frame.
+struct PatternDesc {
+  int image;                        // frame image index
+  int img_w, img_h;
+  int area[4];
+  uint32_t extend;
+  const double* transform;
+};
+
+void style_solid(HostStyle& s, uint32_t argb32);
+void style_gradient(HostStyle& s, const GradientDesc& g, const Mat& final_transform);
+void style_pattern(HostStyle& s, const PatternDesc& p, uint32_t pattern_quality, const Mat& final_transform);
+
+int default_band_height(int width);
+
+}  // namespace blgpu

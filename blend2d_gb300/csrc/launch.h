@@ -1,0 +1,26 @@
+// launch.h - host entry points of the device pipeline (implemented in kernels.cu). Each returns
+// the number of kernels it launched on `st`.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "blgpu_internal.h"
+
+namespace blgpu {
+
+int exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* tmp, cudaStream_t st);
+uint32_t scan_temp_words(uint32_t n);
+int launch_total(const uint32_t* counts, const uint32_t* offsets, uint32_t n, uint32_t* total, cudaStream_t st);
+int launch_sum(const uint32_t* in, uint32_t n, uint32_t* total, cudaStream_t st);
+
+int launch_lut(const FrameView& f, cudaStream_t st);
+int launch_edge_count(const FrameView& f, cudaStream_t st);
+int launch_edge_emit(const FrameView& f, const uint32_t* seg_offsets, cudaStream_t st);
+int launch_cmd_tiles(const FrameView& f, uint32_t* cmdrow_counts_per_cmd, cudaStream_t st);
+int launch_seg_bin(const FrameView& f, int scatter, cudaStream_t st);
+int launch_rows_and_tiles(const FrameView& f, uint32_t* row_canvas, cudaStream_t st);
+int launch_fine(const FrameView& f, cudaStream_t st);
+int fine_grid_size();
+
+}  // namespace blgpu

@@ -1,0 +1,457 @@
+// runtime.cpp - device runtime: one upload per frame, the two halves of the device pipeline, one
+// download per host canvas, CUDA-graph replay of the last frame.
+//
+// The pipeline needs four sizes that only the device knows after edge building (segments,
+// seglist entries, (command, tile-row) slots, row-list entries). The counting half computes them
+// and the host reads them back in one 16-byte copy; the rendering half then runs on buffers
+// sized from them. Replays reuse the cached sizes, so a replayed frame has no host round trip and
+// can be captured into a single CUDA graph.
+#include "runtime.h"
+
+#include <string.h>
+
+#include <algorithm>
+
+#include "launch.h"
+
+namespace blgpu {
+
+BLGpuResult cuda_result(cudaError_t e) {
+  if (e == cudaSuccess) return BLGPU_SUCCESS;
+  if (e == cudaErrorMemoryAllocation) return BLGPU_ERROR_OUT_OF_MEMORY;
+  return BLGPU_ERROR_DEVICE;
+}
+
+#define BLGPU_CHECK(expr)                              \
+  do {                                                 \
+    cudaError_t e_ = (expr);                           \
+    if (e_ != cudaSuccess) return cuda_result(e_);     \
+  } while (0)
+
+static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
+
+// --- Frame ------------------------------------------------------------------------------------
+
+void Frame::clear() {
+  cmds.clear(); styles.clear(); xforms.clear(); canvases.clear(); targets.clear();
+  verts.clear(); path_cmds.clear(); lut_jobs.clear(); stops.clear(); images.clear();
+  image_words = 0; lut_words = 0; tiles = 0; rows = 0;
+  generation++;
+}
+
+static int band_height_for(int width) {
+  int bh = 64;
+  size_t pixel_count = size_t(unsigned(width)) * size_t(bh);
+  do {
+    if (pixel_count * 4u <= 1024u * 256u) break;
+    bh >>= 1;
+    pixel_count >>= 1;
+  } while (bh > 8);
+  return bh;
+}
+
+uint32_t Frame::add_canvas(const BLGpuImage& image, bool upload) {
+  DevCanvas cv{};
+  cv.w = image.width;
+  cv.h = image.height;
+  cv.band_height = band_height_for(image.width);
+  cv.tiles_x = (image.width + kTileW - 1) / kTileW;
+  cv.tiles_y = (image.height + kTileH - 1) / kTileH;
+  cv.tile_base = tiles;
+  cv.row_base = rows;
+  cv.cmd_first = uint32_t(cmds.size());
+  cv.cmd_count = 0;
+  tiles += uint32_t(cv.tiles_x) * uint32_t(cv.tiles_y);
+  rows += uint32_t(cv.tiles_y);
+  canvases.push_back(cv);
+  targets.push_back(FrameTarget{image, upload});
+  return uint32_t(canvases.size() - 1);
+}
+
+uint64_t Frame::add_image(const BLGpuImage& image) {
+  for (const FrameImage& im : images)
+    if (im.pixels == image.pixel_data && im.w == image.width && im.h == image.height && im.stride == image.stride)
+      return im.pool_offset;
+  FrameImage im;
+  im.pixels = image.pixel_data;
+  im.stride = image.stride;
+  im.w = image.width;
+  im.h = image.height;
+  im.device = (image.flags & BLGPU_IMAGE_DEVICE_MEMORY) != 0;
+  im.pool_offset = image_words;
+  image_words += align_up(uint64_t(uint32_t(image.width)) * uint32_t(image.height), 4);
+  images.push_back(im);
+  return im.pool_offset;
+}
+
+// --- device memory ----------------------------------------------------------------------------
+
+cudaError_t DeviceBuffer::reserve(size_t bytes) {
+  if (bytes <= size) return cudaSuccess;
+  release();
+  size_t want = std::max(bytes, size_t(1) << 20);
+  want = align_up(want + want / 4, size_t(1) << 20);
+  cudaError_t e = cudaMalloc(&ptr, want);
+  if (e != cudaSuccess) {
+    ptr = nullptr;
+    e = cudaMalloc(&ptr, bytes);
+    if (e != cudaSuccess) { ptr = nullptr; size = 0; return e; }
+    want = bytes;
+  }
+  size = want;
+  return cudaSuccess;
+}
+
+void DeviceBuffer::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  size = 0;
+}
+
+// Bump allocator over a planned layout: first pass measures, second pass assigns.
+struct Layout {
+  size_t off = 0;
+  char* base = nullptr;
+  template <typename T>
+  T* take(size_t count) {
+    off = align_up(off, 256);
+    T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+    off += sizeof(T) * count;
+    return p;
+  }
+};
+
+// --- runtime ----------------------------------------------------------------------------------
+
+BLGpuResult Runtime::init(const BLGpuRuntimeCreateInfo* info) {
+  device = info ? info->device : 0;
+  lut_variant = info ? info->lut_variant : kLutSSE2;
+  if (lut_variant > kLutScalar) return BLGPU_ERROR_INVALID_VALUE;
+  int count = 0;
+  BLGPU_CHECK(cudaGetDeviceCount(&count));
+  if (device < 0 || device >= count) return BLGPU_ERROR_INVALID_VALUE;
+  BLGPU_CHECK(cudaSetDevice(device));
+  BLGPU_CHECK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
+  if (info && info->cuda_stream) {
+    stream = static_cast<cudaStream_t>(info->cuda_stream);
+    own_stream = false;
+  }
+  else {
+    BLGPU_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    own_stream = true;
+  }
+  for (auto& e : ev) BLGPU_CHECK(cudaEventCreate(&e));
+  BLGPU_CHECK(cudaMallocHost(reinterpret_cast<void**>(&host_totals), 64));
+  return BLGPU_SUCCESS;
+}
+
+void Runtime::destroy() {
+  cudaSetDevice(device);
+  if (stream) cudaStreamSynchronize(stream);
+  if (graph) cudaGraphExecDestroy(graph);
+  graph = nullptr;
+  for (auto& e : ev) if (e) cudaEventDestroy(e);
+  in_buf.release();
+  dyn_buf.release();
+  if (host_staging) cudaFreeHost(host_staging);
+  if (host_totals) cudaFreeHost(host_totals);
+  if (own_stream && stream) cudaStreamDestroy(stream);
+  stream = nullptr;
+}
+
+static bool device_target_direct(const BLGpuImage& im) {
+  return (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) && (reinterpret_cast<uintptr_t>(im.pixel_data) & 15u) == 0 &&
+         (im.stride & 15) == 0 && im.stride >= intptr_t(im.width) * 4;
+}
+
+BLGpuResult Runtime::upload(const Frame& fr) {
+  const uint32_t nc = uint32_t(fr.cmds.size());
+  const uint32_t ncv = uint32_t(fr.canvases.size());
+
+  // Plan: [staged inputs][luts][canvases][work arrays]
+  auto plan = [&](Layout& L, FrameView& v, std::vector<uint32_t*>* cpix) -> size_t {
+    v.cmds_rw = L.take<DevCmd>(nc);
+    v.cmds = v.cmds_rw;
+    v.styles = L.take<DevStyle>(fr.styles.size());
+    v.xforms = L.take<DevXform>(fr.xforms.size());
+    v.canvases = L.take<DevCanvas>(ncv);
+    v.verts = L.take<double>(fr.verts.size());
+    v.path_cmds = L.take<uint8_t>(fr.path_cmds.size());
+    v.lut_jobs = L.take<DevLutJob>(fr.lut_jobs.size());
+    v.stops = L.take<DevStop>(fr.stops.size());
+    v.images = L.take<uint32_t>(fr.image_words);
+    size_t staged_end = align_up(L.off, 256);
+    v.luts = L.take<uint32_t>(fr.lut_words);
+    for (uint32_t i = 0; i < ncv; i++) {
+      const BLGpuImage& im = fr.targets[i].image;
+      uint32_t* p;
+      if (device_target_direct(im)) p = static_cast<uint32_t*>(im.pixel_data);
+      else p = L.take<uint32_t>(size_t(align_up(uint32_t(im.width), 4)) * uint32_t(im.height));
+      if (cpix) (*cpix)[i] = p;
+    }
+    v.seg_counts = L.take<uint32_t>(nc);
+    v.seg_rows = L.take<uint32_t>(nc);
+    seg_offsets = L.take<uint32_t>(nc + 1);
+    v.cmd_tile_x = L.take<uint32_t>(nc);
+    v.cmd_tile_y = L.take<uint32_t>(nc);
+    cmdrow_per_cmd = L.take<uint32_t>(nc + 1);
+    v.cmdrow_base = L.take<uint32_t>(nc + 1);
+    v.row_counts = L.take<uint32_t>(fr.rows + 1);
+    v.row_offsets = L.take<uint32_t>(fr.rows + 1);
+    row_canvas = L.take<uint32_t>(fr.rows + 1);
+    v.tile_order = L.take<uint32_t>(fr.tiles + 1);
+    v.tile_canvas = L.take<uint32_t>(fr.tiles + 1);
+    v.work_counter = L.take<uint32_t>(16);   // [0] work counter, [4..8) totals, [8..12) error flags
+    v.totals = v.work_counter + 4;
+    v.error_flags = v.work_counter + 8;
+    scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, fr.rows + 1)));
+    return staged_end;
+  };
+
+  FrameView v{};
+  Layout measure;
+  plan(measure, v, nullptr);
+  size_t total = measure.off;
+  if (total > in_buf.size) {
+    graph_valid = false;
+    BLGPU_CHECK(cudaStreamSynchronize(stream));
+    BLGPU_CHECK(in_buf.reserve(total));
+  }
+  Layout L;
+  L.base = static_cast<char*>(in_buf.ptr);
+  canvas_dev.assign(ncv, nullptr);
+  size_t staged_bytes = plan(L, v, &canvas_dev);
+
+  // Pack the staged inputs into pinned memory with the same layout, then one H2D copy.
+  if (staged_bytes > host_staging_size) {
+    BLGPU_CHECK(cudaStreamSynchronize(stream));
+    if (host_staging) cudaFreeHost(host_staging);
+    host_staging = nullptr;
+    size_t want = align_up(staged_bytes + staged_bytes / 4, size_t(1) << 20);
+    BLGPU_CHECK(cudaMallocHost(&host_staging, want));
+    host_staging_size = want;
+  }
+  else {
+    // the previous frame's copy out of the staging buffer must have completed
+    BLGPU_CHECK(cudaStreamSynchronize(stream));
+  }
+  char* hs = static_cast<char*>(host_staging);
+  char* db = static_cast<char*>(in_buf.ptr);
+  auto put = [&](const void* dev_ptr, const void* src, size_t bytes) {
+    if (bytes) memcpy(hs + (static_cast<const char*>(dev_ptr) - db), src, bytes);
+  };
+  put(v.cmds, fr.cmds.data(), sizeof(DevCmd) * nc);
+  put(v.styles, fr.styles.data(), sizeof(DevStyle) * fr.styles.size());
+  put(v.xforms, fr.xforms.data(), sizeof(DevXform) * fr.xforms.size());
+  std::vector<DevCanvas> cvs = fr.canvases;
+  canvas_stride.assign(ncv, 0);
+  for (uint32_t i = 0; i < ncv; i++) {
+    const BLGpuImage& im = fr.targets[i].image;
+    cvs[i].pixels = canvas_dev[i];
+    cvs[i].stride = device_target_direct(im) ? int32_t(im.stride / 4) : int32_t(align_up(uint32_t(im.width), 4));
+    canvas_stride[i] = cvs[i].stride;
+  }
+  put(v.canvases, cvs.data(), sizeof(DevCanvas) * ncv);
+  put(v.verts, fr.verts.data(), sizeof(double) * fr.verts.size());
+  put(v.path_cmds, fr.path_cmds.data(), fr.path_cmds.size());
+  put(v.lut_jobs, fr.lut_jobs.data(), sizeof(DevLutJob) * fr.lut_jobs.size());
+  put(v.stops, fr.stops.data(), sizeof(DevStop) * fr.stops.size());
+  for (const FrameImage& im : fr.images) {
+    if (im.device) continue;
+    char* dst = hs + (reinterpret_cast<const char*>(v.images + im.pool_offset) - db);
+    for (int y = 0; y < im.h; y++)
+      memcpy(dst + size_t(y) * size_t(im.w) * 4u, static_cast<const char*>(im.pixels) + intptr_t(y) * im.stride,
+             size_t(im.w) * 4u);
+  }
+  if (staged_bytes) BLGPU_CHECK(cudaMemcpyAsync(in_buf.ptr, host_staging, staged_bytes, cudaMemcpyHostToDevice, stream));
+  for (const FrameImage& im : fr.images) {
+    if (!im.device) continue;
+    BLGPU_CHECK(cudaMemcpy2DAsync(const_cast<uint32_t*>(v.images) + im.pool_offset, size_t(im.w) * 4u, im.pixels,
+                                  size_t(im.stride), size_t(im.w) * 4u, size_t(im.h), cudaMemcpyDeviceToDevice, stream));
+  }
+  // Canvas content (the pipeline composites onto it).
+  for (uint32_t i = 0; i < ncv; i++) {
+    const FrameTarget& t = fr.targets[i];
+    const BLGpuImage& im = t.image;
+    if (!t.upload || device_target_direct(im) || im.width == 0 || im.height == 0) continue;
+    bool dev = (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) != 0;
+    BLGPU_CHECK(cudaMemcpy2DAsync(canvas_dev[i], size_t(canvas_stride[i]) * 4u, im.pixel_data, size_t(im.stride),
+                                  size_t(im.width) * 4u, size_t(im.height),
+                                  dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
+  }
+
+  v.num_cmds = nc;
+  v.num_canvases = ncv;
+  v.num_tiles = fr.tiles;
+  v.num_rows = fr.rows;
+  v.num_lut_jobs = uint32_t(fr.lut_jobs.size());
+  v.pixels = nullptr;
+  view = v;
+  targets = fr.targets;
+  return BLGPU_SUCCESS;
+}
+
+// Counting half: LUTs, edge counts + bboxes, tile ranges, row-list sizes, totals.
+int Runtime::enqueue_count_half(cudaStream_t st) {
+  const FrameView& f = view;
+  int k = 0;
+  cudaMemsetAsync(f.work_counter, 0, sizeof(uint32_t) * 16, st);
+  cudaMemsetAsync(f.row_counts, 0, sizeof(uint32_t) * (f.num_rows + 1), st);
+  k += launch_lut(f, st);
+  k += launch_edge_count(f, st);
+  k += exclusive_scan(f.seg_counts, seg_offsets, f.num_cmds, scan_tmp, st);
+  k += launch_total(f.seg_counts, seg_offsets, f.num_cmds, f.totals + 0, st);
+  k += launch_sum(f.seg_rows, f.num_cmds, f.totals + 1, st);
+  k += launch_cmd_tiles(f, cmdrow_per_cmd, st);
+  k += exclusive_scan(cmdrow_per_cmd, f.cmdrow_base, f.num_cmds, scan_tmp, st);
+  k += launch_total(cmdrow_per_cmd, f.cmdrow_base, f.num_cmds, f.totals + 2, st);
+  k += exclusive_scan(f.row_counts, f.row_offsets, f.num_rows, scan_tmp, st);
+  k += launch_total(f.row_counts, f.row_offsets, f.num_rows, f.totals + 3, st);
+  return k;
+}
+
+// Rendering half: segments, (command, row) segment lists, row command lists, fine tiles.
+int Runtime::enqueue_render_half(cudaStream_t st, bool timed) {
+  const FrameView& f = view;
+  int k = 0;
+  k += launch_edge_emit(f, seg_offsets, st);
+  cudaMemsetAsync(f.cmdrow_counts, 0, sizeof(uint32_t) * (f.num_cmdrows + 1), st);
+  cudaMemsetAsync(f.cmdrow_cursor, 0, sizeof(uint32_t) * (f.num_cmdrows + 1), st);
+  k += launch_seg_bin(f, 0, st);
+  k += exclusive_scan(f.cmdrow_counts, f.cmdrow_offsets, f.num_cmdrows, f.cmdrow_offsets + f.num_cmdrows + 1, st);
+  k += launch_seg_bin(f, 1, st);
+  k += launch_rows_and_tiles(f, row_canvas, st);
+  if (timed) cudaEventRecord(ev[1], st);
+  k += launch_fine(f, st);
+  if (timed) cudaEventRecord(ev[2], st);
+  return k;
+}
+
+BLGpuResult Runtime::download() {
+  for (size_t i = 0; i < targets.size(); i++) {
+    const BLGpuImage& im = targets[i].image;
+    if (device_target_direct(im) || im.width == 0 || im.height == 0) continue;
+    bool dev = (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) != 0;
+    BLGPU_CHECK(cudaMemcpy2DAsync(im.pixel_data, size_t(im.stride), canvas_dev[i], size_t(canvas_stride[i]) * 4u,
+                                  size_t(im.width) * 4u, size_t(im.height),
+                                  dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream));
+  }
+  return BLGPU_SUCCESS;
+}
+
+BLGpuResult Runtime::run(const Frame& fr) {
+  BLGPU_CHECK(cudaSetDevice(device));
+  for (const FrameTarget& t : fr.targets)
+    if (t.image.width < 0 || t.image.height < 0) return BLGPU_ERROR_INVALID_VALUE;
+  graph_valid = false;
+  has_frame = false;
+  pending_timing = 0;
+  BLGpuResult r = upload(fr);
+  if (r) return r;
+
+  BLGPU_CHECK(cudaEventRecord(ev[0], stream));
+  int launches = enqueue_count_half(stream);
+  BLGPU_CHECK(cudaGetLastError());
+  BLGPU_CHECK(cudaMemcpyAsync(host_totals, view.totals, 16, cudaMemcpyDeviceToHost, stream));
+  BLGPU_CHECK(cudaStreamSynchronize(stream));
+  totals.segs = host_totals[0];
+  totals.seglist = host_totals[1];
+  totals.cmdrows = host_totals[2];
+  totals.row_entries = host_totals[3];
+
+  // Dynamic buffers.
+  auto plan = [&](Layout& L) {
+    view.segs = L.take<DevSeg>(totals.segs);
+    view.seg_meta = L.take<uint32_t>(totals.segs);
+    view.cmdrow_counts = L.take<uint32_t>(totals.cmdrows + 1);
+    view.cmdrow_offsets = L.take<uint32_t>(totals.cmdrows + 1 + scan_temp_words(totals.cmdrows + 1));
+    view.cmdrow_cursor = L.take<uint32_t>(totals.cmdrows + 1);
+    view.seglist = L.take<uint32_t>(totals.seglist + 1);
+    view.row_cmds = L.take<uint32_t>(totals.row_entries + 1);
+  };
+  Layout measure;
+  plan(measure);
+  if (measure.off > dyn_buf.size) BLGPU_CHECK(dyn_buf.reserve(measure.off));
+  Layout L;
+  L.base = static_cast<char*>(dyn_buf.ptr);
+  plan(L);
+  view.num_segs = totals.segs;
+  view.num_cmdrows = totals.cmdrows;
+  view.num_seglist = totals.seglist;
+
+  launches += enqueue_render_half(stream, true);
+  BLGPU_CHECK(cudaGetLastError());
+  BLGPU_CHECK(cudaEventRecord(ev[3], stream));
+  r = download();
+  if (r) return r;
+  BLGPU_CHECK(cudaStreamSynchronize(stream));
+  has_frame = true;
+
+  float ms = 0.f, fine_ms = 0.f;
+  cudaEventElapsedTime(&ms, ev[0], ev[3]);
+  cudaEventElapsedTime(&fine_ms, ev[1], ev[2]);
+  stats.frames++;
+  stats.fill_commands = view.num_cmds;
+  stats.segments = totals.segs;
+  stats.tiles = view.num_tiles;
+  stats.kernel_launches = uint64_t(launches);
+  stats.last_gpu_ms = ms;
+  stats.last_fine_ms = fine_ms;
+  return BLGPU_SUCCESS;
+}
+
+// Re-runs the last frame's device pipeline on its device-resident inputs and canvases (the
+// canvases keep what the previous run left in them). Asynchronous with respect to the host.
+BLGpuResult Runtime::replay(bool use_graph) {
+  if (!has_frame) return BLGPU_ERROR_INVALID_STATE;
+  BLGPU_CHECK(cudaSetDevice(device));
+  if (!use_graph) {
+    BLGPU_CHECK(cudaEventRecord(ev[0], stream));
+    int launches = enqueue_count_half(stream);
+    launches += enqueue_render_half(stream, true);
+    BLGPU_CHECK(cudaGetLastError());
+    BLGPU_CHECK(cudaEventRecord(ev[3], stream));
+    stats.kernel_launches = uint64_t(launches);
+    pending_timing = 2;
+    return BLGPU_SUCCESS;
+  }
+  if (!graph_valid) {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    cudaGraph_t g = nullptr;
+    BLGPU_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    int launches = enqueue_count_half(stream);
+    launches += enqueue_render_half(stream, false);
+    cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (e != cudaSuccess) return cuda_result(e);
+    e = cudaGraphInstantiate(&graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { graph = nullptr; return cuda_result(e); }
+    graph_valid = true;
+    stats.kernel_launches = uint64_t(launches);
+  }
+  BLGPU_CHECK(cudaEventRecord(ev[0], stream));
+  BLGPU_CHECK(cudaGraphLaunch(graph, stream));
+  BLGPU_CHECK(cudaEventRecord(ev[3], stream));
+  pending_timing = 1;
+  return BLGPU_SUCCESS;
+}
+
+BLGpuResult Runtime::synchronize() {
+  BLGPU_CHECK(cudaSetDevice(device));
+  BLGPU_CHECK(cudaStreamSynchronize(stream));
+  if (pending_timing) {
+    float ms = 0.f, fine_ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[0], ev[3]);
+    stats.last_gpu_ms = ms;
+    if (pending_timing == 2) {
+      cudaEventElapsedTime(&fine_ms, ev[1], ev[2]);
+      stats.last_fine_ms = fine_ms;
+    }
+    stats.frames++;
+    pending_timing = 0;
+  }
+  return BLGPU_SUCCESS;
+}
+
+}  // namespace blgpu

@@ -1,0 +1,113 @@
+// runtime.h - device runtime: frame staging, device memory, pipeline execution, replay.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "blgpu.h"
+#include "blgpu_internal.h"
+
+namespace blgpu {
+
+// A pattern source registered in a frame (host or device memory).
+struct FrameImage {
+  const void* pixels;
+  intptr_t stride;          // bytes
+  int32_t w, h;
+  bool device;
+  uint64_t pool_offset;     // first pixel in the frame's image pool
+};
+
+// A canvas's render target.
+struct FrameTarget {
+  BLGpuImage image;
+  bool upload;              // the pipeline reads the canvas's current content
+};
+
+// Everything one device pipeline run consumes, recorded on the host in painter's order.
+struct Frame {
+  std::vector<DevCmd> cmds;
+  std::vector<DevStyle> styles;
+  std::vector<DevXform> xforms;
+  std::vector<DevCanvas> canvases;
+  std::vector<FrameTarget> targets;
+  std::vector<double> verts;
+  std::vector<uint8_t> path_cmds;
+  std::vector<DevLutJob> lut_jobs;
+  std::vector<DevStop> stops;
+  std::vector<FrameImage> images;
+  uint64_t image_words = 0;
+  uint32_t lut_words = 0;
+  uint32_t tiles = 0, rows = 0;
+  uint64_t generation = 1;  // bumped by clear(); per-frame registrations compare against it (0 = none)
+
+  void clear();
+  // Adds a canvas (tile/row bases, band height) for `image`; returns its index.
+  uint32_t add_canvas(const BLGpuImage& image, bool upload);
+  // Registers a pattern image (deduplicated by pixel pointer); returns the pool offset.
+  uint64_t add_image(const BLGpuImage& image);
+};
+
+// Sizes produced by the counting half of the pipeline, cached for replay.
+struct FrameTotals {
+  uint32_t segs = 0, seglist = 0, cmdrows = 0, row_entries = 0;
+};
+
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t size = 0;
+  cudaError_t reserve(size_t bytes);
+  void release();
+};
+
+struct Runtime {
+  int device = 0;
+  uint32_t lut_variant = kLutSSE2;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int sm_count = 0;
+
+  DeviceBuffer in_buf;      // uploaded frame data + canvases + fixed-size work arrays
+  DeviceBuffer dyn_buf;     // sizes known after the counting pass (segments, lists)
+  void* host_staging = nullptr;
+  size_t host_staging_size = 0;
+  uint32_t* host_totals = nullptr;   // pinned
+
+  cudaEvent_t ev[4] = {};
+  cudaGraphExec_t graph = nullptr;
+  bool graph_valid = false;
+
+  // last executed frame (kept for replay)
+  FrameView view{};
+  FrameTotals totals;
+  std::vector<FrameTarget> targets;
+  std::vector<uint32_t*> canvas_dev;   // device pixels per canvas
+  std::vector<int32_t> canvas_stride;  // device stride in pixels
+  uint32_t* seg_offsets = nullptr;
+  uint32_t* cmdrow_per_cmd = nullptr;
+  uint32_t* row_canvas = nullptr;
+  uint32_t* scan_tmp = nullptr;
+  bool has_frame = false;
+  int pending_timing = 0;   // 1: graph replay timed, 2: eager replay timed (incl. fine kernel)
+
+  BLGpuStats stats{};
+
+  BLGpuResult init(const BLGpuRuntimeCreateInfo* info);
+  void destroy();
+  // Uploads `fr`, runs the pipeline, downloads the canvases that live in host memory. Blocking.
+  BLGpuResult run(const Frame& fr);
+  BLGpuResult replay(bool use_graph);
+  BLGpuResult synchronize();
+
+ private:
+  int enqueue_count_half(cudaStream_t st);
+  int enqueue_render_half(cudaStream_t st, bool timed);
+  BLGpuResult upload(const Frame& fr);
+  BLGpuResult download();
+};
+
+BLGpuResult cuda_result(cudaError_t e);
+
+}  // namespace blgpu

@@ -1,0 +1,152 @@
+/*
+ * blgpu.h - C ABI of the GB300 raster backend (libblgpu.so).
+ *
+ * The entry points mirror the reference's C rendering-context API (blend2d/core/context.h:631-803,
+ * bl_context_*): same call names modulo the prefix, same argument meaning, same enum values, same
+ * BLResult error codes. A BLGpuContext records fill calls into a frame; flush(SYNC)/end() runs
+ * the frame on the GPU and writes the pixels back into the caller's PRGB32 image. Pixels are
+ * bit-exact to the reference's synchronous fixed pipeline.
+ *
+ * Plain pointers and sizes only; no CUDA or C++ types appear in the signatures.
+ */
+#ifndef BLGPU_H_INCLUDED
+#define BLGPU_H_INCLUDED
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef uint32_t BLGpuResult;
+
+/* BLResult values used by this backend (blend2d/core/api.h, BLResultCode). */
+enum {
+  BLGPU_SUCCESS = 0,
+  BLGPU_ERROR_OUT_OF_MEMORY = 0x00010000u,   /* BL_ERROR_OUT_OF_MEMORY */
+  BLGPU_ERROR_INVALID_VALUE = 0x00010001u,   /* BL_ERROR_INVALID_VALUE */
+  BLGPU_ERROR_INVALID_STATE = 0x00010002u,   /* BL_ERROR_INVALID_STATE */
+  BLGPU_ERROR_NOT_IMPLEMENTED = 0x00010007u, /* BL_ERROR_NOT_IMPLEMENTED */
+  BLGPU_ERROR_NO_STATES_TO_RESTORE = 0x00010038u, /* BL_ERROR_NO_STATES_TO_RESTORE */
+  BLGPU_ERROR_DEVICE = 0x00011000u           /* CUDA failure (no reference counterpart) */
+};
+
+/* Image formats (BLFormat) and image-placement flags. */
+enum {
+  BLGPU_FORMAT_PRGB32 = 1,                   /* BL_FORMAT_PRGB32 */
+  BLGPU_IMAGE_DEVICE_MEMORY = 0x1u           /* pixel_data is a CUDA device pointer */
+};
+
+/* bl_context_flush flags (BLContextFlushFlags). */
+enum { BLGPU_FLUSH_SYNC = 0x80000000u };     /* BL_CONTEXT_FLUSH_SYNC */
+
+/* Gradient LUT builder the backend reproduces (blend2d/pixelops/funcs.cpp:22-34). */
+enum {
+  BLGPU_LUT_SSE2 = 0,    /* reference no-JIT x86-64 build (default) */
+  BLGPU_LUT_AVX2 = 1,    /* reference JIT build on AVX2 machines */
+  BLGPU_LUT_SCALAR = 2   /* reference no-JIT build on non-x86 hosts */
+};
+
+typedef struct BLGpuRuntime BLGpuRuntime;
+typedef struct BLGpuContext BLGpuContext;
+
+typedef struct BLGpuRuntimeCreateInfo {
+  int32_t device;          /* CUDA device ordinal */
+  uint32_t lut_variant;    /* BLGPU_LUT_* */
+  void* cuda_stream;       /* cudaStream_t to run on (NULL = a private stream) */
+  uint32_t reserved[4];
+} BLGpuRuntimeCreateInfo;
+
+typedef struct BLGpuImage {
+  void* pixel_data;        /* PRGB32 pixels (host memory unless BLGPU_IMAGE_DEVICE_MEMORY) */
+  intptr_t stride;         /* bytes per row */
+  int32_t width, height;
+  uint32_t format;         /* BLGPU_FORMAT_PRGB32 */
+  uint32_t flags;          /* BLGPU_IMAGE_* */
+} BLGpuImage;
+
+typedef struct BLGpuGradientStop {
+  double offset;
+  uint64_t rgba64;         /* BLRgba64: a<<48 | r<<32 | g<<16 | b */
+} BLGpuGradientStop;
+
+typedef struct BLGpuGradient {   /* BLGradientCore contents (blend2d/core/gradient.h) */
+  uint32_t type;           /* BL_GRADIENT_TYPE_LINEAR / RADIAL / CONIC */
+  uint32_t extend_mode;    /* BL_EXTEND_MODE_PAD / REPEAT / REFLECT */
+  double values[6];        /* BLLinear/Radial/ConicGradientValues */
+  const BLGpuGradientStop* stops;
+  size_t stop_count;
+  const double* transform; /* BLMatrix2D m00 m01 m10 m11 m20 m21, or NULL */
+} BLGpuGradient;
+
+typedef struct BLGpuPattern {    /* BLPatternCore contents (blend2d/core/pattern.h) */
+  const BLGpuImage* image; /* PRGB32 source (host memory) */
+  int32_t area[4];         /* x, y, w, h; w == 0 selects the whole image */
+  uint32_t extend_mode;    /* simple BL_EXTEND_MODE_* */
+  const double* transform; /* BLMatrix2D, or NULL */
+} BLGpuPattern;
+
+typedef struct BLGpuStats {
+  uint64_t frames;
+  uint64_t fill_commands;  /* commands of the last frame */
+  uint64_t segments;       /* 24.8 segments the last frame's edge builder produced */
+  uint64_t tiles;          /* tiles of the last frame */
+  uint64_t kernel_launches;/* kernels launched by the last frame's device pipeline */
+  double last_gpu_ms;      /* device time of the last frame's pipeline (CUDA events) */
+  double last_fine_ms;     /* device time of its fine (composite) kernel */
+} BLGpuStats;
+
+/* --- runtime (device, stream, memory) --------------------------------------------------- */
+BLGpuResult blgpu_runtime_create(BLGpuRuntime** out, const BLGpuRuntimeCreateInfo* info);
+BLGpuResult blgpu_runtime_destroy(BLGpuRuntime* rt);
+BLGpuResult blgpu_runtime_get_stats(const BLGpuRuntime* rt, BLGpuStats* out);
+/* Re-runs the device pipeline of the last flushed frame on its device-resident inputs (no
+ * host<->device traffic); `use_graph` replays it as a captured CUDA graph. */
+BLGpuResult blgpu_runtime_replay(BLGpuRuntime* rt, int use_graph);
+BLGpuResult blgpu_runtime_synchronize(BLGpuRuntime* rt);
+
+/* --- rendering context: bl_context_* ---------------------------------------------------- */
+/* bl_context_init + bl_context_begin (context.cpp:316-328): bind `image` as the target. */
+BLGpuResult blgpu_context_create(BLGpuContext** out, BLGpuRuntime* rt);
+BLGpuResult blgpu_context_destroy(BLGpuContext* ctx);
+BLGpuResult blgpu_context_begin(BLGpuContext* ctx, const BLGpuImage* image);
+BLGpuResult blgpu_context_end(BLGpuContext* ctx);                         /* bl_context_end */
+BLGpuResult blgpu_context_flush(BLGpuContext* ctx, uint32_t flags);       /* bl_context_flush */
+BLGpuResult blgpu_context_save(BLGpuContext* ctx);                        /* bl_context_save */
+BLGpuResult blgpu_context_restore(BLGpuContext* ctx);                     /* bl_context_restore */
+
+BLGpuResult blgpu_context_set_comp_op(BLGpuContext* ctx, uint32_t comp_op);       /* bl_context_set_comp_op */
+BLGpuResult blgpu_context_set_fill_rule(BLGpuContext* ctx, uint32_t fill_rule);   /* bl_context_set_fill_rule */
+BLGpuResult blgpu_context_set_global_alpha(BLGpuContext* ctx, double alpha);      /* bl_context_set_global_alpha */
+BLGpuResult blgpu_context_set_fill_alpha(BLGpuContext* ctx, double alpha);        /* bl_context_set_fill_alpha */
+BLGpuResult blgpu_context_set_hint(BLGpuContext* ctx, uint32_t hint, uint32_t value); /* bl_context_set_hint */
+BLGpuResult blgpu_context_set_transform(BLGpuContext* ctx, const double m[6]);    /* apply_transform_op(ASSIGN) */
+BLGpuResult blgpu_context_reset_transform(BLGpuContext* ctx);                     /* apply_transform_op(RESET) */
+
+BLGpuResult blgpu_context_set_fill_style_rgba32(BLGpuContext* ctx, uint32_t argb32);           /* bl_context_set_fill_style_rgba32 */
+BLGpuResult blgpu_context_set_fill_style_gradient(BLGpuContext* ctx, const BLGpuGradient* g);  /* bl_context_set_fill_style(BLGradient) */
+BLGpuResult blgpu_context_set_fill_style_pattern(BLGpuContext* ctx, const BLGpuPattern* p);    /* bl_context_set_fill_style(BLPattern) */
+
+BLGpuResult blgpu_context_clear_all(BLGpuContext* ctx);                                       /* bl_context_clear_all */
+BLGpuResult blgpu_context_fill_all(BLGpuContext* ctx);                                        /* bl_context_fill_all */
+BLGpuResult blgpu_context_fill_rect_i(BLGpuContext* ctx, int32_t x, int32_t y, int32_t w, int32_t h); /* bl_context_fill_rect_i */
+BLGpuResult blgpu_context_fill_rect_d(BLGpuContext* ctx, double x, double y, double w, double h);     /* bl_context_fill_rect_d */
+BLGpuResult blgpu_context_fill_box_d(BLGpuContext* ctx, double x0, double y0, double x1, double y1);  /* fill_geometry(BOXD) */
+BLGpuResult blgpu_context_fill_polygon_d(BLGpuContext* ctx, const double* xy, size_t n);              /* fill_geometry(POLYGOND) */
+BLGpuResult blgpu_context_fill_path_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n); /* bl_context_fill_path_d */
+
+/* Replays a serialized command stream (include/blgpu_stream.h) into the context; the stream's
+ * canvas size must match the bound image. */
+BLGpuResult blgpu_context_submit_stream(BLGpuContext* ctx, const void* stream, size_t size);
+
+/* Batched rendering: renders `count` independent command streams (each with its own canvas)
+ * into `images` in one device pipeline (one persistent launch over every canvas's tiles). */
+BLGpuResult blgpu_render_batch(BLGpuRuntime* rt, const void* const* streams, const size_t* sizes,
+                               const BLGpuImage* images, uint32_t count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BLGPU_H_INCLUDED */

@@ -1,0 +1,253 @@
+"""GPU parity: every render goes through the C ABI (libblgpu.so) on cuda:0 and must be bit-exact
+to the reference - directly against the golden hashes of the reference's own renders, and against
+the oracle (pinned to those hashes) on seeded random scenes."""
+import math
+
+import numpy as np
+import pytest
+
+import blend2d_gb300 as bg
+from blend2d_gb300 import scenes
+import oracle_lib
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = oracle_lib.golden()
+LUTS = {"default": bg.LUT_SSE2, "sse2": bg.LUT_SSE2, "avx2": bg.LUT_AVX2, "scalar": bg.LUT_SCALAR}
+
+
+@pytest.fixture(scope="module")
+def runtimes():
+    rts = {}
+    yield lambda variant="default": rts.setdefault(variant, bg.Runtime(0, LUTS[variant]))
+    for rt in rts.values():
+        rt.close()
+
+
+def _diff(got, want):
+    bad = np.argwhere(got != want)
+    if not len(bad):
+        return ""
+    y, x = bad[0]
+    return f"{len(bad)} pixels differ, first at ({x},{y}): got {got[y, x]:08x} want {want[y, x]:08x}"
+
+
+GOLDEN_CASES = [(e["name"], v) for e in GOLDEN["scenes"] for v in e["pixels_sha256"]]
+
+
+@pytest.mark.parametrize("name,variant", GOLDEN_CASES, ids=[f"{n}-{v}" for n, v in GOLDEN_CASES])
+def test_golden_scene(runtimes, name, variant):
+    entry = next(e for e in GOLDEN["scenes"] if e["name"] == name)
+    stream = oracle_lib.golden_stream(entry)
+    got = bg.render_stream(runtimes(variant), stream)
+    if oracle_lib.sha256(got) != entry["pixels_sha256"][variant]:
+        detail = ""
+        if got.size <= 2_000_000:
+            detail = _diff(got, oracle_lib.render(stream, variant))
+        pytest.fail(f"{name}/{variant}: pixels differ from the reference render. {detail}")
+
+
+RANDOM_CASES = [(seed, w, h, variant)
+                for seed, (w, h), variant in zip(range(1000, 1036),
+                                                 [(257, 257), (64, 48), (33, 97), (400, 150), (1, 1), (3, 700),
+                                                  (129, 129), (640, 31)] * 5,
+                                                 ["default", "avx2", "scalar"] * 12)]
+
+
+@pytest.mark.parametrize("seed,w,h,variant", RANDOM_CASES)
+def test_random_mix_vs_oracle(runtimes, seed, w, h, variant):
+    stream = scenes.random_mix(seed, width=w, height=h, count=150).to_bytes()
+    got = bg.render_stream(runtimes(variant), stream)
+    want = oracle_lib.render(stream, variant)
+    assert not _diff(got, want), _diff(got, want)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_edge_cases_vs_oracle(runtimes, seed):
+    stream = scenes.edge_cases(seed=seed, width=131 + 17 * seed, height=97 + 5 * seed).to_bytes()
+    got = bg.render_stream(runtimes(), stream)
+    want = oracle_lib.render(stream)
+    assert not _diff(got, want), _diff(got, want)
+
+
+def test_batch_equals_oracle(runtimes):
+    rng = np.random.default_rng(77)
+    streams, targets = [], []
+    for i in range(24):
+        w, h = int(rng.integers(1, 300)), int(rng.integers(1, 300))
+        streams.append(scenes.random_mix(5000 + i, width=w, height=h, count=int(rng.integers(0, 120))).to_bytes())
+        targets.append(np.zeros((h, w), dtype=np.uint32))
+    rt = runtimes()
+    rt.render_batch(streams, targets)
+    for i, (s, t) in enumerate(zip(streams, targets)):
+        want = oracle_lib.render(s)
+        assert not _diff(t, want), f"canvas {i}: {_diff(t, want)}"
+
+
+def test_batch_canvases_workload_matches_individual(runtimes):
+    """Batched rendering of the many-canvas workload (reduced scale) equals per-canvas rendering."""
+    sws = scenes.batch_canvases(seed=4, count=40, max_side=512, max_paths=300)
+    streams = [sw.to_bytes() for sw in sws]
+    rt = runtimes()
+    batched = [np.zeros((sw.height, sw.width), dtype=np.uint32) for sw in sws]
+    rt.render_batch(streams, batched)
+    for i, s in enumerate(streams):
+        single = bg.render_stream(rt, s)
+        assert np.array_equal(single, batched[i]), f"canvas {i}"
+        if i % 8 == 0:
+            assert np.array_equal(single, oracle_lib.render(s)), f"canvas {i} vs oracle"
+
+
+def test_context_calls_match_stream(runtimes):
+    """The same scene through individual bl_context_* calls and through a submitted stream."""
+    rng = np.random.default_rng(5)
+    w, h = 200, 150
+    sw = scenes.StreamWriter(w, h)
+    img = scenes.premultiplied_noise(rng, 17, 9)
+    sw.add_image(img)
+    out = np.zeros((h, w), dtype=np.uint32)
+    rt = runtimes()
+    ctx = bg.Context(rt, out)
+    ops = []
+
+    def both(name, *args):
+        getattr(sw, {"set_comp_op": "comp_op", "set_fill_rule": "fill_rule", "set_fill_alpha": "fill_alpha",
+                     "set_global_alpha": "global_alpha", "set_transform": "transform",
+                     "reset_transform": "reset_transform", "set_fill_style_rgba32": "solid",
+                     "fill_polygon_d": "fill_polygon", "fill_path_d": "fill_path"}.get(name, name))(*args)
+        getattr(ctx, name)(*args)
+        ops.append(name)
+
+    both("clear_all")
+    both("set_fill_style_rgba32", 0xFF336699)
+    both("fill_rect_i", 10, 10, 50, 40)
+    both("set_fill_alpha", 0.5)
+    both("set_fill_style_rgba32", 0x80FF8000)
+    both("fill_rect_d", 20.25, 15.5, 100.75, 60.125)
+    both("set_fill_rule", 1)
+    both("fill_polygon_d", np.array([[5.0, 5.0], [190.0, 20.0], [40.0, 140.0], [160.0, 130.0]]))
+    both("set_comp_op", 1)
+    both("set_transform", [math.cos(0.3), math.sin(0.3), -math.sin(0.3), math.cos(0.3), 40.0, -10.0])
+    both("fill_box_d", 30.0, 30.0, 120.0, 90.0)
+    both("reset_transform")
+    both("set_comp_op", 0)
+    both("set_fill_alpha", 1.0)
+    stops = [(0.0, 0xFF0000FF), (0.5, 0x8000FF00), (1.0, 0xFFFF0000)]
+    sw.gradient(scenes.RADIAL, [100, 75, 80, 60, 90, 10], scenes.REFLECT, stops)
+    ctx.set_fill_style_gradient(bg.GRADIENT_RADIAL, [100, 75, 80, 60, 90, 10],
+                                [(o, scenes.rgba64_from_rgba32(c)) for o, c in stops], bg.EXTEND_REFLECT)
+    both("fill_path_d", [0, 4, 4, 4, 5], np.array([[10.0, 140.0], [60.0, -40.0], [140.0, 200.0], [190.0, 10.0],
+                                                   [10.0, 140.0]]))
+    sw.hint(2, 0)
+    ctx.set_hint(2, 0)
+    sw.pattern(0, scenes.REPEAT, transform=[1.5, 0.2, -0.2, 1.5, 3.0, 7.0])
+    ctx.set_fill_style_pattern(img, extend_mode=bg.EXTEND_REPEAT, transform=[1.5, 0.2, -0.2, 1.5, 3.0, 7.0])
+    both("save")
+    both("set_global_alpha", 0.7)
+    both("fill_rect_d", 100.0, 20.0, 90.0, 120.0)
+    both("restore")
+    both("fill_rect_i", 0, 100, 60, 50)
+    ctx.end()
+    ctx.close()
+    want = bg.render_stream(rt, sw.to_bytes())
+    assert np.array_equal(out, want)
+    assert np.array_equal(out, oracle_lib.render(sw.to_bytes()))
+
+
+def test_rendering_onto_existing_content(runtimes):
+    """Without clear_all the pipeline composites onto the image's current pixels."""
+    rng = np.random.default_rng(9)
+    w, h = 173, 111
+    base_sw = scenes.StreamWriter(w, h)
+    base_sw.add_image(scenes.premultiplied_noise(rng, w, h))
+    base_sw.comp_op(1)
+    base_sw.pattern(0, scenes.PAD)
+    base_sw.fill_all()
+    base = oracle_lib.render(base_sw.to_bytes())
+    top = scenes.random_mix(31, width=w, height=h, count=80)
+    top.parts = top.parts[1:]             # drop its clear_all
+    # the same drawing appended to the base scene, as one stream, for the oracle
+    both = scenes.StreamWriter(w, h)
+    both.images = base_sw.images + top.images
+    both.parts = list(base_sw.parts)
+    both.comp_op(0)                        # back to the state a fresh context starts with
+    both.reset_transform()
+    both.hint(2, 1)
+    both.solid(0xFF000000)
+    shifted = []
+    for rec in top.parts:
+        shifted.append(_shift_pattern_index(rec, len(base_sw.images)))
+    both.parts += shifted
+    want = oracle_lib.render(both.to_bytes())
+    img = base.copy()
+    bg.render_stream(runtimes(), top.to_bytes(), img)
+    assert not _diff(img, want), _diff(img, want)
+
+
+def _shift_pattern_index(rec: bytes, by: int) -> bytes:
+    import struct
+    op = struct.unpack_from("<I", rec, 0)[0]
+    if op != 10:   # OP_STYLE_PATTERN
+        return rec
+    idx = struct.unpack_from("<I", rec, 8)[0]
+    return rec[:8] + struct.pack("<I", idx + by) + rec[12:]
+
+
+def test_device_targets(runtimes):
+    torch = pytest.importorskip("torch")
+    rt = runtimes()
+    for (w, h) in [(256, 100), (131, 77)]:     # aligned rows (direct) and unaligned rows (staged)
+        stream = scenes.random_mix(77 + w, width=w, height=h, count=100).to_bytes()
+        want = oracle_lib.render(stream)
+        dev = torch.zeros((h, w), dtype=torch.int32, device="cuda")
+        bg.render_stream(rt, stream, dev)
+        torch.cuda.synchronize()
+        got = dev.cpu().numpy().view(np.uint32)
+        assert not _diff(got, want), _diff(got, want)
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_replay(runtimes, use_graph):
+    torch = pytest.importorskip("torch")
+    rt = runtimes()
+    w, h = 300, 200
+    stream = scenes.random_mix(4242, width=w, height=h, count=200).to_bytes()   # starts with clear_all
+    want = oracle_lib.render(stream)
+    dev = torch.zeros((h, w), dtype=torch.int32, device="cuda")
+    bg.render_stream(rt, stream, dev)
+    for _ in range(3):
+        dev.fill_(0x12345678)
+        torch.cuda.synchronize()
+        rt.replay(use_graph)
+        rt.synchronize()
+        got = dev.cpu().numpy().view(np.uint32)
+        assert not _diff(got, want), _diff(got, want)
+    st = rt.stats()
+    assert st.last_gpu_ms > 0 and st.kernel_launches > 0
+
+
+def test_stats_and_errors(runtimes):
+    rt = runtimes()
+    img = np.zeros((10, 10), dtype=np.uint32)
+    ctx = bg.Context(rt, img)
+    for call, args, code in [("set_comp_op", (29,), bg.ERROR_INVALID_VALUE),
+                             ("set_comp_op", (2,), bg.ERROR_NOT_IMPLEMENTED),
+                             ("set_fill_rule", (2,), bg.ERROR_INVALID_VALUE),
+                             ("set_global_alpha", (float("nan"),), bg.ERROR_INVALID_VALUE),
+                             ("set_fill_alpha", (float("nan"),), bg.ERROR_INVALID_VALUE),
+                             ("set_hint", (3, 0), bg.ERROR_INVALID_VALUE),
+                             ("set_hint", (2, 2), bg.ERROR_INVALID_VALUE),
+                             ("restore", (), bg.ERROR_NO_STATES_TO_RESTORE)]:
+        with pytest.raises(bg.BLGpuError) as ei:
+            getattr(ctx, call)(*args)
+        assert ei.value.code == code, (call, args)
+    ctx.set_fill_style_rgba32(0xFFFFFFFF)
+    ctx.fill_rect_i(2, 2, 3, 3)
+    ctx.end()
+    assert img[3, 3] == 0xFFFFFFFF and img[0, 0] == 0
+    with pytest.raises(bg.BLGpuError) as ei:
+        ctx.fill_all()
+    assert ei.value.code == bg.ERROR_INVALID_STATE
+    ctx.close()
+    st = rt.stats()
+    assert st.frames >= 1 and st.fill_commands == 1
