@@ -72,7 +72,8 @@ class Pattern(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("frames", ctypes.c_uint64), ("fill_commands", ctypes.c_uint64), ("segments", ctypes.c_uint64),
                 ("tiles", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("last_gpu_ms", ctypes.c_double),
-                ("last_fine_ms", ctypes.c_double)]
+                ("last_fine_ms", ctypes.c_double), ("pixel_ops", ctypes.c_uint64), ("pattern_ops", ctypes.c_uint64),
+                ("input_vertices", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
 
 
 _P = ctypes.c_void_p

@@ -169,6 +169,7 @@ struct FrameView {
   uint32_t* work_counter;
   uint32_t* totals;            // [4] segments, seglist bound, (cmd,row) slots, row entries
   uint32_t* error_flags;
+  unsigned long long* pixel_ops;   // [2] composited pixels (mask != 0), of which pattern-fetched
   uint32_t num_cmds;
   uint32_t num_canvases;
   uint32_t num_tiles;

@@ -374,6 +374,8 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
   const int prow = tid >> 3;            // pixel row within the tile
   const int pcol = (tid & 7) * 4;       // first of 4 pixel columns
 
+  uint32_t ops = 0, pat_ops = 0;   // composited pixels of this thread (all tiles)
+
   for (;;) {
     if (tid == 0) sh.tile = atomicAdd(f.work_counter, 1u);
     __syncthreads();
@@ -479,13 +481,17 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
 
         if (row_ok && (m[0] | m[1] | m[2] | m[3])) {
           px::RowState rs = px::row_state(st, y, fetch_y0);
+          uint32_t n = 0;
 #pragma unroll
           for (int k = 0; k < 4; k++) {
             if (m[k] && xp + k < cv.w) {
               uint32_t s = px::fetch(st, rs, xp + k, f.luts, f.images);
               pix[k] = px::composite(pix[k], s, m[k], src_copy);
+              n++;
             }
           }
+          ops += n;
+          pat_ops += st.fetch >= kFetchPatAlignedPad ? n : 0u;
         }
       }
       __syncthreads();
@@ -498,6 +504,13 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
 #pragma unroll
       for (int k = 0; k < 4; k++) if (row_ok && xp + k < cv.w) dst[k] = pix[k];
     }
+  }
+
+  ops = __reduce_add_sync(0xFFFFFFFFu, ops);
+  pat_ops = __reduce_add_sync(0xFFFFFFFFu, pat_ops);
+  if (lane == 0 && ops) {
+    atomicAdd(&f.pixel_ops[0], (unsigned long long)ops);
+    if (pat_ops) atomicAdd(&f.pixel_ops[1], (unsigned long long)pat_ops);
   }
 }
 

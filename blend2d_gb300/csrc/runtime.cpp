@@ -201,9 +201,10 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     row_canvas = L.take<uint32_t>(fr.rows + 1);
     v.tile_order = L.take<uint32_t>(fr.tiles + 1);
     v.tile_canvas = L.take<uint32_t>(fr.tiles + 1);
-    v.work_counter = L.take<uint32_t>(16);   // [0] work counter, [4..8) totals, [8..12) error flags
+    v.work_counter = L.take<uint32_t>(16);   // [0] work counter, [4..8) totals, [8..12) error flags, [12..16) pixel ops
     v.totals = v.work_counter + 4;
     v.error_flags = v.work_counter + 8;
+    v.pixel_ops = reinterpret_cast<unsigned long long*>(v.work_counter + 12);
     scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, fr.rows + 1)));
     return staged_end;
   };
@@ -263,6 +264,8 @@ BLGpuResult Runtime::upload(const Frame& fr) {
       memcpy(dst + size_t(y) * size_t(im.w) * 4u, static_cast<const char*>(im.pixels) + intptr_t(y) * im.stride,
              size_t(im.w) * 4u);
   }
+  h2d_bytes = staged_bytes;
+  d2h_bytes = 0;
   if (staged_bytes) BLGPU_CHECK(cudaMemcpyAsync(in_buf.ptr, host_staging, staged_bytes, cudaMemcpyHostToDevice, stream));
   for (const FrameImage& im : fr.images) {
     if (!im.device) continue;
@@ -275,6 +278,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     const BLGpuImage& im = t.image;
     if (!t.upload || device_target_direct(im) || im.width == 0 || im.height == 0) continue;
     bool dev = (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) != 0;
+    if (!dev) h2d_bytes += uint64_t(uint32_t(im.width)) * uint32_t(im.height) * 4u;
     BLGPU_CHECK(cudaMemcpy2DAsync(canvas_dev[i], size_t(canvas_stride[i]) * 4u, im.pixel_data, size_t(im.stride),
                                   size_t(im.width) * 4u, size_t(im.height),
                                   dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
@@ -332,6 +336,7 @@ BLGpuResult Runtime::download() {
     const BLGpuImage& im = targets[i].image;
     if (device_target_direct(im) || im.width == 0 || im.height == 0) continue;
     bool dev = (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) != 0;
+    if (!dev) d2h_bytes += uint64_t(uint32_t(im.width)) * uint32_t(im.height) * 4u;
     BLGPU_CHECK(cudaMemcpy2DAsync(im.pixel_data, size_t(im.stride), canvas_dev[i], size_t(canvas_stride[i]) * 4u,
                                   size_t(im.width) * 4u, size_t(im.height),
                                   dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream));
@@ -353,6 +358,7 @@ BLGpuResult Runtime::run(const Frame& fr) {
   int launches = enqueue_count_half(stream);
   BLGPU_CHECK(cudaGetLastError());
   BLGPU_CHECK(cudaMemcpyAsync(host_totals, view.totals, 16, cudaMemcpyDeviceToHost, stream));
+  d2h_bytes += 16;
   BLGPU_CHECK(cudaStreamSynchronize(stream));
   totals.segs = host_totals[0];
   totals.seglist = host_totals[1];
@@ -382,10 +388,15 @@ BLGpuResult Runtime::run(const Frame& fr) {
   launches += enqueue_render_half(stream, true);
   BLGPU_CHECK(cudaGetLastError());
   BLGPU_CHECK(cudaEventRecord(ev[3], stream));
+  BLGPU_CHECK(cudaMemcpyAsync(host_totals + 8, view.pixel_ops, 16, cudaMemcpyDeviceToHost, stream));
   r = download();
   if (r) return r;
   BLGPU_CHECK(cudaStreamSynchronize(stream));
   has_frame = true;
+  read_pixel_ops();
+  stats.input_vertices = uint64_t(fr.verts.size() / 2);
+  stats.h2d_bytes = h2d_bytes;
+  stats.d2h_bytes = d2h_bytes + 16;
 
   float ms = 0.f, fine_ms = 0.f;
   cudaEventElapsedTime(&ms, ev[0], ev[3]);
@@ -437,10 +448,19 @@ BLGpuResult Runtime::replay(bool use_graph) {
   return BLGPU_SUCCESS;
 }
 
+void Runtime::read_pixel_ops() {
+  uint64_t v[2];
+  memcpy(v, host_totals + 8, sizeof(v));
+  stats.pixel_ops = v[0];
+  stats.pattern_ops = v[1];
+}
+
 BLGpuResult Runtime::synchronize() {
   BLGPU_CHECK(cudaSetDevice(device));
   BLGPU_CHECK(cudaStreamSynchronize(stream));
   if (pending_timing) {
+    BLGPU_CHECK(cudaMemcpy(host_totals + 8, view.pixel_ops, 16, cudaMemcpyDeviceToHost));
+    read_pixel_ops();
     float ms = 0.f, fine_ms = 0.f;
     cudaEventElapsedTime(&ms, ev[0], ev[3]);
     stats.last_gpu_ms = ms;

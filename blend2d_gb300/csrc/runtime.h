@@ -91,6 +91,7 @@ struct Runtime {
   uint32_t* scan_tmp = nullptr;
   bool has_frame = false;
   int pending_timing = 0;   // 1: graph replay timed, 2: eager replay timed (incl. fine kernel)
+  uint64_t h2d_bytes = 0, d2h_bytes = 0;
 
   BLGpuStats stats{};
 
@@ -106,6 +107,7 @@ struct Runtime {
   int enqueue_render_half(cudaStream_t st, bool timed);
   BLGpuResult upload(const Frame& fr);
   BLGpuResult download();
+  void read_pixel_ops();
 };
 
 BLGpuResult cuda_result(cudaError_t e);

@@ -177,8 +177,56 @@ class StreamWriter:
 # Random helpers
 # ------------------------------------------------------------------------------------------------
 
+# Transcendental functions evaluated with IEEE +, -, *, / only (no libm, no SIMD math kernels),
+# so a seed serializes to the same stream bytes on every platform (x86-64 and aarch64 libm and
+# numpy's vectorized exp/log/sin/cos differ in the last bits). Accuracy is ~1e-15 relative, which
+# is all a scene generator needs; determinism is what matters.
+_LN2_HI = 6.93147180369123816490e-01
+_LN2_LO = 1.90821492927058770002e-10
+_TWO_PI = 6.283185307179586
+
+
+def _exp(x):
+    x = np.asarray(x, dtype=np.float64)
+    k = np.floor(x / 0.6931471805599453 + 0.5)
+    r = (x - k * _LN2_HI) - k * _LN2_LO
+    term = np.ones_like(r)
+    acc = np.ones_like(r)
+    for i in range(1, 18):
+        term = term * r / float(i)
+        acc = acc + term
+    return np.ldexp(acc, k.astype(np.int64))
+
+
+def _log(x):
+    x = np.asarray(x, dtype=np.float64)
+    m, e = np.frexp(x)                      # x = m * 2^e, m in [0.5, 1)
+    small = m < 0.7071067811865476
+    m = np.where(small, m * 2.0, m)
+    e = np.where(small, e - 1, e).astype(np.float64)
+    z = (m - 1.0) / (m + 1.0)               # log(m) = 2 atanh(z), |z| < 0.172
+    z2 = z * z
+    acc = np.zeros_like(z)
+    for k in range(25, 0, -2):
+        acc = acc * z2 + 1.0 / float(k)
+    return 2.0 * z * acc + e * _LN2_HI + e * _LN2_LO
+
+
+def _sincos(x: float) -> tuple[float, float]:
+    k = math.floor(x / _TWO_PI + 0.5)
+    r = x - k * _TWO_PI                     # |r| <= pi (up to rounding)
+    r2 = r * r
+    s = 1.0                                 # sin r = r (1 - r^2/(2*3) (1 - r^2/(4*5) (1 - ...)))
+    for k in range(15, 0, -1):
+        s = 1.0 - s * r2 / float((2 * k) * (2 * k + 1))
+    c = 1.0                                 # cos r = 1 - r^2/(1*2) (1 - r^2/(3*4) (1 - ...))
+    for k in range(15, 0, -1):
+        c = 1.0 - c * r2 / float((2 * k - 1) * (2 * k))
+    return r * s, c
+
+
 def _log_uniform(rng, lo, hi, size=None):
-    return np.exp(rng.uniform(math.log(lo), math.log(hi), size))
+    return _exp(rng.uniform(float(_log(lo)), float(_log(hi)), size))
 
 
 def _random_stops(rng, n):
@@ -290,7 +338,8 @@ def patterns(seed: int = 3, width: int = 4096, height: int = 4096, count: int = 
         tx, ty = rng.uniform(0, width), rng.uniform(0, height)
         ang = rng.uniform(0, 2 * math.pi)
         s = float(_log_uniform(rng, 0.25, 4.0))
-        c, sn = math.cos(ang) * s, math.sin(ang) * s
+        sn, c = _sincos(ang)
+        c, sn = c * s, sn * s
         # T = translate(tx, ty) * rotate(ang) * scale(s) * translate(-half, -half), row-vector form.
         m = [c, sn, -sn, c, tx - (c * half - sn * half), ty - (sn * half + c * half)]
         quad = np.stack([corners[:, 0] * m[0] + corners[:, 1] * m[2] + m[4],
@@ -363,7 +412,8 @@ def random_mix(seed: int, width: int = 257, height: int = 257, count: int = 200,
             a = rng.uniform(-0.5, 0.5)
             s = rng.uniform(0.7, 1.3)
             cx, cy = width * 0.5, height * 0.5
-            c, sn = math.cos(a) * s, math.sin(a) * s
+            sn, c = _sincos(a)
+            c, sn = c * s, sn * s
             sw.transform([c, sn, -sn, c, cx - (c * cx - sn * cy), cy - (sn * cx + c * cy)])
         elif transforms:
             sw.reset_transform()
@@ -372,7 +422,7 @@ def random_mix(seed: int, width: int = 257, height: int = 257, count: int = 200,
         if style == "solid":
             sw.solid(int(rng.integers(0, 2**32, dtype=np.uint64)))
         elif style in ("linear", "radial", "conic"):
-            side = float(rng.uniform(20, max(width, height)))
+            side = float(rng.uniform(20, max(20, width, height)))
             x0, y0 = float(rng.uniform(lo_x, max(lo_x, hi_x - side))), float(rng.uniform(lo_y, max(lo_y, hi_y - side)))
             _gradient_style(rng, sw, x0, y0, side, kind={"linear": LINEAR, "radial": RADIAL, "conic": CONIC}[style])
         else:
@@ -380,14 +430,15 @@ def random_mix(seed: int, width: int = 257, height: int = 257, count: int = 200,
             idx = int(rng.integers(0, len(sw.images)))
             ang = rng.uniform(0, 2 * math.pi) if rng.integers(0, 2) else 0.0
             s = float(_log_uniform(rng, 0.3, 3.0))
-            c, sn = math.cos(ang) * s, math.sin(ang) * s
+            sn, c = _sincos(ang)
+            c, sn = c * s, sn * s
             tx, ty = rng.uniform(lo_x, hi_x), rng.uniform(lo_y, hi_y)
             sw.pattern(idx, int(rng.integers(0, 3)), transform=[c, sn, -sn, c, tx, ty])
 
         cmd = commands[int(rng.integers(0, len(commands)))]
         if cmd == "rect_i":
             x, y = rng.integers(-30, width + 30), rng.integers(-30, height + 30)
-            sw.fill_rect_i(x, y, rng.integers(1, width // 2), rng.integers(1, height // 2))
+            sw.fill_rect_i(x, y, rng.integers(1, max(2, width // 2)), rng.integers(1, max(2, height // 2)))
         elif cmd == "rect_d":
             x, y = rng.uniform(lo_x, hi_x), rng.uniform(lo_y, hi_y)
             sw.fill_rect_d(x, y, rng.uniform(0.5, width * 0.5), rng.uniform(0.5, height * 0.5))

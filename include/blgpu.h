@@ -95,6 +95,11 @@ typedef struct BLGpuStats {
   uint64_t kernel_launches;/* kernels launched by the last frame's device pipeline */
   double last_gpu_ms;      /* device time of the last frame's pipeline (CUDA events) */
   double last_fine_ms;     /* device time of its fine (composite) kernel */
+  uint64_t pixel_ops;      /* composited pixels of the last frame (mask != 0, summed over commands) */
+  uint64_t pattern_ops;    /* ... of which fetched from a pattern */
+  uint64_t input_vertices; /* vertices of the last frame's polygon/path fills */
+  uint64_t h2d_bytes;      /* host->device bytes of the last flush (frame data + canvas uploads) */
+  uint64_t d2h_bytes;      /* device->host bytes of the last flush (canvas downloads + sizes) */
 } BLGpuStats;
 
 /* --- runtime (device, stream, memory) --------------------------------------------------- */
