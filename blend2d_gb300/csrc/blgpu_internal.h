@@ -17,6 +17,7 @@
 #pragma once
 
 #include <stdint.h>
+#include <vector_types.h>
 
 namespace blgpu {
 
@@ -134,6 +135,17 @@ struct DevSeg {            // one non-horizontal 24.8 segment, y0 < y1
   int32_t x0, y0, x1, y1;
 };
 
+enum ItemKind : uint32_t { kItemLine = 0, kItemQuad = 1, kItemCubic = 2, kItemConic = 3 };
+
+// One curve or line of an analytic command whose vertices all lie inside the clip box (built
+// independently of the command's other curves). Vertex indices are relative to geom_first.
+struct DevItem {
+  uint32_t cmd;
+  uint32_t kind;           // ItemKind
+  uint32_t a;              // start point (the previous curve's end point)
+  uint32_t b;              // first control point (line: end point)
+};
+
 // Device-side view of a frame (pointers into one device arena).
 struct FrameView {
   const DevCmd* cmds;
@@ -149,13 +161,18 @@ struct FrameView {
   const uint32_t* images;
   uint32_t* pixels;
   // K1
-  uint32_t* seg_counts;        // [num_cmds]
-  uint32_t* seg_rows;          // [num_cmds] tile rows spanned, summed over the command's segments
-  DevSeg* segs;
+  DevItem* items;              // curves/lines of unclipped commands (any order)
+  uint32_t* seq_cmds;          // commands that need the sequential (clipping) builder
+  int4* cmd_bbox;              // [num_cmds] 24.8 bbox of the emitted segments: xmin, ymin, xmax, ymax
+  DevSeg* segs;                // emitted segments (any order)
   uint32_t* seg_meta;          // cmd << 1 | sign
+  uint32_t seg_capacity;       // slots in segs / seg_meta
+  uint32_t item_capacity;      // upper bound of the number of items
   // K2
   uint32_t* cmd_tile_x;        // tx0 | tx1 << 16 (0xFFFFFFFF = nothing)
   uint32_t* cmd_tile_y;        // ty0 | ty1 << 16
+  uint32_t* cmd_xr;            // pixel columns x0 | x1 << 16 (inclusive; x0 > x1 = nothing)
+  uint32_t* cmd_yr;            // pixel rows y0 | y1 << 16
   uint32_t* cmdrow_base;       // [num_cmds + 1]: first (cmd,row) slot
   uint32_t* cmdrow_counts;     // [num_cmdrows + 1]
   uint32_t* cmdrow_offsets;    // exclusive scan of counts
@@ -166,7 +183,7 @@ struct FrameView {
   uint32_t* row_cmds;          // command indices grouped by tile row, painter's order
   uint32_t* tile_order;        // tile processing order for the persistent fine kernel
   uint32_t* tile_canvas;       // canvas index per global tile
-  uint32_t* work_counter;
+  uint32_t* work_counter;      // [0] fine work queue, [1] items, [2] sequential commands
   uint32_t* totals;            // [4] segments, seglist bound, (cmd,row) slots, row entries
   uint32_t* error_flags;
   unsigned long long* pixel_ops;   // [2] composited pixels (mask != 0), of which pattern-fetched

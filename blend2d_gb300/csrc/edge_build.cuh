@@ -29,21 +29,44 @@ __device__ __forceinline__ int trunc_i(double x) {
   return __double2int_rz(x);
 }
 
-// Segment sink: counts (out == nullptr) or writes segments and tracks the pixel bbox.
+// Segment sink: buffers emitted segments and appends them to the frame's segment array in
+// batches (one atomic per batch). Segment order is irrelevant downstream: cell sums commute.
+constexpr int kSinkBatch = 16;
+
 struct Sink {
   DevSeg* out;
   uint32_t* meta;
+  uint32_t* counter;    // segments appended so far (all builders of the frame)
+  uint32_t capacity;    // slots in out/meta; the host re-runs with more when exceeded
   uint32_t cmd;
-  uint32_t n;
+  uint32_t n;           // segments emitted by this builder
   uint32_t rows;        // sum over segments of the tile rows each one spans (seglist size)
   int ymin, ymax, xmin, xmax;
+  int nb;
+  DevSeg buf[kSinkBatch];
+  uint32_t sbuf[kSinkBatch];
 
+  __device__ __forceinline__ void init(DevSeg* o, uint32_t* m, uint32_t* ctr, uint32_t cap, uint32_t c) {
+    out = o; meta = m; counter = ctr; capacity = cap; cmd = c;
+    n = 0; rows = 0; nb = 0;
+    ymin = INT32_MAX; ymax = INT32_MIN; xmin = INT32_MAX; xmax = INT32_MIN;
+  }
+  __device__ void flush() {
+    if (!nb) return;
+    uint32_t base = atomicAdd(counter, uint32_t(nb));
+    for (int k = 0; k < nb; k++) {
+      if (base + uint32_t(k) < capacity) {
+        out[base + k] = buf[k];
+        meta[base + k] = (cmd << 1) | sbuf[k];
+      }
+    }
+    nb = 0;
+  }
   __device__ __forceinline__ void emit(int x0, int y0, int x1, int y1, uint32_t sign) {
     if (y0 == y1) return;
-    if (out) {
-      out[n] = DevSeg{x0, y0, x1, y1};
-      meta[n] = (cmd << 1) | sign;
-    }
+    buf[nb] = DevSeg{x0, y0, x1, y1};
+    sbuf[nb] = sign;
+    if (++nb == kSinkBatch) flush();
     n++;
     rows += (uint32_t((y1 - 1) >> 8) >> kTileShift) - (uint32_t(y0 >> 8) >> kTileShift) + 1u;
     ymin = min(ymin, y0);
@@ -931,6 +954,30 @@ LineTo:
   }
   eb.done();
   return 0;
+}
+
+// One curve of a path whose every vertex lies inside the clip box: with no clipping the
+// builder's output for a curve depends only on its own control points (the previous curve ends
+// exactly at this one's first point), so each curve can be built independently. Same split and
+// safe flattening as curve_to's inside branch.
+template<int DEG>
+__device__ void inside_curve(Builder& eb, Pt* spline) {
+  Mono<DEG> mc;
+  mc.tol_sq = eb.tol_sq;
+  int nout = DEG == 3 ? split_cubic(spline) : split_quad(spline);
+  if (nout == 0) nout = DEG;
+  for (int k = 0; k < nout; k += DEG) {
+    const Pt* sp = spline + k;
+    uint32_t sign = sp[0].y > sp[DEG].y;
+    flatten_safe<DEG>(eb, mc, sp, sign);
+  }
+}
+
+// One line of such a path: the polyline step between two truncated vertices.
+__device__ __forceinline__ void inside_line(Builder& eb, Pt a, Pt b) {
+  int x0 = trunc_i(a.x), y0 = trunc_i(a.y), x1 = trunc_i(b.x), y1 = trunc_i(b.y);
+  if (y0 < y1) eb.sink.emit(x0, y0, x1, y1, 0u);
+  else if (y0 > y1) eb.sink.emit(x1, y1, x0, y0, 1u);
 }
 
 }  // namespace eb

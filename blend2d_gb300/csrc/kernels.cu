@@ -49,79 +49,125 @@ __device__ __forceinline__ int round_to_int(double x) {
   return y + (double(y) - x == -0.5);
 }
 
-__device__ uint32_t lut_entry_simd(const DevStop* s, uint32_t n, uint32_t size, uint32_t e, bool avx2) {
-  uint32_t d_size = size - 1u;
-  double fWidth = double(int32_t(d_size) << 8);
-  uint32_t c0 = rgba32_of(s[0].rgba64);
-  uint32_t u0 = 0, val = 0, span_end = 0;
-  for (uint32_t si = (s[0].offset == 0.0 && n > 1) ? 1u : 0u; si < n; si++) {
-    uint32_t c1 = rgba32_of(s[si].rgba64);
-    uint32_t u1 = uint32_t(round_to_int(s[si].offset * fWidth));
-    uint32_t start = u0 >> 8;
-    uint32_t i = (u1 >> 8) - (u0 >> 8);
-    u0 = u1;
+// One interpolation span of a LUT builder: the FP64 part of the builder (stop positions and the
+// per-channel increments) is evaluated once per span by one thread; entries only do integer work.
+struct LutSpan {
+  uint32_t start, count;   // simd: first entry and i (entries start .. start + i); scalar: start, cnt
+  uint32_t c0, c1;         // colours at both ends (scalar: after its equal-position rule)
+  int32_t inc[4];          // simd: dx per channel (b, g, r, a); scalar: r, g, b, a increments
+};
+
+// Sequential state of a builder between span-table chunks.
+struct LutCarry {
+  uint32_t si;             // next stop
+  uint32_t u0;             // previous stop position (24.8)
+  uint32_t c0, c1;         // previous colours
+};
+
+constexpr int kLutChunk = 128;
+
+// Next spans of the SSE2/AVX2 builders (interpolation_sse2.cpp:18-171, interpolation_avx2.cpp:18-177).
+__device__ int lut_spans_simd(const DevStop* s, uint32_t n, uint32_t size, LutCarry& cr, LutSpan* out) {
+  double fWidth = double(int32_t(size - 1u) << 8);
+  int k = 0;
+  for (; cr.si < n && k < kLutChunk; cr.si++) {
+    uint32_t c1 = rgba32_of(s[cr.si].rgba64);
+    uint32_t u1 = uint32_t(round_to_int(s[cr.si].offset * fWidth));
+    LutSpan sp;
+    sp.start = cr.u0 >> 8;
+    sp.count = (u1 >> 8) - (cr.u0 >> 8);
+    sp.c0 = cr.c0;
+    sp.c1 = c1;
+    cr.u0 = u1;
+    if (sp.count > 1) {
+      double scale = double(1 << 23) / double(int(sp.count));
+      for (int ch = 0; ch < 4; ch++) {
+        int32_t cc = int32_t((cr.c0 >> (8 * ch)) & 255u);
+        int32_t dd = int32_t((c1 >> (8 * ch)) & 255u) - cc;
+        double p = double(dd) * scale;
+        sp.inc[ch] = (p > -2147483649.0 && p < 2147483648.0) ? __double2int_rz(p) : INT32_MIN;
+      }
+    }
+    out[k++] = sp;
+    cr.c0 = c1;
+  }
+  return k;
+}
+
+__device__ uint32_t lut_eval_simd(const LutSpan* sp, int nspans, uint32_t e, uint32_t val, bool avx2) {
+  for (int k = 0; k < nspans; k++) {
+    const LutSpan& q = sp[k];
+    uint32_t start = q.start, i = q.count;
     if (i <= 1) {
-      if (e == start) val = avx2 ? premul_avx2_short_span(c0) : premul_simd(c0);
-      else if (i == 1 && e == start + 1) val = avx2 ? premul_avx2_short_span(c1) : premul_simd(c1);
+      if (e == start) val = avx2 ? premul_avx2_short_span(q.c0) : premul_simd(q.c0);
+      else if (i == 1 && e == start + 1) val = avx2 ? premul_avx2_short_span(q.c1) : premul_simd(q.c1);
     }
     else if (e >= start && e <= start + i) {
       uint32_t j = e - start;
-      double scale = double(1 << 23) / double(int(i));
       uint32_t v[4];
-      for (int k = 0; k < 4; k++) {
-        int32_t cc = int32_t((c0 >> (8 * k)) & 255u);
-        int32_t dd = int32_t((c1 >> (8 * k)) & 255u) - cc;
-        double p = double(dd) * scale;
-        int32_t dx = (p > -2147483649.0 && p < 2147483648.0) ? __double2int_rz(p) : INT32_MIN;
+#pragma unroll
+      for (int ch = 0; ch < 4; ch++) {
+        int32_t cc = int32_t((q.c0 >> (8 * ch)) & 255u);
         int32_t cx = int32_t(uint32_t(cc) << 23) + (1 << 22);
-        v[k] = uint32_t(cx + int32_t(uint32_t(dx) * j)) >> 23;
+        v[ch] = uint32_t(cx + int32_t(uint32_t(q.inc[ch]) * j)) >> 23;
       }
       uint32_t a = v[3];
       val = (sat8(simd_div255(255u * a)) << 24) | (sat8(simd_div255(v[2] * a)) << 16) |
             (sat8(simd_div255(v[1] * a)) << 8) | sat8(simd_div255(v[0] * a));
     }
-    span_end = start + i + 1u;
-    c0 = c1;
   }
-  if (e >= span_end) val = premul_simd(c0);
-  if (e == 0) val = premul_simd(rgba32_of(s[0].rgba64));
   return val;
 }
 
-__device__ uint32_t lut_entry_scalar(const DevStop* s, uint32_t n, uint32_t size, uint32_t e) {
-  uint32_t c0 = rgba32_of(s[0].rgba64), c1 = c0;
-  if (n == 1) return premul_scalar(c0);
-  uint32_t d_size = size - 1u;
-  double fWidth = double(int32_t(d_size) << 8);
-  uint32_t p0 = 0, val = 0, span_end = 0;
-  for (uint32_t si = 0; si < n; si++) {
-    c1 = rgba32_of(s[si].rgba64);
-    uint32_t p1 = uint32_t(round_to_int(s[si].offset * fWidth));
-    uint32_t start = p0 >> 8;
-    uint32_t i = (p1 >> 8) - (p0 >> 8);
-    if (i == 0) c0 = c1;
-    p0 = p1;
-    uint32_t cnt = i + 1u;
+// Next spans of the portable builder (interpolation.cpp:19-156).
+__device__ int lut_spans_scalar(const DevStop* s, uint32_t n, uint32_t size, LutCarry& cr, LutSpan* out) {
+  double fWidth = double(int32_t(size - 1u) << 8);
+  int k = 0;
+  for (; cr.si < n && k < kLutChunk; cr.si++) {
+    cr.c1 = rgba32_of(s[cr.si].rgba64);
+    uint32_t p1 = uint32_t(round_to_int(s[cr.si].offset * fWidth));
+    uint32_t i = (p1 >> 8) - (cr.u0 >> 8);
+    LutSpan sp;
+    sp.start = cr.u0 >> 8;
+    if (i == 0) cr.c0 = cr.c1;
+    cr.u0 = p1;
+    sp.count = i + 1u;
+    sp.c0 = cr.c0;
+    sp.c1 = cr.c1;
+    if (cr.c0 != cr.c1 && sp.count > 1) {
+      const uint32_t kMask = 0xFFu << 23;
+      int32_t div = int32_t(sp.count - 1u);
+      uint32_t c0 = cr.c0, c1 = cr.c1;
+      sp.inc[0] = int32_t(((c1 << 7) & kMask) - ((c0 << 7) & kMask)) / div;
+      sp.inc[1] = int32_t(((c1 << 15) & kMask) - ((c0 << 15) & kMask)) / div;
+      sp.inc[2] = int32_t(((c1 << 23) & kMask) - ((c0 << 23) & kMask)) / div;
+      sp.inc[3] = int32_t(((c1 >> 1) & kMask) - ((c0 >> 1) & kMask)) / div;
+    }
+    out[k++] = sp;
+    if (cr.c0 != cr.c1) cr.c0 = cr.c1;
+  }
+  return k;
+}
+
+__device__ uint32_t lut_eval_scalar(const LutSpan* sp, int nspans, uint32_t e, uint32_t val) {
+  for (int k = 0; k < nspans; k++) {
+    const LutSpan& q = sp[k];
+    uint32_t start = q.start, cnt = q.count, c0 = q.c0, c1 = q.c1;
     if (e >= start && e < start + cnt) {
       if (c0 == c1 || e == start) val = premul_scalar(c0);
       else {
         const uint32_t kMask = 0xFFu << 23;
-        uint32_t k = e - start;
-        uint32_t div = cnt - 1u;
+        uint32_t j = e - start;
         uint32_t r_pos = (c0 << 7) & kMask, g_pos = (c0 << 15) & kMask, b_pos = (c0 << 23) & kMask;
-        uint32_t r_inc = uint32_t(int32_t(((c1 << 7) & kMask) - r_pos) / int32_t(div));
-        uint32_t g_inc = uint32_t(int32_t(((c1 << 15) & kMask) - g_pos) / int32_t(div));
-        uint32_t b_inc = uint32_t(int32_t(((c1 << 23) & kMask) - b_pos) / int32_t(div));
-        r_pos += (1u << 22) + k * r_inc;
-        g_pos += (1u << 22) + k * g_inc;
-        b_pos += (1u << 22) + k * b_inc;
+        r_pos += (1u << 22) + j * uint32_t(q.inc[0]);
+        g_pos += (1u << 22) + j * uint32_t(q.inc[1]);
+        b_pos += (1u << 22) + j * uint32_t(q.inc[2]);
         if (((c0 & c1) >> 24) == 0xFFu) {
           val = 0xFF000000u + ((r_pos & kMask) >> 7) + ((g_pos & kMask) >> 15) + ((b_pos & kMask) >> 23);
         }
         else {
           uint32_t a_pos = (c0 >> 1) & kMask;
-          uint32_t a_inc = uint32_t(int32_t(((c1 >> 1) & kMask) - a_pos) / int32_t(div));
-          a_pos += (1u << 22) + k * a_inc;
+          a_pos += (1u << 22) + j * uint32_t(q.inc[3]);
           uint32_t cp = ((b_pos & kMask) >> 23) + ((r_pos & kMask) >> 7);
           uint32_t ca = ((a_pos & kMask) >> 23);
           uint32_t cg = ((g_pos & kMask) >> 23);
@@ -134,87 +180,225 @@ __device__ uint32_t lut_entry_scalar(const DevStop* s, uint32_t n, uint32_t size
         }
       }
     }
-    if (c0 != c1) c0 = c1;
-    span_end = start + cnt;
   }
-  if (e >= span_end) val = premul_scalar(c1);
-  if (e == 0) val = premul_scalar(rgba32_of(s[0].rgba64));
   return val;
 }
 
+// One block per LUT. Thread 0 builds the span table in chunks of kLutChunk spans in shared memory;
+// after each chunk every thread applies it to its entries (the entry's value is whatever the
+// reference's sequential span writer leaves there: later spans overwrite earlier ones), carrying
+// the values through the LUT itself. The trailing fill and entry 0 are applied last.
 __global__ void lut_kernel(const DevLutJob* jobs, const DevStop* stops, uint32_t* luts) {
-  DevLutJob job = jobs[blockIdx.x];
+  __shared__ LutSpan spans[kLutChunk];
+  __shared__ int nspans;
+  __shared__ uint32_t span_end;
+  __shared__ LutCarry carry;
+  const DevLutJob job = jobs[blockIdx.x];
   const DevStop* s = stops + job.stop_first;
+  const uint32_t n = job.stop_count;
+  const bool scalar = job.variant == kLutScalar;
+  const bool avx2 = job.variant == kLutAVX2;
+  uint32_t* lut = luts + job.lut_offset;
+  const uint32_t first_c = rgba32_of(s[0].rgba64);
+  if (threadIdx.x == 0) {
+    carry.si = (!scalar && s[0].offset == 0.0 && n > 1) ? 1u : 0u;
+    carry.u0 = 0;
+    carry.c0 = first_c;
+    carry.c1 = first_c;
+    span_end = 0;
+  }
+  bool first_chunk = true;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      nspans = scalar ? lut_spans_scalar(s, n, job.lut_size, carry, spans)
+                      : lut_spans_simd(s, n, job.lut_size, carry, spans);
+      if (nspans) span_end = spans[nspans - 1].start + spans[nspans - 1].count + (scalar ? 0u : 1u);
+    }
+    __syncthreads();
+    int ns = nspans;
+    if (!ns) break;
+    for (uint32_t e = threadIdx.x; e < job.lut_size; e += blockDim.x) {
+      uint32_t v = first_chunk ? 0u : lut[e];
+      lut[e] = scalar ? lut_eval_scalar(spans, ns, e, v) : lut_eval_simd(spans, ns, e, v, avx2);
+    }
+    first_chunk = false;
+  }
+  // the carry's last colour is the builder's trailing colour (c0 for SIMD, c1 for scalar)
+  const uint32_t tail = scalar ? carry.c1 : carry.c0;
+  const uint32_t end = span_end;
   for (uint32_t e = threadIdx.x; e < job.lut_size; e += blockDim.x) {
-    uint32_t v = job.variant == kLutScalar ? lut_entry_scalar(s, job.stop_count, job.lut_size, e)
-                                           : lut_entry_simd(s, job.stop_count, job.lut_size, e, job.variant == kLutAVX2);
-    luts[job.lut_offset + e] = v;
+    uint32_t v = first_chunk ? 0u : lut[e];
+    if (scalar && n == 1) v = premul_scalar(first_c);
+    else {
+      if (e >= end) v = scalar ? premul_scalar(tail) : premul_simd(tail);
+      if (e == 0) v = scalar ? premul_scalar(first_c) : premul_simd(first_c);
+    }
+    lut[e] = v;
   }
 }
 
 // ---------------------------------------------------------------------------------------------
-// K1 - FP64 edge building, one thread per analytic command; pass 0 counts, pass 1 writes.
+// K1 - FP64 edge building. `classify` looks at every analytic command: if all its transformed
+// vertices are finite and inside the clip box, no clipping can occur and each curve/line of it is
+// an independent item (built one per thread by `edge_items`); otherwise the whole command goes to
+// `edge_sequential`, one thread running the reference's builder with its clipping state machine.
+// Both append segments to one array with batched atomics.
 // ---------------------------------------------------------------------------------------------
 
-__global__ void edge_kernel(FrameView f, int pass) {
-  uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= f.num_cmds) return;
-  DevCmd cmd = f.cmds[c];
-  if (cmd.kind != kFillAnalytic) {
-    if (pass == 0) { f.seg_counts[c] = 0; f.seg_rows[c] = 0; }
-    return;
+struct Xf {
+  double m00, m01, m10, m11, m20, m21;
+  bool affine;
+  __device__ __forceinline__ eb::Pt map(const double* xy) const {
+    double x = xy[0], y = xy[1];
+    if (affine) return eb::Pt{x * m00 + y * m10 + m20, x * m01 + y * m11 + m21};
+    return eb::Pt{x * m00 + m20, y * m11 + m21};
   }
-  const DevCanvas cv = f.canvases[cmd.canvas];
-  const DevXform xf = f.xforms[cmd.xform];
+};
 
-  eb::Builder b;
-  b.sink.out = pass ? f.segs + cmd.seg_first : nullptr;
-  b.sink.meta = pass ? f.seg_meta + cmd.seg_first : nullptr;
-  b.sink.cmd = c;
-  b.sink.n = 0;
-  b.sink.ymin = INT32_MAX; b.sink.ymax = INT32_MIN; b.sink.xmin = INT32_MAX; b.sink.xmax = INT32_MIN;
+__device__ __forceinline__ Xf load_xf(const DevXform& x) {
+  return Xf{x.m[0], x.m[1], x.m[2], x.m[3], x.m[4], x.m[5], x.affine != 0};
+}
+
+__device__ __forceinline__ void init_builder(eb::Builder& b, const DevCanvas& cv) {
   b.cx0 = 0.0; b.cy0 = 0.0; b.cx1 = double(cv.w) * 256.0; b.cy1 = double(cv.h) * 256.0;
   b.icx0 = eb::trunc_i(b.cx0); b.icx1 = eb::trunc_i(b.cx1);
   const double tol = 0.20 * 256.0;
   b.tol_sq = tol * tol;
   b.acc_x0_y0 = b.acc_x0_y1 = b.acc_x1_y0 = b.acc_x1_y1 = b.cy0;
   b.px = b.py = 0; b.psign = 0; b.pasc = false;
+}
 
-  eb::Src src;
-  src.xy = f.verts + 2ull * cmd.geom_first;
-  src.cmd = cmd.geom == kGeomPath ? f.path_cmds + cmd.geom_first : nullptr;
-  src.i = 0;
-  src.n = int(cmd.geom_count);
-  src.affine = xf.affine != 0;
-  src.m00 = xf.m[0]; src.m01 = xf.m[1]; src.m10 = xf.m[2]; src.m11 = xf.m[3]; src.m20 = xf.m[4]; src.m21 = xf.m[5];
-
-  b.sink.rows = 0;
-  int rc = eb::build(b, src);
-  if (pass == 0) {
-    // An invalid geometry (NaN) aborts the whole command in the reference (the edge builder is
-    // reverted, rastercontextops.cpp:23-28), so nothing of it is rendered.
-    bool ok = rc == 0 && b.sink.n != 0;
-    f.seg_counts[c] = ok ? b.sink.n : 0u;
-    f.seg_rows[c] = ok ? b.sink.rows : 0u;
-    f.cmds_rw[c].status = rc ? 1u : (b.sink.n ? 0u : 2u);
-    if (ok) {
-      // pixel bbox of the coverage: rows [ymin >> 8, (ymax - 1) >> 8], columns [xmin >> 8, xmax >> 8]
-      int y0 = b.sink.ymin >> 8, y1 = (b.sink.ymax - 1) >> 8;
-      int x0 = b.sink.xmin >> 8, x1 = b.sink.xmax >> 8;
-      f.cmds_rw[c].box[0] = max(x0, 0);
-      f.cmds_rw[c].box[1] = max(y0, 0);
-      f.cmds_rw[c].box[2] = min(x1, cv.w - 1);
-      f.cmds_rw[c].box[3] = min(y1, cv.h - 1);
+// Walks the figures of a command the way add_from_source does (edgebuilder_p.h:1032-1070) and
+// calls fn(kind, a, b) for every line, curve and closing line.
+template<typename Fn>
+__device__ void for_each_item(const uint8_t* cmd, int n, Fn&& fn) {
+  int i = 0;
+  for (;;) {
+    if (cmd) { while (i < n && cmd[i] != 0) i++; }
+    if (i >= n) return;
+    int start = i++, prev = start;
+    for (;;) {
+      if (cmd ? (i != n && cmd[i] == 1) : (i != n)) { fn(kItemLine, prev, i); prev = i; i += 1; }
+      else if (cmd && i <= n - 2 && cmd[i] == 2) { fn(kItemQuad, prev, i); prev = i + 1; i += 2; }
+      else if (cmd && i < n - 2 && cmd[i] == 4) { fn(kItemCubic, prev, i); prev = i + 2; i += 3; }
+      else if (cmd && i < n - 2 && cmd[i] == 3) { fn(kItemConic, prev, i); prev = i + 2; i += 2; }
+      else { fn(kItemLine, prev, start); break; }
     }
+    if (!cmd) return;
   }
 }
 
-// The K1 emit pass re-reads seg_first from the command; copy the scanned offsets in.
-__global__ void set_seg_first_kernel(FrameView f, const uint32_t* offsets) {
+__global__ void classify_kernel(FrameView f) {
   uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= f.num_cmds) return;
-  f.cmds_rw[c].seg_first = offsets[c];
-  f.cmds_rw[c].seg_count = f.seg_counts[c];
+  const DevCmd cmd = f.cmds[c];
+  if (cmd.kind != kFillAnalytic) return;
+  f.cmd_bbox[c] = make_int4(INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN);
+  f.cmds_rw[c].status = 2u;
+  const DevCanvas cv = f.canvases[cmd.canvas];
+  const Xf xf = load_xf(f.xforms[cmd.xform]);
+  const double* xy = f.verts + 2ull * cmd.geom_first;
+  const uint8_t* pc = cmd.geom == kGeomPath ? f.path_cmds + cmd.geom_first : nullptr;
+  const int n = int(cmd.geom_count);
+  const double cx1 = double(cv.w) * 256.0, cy1 = double(cv.h) * 256.0;
+  bool inside = true;
+  for (int k = 0; k < n && inside; k++) {
+    eb::Pt p = xf.map(xy + 2 * k);
+    inside = (p.x >= 0.0) & (p.x <= cx1) & (p.y >= 0.0) & (p.y <= cy1);   // false for NaN too
+  }
+  if (!inside) {
+    uint32_t idx = atomicAdd(f.work_counter + 2, 1u);
+    f.seq_cmds[idx] = c;
+    return;
+  }
+  uint32_t count = 0;
+  for_each_item(pc, n, [&](uint32_t, int, int) { count++; });
+  uint32_t base = atomicAdd(f.work_counter + 1, count);
+  for_each_item(pc, n, [&](uint32_t kind, int a, int b) {
+    if (base < f.item_capacity) f.items[base] = DevItem{c, kind, uint32_t(a), uint32_t(b)};
+    base++;
+  });
+}
+
+__global__ void edge_sequential_kernel(FrameView f) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t rows = 0;
+  if (t < f.work_counter[2]) {
+    const uint32_t c = f.seq_cmds[t];
+    const DevCmd cmd = f.cmds[c];
+    const DevCanvas cv = f.canvases[cmd.canvas];
+    const DevXform xf = f.xforms[cmd.xform];
+    eb::Builder b;
+    init_builder(b, cv);
+    b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, c);
+    eb::Src src;
+    src.xy = f.verts + 2ull * cmd.geom_first;
+    src.cmd = cmd.geom == kGeomPath ? f.path_cmds + cmd.geom_first : nullptr;
+    src.i = 0;
+    src.n = int(cmd.geom_count);
+    src.affine = xf.affine != 0;
+    src.m00 = xf.m[0]; src.m01 = xf.m[1]; src.m10 = xf.m[2]; src.m11 = xf.m[3]; src.m20 = xf.m[4]; src.m21 = xf.m[5];
+    int rc = eb::build(b, src);
+    // An invalid geometry (NaN) aborts the whole command in the reference (the edge builder is
+    // reverted, rastercontextops.cpp:23-28): segments already appended are orphaned (the status
+    // keeps the command out of binning).
+    if (rc == 0) b.sink.flush();
+    f.cmds_rw[c].status = rc ? 1u : (b.sink.n ? 0u : 2u);
+    if (rc == 0 && b.sink.n) {
+      f.cmd_bbox[c] = make_int4(b.sink.xmin, b.sink.ymin, b.sink.xmax, b.sink.ymax);
+      rows = b.sink.rows;
+    }
+  }
+  rows = __reduce_add_sync(0xFFFFFFFFu, rows);
+  if ((threadIdx.x & 31) == 0 && rows) atomicAdd(f.totals + 1, rows);
+}
+
+__global__ void edge_items_kernel(FrameView f) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t rows = 0;
+  uint32_t n_items = min(f.work_counter[1], f.item_capacity);
+  if (t < n_items) {
+    const DevItem it = f.items[t];
+    const DevCmd cmd = f.cmds[it.cmd];
+    const DevCanvas cv = f.canvases[cmd.canvas];
+    const Xf xf = load_xf(f.xforms[cmd.xform]);
+    const double* xy = f.verts + 2ull * cmd.geom_first;
+    eb::Builder b;
+    init_builder(b, cv);
+    b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, it.cmd);
+    eb::Pt spline[25];
+    spline[0] = xf.map(xy + 2 * it.a);
+    switch (it.kind) {
+      case kItemLine:
+        eb::inside_line(b, spline[0], xf.map(xy + 2 * it.b));
+        break;
+      case kItemQuad:
+        spline[1] = xf.map(xy + 2 * it.b); spline[2] = xf.map(xy + 2 * (it.b + 1));
+        eb::inside_curve<2>(b, spline);
+        break;
+      case kItemConic:
+        spline[1] = xf.map(xy + 2 * it.b); spline[2] = xf.map(xy + 2 * (it.b + 2));
+        eb::inside_curve<2>(b, spline);
+        break;
+      default:
+        spline[1] = xf.map(xy + 2 * it.b); spline[2] = xf.map(xy + 2 * (it.b + 1)); spline[3] = xf.map(xy + 2 * (it.b + 2));
+        eb::inside_curve<3>(b, spline);
+        break;
+    }
+    b.sink.flush();
+    if (b.sink.n) {
+      int4* bb = f.cmd_bbox + it.cmd;
+      atomicMin(&bb->x, b.sink.xmin);
+      atomicMin(&bb->y, b.sink.ymin);
+      atomicMax(&bb->z, b.sink.xmax);
+      atomicMax(&bb->w, b.sink.ymax);
+      f.cmds_rw[it.cmd].status = 0u;
+      rows = b.sink.rows;
+    }
+  }
+  rows = __reduce_add_sync(0xFFFFFFFFu, rows);
+  if ((threadIdx.x & 31) == 0 && rows) atomicAdd(f.totals + 1, rows);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -286,8 +470,15 @@ __global__ void cmd_tiles_kernel(FrameView f, uint32_t* cmdrow_counts_per_cmd, u
   int x0, y0, x1, y1;   // inclusive pixel range
   bool empty = false;
   if (cmd.kind == kFillAnalytic) {
+    // pixel bbox of the coverage: rows [ymin >> 8, (ymax - 1) >> 8], columns [xmin >> 8, xmax >> 8]
     empty = cmd.status != 0;
-    x0 = cmd.box[0]; y0 = cmd.box[1]; x1 = cmd.box[2]; y1 = cmd.box[3];
+    const int4 bb = f.cmd_bbox[c];
+    x0 = max(bb.x >> 8, 0); y0 = max(bb.y >> 8, 0);
+    x1 = min(bb.z >> 8, cv.w - 1); y1 = min((bb.w - 1) >> 8, cv.h - 1);
+    if (!empty) {
+      f.cmds_rw[c].box[0] = x0; f.cmds_rw[c].box[1] = y0;
+      f.cmds_rw[c].box[2] = x1; f.cmds_rw[c].box[3] = y1;
+    }
   }
   else if (cmd.kind == kFillBoxA) {
     x0 = cmd.box[0]; y0 = cmd.box[1]; x1 = cmd.box[2] - 1; y1 = cmd.box[3] - 1;
@@ -300,9 +491,13 @@ __global__ void cmd_tiles_kernel(FrameView f, uint32_t* cmdrow_counts_per_cmd, u
   if (empty) {
     f.cmd_tile_x[c] = 0xFFFFFFFFu;
     f.cmd_tile_y[c] = 0xFFFFFFFFu;
+    f.cmd_xr[c] = 0x0000FFFFu;   // x0 = 65535 > x1 = 0: overlaps nothing
+    f.cmd_yr[c] = 0x0000FFFFu;
     cmdrow_counts_per_cmd[c] = 0;
     return;
   }
+  f.cmd_xr[c] = uint32_t(x0) | (uint32_t(x1) << 16);
+  f.cmd_yr[c] = uint32_t(y0) | (uint32_t(y1) << 16);
   uint32_t tx0 = uint32_t(x0) >> kTileShift, tx1 = uint32_t(x1) >> kTileShift;
   uint32_t ty0 = uint32_t(y0) >> kTileShift, ty1 = uint32_t(y1) >> kTileShift;
   f.cmd_tile_x[c] = tx0 | (tx1 << 16);
@@ -355,39 +550,46 @@ __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// K3 - persistent fine kernel
+// K3 - persistent fine kernel. The work unit is a strip of kStripRows x kTileW pixels (one warp,
+// 4 pixels per lane held in registers from one 128-bit load to one 128-bit store). Warps pull
+// strips from an atomic queue and never wait on each other: for every command of the strip's tile
+// row that overlaps the strip (painter's order) the warp rasterizes the command's segments of that
+// tile row into its own shared-memory cells, sweeps coverage with 8-lane shuffles, and composites.
 // ---------------------------------------------------------------------------------------------
 
-struct FineShared {
-  uint32_t cells[kTileH * kTileW];
-  uint32_t backdrop[kTileH];
-  uint32_t queue[kFineThreads];
-  uint32_t warp_counts[kFineThreads / 32];
-  uint32_t tile;
-  uint32_t qn;
+constexpr int kStripRows = 4;                       // rows per strip (32 lanes x 4 pixels)
+constexpr int kStripsPerTile = kTileH / kStripRows;
+constexpr int kFineWarps = kFineThreads / 32;
+
+struct StripShared {
+  uint32_t cells[kStripRows * kTileW];
+  uint32_t backdrop[kStripRows];
 };
 
 __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
-  __shared__ FineShared sh;
-  const int tid = threadIdx.x;
-  const int lane = tid & 31, warp = tid >> 5;
-  const int prow = tid >> 3;            // pixel row within the tile
-  const int pcol = (tid & 7) * 4;       // first of 4 pixel columns
-
-  uint32_t ops = 0, pat_ops = 0;   // composited pixels of this thread (all tiles)
+  __shared__ StripShared sh[kFineWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  StripShared& ws = sh[warp];
+  const int prow = lane >> 3;            // row within the strip
+  const int pcol = (lane & 7) * 4;       // first of this lane's 4 columns
+  uint32_t ops = 0, pat_ops = 0;         // composited pixels of this lane (all strips)
+  const uint32_t num_units = f.num_tiles * kStripsPerTile;
 
   for (;;) {
-    if (tid == 0) sh.tile = atomicAdd(f.work_counter, 1u);
-    __syncthreads();
-    uint32_t t = sh.tile;
-    __syncthreads();
-    if (t >= f.num_tiles) break;
-    uint32_t tile = f.tile_order[t];
+    uint32_t unit = 0;
+    if (lane == 0) unit = atomicAdd(f.work_counter, 1u);
+    unit = __shfl_sync(0xFFFFFFFFu, unit, 0);
+    if (unit >= num_units) break;
+    uint32_t tile = f.tile_order[unit / kStripsPerTile];
+    int strip = int(unit % kStripsPerTile);
     const DevCanvas cv = f.canvases[f.tile_canvas[tile]];
     uint32_t local = tile - cv.tile_base;
     int tx = int(local % uint32_t(cv.tiles_x)), ty = int(local / uint32_t(cv.tiles_x));
-    int x_base = tx * kTileW, y = ty * kTileH + prow;
-    int xp = x_base + pcol;
+    int x_base = tx * kTileW;
+    int row0 = ty * kTileH + strip * kStripRows;
+    if (row0 >= cv.h) continue;
+    int row1 = min(row0 + kStripRows, cv.h) - 1;     // last row of the strip inside the canvas
+    int y = row0 + prow, xp = x_base + pcol;
     bool row_ok = y < cv.h;
     uint32_t* dst = cv.pixels + int64_t(y) * cv.stride + xp;
 
@@ -405,69 +607,61 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
     uint32_t row_id = cv.row_base + uint32_t(ty);
     uint32_t list_first = f.row_offsets[row_id];
     uint32_t list_count = f.row_counts[row_id];
-    ras::TileSink sink{sh.cells, sh.backdrop, x_base};
-    int row0 = ty * kTileH;
+    ras::WindowSink sink{ws.cells, ws.backdrop, x_base};
+    const uint32_t strip_y = uint32_t(row0) | (uint32_t(row1) << 16);
+    const uint32_t strip_x = uint32_t(x_base) | (uint32_t(min(x_base + kTileW, cv.w) - 1) << 16);
 
-    for (uint32_t base = 0; base < list_count; base += kFineThreads) {
-      // ordered compaction of the commands of this chunk that overlap the tile's columns
-      uint32_t c = 0xFFFFFFFFu;
+    for (uint32_t base = 0; base < list_count; base += 32) {
+      // commands of this chunk whose pixel bbox overlaps the strip, in painter's order
+      uint32_t c = 0;
       bool hit = false;
-      if (base + tid < list_count) {
-        c = f.row_cmds[list_first + base + tid];
-        uint32_t tr = f.cmd_tile_x[c];
-        hit = (tr & 0xFFFFu) <= uint32_t(tx) && (tr >> 16) >= uint32_t(tx);
+      if (base + lane < list_count) {
+        c = f.row_cmds[list_first + base + lane];
+        uint32_t bx = f.cmd_xr[c], by = f.cmd_yr[c];
+        hit = (bx & 0xFFFFu) <= (strip_x >> 16) && (bx >> 16) >= (strip_x & 0xFFFFu) &&
+              (by & 0xFFFFu) <= (strip_y >> 16) && (by >> 16) >= (strip_y & 0xFFFFu);
       }
       uint32_t ballot = __ballot_sync(0xFFFFFFFFu, hit);
-      if (lane == 0) sh.warp_counts[warp] = __popc(ballot);
-      __syncthreads();
-      uint32_t off = 0, total = 0;
-      for (int w = 0; w < kFineThreads / 32; w++) { uint32_t n = sh.warp_counts[w]; off += w < warp ? n : 0u; total += n; }
-      if (hit) sh.queue[off + __popc(ballot & ((1u << lane) - 1u))] = c;
-      __syncthreads();
-
-      for (uint32_t q = 0; q < total; q++) {
-        uint32_t ci = sh.queue[q];
+      while (ballot) {
+        int bit = __ffs(ballot) - 1;
+        ballot &= ballot - 1;
+        uint32_t ci = __shfl_sync(0xFFFFFFFFu, c, bit);
         const DevCmd& cmd = f.cmds[ci];
         const uint32_t kind = cmd.kind;
-        const DevStyle& st = f.styles[cmd.style];
         const uint32_t alpha = cmd.alpha;
-        const bool src_copy = (cmd.flags & 1u) != 0;
         uint32_t m[4] = {0u, 0u, 0u, 0u};
         int fetch_y0 = cmd.fetch_y0;
 
         if (kind == kFillAnalytic) {
-#pragma unroll
-          for (int k = 0; k < 4; k++) sh.cells[tid * 4 + k] = 0u;
-          if (tid < kTileH) sh.backdrop[tid] = 0u;
-          __syncthreads();
+          *reinterpret_cast<uint4*>(&ws.cells[lane * 4]) = make_uint4(0u, 0u, 0u, 0u);
+          if (lane < kStripRows) ws.backdrop[lane] = 0u;
+          __syncwarp();
           uint32_t ty0 = f.cmd_tile_y[ci] & 0xFFFFu;
           uint32_t slot = f.cmdrow_base[ci] + uint32_t(ty) - ty0;
           uint32_t s_first = f.cmdrow_offsets[slot];
           uint32_t s_count = f.cmdrow_counts[slot];
-          for (uint32_t k = tid; k < s_count; k += kFineThreads) {
+          for (uint32_t k = lane; k < s_count; k += 32) {
             uint32_t si = f.seglist[s_first + k];
-            ras::segment_to_tile(f.segs[si], f.seg_meta[si] & 1u, row0, cv.h - 1, sink);
+            ras::segment_to_window(f.segs[si], f.seg_meta[si] & 1u, row0, kStripRows, cv.h - 1, sink);
           }
-          __syncthreads();
-          // coverage sweep: prefix over the row (8 threads x 4 cells) + the carried-in backdrop
-          uint32_t cl[4];
-#pragma unroll
-          for (int k = 0; k < 4; k++) cl[k] = sh.cells[prow * kTileW + pcol + k];
+          __syncwarp();
+          // coverage sweep: prefix over the row (8 lanes x 4 cells) + the carried-in backdrop
+          uint4 cv4 = *reinterpret_cast<const uint4*>(&ws.cells[lane * 4]);
+          uint32_t cl[4] = {cv4.x, cv4.y, cv4.z, cv4.w};
           uint32_t s4 = cl[0] + cl[1] + cl[2] + cl[3];
           uint32_t incl = s4;
 #pragma unroll
           for (int o = 1; o < 8; o <<= 1) {
             uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o, 8);
-            if ((tid & 7) >= o) incl += v;
+            if ((lane & 7) >= o) incl += v;
           }
-          uint32_t cov = (256u << 9) + sh.backdrop[prow] + incl - s4;
+          uint32_t cov = (256u << 9) + ws.backdrop[prow] + incl - s4;
           uint32_t rule = (cmd.flags & 2u) ? 0x1FFu : 0xFFFFFFFFu;
 #pragma unroll
           for (int k = 0; k < 4; k++) { cov += cl[k]; m[k] = px::calc_mask(cov, rule, alpha); }
           // the reference initializes its fetcher at the start of each band of the command
-          int y_start = cmd.box[1];
-          fetch_y0 = max(y_start, (y / cv.band_height) * cv.band_height);
-          __syncthreads();
+          fetch_y0 = max(cmd.box[1], (y / cv.band_height) * cv.band_height);
+          __syncwarp();
         }
         else if (kind == kFillBoxA) {
           bool in_y = y >= cmd.box[1] && y < cmd.box[3];
@@ -480,13 +674,15 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
         }
 
         if (row_ok && (m[0] | m[1] | m[2] | m[3])) {
+          const DevStyle& st = f.styles[cmd.style];
+          const bool src_copy = (cmd.flags & 1u) != 0;
           px::RowState rs = px::row_state(st, y, fetch_y0);
           uint32_t n = 0;
 #pragma unroll
           for (int k = 0; k < 4; k++) {
             if (m[k] && xp + k < cv.w) {
-              uint32_t s = px::fetch(st, rs, xp + k, f.luts, f.images);
-              pix[k] = px::composite(pix[k], s, m[k], src_copy);
+              uint32_t sv = px::fetch(st, rs, xp + k, f.luts, f.images);
+              pix[k] = px::composite(pix[k], sv, m[k], src_copy);
               n++;
             }
           }
@@ -494,7 +690,6 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
           pat_ops += st.fetch >= kFetchPatAlignedPad ? n : 0u;
         }
       }
-      __syncthreads();
     }
 
     if (full) {
@@ -597,18 +792,12 @@ int launch_lut(const FrameView& f, cudaStream_t st) {
   return 1;
 }
 
-int launch_edge_count(const FrameView& f, cudaStream_t st) {
+int launch_edges(const FrameView& f, cudaStream_t st) {
   if (!f.num_cmds) return 0;
-  edge_kernel<<<cdiv(f.num_cmds, 64), 64, 0, st>>>(f, 0);
-  return 1;
-}
-
-int launch_edge_emit(const FrameView& f, const uint32_t* seg_offsets, cudaStream_t st) {
-  if (!f.num_cmds) return 0;
-  set_seg_first_kernel<<<cdiv(f.num_cmds, 256), 256, 0, st>>>(f, seg_offsets);
-  if (!f.num_segs) return 1;
-  edge_kernel<<<cdiv(f.num_cmds, 64), 64, 0, st>>>(f, 1);
-  return 2;
+  classify_kernel<<<cdiv(f.num_cmds, 128), 128, 0, st>>>(f);
+  edge_sequential_kernel<<<cdiv(f.num_cmds, 64), 64, 0, st>>>(f);
+  edge_items_kernel<<<cdiv(f.item_capacity ? f.item_capacity : 1, 128), 128, 0, st>>>(f);
+  return 3;
 }
 
 int launch_cmd_tiles(const FrameView& f, uint32_t* cmdrow_counts_per_cmd, cudaStream_t st) {
@@ -647,7 +836,8 @@ int fine_grid_size() {
 int launch_fine(const FrameView& f, cudaStream_t st) {
   if (!f.num_tiles) return 0;
   int grid = fine_grid_size();
-  if (uint32_t(grid) > f.num_tiles) grid = int(f.num_tiles);
+  uint32_t max_blocks = (f.num_tiles * kStripsPerTile + kFineWarps - 1) / kFineWarps;
+  if (uint32_t(grid) > max_blocks) grid = int(max_blocks);
   fine_kernel<<<grid, kFineThreads, 0, st>>>(f);
   return 1;
 }

@@ -15,8 +15,7 @@ int launch_total(const uint32_t* counts, const uint32_t* offsets, uint32_t n, ui
 int launch_sum(const uint32_t* in, uint32_t n, uint32_t* total, cudaStream_t st);
 
 int launch_lut(const FrameView& f, cudaStream_t st);
-int launch_edge_count(const FrameView& f, cudaStream_t st);
-int launch_edge_emit(const FrameView& f, const uint32_t* seg_offsets, cudaStream_t st);
+int launch_edges(const FrameView& f, cudaStream_t st);
 int launch_cmd_tiles(const FrameView& f, uint32_t* cmdrow_counts_per_cmd, cudaStream_t st);
 int launch_seg_bin(const FrameView& f, int scatter, cudaStream_t st);
 int launch_rows_and_tiles(const FrameView& f, uint32_t* row_canvas, cudaStream_t st);

@@ -1,13 +1,13 @@
-// raster.cuh - the reference's analytic cell rasterizer, run per (segment, tile row).
+// raster.cuh - the reference's analytic cell rasterizer, run per (segment, window of rows).
 //
 // The cell values come from the reference's integer DDA (AnalyticRasterizer::prepare_ref,
 // advanceToY and rasterize<kOptionBandingMode>, blend2d/raster/analyticrasterizer_p.h:289-1166):
-// cell[x] += (cover << 9) - area, cell[x+1] += area, with the same error accumulators. A tile row
-// is one rasterizer band: a segment that starts above it is jumped to the tile's first row with
-// advanceToY (the reference's own unit test pins advanceToY to the banded state), then rasterized
-// in banding mode for the tile's rows. Cells left of the tile are summed into a per-row backdrop
-// (the coverage carried in from the left), cells right of it are dropped. All sums are modular
-// u32, so the per-tile partial sums equal the reference's band sums.
+// cell[x] += (cover << 9) - area, cell[x+1] += area, with the same error accumulators. A window of
+// rows is one rasterizer band: a segment that starts above it is jumped to the window's first row
+// with advanceToY (the reference's own unit test pins advanceToY to the banded state), then
+// rasterized in banding mode for the window's rows. Cells left of the window are summed into a
+// per-row backdrop (the coverage carried in from the left), cells right of it are dropped. All sums
+// are modular u32, so the per-window partial sums equal the reference's band sums.
 #pragma once
 
 #include "blgpu_internal.h"
@@ -24,9 +24,9 @@ struct State {
   uint32_t flags;
 };
 
-// Destination of cell contributions for one tile: shared-memory cells [kTileH][kTileW] plus a
-// per-row backdrop that receives every contribution left of the tile.
-struct TileSink {
+// Destination of cell contributions for one window of `kWindowRows` rows x kTileW columns:
+// shared-memory cells plus a per-row backdrop that receives every contribution left of it.
+struct WindowSink {
   uint32_t* cells;
   uint32_t* backdrop;
   int tx0;
@@ -165,7 +165,7 @@ __device__ void advance_to_y(State& s, int y_target) {
 }
 
 // rasterize<kOptionBandOffset | kOptionBandingMode> for the band [band_offset, band_end].
-__device__ void rasterize(State& s, uint32_t sm, uint32_t band_offset, uint32_t band_end, TileSink& cs) {
+__device__ void rasterize(State& s, uint32_t sm, uint32_t band_offset, uint32_t band_end, WindowSink& cs) {
   auto SM = [sm](uint32_t v) -> uint32_t { return (v ^ sm) - sm; };
   int ey1_end = min(s.ey1, int(band_end));
   uint32_t i = unsigned(ey1_end) - unsigned(s.ey0);
@@ -536,13 +536,14 @@ HLTRInside:
   }
 }
 
-// All cells of one segment for the tile rows [row0, row0 + kTileH) (clipped to `last_row`).
-// Segments entirely left of the tile only add their per-row cover (cells sum to cover << 9 per
+// All cells of one segment for the window rows [row0, row0 + rows) (clipped to `last_row`).
+// Segments entirely left of the window only add their per-row cover (cells sum to cover << 9 per
 // row, analyticrasterizer_p.h:1203-1211); segments right of it contribute nothing.
-__device__ __forceinline__ void segment_to_tile(const DevSeg& g, uint32_t sign, int row0, int last_row, TileSink& cs) {
+__device__ __forceinline__ void segment_to_window(const DevSeg& g, uint32_t sign, int row0, int rows, int last_row,
+                                                  WindowSink& cs) {
   int ey0 = g.y0 >> 8;
   int ey1 = (g.y1 - 1) >> 8;
-  int band_end = min(row0 + kTileH - 1, last_row);
+  int band_end = min(row0 + rows - 1, last_row);
   if (ey1 < row0 || ey0 > band_end) return;
   int min_x = min(g.x0, g.x1) >> 8;
   if (min_x >= cs.tx0 + kTileW) return;

@@ -153,6 +153,7 @@ void Runtime::destroy() {
   for (auto& e : ev) if (e) cudaEventDestroy(e);
   in_buf.release();
   dyn_buf.release();
+  seg_buf.release();
   if (host_staging) cudaFreeHost(host_staging);
   if (host_totals) cudaFreeHost(host_totals);
   if (own_stream && stream) cudaStreamDestroy(stream);
@@ -167,6 +168,9 @@ static bool device_target_direct(const BLGpuImage& im) {
 BLGpuResult Runtime::upload(const Frame& fr) {
   const uint32_t nc = uint32_t(fr.cmds.size());
   const uint32_t ncv = uint32_t(fr.canvases.size());
+
+  // Curves/lines of unclipped commands: at most one per vertex plus one closing line per figure.
+  const uint32_t item_capacity = uint32_t(std::min<size_t>(fr.verts.size() + 1, 0xFFFFFFF0u));
 
   // Plan: [staged inputs][luts][canvases][work arrays]
   auto plan = [&](Layout& L, FrameView& v, std::vector<uint32_t*>* cpix) -> size_t {
@@ -189,11 +193,13 @@ BLGpuResult Runtime::upload(const Frame& fr) {
       else p = L.take<uint32_t>(size_t(align_up(uint32_t(im.width), 4)) * uint32_t(im.height));
       if (cpix) (*cpix)[i] = p;
     }
-    v.seg_counts = L.take<uint32_t>(nc);
-    v.seg_rows = L.take<uint32_t>(nc);
-    seg_offsets = L.take<uint32_t>(nc + 1);
+    v.items = L.take<DevItem>(item_capacity);
+    v.seq_cmds = L.take<uint32_t>(nc);
+    v.cmd_bbox = L.take<int4>(nc);
     v.cmd_tile_x = L.take<uint32_t>(nc);
     v.cmd_tile_y = L.take<uint32_t>(nc);
+    v.cmd_xr = L.take<uint32_t>(nc);
+    v.cmd_yr = L.take<uint32_t>(nc);
     cmdrow_per_cmd = L.take<uint32_t>(nc + 1);
     v.cmdrow_base = L.take<uint32_t>(nc + 1);
     v.row_counts = L.take<uint32_t>(fr.rows + 1);
@@ -284,6 +290,19 @@ BLGpuResult Runtime::upload(const Frame& fr) {
                                   dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
   }
 
+  // Segment array: kept across frames, sized from the vertex count at first and from the actual
+  // count whenever a frame overflows it (run() then repeats the counting half).
+  size_t want_segs = std::max<size_t>(size_t(seg_capacity), fr.verts.size() * 2 + 65536);
+  want_segs = std::min<size_t>(want_segs, 0xFFFFFFF0u);
+  if (want_segs > seg_capacity) {
+    graph_valid = false;
+    BLGpuResult rr = reserve_segments(uint32_t(want_segs));
+    if (rr) return rr;
+  }
+  v.segs = static_cast<DevSeg*>(seg_buf.ptr);
+  v.seg_meta = reinterpret_cast<uint32_t*>(static_cast<char*>(seg_buf.ptr) + sizeof(DevSeg) * size_t(seg_capacity));
+  v.seg_capacity = seg_capacity;
+  v.item_capacity = item_capacity;
   v.num_cmds = nc;
   v.num_canvases = ncv;
   v.num_tiles = fr.tiles;
@@ -295,17 +314,21 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   return BLGPU_SUCCESS;
 }
 
-// Counting half: LUTs, edge counts + bboxes, tile ranges, row-list sizes, totals.
+BLGpuResult Runtime::reserve_segments(uint32_t count) {
+  BLGPU_CHECK(cudaStreamSynchronize(stream));
+  BLGPU_CHECK(seg_buf.reserve(size_t(count) * (sizeof(DevSeg) + sizeof(uint32_t))));
+  seg_capacity = uint32_t(std::min<size_t>(seg_buf.size / (sizeof(DevSeg) + sizeof(uint32_t)), 0xFFFFFFF0u));
+  return BLGPU_SUCCESS;
+}
+
+// Counting half: LUTs, edge building (segments appended), tile ranges, row-list sizes, totals.
 int Runtime::enqueue_count_half(cudaStream_t st) {
   const FrameView& f = view;
   int k = 0;
   cudaMemsetAsync(f.work_counter, 0, sizeof(uint32_t) * 16, st);
   cudaMemsetAsync(f.row_counts, 0, sizeof(uint32_t) * (f.num_rows + 1), st);
   k += launch_lut(f, st);
-  k += launch_edge_count(f, st);
-  k += exclusive_scan(f.seg_counts, seg_offsets, f.num_cmds, scan_tmp, st);
-  k += launch_total(f.seg_counts, seg_offsets, f.num_cmds, f.totals + 0, st);
-  k += launch_sum(f.seg_rows, f.num_cmds, f.totals + 1, st);
+  k += launch_edges(f, st);
   k += launch_cmd_tiles(f, cmdrow_per_cmd, st);
   k += exclusive_scan(cmdrow_per_cmd, f.cmdrow_base, f.num_cmds, scan_tmp, st);
   k += launch_total(cmdrow_per_cmd, f.cmdrow_base, f.num_cmds, f.totals + 2, st);
@@ -318,7 +341,6 @@ int Runtime::enqueue_count_half(cudaStream_t st) {
 int Runtime::enqueue_render_half(cudaStream_t st, bool timed) {
   const FrameView& f = view;
   int k = 0;
-  k += launch_edge_emit(f, seg_offsets, st);
   cudaMemsetAsync(f.cmdrow_counts, 0, sizeof(uint32_t) * (f.num_cmdrows + 1), st);
   cudaMemsetAsync(f.cmdrow_cursor, 0, sizeof(uint32_t) * (f.num_cmdrows + 1), st);
   k += launch_seg_bin(f, 0, st);
@@ -360,6 +382,21 @@ BLGpuResult Runtime::run(const Frame& fr) {
   BLGPU_CHECK(cudaMemcpyAsync(host_totals, view.totals, 16, cudaMemcpyDeviceToHost, stream));
   d2h_bytes += 16;
   BLGPU_CHECK(cudaStreamSynchronize(stream));
+  if (host_totals[0] > view.seg_capacity) {
+    // more segments than slots: grow and repeat the counting half (it is idempotent)
+    r = reserve_segments(uint32_t(std::min<uint64_t>(uint64_t(host_totals[0]) * 5 / 4 + 1024, 0xFFFFFFF0u)));
+    if (r) return r;
+    view.segs = static_cast<DevSeg*>(seg_buf.ptr);
+    view.seg_meta = reinterpret_cast<uint32_t*>(static_cast<char*>(seg_buf.ptr) + sizeof(DevSeg) * size_t(seg_capacity));
+    view.seg_capacity = seg_capacity;
+    BLGPU_CHECK(cudaEventRecord(ev[0], stream));
+    launches = enqueue_count_half(stream);
+    BLGPU_CHECK(cudaGetLastError());
+    BLGPU_CHECK(cudaMemcpyAsync(host_totals, view.totals, 16, cudaMemcpyDeviceToHost, stream));
+    d2h_bytes += 16;
+    BLGPU_CHECK(cudaStreamSynchronize(stream));
+    if (host_totals[0] > view.seg_capacity) return BLGPU_ERROR_OUT_OF_MEMORY;
+  }
   totals.segs = host_totals[0];
   totals.seglist = host_totals[1];
   totals.cmdrows = host_totals[2];
@@ -367,8 +404,6 @@ BLGpuResult Runtime::run(const Frame& fr) {
 
   // Dynamic buffers.
   auto plan = [&](Layout& L) {
-    view.segs = L.take<DevSeg>(totals.segs);
-    view.seg_meta = L.take<uint32_t>(totals.segs);
     view.cmdrow_counts = L.take<uint32_t>(totals.cmdrows + 1);
     view.cmdrow_offsets = L.take<uint32_t>(totals.cmdrows + 1 + scan_temp_words(totals.cmdrows + 1));
     view.cmdrow_cursor = L.take<uint32_t>(totals.cmdrows + 1);

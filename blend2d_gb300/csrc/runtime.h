@@ -70,7 +70,9 @@ struct Runtime {
   int sm_count = 0;
 
   DeviceBuffer in_buf;      // uploaded frame data + canvases + fixed-size work arrays
-  DeviceBuffer dyn_buf;     // sizes known after the counting pass (segments, lists)
+  DeviceBuffer dyn_buf;     // sizes known after the counting pass (segment and command lists)
+  DeviceBuffer seg_buf;     // segments + their metadata, appended by the edge builders
+  uint32_t seg_capacity = 0;
   void* host_staging = nullptr;
   size_t host_staging_size = 0;
   uint32_t* host_totals = nullptr;   // pinned
@@ -85,7 +87,6 @@ struct Runtime {
   std::vector<FrameTarget> targets;
   std::vector<uint32_t*> canvas_dev;   // device pixels per canvas
   std::vector<int32_t> canvas_stride;  // device stride in pixels
-  uint32_t* seg_offsets = nullptr;
   uint32_t* cmdrow_per_cmd = nullptr;
   uint32_t* row_canvas = nullptr;
   uint32_t* scan_tmp = nullptr;
@@ -107,6 +108,7 @@ struct Runtime {
   int enqueue_render_half(cudaStream_t st, bool timed);
   BLGpuResult upload(const Frame& fr);
   BLGpuResult download();
+  BLGpuResult reserve_segments(uint32_t count);
   void read_pixel_ops();
 };
 
