@@ -101,7 +101,7 @@ struct alignas(16) DevCmd {
   int32_t box[4];          // BoxA: pixels; BoxU: 24.8; analytic: pixel bbox written by K1
   uint32_t seg_first;      // K1 output
   uint32_t seg_count;
-  uint32_t status;         // 0 ok, 1 invalid geometry (NaN), 2 nothing to render
+  uint32_t status;         // after binning: 0 ok, 1 invalid geometry (NaN), 2 nothing to render
   uint32_t pad;
 };
 
@@ -135,10 +135,10 @@ struct DevSeg {            // one non-horizontal 24.8 segment, y0 < y1
   int32_t x0, y0, x1, y1;
 };
 
-enum ItemKind : uint32_t { kItemLine = 0, kItemQuad = 1, kItemCubic = 2, kItemConic = 3 };
+enum ItemKind : uint32_t { kItemLine = 0, kItemQuad = 1, kItemCubic = 2, kItemConic = 3, kItemWhole = 4 };
 
-// One curve or line of an analytic command whose vertices all lie inside the clip box (built
-// independently of the command's other curves). Vertex indices are relative to geom_first.
+// One line, curve or closing line of an analytic command, built independently of the command's
+// other items. Vertex indices are relative to geom_first.
 struct DevItem {
   uint32_t cmd;
   uint32_t kind;           // ItemKind
@@ -161,8 +161,7 @@ struct FrameView {
   const uint32_t* images;
   uint32_t* pixels;
   // K1
-  DevItem* items;              // curves/lines of unclipped commands (any order)
-  uint32_t* seq_cmds;          // commands that need the sequential (clipping) builder
+  DevItem* items;              // lines and curves of every analytic command (any order)
   int4* cmd_bbox;              // [num_cmds] 24.8 bbox of the emitted segments: xmin, ymin, xmax, ymax
   DevSeg* segs;                // emitted segments (any order)
   uint32_t* seg_meta;          // cmd << 1 | sign
@@ -183,7 +182,7 @@ struct FrameView {
   uint32_t* row_cmds;          // command indices grouped by tile row, painter's order
   uint32_t* tile_order;        // tile processing order for the persistent fine kernel
   uint32_t* tile_canvas;       // canvas index per global tile
-  uint32_t* work_counter;      // [0] fine work queue, [1] items, [2] sequential commands
+  uint32_t* work_counter;      // [0] fine work queue, [1] items
   uint32_t* totals;            // [4] segments, seglist bound, (cmd,row) slots, row entries
   uint32_t* error_flags;
   unsigned long long* pixel_ops;   // [2] composited pixels (mask != 0), of which pattern-fetched

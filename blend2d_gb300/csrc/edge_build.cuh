@@ -956,29 +956,5 @@ LineTo:
   return 0;
 }
 
-// One curve of a path whose every vertex lies inside the clip box: with no clipping the
-// builder's output for a curve depends only on its own control points (the previous curve ends
-// exactly at this one's first point), so each curve can be built independently. Same split and
-// safe flattening as curve_to's inside branch.
-template<int DEG>
-__device__ void inside_curve(Builder& eb, Pt* spline) {
-  Mono<DEG> mc;
-  mc.tol_sq = eb.tol_sq;
-  int nout = DEG == 3 ? split_cubic(spline) : split_quad(spline);
-  if (nout == 0) nout = DEG;
-  for (int k = 0; k < nout; k += DEG) {
-    const Pt* sp = spline + k;
-    uint32_t sign = sp[0].y > sp[DEG].y;
-    flatten_safe<DEG>(eb, mc, sp, sign);
-  }
-}
-
-// One line of such a path: the polyline step between two truncated vertices.
-__device__ __forceinline__ void inside_line(Builder& eb, Pt a, Pt b) {
-  int x0 = trunc_i(a.x), y0 = trunc_i(a.y), x1 = trunc_i(b.x), y1 = trunc_i(b.y);
-  if (y0 < y1) eb.sink.emit(x0, y0, x1, y1, 0u);
-  else if (y0 > y1) eb.sink.emit(x1, y1, x0, y0, 1u);
-}
-
 }  // namespace eb
 }  // namespace blgpu

@@ -239,26 +239,19 @@ __global__ void lut_kernel(const DevLutJob* jobs, const DevStop* stops, uint32_t
 }
 
 // ---------------------------------------------------------------------------------------------
-// K1 - FP64 edge building. `classify` looks at every analytic command: if all its transformed
-// vertices are finite and inside the clip box, no clipping can occur and each curve/line of it is
-// an independent item (built one per thread by `edge_items`); otherwise the whole command goes to
-// `edge_sequential`, one thread running the reference's builder with its clipping state machine.
-// Both append segments to one array with batched atomics.
+// K1 - FP64 edge building. The reference's builder walks a command's figures sequentially, but
+// the cells it produces depend only on the multiset of segments, and the segments of one line or
+// curve depend only on that line's or curve's own points: clipping decisions come from the
+// points' clip flags, the previous curve ends exactly on this one's first point, and the
+// left/right border runs it accumulates are vertical lines at the clip box's x0/x1, whose cells
+// add up the same whether consecutive runs are merged or not. So `classify` splits every
+// analytic command into items (lines, curves, closing lines) and `edge_items` builds each item
+// on its own thread with the reference's clipping builder, appending segments with batched
+// atomics. An invalid point (NaN) makes the reference reject the whole command; here it marks the
+// command invalid and binning drops it.
 // ---------------------------------------------------------------------------------------------
 
-struct Xf {
-  double m00, m01, m10, m11, m20, m21;
-  bool affine;
-  __device__ __forceinline__ eb::Pt map(const double* xy) const {
-    double x = xy[0], y = xy[1];
-    if (affine) return eb::Pt{x * m00 + y * m10 + m20, x * m01 + y * m11 + m21};
-    return eb::Pt{x * m00 + m20, y * m11 + m21};
-  }
-};
-
-__device__ __forceinline__ Xf load_xf(const DevXform& x) {
-  return Xf{x.m[0], x.m[1], x.m[2], x.m[3], x.m[4], x.m[5], x.affine != 0};
-}
+enum : uint32_t { kCmdHasSegments = 1u, kCmdInvalid = 2u };
 
 __device__ __forceinline__ void init_builder(eb::Builder& b, const DevCanvas& cv) {
   b.cx0 = 0.0; b.cy0 = 0.0; b.cx1 = double(cv.w) * 256.0; b.cy1 = double(cv.h) * 256.0;
@@ -295,22 +288,26 @@ __global__ void classify_kernel(FrameView f) {
   const DevCmd cmd = f.cmds[c];
   if (cmd.kind != kFillAnalytic) return;
   f.cmd_bbox[c] = make_int4(INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN);
-  f.cmds_rw[c].status = 2u;
-  const DevCanvas cv = f.canvases[cmd.canvas];
-  const Xf xf = load_xf(f.xforms[cmd.xform]);
-  const double* xy = f.verts + 2ull * cmd.geom_first;
+  f.cmds_rw[c].status = 0u;
   const uint8_t* pc = cmd.geom == kGeomPath ? f.path_cmds + cmd.geom_first : nullptr;
   const int n = int(cmd.geom_count);
-  const double cx1 = double(cv.w) * 256.0, cy1 = double(cv.h) * 256.0;
-  bool inside = true;
-  for (int k = 0; k < n && inside; k++) {
-    eb::Pt p = xf.map(xy + 2 * k);
-    inside = (p.x >= 0.0) & (p.x <= cx1) & (p.y >= 0.0) & (p.y <= cy1);   // false for NaN too
-  }
-  if (!inside) {
-    uint32_t idx = atomicAdd(f.work_counter + 2, 1u);
-    f.seq_cmds[idx] = c;
-    return;
+  // A command with a non-finite transformed point is built whole, by one thread, exactly as the
+  // reference builds it (its clip flags then depend on the order points are visited in).
+  {
+    const DevXform xf = f.xforms[cmd.xform];
+    const double* xy = f.verts + 2ull * cmd.geom_first;
+    bool finite = true;
+    for (int k = 0; k < n; k++) {
+      double x = xy[2 * k], y = xy[2 * k + 1], tx, ty;
+      if (xf.affine) { tx = x * xf.m[0] + y * xf.m[2] + xf.m[4]; ty = x * xf.m[1] + y * xf.m[3] + xf.m[5]; }
+      else { tx = x * xf.m[0] + xf.m[4]; ty = y * xf.m[3] + xf.m[5]; }
+      finite &= isfinite(tx) & isfinite(ty);
+    }
+    if (!finite) {
+      uint32_t base = atomicAdd(f.work_counter + 1, 1u);
+      if (base < f.item_capacity) f.items[base] = DevItem{c, kItemWhole, 0u, 0u};
+      return;
+    }
   }
   uint32_t count = 0;
   for_each_item(pc, n, [&](uint32_t, int, int) { count++; });
@@ -321,39 +318,6 @@ __global__ void classify_kernel(FrameView f) {
   });
 }
 
-__global__ void edge_sequential_kernel(FrameView f) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t rows = 0;
-  if (t < f.work_counter[2]) {
-    const uint32_t c = f.seq_cmds[t];
-    const DevCmd cmd = f.cmds[c];
-    const DevCanvas cv = f.canvases[cmd.canvas];
-    const DevXform xf = f.xforms[cmd.xform];
-    eb::Builder b;
-    init_builder(b, cv);
-    b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, c);
-    eb::Src src;
-    src.xy = f.verts + 2ull * cmd.geom_first;
-    src.cmd = cmd.geom == kGeomPath ? f.path_cmds + cmd.geom_first : nullptr;
-    src.i = 0;
-    src.n = int(cmd.geom_count);
-    src.affine = xf.affine != 0;
-    src.m00 = xf.m[0]; src.m01 = xf.m[1]; src.m10 = xf.m[2]; src.m11 = xf.m[3]; src.m20 = xf.m[4]; src.m21 = xf.m[5];
-    int rc = eb::build(b, src);
-    // An invalid geometry (NaN) aborts the whole command in the reference (the edge builder is
-    // reverted, rastercontextops.cpp:23-28): segments already appended are orphaned (the status
-    // keeps the command out of binning).
-    if (rc == 0) b.sink.flush();
-    f.cmds_rw[c].status = rc ? 1u : (b.sink.n ? 0u : 2u);
-    if (rc == 0 && b.sink.n) {
-      f.cmd_bbox[c] = make_int4(b.sink.xmin, b.sink.ymin, b.sink.xmax, b.sink.ymax);
-      rows = b.sink.rows;
-    }
-  }
-  rows = __reduce_add_sync(0xFFFFFFFFu, rows);
-  if ((threadIdx.x & 31) == 0 && rows) atomicAdd(f.totals + 1, rows);
-}
-
 __global__ void edge_items_kernel(FrameView f) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t rows = 0;
@@ -362,39 +326,50 @@ __global__ void edge_items_kernel(FrameView f) {
     const DevItem it = f.items[t];
     const DevCmd cmd = f.cmds[it.cmd];
     const DevCanvas cv = f.canvases[cmd.canvas];
-    const Xf xf = load_xf(f.xforms[cmd.xform]);
-    const double* xy = f.verts + 2ull * cmd.geom_first;
+    const DevXform xf = f.xforms[cmd.xform];
     eb::Builder b;
     init_builder(b, cv);
     b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, it.cmd);
-    eb::Pt spline[25];
-    spline[0] = xf.map(xy + 2 * it.a);
-    switch (it.kind) {
-      case kItemLine:
-        eb::inside_line(b, spline[0], xf.map(xy + 2 * it.b));
-        break;
-      case kItemQuad:
-        spline[1] = xf.map(xy + 2 * it.b); spline[2] = xf.map(xy + 2 * (it.b + 1));
-        eb::inside_curve<2>(b, spline);
-        break;
-      case kItemConic:
-        spline[1] = xf.map(xy + 2 * it.b); spline[2] = xf.map(xy + 2 * (it.b + 2));
-        eb::inside_curve<2>(b, spline);
-        break;
-      default:
-        spline[1] = xf.map(xy + 2 * it.b); spline[2] = xf.map(xy + 2 * (it.b + 1)); spline[3] = xf.map(xy + 2 * (it.b + 2));
-        eb::inside_curve<3>(b, spline);
-        break;
+    eb::Src src;
+    src.xy = f.verts + 2ull * cmd.geom_first;
+    src.cmd = cmd.geom == kGeomPath ? f.path_cmds + cmd.geom_first : nullptr;
+    src.affine = xf.affine != 0;
+    src.m00 = xf.m[0]; src.m01 = xf.m[1]; src.m10 = xf.m[2]; src.m11 = xf.m[3]; src.m20 = xf.m[4]; src.m21 = xf.m[5];
+    eb::Pt a = src.tf(int(it.a));
+    uint32_t a_flags = b.fxy(a);
+    int rc = 0;
+    if (it.kind == kItemWhole) {
+      src.i = 0;
+      src.n = int(cmd.geom_count);
+      rc = eb::build(b, src);                  // includes done()
     }
-    b.sink.flush();
-    if (b.sink.n) {
-      int4* bb = f.cmd_bbox + it.cmd;
-      atomicMin(&bb->x, b.sink.xmin);
-      atomicMin(&bb->y, b.sink.ymin);
-      atomicMax(&bb->z, b.sink.xmax);
-      atomicMax(&bb->w, b.sink.ymax);
-      f.cmds_rw[it.cmd].status = 0u;
-      rows = b.sink.rows;
+    else if (it.kind == kItemLine) {
+      src.i = src.n = 0;                       // no further lines: line_to builds exactly this one
+      rc = eb::line_to(b, src, a, a_flags, src.tf(int(it.b)));
+    }
+    else {
+      // the source ends right after this curve, so curve_to consumes exactly one
+      src.i = int(it.b);
+      src.n = int(it.b) + (it.kind == kItemQuad ? 2 : 3);
+      if (it.kind == kItemCubic) eb::curve_to<3>(b, src, a, a_flags, false);
+      else eb::curve_to<2>(b, src, a, a_flags, it.kind == kItemConic);
+    }
+    uint32_t* status = &f.cmds_rw[it.cmd].status;
+    if (rc) {
+      atomicOr(status, kCmdInvalid);
+    }
+    else {
+      if (it.kind != kItemWhole) b.done();
+      b.sink.flush();
+      if (b.sink.n) {
+        int4* bb = f.cmd_bbox + it.cmd;
+        atomicMin(&bb->x, b.sink.xmin);
+        atomicMin(&bb->y, b.sink.ymin);
+        atomicMax(&bb->z, b.sink.xmax);
+        atomicMax(&bb->w, b.sink.ymax);
+        atomicOr(status, kCmdHasSegments);
+        rows = b.sink.rows;
+      }
     }
   }
   rows = __reduce_add_sync(0xFFFFFFFFu, rows);
@@ -471,7 +446,9 @@ __global__ void cmd_tiles_kernel(FrameView f, uint32_t* cmdrow_counts_per_cmd, u
   bool empty = false;
   if (cmd.kind == kFillAnalytic) {
     // pixel bbox of the coverage: rows [ymin >> 8, (ymax - 1) >> 8], columns [xmin >> 8, xmax >> 8]
-    empty = cmd.status != 0;
+    const uint32_t st = cmd.status;
+    empty = (st & kCmdInvalid) || !(st & kCmdHasSegments);
+    f.cmds_rw[c].status = (st & kCmdInvalid) ? 1u : (empty ? 2u : 0u);
     const int4 bb = f.cmd_bbox[c];
     x0 = max(bb.x >> 8, 0); y0 = max(bb.y >> 8, 0);
     x1 = min(bb.z >> 8, cv.w - 1); y1 = min((bb.w - 1) >> 8, cv.h - 1);
@@ -678,13 +655,16 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
           const bool src_copy = (cmd.flags & 1u) != 0;
           px::RowState rs = px::row_state(st, y, fetch_y0);
           uint32_t n = 0;
-#pragma unroll
+          // one copy of the fetch + composite code: the 4 pixels rotate through slot 0
+#pragma unroll 1
           for (int k = 0; k < 4; k++) {
-            if (m[k] && xp + k < cv.w) {
+            if (m[0] && xp + k < cv.w) {
               uint32_t sv = px::fetch(st, rs, xp + k, f.luts, f.images);
-              pix[k] = px::composite(pix[k], sv, m[k], src_copy);
+              pix[0] = px::composite(pix[0], sv, m[0], src_copy);
               n++;
             }
+            uint32_t tp = pix[0]; pix[0] = pix[1]; pix[1] = pix[2]; pix[2] = pix[3]; pix[3] = tp;
+            uint32_t tm = m[0]; m[0] = m[1]; m[1] = m[2]; m[2] = m[3]; m[3] = tm;
           }
           ops += n;
           pat_ops += st.fetch >= kFetchPatAlignedPad ? n : 0u;
@@ -795,9 +775,8 @@ int launch_lut(const FrameView& f, cudaStream_t st) {
 int launch_edges(const FrameView& f, cudaStream_t st) {
   if (!f.num_cmds) return 0;
   classify_kernel<<<cdiv(f.num_cmds, 128), 128, 0, st>>>(f);
-  edge_sequential_kernel<<<cdiv(f.num_cmds, 64), 64, 0, st>>>(f);
   edge_items_kernel<<<cdiv(f.item_capacity ? f.item_capacity : 1, 128), 128, 0, st>>>(f);
-  return 3;
+  return 2;
 }
 
 int launch_cmd_tiles(const FrameView& f, uint32_t* cmdrow_counts_per_cmd, cudaStream_t st) {

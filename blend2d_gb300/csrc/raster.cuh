@@ -53,11 +53,21 @@ __device__ __forceinline__ void acc_step_u(uint32_t& acc, int& iter, int step, i
   acc -= uint32_t(m);
   iter += m & corr;
 }
+// 64-by-32-bit unsigned division with a 32-bit fast path (the common case: short segments).
+__device__ __forceinline__ uint64_t udiv64(uint64_t n, uint32_t d) {
+  if ((n >> 32) == 0) return uint32_t(n) / d;
+  return n / d;
+}
+__device__ __forceinline__ uint64_t umod64(uint64_t n, uint32_t d) {
+  if ((n >> 32) == 0) return uint32_t(n) % d;
+  return n % d;
+}
+
 __device__ __forceinline__ void acc_multi_step(int& acc, int& iter, int step, int corr, int count) {
   int64_t i = int64_t(uint32_t(iter));
   i -= int64_t(uint64_t(uint32_t(step)) * uint32_t(count));
   if (i < 0) {
-    int n = int((uint64_t(-i) + uint32_t(corr) - 1u) / uint64_t(uint32_t(corr)));
+    int n = int(udiv64(uint64_t(-i) + uint32_t(corr) - 1u, uint32_t(corr)));
     acc += n;
     i += int64_t(corr) * n;
   }
@@ -78,21 +88,21 @@ __device__ bool prepare(State& s, int x0, int y0, int x1, int y1) {
   if (s.ex0 == s.ex1 && (s.ey0 == s.ey1 || s.dx == 0)) { s.flags |= kVertOrSingle; return true; }
   uint64_t xb = uint64_t(uint32_t(s.dx)) * 256u;
   uint64_t yb = uint64_t(uint32_t(s.dy)) * 256u;
-  s.xLift = int(xb / unsigned(s.dy)); s.xRem = int(xb % unsigned(s.dy));
-  s.yLift = int(yb / unsigned(s.dx)); s.yRem = int(yb % unsigned(s.dx));
+  s.xLift = int(udiv64(xb, unsigned(s.dy))); s.xRem = int(umod64(xb, unsigned(s.dy)));
+  s.yLift = int(udiv64(yb, unsigned(s.dx))); s.yRem = int(umod64(yb, unsigned(s.dx)));
   s.xDlt = s.dx; s.yDlt = s.dy;
   s.xErr = (s.dy >> 1) - 1;
   s.yErr = (s.dx >> 1) - 1;
   if (s.ey0 != s.ey1) {
     uint64_t p = uint64_t(256u - uint32_t(s.fy0)) * uint32_t(s.dx);
-    s.xDlt = int(p / unsigned(s.dy));
-    s.xErr -= int(p % unsigned(s.dy));
+    s.xDlt = int(udiv64(p, unsigned(s.dy)));
+    s.xErr -= int(umod64(p, unsigned(s.dy)));
     acc_step(s.xDlt, s.xErr, 0, s.dy);
   }
   if (s.ex0 != s.ex1) {
     uint64_t p = uint64_t((s.flags & kRTL) ? uint32_t(s.fx0) : 256u - uint32_t(s.fx0)) * uint32_t(s.dy);
-    s.yDlt = int(p / unsigned(s.dx));
-    s.yErr -= int(p % unsigned(s.dx));
+    s.yDlt = int(udiv64(p, unsigned(s.dx)));
+    s.yErr -= int(umod64(p, unsigned(s.dx)));
     acc_step(s.yDlt, s.yErr, 0, s.dx);
   }
   s.yDlt += s.fy0;

@@ -169,7 +169,8 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   const uint32_t nc = uint32_t(fr.cmds.size());
   const uint32_t ncv = uint32_t(fr.canvases.size());
 
-  // Curves/lines of unclipped commands: at most one per vertex plus one closing line per figure.
+  // Items: at most one per vertex (a line or curve consumes at least one; a closing line takes
+  // the place of the figure's move-to).
   const uint32_t item_capacity = uint32_t(std::min<size_t>(fr.verts.size() + 1, 0xFFFFFFF0u));
 
   // Plan: [staged inputs][luts][canvases][work arrays]
@@ -194,7 +195,6 @@ BLGpuResult Runtime::upload(const Frame& fr) {
       if (cpix) (*cpix)[i] = p;
     }
     v.items = L.take<DevItem>(item_capacity);
-    v.seq_cmds = L.take<uint32_t>(nc);
     v.cmd_bbox = L.take<int4>(nc);
     v.cmd_tile_x = L.take<uint32_t>(nc);
     v.cmd_tile_y = L.take<uint32_t>(nc);
