@@ -24,7 +24,9 @@ namespace blgpu {
 constexpr int kTileW = 32;          // tile width in pixels
 constexpr int kTileH = 32;          // tile height in pixels (also the rasterizer band)
 constexpr int kTileShift = 5;
-constexpr int kFineThreads = 256;   // 4 pixels per thread, 8 threads per tile row
+constexpr int kFineThreads = 256;   // 8 warps per block
+constexpr int kStripRows = 4;       // a strip (one warp: 32 lanes x 4 pixels) is 4 rows of a tile
+constexpr int kStripShift = 2;
 
 enum FillKind : uint32_t {
   kFillAnalytic = 0,   // edges -> analytic coverage (FillAnalytic_Base)
@@ -172,7 +174,7 @@ struct FrameView {
   uint32_t* cmd_tile_y;        // ty0 | ty1 << 16
   uint32_t* cmd_xr;            // pixel columns x0 | x1 << 16 (inclusive; x0 > x1 = nothing)
   uint32_t* cmd_yr;            // pixel rows y0 | y1 << 16
-  uint32_t* cmdrow_base;       // [num_cmds + 1]: first (cmd,row) slot
+  uint32_t* cmdrow_base;       // [num_cmds + 1]: first (cmd, strip row) slot
   uint32_t* cmdrow_counts;     // [num_cmdrows + 1]
   uint32_t* cmdrow_offsets;    // exclusive scan of counts
   uint32_t* cmdrow_cursor;

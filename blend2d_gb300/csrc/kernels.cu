@@ -479,7 +479,8 @@ __global__ void cmd_tiles_kernel(FrameView f, uint32_t* cmdrow_counts_per_cmd, u
   uint32_t ty0 = uint32_t(y0) >> kTileShift, ty1 = uint32_t(y1) >> kTileShift;
   f.cmd_tile_x[c] = tx0 | (tx1 << 16);
   f.cmd_tile_y[c] = ty0 | (ty1 << 16);
-  cmdrow_counts_per_cmd[c] = cmd.kind == kFillAnalytic ? (ty1 - ty0 + 1u) : 0u;
+  // segment lists are kept per (command, strip row)
+  cmdrow_counts_per_cmd[c] = cmd.kind == kFillAnalytic ? ((uint32_t(y1) >> kStripShift) - (uint32_t(y0) >> kStripShift) + 1u) : 0u;
   for (uint32_t r = ty0; r <= ty1; r++) atomicAdd(&row_counts[cv.row_base + r], 1u);
 }
 
@@ -488,15 +489,15 @@ __global__ void seg_bin_kernel(FrameView f, int scatter) {
   uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= f.num_segs) return;
   uint32_t c = f.seg_meta[s] >> 1;
-  uint32_t ty = f.cmd_tile_y[c];
-  if (ty == 0xFFFFFFFFu) return;
-  int ty0 = int(ty & 0xFFFFu), ty1 = int(ty >> 16);
+  if (f.cmd_tile_y[c] == 0xFFFFFFFFu) return;
+  uint32_t yr = f.cmd_yr[c];
+  int sr0 = int((yr & 0xFFFFu) >> kStripShift), sr1 = int((yr >> 16) >> kStripShift);
   const DevSeg g = f.segs[s];
-  int r0 = max(int(uint32_t(g.y0 >> 8) >> kTileShift), ty0);
-  int r1 = min(int(uint32_t((g.y1 - 1) >> 8) >> kTileShift), ty1);
+  int r0 = max(int(uint32_t(g.y0 >> 8) >> kStripShift), sr0);
+  int r1 = min(int(uint32_t((g.y1 - 1) >> 8) >> kStripShift), sr1);
   uint32_t base = f.cmdrow_base[c];
   for (int r = r0; r <= r1; r++) {
-    uint32_t slot = base + uint32_t(r - ty0);
+    uint32_t slot = base + uint32_t(r - sr0);
     if (!scatter) atomicAdd(&f.cmdrow_counts[slot], 1u);
     else {
       uint32_t pos = atomicAdd(&f.cmdrow_cursor[slot], 1u);
@@ -529,18 +530,23 @@ __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
 // ---------------------------------------------------------------------------------------------
 // K3 - persistent fine kernel. The work unit is a strip of kStripRows x kTileW pixels (one warp,
 // 4 pixels per lane held in registers from one 128-bit load to one 128-bit store). Warps pull
-// strips from an atomic queue and never wait on each other: for every command of the strip's tile
-// row that overlaps the strip (painter's order) the warp rasterizes the command's segments of that
-// tile row into its own shared-memory cells, sweeps coverage with 8-lane shuffles, and composites.
+// strips from an atomic queue and never wait on each other. The commands of the strip's tile row
+// that overlap the strip are taken in painter's order, up to kGroup at a time: the lanes first
+// rasterize the segments of all analytic commands of the group together (each command into its
+// own shared-memory cell slot), then the group's commands are swept (8-lane shuffle prefix) and
+// composited one after the other.
 // ---------------------------------------------------------------------------------------------
 
-constexpr int kStripRows = 4;                       // rows per strip (32 lanes x 4 pixels)
 constexpr int kStripsPerTile = kTileH / kStripRows;
 constexpr int kFineWarps = kFineThreads / 32;
+constexpr int kGroup = 8;
 
 struct StripShared {
-  uint32_t cells[kStripRows * kTileW];
-  uint32_t backdrop[kStripRows];
+  uint32_t cells[kGroup][kStripRows * kTileW];
+  uint32_t backdrop[kGroup][kStripRows];
+  uint32_t cmd[kGroup];
+  uint32_t seg_first[kGroup];
+  uint32_t seg_excl[kGroup + 1];
 };
 
 __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
@@ -565,6 +571,7 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
     int x_base = tx * kTileW;
     int row0 = ty * kTileH + strip * kStripRows;
     if (row0 >= cv.h) continue;
+    const uint32_t strip_row = uint32_t(row0) >> kStripShift;
     int row1 = min(row0 + kStripRows, cv.h) - 1;     // last row of the strip inside the canvas
     int y = row0 + prow, xp = x_base + pcol;
     bool row_ok = y < cv.h;
@@ -584,7 +591,6 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
     uint32_t row_id = cv.row_base + uint32_t(ty);
     uint32_t list_first = f.row_offsets[row_id];
     uint32_t list_count = f.row_counts[row_id];
-    ras::WindowSink sink{ws.cells, ws.backdrop, x_base};
     const uint32_t strip_y = uint32_t(row0) | (uint32_t(row1) << 16);
     const uint32_t strip_x = uint32_t(x_base) | (uint32_t(min(x_base + kTileW, cv.w) - 1) << 16);
 
@@ -600,75 +606,112 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
       }
       uint32_t ballot = __ballot_sync(0xFFFFFFFFu, hit);
       while (ballot) {
-        int bit = __ffs(ballot) - 1;
-        ballot &= ballot - 1;
-        uint32_t ci = __shfl_sync(0xFFFFFFFFu, c, bit);
-        const DevCmd& cmd = f.cmds[ci];
-        const uint32_t kind = cmd.kind;
-        const uint32_t alpha = cmd.alpha;
-        uint32_t m[4] = {0u, 0u, 0u, 0u};
-        int fetch_y0 = cmd.fetch_y0;
-
-        if (kind == kFillAnalytic) {
-          *reinterpret_cast<uint4*>(&ws.cells[lane * 4]) = make_uint4(0u, 0u, 0u, 0u);
-          if (lane < kStripRows) ws.backdrop[lane] = 0u;
-          __syncwarp();
-          uint32_t ty0 = f.cmd_tile_y[ci] & 0xFFFFu;
-          uint32_t slot = f.cmdrow_base[ci] + uint32_t(ty) - ty0;
-          uint32_t s_first = f.cmdrow_offsets[slot];
-          uint32_t s_count = f.cmdrow_counts[slot];
-          for (uint32_t k = lane; k < s_count; k += 32) {
-            uint32_t si = f.seglist[s_first + k];
-            ras::segment_to_window(f.segs[si], f.seg_meta[si] & 1u, row0, kStripRows, cv.h - 1, sink);
+        // ---- next group: up to kGroup hit commands, in order
+        int ng = 0;
+        uint32_t gcmd = 0;                 // lane g < ng holds the group's g-th command
+        while (ballot && ng < kGroup) {
+          int bit = __ffs(ballot) - 1;
+          ballot &= ballot - 1;
+          uint32_t ci = __shfl_sync(0xFFFFFFFFu, c, bit);
+          if (lane == ng) gcmd = ci;
+          ng++;
+        }
+        // segment lists of the group's analytic commands for this strip row
+        uint32_t s_count = 0, s_first = 0;
+        if (lane < ng) {
+          const DevCmd& gc = f.cmds[gcmd];
+          if (gc.kind == kFillAnalytic) {
+            uint32_t slot = f.cmdrow_base[gcmd] + strip_row - ((f.cmd_yr[gcmd] & 0xFFFFu) >> kStripShift);
+            s_first = f.cmdrow_offsets[slot];
+            s_count = f.cmdrow_counts[slot];
           }
-          __syncwarp();
-          // coverage sweep: prefix over the row (8 lanes x 4 cells) + the carried-in backdrop
-          uint4 cv4 = *reinterpret_cast<const uint4*>(&ws.cells[lane * 4]);
-          uint32_t cl[4] = {cv4.x, cv4.y, cv4.z, cv4.w};
-          uint32_t s4 = cl[0] + cl[1] + cl[2] + cl[3];
-          uint32_t incl = s4;
-#pragma unroll
-          for (int o = 1; o < 8; o <<= 1) {
-            uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o, 8);
-            if ((lane & 7) >= o) incl += v;
-          }
-          uint32_t cov = (256u << 9) + ws.backdrop[prow] + incl - s4;
-          uint32_t rule = (cmd.flags & 2u) ? 0x1FFu : 0xFFFFFFFFu;
-#pragma unroll
-          for (int k = 0; k < 4; k++) { cov += cl[k]; m[k] = px::calc_mask(cov, rule, alpha); }
-          // the reference initializes its fetcher at the start of each band of the command
-          fetch_y0 = max(cmd.box[1], (y / cv.band_height) * cv.band_height);
-          __syncwarp();
         }
-        else if (kind == kFillBoxA) {
-          bool in_y = y >= cmd.box[1] && y < cmd.box[3];
+        uint32_t incl = s_count;
 #pragma unroll
-          for (int k = 0; k < 4; k++) m[k] = (in_y && xp + k >= cmd.box[0] && xp + k < cmd.box[2]) ? alpha : 0u;
+        for (int o = 1; o < kGroup; o <<= 1) {
+          uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+          if (lane >= o) incl += v;
         }
-        else {
-#pragma unroll
-          for (int k = 0; k < 4; k++) m[k] = px::box_u_mask(cmd.box, alpha, xp + k, y);
+        uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, kGroup - 1);
+        if (lane < kGroup) {
+          ws.cmd[lane] = gcmd;
+          ws.seg_first[lane] = s_first;
+          ws.seg_excl[lane] = incl - s_count;
         }
+        if (lane == 0) ws.seg_excl[kGroup] = total;
+        // zero the group's cell slots (each lane its own 4 cells) and backdrops
+        for (int g = 0; g < ng; g++)
+          *reinterpret_cast<uint4*>(&ws.cells[g][lane * 4]) = make_uint4(0u, 0u, 0u, 0u);
+        ws.backdrop[lane >> 2][lane & 3] = 0u;
+        __syncwarp();
 
-        if (row_ok && (m[0] | m[1] | m[2] | m[3])) {
-          const DevStyle& st = f.styles[cmd.style];
-          const bool src_copy = (cmd.flags & 1u) != 0;
-          px::RowState rs = px::row_state(st, y, fetch_y0);
-          uint32_t n = 0;
-          // one copy of the fetch + composite code: the 4 pixels rotate through slot 0
-#pragma unroll 1
-          for (int k = 0; k < 4; k++) {
-            if (m[0] && xp + k < cv.w) {
-              uint32_t sv = px::fetch(st, rs, xp + k, f.luts, f.images);
-              pix[0] = px::composite(pix[0], sv, m[0], src_copy);
-              n++;
+        // ---- rasterize every segment of the group, lanes spread over all of them
+        for (uint32_t idx = lane; idx < total; idx += 32) {
+          int g = 0;
+#pragma unroll
+          for (int k = 1; k < kGroup; k++) g += (k < ng && idx >= ws.seg_excl[k]) ? 1 : 0;
+          uint32_t si = f.seglist[ws.seg_first[g] + (idx - ws.seg_excl[g])];
+          ras::WindowSink sink{ws.cells[g], ws.backdrop[g], x_base};
+          ras::segment_to_window(f.segs[si], f.seg_meta[si] & 1u, row0, kStripRows, cv.h - 1, sink);
+        }
+        __syncwarp();
+
+        // ---- sweep + composite the group's commands in order
+        for (int g = 0; g < ng; g++) {
+          const uint32_t ci = ws.cmd[g];
+          const DevCmd& cmd = f.cmds[ci];
+          const uint32_t kind = cmd.kind;
+          const uint32_t alpha = cmd.alpha;
+          uint32_t m[4] = {0u, 0u, 0u, 0u};
+          int fetch_y0 = cmd.fetch_y0;
+          if (kind == kFillAnalytic) {
+            uint4 cv4 = *reinterpret_cast<const uint4*>(&ws.cells[g][lane * 4]);
+            uint32_t cl[4] = {cv4.x, cv4.y, cv4.z, cv4.w};
+            uint32_t s4 = cl[0] + cl[1] + cl[2] + cl[3];
+            uint32_t inc = s4;
+#pragma unroll
+            for (int o = 1; o < 8; o <<= 1) {
+              uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o, 8);
+              if ((lane & 7) >= o) inc += v;
             }
-            uint32_t tp = pix[0]; pix[0] = pix[1]; pix[1] = pix[2]; pix[2] = pix[3]; pix[3] = tp;
-            uint32_t tm = m[0]; m[0] = m[1]; m[1] = m[2]; m[2] = m[3]; m[3] = tm;
+            uint32_t cov = (256u << 9) + ws.backdrop[g][prow] + inc - s4;
+            uint32_t rule = (cmd.flags & 2u) ? 0x1FFu : 0xFFFFFFFFu;
+#pragma unroll
+            for (int k = 0; k < 4; k++) { cov += cl[k]; m[k] = px::calc_mask(cov, rule, alpha); }
+            // the reference initializes its fetcher at the start of each band of the command
+            fetch_y0 = max(cmd.box[1], (y / cv.band_height) * cv.band_height);
           }
-          ops += n;
-          pat_ops += st.fetch >= kFetchPatAlignedPad ? n : 0u;
+          else if (kind == kFillBoxA) {
+            bool in_y = y >= cmd.box[1] && y < cmd.box[3];
+#pragma unroll
+            for (int k = 0; k < 4; k++) m[k] = (in_y && xp + k >= cmd.box[0] && xp + k < cmd.box[2]) ? alpha : 0u;
+          }
+          else {
+#pragma unroll
+            for (int k = 0; k < 4; k++) m[k] = px::box_u_mask(cmd.box, alpha, xp + k, y);
+          }
+
+          if (row_ok && (m[0] | m[1] | m[2] | m[3])) {
+            const DevStyle& st = f.styles[cmd.style];
+            const bool src_copy = (cmd.flags & 1u) != 0;
+            px::RowState rs = px::row_state(st, y, fetch_y0);
+            uint32_t n = 0;
+            // one copy of the fetch + composite code: the 4 pixels rotate through slot 0
+#pragma unroll 1
+            for (int k = 0; k < 4; k++) {
+              if (m[0] && xp + k < cv.w) {
+                uint32_t sv = px::fetch(st, rs, xp + k, f.luts, f.images);
+                pix[0] = px::composite(pix[0], sv, m[0], src_copy);
+                n++;
+              }
+              uint32_t tp = pix[0]; pix[0] = pix[1]; pix[1] = pix[2]; pix[2] = pix[3]; pix[3] = tp;
+              uint32_t tm = m[0]; m[0] = m[1]; m[1] = m[2]; m[2] = m[3]; m[3] = tm;
+            }
+            ops += n;
+            pat_ops += st.fetch >= kFetchPatAlignedPad ? n : 0u;
+          }
         }
+        __syncwarp();
       }
     }
 

@@ -1,0 +1,96 @@
+"""Host-side logic of the continuous-batching server, with a fake renderer (no GPU): admission
+by footprint, FIFO batching, overlap across workers, per-request results and error delivery."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from blend2d_gb300 import scenes
+from blend2d_gb300.serving import RenderServer, footprint_bytes, percentile
+
+
+class FakeRuntime:
+    """Fills each target with a value derived from its stream; records concurrency."""
+    active = 0
+    max_active = 0
+    lock = threading.Lock()
+
+    def __init__(self, delay=0.02, fail_on=None):
+        self.delay = delay
+        self.fail_on = fail_on
+        self.batches = []
+
+    def render_batch(self, streams, targets):
+        with FakeRuntime.lock:
+            FakeRuntime.active += 1
+            FakeRuntime.max_active = max(FakeRuntime.max_active, FakeRuntime.active)
+        try:
+            self.batches.append(len(streams))
+            time.sleep(self.delay)
+            for s, t in zip(streams, targets):
+                if self.fail_on is not None and self.fail_on in s:
+                    raise RuntimeError("render failed")
+                t[...] = np.uint32(len(s) & 0xFFFFFFFF)
+        finally:
+            with FakeRuntime.lock:
+                FakeRuntime.active -= 1
+
+
+def _streams(n, seed=0):
+    return [scenes.random_mix(seed + i, width=16 + i, height=9 + 2 * i, count=3).to_bytes() for i in range(n)]
+
+
+def test_results_and_batching():
+    FakeRuntime.max_active = 0
+    rts = []
+
+    def factory():
+        rts.append(FakeRuntime())
+        return rts[-1]
+
+    streams = _streams(40)
+    with RenderServer(workers=2, runtime_factory=factory, max_batch=8) as srv:
+        futs = []
+        for s in streams:
+            futs.append(srv.submit(s))
+            time.sleep(0.001)
+        outs = [f.result(timeout=10) for f in futs]
+    for s, o in zip(streams, outs):
+        assert o.shape == (int.from_bytes(s[12:16], "little"), int.from_bytes(s[8:12], "little"))
+        assert o.dtype == np.uint32 and np.all(o == (len(s) & 0xFFFFFFFF))
+    assert srv.stats.completed == 40
+    assert max(srv.stats.batch_sizes) <= 8
+    assert srv.stats.batches < 40               # requests were batched
+    assert FakeRuntime.max_active == 2          # both workers ran at the same time
+    assert len(srv.stats.latencies) == 40 and percentile(srv.stats.latencies, 99) > 0
+
+
+def test_admission_respects_budget():
+    streams = _streams(12)
+    budget = max(footprint_bytes(s) for s in streams) * 2
+    with RenderServer(workers=3, hbm_budget=budget, runtime_factory=lambda: FakeRuntime(0.01)) as srv:
+        futs = [srv.submit(s) for s in streams]
+        for f in futs:
+            f.result(timeout=10)
+    assert srv.stats.max_inflight_bytes <= budget
+
+
+def test_oversized_request_rejected():
+    s = _streams(1)[0]
+    with RenderServer(workers=1, hbm_budget=footprint_bytes(s) - 1, runtime_factory=FakeRuntime) as srv:
+        with pytest.raises(MemoryError):
+            srv.submit(s).result(timeout=5)
+
+
+def test_errors_reach_every_request_of_the_batch():
+    streams = _streams(4)
+    marker = streams[2][-40:]
+    with RenderServer(workers=1, max_batch=8, runtime_factory=lambda: FakeRuntime(0.05, fail_on=marker)) as srv:
+        first = srv.submit(streams[0])          # dispatched alone while the others queue up
+        time.sleep(0.01)
+        rest = [srv.submit(s) for s in streams[1:]]
+        first.result(timeout=5)
+        for f in rest:
+            with pytest.raises(RuntimeError):
+                f.result(timeout=5)
