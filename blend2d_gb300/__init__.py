@@ -39,8 +39,8 @@ PATH_MOVE, PATH_ON, PATH_QUAD, PATH_CONIC, PATH_CUBIC, PATH_CLOSE = 0, 1, 2, 3, 
 
 
 class BLGpuError(RuntimeError):
-    def __init__(self, code: int, what: str = ""):
-        super().__init__(f"{what} failed with BLResult 0x{code:08x}")
+    def __init__(self, code: int, what: str = "", detail: str = ""):
+        super().__init__(f"{what} failed with BLResult 0x{code:08x}{detail}")
         self.code = code
 
 
@@ -73,7 +73,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("frames", ctypes.c_uint64), ("fill_commands", ctypes.c_uint64), ("segments", ctypes.c_uint64),
                 ("tiles", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("last_gpu_ms", ctypes.c_double),
                 ("last_fine_ms", ctypes.c_double), ("pixel_ops", ctypes.c_uint64), ("pattern_ops", ctypes.c_uint64),
-                ("input_vertices", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+                ("input_vertices", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
+                ("last_cuda_error", ctypes.c_int64)]
 
 
 _P = ctypes.c_void_p
@@ -134,9 +135,14 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         return _lib
 
 
-def _check(code: int, what: str):
+def _check(code: int, what: str, runtime=None):
     if code != SUCCESS:
-        raise BLGpuError(code, what)
+        detail = ""
+        if code == ERROR_DEVICE and runtime is not None:
+            st = Stats()
+            if _lib.blgpu_runtime_get_stats(runtime, ctypes.byref(st)) == SUCCESS:
+                detail = f" (cudaError {st.last_cuda_error})"
+        raise BLGpuError(code, what, detail)
 
 
 def _mat(m):
@@ -211,7 +217,7 @@ class Runtime:
             keep.append(k)
         ptrs = (ctypes.c_char_p * n)(*streams)
         sizes = (ctypes.c_size_t * n)(*[len(s) for s in streams])
-        _check(self._lib.blgpu_render_batch(self.handle, ptrs, sizes, imgs, n), "blgpu_render_batch")
+        _check(self._lib.blgpu_render_batch(self.handle, ptrs, sizes, imgs, n), "blgpu_render_batch", self.handle)
 
 
 class Context:
@@ -228,7 +234,7 @@ class Context:
             self.begin(target)
 
     def _call(self, name, *args):
-        _check(getattr(self._lib, name)(self.handle, *args), name)
+        _check(getattr(self._lib, name)(self.handle, *args), name, self.rt.handle)
 
     def begin(self, target):
         img, keep = make_image(target)

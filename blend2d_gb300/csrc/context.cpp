@@ -658,6 +658,7 @@ BLGPU_API BLGpuResult blgpu_runtime_destroy(BLGpuRuntime* rt) {
 BLGPU_API BLGpuResult blgpu_runtime_get_stats(const BLGpuRuntime* rt, BLGpuStats* out) {
   if (!rt || !out) return BLGPU_ERROR_INVALID_VALUE;
   *out = rt->rt.stats;
+  out->last_cuda_error = last_cuda_error();
   return BLGPU_SUCCESS;
 }
 

@@ -541,13 +541,16 @@ constexpr int kStripsPerTile = kTileH / kStripRows;
 constexpr int kFineWarps = kFineThreads / 32;
 constexpr int kGroup = 8;
 
-struct StripShared {
+// 16-byte aligned: each lane moves its 4 cells with one 128-bit shared-memory access, and the
+// per-warp structs sit back to back in one array.
+struct alignas(16) StripShared {
   uint32_t cells[kGroup][kStripRows * kTileW];
   uint32_t backdrop[kGroup][kStripRows];
   uint32_t cmd[kGroup];
   uint32_t seg_first[kGroup];
   uint32_t seg_excl[kGroup + 1];
 };
+static_assert(sizeof(StripShared) % 16 == 0, "per-warp shared state must keep 16-byte alignment");
 
 __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
   __shared__ StripShared sh[kFineWarps];

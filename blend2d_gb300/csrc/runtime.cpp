@@ -11,13 +11,17 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "launch.h"
 
 namespace blgpu {
 
+std::atomic<int> g_last_cuda_error{0};
+
 BLGpuResult cuda_result(cudaError_t e) {
   if (e == cudaSuccess) return BLGPU_SUCCESS;
+  g_last_cuda_error.store(int(e));
   if (e == cudaErrorMemoryAllocation) return BLGPU_ERROR_OUT_OF_MEMORY;
   return BLGPU_ERROR_DEVICE;
 }
@@ -27,6 +31,8 @@ BLGpuResult cuda_result(cudaError_t e) {
     cudaError_t e_ = (expr);                           \
     if (e_ != cudaSuccess) return cuda_result(e_);     \
   } while (0)
+
+int last_cuda_error() { return g_last_cuda_error.load(); }
 
 static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
 

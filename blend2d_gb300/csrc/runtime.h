@@ -113,5 +113,6 @@ struct Runtime {
 };
 
 BLGpuResult cuda_result(cudaError_t e);
+int last_cuda_error();
 
 }  // namespace blgpu

@@ -100,6 +100,7 @@ typedef struct BLGpuStats {
   uint64_t input_vertices; /* vertices of the last frame's polygon/path fills */
   uint64_t h2d_bytes;      /* host->device bytes of the last flush (frame data + canvas uploads) */
   uint64_t d2h_bytes;      /* device->host bytes of the last flush (canvas downloads + sizes) */
+  int64_t last_cuda_error; /* cudaError_t behind the last BLGPU_ERROR_DEVICE (0 if none) */
 } BLGpuStats;
 
 /* --- runtime (device, stream, memory) --------------------------------------------------- */
