@@ -31,8 +31,10 @@ def test_results_alone_equal_results_in_the_mix():
     rng = random.Random(5)
     with RenderServer(workers=3, max_batch=6, hbm_budget=2 << 30) as srv:
         futs = []
-        for s in reqs:
-            futs.append(srv.submit(s))
+        # bursts of arrivals: requests that arrive while earlier batches run are batched together
+        for k in range(0, len(reqs), 7):
+            for s in reqs[k:k + 7]:
+                futs.append(srv.submit(s))
             time.sleep(rng.uniform(0.0, 0.004))
         mixed = [f.result(timeout=120) for f in futs]
         stats = srv.stats
