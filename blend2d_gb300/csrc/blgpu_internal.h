@@ -174,18 +174,23 @@ struct FrameView {
   uint32_t* cmd_tile_y;        // ty0 | ty1 << 16
   uint32_t* cmd_xr;            // pixel columns x0 | x1 << 16 (inclusive; x0 > x1 = nothing)
   uint32_t* cmd_yr;            // pixel rows y0 | y1 << 16
-  uint32_t* cmdrow_base;       // [num_cmds + 1]: first (cmd, strip row) slot
+  uint32_t* cmdrow_base;       // [num_cmds + 1]: first (cmd, strip row, tile column) slot
   uint32_t* cmdrow_counts;     // [num_cmdrows + 1]
   uint32_t* cmdrow_offsets;    // exclusive scan of counts
   uint32_t* cmdrow_cursor;
-  uint32_t* seglist;           // segment indices grouped by (cmd,row)
+  uint32_t* seglist;           // segment indices grouped by (cmd, strip row, tile column)
+  uint32_t* backdrop;          // [num_cmdrows][kStripRows]: coverage carried into the slot's tile
+                               //   from segments entirely left of it (cover << 9 per row)
   uint32_t* row_counts;        // [num_rows + 1]
   uint32_t* row_offsets;
   uint32_t* row_cmds;          // command indices grouped by tile row, painter's order
   uint32_t* tile_order;        // tile processing order for the persistent fine kernel
   uint32_t* tile_canvas;       // canvas index per global tile
   uint32_t* work_counter;      // [0] fine work queue, [1] items
-  uint32_t* totals;            // [4] segments, seglist bound, (cmd,row) slots, row entries
+  uint32_t* totals;            // [8] segments, seglist bound, (cmd,strip) slots, row entries, gradient rows
+  uint32_t* rs_count;          // [num_cmds + 1] gradient row states per command (radial/conic styles)
+  uint32_t* rs_base;           // exclusive scan of rs_count
+  float4* row_states;          // per (command, row): the fetcher's row values f0, f1, f2
   uint32_t* error_flags;
   unsigned long long* pixel_ops;   // [2] composited pixels (mask != 0), of which pattern-fetched
   uint32_t num_cmds;
@@ -196,6 +201,7 @@ struct FrameView {
   uint32_t num_segs;
   uint32_t num_cmdrows;
   uint32_t num_seglist;
+  uint32_t num_row_states;
 };
 
 }  // namespace blgpu

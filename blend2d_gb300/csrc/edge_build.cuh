@@ -40,7 +40,7 @@ struct Sink {
   uint32_t capacity;    // slots in out/meta; the host re-runs with more when exceeded
   uint32_t cmd;
   uint32_t n;           // segments emitted by this builder
-  uint32_t rows;        // sum over segments of the strip rows each one spans (seglist size)
+  uint32_t rows;        // bound of the seglist entries of the emitted segments
   int ymin, ymax, xmin, xmax;
   int nb;
   DevSeg buf[kSinkBatch];
@@ -68,7 +68,9 @@ struct Sink {
     sbuf[nb] = sign;
     if (++nb == kSinkBatch) flush();
     n++;
-    rows += (uint32_t((y1 - 1) >> 8) >> kStripShift) - (uint32_t(y0 >> 8) >> kStripShift) + 1u;
+    // seglist entries: strip rows x tile columns the segment's cells touch (cells reach x + 1)
+    rows += ((uint32_t((y1 - 1) >> 8) >> kStripShift) - (uint32_t(y0 >> 8) >> kStripShift) + 1u) *
+            ((uint32_t(((max(x0, x1) >> 8) + 1)) >> kTileShift) - (uint32_t(min(x0, x1) >> 8) >> kTileShift) + 1u);
     ymin = min(ymin, y0);
     ymax = max(ymax, y1);
     xmin = min(xmin, min(x0, x1));

@@ -471,39 +471,88 @@ __global__ void cmd_tiles_kernel(FrameView f, uint32_t* cmdrow_counts_per_cmd, u
     f.cmd_xr[c] = 0x0000FFFFu;   // x0 = 65535 > x1 = 0: overlaps nothing
     f.cmd_yr[c] = 0x0000FFFFu;
     cmdrow_counts_per_cmd[c] = 0;
+    f.rs_count[c] = 0;
     return;
   }
+  f.rs_count[c] = px::has_row_table(f.styles[cmd.style].fetch) ? uint32_t(y1 - y0 + 1) : 0u;
   f.cmd_xr[c] = uint32_t(x0) | (uint32_t(x1) << 16);
   f.cmd_yr[c] = uint32_t(y0) | (uint32_t(y1) << 16);
   uint32_t tx0 = uint32_t(x0) >> kTileShift, tx1 = uint32_t(x1) >> kTileShift;
   uint32_t ty0 = uint32_t(y0) >> kTileShift, ty1 = uint32_t(y1) >> kTileShift;
   f.cmd_tile_x[c] = tx0 | (tx1 << 16);
   f.cmd_tile_y[c] = ty0 | (ty1 << 16);
-  // segment lists are kept per (command, strip row)
-  cmdrow_counts_per_cmd[c] = cmd.kind == kFillAnalytic ? ((uint32_t(y1) >> kStripShift) - (uint32_t(y0) >> kStripShift) + 1u) : 0u;
+  // segment lists are kept per (command, strip row, tile column)
+  cmdrow_counts_per_cmd[c] = cmd.kind == kFillAnalytic
+      ? ((uint32_t(y1) >> kStripShift) - (uint32_t(y0) >> kStripShift) + 1u) * (tx1 - tx0 + 1u) : 0u;
+
   for (uint32_t r = ty0; r <= ty1; r++) atomicAdd(&row_counts[cv.row_base + r], 1u);
 }
 
-// Segments per (command, tile row).
+// Segments per (command, strip row, tile column): a segment is listed in every tile its cells touch
+// (cells reach x + 1). Tiles entirely right of it get its per-row cover in their backdrop (the
+// count pass adds it once, at the first tile right of the segment; a prefix over tile columns
+// then carries it to all of them).
 __global__ void seg_bin_kernel(FrameView f, int scatter) {
   uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= f.num_segs) return;
   uint32_t c = f.seg_meta[s] >> 1;
-  if (f.cmd_tile_y[c] == 0xFFFFFFFFu) return;
-  uint32_t yr = f.cmd_yr[c];
-  int sr0 = int((yr & 0xFFFFu) >> kStripShift), sr1 = int((yr >> 16) >> kStripShift);
+  uint32_t ctx = f.cmd_tile_x[c];
+  if (ctx == 0xFFFFFFFFu) return;
+  const uint32_t sign = f.seg_meta[s] & 1u;
+  const int tx0 = int(ctx & 0xFFFFu), tx1 = int(ctx >> 16), ntx = tx1 - tx0 + 1;
+  const uint32_t yr = f.cmd_yr[c];
+  const int sr0 = int((yr & 0xFFFFu) >> kStripShift), sr1 = int((yr >> 16) >> kStripShift);
   const DevSeg g = f.segs[s];
-  int r0 = max(int(uint32_t(g.y0 >> 8) >> kStripShift), sr0);
-  int r1 = min(int(uint32_t((g.y1 - 1) >> 8) >> kStripShift), sr1);
-  uint32_t base = f.cmdrow_base[c];
+  const int ey0 = g.y0 >> 8, ey1 = (g.y1 - 1) >> 8;
+  const int r0 = max(ey0 >> kStripShift, sr0), r1 = min(ey1 >> kStripShift, sr1);
+  const int t0 = max((min(g.x0, g.x1) >> 8) >> kTileShift, tx0);
+  const int t_last = ((max(g.x0, g.x1) >> 8) + 1) >> kTileShift;
+  const int t1 = min(t_last, tx1);
+  const uint32_t base = f.cmdrow_base[c];
+  const uint32_t sm = 0u - sign;
   for (int r = r0; r <= r1; r++) {
-    uint32_t slot = base + uint32_t(r - sr0);
-    if (!scatter) atomicAdd(&f.cmdrow_counts[slot], 1u);
-    else {
-      uint32_t pos = atomicAdd(&f.cmdrow_cursor[slot], 1u);
-      f.seglist[f.cmdrow_offsets[slot] + pos] = s;
+    uint32_t row_slot = base + uint32_t(r - sr0) * uint32_t(ntx);
+    for (int t = t0; t <= t1; t++) {
+      uint32_t slot = row_slot + uint32_t(t - tx0);
+      if (!scatter) atomicAdd(&f.cmdrow_counts[slot], 1u);
+      else {
+        uint32_t pos = atomicAdd(&f.cmdrow_cursor[slot], 1u);
+        f.seglist[f.cmdrow_offsets[slot] + pos] = s;
+      }
+    }
+    if (!scatter && t_last + 1 <= tx1) {
+      uint32_t* bd = f.backdrop + size_t(row_slot + uint32_t(t_last + 1 - tx0)) * kStripRows;
+      int ya = max(ey0, r << kStripShift), yb = min(ey1, (r << kStripShift) + kStripRows - 1);
+      for (int y = ya; y <= yb; y++) {
+        int top = max(g.y0, y << 8), bot = min(g.y1, (y + 1) << 8);
+        uint32_t cov = (uint32_t(bot - top) ^ sm) - sm;
+        atomicAdd(&bd[y & (kStripRows - 1)], cov << 9);
+      }
     }
   }
+}
+
+// Prefix of the backdrop deltas over the tile columns of every (command, strip row, row).
+__global__ void backdrop_prefix_kernel(FrameView f) {
+  uint32_t c = blockIdx.x;
+  uint32_t ctx = f.cmd_tile_x[c];
+  if (ctx == 0xFFFFFFFFu || f.cmds[c].kind != kFillAnalytic) return;
+  const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
+  const uint32_t yr = f.cmd_yr[c];
+  const uint32_t nsr = ((yr >> 16) >> kStripShift) - ((yr & 0xFFFFu) >> kStripShift) + 1u;
+  const uint32_t base = f.cmdrow_base[c];
+  for (uint32_t i = threadIdx.x; i < nsr * kStripRows; i += blockDim.x) {
+    uint32_t sr = i / kStripRows, row = i % kStripRows;
+    uint32_t* bd = f.backdrop + size_t(base + sr * ntx) * kStripRows + row;
+    uint32_t acc = 0;
+    for (uint32_t t = 0; t < ntx; t++) { acc += bd[t * kStripRows]; bd[t * kStripRows] = acc; }
+  }
+}
+
+int launch_backdrop_prefix(const FrameView& f, cudaStream_t st) {
+  if (!f.num_cmds || !f.num_cmdrows) return 0;
+  backdrop_prefix_kernel<<<f.num_cmds, 64, 0, st>>>(f);
+  return 1;
 }
 
 // Per tile row: commands overlapping the row in painter's order (one block per row).
@@ -619,12 +668,15 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
           if (lane == ng) gcmd = ci;
           ng++;
         }
-        // segment lists of the group's analytic commands for this strip row
-        uint32_t s_count = 0, s_first = 0;
+        // segment lists of the group's analytic commands for this strip row and tile column
+        uint32_t s_count = 0, s_first = 0, slot = 0xFFFFFFFFu;
         if (lane < ng) {
           const DevCmd& gc = f.cmds[gcmd];
           if (gc.kind == kFillAnalytic) {
-            uint32_t slot = f.cmdrow_base[gcmd] + strip_row - ((f.cmd_yr[gcmd] & 0xFFFFu) >> kStripShift);
+            uint32_t ctx = f.cmd_tile_x[gcmd];
+            uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
+            slot = f.cmdrow_base[gcmd] + (strip_row - ((f.cmd_yr[gcmd] & 0xFFFFu) >> kStripShift)) * ntx +
+                   (uint32_t(tx) - (ctx & 0xFFFFu));
             s_first = f.cmdrow_offsets[slot];
             s_count = f.cmdrow_counts[slot];
           }
@@ -642,10 +694,14 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
           ws.seg_excl[lane] = incl - s_count;
         }
         if (lane == 0) ws.seg_excl[kGroup] = total;
-        // zero the group's cell slots (each lane its own 4 cells) and backdrops
+        // zero the group's cell slots (each lane its own 4 cells); backdrops start from the table
         for (int g = 0; g < ng; g++)
           *reinterpret_cast<uint4*>(&ws.cells[g][lane * 4]) = make_uint4(0u, 0u, 0u, 0u);
-        ws.backdrop[lane >> 2][lane & 3] = 0u;
+        {
+          int g = lane >> 2;
+          uint32_t gslot = __shfl_sync(0xFFFFFFFFu, slot, g);
+          ws.backdrop[g][lane & 3] = (g < ng && gslot != 0xFFFFFFFFu) ? f.backdrop[size_t(gslot) * kStripRows + (lane & 3)] : 0u;
+        }
         __syncwarp();
 
         // ---- rasterize every segment of the group, lanes spread over all of them
@@ -697,7 +753,14 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
           if (row_ok && (m[0] | m[1] | m[2] | m[3])) {
             const DevStyle& st = f.styles[cmd.style];
             const bool src_copy = (cmd.flags & 1u) != 0;
-            px::RowState rs = px::row_state(st, y, fetch_y0);
+            px::RowState rs;
+            if (px::has_row_table(st.fetch)) {
+              const float4 t4 = f.row_states[f.rs_base[ci] + uint32_t(y - int(f.cmd_yr[ci] & 0xFFFFu))];
+              rs.f0 = t4.x; rs.f1 = t4.y; rs.f2 = t4.z;
+            }
+            else {
+              rs = px::row_state(st, y, fetch_y0);
+            }
             uint32_t n = 0;
             // one copy of the fetch + composite code: the 4 pixels rotate through slot 0
 #pragma unroll 1
@@ -733,6 +796,22 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
     atomicAdd(&f.pixel_ops[0], (unsigned long long)ops);
     if (pat_ops) atomicAdd(&f.pixel_ops[1], (unsigned long long)pat_ops);
   }
+}
+
+// Gradient row states: one thread per (command, row) of every radial/conic command's bbox.
+__global__ void row_state_kernel(FrameView f, uint32_t total) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  uint32_t lo = 0, hi = f.num_cmds - 1;       // last command whose first row state is <= t
+  while (lo < hi) { uint32_t mid = (lo + hi + 1) >> 1; if (f.rs_base[mid] <= t) lo = mid; else hi = mid - 1; }
+  const uint32_t c = lo;
+  const DevCmd& cmd = f.cmds[c];
+  const DevCanvas& cv = f.canvases[cmd.canvas];
+  const int y = int(f.cmd_yr[c] & 0xFFFFu) + int(t - f.rs_base[c]);
+  // the row the reference initialized its fetcher at (start of the band for analytic fills)
+  int fetch_y0 = cmd.kind == kFillAnalytic ? max(cmd.box[1], (y / cv.band_height) * cv.band_height) : cmd.fetch_y0;
+  px::RowState rs = px::row_state(f.styles[cmd.style], y, fetch_y0);
+  f.row_states[t] = make_float4(rs.f0, rs.f1, rs.f2, 0.0f);
 }
 
 // Tile/row bookkeeping: canvas of every global tile and tile row, identity processing order.
@@ -855,6 +934,12 @@ int fine_grid_size() {
     grid = sms * (per_sm > 0 ? per_sm : 1);
   }
   return grid;
+}
+
+int launch_row_states(const FrameView& f, cudaStream_t st) {
+  if (!f.num_row_states) return 0;
+  row_state_kernel<<<cdiv(f.num_row_states, 128), 128, 0, st>>>(f, f.num_row_states);
+  return 1;
 }
 
 // work_counter must be zero on entry.

@@ -20,6 +20,8 @@ int launch_cmd_tiles(const FrameView& f, uint32_t* cmdrow_counts_per_cmd, cudaSt
 int launch_seg_bin(const FrameView& f, int scatter, cudaStream_t st);
 int launch_rows_and_tiles(const FrameView& f, uint32_t* row_canvas, cudaStream_t st);
 int launch_fine(const FrameView& f, cudaStream_t st);
+int launch_row_states(const FrameView& f, cudaStream_t st);
+int launch_backdrop_prefix(const FrameView& f, cudaStream_t st);
 int fine_grid_size();
 
 }  // namespace blgpu

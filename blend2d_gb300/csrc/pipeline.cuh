@@ -26,11 +26,25 @@ __device__ __forceinline__ uint64_t div255(uint64_t u) {
 }
 __device__ __forceinline__ uint64_t div256(uint64_t u) { return (u >> 8) & kLaneFF; }
 
+// The same per-channel arithmetic on two 16-bit lanes of a 32-bit word (every product and sum
+// stays below 2^16, so lanes never carry into each other).
+__device__ __forceinline__ uint32_t div255_2x16(uint32_t x) {
+  x += 0x00800080u;
+  return ((x + ((x >> 8) & 0x00FF00FFu)) >> 8) & 0x00FF00FFu;
+}
+
 // CompOp_SrcOver_Op / CompOp_SrcCopy_Op (compopgeneric_p.h:24-63) with a mask m in [0, 255].
 __device__ __forceinline__ uint32_t composite(uint32_t d, uint32_t s, uint32_t m, bool src_copy) {
-  if (src_copy) return pack(div255(unpack(d) * (m ^ 0xFFu) + unpack(s) * m));
-  uint32_t sm = pack(div255(unpack(s) * m));
-  return sm + pack(div255(unpack(d) * ((sm >> 24) ^ 0xFFu)));
+  const uint32_t kM = 0x00FF00FFu;
+  if (src_copy) {
+    uint32_t im = m ^ 0xFFu;
+    uint32_t rb = div255_2x16((d & kM) * im + (s & kM) * m);
+    uint32_t ag = div255_2x16(((d >> 8) & kM) * im + ((s >> 8) & kM) * m);
+    return rb | (ag << 8);
+  }
+  uint32_t sm = div255_2x16((s & kM) * m) | (div255_2x16(((s >> 8) & kM) * m) << 8);
+  uint32_t ia = (sm >> 24) ^ 0xFFu;
+  return sm + (div255_2x16((d & kM) * ia) | (div255_2x16(((d >> 8) & kM) * ia) << 8));
 }
 
 // x86 cvttss2si / cvtss2si semantics (INT_MIN for NaN and out-of-range values).
@@ -108,6 +122,12 @@ __device__ __forceinline__ void af_index(const DevStyle& s, uint64_t px, uint64_
 
 // Row state. `fetch_y0` is the row where the reference initialized its fetcher for this row
 // (only the conic gradient depends on it).
+// Radial and conic fetchers carry FP64 row state; it is tabulated per (command, row) once per
+// frame instead of being recomputed by every lane that composites the row.
+__device__ __forceinline__ bool has_row_table(uint32_t fetch) {
+  return fetch == kFetchRadialPad || fetch == kFetchRadialRoR || fetch == kFetchConic;
+}
+
 __device__ RowState row_state(const DevStyle& st, int y, int fetch_y0) {
   RowState r{};
   switch (st.fetch) {

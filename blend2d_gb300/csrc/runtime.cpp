@@ -147,7 +147,7 @@ BLGpuResult Runtime::init(const BLGpuRuntimeCreateInfo* info) {
     own_stream = true;
   }
   for (auto& e : ev) BLGPU_CHECK(cudaEventCreate(&e));
-  BLGPU_CHECK(cudaMallocHost(reinterpret_cast<void**>(&host_totals), 64));
+  BLGPU_CHECK(cudaMallocHost(reinterpret_cast<void**>(&host_totals), 128));
   return BLGPU_SUCCESS;
 }
 
@@ -213,10 +213,13 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     row_canvas = L.take<uint32_t>(fr.rows + 1);
     v.tile_order = L.take<uint32_t>(fr.tiles + 1);
     v.tile_canvas = L.take<uint32_t>(fr.tiles + 1);
-    v.work_counter = L.take<uint32_t>(16);   // [0] work counter, [4..8) totals, [8..12) error flags, [12..16) pixel ops
+    // [0] work queue, [1] items, [4..12) totals, [12..16) error flags, [16..20) pixel ops (2 x u64)
+    v.work_counter = L.take<uint32_t>(kCounterWords);
     v.totals = v.work_counter + 4;
-    v.error_flags = v.work_counter + 8;
-    v.pixel_ops = reinterpret_cast<unsigned long long*>(v.work_counter + 12);
+    v.error_flags = v.work_counter + 12;
+    v.pixel_ops = reinterpret_cast<unsigned long long*>(v.work_counter + 16);
+    v.rs_count = L.take<uint32_t>(nc + 1);
+    v.rs_base = L.take<uint32_t>(nc + 1);
     scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, fr.rows + 1)));
     return staged_end;
   };
@@ -331,7 +334,7 @@ BLGpuResult Runtime::reserve_segments(uint32_t count) {
 int Runtime::enqueue_count_half(cudaStream_t st) {
   const FrameView& f = view;
   int k = 0;
-  cudaMemsetAsync(f.work_counter, 0, sizeof(uint32_t) * 16, st);
+  cudaMemsetAsync(f.work_counter, 0, sizeof(uint32_t) * kCounterWords, st);
   cudaMemsetAsync(f.row_counts, 0, sizeof(uint32_t) * (f.num_rows + 1), st);
   k += launch_lut(f, st);
   k += launch_edges(f, st);
@@ -340,6 +343,8 @@ int Runtime::enqueue_count_half(cudaStream_t st) {
   k += launch_total(cmdrow_per_cmd, f.cmdrow_base, f.num_cmds, f.totals + 2, st);
   k += exclusive_scan(f.row_counts, f.row_offsets, f.num_rows, scan_tmp, st);
   k += launch_total(f.row_counts, f.row_offsets, f.num_rows, f.totals + 3, st);
+  k += exclusive_scan(f.rs_count, f.rs_base, f.num_cmds, scan_tmp, st);
+  k += launch_total(f.rs_count, f.rs_base, f.num_cmds, f.totals + 4, st);
   return k;
 }
 
@@ -349,10 +354,13 @@ int Runtime::enqueue_render_half(cudaStream_t st, bool timed) {
   int k = 0;
   cudaMemsetAsync(f.cmdrow_counts, 0, sizeof(uint32_t) * (f.num_cmdrows + 1), st);
   cudaMemsetAsync(f.cmdrow_cursor, 0, sizeof(uint32_t) * (f.num_cmdrows + 1), st);
+  cudaMemsetAsync(f.backdrop, 0, sizeof(uint32_t) * kStripRows * (size_t(f.num_cmdrows) + 1), st);
   k += launch_seg_bin(f, 0, st);
+  k += launch_backdrop_prefix(f, st);
   k += exclusive_scan(f.cmdrow_counts, f.cmdrow_offsets, f.num_cmdrows, f.cmdrow_offsets + f.num_cmdrows + 1, st);
   k += launch_seg_bin(f, 1, st);
   k += launch_rows_and_tiles(f, row_canvas, st);
+  k += launch_row_states(f, st);
   if (timed) cudaEventRecord(ev[1], st);
   k += launch_fine(f, st);
   if (timed) cudaEventRecord(ev[2], st);
@@ -385,8 +393,8 @@ BLGpuResult Runtime::run(const Frame& fr) {
   BLGPU_CHECK(cudaEventRecord(ev[0], stream));
   int launches = enqueue_count_half(stream);
   BLGPU_CHECK(cudaGetLastError());
-  BLGPU_CHECK(cudaMemcpyAsync(host_totals, view.totals, 16, cudaMemcpyDeviceToHost, stream));
-  d2h_bytes += 16;
+  BLGPU_CHECK(cudaMemcpyAsync(host_totals, view.totals, 32, cudaMemcpyDeviceToHost, stream));
+  d2h_bytes += 32;
   BLGPU_CHECK(cudaStreamSynchronize(stream));
   if (host_totals[0] > view.seg_capacity) {
     // more segments than slots: grow and repeat the counting half (it is idempotent)
@@ -398,8 +406,8 @@ BLGpuResult Runtime::run(const Frame& fr) {
     BLGPU_CHECK(cudaEventRecord(ev[0], stream));
     launches = enqueue_count_half(stream);
     BLGPU_CHECK(cudaGetLastError());
-    BLGPU_CHECK(cudaMemcpyAsync(host_totals, view.totals, 16, cudaMemcpyDeviceToHost, stream));
-    d2h_bytes += 16;
+    BLGPU_CHECK(cudaMemcpyAsync(host_totals, view.totals, 32, cudaMemcpyDeviceToHost, stream));
+    d2h_bytes += 32;
     BLGPU_CHECK(cudaStreamSynchronize(stream));
     if (host_totals[0] > view.seg_capacity) return BLGPU_ERROR_OUT_OF_MEMORY;
   }
@@ -407,6 +415,7 @@ BLGpuResult Runtime::run(const Frame& fr) {
   totals.seglist = host_totals[1];
   totals.cmdrows = host_totals[2];
   totals.row_entries = host_totals[3];
+  totals.row_states = host_totals[4];
 
   // Dynamic buffers.
   auto plan = [&](Layout& L) {
@@ -414,7 +423,9 @@ BLGpuResult Runtime::run(const Frame& fr) {
     view.cmdrow_offsets = L.take<uint32_t>(totals.cmdrows + 1 + scan_temp_words(totals.cmdrows + 1));
     view.cmdrow_cursor = L.take<uint32_t>(totals.cmdrows + 1);
     view.seglist = L.take<uint32_t>(totals.seglist + 1);
+    view.backdrop = L.take<uint32_t>((size_t(totals.cmdrows) + 1) * kStripRows);
     view.row_cmds = L.take<uint32_t>(totals.row_entries + 1);
+    view.row_states = L.take<float4>(totals.row_states + 1);
   };
   Layout measure;
   plan(measure);
@@ -425,6 +436,7 @@ BLGpuResult Runtime::run(const Frame& fr) {
   view.num_segs = totals.segs;
   view.num_cmdrows = totals.cmdrows;
   view.num_seglist = totals.seglist;
+  view.num_row_states = totals.row_states;
 
   launches += enqueue_render_half(stream, true);
   BLGPU_CHECK(cudaGetLastError());

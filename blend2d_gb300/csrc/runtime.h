@@ -52,8 +52,10 @@ struct Frame {
 
 // Sizes produced by the counting half of the pipeline, cached for replay.
 struct FrameTotals {
-  uint32_t segs = 0, seglist = 0, cmdrows = 0, row_entries = 0;
+  uint32_t segs = 0, seglist = 0, cmdrows = 0, row_entries = 0, row_states = 0;
 };
+
+constexpr int kCounterWords = 32;
 
 struct DeviceBuffer {
   void* ptr = nullptr;
@@ -75,7 +77,7 @@ struct Runtime {
   uint32_t seg_capacity = 0;
   void* host_staging = nullptr;
   size_t host_staging_size = 0;
-  uint32_t* host_totals = nullptr;   // pinned
+  uint32_t* host_totals = nullptr;   // pinned: [0..8) frame totals, [8..12) pixel ops
 
   cudaEvent_t ev[4] = {};
   cudaGraphExec_t graph = nullptr;
