@@ -148,6 +148,24 @@ struct DevItem {
   uint32_t b;              // first control point (line: end point)
 };
 
+#ifdef __CUDACC__
+// Tile columns whose cells a segment can touch within strip row `r` (pixel rows [4r, 4r + 3]):
+// the line's x at the strip's clipped y extent, one pixel of slack on both sides (the integer DDA
+// stays within a 24.8 unit of the exact line), plus the cell right of the last one (area).
+// `t_last` is the last such column; columns after it only see the segment's full row cover.
+__device__ __forceinline__ void strip_tile_range(const DevSeg& g, int r, int& t0, int& t_last) {
+  int ya = max(g.y0, (r << kStripShift) << 8);
+  int yb = min(g.y1, ((r + 1) << kStripShift) << 8);
+  int64_t dy = int64_t(g.y1) - g.y0, dx = int64_t(g.x1) - g.x0;
+  int xa = g.x0 + int((dx * (ya - g.y0)) / dy);
+  int xb = g.x0 + int((dx * (yb - g.y0)) / dy);
+  int lo = max(min(xa, xb) - 256, min(g.x0, g.x1));
+  int hi = min(max(xa, xb) + 256, max(g.x0, g.x1));
+  t0 = (lo >> 8) >> kTileShift;
+  t_last = ((hi >> 8) + 1) >> kTileShift;
+}
+#endif
+
 // Device-side view of a frame (pointers into one device arena).
 struct FrameView {
   const DevCmd* cmds;

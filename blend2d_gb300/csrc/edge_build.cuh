@@ -68,9 +68,15 @@ struct Sink {
     sbuf[nb] = sign;
     if (++nb == kSinkBatch) flush();
     n++;
-    // seglist entries: strip rows x tile columns the segment's cells touch (cells reach x + 1)
-    rows += ((uint32_t((y1 - 1) >> 8) >> kStripShift) - (uint32_t(y0 >> 8) >> kStripShift) + 1u) *
-            ((uint32_t(((max(x0, x1) >> 8) + 1)) >> kTileShift) - (uint32_t(min(x0, x1) >> 8) >> kTileShift) + 1u);
+    // seglist entries: per strip row, the tile columns the segment's cells can touch there
+    {
+      const DevSeg g{x0, y0, x1, y1};
+      for (int r = (y0 >> 8) >> kStripShift, r1 = ((y1 - 1) >> 8) >> kStripShift; r <= r1; r++) {
+        int t0, tl;
+        strip_tile_range(g, r, t0, tl);
+        rows += uint32_t(tl - t0 + 1);
+      }
+    }
     ymin = min(ymin, y0);
     ymax = max(ymax, y1);
     xmin = min(xmin, min(x0, x1));

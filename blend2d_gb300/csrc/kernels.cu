@@ -505,12 +505,12 @@ __global__ void seg_bin_kernel(FrameView f, int scatter) {
   const DevSeg g = f.segs[s];
   const int ey0 = g.y0 >> 8, ey1 = (g.y1 - 1) >> 8;
   const int r0 = max(ey0 >> kStripShift, sr0), r1 = min(ey1 >> kStripShift, sr1);
-  const int t0 = max((min(g.x0, g.x1) >> 8) >> kTileShift, tx0);
-  const int t_last = ((max(g.x0, g.x1) >> 8) + 1) >> kTileShift;
-  const int t1 = min(t_last, tx1);
   const uint32_t base = f.cmdrow_base[c];
   const uint32_t sm = 0u - sign;
   for (int r = r0; r <= r1; r++) {
+    int t_first, t_last;
+    strip_tile_range(g, r, t_first, t_last);
+    const int t0 = max(t_first, tx0), t1 = min(t_last, tx1);
     uint32_t row_slot = base + uint32_t(r - sr0) * uint32_t(ntx);
     for (int t = t0; t <= t1; t++) {
       uint32_t slot = row_slot + uint32_t(t - tx0);
