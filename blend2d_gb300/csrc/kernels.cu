@@ -594,9 +594,6 @@ constexpr int kGroup = 8;
 // per-warp structs sit back to back in one array.
 struct alignas(16) StripShared {
   uint32_t cells[kGroup][kStripRows * kTileW];
-  uint32_t pix[kStripRows * kTileW];     // the strip's pixels while its commands are composited
-  uint8_t mask[kStripRows * kTileW];     // the current command's mask per pixel
-  uint8_t active[kStripRows * kTileW];   // the current command's pixels with a non-zero mask
   uint32_t backdrop[kGroup][kStripRows];
   uint32_t cmd[kGroup];
   uint32_t seg_first[kGroup];
@@ -632,16 +629,15 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
     bool row_ok = y < cv.h;
     uint32_t* dst = cv.pixels + int64_t(y) * cv.stride + xp;
 
-    // pixel p of the strip (lane p / 4, its (p % 4)-th pixel) lives in ws.pix[p]
+    uint32_t pix[4];
     bool full = row_ok && (xp + 3 < cv.w);
-    {
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (full) v = *reinterpret_cast<const uint4*>(dst);
-      else if (row_ok) {
-        v.x = xp < cv.w ? dst[0] : 0u; v.y = xp + 1 < cv.w ? dst[1] : 0u;
-        v.z = xp + 2 < cv.w ? dst[2] : 0u; v.w = xp + 3 < cv.w ? dst[3] : 0u;
-      }
-      *reinterpret_cast<uint4*>(&ws.pix[lane * 4]) = v;
+    if (full) {
+      uint4 v = *reinterpret_cast<const uint4*>(dst);
+      pix[0] = v.x; pix[1] = v.y; pix[2] = v.z; pix[3] = v.w;
+    }
+    else {
+#pragma unroll
+      for (int k = 0; k < 4; k++) pix[k] = (row_ok && xp + k < cv.w) ? dst[k] : 0u;
     }
 
     uint32_t row_id = cv.row_base + uint32_t(ty);
@@ -754,71 +750,44 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
             for (int k = 0; k < 4; k++) m[k] = px::box_u_mask(cmd.box, alpha, xp + k, y);
           }
 
-          // compact this command's covered pixels so that lanes stay busy on partial strips
-          uint32_t cnt = 0;
-#pragma unroll
-          for (int k = 0; k < 4; k++) {
-            if (!(row_ok && xp + k < cv.w)) m[k] = 0u;
-            cnt += m[k] ? 1u : 0u;
-          }
-          uint32_t incl = cnt;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= o) incl += v;
-          }
-          const uint32_t n_active = __shfl_sync(0xFFFFFFFFu, incl, 31);
-          if (n_active) {
-            uint32_t pos = incl - cnt;
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-              if (m[k]) { ws.active[pos++] = uint8_t(lane * 4 + k); ws.mask[lane * 4 + k] = uint8_t(m[k]); }
-            }
-            __syncwarp();
+          if (row_ok && (m[0] | m[1] | m[2] | m[3])) {
             const DevStyle& st = f.styles[cmd.style];
             const bool src_copy = (cmd.flags & 1u) != 0;
-            const bool table = px::has_row_table(st.fetch);
-            const int cmd_y0 = int(f.cmd_yr[ci] & 0xFFFFu);
-            const uint32_t rs_first = table ? f.rs_base[ci] : 0u;
-            const int box_y0 = cmd.box[1];
-            for (uint32_t i = lane; i < n_active; i += 32) {
-              const uint32_t p = ws.active[i];
-              const int py = row0 + int(p >> 5);
-              const int pxx = x_base + int(p & 31u);
-              px::RowState rs;
-              if (table) {
-                const float4 t4 = f.row_states[rs_first + uint32_t(py - cmd_y0)];
-                rs.f0 = t4.x; rs.f1 = t4.y; rs.f2 = t4.z;
-              }
-              else {
-                // the reference initializes its fetcher at the start of each band of an analytic fill
-                int fy0 = kind == kFillAnalytic ? max(box_y0, (py / cv.band_height) * cv.band_height) : fetch_y0;
-                rs = px::row_state(st, py, fy0);
-              }
-              uint32_t sv = px::fetch(st, rs, pxx, f.luts, f.images);
-              ws.pix[p] = px::composite(ws.pix[p], sv, ws.mask[p], src_copy);
+            px::RowState rs;
+            if (px::has_row_table(st.fetch)) {
+              const float4 t4 = f.row_states[f.rs_base[ci] + uint32_t(y - int(f.cmd_yr[ci] & 0xFFFFu))];
+              rs.f0 = t4.x; rs.f1 = t4.y; rs.f2 = t4.z;
             }
-            ops += lane == 0 ? n_active : 0u;
-            pat_ops += (lane == 0 && st.fetch >= kFetchPatAlignedPad) ? n_active : 0u;
-            __syncwarp();
+            else {
+              rs = px::row_state(st, y, fetch_y0);
+            }
+            uint32_t n = 0;
+            // one copy of the fetch + composite code: the 4 pixels rotate through slot 0
+#pragma unroll 1
+            for (int k = 0; k < 4; k++) {
+              if (m[0] && xp + k < cv.w) {
+                uint32_t sv = px::fetch(st, rs, xp + k, f.luts, f.images);
+                pix[0] = px::composite(pix[0], sv, m[0], src_copy);
+                n++;
+              }
+              uint32_t tp = pix[0]; pix[0] = pix[1]; pix[1] = pix[2]; pix[2] = pix[3]; pix[3] = tp;
+              uint32_t tm = m[0]; m[0] = m[1]; m[1] = m[2]; m[2] = m[3]; m[3] = tm;
+            }
+            ops += n;
+            pat_ops += st.fetch >= kFetchPatAlignedPad ? n : 0u;
           }
         }
         __syncwarp();
       }
     }
 
-    __syncwarp();
-    {
-      const uint4 v = *reinterpret_cast<const uint4*>(&ws.pix[lane * 4]);
-      if (full) *reinterpret_cast<uint4*>(dst) = v;
-      else if (row_ok) {
-        if (xp < cv.w) dst[0] = v.x;
-        if (xp + 1 < cv.w) dst[1] = v.y;
-        if (xp + 2 < cv.w) dst[2] = v.z;
-        if (xp + 3 < cv.w) dst[3] = v.w;
-      }
+    if (full) {
+      *reinterpret_cast<uint4*>(dst) = make_uint4(pix[0], pix[1], pix[2], pix[3]);
     }
-    __syncwarp();
+    else {
+#pragma unroll
+      for (int k = 0; k < 4; k++) if (row_ok && xp + k < cv.w) dst[k] = pix[k];
+    }
   }
 
   ops = __reduce_add_sync(0xFFFFFFFFu, ops);
