@@ -55,6 +55,14 @@ def parse_args(argv=None):
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="bounded CPU-baseline sample (seconds)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="frame", choices=["frame", "batch", "serving"],
+                    help="frame: one canvas per step (default); batch: many canvases in one pipeline vs one "
+                         "pipeline per canvas; serving: Poisson arrivals through the continuous-batching server")
+    ap.add_argument("--batch-count", type=int, default=1024, help="canvases of the batched workload")
+    ap.add_argument("--batch-scale", type=float, default=0.02, help="path-count scale of the batched workload")
+    ap.add_argument("--serve-requests", type=int, default=48, help="requests per arrival-rate point")
+    ap.add_argument("--serve-scale", type=float, default=0.05, help="path-count scale of the serving requests")
+    ap.add_argument("--serve-rates", default="20,60,200", help="arrival rates (requests/s) to sweep")
     return ap.parse_args(argv)
 
 
@@ -393,12 +401,128 @@ def run_reference(args) -> int:
     return 0
 
 
+def run_batch(args) -> int:
+    """Many independent canvases (width/height log-uniform 32-2048, log-uniform path counts of the
+    polygon and cubic-gradient kinds): one device pipeline for all of them (blgpu_render_batch,
+    one persistent fine launch over every canvas's tiles) against one pipeline per canvas."""
+    import numpy as np
+    import torch
+
+    import blend2d_gb300 as bg
+    from blend2d_gb300 import scenes
+
+    sws = scenes.batch_canvases(seed=4, count=args.batch_count, scale=args.batch_scale)
+    streams = [sw.to_bytes() for sw in sws]
+    mpix = sum(sw.width * sw.height for sw in sws) / 1e6
+    paths = sum(sw.fill_count for sw in sws)
+    s = torch.cuda.Stream()
+    rt = bg.Runtime(0, cuda_stream=s.cuda_stream)
+    batched = [np.zeros((sw.height, sw.width), dtype=np.uint32) for sw in sws]
+    singles = [np.zeros((sw.height, sw.width), dtype=np.uint32) for sw in sws]
+    for _ in range(max(1, args.warmup // 2)):
+        rt.render_batch(streams, batched)
+    steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        rt.render_batch(streams, batched)
+    batch_s = (time.perf_counter() - t0) / steps
+    batch_dev_ms = rt.stats().last_gpu_ms
+    batch_launches = int(rt.stats().kernel_launches)
+    # device-resident replay of the whole batch as one CUDA graph
+    rt.replay(True)
+    rt.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(s):
+        ev0.record(s)
+        for _ in range(steps):
+            rt.replay(True)
+        ev1.record(s)
+    torch.cuda.synchronize()
+    graph_ms = ev0.elapsed_time(ev1) / steps
+    # one pipeline per canvas, same public API, same host buffers
+    for sw_stream, img in zip(streams[:8], singles[:8]):
+        bg.render_stream(rt, sw_stream, img)
+    dev_ms = 0.0
+    t0 = time.perf_counter()
+    for sw_stream, img in zip(streams, singles):
+        bg.render_stream(rt, sw_stream, img)
+        dev_ms += rt.stats().last_gpu_ms
+    single_s = time.perf_counter() - t0
+    identical = all(np.array_equal(a, b) for a, b in zip(batched, singles))
+    line = {
+        "metric": "canvases/s", "mode": "batch", "unit": "canvases/s",
+        "value": round(len(sws) / batch_s, 2), "higher_is_better": True, "n_gpus": 1, "steps": steps,
+        "config": {"workload": f"batch_{len(sws)}_canvases_32-2048px_scale{args.batch_scale}", "canvases": len(sws),
+                   "paths": paths, "mpix": round(mpix, 2), "seed": 4},
+        "batched": {"e2e_s": round(batch_s, 4), "canvases_per_s": round(len(sws) / batch_s, 2),
+                    "mpix_per_s": round(mpix / batch_s, 2), "device_ms": round(batch_dev_ms, 3),
+                    "graph_replay_ms": round(graph_ms, 3), "kernel_launches": batch_launches},
+        "per_canvas": {"e2e_s": round(single_s, 4), "canvases_per_s": round(len(sws) / single_s, 2),
+                       "mpix_per_s": round(mpix / single_s, 2), "device_ms_sum": round(dev_ms, 3)},
+        "speedup_e2e": round(single_s / batch_s, 2),
+        "speedup_device": round(dev_ms / max(graph_ms, 1e-9), 2),
+        "bit_identical": identical,
+    }
+    rt.close()
+    print(json.dumps(line), flush=True)
+    return 0 if identical else 1
+
+
+def run_serving(args) -> int:
+    """Poisson arrivals of render requests (square canvases, side log-uniform 64-4096 px, 1-20,000
+    log-uniform paths times a scale) through the continuous-batching server; p50/p99 latency and
+    Mpix/s per arrival rate."""
+    import random
+
+    import blend2d_gb300 as bg  # noqa: F401
+    from blend2d_gb300 import scenes
+    from blend2d_gb300.serving import RenderServer, percentile
+
+    reqs = [sw.to_bytes() for sw in scenes.serving_requests(seed=5, count=args.serve_requests, scale=args.serve_scale)]
+    mpix_req = [int.from_bytes(r[8:12], "little") * int.from_bytes(r[12:16], "little") / 1e6 for r in reqs]
+    points = []
+    with RenderServer(workers=2, hbm_budget=150 << 30) as srv:
+        for f in [srv.submit(r) for r in reqs[:4]]:     # warm-up: device arenas grow once
+            f.result()
+        for rate in [float(x) for x in args.serve_rates.split(",")]:
+            rng = random.Random(int(rate))
+            srv.stats.latencies.clear()
+            t0 = time.perf_counter()
+            futs = []
+            t_next = t0
+            for r in reqs:
+                now = time.perf_counter()
+                if t_next > now:
+                    time.sleep(t_next - now)
+                futs.append(srv.submit(r))
+                t_next += rng.expovariate(rate)
+            for f in futs:
+                f.result()
+            wall = time.perf_counter() - t0
+            lat = list(srv.stats.latencies)
+            points.append({"rate_rps": rate, "requests": len(reqs), "p50_ms": round(1e3 * percentile(lat, 50), 2),
+                           "p99_ms": round(1e3 * percentile(lat, 99), 2), "mpix_per_s": round(sum(mpix_req) / wall, 2),
+                           "wall_s": round(wall, 3)})
+        batches = srv.stats.batches
+        max_inflight = srv.stats.max_inflight_bytes
+    line = {"metric": "p50/p99 latency and Mpix/s", "mode": "serving", "unit": "ms | Mpix/s", "n_gpus": 1,
+            "config": {"workload": f"serving_{len(reqs)}_requests_side64-4096_paths1-20000_scale{args.serve_scale}",
+                       "mpix_per_pass": round(sum(mpix_req), 2), "workers": 2, "hbm_budget_gb": 150, "seed": 5},
+            "points": points, "batches": batches, "max_inflight_bytes": max_inflight}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None) -> int:
     args = parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "batch":
+        return run_batch(args)
+    if args.mode == "serving":
+        return run_serving(args)
     return run_ours(args)
 
 

@@ -197,6 +197,7 @@ struct FrameView {
   uint32_t* cmdrow_offsets;    // exclusive scan of counts
   uint32_t* cmdrow_cursor;
   uint32_t* seglist;           // segment indices grouped by (cmd, strip row, tile column)
+  uint8_t* masks;              // [num_cmdrows][kStripRows * kTileW]: analytic masks from the coverage pass
   uint32_t* backdrop;          // [num_cmdrows][kStripRows]: coverage carried into the slot's tile
                                //   from segments entirely left of it (cover << 9 per row)
   uint32_t* row_counts;        // [num_rows + 1]

@@ -68,14 +68,14 @@ struct Sink {
     sbuf[nb] = sign;
     if (++nb == kSinkBatch) flush();
     n++;
-    // seglist entries: per strip row, the tile columns the segment's cells can touch there
+    // bound of the seglist entries (strip_tile_range summed over the segment's strip rows): the
+    // per-strip ranges of a line tile its slackened x extent, overlapping by at most one tile at
+    // each strip boundary and widened by at most one tile on each side by the slack
     {
-      const DevSeg g{x0, y0, x1, y1};
-      for (int r = (y0 >> 8) >> kStripShift, r1 = ((y1 - 1) >> 8) >> kStripShift; r <= r1; r++) {
-        int t0, tl;
-        strip_tile_range(g, r, t0, tl);
-        rows += uint32_t(tl - t0 + 1);
-      }
+      const uint32_t strips = (uint32_t((y1 - 1) >> 8) >> kStripShift) - (uint32_t(y0 >> 8) >> kStripShift) + 1u;
+      const int lo = min(x0, x1) - 256, hi = max(x0, x1) + 256;
+      const uint32_t tiles = uint32_t((((hi >> 8) + 1) >> kTileShift) - ((lo >> 8) >> kTileShift) + 1);
+      rows += tiles + 3u * strips;
     }
     ymin = min(ymin, y0);
     ymax = max(ymax, y1);

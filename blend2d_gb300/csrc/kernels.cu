@@ -577,34 +577,123 @@ __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// K3 - persistent fine kernel. The work unit is a strip of kStripRows x kTileW pixels (one warp,
-// 4 pixels per lane held in registers from one 128-bit load to one 128-bit store). Warps pull
-// strips from an atomic queue and never wait on each other. The commands of the strip's tile row
-// that overlap the strip are taken in painter's order, up to kGroup at a time: the lanes first
-// rasterize the segments of all analytic commands of the group together (each command into its
-// own shared-memory cell slot), then the group's commands are swept (8-lane shuffle prefix) and
-// composited one after the other.
+// K3a - coverage. A slot is (analytic command, strip row, tile column): 4 rows x 32 pixels. Slots
+// are independent, so each warp takes kSlotGroup consecutive slots at once: its lanes rasterize
+// the segments of all of them together (each slot into its own shared-memory cells, starting from
+// the slot's backdrop), then every slot is swept (8-lane shuffle prefix per row) into 128 8-bit
+// masks, stored as one coalesced 128-byte row per slot.
 // ---------------------------------------------------------------------------------------------
 
 constexpr int kStripsPerTile = kTileH / kStripRows;
 constexpr int kFineWarps = kFineThreads / 32;
-constexpr int kGroup = 8;
+constexpr int kSlotGroup = 16;
+constexpr int kSlotPixels = kStripRows * kTileW;
 
-// 16-byte aligned: each lane moves its 4 cells with one 128-bit shared-memory access, and the
-// per-warp structs sit back to back in one array.
-struct alignas(16) StripShared {
-  uint32_t cells[kGroup][kStripRows * kTileW];
-  uint32_t backdrop[kGroup][kStripRows];
-  uint32_t cmd[kGroup];
-  uint32_t seg_first[kGroup];
-  uint32_t seg_excl[kGroup + 1];
+struct alignas(16) CoverShared {
+  uint32_t cells[kSlotGroup][kSlotPixels];
+  uint32_t backdrop[kSlotGroup][kStripRows];
+  uint32_t seg_first[kSlotGroup];
+  uint32_t seg_excl[kSlotGroup + 1];
+  int32_t x_base[kSlotGroup];
+  int32_t row0[kSlotGroup];
 };
-static_assert(sizeof(StripShared) % 16 == 0, "per-warp shared state must keep 16-byte alignment");
+static_assert(sizeof(CoverShared) % 16 == 0, "per-warp shared state must keep 16-byte alignment");
+
+__global__ void __launch_bounds__(kFineThreads) coverage_kernel(FrameView f) {
+  extern __shared__ __align__(16) unsigned char cover_smem[];
+  CoverShared& ws = reinterpret_cast<CoverShared*>(cover_smem)[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const uint32_t num_groups = (f.num_cmdrows + kSlotGroup - 1) / kSlotGroup;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+
+  for (uint32_t grp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); grp < num_groups; grp += warps) {
+    const uint32_t first = grp * kSlotGroup;
+    const int ns = int(min(uint32_t(kSlotGroup), f.num_cmdrows - first));
+    // lane g < ns describes slot first + g
+    uint32_t s_count = 0, s_first = 0, cmd_of = 0;
+    int xb = 0, r0 = 0;
+    if (lane < ns) {
+      const uint32_t slot = first + uint32_t(lane);
+      uint32_t lo = 0, hi = f.num_cmds - 1;          // last command whose first slot is <= slot
+      while (lo < hi) { uint32_t mid = (lo + hi + 1) >> 1; if (f.cmdrow_base[mid] <= slot) lo = mid; else hi = mid - 1; }
+      cmd_of = lo;
+      const uint32_t ctx = f.cmd_tile_x[lo];
+      const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
+      const uint32_t local = slot - f.cmdrow_base[lo];
+      const uint32_t sr = ((f.cmd_yr[lo] & 0xFFFFu) >> kStripShift) + local / ntx;
+      xb = int(((ctx & 0xFFFFu) + local % ntx) << kTileShift);
+      r0 = int(sr << kStripShift);
+      s_first = f.cmdrow_offsets[slot];
+      s_count = f.cmdrow_counts[slot];
+    }
+    uint32_t incl = s_count;
+#pragma unroll
+    for (int o = 1; o < kSlotGroup; o <<= 1) {
+      uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, kSlotGroup - 1);
+    if (lane < kSlotGroup) {
+      ws.seg_first[lane] = s_first;
+      ws.seg_excl[lane] = incl - s_count;
+      ws.x_base[lane] = xb;
+      ws.row0[lane] = r0;
+    }
+    if (lane == 0) ws.seg_excl[kSlotGroup] = total;
+    for (int g = 0; g < ns; g++)
+      *reinterpret_cast<uint4*>(&ws.cells[g][lane * 4]) = make_uint4(0u, 0u, 0u, 0u);
+    for (int i = lane; i < ns * kStripRows; i += 32)
+      ws.backdrop[i / kStripRows][i % kStripRows] = f.backdrop[size_t(first) * kStripRows + i];
+    __syncwarp();
+
+    for (uint32_t idx = lane; idx < total; idx += 32) {
+      int g = 0;
+#pragma unroll
+      for (int k = 1; k < kSlotGroup; k++) g += (k < ns && idx >= ws.seg_excl[k]) ? 1 : 0;
+      const uint32_t si = f.seglist[ws.seg_first[g] + (idx - ws.seg_excl[g])];
+      const uint32_t c = f.seg_meta[si] >> 1;
+      const DevCanvas& cv = f.canvases[f.cmds[c].canvas];
+      ras::WindowSink sink{ws.cells[g], ws.backdrop[g], ws.x_base[g]};
+      ras::segment_to_window(f.segs[si], f.seg_meta[si] & 1u, ws.row0[g], kStripRows, cv.h - 1, sink);
+    }
+    __syncwarp();
+
+    // sweep: lane covers row lane / 8, columns (lane % 8) * 4 .. + 3 of each slot
+    const int prow = lane >> 3;
+    for (int g = 0; g < ns; g++) {
+      const uint32_t c = __shfl_sync(0xFFFFFFFFu, cmd_of, g);
+      const uint32_t flags = f.cmds[c].flags, alpha = f.cmds[c].alpha;
+      const uint4 cv4 = *reinterpret_cast<const uint4*>(&ws.cells[g][lane * 4]);
+      const uint32_t s4 = cv4.x + cv4.y + cv4.z + cv4.w;
+      uint32_t inc = s4;
+#pragma unroll
+      for (int o = 1; o < 8; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o, 8);
+        if ((lane & 7) >= o) inc += v;
+      }
+      uint32_t cov = (256u << 9) + ws.backdrop[g][prow] + inc - s4;
+      const uint32_t rule = (flags & 2u) ? 0x1FFu : 0xFFFFFFFFu;
+      uint32_t m;
+      cov += cv4.x; m = px::calc_mask(cov, rule, alpha);
+      cov += cv4.y; m |= px::calc_mask(cov, rule, alpha) << 8;
+      cov += cv4.z; m |= px::calc_mask(cov, rule, alpha) << 16;
+      cov += cv4.w; m |= px::calc_mask(cov, rule, alpha) << 24;
+      reinterpret_cast<uint32_t*>(f.masks + size_t(first + uint32_t(g)) * kSlotPixels)[lane] = m;
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// K3b - composite, persistent. The work unit is a strip of kStripRows x kTileW pixels (one warp,
+// 4 pixels per lane held in registers from one 128-bit load to one 128-bit store). Warps pull
+// strips from an atomic queue and never wait on each other; the commands of the strip's tile row
+// that overlap the strip are applied in painter's order: analytic commands read their 4 masks per
+// lane from the coverage pass, box fills compute theirs, then fetch + SrcOver/SrcCopy.
+// ---------------------------------------------------------------------------------------------
 
 __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
-  __shared__ StripShared sh[kFineWarps];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  StripShared& ws = sh[warp];
+  const int lane = threadIdx.x & 31;
   const int prow = lane >> 3;            // row within the strip
   const int pcol = (lane & 7) * 4;       // first of this lane's 4 columns
   uint32_t ops = 0, pat_ops = 0;         // composited pixels of this lane (all strips)
@@ -658,126 +747,59 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
       }
       uint32_t ballot = __ballot_sync(0xFFFFFFFFu, hit);
       while (ballot) {
-        // ---- next group: up to kGroup hit commands, in order
-        int ng = 0;
-        uint32_t gcmd = 0;                 // lane g < ng holds the group's g-th command
-        while (ballot && ng < kGroup) {
-          int bit = __ffs(ballot) - 1;
-          ballot &= ballot - 1;
-          uint32_t ci = __shfl_sync(0xFFFFFFFFu, c, bit);
-          if (lane == ng) gcmd = ci;
-          ng++;
+        const int bit = __ffs(ballot) - 1;
+        ballot &= ballot - 1;
+        const uint32_t ci = __shfl_sync(0xFFFFFFFFu, c, bit);
+        const DevCmd& cmd = f.cmds[ci];
+        const uint32_t kind = cmd.kind;
+        const uint32_t alpha = cmd.alpha;
+        uint32_t m[4];
+        if (kind == kFillAnalytic) {
+          const uint32_t ctx = f.cmd_tile_x[ci];
+          const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
+          const uint32_t slot = f.cmdrow_base[ci] + (strip_row - ((f.cmd_yr[ci] & 0xFFFFu) >> kStripShift)) * ntx +
+                                (uint32_t(tx) - (ctx & 0xFFFFu));
+          const uint32_t mw = reinterpret_cast<const uint32_t*>(f.masks + size_t(slot) * kSlotPixels)[lane];
+          m[0] = mw & 0xFFu; m[1] = (mw >> 8) & 0xFFu; m[2] = (mw >> 16) & 0xFFu; m[3] = mw >> 24;
         }
-        // segment lists of the group's analytic commands for this strip row and tile column
-        uint32_t s_count = 0, s_first = 0, slot = 0xFFFFFFFFu;
-        if (lane < ng) {
-          const DevCmd& gc = f.cmds[gcmd];
-          if (gc.kind == kFillAnalytic) {
-            uint32_t ctx = f.cmd_tile_x[gcmd];
-            uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
-            slot = f.cmdrow_base[gcmd] + (strip_row - ((f.cmd_yr[gcmd] & 0xFFFFu) >> kStripShift)) * ntx +
-                   (uint32_t(tx) - (ctx & 0xFFFFu));
-            s_first = f.cmdrow_offsets[slot];
-            s_count = f.cmdrow_counts[slot];
-          }
-        }
-        uint32_t incl = s_count;
+        else if (kind == kFillBoxA) {
+          bool in_y = y >= cmd.box[1] && y < cmd.box[3];
 #pragma unroll
-        for (int o = 1; o < kGroup; o <<= 1) {
-          uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-          if (lane >= o) incl += v;
+          for (int k = 0; k < 4; k++) m[k] = (in_y && xp + k >= cmd.box[0] && xp + k < cmd.box[2]) ? alpha : 0u;
         }
-        uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, kGroup - 1);
-        if (lane < kGroup) {
-          ws.cmd[lane] = gcmd;
-          ws.seg_first[lane] = s_first;
-          ws.seg_excl[lane] = incl - s_count;
+        else {
+#pragma unroll
+          for (int k = 0; k < 4; k++) m[k] = px::box_u_mask(cmd.box, alpha, xp + k, y);
         }
-        if (lane == 0) ws.seg_excl[kGroup] = total;
-        // zero the group's cell slots (each lane its own 4 cells); backdrops start from the table
-        for (int g = 0; g < ng; g++)
-          *reinterpret_cast<uint4*>(&ws.cells[g][lane * 4]) = make_uint4(0u, 0u, 0u, 0u);
-        {
-          int g = lane >> 2;
-          uint32_t gslot = __shfl_sync(0xFFFFFFFFu, slot, g);
-          ws.backdrop[g][lane & 3] = (g < ng && gslot != 0xFFFFFFFFu) ? f.backdrop[size_t(gslot) * kStripRows + (lane & 3)] : 0u;
-        }
-        __syncwarp();
 
-        // ---- rasterize every segment of the group, lanes spread over all of them
-        for (uint32_t idx = lane; idx < total; idx += 32) {
-          int g = 0;
-#pragma unroll
-          for (int k = 1; k < kGroup; k++) g += (k < ng && idx >= ws.seg_excl[k]) ? 1 : 0;
-          uint32_t si = f.seglist[ws.seg_first[g] + (idx - ws.seg_excl[g])];
-          ras::WindowSink sink{ws.cells[g], ws.backdrop[g], x_base};
-          ras::segment_to_window(f.segs[si], f.seg_meta[si] & 1u, row0, kStripRows, cv.h - 1, sink);
-        }
-        __syncwarp();
-
-        // ---- sweep + composite the group's commands in order
-        for (int g = 0; g < ng; g++) {
-          const uint32_t ci = ws.cmd[g];
-          const DevCmd& cmd = f.cmds[ci];
-          const uint32_t kind = cmd.kind;
-          const uint32_t alpha = cmd.alpha;
-          uint32_t m[4] = {0u, 0u, 0u, 0u};
-          int fetch_y0 = cmd.fetch_y0;
-          if (kind == kFillAnalytic) {
-            uint4 cv4 = *reinterpret_cast<const uint4*>(&ws.cells[g][lane * 4]);
-            uint32_t cl[4] = {cv4.x, cv4.y, cv4.z, cv4.w};
-            uint32_t s4 = cl[0] + cl[1] + cl[2] + cl[3];
-            uint32_t inc = s4;
-#pragma unroll
-            for (int o = 1; o < 8; o <<= 1) {
-              uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o, 8);
-              if ((lane & 7) >= o) inc += v;
-            }
-            uint32_t cov = (256u << 9) + ws.backdrop[g][prow] + inc - s4;
-            uint32_t rule = (cmd.flags & 2u) ? 0x1FFu : 0xFFFFFFFFu;
-#pragma unroll
-            for (int k = 0; k < 4; k++) { cov += cl[k]; m[k] = px::calc_mask(cov, rule, alpha); }
-            // the reference initializes its fetcher at the start of each band of the command
-            fetch_y0 = max(cmd.box[1], (y / cv.band_height) * cv.band_height);
-          }
-          else if (kind == kFillBoxA) {
-            bool in_y = y >= cmd.box[1] && y < cmd.box[3];
-#pragma unroll
-            for (int k = 0; k < 4; k++) m[k] = (in_y && xp + k >= cmd.box[0] && xp + k < cmd.box[2]) ? alpha : 0u;
+        if (row_ok && (m[0] | m[1] | m[2] | m[3])) {
+          const DevStyle& st = f.styles[cmd.style];
+          const bool src_copy = (cmd.flags & 1u) != 0;
+          px::RowState rs;
+          if (px::has_row_table(st.fetch)) {
+            const float4 t4 = f.row_states[f.rs_base[ci] + uint32_t(y - int(f.cmd_yr[ci] & 0xFFFFu))];
+            rs.f0 = t4.x; rs.f1 = t4.y; rs.f2 = t4.z;
           }
           else {
-#pragma unroll
-            for (int k = 0; k < 4; k++) m[k] = px::box_u_mask(cmd.box, alpha, xp + k, y);
+            // the reference initializes its fetcher at the start of each band of an analytic fill
+            int fetch_y0 = kind == kFillAnalytic ? max(cmd.box[1], (y / cv.band_height) * cv.band_height) : cmd.fetch_y0;
+            rs = px::row_state(st, y, fetch_y0);
           }
-
-          if (row_ok && (m[0] | m[1] | m[2] | m[3])) {
-            const DevStyle& st = f.styles[cmd.style];
-            const bool src_copy = (cmd.flags & 1u) != 0;
-            px::RowState rs;
-            if (px::has_row_table(st.fetch)) {
-              const float4 t4 = f.row_states[f.rs_base[ci] + uint32_t(y - int(f.cmd_yr[ci] & 0xFFFFu))];
-              rs.f0 = t4.x; rs.f1 = t4.y; rs.f2 = t4.z;
-            }
-            else {
-              rs = px::row_state(st, y, fetch_y0);
-            }
-            uint32_t n = 0;
-            // one copy of the fetch + composite code: the 4 pixels rotate through slot 0
+          uint32_t n = 0;
+          // one copy of the fetch + composite code: the 4 pixels rotate through slot 0
 #pragma unroll 1
-            for (int k = 0; k < 4; k++) {
-              if (m[0] && xp + k < cv.w) {
-                uint32_t sv = px::fetch(st, rs, xp + k, f.luts, f.images);
-                pix[0] = px::composite(pix[0], sv, m[0], src_copy);
-                n++;
-              }
-              uint32_t tp = pix[0]; pix[0] = pix[1]; pix[1] = pix[2]; pix[2] = pix[3]; pix[3] = tp;
-              uint32_t tm = m[0]; m[0] = m[1]; m[1] = m[2]; m[2] = m[3]; m[3] = tm;
+          for (int k = 0; k < 4; k++) {
+            if (m[0] && xp + k < cv.w) {
+              uint32_t sv = px::fetch(st, rs, xp + k, f.luts, f.images);
+              pix[0] = px::composite(pix[0], sv, m[0], src_copy);
+              n++;
             }
-            ops += n;
-            pat_ops += st.fetch >= kFetchPatAlignedPad ? n : 0u;
+            uint32_t tp = pix[0]; pix[0] = pix[1]; pix[1] = pix[2]; pix[2] = pix[3]; pix[3] = tp;
+            uint32_t tm = m[0]; m[0] = m[1]; m[1] = m[2]; m[2] = m[3]; m[3] = tm;
           }
+          ops += n;
+          pat_ops += st.fetch >= kFetchPatAlignedPad ? n : 0u;
         }
-        __syncwarp();
       }
     }
 
@@ -934,6 +956,24 @@ int fine_grid_size() {
     grid = sms * (per_sm > 0 ? per_sm : 1);
   }
   return grid;
+}
+
+int launch_coverage(const FrameView& f, cudaStream_t st) {
+  if (!f.num_cmdrows) return 0;
+  static int grid = 0;
+  const int smem = int(sizeof(CoverShared)) * kFineWarps;
+  if (!grid) {
+    cudaFuncSetAttribute(coverage_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coverage_kernel, kFineThreads, smem);
+    grid = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  uint32_t groups = (f.num_cmdrows + kSlotGroup - 1) / kSlotGroup;
+  uint32_t blocks = (groups + kFineWarps - 1) / kFineWarps;
+  coverage_kernel<<<blocks < uint32_t(grid) ? blocks : uint32_t(grid), kFineThreads, smem, st>>>(f);
+  return 1;
 }
 
 int launch_row_states(const FrameView& f, cudaStream_t st) {

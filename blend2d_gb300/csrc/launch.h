@@ -22,6 +22,7 @@ int launch_rows_and_tiles(const FrameView& f, uint32_t* row_canvas, cudaStream_t
 int launch_fine(const FrameView& f, cudaStream_t st);
 int launch_row_states(const FrameView& f, cudaStream_t st);
 int launch_backdrop_prefix(const FrameView& f, cudaStream_t st);
+int launch_coverage(const FrameView& f, cudaStream_t st);
 int fine_grid_size();
 
 }  // namespace blgpu

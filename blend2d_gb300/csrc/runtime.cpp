@@ -361,6 +361,7 @@ int Runtime::enqueue_render_half(cudaStream_t st, bool timed) {
   k += launch_seg_bin(f, 1, st);
   k += launch_rows_and_tiles(f, row_canvas, st);
   k += launch_row_states(f, st);
+  k += launch_coverage(f, st);
   if (timed) cudaEventRecord(ev[1], st);
   k += launch_fine(f, st);
   if (timed) cudaEventRecord(ev[2], st);
@@ -424,6 +425,7 @@ BLGpuResult Runtime::run(const Frame& fr) {
     view.cmdrow_cursor = L.take<uint32_t>(totals.cmdrows + 1);
     view.seglist = L.take<uint32_t>(totals.seglist + 1);
     view.backdrop = L.take<uint32_t>((size_t(totals.cmdrows) + 1) * kStripRows);
+    view.masks = L.take<uint8_t>((size_t(totals.cmdrows) + 1) * kStripRows * kTileW);
     view.row_cmds = L.take<uint32_t>(totals.row_entries + 1);
     view.row_states = L.take<float4>(totals.row_states + 1);
   };

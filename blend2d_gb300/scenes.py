@@ -351,6 +351,28 @@ def patterns(seed: int = 3, width: int = 4096, height: int = 4096, count: int = 
     return sw
 
 
+def _mixed_canvas(rng, w: int, h: int, n: int) -> StreamWriter:
+    """Opaque-black canvas with `n` paths of the polygon kind (10-vertex polygon, solid colour) or
+    the curve kind (closed cubic path, gradient), mixed comp-ops and fill rules."""
+    sw = StreamWriter(w, h)
+    sw.solid(0xFF000000)
+    sw.fill_all()
+    for _ in range(n):
+        side = float(min(_log_uniform(rng, 8.0, 256.0), max(w, h)))
+        x0 = float(rng.uniform(-side * 0.25, max(w - side * 0.75, 1.0)))
+        y0 = float(rng.uniform(-side * 0.25, max(h - side * 0.75, 1.0)))
+        sw.comp_op(int(rng.integers(0, 2)))
+        sw.fill_rule(int(rng.integers(0, 2)))
+        if rng.integers(0, 2) == 0:
+            sw.solid(int(rng.integers(0, 2**32, dtype=np.uint64)))
+            sw.fill_polygon(rng.uniform(0, side, (10, 2)) + np.array([x0, y0]))
+        else:
+            _gradient_style(rng, sw, x0, y0, side)
+            cmds, xy = _cubic_path(rng, x0, y0, side, int(rng.integers(4, 13)))
+            sw.fill_path(cmds, xy)
+    return sw
+
+
 def batch_canvases(seed: int = 4, count: int = 4096, min_side: int = 32, max_side: int = 2048,
                    min_paths: int = 10, max_paths: int = 5000, scale: float = 1.0):
     """Independent canvases for the batched renderer: width and height log-uniform in
@@ -362,23 +384,21 @@ def batch_canvases(seed: int = 4, count: int = 4096, min_side: int = 32, max_sid
         w = int(_log_uniform(rng, min_side, max_side))
         h = int(_log_uniform(rng, min_side, max_side))
         n = max(1, int(_log_uniform(rng, min_paths, max_paths) * scale))
-        sw = StreamWriter(w, h)
-        sw.solid(0xFF000000)
-        sw.fill_all()
-        for _ in range(n):
-            side = float(min(_log_uniform(rng, 8.0, 256.0), max(w, h)))
-            x0 = float(rng.uniform(-side * 0.25, max(w - side * 0.75, 1.0)))
-            y0 = float(rng.uniform(-side * 0.25, max(h - side * 0.75, 1.0)))
-            sw.comp_op(int(rng.integers(0, 2)))
-            sw.fill_rule(int(rng.integers(0, 2)))
-            if rng.integers(0, 2) == 0:
-                sw.solid(int(rng.integers(0, 2**32, dtype=np.uint64)))
-                sw.fill_polygon(rng.uniform(0, side, (10, 2)) + np.array([x0, y0]))
-            else:
-                _gradient_style(rng, sw, x0, y0, side)
-                cmds, xy = _cubic_path(rng, x0, y0, side, int(rng.integers(4, 13)))
-                sw.fill_path(cmds, xy)
-        out.append(sw)
+        out.append(_mixed_canvas(rng, w, h, n))
+    return out
+
+
+def serving_requests(seed: int = 5, count: int = 32, min_side: int = 64, max_side: int = 4096,
+                     min_paths: int = 1, max_paths: int = 20000, scale: float = 1.0):
+    """Render requests for the serving loop: square canvases with side log-uniform in
+    [min_side, max_side] and log-uniform path counts in [min_paths, max_paths] (times `scale`),
+    paths of the polygon and curve kinds with mixed styles."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for _ in range(count):
+        side = int(_log_uniform(rng, min_side, max_side))
+        n = max(1, int(_log_uniform(rng, min_paths, max_paths) * scale))
+        out.append(_mixed_canvas(rng, side, side, n))
     return out
 
 
