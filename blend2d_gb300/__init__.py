@@ -23,6 +23,7 @@ ERROR_INVALID_VALUE = 0x00010001
 ERROR_INVALID_STATE = 0x00010002
 ERROR_NOT_IMPLEMENTED = 0x00010007
 ERROR_NO_STATES_TO_RESTORE = 0x00010038
+ERROR_DATA_TOO_LARGE = 0x00010032
 ERROR_DEVICE = 0x00011000
 
 FORMAT_PRGB32 = 1
@@ -113,6 +114,7 @@ _SIGNATURES = {
     "blgpu_context_submit_stream": [_P, ctypes.c_char_p, ctypes.c_size_t],
     "blgpu_render_batch": [_P, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(Image),
                            _U32],
+    "blgpu_render_stream_noalloc": [_P, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(Image)],
 }
 
 _lock = threading.Lock()
@@ -206,6 +208,12 @@ class Runtime:
 
     def synchronize(self):
         _check(self._lib.blgpu_runtime_synchronize(self.handle), "blgpu_runtime_synchronize")
+
+    def render_stream_noalloc(self, stream: bytes, device_target) -> None:
+        """Renders `stream` into a CUDA tensor without any allocating call (fixed scratch area)."""
+        img, _keep = make_image(device_target)
+        _check(self._lib.blgpu_render_stream_noalloc(self.handle, stream, len(stream), ctypes.byref(img)),
+               "blgpu_render_stream_noalloc", self.handle)
 
     def render_batch(self, streams: list[bytes], targets: list) -> None:
         """Renders each stream into its target (numpy or torch image) in one device pipeline."""

@@ -13,6 +13,7 @@
 #include <string.h>
 
 #include <deque>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -751,4 +752,33 @@ BLGPU_API BLGpuResult blgpu_render_batch(BLGpuRuntime* rt, const void* const* st
   if (frame.cmds.empty()) return BLGPU_SUCCESS;
   BLGpuContext::mark_uploads(frame);
   return rt->rt.run(frame);
+}
+
+// No-allocation variant: the stream is recorded on the host into a one-canvas frame, then run
+// entirely inside the device's fixed scratch area (Runtime::run_noalloc).
+BLGPU_API BLGpuResult blgpu_render_stream_noalloc(BLGpuRuntime* rt, const void* stream, size_t size,
+                                                  const BLGpuImage* device_image) {
+  static std::mutex lock;   // one scratch area per device: calls in this process take turns
+  if (!rt || !stream || !device_image) return BLGPU_ERROR_INVALID_VALUE;
+  const BLGpuImage& im = *device_image;
+  if (!(im.flags & BLGPU_IMAGE_DEVICE_MEMORY) || im.format != BLGPU_FORMAT_PRGB32 || im.width <= 0 ||
+      im.height <= 0 || im.width > 65535 || im.height > 65535 || !im.pixel_data ||
+      im.stride < intptr_t(im.width) * 4 || (im.stride & 15) || (reinterpret_cast<uintptr_t>(im.pixel_data) & 15))
+    return BLGPU_ERROR_INVALID_VALUE;
+  std::lock_guard<std::mutex> guard(lock);
+  Frame frame;
+  BLGpuContext c;
+  c.rt = rt;
+  c.frame = &frame;
+  c.target = im;
+  c.w = im.width;
+  c.h = im.height;
+  c.bound = true;
+  c.canvas = frame.add_canvas(im, true);
+  c.reset_state();
+  BLGpuResult r = c.submit_stream(static_cast<const uint8_t*>(stream), size);
+  c.bound = false;
+  if (r) return r;
+  if (frame.cmds.empty()) return BLGPU_SUCCESS;
+  return rt->rt.run_noalloc(frame);
 }

@@ -14,6 +14,7 @@
 #include <atomic>
 
 #include "launch.h"
+#include "noalloc.h"
 
 namespace blgpu {
 
@@ -464,6 +465,147 @@ BLGpuResult Runtime::run(const Frame& fr) {
   stats.last_gpu_ms = ms;
   stats.last_fine_ms = fine_ms;
   return BLGPU_SUCCESS;
+}
+
+// One frame, one device-memory canvas, every device buffer carved out of the fixed scratch area
+// (noalloc.h): no allocating call at all. Inputs are copied straight from the frame's host vectors.
+// The runtime's own frame (kept for replay) is left untouched.
+BLGpuResult Runtime::run_noalloc(const Frame& fr) {
+  BLGPU_CHECK(cudaSetDevice(device));
+  if (fr.canvases.size() != 1 || !device_target_direct(fr.targets[0].image)) return BLGPU_ERROR_INVALID_VALUE;
+  void* arena = nullptr;
+  BLGPU_CHECK(noalloc_arena(device, &arena));
+  const uint32_t nc = uint32_t(fr.cmds.size());
+  const uint32_t item_capacity = uint32_t(std::min<size_t>(fr.verts.size() / 2 + 1, 0xFFFFFFF0u));   // <= one per vertex
+
+  FrameView v{};
+  uint32_t* a_cmdrow_per_cmd = nullptr;
+  uint32_t* a_row_canvas = nullptr;
+  uint32_t* a_scan_tmp = nullptr;
+  auto plan_fixed = [&](Layout& L) {
+    v.cmds_rw = L.take<DevCmd>(nc);
+    v.cmds = v.cmds_rw;
+    v.styles = L.take<DevStyle>(fr.styles.size());
+    v.xforms = L.take<DevXform>(fr.xforms.size());
+    v.canvases = L.take<DevCanvas>(1);
+    v.verts = L.take<double>(fr.verts.size());
+    v.path_cmds = L.take<uint8_t>(fr.path_cmds.size());
+    v.lut_jobs = L.take<DevLutJob>(fr.lut_jobs.size());
+    v.stops = L.take<DevStop>(fr.stops.size());
+    v.images = L.take<uint32_t>(fr.image_words);
+    v.luts = L.take<uint32_t>(fr.lut_words);
+    v.items = L.take<DevItem>(item_capacity);
+    v.cmd_bbox = L.take<int4>(nc);
+    v.cmd_tile_x = L.take<uint32_t>(nc);
+    v.cmd_tile_y = L.take<uint32_t>(nc);
+    v.cmd_xr = L.take<uint32_t>(nc);
+    v.cmd_yr = L.take<uint32_t>(nc);
+    a_cmdrow_per_cmd = L.take<uint32_t>(nc + 1);
+    v.cmdrow_base = L.take<uint32_t>(nc + 1);
+    v.row_counts = L.take<uint32_t>(fr.rows + 1);
+    v.row_offsets = L.take<uint32_t>(fr.rows + 1);
+    a_row_canvas = L.take<uint32_t>(fr.rows + 1);
+    v.tile_order = L.take<uint32_t>(fr.tiles + 1);
+    v.tile_canvas = L.take<uint32_t>(fr.tiles + 1);
+    v.work_counter = L.take<uint32_t>(kCounterWords);
+    v.totals = v.work_counter + 4;
+    v.error_flags = v.work_counter + 12;
+    v.pixel_ops = reinterpret_cast<unsigned long long*>(v.work_counter + 16);
+    v.rs_count = L.take<uint32_t>(nc + 1);
+    v.rs_base = L.take<uint32_t>(nc + 1);
+    a_scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, fr.rows + 1)));
+  };
+  Layout L;
+  L.base = static_cast<char*>(arena);
+  plan_fixed(L);
+  size_t fixed_end = align_up(L.off, 256);
+  if (fixed_end >= kNoAllocArenaBytes) return BLGPU_ERROR_DATA_TOO_LARGE;
+  // half of what is left holds segments (20 bytes each), the other half the binning lists
+  const size_t seg_bytes = ((kNoAllocArenaBytes - fixed_end) / 2) & ~size_t(255);
+  v.seg_capacity = uint32_t(seg_bytes / (sizeof(DevSeg) + sizeof(uint32_t)));
+  v.segs = reinterpret_cast<DevSeg*>(static_cast<char*>(arena) + fixed_end);
+  v.seg_meta = reinterpret_cast<uint32_t*>(static_cast<char*>(arena) + fixed_end + sizeof(DevSeg) * size_t(v.seg_capacity));
+  const size_t dyn_begin = fixed_end + seg_bytes;
+  v.item_capacity = item_capacity;
+  v.num_cmds = nc;
+  v.num_canvases = 1;
+  v.num_tiles = fr.tiles;
+  v.num_rows = fr.rows;
+  v.num_lut_jobs = uint32_t(fr.lut_jobs.size());
+
+  auto put = [&](const void* dev, const void* src, size_t bytes) -> cudaError_t {
+    if (!bytes) return cudaSuccess;
+    return cudaMemcpyAsync(const_cast<void*>(dev), src, bytes, cudaMemcpyHostToDevice, stream);
+  };
+  DevCanvas cv = fr.canvases[0];
+  const BLGpuImage& im = fr.targets[0].image;
+  cv.pixels = static_cast<uint32_t*>(im.pixel_data);
+  cv.stride = int32_t(im.stride / 4);
+  BLGPU_CHECK(put(v.cmds, fr.cmds.data(), sizeof(DevCmd) * nc));
+  BLGPU_CHECK(put(v.styles, fr.styles.data(), sizeof(DevStyle) * fr.styles.size()));
+  BLGPU_CHECK(put(v.xforms, fr.xforms.data(), sizeof(DevXform) * fr.xforms.size()));
+  BLGPU_CHECK(put(v.canvases, &cv, sizeof(DevCanvas)));
+  BLGPU_CHECK(put(v.verts, fr.verts.data(), sizeof(double) * fr.verts.size()));
+  BLGPU_CHECK(put(v.path_cmds, fr.path_cmds.data(), fr.path_cmds.size()));
+  BLGPU_CHECK(put(v.lut_jobs, fr.lut_jobs.data(), sizeof(DevLutJob) * fr.lut_jobs.size()));
+  BLGPU_CHECK(put(v.stops, fr.stops.data(), sizeof(DevStop) * fr.stops.size()));
+  for (const FrameImage& fi : fr.images) {
+    BLGPU_CHECK(cudaMemcpy2DAsync(const_cast<uint32_t*>(v.images) + fi.pool_offset, size_t(fi.w) * 4u, fi.pixels,
+                                  size_t(fi.stride), size_t(fi.w) * 4u, size_t(fi.h),
+                                  fi.device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
+  }
+
+  // the pipeline halves read the runtime's current view: point it at the arena for this call
+  const FrameView saved_view = view;
+  uint32_t* const saved[3] = {cmdrow_per_cmd, row_canvas, scan_tmp};
+  auto restore = [&]() {
+    view = saved_view;
+    cmdrow_per_cmd = saved[0]; row_canvas = saved[1]; scan_tmp = saved[2];
+  };
+  view = v;
+  cmdrow_per_cmd = a_cmdrow_per_cmd; row_canvas = a_row_canvas; scan_tmp = a_scan_tmp;
+
+  BLGpuResult r = BLGPU_SUCCESS;
+  do {
+    int launches = enqueue_count_half(stream);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host_totals, view.totals, 32, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) { r = cuda_result(e); break; }
+    FrameTotals t;
+    t.segs = host_totals[0];
+    t.seglist = host_totals[1];
+    t.cmdrows = host_totals[2];
+    t.row_entries = host_totals[3];
+    t.row_states = host_totals[4];
+    if (t.segs > view.seg_capacity) { r = BLGPU_ERROR_DATA_TOO_LARGE; break; }
+    Layout D;
+    D.base = static_cast<char*>(arena);
+    D.off = dyn_begin;
+    view.cmdrow_counts = D.take<uint32_t>(t.cmdrows + 1);
+    view.cmdrow_offsets = D.take<uint32_t>(t.cmdrows + 1 + scan_temp_words(t.cmdrows + 1));
+    view.cmdrow_cursor = D.take<uint32_t>(t.cmdrows + 1);
+    view.seglist = D.take<uint32_t>(t.seglist + 1);
+    view.backdrop = D.take<uint32_t>((size_t(t.cmdrows) + 1) * kStripRows);
+    view.masks = D.take<uint8_t>((size_t(t.cmdrows) + 1) * kStripRows * kTileW);
+    view.row_cmds = D.take<uint32_t>(t.row_entries + 1);
+    view.row_states = D.take<float4>(t.row_states + 1);
+    if (D.off > kNoAllocArenaBytes) { r = BLGPU_ERROR_DATA_TOO_LARGE; break; }
+    view.num_segs = t.segs;
+    view.num_cmdrows = t.cmdrows;
+    view.num_seglist = t.seglist;
+    view.num_row_states = t.row_states;
+    launches += enqueue_render_half(stream, false);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) { r = cuda_result(e); break; }
+    stats.fill_commands = nc;
+    stats.segments = t.segs;
+    stats.tiles = fr.tiles;
+    stats.kernel_launches = uint64_t(launches);
+  } while (false);
+  restore();
+  return r;
 }
 
 // Re-runs the last frame's device pipeline on its device-resident inputs and canvases (the

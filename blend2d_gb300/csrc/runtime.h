@@ -104,6 +104,9 @@ struct Runtime {
   BLGpuResult run(const Frame& fr);
   BLGpuResult replay(bool use_graph);
   BLGpuResult synchronize();
+  // Renders a one-canvas frame into its device-memory image using only the fixed device scratch
+  // area (noalloc.h). Blocking. Does not touch the frame kept for replay.
+  BLGpuResult run_noalloc(const Frame& fr);
 
  private:
   int enqueue_count_half(cudaStream_t st);

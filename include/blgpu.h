@@ -29,6 +29,7 @@ enum {
   BLGPU_ERROR_INVALID_STATE = 0x00010002u,   /* BL_ERROR_INVALID_STATE */
   BLGPU_ERROR_NOT_IMPLEMENTED = 0x00010007u, /* BL_ERROR_NOT_IMPLEMENTED */
   BLGPU_ERROR_NO_STATES_TO_RESTORE = 0x00010038u, /* BL_ERROR_NO_STATES_TO_RESTORE */
+  BLGPU_ERROR_DATA_TOO_LARGE = 0x00010032u,   /* BL_ERROR_DATA_TOO_LARGE */
   BLGPU_ERROR_DEVICE = 0x00011000u           /* CUDA failure (no reference counterpart) */
 };
 
@@ -150,6 +151,29 @@ BLGpuResult blgpu_context_submit_stream(BLGpuContext* ctx, const void* stream, s
  * into `images` in one device pipeline (one persistent launch over every canvas's tiles). */
 BLGpuResult blgpu_render_batch(BLGpuRuntime* rt, const void* const* streams, const size_t* sizes,
                                const BLGpuImage* images, uint32_t count);
+
+/* --- no-allocation variant --------------------------------------------------------------
+ * No counterpart in the reference (its raster context allocates band and cell buffers of its own).
+ *
+ * Renders one command stream (include/blgpu_stream.h) into `device_image`, a PRGB32 image in
+ * device memory (BLGPU_IMAGE_DEVICE_MEMORY, 16-byte aligned rows), on the runtime's stream,
+ * without any allocating call: no cudaMalloc/cudaFree, no pinned host allocation, no allocating
+ * library call. Every device buffer the pipeline needs is carved out of one fixed scratch area per
+ * device, a statically allocated 256-byte aligned array of 32 MiB whose address is looked up once
+ * per device (cudaGetSymbolAddress, with that device current) on the first call - make the first
+ * call before any stream capture. Pixels are identical to blgpu_context_submit_stream + end.
+ *
+ * Limit: the frame's data, LUTs, pattern images, segments and binning lists must fit in the 32 MiB
+ * area (a few thousand fills on a canvas up to about 2048 x 2048); larger frames return
+ * BLGPU_ERROR_DATA_TOO_LARGE and leave the image unchanged. Nothing in the area has to start at
+ * zero: the call clears every counter and list it accumulates into before use. The area is shared
+ * by every call on the device: calls that overlap in time (other threads or processes on the same
+ * device) race on it; in one process the calls are serialized on a lock. Blocking: returns when
+ * the image is written. For callers that must not allocate device memory while rendering, e.g. a
+ * renderer running next to a job that owns the device's memory pool, or a process whose memory
+ * budget is fixed up front. */
+BLGpuResult blgpu_render_stream_noalloc(BLGpuRuntime* rt, const void* stream, size_t size,
+                                        const BLGpuImage* device_image);
 
 #ifdef __cplusplus
 }
