@@ -658,11 +658,16 @@ __global__ void __launch_bounds__(kFineThreads) coverage_kernel(FrameView f) {
     }
     __syncwarp();
 
-    // sweep: lane covers row lane / 8, columns (lane % 8) * 4 .. + 3 of each slot
+    // sweep: lane covers row lane / 8, columns (lane % 8) * 4 .. + 3 of each slot. Slots without
+    // segments are skipped: their coverage is the backdrop alone, which the composite pass reads.
     const int prow = lane >> 3;
+    uint32_t fa = 0;                                   // lane g < ns: flags << 16 | alpha of slot g
+    if (lane < ns) fa = (f.cmds[cmd_of].flags << 16) | f.cmds[cmd_of].alpha;
+    const uint32_t nonempty = __ballot_sync(0xFFFFFFFFu, lane < ns && s_count != 0);
     for (int g = 0; g < ns; g++) {
-      const uint32_t c = __shfl_sync(0xFFFFFFFFu, cmd_of, g);
-      const uint32_t flags = f.cmds[c].flags, alpha = f.cmds[c].alpha;
+      const uint32_t gfa = __shfl_sync(0xFFFFFFFFu, fa, g);
+      if (!((nonempty >> g) & 1u)) continue;
+      const uint32_t flags = gfa >> 16, alpha = gfa & 0xFFFFu;
       const uint4 cv4 = *reinterpret_cast<const uint4*>(&ws.cells[g][lane * 4]);
       const uint32_t s4 = cv4.x + cv4.y + cv4.z + cv4.w;
       uint32_t inc = s4;
@@ -759,8 +764,16 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
           const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
           const uint32_t slot = f.cmdrow_base[ci] + (strip_row - ((f.cmd_yr[ci] & 0xFFFFu) >> kStripShift)) * ntx +
                                 (uint32_t(tx) - (ctx & 0xFFFFu));
-          const uint32_t mw = reinterpret_cast<const uint32_t*>(f.masks + size_t(slot) * kSlotPixels)[lane];
-          m[0] = mw & 0xFFu; m[1] = (mw >> 8) & 0xFFu; m[2] = (mw >> 16) & 0xFFu; m[3] = mw >> 24;
+          if (f.cmdrow_counts[slot]) {
+            const uint32_t mw = reinterpret_cast<const uint32_t*>(f.masks + size_t(slot) * kSlotPixels)[lane];
+            m[0] = mw & 0xFFu; m[1] = (mw >> 8) & 0xFFu; m[2] = (mw >> 16) & 0xFFu; m[3] = mw >> 24;
+          }
+          else {
+            // no segment reaches this slot: every pixel of a row has the row's carried-in coverage
+            const uint32_t rule = (cmd.flags & 2u) ? 0x1FFu : 0xFFFFFFFFu;
+            m[0] = px::calc_mask((256u << 9) + f.backdrop[size_t(slot) * kStripRows + prow], rule, alpha);
+            m[1] = m[2] = m[3] = m[0];
+          }
         }
         else if (kind == kFillBoxA) {
           bool in_y = y >= cmd.box[1] && y < cmd.box[3];
