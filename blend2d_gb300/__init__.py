@@ -70,6 +70,15 @@ class Pattern(ctypes.Structure):
                 ("transform", ctypes.POINTER(ctypes.c_double))]
 
 
+class LaunchConfig(ctypes.Structure):
+    _fields_ = [("cover_group", ctypes.c_int32), ("cover_blocks_per_sm", ctypes.c_int32),
+                ("fine_blocks_per_sm", ctypes.c_int32), ("edge_block", ctypes.c_int32),
+                ("cubic_blocks_per_sm", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("frames", ctypes.c_uint64), ("fill_commands", ctypes.c_uint64), ("segments", ctypes.c_uint64),
                 ("tiles", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("last_gpu_ms", ctypes.c_double),
@@ -87,6 +96,9 @@ _SIGNATURES = {
     "blgpu_runtime_get_stats": [_P, ctypes.POINTER(Stats)],
     "blgpu_runtime_replay": [_P, ctypes.c_int],
     "blgpu_runtime_synchronize": [_P],
+    "blgpu_runtime_get_launch_config": [_P, ctypes.POINTER(LaunchConfig)],
+    "blgpu_runtime_set_launch_config": [_P, ctypes.POINTER(LaunchConfig)],
+    "blgpu_runtime_autotune": [_P, _U32, ctypes.POINTER(LaunchConfig), ctypes.POINTER(ctypes.c_double)],
     "blgpu_context_create": [ctypes.POINTER(_P), _P],
     "blgpu_context_destroy": [_P],
     "blgpu_context_begin": [_P, ctypes.POINTER(Image)],
@@ -208,6 +220,21 @@ class Runtime:
 
     def synchronize(self):
         _check(self._lib.blgpu_runtime_synchronize(self.handle), "blgpu_runtime_synchronize")
+
+    def launch_config(self) -> LaunchConfig:
+        c = LaunchConfig()
+        _check(self._lib.blgpu_runtime_get_launch_config(self.handle, ctypes.byref(c)), "get_launch_config")
+        return c
+
+    def set_launch_config(self, config: LaunchConfig):
+        _check(self._lib.blgpu_runtime_set_launch_config(self.handle, ctypes.byref(config)), "set_launch_config")
+
+    def autotune(self, trials: int = 3) -> tuple[LaunchConfig, float]:
+        """Tunes the launch shapes on the last flushed frame; returns (best config, its ms)."""
+        c, ms = LaunchConfig(), ctypes.c_double()
+        _check(self._lib.blgpu_runtime_autotune(self.handle, trials, ctypes.byref(c), ctypes.byref(ms)),
+               "blgpu_runtime_autotune", self.handle)
+        return c, ms.value
 
     def render_stream_noalloc(self, stream: bytes, device_target) -> None:
         """Renders `stream` into a CUDA tensor without any allocating call (fixed scratch area)."""

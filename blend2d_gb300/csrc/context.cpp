@@ -673,6 +673,48 @@ BLGPU_API BLGpuResult blgpu_runtime_synchronize(BLGpuRuntime* rt) {
   return rt->rt.synchronize();
 }
 
+static void to_abi(const LaunchConfig& c, BLGpuLaunchConfig* out) {
+  *out = BLGpuLaunchConfig{};
+  out->cover_group = c.cover_group;
+  out->cover_blocks_per_sm = c.cover_blocks_per_sm;
+  out->fine_blocks_per_sm = c.fine_blocks_per_sm;
+  out->edge_block = c.edge_block;
+  out->cubic_blocks_per_sm = c.cubic_blocks_per_sm;
+}
+
+BLGPU_API BLGpuResult blgpu_runtime_get_launch_config(const BLGpuRuntime* rt, BLGpuLaunchConfig* out) {
+  if (!rt || !out) return BLGPU_ERROR_INVALID_VALUE;
+  to_abi(rt->rt.cfg, out);
+  return BLGPU_SUCCESS;
+}
+
+BLGPU_API BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BLGpuLaunchConfig* c) {
+  if (!rt || !c) return BLGPU_ERROR_INVALID_VALUE;
+  if ((c->cover_group != 8 && c->cover_group != 16) ||
+      (c->edge_block != 64 && c->edge_block != 128 && c->edge_block != 256) ||
+      c->cover_blocks_per_sm < 0 || c->fine_blocks_per_sm < 0 || c->cubic_blocks_per_sm < 0)
+    return BLGPU_ERROR_INVALID_VALUE;
+  LaunchConfig lc;
+  lc.cover_group = c->cover_group;
+  lc.cover_blocks_per_sm = c->cover_blocks_per_sm;
+  lc.fine_blocks_per_sm = c->fine_blocks_per_sm;
+  lc.edge_block = c->edge_block;
+  lc.cubic_blocks_per_sm = c->cubic_blocks_per_sm;
+  rt->rt.cfg = lc;
+  rt->rt.graph_valid = false;
+  return BLGPU_SUCCESS;
+}
+
+BLGPU_API BLGpuResult blgpu_runtime_autotune(BLGpuRuntime* rt, uint32_t trials, BLGpuLaunchConfig* best, double* best_ms) {
+  if (!rt) return BLGPU_ERROR_INVALID_VALUE;
+  LaunchConfig c;
+  double ms = 0.0;
+  BLGpuResult r = rt->rt.autotune(int(trials), &c, &ms);
+  if (best) to_abi(c, best);
+  if (best_ms) *best_ms = ms;
+  return r;
+}
+
 BLGPU_API BLGpuResult blgpu_context_create(BLGpuContext** out, BLGpuRuntime* rt) {
   if (!out || !rt) return BLGPU_ERROR_INVALID_VALUE;
   BLGpuContext* c = new (std::nothrow) BLGpuContext();

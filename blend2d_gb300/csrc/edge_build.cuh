@@ -24,9 +24,16 @@ __device__ __forceinline__ double dmax(double a, double b) { return a < b ? b : 
 __device__ __forceinline__ double dclamp(double a, double lo, double hi) { return dmin(hi, dmax(lo, a)); }
 
 // x86 cvttsd2si: truncation, INT_MIN for NaN / out-of-range (the reference is an x86-64 build).
+// Done on the bits with integer instructions: |x| < 1 -> 0; exponent >= 31 (|x| >= 2^31, inf,
+// NaN) -> INT_MIN, which is also the right value for the only in-range case there, -2^31 <= x <
+// -2^31 + 1; otherwise the mantissa shifted by the exponent, negated for negative x.
 __device__ __forceinline__ int trunc_i(double x) {
-  if (!(x > -2147483649.0 && x < 2147483648.0)) return INT32_MIN;
-  return __double2int_rz(x);
+  const uint64_t b = uint64_t(__double_as_longlong(x));
+  const int e = int((b >> 52) & 0x7FFu) - 1023;
+  if (e < 0) return 0;
+  if (e >= 31) return INT32_MIN;
+  const uint32_t v = uint32_t(((b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull) >> (52 - e));
+  return (b >> 63) ? -int(v) : int(v);
 }
 
 // Segment sink: buffers emitted segments and appends them to the frame's segment array in

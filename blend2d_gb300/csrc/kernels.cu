@@ -309,16 +309,141 @@ __global__ void classify_kernel(FrameView f) {
       return;
     }
   }
-  uint32_t count = 0;
-  for_each_item(pc, n, [&](uint32_t, int, int) { count++; });
-  uint32_t base = atomicAdd(f.work_counter + 1, count);
+  // Cubic curves with all four points inside the clip box go to their own list (built by
+  // edge_cubics_kernel); everything else is built by edge_items_kernel.
+  const DevXform xf = f.xforms[cmd.xform];
+  const double* xy = f.verts + 2ull * cmd.geom_first;
+  const DevCanvas& cv = f.canvases[cmd.canvas];
+  const double cx1 = double(cv.w) * 256.0, cy1 = double(cv.h) * 256.0;
+  auto inside = [&](int k) {
+    double x = xy[2 * k], y = xy[2 * k + 1], tx, ty;
+    if (xf.affine) { tx = x * xf.m[0] + y * xf.m[2] + xf.m[4]; ty = x * xf.m[1] + y * xf.m[3] + xf.m[5]; }
+    else { tx = x * xf.m[0] + xf.m[4]; ty = y * xf.m[3] + xf.m[5]; }
+    return (tx >= 0.0) & (tx <= cx1) & (ty >= 0.0) & (ty <= cy1);
+  };
+  auto unclipped_cubic = [&](uint32_t kind, int a, int b) {
+    return kind == kItemCubic && inside(a) && inside(b) && inside(b + 1) && inside(b + 2);
+  };
+  uint32_t count = 0, cubics = 0;
   for_each_item(pc, n, [&](uint32_t kind, int a, int b) {
-    if (base < f.item_capacity) f.items[base] = DevItem{c, kind, uint32_t(a), uint32_t(b)};
-    base++;
+    if (unclipped_cubic(kind, a, b)) cubics++; else count++;
+  });
+  uint32_t base = count ? atomicAdd(f.work_counter + 1, count) : 0u;
+  uint32_t cbase = cubics ? atomicAdd(f.work_counter + 2, cubics) : 0u;
+  for_each_item(pc, n, [&](uint32_t kind, int a, int b) {
+    const DevItem it{c, kind, uint32_t(a), uint32_t(b)};
+    if (unclipped_cubic(kind, a, b)) {
+      if (cbase < f.item_capacity) f.cubic_items[cbase] = it;
+      cbase++;
+    }
+    else {
+      if (base < f.item_capacity) f.items[base] = it;
+      base++;
+    }
   });
 }
 
-__global__ void edge_items_kernel(FrameView f) {
+// Unclipped cubic curves (classify's second list): split into monotonic pieces and flattened with
+// the reference's safe flattener (flatten_safe, edgebuilder_p.h:2029-2445), but scheduled per
+// lane: every lane advances its own curve by one subdivision step per iteration of a warp-wide
+// loop and takes the next curve from the list as soon as its current one is done, so the lanes
+// stay busy whatever the curves' subdivision depths. Each curve's segments are the same as when
+// it is built alone.
+__global__ void __launch_bounds__(128) edge_cubics_kernel(FrameView f) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t n_items = min(f.work_counter[2], f.item_capacity);
+  const double tol = 0.20 * 256.0;
+  eb::Builder b;
+  b.tol_sq = tol * tol;
+  b.px = b.py = 0; b.psign = 0; b.pasc = false;
+  b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, 0u);
+  eb::Mono<3> mc;
+  mc.tol_sq = b.tol_sq;
+  mc.sp = 0;
+  eb::Pt spline[25];
+  int nout = 0, piece = 0;
+  bool busy = false, exhausted = false;
+  uint32_t cur = 0, rows = 0;
+
+  auto start_piece = [&]() {
+    const eb::Pt* sp = spline + piece;
+    uint32_t sign = sp[0].y > sp[3].y;
+    mc.begin(sp, sign);
+    if (mc.ltr()) mc.bound_ltr(); else mc.bound_rtl();
+    b.desc_open(eb::trunc_i(mc.first().x), eb::trunc_i(mc.first().y), sign);
+  };
+
+  for (;;) {
+    // hand the next curves of the list to the idle lanes (one atomic per warp)
+    const uint32_t want = __ballot_sync(0xFFFFFFFFu, !busy && !exhausted);
+    if (want) {
+      const int leader = __ffs(want) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(f.work_counter + 3, uint32_t(__popc(want)));
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (!busy && !exhausted) {
+        const uint32_t t = base + uint32_t(__popc(want & ((1u << lane) - 1u)));
+        if (t >= n_items) {
+          exhausted = true;
+        }
+        else {
+          const DevItem it = f.cubic_items[t];
+          const DevCmd& cmd = f.cmds[it.cmd];
+          const DevXform& xf = f.xforms[cmd.xform];
+          eb::Src src;
+          src.xy = f.verts + 2ull * cmd.geom_first;
+          src.affine = xf.affine != 0;
+          src.m00 = xf.m[0]; src.m01 = xf.m[1]; src.m10 = xf.m[2]; src.m11 = xf.m[3]; src.m20 = xf.m[4]; src.m21 = xf.m[5];
+          spline[0] = src.tf(int(it.a));
+          spline[1] = src.tf(int(it.b));
+          spline[2] = src.tf(int(it.b) + 1);
+          spline[3] = src.tf(int(it.b) + 2);
+          nout = eb::split_cubic(spline);
+          if (nout == 0) nout = 3;
+          piece = 0;
+          cur = it.cmd;
+          b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, cur);
+          start_piece();
+          busy = true;
+        }
+      }
+    }
+    if (__all_sync(0xFFFFFFFFu, !busy)) break;     // every lane idle: the list is exhausted
+    if (busy) {
+      eb::Step st;
+      if (!mc.is_flat(st) && mc.can_push()) {
+        mc.split(st);
+        mc.push(st);
+      }
+      else {
+        b.add(eb::trunc_i(mc.last().x), eb::trunc_i(mc.last().y));
+        if (mc.can_pop()) {
+          mc.pop();
+        }
+        else if ((piece += 3) < nout) {
+          start_piece();
+        }
+        else {
+          b.sink.flush();
+          if (b.sink.n) {
+            int4* bb = f.cmd_bbox + cur;
+            atomicMin(&bb->x, b.sink.xmin);
+            atomicMin(&bb->y, b.sink.ymin);
+            atomicMax(&bb->z, b.sink.xmax);
+            atomicMax(&bb->w, b.sink.ymax);
+            atomicOr(&f.cmds_rw[cur].status, kCmdHasSegments);
+            rows += b.sink.rows;
+          }
+          busy = false;
+        }
+      }
+    }
+  }
+  rows = __reduce_add_sync(0xFFFFFFFFu, rows);
+  if (lane == 0 && rows) atomicAdd(f.totals + 1, rows);
+}
+
+__global__ void __launch_bounds__(256) edge_items_kernel(FrameView f) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t rows = 0;
   uint32_t n_items = min(f.work_counter[1], f.item_capacity);
@@ -586,9 +711,9 @@ __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
 
 constexpr int kStripsPerTile = kTileH / kStripRows;
 constexpr int kFineWarps = kFineThreads / 32;
-constexpr int kSlotGroup = 16;
 constexpr int kSlotPixels = kStripRows * kTileW;
 
+template<int kSlotGroup>
 struct alignas(16) CoverShared {
   uint32_t cells[kSlotGroup][kSlotPixels];
   uint32_t backdrop[kSlotGroup][kStripRows];
@@ -597,11 +722,13 @@ struct alignas(16) CoverShared {
   int32_t x_base[kSlotGroup];
   int32_t row0[kSlotGroup];
 };
-static_assert(sizeof(CoverShared) % 16 == 0, "per-warp shared state must keep 16-byte alignment");
+static_assert(sizeof(CoverShared<8>) % 16 == 0 && sizeof(CoverShared<16>) % 16 == 0,
+              "per-warp shared state must keep 16-byte alignment");
 
+template<int kSlotGroup>
 __global__ void __launch_bounds__(kFineThreads) coverage_kernel(FrameView f) {
   extern __shared__ __align__(16) unsigned char cover_smem[];
-  CoverShared& ws = reinterpret_cast<CoverShared*>(cover_smem)[threadIdx.x >> 5];
+  CoverShared<kSlotGroup>& ws = reinterpret_cast<CoverShared<kSlotGroup>*>(cover_smem)[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   const uint32_t num_groups = (f.num_cmdrows + kSlotGroup - 1) / kSlotGroup;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
@@ -750,44 +877,77 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
         hit = (bx & 0xFFFFu) <= (strip_x >> 16) && (bx >> 16) >= (strip_x & 0xFFFFu) &&
               (by & 0xFFFFu) <= (strip_y >> 16) && (by >> 16) >= (strip_y & 0xFFFFu);
       }
-      uint32_t ballot = __ballot_sync(0xFFFFFFFFu, hit);
-      while (ballot) {
-        const int bit = __ffs(ballot) - 1;
-        ballot &= ballot - 1;
-        const uint32_t ci = __shfl_sync(0xFFFFFFFFu, c, bit);
-        const DevCmd& cmd = f.cmds[ci];
-        const uint32_t kind = cmd.kind;
-        const uint32_t alpha = cmd.alpha;
-        uint32_t m[4];
+      const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, hit);
+      if (!ballot) continue;
+      // Each hit lane fetches its command's metadata in parallel (one command per lane), so the
+      // painter's-order loop below only waits on the mask words.
+      uint32_t kind = 0, slot = 0xFFFFFFFFu, nseg = 0, meta = 0;   // meta: flags << 16 | alpha
+      if (hit) {
+        const DevCmd& hc = f.cmds[c];
+        kind = hc.kind;
+        meta = (hc.flags << 16) | hc.alpha;
         if (kind == kFillAnalytic) {
-          const uint32_t ctx = f.cmd_tile_x[ci];
+          const uint32_t ctx = f.cmd_tile_x[c];
           const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
-          const uint32_t slot = f.cmdrow_base[ci] + (strip_row - ((f.cmd_yr[ci] & 0xFFFFu) >> kStripShift)) * ntx +
-                                (uint32_t(tx) - (ctx & 0xFFFFu));
-          if (f.cmdrow_counts[slot]) {
-            const uint32_t mw = reinterpret_cast<const uint32_t*>(f.masks + size_t(slot) * kSlotPixels)[lane];
+          slot = f.cmdrow_base[c] + (strip_row - ((f.cmd_yr[c] & 0xFFFFu) >> kStripShift)) * ntx + (uint32_t(tx) - (ctx & 0xFFFFu));
+          nseg = f.cmdrow_counts[slot];
+        }
+      }
+      uint32_t todo = ballot;
+      // the first command's mask word, then each next one's while the current one composites
+      int bit = __ffs(todo) - 1;
+      uint32_t next_mw = 0;
+      {
+        const uint32_t s0 = __shfl_sync(0xFFFFFFFFu, slot, bit), n0 = __shfl_sync(0xFFFFFFFFu, nseg, bit);
+        if (s0 != 0xFFFFFFFFu)
+          next_mw = n0 ? reinterpret_cast<const uint32_t*>(f.masks + size_t(s0) * kSlotPixels)[lane]
+                       : f.backdrop[size_t(s0) * kStripRows + prow];
+      }
+      while (todo) {
+        todo &= todo - 1;
+        const uint32_t ci = __shfl_sync(0xFFFFFFFFu, c, bit);
+        const uint32_t ckind = __shfl_sync(0xFFFFFFFFu, kind, bit);
+        const uint32_t cmeta = __shfl_sync(0xFFFFFFFFu, meta, bit);
+        const uint32_t cnseg = __shfl_sync(0xFFFFFFFFu, nseg, bit);
+        const uint32_t mw = next_mw;
+        if (todo) {
+          const int nb = __ffs(todo) - 1;
+          const uint32_t s1 = __shfl_sync(0xFFFFFFFFu, slot, nb), n1 = __shfl_sync(0xFFFFFFFFu, nseg, nb);
+          if (s1 != 0xFFFFFFFFu)
+            next_mw = n1 ? reinterpret_cast<const uint32_t*>(f.masks + size_t(s1) * kSlotPixels)[lane]
+                         : f.backdrop[size_t(s1) * kStripRows + prow];
+          bit = nb;
+        }
+        const uint32_t alpha = cmeta & 0xFFFFu;
+        uint32_t m[4];
+        if (ckind == kFillAnalytic) {
+          if (cnseg) {
             m[0] = mw & 0xFFu; m[1] = (mw >> 8) & 0xFFu; m[2] = (mw >> 16) & 0xFFu; m[3] = mw >> 24;
           }
           else {
             // no segment reaches this slot: every pixel of a row has the row's carried-in coverage
-            const uint32_t rule = (cmd.flags & 2u) ? 0x1FFu : 0xFFFFFFFFu;
-            m[0] = px::calc_mask((256u << 9) + f.backdrop[size_t(slot) * kStripRows + prow], rule, alpha);
+            const uint32_t rule = ((cmeta >> 16) & 2u) ? 0x1FFu : 0xFFFFFFFFu;
+            m[0] = px::calc_mask((256u << 9) + mw, rule, alpha);
             m[1] = m[2] = m[3] = m[0];
           }
         }
-        else if (kind == kFillBoxA) {
-          bool in_y = y >= cmd.box[1] && y < cmd.box[3];
-#pragma unroll
-          for (int k = 0; k < 4; k++) m[k] = (in_y && xp + k >= cmd.box[0] && xp + k < cmd.box[2]) ? alpha : 0u;
-        }
         else {
+          const DevCmd& cmd = f.cmds[ci];
+          if (ckind == kFillBoxA) {
+            bool in_y = y >= cmd.box[1] && y < cmd.box[3];
 #pragma unroll
-          for (int k = 0; k < 4; k++) m[k] = px::box_u_mask(cmd.box, alpha, xp + k, y);
+            for (int k = 0; k < 4; k++) m[k] = (in_y && xp + k >= cmd.box[0] && xp + k < cmd.box[2]) ? alpha : 0u;
+          }
+          else {
+#pragma unroll
+            for (int k = 0; k < 4; k++) m[k] = px::box_u_mask(cmd.box, alpha, xp + k, y);
+          }
         }
 
         if (row_ok && (m[0] | m[1] | m[2] | m[3])) {
+          const DevCmd& cmd = f.cmds[ci];
           const DevStyle& st = f.styles[cmd.style];
-          const bool src_copy = (cmd.flags & 1u) != 0;
+          const bool src_copy = (cmeta >> 16) & 1u;
           px::RowState rs;
           if (px::has_row_table(st.fetch)) {
             const float4 t4 = f.row_states[f.rs_base[ci] + uint32_t(y - int(f.cmd_yr[ci] & 0xFFFFu))];
@@ -795,7 +955,7 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
           }
           else {
             // the reference initializes its fetcher at the start of each band of an analytic fill
-            int fetch_y0 = kind == kFillAnalytic ? max(cmd.box[1], (y / cv.band_height) * cv.band_height) : cmd.fetch_y0;
+            int fetch_y0 = ckind == kFillAnalytic ? max(cmd.box[1], (y / cv.band_height) * cv.band_height) : cmd.fetch_y0;
             rs = px::row_state(st, y, fetch_y0);
           }
           uint32_t n = 0;
@@ -932,11 +1092,24 @@ int launch_lut(const FrameView& f, cudaStream_t st) {
   return 1;
 }
 
-int launch_edges(const FrameView& f, cudaStream_t st) {
+int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   if (!f.num_cmds) return 0;
+  static int sms = 0, max_per_sm = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, edge_cubics_kernel, 128, 0);
+    if (max_per_sm < 1) max_per_sm = 1;
+  }
+  const int per_sm = cfg.cubic_blocks_per_sm > 0 && cfg.cubic_blocks_per_sm < max_per_sm ? cfg.cubic_blocks_per_sm : max_per_sm;
+  const uint32_t eb = cfg.edge_block == 64 || cfg.edge_block == 256 ? uint32_t(cfg.edge_block) : 128u;
   classify_kernel<<<cdiv(f.num_cmds, 128), 128, 0, st>>>(f);
-  edge_items_kernel<<<cdiv(f.item_capacity ? f.item_capacity : 1, 128), 128, 0, st>>>(f);
-  return 2;
+  edge_items_kernel<<<cdiv(f.item_capacity ? f.item_capacity : 1, eb), eb, 0, st>>>(f);
+  uint32_t grid = cdiv(f.item_capacity ? f.item_capacity : 1, 128);
+  uint32_t cubic_grid = uint32_t(sms * per_sm);
+  edge_cubics_kernel<<<grid < cubic_grid ? grid : cubic_grid, 128, 0, st>>>(f);
+  return 3;
 }
 
 int launch_cmd_tiles(const FrameView& f, uint32_t* cmdrow_counts_per_cmd, cudaStream_t st) {
@@ -959,34 +1132,42 @@ int launch_rows_and_tiles(const FrameView& f, uint32_t* row_canvas, cudaStream_t
   return k;
 }
 
-int fine_grid_size() {
-  static int grid = 0;
-  if (!grid) {
-    int dev = 0, sms = 0, per_sm = 0;
+int fine_grid_size(int blocks_per_sm) {
+  static int sms = 0, max_per_sm = 0;
+  if (!sms) {
+    int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fine_kernel, kFineThreads, 0);
-    grid = sms * (per_sm > 0 ? per_sm : 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, fine_kernel, kFineThreads, 0);
+    if (max_per_sm < 1) max_per_sm = 1;
   }
-  return grid;
+  return sms * (blocks_per_sm > 0 && blocks_per_sm < max_per_sm ? blocks_per_sm : max_per_sm);
 }
 
-int launch_coverage(const FrameView& f, cudaStream_t st) {
-  if (!f.num_cmdrows) return 0;
-  static int grid = 0;
-  const int smem = int(sizeof(CoverShared)) * kFineWarps;
-  if (!grid) {
-    cudaFuncSetAttribute(coverage_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    int dev = 0, sms = 0, per_sm = 0;
+template<int G>
+static int launch_coverage_g(const FrameView& f, cudaStream_t st, int blocks_per_sm) {
+  static int sms = 0, max_per_sm = 0;
+  const int smem = int(sizeof(CoverShared<G>)) * kFineWarps;
+  if (!sms) {
+    cudaFuncSetAttribute(coverage_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coverage_kernel, kFineThreads, smem);
-    grid = sms * (per_sm > 0 ? per_sm : 1);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, coverage_kernel<G>, kFineThreads, smem);
+    if (max_per_sm < 1) max_per_sm = 1;
   }
-  uint32_t groups = (f.num_cmdrows + kSlotGroup - 1) / kSlotGroup;
+  int per_sm = blocks_per_sm > 0 && blocks_per_sm < max_per_sm ? blocks_per_sm : max_per_sm;
+  uint32_t groups = (f.num_cmdrows + G - 1) / G;
   uint32_t blocks = (groups + kFineWarps - 1) / kFineWarps;
-  coverage_kernel<<<blocks < uint32_t(grid) ? blocks : uint32_t(grid), kFineThreads, smem, st>>>(f);
+  uint32_t grid = uint32_t(sms * per_sm);
+  coverage_kernel<G><<<blocks < grid ? blocks : grid, kFineThreads, smem, st>>>(f);
   return 1;
+}
+
+int launch_coverage(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
+  if (!f.num_cmdrows) return 0;
+  if (cfg.cover_group == 8) return launch_coverage_g<8>(f, st, cfg.cover_blocks_per_sm);
+  return launch_coverage_g<16>(f, st, cfg.cover_blocks_per_sm);
 }
 
 int launch_row_states(const FrameView& f, cudaStream_t st) {
@@ -996,9 +1177,9 @@ int launch_row_states(const FrameView& f, cudaStream_t st) {
 }
 
 // work_counter must be zero on entry.
-int launch_fine(const FrameView& f, cudaStream_t st) {
+int launch_fine(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   if (!f.num_tiles) return 0;
-  int grid = fine_grid_size();
+  int grid = fine_grid_size(cfg.fine_blocks_per_sm);
   uint32_t max_blocks = (f.num_tiles * kStripsPerTile + kFineWarps - 1) / kFineWarps;
   if (uint32_t(grid) > max_blocks) grid = int(max_blocks);
   fine_kernel<<<grid, kFineThreads, 0, st>>>(f);

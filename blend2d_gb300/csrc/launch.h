@@ -9,20 +9,29 @@
 
 namespace blgpu {
 
+// Launch shapes the autotuner chooses between (0 = the default for that field).
+struct LaunchConfig {
+  int cover_group = 16;           // slots per warp in the coverage pass (8 or 16)
+  int cover_blocks_per_sm = 0;    // coverage grid: blocks per SM (0 = as many as fit)
+  int fine_blocks_per_sm = 0;     // composite grid: blocks per SM (0 = as many as fit)
+  int edge_block = 128;           // threads per block of the per-item edge builder (64/128/256)
+  int cubic_blocks_per_sm = 0;    // lane-scheduled cubic flattener: blocks per SM
+};
+
 int exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* tmp, cudaStream_t st);
 uint32_t scan_temp_words(uint32_t n);
 int launch_total(const uint32_t* counts, const uint32_t* offsets, uint32_t n, uint32_t* total, cudaStream_t st);
 int launch_sum(const uint32_t* in, uint32_t n, uint32_t* total, cudaStream_t st);
 
 int launch_lut(const FrameView& f, cudaStream_t st);
-int launch_edges(const FrameView& f, cudaStream_t st);
+int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st);
 int launch_cmd_tiles(const FrameView& f, uint32_t* cmdrow_counts_per_cmd, cudaStream_t st);
 int launch_seg_bin(const FrameView& f, int scatter, cudaStream_t st);
 int launch_rows_and_tiles(const FrameView& f, uint32_t* row_canvas, cudaStream_t st);
-int launch_fine(const FrameView& f, cudaStream_t st);
+int launch_fine(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st);
 int launch_row_states(const FrameView& f, cudaStream_t st);
 int launch_backdrop_prefix(const FrameView& f, cudaStream_t st);
-int launch_coverage(const FrameView& f, cudaStream_t st);
-int fine_grid_size();
+int launch_coverage(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st);
+int fine_grid_size(int blocks_per_sm);
 
 }  // namespace blgpu

@@ -202,6 +202,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
       if (cpix) (*cpix)[i] = p;
     }
     v.items = L.take<DevItem>(item_capacity);
+    v.cubic_items = L.take<DevItem>(item_capacity);
     v.cmd_bbox = L.take<int4>(nc);
     v.cmd_tile_x = L.take<uint32_t>(nc);
     v.cmd_tile_y = L.take<uint32_t>(nc);
@@ -338,7 +339,7 @@ int Runtime::enqueue_count_half(cudaStream_t st) {
   cudaMemsetAsync(f.work_counter, 0, sizeof(uint32_t) * kCounterWords, st);
   cudaMemsetAsync(f.row_counts, 0, sizeof(uint32_t) * (f.num_rows + 1), st);
   k += launch_lut(f, st);
-  k += launch_edges(f, st);
+  k += launch_edges(f, cfg, st);
   k += launch_cmd_tiles(f, cmdrow_per_cmd, st);
   k += exclusive_scan(cmdrow_per_cmd, f.cmdrow_base, f.num_cmds, scan_tmp, st);
   k += launch_total(cmdrow_per_cmd, f.cmdrow_base, f.num_cmds, f.totals + 2, st);
@@ -362,9 +363,9 @@ int Runtime::enqueue_render_half(cudaStream_t st, bool timed) {
   k += launch_seg_bin(f, 1, st);
   k += launch_rows_and_tiles(f, row_canvas, st);
   k += launch_row_states(f, st);
-  k += launch_coverage(f, st);
+  k += launch_coverage(f, cfg, st);
   if (timed) cudaEventRecord(ev[1], st);
-  k += launch_fine(f, st);
+  k += launch_fine(f, cfg, st);
   if (timed) cudaEventRecord(ev[2], st);
   return k;
 }
@@ -495,6 +496,7 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     v.images = L.take<uint32_t>(fr.image_words);
     v.luts = L.take<uint32_t>(fr.lut_words);
     v.items = L.take<DevItem>(item_capacity);
+    v.cubic_items = L.take<DevItem>(item_capacity);
     v.cmd_bbox = L.take<int4>(nc);
     v.cmd_tile_x = L.take<uint32_t>(nc);
     v.cmd_tile_y = L.take<uint32_t>(nc);
@@ -650,6 +652,80 @@ void Runtime::read_pixel_ops() {
   memcpy(v, host_totals + 8, sizeof(v));
   stats.pixel_ops = v[0];
   stats.pattern_ops = v[1];
+}
+
+// Launch-shape autotuner: coordinate descent over the LaunchConfig fields, each candidate timed
+// by replaying the last frame (median of `trials` eager replays, CUDA events). The canvases are
+// saved before and restored after, so the frame's pixels are unchanged.
+BLGpuResult Runtime::autotune(int trials, LaunchConfig* best_out, double* best_ms_out) {
+  if (!has_frame) return BLGPU_ERROR_INVALID_STATE;
+  BLGPU_CHECK(cudaSetDevice(device));
+  BLGPU_CHECK(cudaStreamSynchronize(stream));
+  if (trials < 1) trials = 3;
+  // save every canvas
+  size_t bytes = 0;
+  for (size_t i = 0; i < targets.size(); i++)
+    bytes += size_t(targets[i].image.height) * size_t(canvas_stride[i]) * 4u;
+  void* save = nullptr;
+  if (bytes) BLGPU_CHECK(cudaMalloc(&save, bytes));
+  auto copy_canvases = [&](bool to_save) -> cudaError_t {
+    size_t off = 0;
+    for (size_t i = 0; i < targets.size(); i++) {
+      size_t pitch = size_t(canvas_stride[i]) * 4u, h = size_t(targets[i].image.height);
+      char* a = static_cast<char*>(save) + off;
+      cudaError_t e = to_save ? cudaMemcpyAsync(a, canvas_dev[i], pitch * h, cudaMemcpyDeviceToDevice, stream)
+                              : cudaMemcpyAsync(canvas_dev[i], a, pitch * h, cudaMemcpyDeviceToDevice, stream);
+      if (e != cudaSuccess) return e;
+      off += pitch * h;
+    }
+    return cudaSuccess;
+  };
+  cudaError_t e = copy_canvases(true);
+  auto measure = [&](const LaunchConfig& c, double& ms) -> BLGpuResult {
+    cfg = c;
+    std::vector<double> t;
+    for (int k = 0; k < trials + 1; k++) {
+      BLGpuResult r = replay(false);
+      if (r) return r;
+      r = synchronize();
+      if (r) return r;
+      if (k) t.push_back(stats.last_gpu_ms);   // the first run warms caches and lazy set-up
+    }
+    std::sort(t.begin(), t.end());
+    ms = t[t.size() / 2];
+    return BLGPU_SUCCESS;
+  };
+  BLGpuResult r = e == cudaSuccess ? BLGPU_SUCCESS : cuda_result(e);
+  LaunchConfig best = cfg;
+  double best_ms = 0.0;
+  if (!r) r = measure(best, best_ms);
+  const int cover_groups[] = {8, 16};
+  const int blocks[] = {0, 1, 2, 3};
+  const int edge_blocks[] = {64, 128, 256};
+  for (int field = 0; field < 5 && !r; field++) {
+    const int* vals = field == 0 ? cover_groups : (field == 3 ? edge_blocks : blocks);
+    const int nvals = field == 0 ? 2 : (field == 3 ? 3 : 4);
+    for (int k = 0; k < nvals && !r; k++) {
+      LaunchConfig c = best;
+      int* slot = field == 0 ? &c.cover_group : field == 1 ? &c.cover_blocks_per_sm : field == 2 ? &c.fine_blocks_per_sm
+                : field == 3 ? &c.edge_block : &c.cubic_blocks_per_sm;
+      if (*slot == vals[k]) continue;
+      *slot = vals[k];
+      double ms = 0.0;
+      r = measure(c, ms);
+      if (!r && ms < best_ms) { best = c; best_ms = ms; }
+    }
+  }
+  cfg = best;
+  graph_valid = false;                         // a captured graph holds the old launch shapes
+  e = copy_canvases(false);
+  if (!r && e != cudaSuccess) r = cuda_result(e);
+  cudaError_t e2 = cudaStreamSynchronize(stream);
+  if (!r && e2 != cudaSuccess) r = cuda_result(e2);
+  if (save) cudaFree(save);
+  if (best_out) *best_out = best;
+  if (best_ms_out) *best_ms_out = best_ms;
+  return r;
 }
 
 BLGpuResult Runtime::synchronize() {

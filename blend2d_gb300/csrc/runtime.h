@@ -8,6 +8,7 @@
 
 #include "blgpu.h"
 #include "blgpu_internal.h"
+#include "launch.h"
 
 namespace blgpu {
 
@@ -97,6 +98,7 @@ struct Runtime {
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
 
   BLGpuStats stats{};
+  LaunchConfig cfg;
 
   BLGpuResult init(const BLGpuRuntimeCreateInfo* info);
   void destroy();
@@ -104,6 +106,8 @@ struct Runtime {
   BLGpuResult run(const Frame& fr);
   BLGpuResult replay(bool use_graph);
   BLGpuResult synchronize();
+  // Picks the fastest launch shapes for the last frame (its pixels are left unchanged).
+  BLGpuResult autotune(int trials, LaunchConfig* best, double* best_ms);
   // Renders a one-canvas frame into its device-memory image using only the fixed device scratch
   // area (noalloc.h). Blocking. Does not touch the frame kept for replay.
   BLGpuResult run_noalloc(const Frame& fr);

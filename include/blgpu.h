@@ -104,6 +104,18 @@ typedef struct BLGpuStats {
   int64_t last_cuda_error; /* cudaError_t behind the last BLGPU_ERROR_DEVICE (0 if none) */
 } BLGpuStats;
 
+/* Launch shapes of the device pipeline (0 in a *_blocks_per_sm field = as many as fit). Tile and
+ * band geometry are fixed by the pipeline (32-pixel tile columns matching a warp's lanes, the
+ * reference's band heights), so the tunable parameters are how work is grouped and gridded. */
+typedef struct BLGpuLaunchConfig {
+  int32_t cover_group;          /* (command, strip, tile) slots per warp in the coverage pass: 8 or 16 */
+  int32_t cover_blocks_per_sm;  /* coverage pass grid */
+  int32_t fine_blocks_per_sm;   /* composite pass grid */
+  int32_t edge_block;           /* threads per block of the per-item edge builder: 64, 128 or 256 */
+  int32_t cubic_blocks_per_sm;  /* lane-scheduled cubic flattener grid */
+  int32_t reserved[3];
+} BLGpuLaunchConfig;
+
 /* --- runtime (device, stream, memory) --------------------------------------------------- */
 BLGpuResult blgpu_runtime_create(BLGpuRuntime** out, const BLGpuRuntimeCreateInfo* info);
 BLGpuResult blgpu_runtime_destroy(BLGpuRuntime* rt);
@@ -112,6 +124,12 @@ BLGpuResult blgpu_runtime_get_stats(const BLGpuRuntime* rt, BLGpuStats* out);
  * host<->device traffic); `use_graph` replays it as a captured CUDA graph. */
 BLGpuResult blgpu_runtime_replay(BLGpuRuntime* rt, int use_graph);
 BLGpuResult blgpu_runtime_synchronize(BLGpuRuntime* rt);
+BLGpuResult blgpu_runtime_get_launch_config(const BLGpuRuntime* rt, BLGpuLaunchConfig* out);
+BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BLGpuLaunchConfig* config);
+/* Autotuner: times the last flushed frame's pipeline under candidate launch shapes (coordinate
+ * descent, median of `trials` replays each), keeps the fastest and reports it; the frame's pixels
+ * are restored afterwards. No counterpart in the reference (its pipelines are JIT-specialized). */
+BLGpuResult blgpu_runtime_autotune(BLGpuRuntime* rt, uint32_t trials, BLGpuLaunchConfig* best, double* best_ms);
 
 /* --- rendering context: bl_context_* ---------------------------------------------------- */
 /* bl_context_init + bl_context_begin (context.cpp:316-328): bind `image` as the target. */

@@ -251,3 +251,24 @@ def test_stats_and_errors(runtimes):
     ctx.close()
     st = rt.stats()
     assert st.frames >= 1 and st.fill_commands == 1
+
+
+def test_autotune_keeps_pixels_and_every_config_renders_the_same():
+    torch = pytest.importorskip("torch")
+    w, h = 320, 200
+    stream = scenes.random_mix(777, width=w, height=h, count=250).to_bytes()
+    want = oracle_lib.render(stream)
+    with bg.Runtime(0) as rt:
+        dev = torch.zeros((h, w), dtype=torch.int32, device="cuda")
+        bg.render_stream(rt, stream, dev)
+        best, ms = rt.autotune(trials=2)
+        torch.cuda.synchronize()
+        assert ms > 0 and best.cover_group in (8, 16) and best.edge_block in (64, 128, 256)
+        assert not _diff(dev.cpu().numpy().view(np.uint32), want)       # tuning left the pixels alone
+        for cfg in [dict(cover_group=8, edge_block=64, fine_blocks_per_sm=1, cover_blocks_per_sm=1, cubic_blocks_per_sm=1),
+                    dict(cover_group=16, edge_block=256, fine_blocks_per_sm=0, cover_blocks_per_sm=0, cubic_blocks_per_sm=0)]:
+            rt.set_launch_config(bg.LaunchConfig(**cfg))
+            got = bg.render_stream(rt, stream)
+            assert not _diff(got, want), cfg
+        with pytest.raises(bg.BLGpuError):
+            rt.set_launch_config(bg.LaunchConfig(cover_group=12, edge_block=128))
