@@ -84,7 +84,7 @@ class Stats(ctypes.Structure):
                 ("tiles", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("last_gpu_ms", ctypes.c_double),
                 ("last_fine_ms", ctypes.c_double), ("pixel_ops", ctypes.c_uint64), ("pattern_ops", ctypes.c_uint64),
                 ("input_vertices", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
-                ("last_cuda_error", ctypes.c_int64)]
+                ("last_cuda_error", ctypes.c_int64), ("last_composite_ms", ctypes.c_double)]
 
 
 _P = ctypes.c_void_p

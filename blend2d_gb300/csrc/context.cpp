@@ -26,6 +26,8 @@ using namespace blgpu;
 
 struct BLGpuRuntime {
   Runtime rt;
+  Frame batch_frame;               // reused by blgpu_render_batch (its page-locked arrays persist)
+  std::mutex batch_lock;
 };
 
 namespace {
@@ -129,7 +131,7 @@ struct BLGpuContext {
       job.lut_offset = frame->lut_words;
       job.lut_size = d.lut_size;
       job.variant = rt->rt.lut_variant;
-      frame->stops.insert(frame->stops.end(), cs.hs.stops.begin(), cs.hs.stops.end());
+      frame->stops.append(cs.hs.stops.data(), cs.hs.stops.size());
       frame->lut_jobs.push_back(job);
       d.lut_offset = frame->lut_words;
       frame->lut_words += d.lut_size;
@@ -243,9 +245,9 @@ struct BLGpuContext {
     c.geom_first = uint32_t(frame->verts.size() / 2);
     c.geom_count = uint32_t(n);
     c.xform = xform;
-    frame->verts.insert(frame->verts.end(), xy, xy + 2 * n);
-    if (cmds) frame->path_cmds.insert(frame->path_cmds.end(), cmds, cmds + n);
-    else frame->path_cmds.resize(frame->path_cmds.size() + n, uint8_t(0));
+    frame->verts.append(xy, 2 * n);
+    if (cmds) frame->path_cmds.append(cmds, n);
+    else frame->path_cmds.append_fill(n, uint8_t(0));
   }
 
   void fill_box_d(const Fill& f, double bx0, double by0, double bx1, double by1) {
@@ -385,8 +387,16 @@ struct BLGpuContext {
     return BLGPU_SUCCESS;
   }
 
+  // A new fill style: the previous one's registration is dropped, its stop storage reused.
+  void reset_style_slot() {
+    s.style.has_image = false;
+    s.style.image = BLGpuImage{};
+    s.style.frame_gen = 0;
+    s.style.frame_index = 0;
+  }
+
   BLGpuResult set_style_rgba32(uint32_t c) {
-    s.style = CtxStyle{};
+    reset_style_slot();
     style_solid(s.style.hs, c);
     return BLGPU_SUCCESS;
   }
@@ -400,7 +410,7 @@ struct BLGpuContext {
     d.stops = reinterpret_cast<const DevStop*>(g->stops);
     d.stop_count = g->stop_count;
     d.transform = g->transform;
-    s.style = CtxStyle{};
+    reset_style_slot();
     style_gradient(s.style.hs, d, s.final_t);
     return BLGPU_SUCCESS;
   }
@@ -424,7 +434,7 @@ struct BLGpuContext {
     memcpy(d.area, p->area, sizeof(d.area));
     d.extend = p->extend_mode;
     d.transform = p->transform;
-    s.style = CtxStyle{};
+    reset_style_slot();
     style_pattern(s.style.hs, d, s.pattern_quality, s.final_t);
     if (!s.style.hs.nop) {
       s.style.has_image = true;
@@ -505,6 +515,16 @@ struct BLGpuContext {
   }
 
   BLGpuResult submit_stream(const uint8_t* base, size_t size);
+
+  // Stream payloads are read in place when 8-byte aligned (the normal case), else via scratch.
+  std::vector<double> scratch_xy;
+  std::vector<BLGpuGradientStop> scratch_stops;
+  const double* aligned_doubles(const uint8_t* p, size_t count) {
+    if (!(reinterpret_cast<uintptr_t>(p) & 7u)) return reinterpret_cast<const double*>(p);
+    scratch_xy.resize(count);
+    if (count) memcpy(scratch_xy.data(), p, count * sizeof(double));
+    return scratch_xy.data();
+  }
 };
 
 // Stream replay: the same record semantics as the context calls above.
@@ -559,13 +579,17 @@ BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
         if (!need(sizeof(g))) return BLGPU_ERROR_INVALID_VALUE;
         memcpy(&g, p, sizeof(g));
         if (!need(sizeof(g) + size_t(g.stop_count) * sizeof(BLGpuStreamGradientStop))) return BLGPU_ERROR_INVALID_VALUE;
-        std::vector<BLGpuGradientStop> stops(g.stop_count);
-        if (g.stop_count) memcpy(stops.data(), p + sizeof(g), sizeof(BLGpuGradientStop) * g.stop_count);
+        const uint8_t* sp = p + sizeof(g);
+        if (g.stop_count && (reinterpret_cast<uintptr_t>(sp) & 7u)) {
+          scratch_stops.resize(g.stop_count);
+          memcpy(scratch_stops.data(), sp, sizeof(BLGpuGradientStop) * g.stop_count);
+          sp = reinterpret_cast<const uint8_t*>(scratch_stops.data());
+        }
         BLGpuGradient gg;
         gg.type = g.type;
         gg.extend_mode = g.extend_mode;
         memcpy(gg.values, g.values, sizeof(gg.values));
-        gg.stops = stops.data();
+        gg.stops = reinterpret_cast<const BLGpuGradientStop*>(sp);
         gg.stop_count = g.stop_count;
         gg.transform = g.has_transform ? g.transform : nullptr;
         r = set_style_gradient(&gg);
@@ -608,9 +632,7 @@ BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
         if (!need(8)) return BLGPU_ERROR_INVALID_VALUE;
         uint32_t n; memcpy(&n, p, 4);
         if (!need(8 + size_t(n) * 16)) return BLGPU_ERROR_INVALID_VALUE;
-        std::vector<double> xy(size_t(n) * 2);
-        if (n) memcpy(xy.data(), p + 8, size_t(n) * 16);
-        r = fill_polygon(xy.data(), n);
+        r = fill_polygon(aligned_doubles(p + 8, size_t(n) * 2), n);
         break;
       }
       case BLGPU_OP_FILL_PATH_D: {
@@ -618,9 +640,7 @@ BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
         uint32_t n; memcpy(&n, p, 4);
         size_t cmd_bytes = (size_t(n) + 7u) & ~size_t(7);
         if (!need(8 + cmd_bytes + size_t(n) * 16)) return BLGPU_ERROR_INVALID_VALUE;
-        std::vector<double> xy(size_t(n) * 2);
-        if (n) memcpy(xy.data(), p + 8 + cmd_bytes, size_t(n) * 16);
-        r = fill_path(p + 8, xy.data(), n);
+        r = fill_path(p + 8, aligned_doubles(p + 8 + cmd_bytes, size_t(n) * 2), n);
         break;
       }
       case BLGPU_OP_SAVE: save(); break;
@@ -771,7 +791,9 @@ BLGPU_API BLGpuResult blgpu_render_batch(BLGpuRuntime* rt, const void* const* st
                                          const BLGpuImage* images, uint32_t count) {
   if (!rt || (count && (!streams || !sizes || !images))) return BLGPU_ERROR_INVALID_VALUE;
   if (!count) return BLGPU_SUCCESS;
-  Frame frame;
+  std::lock_guard<std::mutex> guard(rt->batch_lock);
+  Frame& frame = rt->batch_frame;
+  frame.clear();
   std::vector<BLGpuContext> ctxs(count);
   for (uint32_t i = 0; i < count; i++) {
     BLGpuContext& c = ctxs[i];
@@ -808,7 +830,7 @@ BLGPU_API BLGpuResult blgpu_render_stream_noalloc(BLGpuRuntime* rt, const void* 
       im.stride < intptr_t(im.width) * 4 || (im.stride & 15) || (reinterpret_cast<uintptr_t>(im.pixel_data) & 15))
     return BLGPU_ERROR_INVALID_VALUE;
   std::lock_guard<std::mutex> guard(lock);
-  Frame frame;
+  Frame frame(false);              // plain heap memory: no page-locked allocation either
   BLGpuContext c;
   c.rt = rt;
   c.frame = &frame;

@@ -92,7 +92,9 @@ int default_band_height(int width) {
 }
 
 void style_solid(HostStyle& s, uint32_t argb32) {
-  s = HostStyle{};
+  s.dev = DevStyle{};
+  s.image = -1;
+  s.stops.clear();
   s.nop = false;
   s.dev.fetch = kFetchSolid;
   s.dev.solid = premultiply(argb32);
@@ -266,8 +268,12 @@ static bool init_conic(DevStyle& d, const double* v, const Mat& t) {   // pipede
 // init_non_solid_fetch_data, gradient branch (blend2d/raster/rastercontext.cpp:423-478) with
 // GradientInternal::ensure_info (blend2d/core/gradient.cpp:202-287).
 void style_gradient(HostStyle& s, const GradientDesc& g, const Mat& final_transform) {
-  s = HostStyle{};
-  std::vector<DevStop> stops;
+  // reset in place: the stop vector keeps its capacity from style to style
+  std::vector<DevStop> stops = std::move(s.stops);
+  s.nop = true;
+  s.format = kFmtPRGB32;
+  s.dev = DevStyle{};
+  s.image = -1;
   if (!normalize_stops(stops, g.stops, g.stop_count)) stops.clear();
   Mat tf = final_transform;
   if (g.transform) {
@@ -429,7 +435,10 @@ static bool pattern_affine(DevStyle& d, uint32_t extend, uint32_t quality, const
 
 // init_non_solid_fetch_data, pattern branch (blend2d/raster/rastercontext.cpp:377-421).
 void style_pattern(HostStyle& s, const PatternDesc& p, uint32_t quality, const Mat& final_transform) {
-  s = HostStyle{};
+  s.nop = true;
+  s.dev = DevStyle{};
+  s.image = -1;
+  s.stops.clear();
   s.format = kFmtPRGB32;
   int ax = 0, ay = 0, aw = p.img_w, ah = p.img_h;
   if (p.area[2] > 0) { ax = p.area[0]; ay = p.area[1]; aw = p.area[2]; ah = p.area[3]; }

@@ -238,29 +238,48 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   Layout L;
   L.base = static_cast<char*>(in_buf.ptr);
   canvas_dev.assign(ncv, nullptr);
-  size_t staged_bytes = plan(L, v, &canvas_dev);
+  plan(L, v, &canvas_dev);
 
-  // Pack the staged inputs into pinned memory with the same layout, then one H2D copy.
-  if (staged_bytes > host_staging_size) {
-    BLGPU_CHECK(cudaStreamSynchronize(stream));
+  // Frame arrays recorded in page-locked memory go to the device by DMA straight from where they
+  // were recorded; anything else (the canvas table, pattern images, arrays that had to fall back
+  // to pageable memory) is packed into the page-locked staging buffer first.
+  size_t pack_bytes = align_up(sizeof(DevCanvas) * ncv, 256);
+  auto needs_pack = [&](bool pinned_array, size_t bytes) { if (!pinned_array) pack_bytes += align_up(bytes, 256); };
+  needs_pack(fr.cmds.ptr_pinned, sizeof(DevCmd) * nc);
+  needs_pack(fr.styles.ptr_pinned, sizeof(DevStyle) * fr.styles.size());
+  needs_pack(fr.xforms.ptr_pinned, sizeof(DevXform) * fr.xforms.size());
+  needs_pack(fr.verts.ptr_pinned, sizeof(double) * fr.verts.size());
+  needs_pack(fr.path_cmds.ptr_pinned, fr.path_cmds.size());
+  needs_pack(fr.lut_jobs.ptr_pinned, sizeof(DevLutJob) * fr.lut_jobs.size());
+  needs_pack(fr.stops.ptr_pinned, sizeof(DevStop) * fr.stops.size());
+  for (const FrameImage& im : fr.images)
+    if (!im.device) pack_bytes += align_up(size_t(im.w) * size_t(im.h) * 4u, 256);
+  // the previous frame's copies out of the staging buffer must have completed
+  BLGPU_CHECK(cudaStreamSynchronize(stream));
+  if (pack_bytes > host_staging_size) {
     if (host_staging) cudaFreeHost(host_staging);
     host_staging = nullptr;
-    size_t want = align_up(staged_bytes + staged_bytes / 4, size_t(1) << 20);
+    size_t want = align_up(pack_bytes + pack_bytes / 4, size_t(1) << 20);
     BLGPU_CHECK(cudaMallocHost(&host_staging, want));
     host_staging_size = want;
   }
-  else {
-    // the previous frame's copy out of the staging buffer must have completed
-    BLGPU_CHECK(cudaStreamSynchronize(stream));
-  }
   char* hs = static_cast<char*>(host_staging);
-  char* db = static_cast<char*>(in_buf.ptr);
-  auto put = [&](const void* dev_ptr, const void* src, size_t bytes) {
-    if (bytes) memcpy(hs + (static_cast<const char*>(dev_ptr) - db), src, bytes);
+  size_t hs_off = 0;
+  h2d_bytes = 0;
+  d2h_bytes = 0;
+  auto put = [&](const void* dev_ptr, const void* src, size_t bytes, bool src_pinned) -> cudaError_t {
+    if (!bytes) return cudaSuccess;
+    h2d_bytes += bytes;
+    if (!src_pinned) {
+      memcpy(hs + hs_off, src, bytes);
+      src = hs + hs_off;
+      hs_off += align_up(bytes, 256);
+    }
+    return cudaMemcpyAsync(const_cast<void*>(dev_ptr), src, bytes, cudaMemcpyHostToDevice, stream);
   };
-  put(v.cmds, fr.cmds.data(), sizeof(DevCmd) * nc);
-  put(v.styles, fr.styles.data(), sizeof(DevStyle) * fr.styles.size());
-  put(v.xforms, fr.xforms.data(), sizeof(DevXform) * fr.xforms.size());
+  BLGPU_CHECK(put(v.cmds, fr.cmds.data(), sizeof(DevCmd) * nc, fr.cmds.ptr_pinned));
+  BLGPU_CHECK(put(v.styles, fr.styles.data(), sizeof(DevStyle) * fr.styles.size(), fr.styles.ptr_pinned));
+  BLGPU_CHECK(put(v.xforms, fr.xforms.data(), sizeof(DevXform) * fr.xforms.size(), fr.xforms.ptr_pinned));
   std::vector<DevCanvas> cvs = fr.canvases;
   canvas_stride.assign(ncv, 0);
   for (uint32_t i = 0; i < ncv; i++) {
@@ -269,21 +288,21 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     cvs[i].stride = device_target_direct(im) ? int32_t(im.stride / 4) : int32_t(align_up(uint32_t(im.width), 4));
     canvas_stride[i] = cvs[i].stride;
   }
-  put(v.canvases, cvs.data(), sizeof(DevCanvas) * ncv);
-  put(v.verts, fr.verts.data(), sizeof(double) * fr.verts.size());
-  put(v.path_cmds, fr.path_cmds.data(), fr.path_cmds.size());
-  put(v.lut_jobs, fr.lut_jobs.data(), sizeof(DevLutJob) * fr.lut_jobs.size());
-  put(v.stops, fr.stops.data(), sizeof(DevStop) * fr.stops.size());
+  BLGPU_CHECK(put(v.canvases, cvs.data(), sizeof(DevCanvas) * ncv, false));
+  BLGPU_CHECK(put(v.verts, fr.verts.data(), sizeof(double) * fr.verts.size(), fr.verts.ptr_pinned));
+  BLGPU_CHECK(put(v.path_cmds, fr.path_cmds.data(), fr.path_cmds.size(), fr.path_cmds.ptr_pinned));
+  BLGPU_CHECK(put(v.lut_jobs, fr.lut_jobs.data(), sizeof(DevLutJob) * fr.lut_jobs.size(), fr.lut_jobs.ptr_pinned));
+  BLGPU_CHECK(put(v.stops, fr.stops.data(), sizeof(DevStop) * fr.stops.size(), fr.stops.ptr_pinned));
   for (const FrameImage& im : fr.images) {
     if (im.device) continue;
-    char* dst = hs + (reinterpret_cast<const char*>(v.images + im.pool_offset) - db);
+    const size_t row = size_t(im.w) * 4u, bytes = row * size_t(im.h);
+    char* dst = hs + hs_off;
     for (int y = 0; y < im.h; y++)
-      memcpy(dst + size_t(y) * size_t(im.w) * 4u, static_cast<const char*>(im.pixels) + intptr_t(y) * im.stride,
-             size_t(im.w) * 4u);
+      memcpy(dst + size_t(y) * row, static_cast<const char*>(im.pixels) + intptr_t(y) * im.stride, row);
+    hs_off += align_up(bytes, 256);
+    h2d_bytes += bytes;
+    BLGPU_CHECK(cudaMemcpyAsync(const_cast<uint32_t*>(v.images) + im.pool_offset, dst, bytes, cudaMemcpyHostToDevice, stream));
   }
-  h2d_bytes = staged_bytes;
-  d2h_bytes = 0;
-  if (staged_bytes) BLGPU_CHECK(cudaMemcpyAsync(in_buf.ptr, host_staging, staged_bytes, cudaMemcpyHostToDevice, stream));
   for (const FrameImage& im : fr.images) {
     if (!im.device) continue;
     BLGPU_CHECK(cudaMemcpy2DAsync(const_cast<uint32_t*>(v.images) + im.pool_offset, size_t(im.w) * 4u, im.pixels,
@@ -363,8 +382,10 @@ int Runtime::enqueue_render_half(cudaStream_t st, bool timed) {
   k += launch_seg_bin(f, 1, st);
   k += launch_rows_and_tiles(f, row_canvas, st);
   k += launch_row_states(f, st);
-  k += launch_coverage(f, cfg, st);
+  // the fine stage: coverage (masks of analytic fills) + composite, timed together
   if (timed) cudaEventRecord(ev[1], st);
+  k += launch_coverage(f, cfg, st);
+  if (timed) cudaEventRecord(ev[4], st);
   k += launch_fine(f, cfg, st);
   if (timed) cudaEventRecord(ev[2], st);
   return k;
@@ -458,6 +479,9 @@ BLGpuResult Runtime::run(const Frame& fr) {
   float ms = 0.f, fine_ms = 0.f;
   cudaEventElapsedTime(&ms, ev[0], ev[3]);
   cudaEventElapsedTime(&fine_ms, ev[1], ev[2]);
+  float comp_ms = 0.f;
+  cudaEventElapsedTime(&comp_ms, ev[4], ev[2]);
+  stats.last_composite_ms = comp_ms;
   stats.frames++;
   stats.fill_commands = view.num_cmds;
   stats.segments = totals.segs;
@@ -740,6 +764,9 @@ BLGpuResult Runtime::synchronize() {
     if (pending_timing == 2) {
       cudaEventElapsedTime(&fine_ms, ev[1], ev[2]);
       stats.last_fine_ms = fine_ms;
+      float comp_ms = 0.f;
+      cudaEventElapsedTime(&comp_ms, ev[4], ev[2]);
+      stats.last_composite_ms = comp_ms;
     }
     stats.frames++;
     pending_timing = 0;

@@ -4,6 +4,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <stdlib.h>
+#include <string.h>
+
+#include <new>
 #include <vector>
 
 #include "blgpu.h"
@@ -27,17 +31,82 @@ struct FrameTarget {
   bool upload;              // the pipeline reads the canvas's current content
 };
 
+// Growable array of trivially copyable elements in page-locked host memory (or plain heap memory
+// when `pinned` is false), so that a frame recorded into it can be copied to the device by DMA
+// without an intermediate copy. Capacity is kept across clear().
+template <typename T>
+struct HostArray {
+  T* ptr = nullptr;
+  size_t n = 0, cap = 0;
+  bool pinned = true;          // allocate page-locked memory
+  bool ptr_pinned = false;     // the current block is page-locked (allocation may fall back)
+
+  HostArray() = default;
+  HostArray(const HostArray&) = delete;
+  HostArray& operator=(const HostArray&) = delete;
+  ~HostArray() { release(); }
+
+  void release() {
+    if (ptr) { if (ptr_pinned) cudaFreeHost(ptr); else free(ptr); }
+    ptr = nullptr; n = cap = 0; ptr_pinned = false;
+  }
+  void reserve(size_t want) {
+    if (want <= cap) return;
+    size_t nc = cap ? cap : 1024;
+    while (nc < want) nc += nc / 2 + 1;
+    T* np = nullptr;
+    bool np_pinned = false;
+    if (pinned) {
+      if (cudaMallocHost(reinterpret_cast<void**>(&np), nc * sizeof(T)) == cudaSuccess) np_pinned = true;
+      else { np = nullptr; cudaGetLastError(); }
+    }
+    if (!np) np = static_cast<T*>(malloc(nc * sizeof(T)));   // pageable fallback still works
+    if (!np) throw std::bad_alloc();
+    if (n) memcpy(np, ptr, n * sizeof(T));
+    if (ptr) { if (ptr_pinned) cudaFreeHost(ptr); else free(ptr); }
+    ptr = np; cap = nc; ptr_pinned = np_pinned;
+  }
+  size_t size() const { return n; }
+  bool empty() const { return n == 0; }
+  T* data() { return ptr; }
+  const T* data() const { return ptr; }
+  T* begin() { return ptr; }
+  T* end() { return ptr + n; }
+  const T* begin() const { return ptr; }
+  const T* end() const { return ptr + n; }
+  T& operator[](size_t i) { return ptr[i]; }
+  const T& operator[](size_t i) const { return ptr[i]; }
+  T& back() { return ptr[n - 1]; }
+  void clear() { n = 0; }
+  void push_back(const T& v) { if (n == cap) reserve(n + 1); ptr[n++] = v; }
+  void append(const T* first, size_t count) {
+    if (!count) return;
+    reserve(n + count);
+    memcpy(ptr + n, first, count * sizeof(T));
+    n += count;
+  }
+  void append_fill(size_t count, const T& v) {
+    reserve(n + count);
+    for (size_t i = 0; i < count; i++) ptr[n + i] = v;
+    n += count;
+  }
+};
+
 // Everything one device pipeline run consumes, recorded on the host in painter's order.
 struct Frame {
-  std::vector<DevCmd> cmds;
-  std::vector<DevStyle> styles;
-  std::vector<DevXform> xforms;
+  explicit Frame(bool pinned_memory = true) {
+    cmds.pinned = styles.pinned = xforms.pinned = verts.pinned = path_cmds.pinned = lut_jobs.pinned = stops.pinned =
+        pinned_memory;
+  }
+  HostArray<DevCmd> cmds;
+  HostArray<DevStyle> styles;
+  HostArray<DevXform> xforms;
   std::vector<DevCanvas> canvases;
   std::vector<FrameTarget> targets;
-  std::vector<double> verts;
-  std::vector<uint8_t> path_cmds;
-  std::vector<DevLutJob> lut_jobs;
-  std::vector<DevStop> stops;
+  HostArray<double> verts;
+  HostArray<uint8_t> path_cmds;
+  HostArray<DevLutJob> lut_jobs;
+  HostArray<DevStop> stops;
   std::vector<FrameImage> images;
   uint64_t image_words = 0;
   uint32_t lut_words = 0;
@@ -80,7 +149,7 @@ struct Runtime {
   size_t host_staging_size = 0;
   uint32_t* host_totals = nullptr;   // pinned: [0..8) frame totals, [8..12) pixel ops
 
-  cudaEvent_t ev[4] = {};
+  cudaEvent_t ev[5] = {};
   cudaGraphExec_t graph = nullptr;
   bool graph_valid = false;
 

@@ -478,6 +478,42 @@ def random_mix(seed: int, width: int = 257, height: int = 257, count: int = 200,
     return sw
 
 
+def conic_paths(seed: int = 8, width: int = 300, height: int = 200, count: int = 120) -> StreamWriter:
+    """Closed paths of conic segments as BLPath stores them (CONIC p1, WEIGHT (w, NaN), ON p2),
+    partly outside the canvas, solid and gradient styles, both fill rules, with transforms."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sw = StreamWriter(width, height)
+    sw.solid(0xFF000000)
+    sw.fill_all()
+    for i in range(count):
+        sw.fill_rule(int(rng.integers(0, 2)))
+        sw.comp_op(int(rng.integers(0, 2)))
+        side = float(_log_uniform(rng, 10.0, 160.0))
+        x0 = float(rng.uniform(-side * 0.3, width - side * 0.7))
+        y0 = float(rng.uniform(-side * 0.3, height - side * 0.7))
+        if i % 3:
+            sw.solid(int(rng.integers(0, 2**32, dtype=np.uint64)))
+        else:
+            _gradient_style(rng, sw, x0, y0, side)
+        if i % 5 == 0:
+            a = float(rng.uniform(-0.4, 0.4))
+            sn, c = _sincos(a)
+            sw.transform([c, sn, -sn, c, 20.0, -10.0])
+        elif i % 5 == 1:
+            sw.reset_transform()
+        n = int(rng.integers(2, 6))
+        pts = rng.uniform(0, side, (2 * n + 1, 2)) + np.array([x0, y0])
+        cmds, xy = [P_MOVE], [pts[0]]
+        for k in range(n):
+            w = float(_log_uniform(rng, 0.25, 4.0))
+            cmds += [P_CONIC, 6, P_ON]
+            xy += [pts[2 * k + 1], np.array([w, np.nan]), pts[2 * k + 2]]
+        cmds.append(P_CLOSE)
+        xy.append(pts[0])
+        sw.fill_path(cmds, np.array(xy))
+    return sw
+
+
 WORKLOADS = {
     "polygons": polygons,
     "curves": curves,

@@ -95,13 +95,14 @@ typedef struct BLGpuStats {
   uint64_t tiles;          /* tiles of the last frame */
   uint64_t kernel_launches;/* kernels launched by the last frame's device pipeline */
   double last_gpu_ms;      /* device time of the last frame's pipeline (CUDA events) */
-  double last_fine_ms;     /* device time of its fine (composite) kernel */
+  double last_fine_ms;     /* device time of its fine stage: coverage + composite kernels */
   uint64_t pixel_ops;      /* composited pixels of the last frame (mask != 0, summed over commands) */
   uint64_t pattern_ops;    /* ... of which fetched from a pattern */
   uint64_t input_vertices; /* vertices of the last frame's polygon/path fills */
   uint64_t h2d_bytes;      /* host->device bytes of the last flush (frame data + canvas uploads) */
   uint64_t d2h_bytes;      /* device->host bytes of the last flush (canvas downloads + sizes) */
   int64_t last_cuda_error; /* cudaError_t behind the last BLGPU_ERROR_DEVICE (0 if none) */
+  double last_composite_ms;/* ... of which the composite kernel */
 } BLGpuStats;
 
 /* Launch shapes of the device pipeline (0 in a *_blocks_per_sm field = as many as fit). Tile and

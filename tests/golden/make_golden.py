@@ -46,6 +46,7 @@ def scene_catalog(full: bool):
         ("curves_2k", "scenes.curves(count=2000)", ("default",)),
         ("patterns_1k", "scenes.patterns(count=500, width=1024, height=1024)", ("default",)),
         ("edge_cases", "scenes.edge_cases()", ("default", "scalar")),
+        ("conics", "scenes.conic_paths()", ("default",)),
     ]
     for s in range(24):
         cat.append((f"mix_{s}", f"scenes.random_mix({s})", ("default",) if s % 4 else ("default", "scalar")))

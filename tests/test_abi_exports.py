@@ -60,7 +60,7 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(bg.GradientStop) == 16
     assert ctypes.sizeof(bg.Gradient) == 8 + 48 + 8 + 8 + 8
     assert ctypes.sizeof(bg.Pattern) == 8 + 16 + 8 + 8
-    assert ctypes.sizeof(bg.Stats) == 104
+    assert ctypes.sizeof(bg.Stats) == 112
 
 
 def test_missing_library_fails_loudly(tmp_path):
