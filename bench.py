@@ -331,7 +331,7 @@ def run_ours(args) -> int:
                 "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_s * 1e3 / args.steps, 3)},
         "gpu_launches": launches,
         "clocks": clock_info,
-        "roofline": {"bound": "hbm", "kernel": "fine stage (coverage_kernel + fine_kernel, the composite pass)",
+        "roofline": {"bound": "hbm", "kernel": "fine stage (coverage: raster_kernel + sweep_kernel; composite: fine_kernel)",
                      "achieved": round(achieved, 2), "peak": peak,
                      "peak_kind": f"of {peak_kind}", "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": traffic, "traffic_source": traffic_src,

@@ -195,10 +195,15 @@ struct FrameView {
   uint32_t* cmd_yr;            // pixel rows y0 | y1 << 16
   uint32_t* cmdrow_base;       // [num_cmds + 1]: first (cmd, strip row, tile column) slot
   uint32_t* cmdrow_counts;     // [num_cmdrows + 1]
-  uint32_t* cmdrow_offsets;    // exclusive scan of counts
-  uint32_t* cmdrow_cursor;
-  uint32_t* seglist;           // segment indices grouped by (cmd, strip row, tile column)
-  uint8_t* masks;              // [num_cmdrows][kStripRows * kTileW]: analytic masks from the coverage pass
+  uint32_t* cmdrow_offsets;    // scratch for the scan of non-empty slots
+  uint32_t* slot_cmd;          // [num_cmdrows] command of each slot with segments
+  uint32_t* slot_mask;         // [num_cmdrows + 1] 1 + index of the slot's masks, 0 = no segments
+  uint32_t* mask_slot;         // [non-empty slots] slot of each compact mask index
+  uint32_t* cells;             // [non-empty slots][kStripRows * kTileW] cell sums of the coverage pass
+  uint4* entries;              // raster work: {segment, slot, mask index, x0 | row0 << 16}, by DDA kind
+  uint32_t* kind_info;         // [16]: entries per kind [0..5), cursors [5..10), offsets [10..16)
+  uint32_t mask_capacity;      // slots the cells/masks arrays hold
+  uint8_t* masks;              // [non-empty slots][kStripRows * kTileW]: analytic masks from the coverage pass
   uint32_t* backdrop;          // [num_cmdrows][kStripRows]: coverage carried into the slot's tile
                                //   from segments entirely left of it (cover << 9 per row)
   uint32_t* row_counts;        // [num_rows + 1]

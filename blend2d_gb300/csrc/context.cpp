@@ -695,7 +695,7 @@ BLGPU_API BLGpuResult blgpu_runtime_synchronize(BLGpuRuntime* rt) {
 
 static void to_abi(const LaunchConfig& c, BLGpuLaunchConfig* out) {
   *out = BLGpuLaunchConfig{};
-  out->cover_group = c.cover_group;
+  out->raster_block = c.raster_block;
   out->cover_blocks_per_sm = c.cover_blocks_per_sm;
   out->fine_blocks_per_sm = c.fine_blocks_per_sm;
   out->edge_block = c.edge_block;
@@ -710,12 +710,12 @@ BLGPU_API BLGpuResult blgpu_runtime_get_launch_config(const BLGpuRuntime* rt, BL
 
 BLGPU_API BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BLGpuLaunchConfig* c) {
   if (!rt || !c) return BLGPU_ERROR_INVALID_VALUE;
-  if ((c->cover_group != 8 && c->cover_group != 16) ||
+  if ((c->raster_block != 128 && c->raster_block != 256) ||
       (c->edge_block != 64 && c->edge_block != 128 && c->edge_block != 256) ||
       c->cover_blocks_per_sm < 0 || c->fine_blocks_per_sm < 0 || c->cubic_blocks_per_sm < 0)
     return BLGPU_ERROR_INVALID_VALUE;
   LaunchConfig lc;
-  lc.cover_group = c->cover_group;
+  lc.raster_block = c->raster_block;
   lc.cover_blocks_per_sm = c->cover_blocks_per_sm;
   lc.fine_blocks_per_sm = c->fine_blocks_per_sm;
   lc.edge_block = c->edge_block;

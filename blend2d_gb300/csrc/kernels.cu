@@ -613,39 +613,60 @@ __global__ void cmd_tiles_kernel(FrameView f, uint32_t* cmdrow_counts_per_cmd, u
   for (uint32_t r = ty0; r <= ty1; r++) atomicAdd(&row_counts[cv.row_base + r], 1u);
 }
 
-// Segments per (command, strip row, tile column): a segment is listed in every tile its cells touch
-// (cells reach x + 1). Tiles entirely right of it get its per-row cover in their backdrop (the
-// count pass adds it once, at the first tile right of the segment; a prefix over tile columns
-// then carries it to all of them).
-__global__ void seg_bin_kernel(FrameView f, int scatter) {
-  uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= f.num_segs) return;
-  uint32_t c = f.seg_meta[s] >> 1;
-  uint32_t ctx = f.cmd_tile_x[c];
-  if (ctx == 0xFFFFFFFFu) return;
-  const uint32_t sign = f.seg_meta[s] & 1u;
-  const int tx0 = int(ctx & 0xFFFFu), tx1 = int(ctx >> 16), ntx = tx1 - tx0 + 1;
-  const uint32_t yr = f.cmd_yr[c];
-  const int sr0 = int((yr & 0xFFFFu) >> kStripShift), sr1 = int((yr >> 16) >> kStripShift);
-  const DevSeg g = f.segs[s];
-  const int ey0 = g.y0 >> 8, ey1 = (g.y1 - 1) >> 8;
-  const int r0 = max(ey0 >> kStripShift, sr0), r1 = min(ey1 >> kStripShift, sr1);
-  const uint32_t base = f.cmdrow_base[c];
-  const uint32_t sm = 0u - sign;
+// DDA path a segment takes through the reference rasterizer (prepare_ref's classification): the
+// coverage pass processes segments grouped by it so that a warp's lanes run the same code.
+__device__ __forceinline__ uint32_t dda_kind(const DevSeg& g) {
+  const int dx = g.x1 - g.x0, adx = dx < 0 ? -dx : dx, dy = g.y1 - g.y0;
+  if ((g.x0 >> 8) == (g.x1 >> 8) && ((g.y0 >> 8) == ((g.y1 - 1) >> 8) || adx == 0)) return 0u;
+  return dy >= adx ? (dx < 0 ? 2u : 1u) : (dx < 0 ? 4u : 3u);
+}
+
+// Segments per (command, strip row, tile column) slot: a segment belongs to every slot its cells
+// can touch within each strip row. Pass 0 counts the slots' segments, records each slot's command
+// and counts the work per DDA kind; tiles entirely right of a segment get its per-row cover in
+// their backdrop (added once, at the first tile right of it; a prefix over tile columns carries it
+// on). Pass 1 writes the raster work items, grouped by DDA kind.
+__global__ void __launch_bounds__(256) seg_bin_kernel(FrameView f, int scatter) {
+  __shared__ uint32_t s_count[5], s_base[5];
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (threadIdx.x < 5) s_count[threadIdx.x] = 0;
+  uint32_t c = 0, ctx = 0xFFFFFFFFu;
+  if (s < f.num_segs) {
+    c = f.seg_meta[s] >> 1;
+    ctx = f.cmd_tile_x[c];
+  }
+  const bool valid = ctx != 0xFFFFFFFFu;
+  DevSeg g{};
+  uint32_t kind = 0, base = 0, sm = 0;
+  int tx0 = 0, tx1 = -1, ntx = 0, sr0 = 0, r0 = 0, r1 = -1, ey0 = 0, ey1 = 0;
+  if (valid) {
+    sm = 0u - (f.seg_meta[s] & 1u);
+    tx0 = int(ctx & 0xFFFFu); tx1 = int(ctx >> 16); ntx = tx1 - tx0 + 1;
+    const uint32_t yr = f.cmd_yr[c];
+    sr0 = int((yr & 0xFFFFu) >> kStripShift);
+    const int sr1 = int((yr >> 16) >> kStripShift);
+    g = f.segs[s];
+    kind = dda_kind(g);
+    ey0 = g.y0 >> 8; ey1 = (g.y1 - 1) >> 8;
+    r0 = max(ey0 >> kStripShift, sr0); r1 = min(ey1 >> kStripShift, sr1);
+    base = f.cmdrow_base[c];
+  }
+  __syncthreads();
+  // per strip row: slots [t0, t1] get the segment, the first tile right of it its cover
+  uint32_t n_entries = 0;
   for (int r = r0; r <= r1; r++) {
     int t_first, t_last;
     strip_tile_range(g, r, t_first, t_last);
     const int t0 = max(t_first, tx0), t1 = min(t_last, tx1);
-    uint32_t row_slot = base + uint32_t(r - sr0) * uint32_t(ntx);
+    if (t1 >= t0) n_entries += uint32_t(t1 - t0 + 1);
+    if (scatter) continue;
+    const uint32_t row_slot = base + uint32_t(r - sr0) * uint32_t(ntx);
     for (int t = t0; t <= t1; t++) {
-      uint32_t slot = row_slot + uint32_t(t - tx0);
-      if (!scatter) atomicAdd(&f.cmdrow_counts[slot], 1u);
-      else {
-        uint32_t pos = atomicAdd(&f.cmdrow_cursor[slot], 1u);
-        f.seglist[f.cmdrow_offsets[slot] + pos] = s;
-      }
+      const uint32_t slot = row_slot + uint32_t(t - tx0);
+      atomicAdd(&f.cmdrow_counts[slot], 1u);
+      f.slot_cmd[slot] = c;
     }
-    if (!scatter && t_last + 1 <= tx1) {
+    if (t_last + 1 <= tx1) {
       uint32_t* bd = f.backdrop + size_t(row_slot + uint32_t(t_last + 1 - tx0)) * kStripRows;
       int ya = max(ey0, r << kStripShift), yb = min(ey1, (r << kStripShift) + kStripRows - 1);
       for (int y = ya; y <= yb; y++) {
@@ -655,6 +676,54 @@ __global__ void seg_bin_kernel(FrameView f, int scatter) {
       }
     }
   }
+  // work per DDA kind, aggregated per block before it reaches the five global counters
+  const uint32_t local = n_entries ? atomicAdd(&s_count[kind], n_entries) : 0u;
+  __syncthreads();
+  if (threadIdx.x < 5 && s_count[threadIdx.x])
+    s_base[threadIdx.x] = atomicAdd(&f.kind_info[(scatter ? 5 : 0) + threadIdx.x], s_count[threadIdx.x]);
+  if (!scatter) return;                               // uniform over the block
+  __syncthreads();
+  if (!n_entries) return;
+  uint32_t pos = f.kind_info[10 + kind] + s_base[kind] + local;
+  if (pos + n_entries > f.num_seglist + 1u) { atomicOr(&f.error_flags[0], 4u); return; }
+  for (int r = r0; r <= r1; r++) {
+    int t_first, t_last;
+    strip_tile_range(g, r, t_first, t_last);
+    const int t0 = max(t_first, tx0), t1 = min(t_last, tx1);
+    const uint32_t row_slot = base + uint32_t(r - sr0) * uint32_t(ntx);
+    for (int t = t0; t <= t1; t++) {
+      const uint32_t slot = row_slot + uint32_t(t - tx0);
+      f.entries[pos++] = make_uint4(s, slot, f.slot_mask[slot] - 1u, uint32_t(t << kTileShift) | (uint32_t(r << kStripShift) << 16));
+    }
+  }
+}
+
+// Slots with segments get a compact mask index: flags for the scan ...
+__global__ void slot_flags_kernel(FrameView f) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < f.num_cmdrows) f.cmdrow_offsets[i] = f.cmdrow_counts[i] ? 1u : 0u;
+}
+
+// ... and, after the scan, the maps between slots and mask indices.
+__global__ void slot_compact_kernel(FrameView f) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= f.num_cmdrows) return;
+  if (f.cmdrow_counts[i]) {
+    const uint32_t idx = f.cmdrow_offsets[i];
+    f.slot_mask[i] = idx + 1u;
+    f.mask_slot[idx] = i;
+  }
+  else {
+    f.slot_mask[i] = 0u;
+  }
+  if (i == f.num_cmdrows - 1) f.totals[5] = f.cmdrow_offsets[i] + (f.cmdrow_counts[i] ? 1u : 0u);
+}
+
+__global__ void kind_offsets_kernel(FrameView f) {
+  if (threadIdx.x || blockIdx.x) return;
+  uint32_t acc = 0;
+  for (int k = 0; k < 5; k++) { f.kind_info[10 + k] = acc; acc += f.kind_info[k]; }
+  f.kind_info[15] = acc;
 }
 
 // Prefix of the backdrop deltas over the tile columns of every (command, strip row, row).
@@ -702,117 +771,60 @@ __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// K3a - coverage. A slot is (analytic command, strip row, tile column): 4 rows x 32 pixels. Slots
-// are independent, so each warp takes kSlotGroup consecutive slots at once: its lanes rasterize
-// the segments of all of them together (each slot into its own shared-memory cells, starting from
-// the slot's backdrop), then every slot is swept (8-lane shuffle prefix per row) into 128 8-bit
-// masks, stored as one coalesced 128-byte row per slot.
+// K3a - coverage, in two kernels. A slot is (analytic command, strip row, tile column): 4 rows x 32
+// pixels. `raster_kernel` takes one (segment, slot) work item per thread, in DDA-kind order so that
+// a warp's lanes follow the same path through the rasterizer, and adds the cells into the slot's
+// cell block in global memory (and its left-of-tile cover into the slot's backdrop). The sums are
+// modular u32, so the order of the atomic adds does not matter. `sweep_kernel` then turns each
+// slot's cells into 128 8-bit masks (8-lane shuffle prefix per row from the backdrop).
 // ---------------------------------------------------------------------------------------------
 
 constexpr int kStripsPerTile = kTileH / kStripRows;
 constexpr int kFineWarps = kFineThreads / 32;
 constexpr int kSlotPixels = kStripRows * kTileW;
 
-template<int kSlotGroup>
-struct alignas(16) CoverShared {
-  uint32_t cells[kSlotGroup][kSlotPixels];
-  uint32_t backdrop[kSlotGroup][kStripRows];
-  uint32_t seg_first[kSlotGroup];
-  uint32_t seg_excl[kSlotGroup + 1];
-  int32_t x_base[kSlotGroup];
-  int32_t row0[kSlotGroup];
-};
-static_assert(sizeof(CoverShared<8>) % 16 == 0 && sizeof(CoverShared<16>) % 16 == 0,
-              "per-warp shared state must keep 16-byte alignment");
+__global__ void zero_cells_kernel(FrameView f) {
+  const uint32_t n = min(f.totals[5], f.mask_capacity) * uint32_t(kSlotPixels / 4);
+  uint4* cells = reinterpret_cast<uint4*>(f.cells);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    cells[i] = make_uint4(0u, 0u, 0u, 0u);
+}
 
-template<int kSlotGroup>
-__global__ void __launch_bounds__(kFineThreads) coverage_kernel(FrameView f) {
-  extern __shared__ __align__(16) unsigned char cover_smem[];
-  CoverShared<kSlotGroup>& ws = reinterpret_cast<CoverShared<kSlotGroup>*>(cover_smem)[threadIdx.x >> 5];
-  const int lane = threadIdx.x & 31;
-  const uint32_t num_groups = (f.num_cmdrows + kSlotGroup - 1) / kSlotGroup;
+__global__ void __launch_bounds__(256) raster_kernel(FrameView f) {
+  const uint32_t n = f.kind_info[15];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint4 e = f.entries[i];
+    if (e.z >= f.mask_capacity) continue;
+    ras::WindowSink sink{f.cells + size_t(e.z) * kSlotPixels, f.backdrop + size_t(e.y) * kStripRows,
+                         int(e.w & 0xFFFFu)};
+    ras::segment_to_window(f.segs[e.x], f.seg_meta[e.x] & 1u, int(e.w >> 16), kStripRows, INT32_MAX, sink);
+  }
+}
+
+__global__ void __launch_bounds__(256) sweep_kernel(FrameView f) {
+  const int lane = threadIdx.x & 31, prow = lane >> 3;
+  const uint32_t n = min(f.totals[5], f.mask_capacity);
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-
-  for (uint32_t grp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); grp < num_groups; grp += warps) {
-    const uint32_t first = grp * kSlotGroup;
-    const int ns = int(min(uint32_t(kSlotGroup), f.num_cmdrows - first));
-    // lane g < ns describes slot first + g
-    uint32_t s_count = 0, s_first = 0, cmd_of = 0;
-    int xb = 0, r0 = 0;
-    if (lane < ns) {
-      const uint32_t slot = first + uint32_t(lane);
-      uint32_t lo = 0, hi = f.num_cmds - 1;          // last command whose first slot is <= slot
-      while (lo < hi) { uint32_t mid = (lo + hi + 1) >> 1; if (f.cmdrow_base[mid] <= slot) lo = mid; else hi = mid - 1; }
-      cmd_of = lo;
-      const uint32_t ctx = f.cmd_tile_x[lo];
-      const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
-      const uint32_t local = slot - f.cmdrow_base[lo];
-      const uint32_t sr = ((f.cmd_yr[lo] & 0xFFFFu) >> kStripShift) + local / ntx;
-      xb = int(((ctx & 0xFFFFu) + local % ntx) << kTileShift);
-      r0 = int(sr << kStripShift);
-      s_first = f.cmdrow_offsets[slot];
-      s_count = f.cmdrow_counts[slot];
-    }
-    uint32_t incl = s_count;
+  for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+    const uint32_t slot = f.mask_slot[i];
+    const DevCmd& cmd = f.cmds[f.slot_cmd[slot]];
+    const uint32_t flags = cmd.flags, alpha = cmd.alpha;
+    const uint4 cv4 = reinterpret_cast<const uint4*>(f.cells + size_t(i) * kSlotPixels)[lane];
+    const uint32_t s4 = cv4.x + cv4.y + cv4.z + cv4.w;
+    uint32_t inc = s4;
 #pragma unroll
-    for (int o = 1; o < kSlotGroup; o <<= 1) {
-      uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-      if (lane >= o) incl += v;
+    for (int o = 1; o < 8; o <<= 1) {
+      uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o, 8);
+      if ((lane & 7) >= o) inc += v;
     }
-    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, kSlotGroup - 1);
-    if (lane < kSlotGroup) {
-      ws.seg_first[lane] = s_first;
-      ws.seg_excl[lane] = incl - s_count;
-      ws.x_base[lane] = xb;
-      ws.row0[lane] = r0;
-    }
-    if (lane == 0) ws.seg_excl[kSlotGroup] = total;
-    for (int g = 0; g < ns; g++)
-      *reinterpret_cast<uint4*>(&ws.cells[g][lane * 4]) = make_uint4(0u, 0u, 0u, 0u);
-    for (int i = lane; i < ns * kStripRows; i += 32)
-      ws.backdrop[i / kStripRows][i % kStripRows] = f.backdrop[size_t(first) * kStripRows + i];
-    __syncwarp();
-
-    for (uint32_t idx = lane; idx < total; idx += 32) {
-      int g = 0;
-#pragma unroll
-      for (int k = 1; k < kSlotGroup; k++) g += (k < ns && idx >= ws.seg_excl[k]) ? 1 : 0;
-      const uint32_t si = f.seglist[ws.seg_first[g] + (idx - ws.seg_excl[g])];
-      const uint32_t c = f.seg_meta[si] >> 1;
-      const DevCanvas& cv = f.canvases[f.cmds[c].canvas];
-      ras::WindowSink sink{ws.cells[g], ws.backdrop[g], ws.x_base[g]};
-      ras::segment_to_window(f.segs[si], f.seg_meta[si] & 1u, ws.row0[g], kStripRows, cv.h - 1, sink);
-    }
-    __syncwarp();
-
-    // sweep: lane covers row lane / 8, columns (lane % 8) * 4 .. + 3 of each slot. Slots without
-    // segments are skipped: their coverage is the backdrop alone, which the composite pass reads.
-    const int prow = lane >> 3;
-    uint32_t fa = 0;                                   // lane g < ns: flags << 16 | alpha of slot g
-    if (lane < ns) fa = (f.cmds[cmd_of].flags << 16) | f.cmds[cmd_of].alpha;
-    const uint32_t nonempty = __ballot_sync(0xFFFFFFFFu, lane < ns && s_count != 0);
-    for (int g = 0; g < ns; g++) {
-      const uint32_t gfa = __shfl_sync(0xFFFFFFFFu, fa, g);
-      if (!((nonempty >> g) & 1u)) continue;
-      const uint32_t flags = gfa >> 16, alpha = gfa & 0xFFFFu;
-      const uint4 cv4 = *reinterpret_cast<const uint4*>(&ws.cells[g][lane * 4]);
-      const uint32_t s4 = cv4.x + cv4.y + cv4.z + cv4.w;
-      uint32_t inc = s4;
-#pragma unroll
-      for (int o = 1; o < 8; o <<= 1) {
-        uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o, 8);
-        if ((lane & 7) >= o) inc += v;
-      }
-      uint32_t cov = (256u << 9) + ws.backdrop[g][prow] + inc - s4;
-      const uint32_t rule = (flags & 2u) ? 0x1FFu : 0xFFFFFFFFu;
-      uint32_t m;
-      cov += cv4.x; m = px::calc_mask(cov, rule, alpha);
-      cov += cv4.y; m |= px::calc_mask(cov, rule, alpha) << 8;
-      cov += cv4.z; m |= px::calc_mask(cov, rule, alpha) << 16;
-      cov += cv4.w; m |= px::calc_mask(cov, rule, alpha) << 24;
-      reinterpret_cast<uint32_t*>(f.masks + size_t(first + uint32_t(g)) * kSlotPixels)[lane] = m;
-    }
-    __syncwarp();
+    uint32_t cov = (256u << 9) + f.backdrop[size_t(slot) * kStripRows + prow] + inc - s4;
+    const uint32_t rule = (flags & 2u) ? 0x1FFu : 0xFFFFFFFFu;
+    uint32_t m;
+    cov += cv4.x; m = px::calc_mask(cov, rule, alpha);
+    cov += cv4.y; m |= px::calc_mask(cov, rule, alpha) << 8;
+    cov += cv4.z; m |= px::calc_mask(cov, rule, alpha) << 16;
+    cov += cv4.w; m |= px::calc_mask(cov, rule, alpha) << 24;
+    reinterpret_cast<uint32_t*>(f.masks + size_t(i) * kSlotPixels)[lane] = m;
   }
 }
 
@@ -890,7 +902,7 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
           const uint32_t ctx = f.cmd_tile_x[c];
           const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
           slot = f.cmdrow_base[c] + (strip_row - ((f.cmd_yr[c] & 0xFFFFu) >> kStripShift)) * ntx + (uint32_t(tx) - (ctx & 0xFFFFu));
-          nseg = f.cmdrow_counts[slot];
+          nseg = f.slot_mask[slot];                    // 1 + mask index, 0 = no segment reaches the slot
         }
       }
       uint32_t todo = ballot;
@@ -900,7 +912,7 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
       {
         const uint32_t s0 = __shfl_sync(0xFFFFFFFFu, slot, bit), n0 = __shfl_sync(0xFFFFFFFFu, nseg, bit);
         if (s0 != 0xFFFFFFFFu)
-          next_mw = n0 ? reinterpret_cast<const uint32_t*>(f.masks + size_t(s0) * kSlotPixels)[lane]
+          next_mw = n0 ? reinterpret_cast<const uint32_t*>(f.masks + size_t(n0 - 1u) * kSlotPixels)[lane]
                        : f.backdrop[size_t(s0) * kStripRows + prow];
       }
       while (todo) {
@@ -914,7 +926,7 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
           const int nb = __ffs(todo) - 1;
           const uint32_t s1 = __shfl_sync(0xFFFFFFFFu, slot, nb), n1 = __shfl_sync(0xFFFFFFFFu, nseg, nb);
           if (s1 != 0xFFFFFFFFu)
-            next_mw = n1 ? reinterpret_cast<const uint32_t*>(f.masks + size_t(s1) * kSlotPixels)[lane]
+            next_mw = n1 ? reinterpret_cast<const uint32_t*>(f.masks + size_t(n1 - 1u) * kSlotPixels)[lane]
                          : f.backdrop[size_t(s1) * kStripRows + prow];
           bit = nb;
         }
@@ -1144,30 +1156,28 @@ int fine_grid_size(int blocks_per_sm) {
   return sms * (blocks_per_sm > 0 && blocks_per_sm < max_per_sm ? blocks_per_sm : max_per_sm);
 }
 
-template<int G>
-static int launch_coverage_g(const FrameView& f, cudaStream_t st, int blocks_per_sm) {
-  static int sms = 0, max_per_sm = 0;
-  const int smem = int(sizeof(CoverShared<G>)) * kFineWarps;
+// Coverage pass: compact the slots with segments, write the kind-ordered raster work, rasterize,
+// sweep. Called after the binning count pass and the backdrop prefix.
+int launch_coverage(const FrameView& f, const LaunchConfig& cfg, uint32_t* scan_tmp, cudaStream_t st) {
+  if (!f.num_cmdrows) return 0;
+  static int sms = 0;
   if (!sms) {
-    cudaFuncSetAttribute(coverage_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, coverage_kernel<G>, kFineThreads, smem);
-    if (max_per_sm < 1) max_per_sm = 1;
   }
-  int per_sm = blocks_per_sm > 0 && blocks_per_sm < max_per_sm ? blocks_per_sm : max_per_sm;
-  uint32_t groups = (f.num_cmdrows + G - 1) / G;
-  uint32_t blocks = (groups + kFineWarps - 1) / kFineWarps;
-  uint32_t grid = uint32_t(sms * per_sm);
-  coverage_kernel<G><<<blocks < grid ? blocks : grid, kFineThreads, smem, st>>>(f);
-  return 1;
-}
-
-int launch_coverage(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
-  if (!f.num_cmdrows) return 0;
-  if (cfg.cover_group == 8) return launch_coverage_g<8>(f, st, cfg.cover_blocks_per_sm);
-  return launch_coverage_g<16>(f, st, cfg.cover_blocks_per_sm);
+  int k = 0;
+  slot_flags_kernel<<<cdiv(f.num_cmdrows, 256), 256, 0, st>>>(f); k++;
+  k += exclusive_scan(f.cmdrow_offsets, f.cmdrow_offsets, f.num_cmdrows, scan_tmp, st);
+  slot_compact_kernel<<<cdiv(f.num_cmdrows, 256), 256, 0, st>>>(f); k++;
+  kind_offsets_kernel<<<1, 32, 0, st>>>(f); k++;
+  k += launch_seg_bin(f, 1, st);
+  const int per_sm = cfg.cover_blocks_per_sm > 0 ? cfg.cover_blocks_per_sm : 8;
+  const int rb = cfg.raster_block == 128 ? 128 : 256;
+  zero_cells_kernel<<<sms * 4, 256, 0, st>>>(f); k++;
+  raster_kernel<<<sms * per_sm * (256 / rb), rb, 0, st>>>(f); k++;
+  sweep_kernel<<<sms * per_sm, 256, 0, st>>>(f); k++;
+  return k;
 }
 
 int launch_row_states(const FrameView& f, cudaStream_t st) {

@@ -11,7 +11,7 @@ namespace blgpu {
 
 // Launch shapes the autotuner chooses between (0 = the default for that field).
 struct LaunchConfig {
-  int cover_group = 16;           // slots per warp in the coverage pass (8 or 16)
+  int raster_block = 256;         // threads per block of the raster kernel (128 or 256)
   int cover_blocks_per_sm = 0;    // coverage grid: blocks per SM (0 = as many as fit)
   int fine_blocks_per_sm = 0;     // composite grid: blocks per SM (0 = as many as fit)
   int edge_block = 128;           // threads per block of the per-item edge builder (64/128/256)
@@ -31,7 +31,7 @@ int launch_rows_and_tiles(const FrameView& f, uint32_t* row_canvas, cudaStream_t
 int launch_fine(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st);
 int launch_row_states(const FrameView& f, cudaStream_t st);
 int launch_backdrop_prefix(const FrameView& f, cudaStream_t st);
-int launch_coverage(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st);
+int launch_coverage(const FrameView& f, const LaunchConfig& cfg, uint32_t* scan_tmp, cudaStream_t st);
 int fine_grid_size(int blocks_per_sm);
 
 }  // namespace blgpu

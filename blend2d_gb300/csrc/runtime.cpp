@@ -215,11 +215,13 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     row_canvas = L.take<uint32_t>(fr.rows + 1);
     v.tile_order = L.take<uint32_t>(fr.tiles + 1);
     v.tile_canvas = L.take<uint32_t>(fr.tiles + 1);
-    // [0] work queue, [1] items, [4..12) totals, [12..16) error flags, [16..20) pixel ops (2 x u64)
+    // [0] work queue, [1] items, [4..12) totals, [12..16) error flags, [16..20) pixel ops (2 x u64),
+    // [32..48) raster work per DDA kind
     v.work_counter = L.take<uint32_t>(kCounterWords);
     v.totals = v.work_counter + 4;
     v.error_flags = v.work_counter + 12;
     v.pixel_ops = reinterpret_cast<unsigned long long*>(v.work_counter + 16);
+    v.kind_info = v.work_counter + 32;
     v.rs_count = L.take<uint32_t>(nc + 1);
     v.rs_base = L.take<uint32_t>(nc + 1);
     scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, fr.rows + 1)));
@@ -369,26 +371,46 @@ int Runtime::enqueue_count_half(cudaStream_t st) {
   return k;
 }
 
-// Rendering half: segments, (command, row) segment lists, row command lists, fine tiles.
+// Rendering half: segments binned into (command, strip, tile) slots, row command lists, the
+// coverage pass, the composite pass.
 int Runtime::enqueue_render_half(cudaStream_t st, bool timed) {
   const FrameView& f = view;
   int k = 0;
   cudaMemsetAsync(f.cmdrow_counts, 0, sizeof(uint32_t) * (f.num_cmdrows + 1), st);
-  cudaMemsetAsync(f.cmdrow_cursor, 0, sizeof(uint32_t) * (f.num_cmdrows + 1), st);
   cudaMemsetAsync(f.backdrop, 0, sizeof(uint32_t) * kStripRows * (size_t(f.num_cmdrows) + 1), st);
   k += launch_seg_bin(f, 0, st);
   k += launch_backdrop_prefix(f, st);
-  k += exclusive_scan(f.cmdrow_counts, f.cmdrow_offsets, f.num_cmdrows, f.cmdrow_offsets + f.num_cmdrows + 1, st);
-  k += launch_seg_bin(f, 1, st);
   k += launch_rows_and_tiles(f, row_canvas, st);
   k += launch_row_states(f, st);
   // the fine stage: coverage (masks of analytic fills) + composite, timed together
   if (timed) cudaEventRecord(ev[1], st);
-  k += launch_coverage(f, cfg, st);
+  k += launch_coverage(f, cfg, f.cmdrow_offsets + f.num_cmdrows + 1, st);
   if (timed) cudaEventRecord(ev[4], st);
   k += launch_fine(f, cfg, st);
   if (timed) cudaEventRecord(ev[2], st);
   return k;
+}
+
+// Buffers sized by the counting half's totals. Slots with segments are at most min(slots, raster
+// work items), and each has one block of cells and one block of masks.
+static void plan_dynamic(Layout& L, FrameView& v, const FrameTotals& t) {
+  const uint32_t slots = std::min(t.cmdrows, t.seglist);
+  v.cmdrow_counts = L.take<uint32_t>(t.cmdrows + 1);
+  v.cmdrow_offsets = L.take<uint32_t>(t.cmdrows + 1 + scan_temp_words(t.cmdrows + 1));
+  v.slot_cmd = L.take<uint32_t>(t.cmdrows + 1);
+  v.slot_mask = L.take<uint32_t>(t.cmdrows + 1);
+  v.backdrop = L.take<uint32_t>((size_t(t.cmdrows) + 1) * kStripRows);
+  v.entries = L.take<uint4>(size_t(t.seglist) + 1);
+  v.mask_slot = L.take<uint32_t>(size_t(slots) + 1);
+  v.cells = L.take<uint32_t>((size_t(slots) + 1) * kStripRows * kTileW);
+  v.masks = L.take<uint8_t>((size_t(slots) + 1) * kStripRows * kTileW);
+  v.row_cmds = L.take<uint32_t>(t.row_entries + 1);
+  v.row_states = L.take<float4>(t.row_states + 1);
+  v.mask_capacity = slots + 1;
+  v.num_segs = t.segs;
+  v.num_cmdrows = t.cmdrows;
+  v.num_seglist = t.seglist;
+  v.num_row_states = t.row_states;
 }
 
 BLGpuResult Runtime::download() {
@@ -442,26 +464,13 @@ BLGpuResult Runtime::run(const Frame& fr) {
   totals.row_states = host_totals[4];
 
   // Dynamic buffers.
-  auto plan = [&](Layout& L) {
-    view.cmdrow_counts = L.take<uint32_t>(totals.cmdrows + 1);
-    view.cmdrow_offsets = L.take<uint32_t>(totals.cmdrows + 1 + scan_temp_words(totals.cmdrows + 1));
-    view.cmdrow_cursor = L.take<uint32_t>(totals.cmdrows + 1);
-    view.seglist = L.take<uint32_t>(totals.seglist + 1);
-    view.backdrop = L.take<uint32_t>((size_t(totals.cmdrows) + 1) * kStripRows);
-    view.masks = L.take<uint8_t>((size_t(totals.cmdrows) + 1) * kStripRows * kTileW);
-    view.row_cmds = L.take<uint32_t>(totals.row_entries + 1);
-    view.row_states = L.take<float4>(totals.row_states + 1);
-  };
   Layout measure;
-  plan(measure);
+  FrameView probe = view;
+  plan_dynamic(measure, probe, totals);
   if (measure.off > dyn_buf.size) BLGPU_CHECK(dyn_buf.reserve(measure.off));
   Layout L;
   L.base = static_cast<char*>(dyn_buf.ptr);
-  plan(L);
-  view.num_segs = totals.segs;
-  view.num_cmdrows = totals.cmdrows;
-  view.num_seglist = totals.seglist;
-  view.num_row_states = totals.row_states;
+  plan_dynamic(L, view, totals);
 
   launches += enqueue_render_half(stream, true);
   BLGPU_CHECK(cudaGetLastError());
@@ -537,6 +546,7 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     v.totals = v.work_counter + 4;
     v.error_flags = v.work_counter + 12;
     v.pixel_ops = reinterpret_cast<unsigned long long*>(v.work_counter + 16);
+    v.kind_info = v.work_counter + 32;
     v.rs_count = L.take<uint32_t>(nc + 1);
     v.rs_base = L.take<uint32_t>(nc + 1);
     a_scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, fr.rows + 1)));
@@ -608,19 +618,8 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     Layout D;
     D.base = static_cast<char*>(arena);
     D.off = dyn_begin;
-    view.cmdrow_counts = D.take<uint32_t>(t.cmdrows + 1);
-    view.cmdrow_offsets = D.take<uint32_t>(t.cmdrows + 1 + scan_temp_words(t.cmdrows + 1));
-    view.cmdrow_cursor = D.take<uint32_t>(t.cmdrows + 1);
-    view.seglist = D.take<uint32_t>(t.seglist + 1);
-    view.backdrop = D.take<uint32_t>((size_t(t.cmdrows) + 1) * kStripRows);
-    view.masks = D.take<uint8_t>((size_t(t.cmdrows) + 1) * kStripRows * kTileW);
-    view.row_cmds = D.take<uint32_t>(t.row_entries + 1);
-    view.row_states = D.take<float4>(t.row_states + 1);
+    plan_dynamic(D, view, t);
     if (D.off > kNoAllocArenaBytes) { r = BLGPU_ERROR_DATA_TOO_LARGE; break; }
-    view.num_segs = t.segs;
-    view.num_cmdrows = t.cmdrows;
-    view.num_seglist = t.seglist;
-    view.num_row_states = t.row_states;
     launches += enqueue_render_half(stream, false);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
@@ -723,15 +722,15 @@ BLGpuResult Runtime::autotune(int trials, LaunchConfig* best_out, double* best_m
   LaunchConfig best = cfg;
   double best_ms = 0.0;
   if (!r) r = measure(best, best_ms);
-  const int cover_groups[] = {8, 16};
+  const int raster_blocks[] = {128, 256};
   const int blocks[] = {0, 1, 2, 3};
   const int edge_blocks[] = {64, 128, 256};
   for (int field = 0; field < 5 && !r; field++) {
-    const int* vals = field == 0 ? cover_groups : (field == 3 ? edge_blocks : blocks);
+    const int* vals = field == 0 ? raster_blocks : (field == 3 ? edge_blocks : blocks);
     const int nvals = field == 0 ? 2 : (field == 3 ? 3 : 4);
     for (int k = 0; k < nvals && !r; k++) {
       LaunchConfig c = best;
-      int* slot = field == 0 ? &c.cover_group : field == 1 ? &c.cover_blocks_per_sm : field == 2 ? &c.fine_blocks_per_sm
+      int* slot = field == 0 ? &c.raster_block : field == 1 ? &c.cover_blocks_per_sm : field == 2 ? &c.fine_blocks_per_sm
                 : field == 3 ? &c.edge_block : &c.cubic_blocks_per_sm;
       if (*slot == vals[k]) continue;
       *slot = vals[k];

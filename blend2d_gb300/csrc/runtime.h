@@ -125,7 +125,7 @@ struct FrameTotals {
   uint32_t segs = 0, seglist = 0, cmdrows = 0, row_entries = 0, row_states = 0;
 };
 
-constexpr int kCounterWords = 32;
+constexpr int kCounterWords = 48;
 
 struct DeviceBuffer {
   void* ptr = nullptr;

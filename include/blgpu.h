@@ -109,7 +109,7 @@ typedef struct BLGpuStats {
  * band geometry are fixed by the pipeline (32-pixel tile columns matching a warp's lanes, the
  * reference's band heights), so the tunable parameters are how work is grouped and gridded. */
 typedef struct BLGpuLaunchConfig {
-  int32_t cover_group;          /* (command, strip, tile) slots per warp in the coverage pass: 8 or 16 */
+  int32_t raster_block;         /* threads per block of the coverage pass's raster kernel: 128 or 256 */
   int32_t cover_blocks_per_sm;  /* coverage pass grid */
   int32_t fine_blocks_per_sm;   /* composite pass grid */
   int32_t edge_block;           /* threads per block of the per-item edge builder: 64, 128 or 256 */
