@@ -182,7 +182,7 @@ struct FrameView {
   uint32_t* pixels;
   // K1
   DevItem* items;              // lines and curves of every analytic command (any order)
-  DevItem* cubic_items;        // cubic curves whose four points lie inside the clip box
+  DevItem* curve_items;        // cubic curves from the front, quadratic / conic curves from the back
   int4* cmd_bbox;              // [num_cmds] 24.8 bbox of the emitted segments: xmin, ymin, xmax, ymax
   DevSeg* segs;                // emitted segments (any order)
   uint32_t* seg_meta;          // cmd << 1 | sign
@@ -211,7 +211,7 @@ struct FrameView {
   uint32_t* row_cmds;          // command indices grouped by tile row, painter's order
   uint32_t* tile_order;        // tile processing order for the persistent fine kernel
   uint32_t* tile_canvas;       // canvas index per global tile
-  uint32_t* work_counter;      // [0] fine work queue, [1] items, [2] unclipped cubics, [3] their queue
+  uint32_t* work_counter;      // [0] fine work queue, [1] items, [2] cubics, [3] their queue, [21] quads, [22] their queue
   uint32_t* totals;            // [8] segments, seglist bound, (cmd,strip) slots, row entries, gradient rows
   uint32_t* rs_count;          // [num_cmds + 1] gradient row states per command (radial/conic styles)
   uint32_t* rs_base;           // exclusive scan of rs_count

@@ -942,6 +942,294 @@ __device__ void curve_to(Builder& eb, Src& src, Pt& p0, uint32_t& p0_flags, bool
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// One curve of an item, flattened one subdivision step per call (the lane-scheduled kernels call
+// step() once per iteration of a warp-wide loop, so the FP64 flatness test and split of all lanes
+// issue together whatever branch of the clipper each lane is in). The states are the loops of
+// flatten_safe / flatten_unsafe above and step() runs one pass of the loop body; the jumps between
+// the loops (goto in flatten_unsafe) become state changes taken within the same step. Every
+// piece emits the same segments and accumulations as flatten_safe / flatten_unsafe.
+// ---------------------------------------------------------------------------------------------
+
+enum : int {
+  kLsDone = 0,     // piece finished
+  kLsSafe,         // flatten_safe loop
+  kLsLTop,         // left-to-right, above the clip box
+  kLsLLeft,        // left-to-right, left of the clip box (LTR_BeforeX0)
+  kLsLIn,          // left-to-right, inside (LTR_AddLine)
+  kLsRTop,         // right-to-left, above the clip box
+  kLsRRight,       // right-to-left, right of the clip box (RTL_AfterX1)
+  kLsRIn           // right-to-left, inside (RTL_AddLine)
+};
+
+template<int DEG>
+struct LaneCurve {
+  Mono<DEG> mc;
+  Pt spline[DEG == 3 ? 25 : 7];
+  int nout, piece, state;
+  uint32_t any, sign, out;
+  double y_start, y_end;
+
+  // curve_to for a source holding exactly this one curve: p0 (with its clip flags) and
+  // spline[1..DEG] set by the caller. Returns false when the curve has nothing to flatten.
+  __device__ bool begin_curve(Builder& eb, Pt p0, uint32_t p0_flags) {
+    mc.tol_sq = eb.tol_sq;
+    uint32_t common = p0_flags, fl_any = p0_flags;
+#pragma unroll
+    for (int i = 1; i <= DEG; i++) { const uint32_t fl = eb.fxy(spline[i]); common &= fl; fl_any |= fl; }
+    if (common) {
+      if (!(common & (CF_Y0 | CF_Y1))) {
+        const double y0 = dclamp(p0.y, eb.cy0, eb.cy1), y1 = dclamp(spline[DEG].y, eb.cy0, eb.cy1);
+        if (common & CF_X0) eb.acc_left(y0, y1); else eb.acc_right(y0, y1);
+      }
+      return false;
+    }
+    spline[0] = p0;
+    nout = DEG == 3 ? split_cubic(spline) : split_quad(spline);
+    if (nout == 0) nout = DEG;
+    any = fl_any;
+    piece = 0;
+    return next_piece(eb, false);
+  }
+
+  // Starts the next piece with work (pieces that finish at their start are skipped). Returns
+  // false when the curve is done.
+  __device__ bool next_piece(Builder& eb, bool advance) {
+    if (advance) piece += DEG;
+    for (; piece < nout; piece += DEG) {
+      start_piece(eb);
+      if (state != kLsDone) return true;
+    }
+    return false;
+  }
+
+  __device__ void finish(Builder& eb) {
+    if (out && y_start < y_end) {
+      if (out & CF_X0) eb.acc_left_s(y_start, y_end, sign);
+      else eb.acc_right_s(y_start, y_end, sign);
+    }
+    state = kLsDone;
+  }
+  // Leaving a loop: the left-to-right top and inside loops and the right-to-left right loop
+  // shift `out` (1 -> CF_X1), the others leave it (1 = CF_X0).
+  __device__ __forceinline__ void exit_loop(Builder& eb, bool shift) {
+    if (shift) out <<= 2;
+    finish(eb);
+  }
+
+  __device__ void start_piece(Builder& eb) {
+    const Pt* sp = spline + piece;
+    sign = sp[0].y > sp[DEG].y;
+    mc.begin(sp, sign);
+    if (!any) {
+      if (mc.ltr()) mc.bound_ltr(); else mc.bound_rtl();
+      eb.desc_open(trunc_i(mc.first().x), trunc_i(mc.first().y), sign);
+      state = kLsSafe;
+      return;
+    }
+    state = kLsDone;
+    out = 0;
+    y_start = mc.first().y;
+    y_end = dmin(mc.last().y, eb.cy1);
+    if ((y_start >= y_end) | (y_end <= eb.cy0)) return;
+    const double kDeltaLimit = 0.00390625;
+    const double x_delta = fabs(mc.first().x - mc.last().x);
+    if (x_delta <= kDeltaLimit) {
+      y_start = dmax(y_start, eb.cy0);
+      const double x_min = dmin(mc.first().x, mc.last().x), x_max = dmax(mc.first().x, mc.last().x);
+      if (x_max <= eb.cx0) eb.acc_left_s(y_start, y_end, sign);
+      else if (x_min >= eb.cx1) eb.acc_right_s(y_start, y_end, sign);
+      else {
+        eb.desc_open(trunc_i(mc.first().x), trunc_i(y_start), sign);
+        eb.add(trunc_i(mc.last().x), trunc_i(y_end));
+      }
+      return;
+    }
+    if (mc.ltr()) {
+      mc.bound_ltr();
+      if (y_start < eb.cy0) { y_start = eb.cy0; state = kLsLTop; }
+      else if (y_start < eb.cy1) {
+        if (mc.first().x < eb.cx0) state = kLsLLeft;
+        else if (mc.first().x < eb.cx1) { eb.desc_open(trunc_i(mc.first().x), trunc_i(mc.first().y), sign); state = kLsLIn; }
+        else { out = CF_X1; finish(eb); }
+      }
+    }
+    else {
+      mc.bound_rtl();
+      if (y_start < eb.cy0) { y_start = eb.cy0; state = kLsRTop; }
+      else if (y_start < eb.cy1) {
+        if (mc.first().x > eb.cx1) state = kLsRRight;
+        else if (mc.first().x > eb.cx0) { eb.desc_open(trunc_i(mc.first().x), trunc_i(mc.first().y), sign); state = kLsRIn; }
+        else { out = CF_X0; finish(eb); }
+      }
+    }
+  }
+
+  // One pass of the current loop's body.
+  __device__ void step(Builder& eb) {
+    switch (state) {
+      case kLsLTop: out = mc.first().x >= eb.cx1; if (out) { exit_loop(eb, true); return; } break;
+      case kLsLLeft: out = mc.first().y >= eb.cy1; if (out) { exit_loop(eb, false); return; } break;
+      case kLsRTop: out = mc.first().x <= eb.cx0; if (out) { exit_loop(eb, false); return; } break;
+      case kLsRRight: out = mc.first().y >= eb.cy1; if (out) { exit_loop(eb, true); return; } break;
+      default: break;
+    }
+    Step st;
+    if (!mc.is_flat(st)) {
+      mc.split(st);
+      const Pt m = mc.step_mid(st);
+      const bool discard = ((state == kLsLTop) | (state == kLsRTop)) ? (m.y <= eb.cy0)
+                         : state == kLsLLeft ? (m.x <= eb.cx0)
+                         : state == kLsRRight ? (m.x >= eb.cx1) : false;
+      if (discard) { mc.discard_and_advance(st); return; }
+      if (mc.can_push()) { mc.push(st); return; }
+    }
+    leaf(eb);
+  }
+
+  __device__ void leaf(Builder& eb) {
+    const Pt a = mc.first(), b = mc.last();
+    switch (state) {
+      case kLsSafe:
+        eb.add(trunc_i(b.x), trunc_i(b.y));
+        if (!mc.can_pop()) { state = kLsDone; return; }
+        mc.pop();
+        return;
+      case kLsLTop:
+        if (b.y > eb.cy0) {
+          out = b.x < eb.cx0;
+          if (out) { l_left_pop(eb); return; }
+          const double xc = a.x + (eb.cy0 - a.y) * dx_div_dy(a, b);
+          if (xc <= eb.cx0) { l_left_clip(eb); return; }
+          out = xc >= eb.cx1;
+          if (out) { exit_loop(eb, true); return; }
+          eb.desc_open(trunc_i(xc), trunc_i(eb.cy0), sign);
+          l_add_line(eb);
+          return;
+        }
+        if (!mc.can_pop()) { exit_loop(eb, true); return; }
+        mc.pop();
+        return;
+      case kLsLLeft:
+        if (b.x > eb.cx0) { l_left_clip(eb); return; }
+        out = b.y >= y_end;
+        if (out) { exit_loop(eb, false); return; }
+        l_left_pop(eb);
+        return;
+      case kLsLIn:
+        l_add_line(eb);
+        return;
+      case kLsRTop:
+        if (b.y > eb.cy0) {
+          out = b.x > eb.cx1;
+          if (out) { r_right_pop(eb); return; }
+          const double xc = a.x + (eb.cy0 - a.y) * dx_div_dy(a, b);
+          if (xc >= eb.cx1) { r_right_clip(eb); return; }
+          out = xc <= eb.cx0;
+          if (out) { exit_loop(eb, false); return; }
+          eb.desc_open(trunc_i(xc), trunc_i(eb.cy0), sign);
+          r_add_line(eb);
+          return;
+        }
+        if (!mc.can_pop()) { exit_loop(eb, false); return; }
+        mc.pop();
+        return;
+      case kLsRRight:
+        if (b.x < eb.cx1) { r_right_clip(eb); return; }
+        out = b.y >= y_end;
+        if (out) { exit_loop(eb, true); return; }
+        r_right_pop(eb);
+        return;
+      case kLsRIn:
+        r_add_line(eb);
+        return;
+      default:
+        return;
+    }
+  }
+
+  __device__ void l_left_pop(Builder& eb) {           // LTR_BeforeX0_Pop
+    state = kLsLLeft;
+    if (!mc.can_pop()) { exit_loop(eb, false); return; }
+    mc.pop();
+  }
+  __device__ void l_left_clip(Builder& eb) {          // LTR_BeforeX0_Clip
+    state = kLsLLeft;
+    const Pt a = mc.first(), b = mc.last();
+    const double yc = a.y + (eb.cx0 - a.x) * dy_div_dx(a, b);
+    out = yc >= y_end;
+    if (out) { exit_loop(eb, false); return; }
+    if (y_start < yc) eb.acc_left_s(y_start, yc, sign);
+    eb.desc_open(trunc_i(eb.cx0), trunc_i(yc), sign);
+    l_add_line(eb);
+  }
+  __device__ void l_add_line(Builder& eb) {           // LTR_AddLine
+    state = kLsLIn;
+    const Pt a = mc.first(), b = mc.last();
+    out = b.x > eb.cx1;
+    if (out) {
+      const double yc = a.y + (eb.cx1 - a.x) * dy_div_dx(a, b);
+      if (yc <= y_end) {
+        y_start = yc;
+        eb.add(trunc_i(eb.cx1), trunc_i(yc));
+        exit_loop(eb, true);
+        return;
+      }
+    }
+    out = b.y >= eb.cy1;
+    if (out) {
+      const double xc = dmin(a.x + (eb.cy1 - a.y) * dx_div_dy(a, b), eb.cx1);
+      eb.add(trunc_i(xc), trunc_i(eb.cy1));
+      out = 0;
+      exit_loop(eb, true);
+      return;
+    }
+    eb.add(trunc_i(b.x), trunc_i(b.y));
+    if (!mc.can_pop()) { exit_loop(eb, true); return; }
+    mc.pop();
+  }
+  __device__ void r_right_pop(Builder& eb) {          // RTL_AfterX1_Pop
+    state = kLsRRight;
+    if (!mc.can_pop()) { exit_loop(eb, true); return; }
+    mc.pop();
+  }
+  __device__ void r_right_clip(Builder& eb) {         // RTL_AfterX1_Clip
+    state = kLsRRight;
+    const Pt a = mc.first(), b = mc.last();
+    const double yc = a.y + (eb.cx1 - a.x) * dy_div_dx(a, b);
+    out = yc >= y_end;
+    if (out) { exit_loop(eb, true); return; }
+    if (y_start < yc) eb.acc_right_s(y_start, yc, sign);
+    eb.desc_open(trunc_i(eb.cx1), trunc_i(yc), sign);
+    r_add_line(eb);
+  }
+  __device__ void r_add_line(Builder& eb) {           // RTL_AddLine
+    state = kLsRIn;
+    const Pt a = mc.first(), b = mc.last();
+    out = b.x < eb.cx0;
+    if (out) {
+      const double yc = a.y + (eb.cx0 - a.x) * dy_div_dx(a, b);
+      if (yc <= y_end) {
+        y_start = yc;
+        eb.add(trunc_i(eb.cx0), trunc_i(yc));
+        exit_loop(eb, false);
+        return;
+      }
+    }
+    out = b.y >= eb.cy1;
+    if (out) {
+      const double xc = dmax(a.x + (eb.cy1 - a.y) * dx_div_dy(a, b), eb.cx0);
+      eb.add(trunc_i(xc), trunc_i(eb.cy1));
+      out = 0;
+      exit_loop(eb, false);
+      return;
+    }
+    eb.add(trunc_i(b.x), trunc_i(b.y));
+    if (!mc.can_pop()) { exit_loop(eb, false); return; }
+    mc.pop();
+  }
+};
+
 // add_from_source (edgebuilder_p.h:1032-1070) for a closed fill. Returns 0 or 1 (invalid).
 __device__ int build(Builder& eb, Src& src) {
   Pt a;

@@ -309,69 +309,64 @@ __global__ void classify_kernel(FrameView f) {
       return;
     }
   }
-  // Cubic curves with all four points inside the clip box go to their own list (built by
-  // edge_cubics_kernel); everything else is built by edge_items_kernel.
-  const DevXform xf = f.xforms[cmd.xform];
-  const double* xy = f.verts + 2ull * cmd.geom_first;
-  const DevCanvas& cv = f.canvases[cmd.canvas];
-  const double cx1 = double(cv.w) * 256.0, cy1 = double(cv.h) * 256.0;
-  auto inside = [&](int k) {
-    double x = xy[2 * k], y = xy[2 * k + 1], tx, ty;
-    if (xf.affine) { tx = x * xf.m[0] + y * xf.m[2] + xf.m[4]; ty = x * xf.m[1] + y * xf.m[3] + xf.m[5]; }
-    else { tx = x * xf.m[0] + xf.m[4]; ty = y * xf.m[3] + xf.m[5]; }
-    return (tx >= 0.0) & (tx <= cx1) & (ty >= 0.0) & (ty <= cy1);
-  };
-  auto unclipped_cubic = [&](uint32_t kind, int a, int b) {
-    return kind == kItemCubic && inside(a) && inside(b) && inside(b + 1) && inside(b + 2);
-  };
-  uint32_t count = 0, cubics = 0;
-  for_each_item(pc, n, [&](uint32_t kind, int a, int b) {
-    if (unclipped_cubic(kind, a, b)) cubics++; else count++;
+  // Lines go to the item list (edge_items_kernel); cubic curves to the front of the curve list
+  // and quadratic / conic curves to its back (edge_curves_kernel<3> / <2>).
+  uint32_t lines = 0, cubics = 0, quads = 0;
+  for_each_item(pc, n, [&](uint32_t kind, int, int) {
+    lines += kind == kItemLine ? 1u : 0u;
+    cubics += kind == kItemCubic ? 1u : 0u;
+    quads += (kind == kItemQuad) | (kind == kItemConic) ? 1u : 0u;
   });
-  uint32_t base = count ? atomicAdd(f.work_counter + 1, count) : 0u;
+  uint32_t base = lines ? atomicAdd(f.work_counter + 1, lines) : 0u;
   uint32_t cbase = cubics ? atomicAdd(f.work_counter + 2, cubics) : 0u;
+  uint32_t qbase = quads ? atomicAdd(f.work_counter + 21, quads) : 0u;
   for_each_item(pc, n, [&](uint32_t kind, int a, int b) {
     const DevItem it{c, kind, uint32_t(a), uint32_t(b)};
-    if (unclipped_cubic(kind, a, b)) {
-      if (cbase < f.item_capacity) f.cubic_items[cbase] = it;
+    if (kind == kItemLine) {
+      if (base < f.item_capacity) f.items[base] = it;
+      base++;
+    }
+    else if (kind == kItemCubic) {
+      if (cbase < f.item_capacity) f.curve_items[cbase] = it;
       cbase++;
     }
     else {
-      if (base < f.item_capacity) f.items[base] = it;
-      base++;
+      if (qbase < f.item_capacity) f.curve_items[f.item_capacity - 1u - qbase] = it;
+      qbase++;
     }
   });
 }
 
-// Unclipped cubic curves (classify's second list): split into monotonic pieces and flattened with
-// the reference's safe flattener (flatten_safe, edgebuilder_p.h:2029-2445), but scheduled per
-// lane: every lane advances its own curve by one subdivision step per iteration of a warp-wide
-// loop and takes the next curve from the list as soon as its current one is done, so the lanes
-// stay busy whatever the curves' subdivision depths. Each curve's segments are the same as when
-// it is built alone.
-__global__ void __launch_bounds__(128) edge_cubics_kernel(FrameView f) {
+// Curves (classify's curve list: cubics from the front, quadratic and conic curves from the
+// back), flattened per lane: every lane advances its own curve by one subdivision step per
+// iteration of a warp-wide loop (eb::LaneCurve) and takes the next curve from the list as soon as
+// its current one is done, so the lanes stay busy whatever the curves' subdivision depths and
+// clipping paths. Each curve is built by its own builder, as curve_to builds it
+// (edgebuilder_p.h:1618-2022) when the source holds just that curve.
+__device__ __forceinline__ void finish_curve(FrameView& f, eb::Builder& b, uint32_t cmd, uint32_t& rows) {
+  b.done();
+  b.sink.flush();
+  if (b.sink.n) {
+    int4* bb = f.cmd_bbox + cmd;
+    atomicMin(&bb->x, b.sink.xmin);
+    atomicMin(&bb->y, b.sink.ymin);
+    atomicMax(&bb->z, b.sink.xmax);
+    atomicMax(&bb->w, b.sink.ymax);
+    atomicOr(&f.cmds_rw[cmd].status, kCmdHasSegments);
+    rows += b.sink.rows;
+  }
+}
+
+template<int DEG>
+__global__ void __launch_bounds__(128) edge_curves_kernel(FrameView f) {
   const int lane = threadIdx.x & 31;
-  const uint32_t n_items = min(f.work_counter[2], f.item_capacity);
-  const double tol = 0.20 * 256.0;
+  const uint32_t n_cubic = min(f.work_counter[2], f.item_capacity);
+  const uint32_t n_items = DEG == 3 ? n_cubic : min(f.work_counter[21], f.item_capacity - n_cubic);
+  uint32_t* queue = f.work_counter + (DEG == 3 ? 3 : 22);
   eb::Builder b;
-  b.tol_sq = tol * tol;
-  b.px = b.py = 0; b.psign = 0; b.pasc = false;
-  b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, 0u);
-  eb::Mono<3> mc;
-  mc.tol_sq = b.tol_sq;
-  mc.sp = 0;
-  eb::Pt spline[25];
-  int nout = 0, piece = 0;
+  eb::LaneCurve<DEG> lc;
   bool busy = false, exhausted = false;
   uint32_t cur = 0, rows = 0;
-
-  auto start_piece = [&]() {
-    const eb::Pt* sp = spline + piece;
-    uint32_t sign = sp[0].y > sp[3].y;
-    mc.begin(sp, sign);
-    if (mc.ltr()) mc.bound_ltr(); else mc.bound_rtl();
-    b.desc_open(eb::trunc_i(mc.first().x), eb::trunc_i(mc.first().y), sign);
-  };
 
   for (;;) {
     // hand the next curves of the list to the idle lanes (one atomic per warp)
@@ -379,7 +374,7 @@ __global__ void __launch_bounds__(128) edge_cubics_kernel(FrameView f) {
     if (want) {
       const int leader = __ffs(want) - 1;
       uint32_t base = 0;
-      if (lane == leader) base = atomicAdd(f.work_counter + 3, uint32_t(__popc(want)));
+      if (lane == leader) base = atomicAdd(queue, uint32_t(__popc(want)));
       base = __shfl_sync(0xFFFFFFFFu, base, leader);
       if (!busy && !exhausted) {
         const uint32_t t = base + uint32_t(__popc(want & ((1u << lane) - 1u)));
@@ -387,55 +382,31 @@ __global__ void __launch_bounds__(128) edge_cubics_kernel(FrameView f) {
           exhausted = true;
         }
         else {
-          const DevItem it = f.cubic_items[t];
+          const DevItem it = f.curve_items[DEG == 3 ? t : f.item_capacity - 1u - t];
           const DevCmd& cmd = f.cmds[it.cmd];
           const DevXform& xf = f.xforms[cmd.xform];
+          init_builder(b, f.canvases[cmd.canvas]);
+          b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, it.cmd);
           eb::Src src;
           src.xy = f.verts + 2ull * cmd.geom_first;
           src.affine = xf.affine != 0;
           src.m00 = xf.m[0]; src.m01 = xf.m[1]; src.m10 = xf.m[2]; src.m11 = xf.m[3]; src.m20 = xf.m[4]; src.m21 = xf.m[5];
-          spline[0] = src.tf(int(it.a));
-          spline[1] = src.tf(int(it.b));
-          spline[2] = src.tf(int(it.b) + 1);
-          spline[3] = src.tf(int(it.b) + 2);
-          nout = eb::split_cubic(spline);
-          if (nout == 0) nout = 3;
-          piece = 0;
+          const eb::Pt p0 = src.tf(int(it.a));
+          lc.spline[1] = src.tf(int(it.b));
+          if (DEG == 3) { lc.spline[2] = src.tf(int(it.b) + 1); lc.spline[DEG] = src.tf(int(it.b) + 2); }
+          else lc.spline[DEG] = src.tf(int(it.b) + (it.kind == kItemConic ? 2 : 1));
           cur = it.cmd;
-          b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, cur);
-          start_piece();
-          busy = true;
+          busy = lc.begin_curve(b, p0, b.fxy(p0));
+          if (!busy) finish_curve(f, b, cur, rows);
         }
       }
     }
-    if (__all_sync(0xFFFFFFFFu, !busy)) break;     // every lane idle: the list is exhausted
+    if (__all_sync(0xFFFFFFFFu, !busy && exhausted)) break;   // the list is exhausted
     if (busy) {
-      eb::Step st;
-      if (!mc.is_flat(st) && mc.can_push()) {
-        mc.split(st);
-        mc.push(st);
-      }
-      else {
-        b.add(eb::trunc_i(mc.last().x), eb::trunc_i(mc.last().y));
-        if (mc.can_pop()) {
-          mc.pop();
-        }
-        else if ((piece += 3) < nout) {
-          start_piece();
-        }
-        else {
-          b.sink.flush();
-          if (b.sink.n) {
-            int4* bb = f.cmd_bbox + cur;
-            atomicMin(&bb->x, b.sink.xmin);
-            atomicMin(&bb->y, b.sink.ymin);
-            atomicMax(&bb->z, b.sink.xmax);
-            atomicMax(&bb->w, b.sink.ymax);
-            atomicOr(&f.cmds_rw[cur].status, kCmdHasSegments);
-            rows += b.sink.rows;
-          }
-          busy = false;
-        }
+      lc.step(b);
+      if (lc.state == eb::kLsDone && !lc.next_piece(b, true)) {
+        finish_curve(f, b, cur, rows);
+        busy = false;
       }
     }
   }
@@ -444,9 +415,9 @@ __global__ void __launch_bounds__(128) edge_cubics_kernel(FrameView f) {
 }
 
 __global__ void __launch_bounds__(256) edge_items_kernel(FrameView f) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t rows = 0;
-  uint32_t n_items = min(f.work_counter[1], f.item_capacity);
+  const uint32_t n_items = min(f.work_counter[1], f.item_capacity);
   if (t < n_items) {
     const DevItem it = f.items[t];
     const DevCmd cmd = f.cmds[it.cmd];
@@ -1111,7 +1082,7 @@ int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, edge_cubics_kernel, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, edge_curves_kernel<3>, 128, 0);
     if (max_per_sm < 1) max_per_sm = 1;
   }
   const int per_sm = cfg.cubic_blocks_per_sm > 0 && cfg.cubic_blocks_per_sm < max_per_sm ? cfg.cubic_blocks_per_sm : max_per_sm;
@@ -1120,8 +1091,9 @@ int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   edge_items_kernel<<<cdiv(f.item_capacity ? f.item_capacity : 1, eb), eb, 0, st>>>(f);
   uint32_t grid = cdiv(f.item_capacity ? f.item_capacity : 1, 128);
   uint32_t cubic_grid = uint32_t(sms * per_sm);
-  edge_cubics_kernel<<<grid < cubic_grid ? grid : cubic_grid, 128, 0, st>>>(f);
-  return 3;
+  edge_curves_kernel<3><<<grid < cubic_grid ? grid : cubic_grid, 128, 0, st>>>(f);
+  edge_curves_kernel<2><<<sms, 128, 0, st>>>(f);
+  return 4;
 }
 
 int launch_cmd_tiles(const FrameView& f, uint32_t* cmdrow_counts_per_cmd, cudaStream_t st) {

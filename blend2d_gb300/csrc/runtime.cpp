@@ -202,7 +202,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
       if (cpix) (*cpix)[i] = p;
     }
     v.items = L.take<DevItem>(item_capacity);
-    v.cubic_items = L.take<DevItem>(item_capacity);
+    v.curve_items = L.take<DevItem>(item_capacity);
     v.cmd_bbox = L.take<int4>(nc);
     v.cmd_tile_x = L.take<uint32_t>(nc);
     v.cmd_tile_y = L.take<uint32_t>(nc);
@@ -215,8 +215,9 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     row_canvas = L.take<uint32_t>(fr.rows + 1);
     v.tile_order = L.take<uint32_t>(fr.tiles + 1);
     v.tile_canvas = L.take<uint32_t>(fr.tiles + 1);
-    // [0] work queue, [1] items, [4..12) totals, [12..16) error flags, [16..20) pixel ops (2 x u64),
-    // [32..48) raster work per DDA kind
+    // [0] work queue, [1] line items, [2] cubic curves, [3] their queue, [4..12) totals,
+    // [12..16) error flags, [16..20) pixel ops (2 x u64), [21] quadratic / conic curves, [22] their
+    // queue, [32..48) raster work per DDA kind
     v.work_counter = L.take<uint32_t>(kCounterWords);
     v.totals = v.work_counter + 4;
     v.error_flags = v.work_counter + 12;
@@ -529,7 +530,7 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     v.images = L.take<uint32_t>(fr.image_words);
     v.luts = L.take<uint32_t>(fr.lut_words);
     v.items = L.take<DevItem>(item_capacity);
-    v.cubic_items = L.take<DevItem>(item_capacity);
+    v.curve_items = L.take<DevItem>(item_capacity);
     v.cmd_bbox = L.take<int4>(nc);
     v.cmd_tile_x = L.take<uint32_t>(nc);
     v.cmd_tile_y = L.take<uint32_t>(nc);
