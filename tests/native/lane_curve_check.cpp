@@ -1,0 +1,116 @@
+// Host build of the device edge builder (edge_build.cuh) checking that the lane-stepped curve
+// flattener (eb::LaneCurve, one subdivision step per call) emits exactly the segments, in the same
+// order, as the loop flattener (eb::curve_to) for random cubic, quadratic and conic curves around
+// and across the clip box. Usage: lane_curve_check <seed> <curves>; exit status 0 when all match.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#define __device__
+#define __forceinline__ inline
+using std::max;
+using std::min;
+static inline long long __double_as_longlong(double x) { long long v; memcpy(&v, &x, 8); return v; }
+static inline uint32_t atomicAdd(uint32_t* p, uint32_t v) { uint32_t o = *p; *p += v; return o; }
+#include "edge_build.cuh"
+
+using namespace blgpu;
+using namespace blgpu::eb;
+
+struct Out { std::vector<DevSeg> segs; std::vector<uint32_t> meta; uint32_t counter = 0; };
+
+static void init_builder(Builder& b, double w, double h, Out& o) {
+  b.cx0 = 0.0; b.cy0 = 0.0; b.cx1 = w * 256.0; b.cy1 = h * 256.0;
+  b.icx0 = trunc_i(b.cx0); b.icx1 = trunc_i(b.cx1);
+  const double tol = 0.20 * 256.0;
+  b.tol_sq = tol * tol;
+  b.acc_x0_y0 = b.acc_x0_y1 = b.acc_x1_y0 = b.acc_x1_y1 = b.cy0;
+  b.px = b.py = 0; b.psign = 0; b.pasc = false;
+  if (o.segs.empty()) { o.segs.resize(1 << 14); o.meta.resize(1 << 14); }
+  o.counter = 0;
+  b.sink.init(o.segs.data(), o.meta.data(), &o.counter, 1u << 14, 7u);
+}
+
+template<int DEG>
+static bool same_segments(const double* xy, const uint8_t* cmd, int npts, bool conic, double w, double h) {
+  Src src;
+  src.xy = xy; src.cmd = cmd; src.affine = false;
+  src.m00 = 256.0; src.m01 = 0.0; src.m10 = 0.0; src.m11 = 256.0; src.m20 = 0.0; src.m21 = 0.0;
+
+  static Out o1, o2;
+  Builder b1;
+  init_builder(b1, w, h, o1);
+  Pt p0 = src.tf(0);
+  uint32_t f0 = b1.fxy(p0);
+  src.i = 1; src.n = npts;
+  curve_to<DEG>(b1, src, p0, f0, conic);
+  b1.done(); b1.sink.flush();
+
+  Builder b2;
+  init_builder(b2, w, h, o2);
+  LaneCurve<DEG> lc;
+  const Pt q0 = src.tf(0);
+  lc.spline[1] = src.tf(1);
+  if (DEG == 3) { lc.spline[2] = src.tf(2); lc.spline[3] = src.tf(3); }
+  else lc.spline[DEG] = src.tf(conic ? 3 : 2);
+  bool busy = lc.begin_curve(b2, q0, b2.fxy(q0));
+  for (long guard = 0; busy; guard++) {
+    if (guard > 10000000) return false;
+    lc.step(b2);
+    if (lc.state == kLsDone && !lc.next_piece(b2, true)) busy = false;
+  }
+  b2.done(); b2.sink.flush();
+
+  if (o1.counter != o2.counter || o1.counter > (1u << 14)) return false;
+  for (uint32_t i = 0; i < o1.counter; i++) {
+    const DevSeg &a = o1.segs[i], &c = o2.segs[i];
+    if (a.x0 != c.x0 || a.y0 != c.y0 || a.x1 != c.x1 || a.y1 != c.y1 || o1.meta[i] != o2.meta[i]) return false;
+  }
+  return true;
+}
+
+int main(int argc, char** argv) {
+  std::mt19937_64 rng(argc > 1 ? strtoull(argv[1], nullptr, 10) : 1);
+  const int n = argc > 2 ? atoi(argv[2]) : 100000;
+  std::uniform_real_distribution<double> u(0.0, 1.0);
+  long fails = 0;
+  for (int it = 0; it < n; it++) {
+    const double w = 16 + std::floor(u(rng) * 200), h = 16 + std::floor(u(rng) * 200);
+    // mostly around the canvas; some points on its borders, on the pixel grid, or far outside
+    auto coord = [&](double lim) {
+      const double r = u(rng);
+      if (r < 0.08) return 0.0;
+      if (r < 0.16) return lim;
+      if (r < 0.22) return std::floor(u(rng) * lim);
+      if (r < 0.26) return -1e6 + 2e6 * u(rng);
+      if (r < 0.6) return std::floor(-0.25 * lim + 1.5 * lim * u(rng)) + (u(rng) < 0.5 ? 0.5 : 0.0);
+      return -0.5 * lim + 2.0 * lim * u(rng);
+    };
+    double xy[8];
+    for (int k = 0; k < 4; k++) { xy[2 * k] = coord(w); xy[2 * k + 1] = coord(h); }
+    if (u(rng) < 0.1) xy[2] = xy[0];
+    if (u(rng) < 0.05) xy[7] = xy[1];
+    bool ok;
+    if (it % 3 == 0) {
+      const uint8_t c[4] = {0, 4, 4, 4};
+      ok = same_segments<3>(xy, c, 4, false, w, h);
+    }
+    else if (it % 3 == 1) {
+      const uint8_t c[3] = {0, 2, 2};
+      ok = same_segments<2>(xy, c, 3, false, w, h);
+    }
+    else {
+      const uint8_t c[4] = {0, 3, 3, 3};
+      const double cx[8] = {xy[0], xy[1], xy[2], xy[3], 1.0, 0.0, xy[4], xy[5]};
+      ok = same_segments<2>(cx, c, 4, true, w, h);
+    }
+    if (!ok && ++fails <= 5) printf("mismatch: curve %d (kind %d)\n", it, it % 3);
+  }
+  printf("curves %d mismatches %ld\n", n, fails);
+  return fails ? 1 : 0;
+}
