@@ -542,6 +542,17 @@ struct Step { double value, limit; Pt p01, p12, p23, p012, p123, p0123; };
 
 __device__ __forceinline__ Pt mid(Pt a, Pt b) { return Pt{(a.x + b.x) * 0.5, (a.y + b.y) * 0.5}; }
 
+// v * 0.5 by decrementing the exponent field: exact, and so equal to the multiply, for biased
+// exponents 2..0x7FE. `ok` is cleared for the other values (zero, subnormal, the smallest normal
+// exponent, inf, NaN), for which the caller falls back to the multiply. This keeps the halvings of
+// the subdivision off the FP64 pipe, which bounds the flattening kernels.
+__device__ __forceinline__ double half_exp(double v, bool& ok) {
+  const int hi = __double2hiint(v), lo = __double2loint(v);
+  ok &= ((unsigned(hi) >> 20) & 0x7FFu) - 2u < 0x7FDu;
+  return __hiloint2double(hi - 0x100000, lo);
+}
+__device__ __forceinline__ Pt mid_exp(Pt a, Pt b, bool& ok) { return Pt{half_exp(a.x + b.x, ok), half_exp(a.y + b.y, ok)}; }
+
 // Monotonic curve with an explicit subdivision stack (FlattenMonoQuad / FlattenMonoCubic).
 template<int DEG>
 struct Mono {
@@ -588,12 +599,18 @@ struct Mono {
     return s.value <= s.limit;
   }
   __device__ void split(Step& s) const {
+    bool ok = true;
     if (DEG == 2) {
-      s.p01 = mid(p[0], p[1]); s.p12 = mid(p[1], p[2]); s.p012 = mid(s.p01, s.p12);
+      s.p01 = mid_exp(p[0], p[1], ok); s.p12 = mid_exp(p[1], p[2], ok); s.p012 = mid_exp(s.p01, s.p12, ok);
+      if (!ok) { s.p01 = mid(p[0], p[1]); s.p12 = mid(p[1], p[2]); s.p012 = mid(s.p01, s.p12); }
     }
     else {
-      s.p01 = mid(p[0], p[1]); s.p12 = mid(p[1], p[2]); s.p23 = mid(p[2], p[DEG]);
-      s.p012 = mid(s.p01, s.p12); s.p123 = mid(s.p12, s.p23); s.p0123 = mid(s.p012, s.p123);
+      s.p01 = mid_exp(p[0], p[1], ok); s.p12 = mid_exp(p[1], p[2], ok); s.p23 = mid_exp(p[2], p[DEG], ok);
+      s.p012 = mid_exp(s.p01, s.p12, ok); s.p123 = mid_exp(s.p12, s.p23, ok); s.p0123 = mid_exp(s.p012, s.p123, ok);
+      if (!ok) {
+        s.p01 = mid(p[0], p[1]); s.p12 = mid(p[1], p[2]); s.p23 = mid(p[2], p[DEG]);
+        s.p012 = mid(s.p01, s.p12); s.p123 = mid(s.p12, s.p23); s.p0123 = mid(s.p012, s.p123);
+      }
     }
   }
   __device__ __forceinline__ Pt step_mid(const Step& s) const { return DEG == 2 ? s.p012 : s.p0123; }

@@ -50,49 +50,12 @@ __device__ __forceinline__ int round_to_int(double x) {
 }
 
 // One interpolation span of a LUT builder: the FP64 part of the builder (stop positions and the
-// per-channel increments) is evaluated once per span by one thread; entries only do integer work.
+// per-channel increments) is evaluated once per span, one lane per stop; entries only do integer work.
 struct LutSpan {
   uint32_t start, count;   // simd: first entry and i (entries start .. start + i); scalar: start, cnt
   uint32_t c0, c1;         // colours at both ends (scalar: after its equal-position rule)
   int32_t inc[4];          // simd: dx per channel (b, g, r, a); scalar: r, g, b, a increments
 };
-
-// Sequential state of a builder between span-table chunks.
-struct LutCarry {
-  uint32_t si;             // next stop
-  uint32_t u0;             // previous stop position (24.8)
-  uint32_t c0, c1;         // previous colours
-};
-
-constexpr int kLutChunk = 128;
-
-// Next spans of the SSE2/AVX2 builders (interpolation_sse2.cpp:18-171, interpolation_avx2.cpp:18-177).
-__device__ int lut_spans_simd(const DevStop* s, uint32_t n, uint32_t size, LutCarry& cr, LutSpan* out) {
-  double fWidth = double(int32_t(size - 1u) << 8);
-  int k = 0;
-  for (; cr.si < n && k < kLutChunk; cr.si++) {
-    uint32_t c1 = rgba32_of(s[cr.si].rgba64);
-    uint32_t u1 = uint32_t(round_to_int(s[cr.si].offset * fWidth));
-    LutSpan sp;
-    sp.start = cr.u0 >> 8;
-    sp.count = (u1 >> 8) - (cr.u0 >> 8);
-    sp.c0 = cr.c0;
-    sp.c1 = c1;
-    cr.u0 = u1;
-    if (sp.count > 1) {
-      double scale = double(1 << 23) / double(int(sp.count));
-      for (int ch = 0; ch < 4; ch++) {
-        int32_t cc = int32_t((cr.c0 >> (8 * ch)) & 255u);
-        int32_t dd = int32_t((c1 >> (8 * ch)) & 255u) - cc;
-        double p = double(dd) * scale;
-        sp.inc[ch] = (p > -2147483649.0 && p < 2147483648.0) ? __double2int_rz(p) : INT32_MIN;
-      }
-    }
-    out[k++] = sp;
-    cr.c0 = c1;
-  }
-  return k;
-}
 
 __device__ uint32_t lut_eval_simd(const LutSpan* sp, int nspans, uint32_t e, uint32_t val, bool avx2) {
   for (int k = 0; k < nspans; k++) {
@@ -117,36 +80,6 @@ __device__ uint32_t lut_eval_simd(const LutSpan* sp, int nspans, uint32_t e, uin
     }
   }
   return val;
-}
-
-// Next spans of the portable builder (interpolation.cpp:19-156).
-__device__ int lut_spans_scalar(const DevStop* s, uint32_t n, uint32_t size, LutCarry& cr, LutSpan* out) {
-  double fWidth = double(int32_t(size - 1u) << 8);
-  int k = 0;
-  for (; cr.si < n && k < kLutChunk; cr.si++) {
-    cr.c1 = rgba32_of(s[cr.si].rgba64);
-    uint32_t p1 = uint32_t(round_to_int(s[cr.si].offset * fWidth));
-    uint32_t i = (p1 >> 8) - (cr.u0 >> 8);
-    LutSpan sp;
-    sp.start = cr.u0 >> 8;
-    if (i == 0) cr.c0 = cr.c1;
-    cr.u0 = p1;
-    sp.count = i + 1u;
-    sp.c0 = cr.c0;
-    sp.c1 = cr.c1;
-    if (cr.c0 != cr.c1 && sp.count > 1) {
-      const uint32_t kMask = 0xFFu << 23;
-      int32_t div = int32_t(sp.count - 1u);
-      uint32_t c0 = cr.c0, c1 = cr.c1;
-      sp.inc[0] = int32_t(((c1 << 7) & kMask) - ((c0 << 7) & kMask)) / div;
-      sp.inc[1] = int32_t(((c1 << 15) & kMask) - ((c0 << 15) & kMask)) / div;
-      sp.inc[2] = int32_t(((c1 << 23) & kMask) - ((c0 << 23) & kMask)) / div;
-      sp.inc[3] = int32_t(((c1 >> 1) & kMask) - ((c0 >> 1) & kMask)) / div;
-    }
-    out[k++] = sp;
-    if (cr.c0 != cr.c1) cr.c0 = cr.c1;
-  }
-  return k;
 }
 
 __device__ uint32_t lut_eval_scalar(const LutSpan* sp, int nspans, uint32_t e, uint32_t val) {
@@ -184,54 +117,95 @@ __device__ uint32_t lut_eval_scalar(const LutSpan* sp, int nspans, uint32_t e, u
   return val;
 }
 
-// One block per LUT. Thread 0 builds the span table in chunks of kLutChunk spans in shared memory;
-// after each chunk every thread applies it to its entries (the entry's value is whatever the
-// reference's sequential span writer leaves there: later spans overwrite earlier ones), carrying
-// the values through the LUT itself. The trailing fill and entry 0 are applied last.
-__global__ void lut_kernel(const DevLutJob* jobs, const DevStop* stops, uint32_t* luts) {
-  __shared__ LutSpan spans[kLutChunk];
-  __shared__ int nspans;
-  __shared__ uint32_t span_end;
-  __shared__ LutCarry carry;
-  const DevLutJob job = jobs[blockIdx.x];
+// One warp per LUT. The span table is built 32 stops at a time, one stop per lane: a span depends
+// only on its stop and the one before it (position and colour, passed up one lane; the previous
+// chunk's last stop is carried), so the FP64 stop positions and increments of a chunk are computed
+// in parallel. Every lane then applies the chunk's spans, in order, to its entries (the entry's
+// value is whatever the reference's sequential span writer leaves there: later spans overwrite
+// earlier ones). The trailing fill and entry 0 are applied last.
+constexpr int kLutWarps = 8;
+
+__global__ void __launch_bounds__(32 * kLutWarps) lut_kernel(const DevLutJob* jobs, const DevStop* stops, uint32_t* luts,
+                                                             uint32_t num_jobs) {
+  __shared__ LutSpan spans_all[kLutWarps][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t jid = blockIdx.x * kLutWarps + uint32_t(warp);
+  if (jid >= num_jobs) return;                         // whole warps leave together
+  LutSpan* spans = spans_all[warp];
+  const DevLutJob job = jobs[jid];
   const DevStop* s = stops + job.stop_first;
   const uint32_t n = job.stop_count;
   const bool scalar = job.variant == kLutScalar;
   const bool avx2 = job.variant == kLutAVX2;
   uint32_t* lut = luts + job.lut_offset;
   const uint32_t first_c = rgba32_of(s[0].rgba64);
-  if (threadIdx.x == 0) {
-    carry.si = (!scalar && s[0].offset == 0.0 && n > 1) ? 1u : 0u;
-    carry.u0 = 0;
-    carry.c0 = first_c;
-    carry.c1 = first_c;
-    span_end = 0;
-  }
+  const double fWidth = double(int32_t(job.lut_size - 1u) << 8);
+  uint32_t car_u0 = 0, car_c0 = first_c, car_c1 = first_c, span_end = 0;
   bool first_chunk = true;
-  for (;;) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      nspans = scalar ? lut_spans_scalar(s, n, job.lut_size, carry, spans)
-                      : lut_spans_simd(s, n, job.lut_size, carry, spans);
-      if (nspans) span_end = spans[nspans - 1].start + spans[nspans - 1].count + (scalar ? 0u : 1u);
+  for (uint32_t si = (!scalar && s[0].offset == 0.0 && n > 1) ? 1u : 0u; si < n; si += 32) {
+    const uint32_t k = si + uint32_t(lane);
+    const int ns = int(min(32u, n - si));
+    uint32_t c1 = 0, u1 = 0;
+    if (k < n) {
+      c1 = rgba32_of(s[k].rgba64);
+      u1 = uint32_t(round_to_int(s[k].offset * fWidth));
     }
-    __syncthreads();
-    int ns = nspans;
-    if (!ns) break;
-    for (uint32_t e = threadIdx.x; e < job.lut_size; e += blockDim.x) {
-      uint32_t v = first_chunk ? 0u : lut[e];
+    uint32_t u0 = __shfl_up_sync(0xFFFFFFFFu, u1, 1), c0 = __shfl_up_sync(0xFFFFFFFFu, c1, 1);
+    if (lane == 0) { u0 = car_u0; c0 = car_c0; }
+    if (lane < ns) {
+      LutSpan sp;
+      sp.start = u0 >> 8;
+      if (scalar) {                                     // lut_spans_scalar, one stop
+        const uint32_t i = (u1 >> 8) - (u0 >> 8);
+        if (i == 0) c0 = c1;
+        sp.count = i + 1u;
+        sp.c0 = c0;
+        sp.c1 = c1;
+        if (c0 != c1 && sp.count > 1) {
+          const uint32_t kMask = 0xFFu << 23;
+          const int32_t div = int32_t(sp.count - 1u);
+          sp.inc[0] = int32_t(((c1 << 7) & kMask) - ((c0 << 7) & kMask)) / div;
+          sp.inc[1] = int32_t(((c1 << 15) & kMask) - ((c0 << 15) & kMask)) / div;
+          sp.inc[2] = int32_t(((c1 << 23) & kMask) - ((c0 << 23) & kMask)) / div;
+          sp.inc[3] = int32_t(((c1 >> 1) & kMask) - ((c0 >> 1) & kMask)) / div;
+        }
+      }
+      else {                                            // lut_spans_simd, one stop
+        sp.count = (u1 >> 8) - (u0 >> 8);
+        sp.c0 = c0;
+        sp.c1 = c1;
+        if (sp.count > 1) {
+          const double scale = double(1 << 23) / double(int(sp.count));
+          for (int ch = 0; ch < 4; ch++) {
+            const int32_t cc = int32_t((c0 >> (8 * ch)) & 255u);
+            const int32_t dd = int32_t((c1 >> (8 * ch)) & 255u) - cc;
+            const double pv = double(dd) * scale;
+            sp.inc[ch] = (pv > -2147483649.0 && pv < 2147483648.0) ? __double2int_rz(pv) : INT32_MIN;
+          }
+        }
+      }
+      spans[lane] = sp;
+    }
+    // carry the chunk's last stop
+    car_u0 = __shfl_sync(0xFFFFFFFFu, u1, ns - 1);
+    car_c1 = __shfl_sync(0xFFFFFFFFu, c1, ns - 1);
+    car_c0 = car_c1;
+    __syncwarp();
+    span_end = spans[ns - 1].start + spans[ns - 1].count + (scalar ? 0u : 1u);
+    for (uint32_t e = uint32_t(lane); e < job.lut_size; e += 32) {
+      const uint32_t v = first_chunk ? 0u : lut[e];
       lut[e] = scalar ? lut_eval_scalar(spans, ns, e, v) : lut_eval_simd(spans, ns, e, v, avx2);
     }
     first_chunk = false;
+    __syncwarp();
   }
-  // the carry's last colour is the builder's trailing colour (c0 for SIMD, c1 for scalar)
-  const uint32_t tail = scalar ? carry.c1 : carry.c0;
-  const uint32_t end = span_end;
-  for (uint32_t e = threadIdx.x; e < job.lut_size; e += blockDim.x) {
+  // the last stop's colour is the builder's trailing colour (c0 for SIMD, c1 for scalar)
+  const uint32_t tail = scalar ? car_c1 : car_c0;
+  for (uint32_t e = uint32_t(lane); e < job.lut_size; e += 32) {
     uint32_t v = first_chunk ? 0u : lut[e];
     if (scalar && n == 1) v = premul_scalar(first_c);
     else {
-      if (e >= end) v = scalar ? premul_scalar(tail) : premul_simd(tail);
+      if (e >= span_end) v = scalar ? premul_scalar(tail) : premul_simd(tail);
       if (e == 0) v = scalar ? premul_scalar(first_c) : premul_simd(first_c);
     }
     lut[e] = v;
@@ -1071,7 +1045,7 @@ int launch_total(const uint32_t* counts, const uint32_t* offsets, uint32_t n, ui
 
 int launch_lut(const FrameView& f, cudaStream_t st) {
   if (!f.num_lut_jobs) return 0;
-  lut_kernel<<<f.num_lut_jobs, 256, 0, st>>>(f.lut_jobs, f.stops, f.luts);
+  lut_kernel<<<cdiv(f.num_lut_jobs, kLutWarps), 32 * kLutWarps, 0, st>>>(f.lut_jobs, f.stops, f.luts, f.num_lut_jobs);
   return 1;
 }
 

@@ -148,6 +148,9 @@ BLGpuResult Runtime::init(const BLGpuRuntimeCreateInfo* info) {
     own_stream = true;
   }
   for (auto& e : ev) BLGPU_CHECK(cudaEventCreate(&e));
+  BLGPU_CHECK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+  BLGPU_CHECK(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+  BLGPU_CHECK(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
   BLGPU_CHECK(cudaMallocHost(reinterpret_cast<void**>(&host_totals), 128));
   return BLGPU_SUCCESS;
 }
@@ -158,6 +161,10 @@ void Runtime::destroy() {
   if (graph) cudaGraphExecDestroy(graph);
   graph = nullptr;
   for (auto& e : ev) if (e) cudaEventDestroy(e);
+  if (side) { cudaStreamSynchronize(side); cudaStreamDestroy(side); }
+  if (fork_ev) cudaEventDestroy(fork_ev);
+  if (join_ev) cudaEventDestroy(join_ev);
+  side = nullptr; fork_ev = join_ev = nullptr;
   in_buf.release();
   dyn_buf.release();
   seg_buf.release();
@@ -360,7 +367,12 @@ int Runtime::enqueue_count_half(cudaStream_t st) {
   int k = 0;
   cudaMemsetAsync(f.work_counter, 0, sizeof(uint32_t) * kCounterWords, st);
   cudaMemsetAsync(f.row_counts, 0, sizeof(uint32_t) * (f.num_rows + 1), st);
-  k += launch_lut(f, st);
+  if (f.num_lut_jobs) {
+    cudaEventRecord(fork_ev, st);
+    cudaStreamWaitEvent(side, fork_ev, 0);
+    k += launch_lut(f, side);
+    cudaEventRecord(join_ev, side);
+  }
   k += launch_edges(f, cfg, st);
   k += launch_cmd_tiles(f, cmdrow_per_cmd, st);
   k += exclusive_scan(cmdrow_per_cmd, f.cmdrow_base, f.num_cmds, scan_tmp, st);
@@ -387,6 +399,7 @@ int Runtime::enqueue_render_half(cudaStream_t st, bool timed) {
   if (timed) cudaEventRecord(ev[1], st);
   k += launch_coverage(f, cfg, f.cmdrow_offsets + f.num_cmdrows + 1, st);
   if (timed) cudaEventRecord(ev[4], st);
+  if (f.num_lut_jobs) cudaStreamWaitEvent(st, join_ev, 0);     // the composite reads the LUTs
   k += launch_fine(f, cfg, st);
   if (timed) cudaEventRecord(ev[2], st);
   return k;
@@ -630,6 +643,7 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     stats.tiles = fr.tiles;
     stats.kernel_launches = uint64_t(launches);
   } while (false);
+  cudaStreamSynchronize(side);                 // a LUT build forked before an early exit
   restore();
   return r;
 }

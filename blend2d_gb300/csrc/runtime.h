@@ -150,6 +150,10 @@ struct Runtime {
   uint32_t* host_totals = nullptr;   // pinned: [0..8) frame totals, [8..12) pixel ops
 
   cudaEvent_t ev[5] = {};
+  // Gradient LUTs are built on a side stream, forked after the upload and joined before the
+  // composite pass, so they overlap the FP64-bound edge building.
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   cudaGraphExec_t graph = nullptr;
   bool graph_valid = false;
 

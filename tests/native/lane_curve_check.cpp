@@ -16,6 +16,12 @@
 using std::max;
 using std::min;
 static inline long long __double_as_longlong(double x) { long long v; memcpy(&v, &x, 8); return v; }
+static inline int __double2hiint(double x) { return int(uint64_t(__double_as_longlong(x)) >> 32); }
+static inline int __double2loint(double x) { return int(uint32_t(uint64_t(__double_as_longlong(x)))); }
+static inline double __hiloint2double(int hi, int lo) {
+  const uint64_t b = (uint64_t(uint32_t(hi)) << 32) | uint32_t(lo);
+  double v; memcpy(&v, &b, 8); return v;
+}
 static inline uint32_t atomicAdd(uint32_t* p, uint32_t v) { uint32_t o = *p; *p += v; return o; }
 #include "edge_build.cuh"
 
@@ -79,6 +85,27 @@ int main(int argc, char** argv) {
   const int n = argc > 2 ? atoi(argv[2]) : 100000;
   std::uniform_real_distribution<double> u(0.0, 1.0);
   long fails = 0;
+  // half_exp against the multiply, wherever it claims to be exact
+  {
+    const double specials[] = {0.0, -0.0, 1.0, -1.0, 5e-324, 2.2250738585072014e-308, 4.4501477170144028e-308,
+                               1.7976931348623157e308, INFINITY, -INFINITY, NAN, 3.0, 0.75, 65536.0 * 256.0};
+    long bad = 0, fast = 0;
+    auto one = [&](double v) {
+      bool ok = true;
+      const double h = half_exp(v, ok);
+      const double m = v * 0.5;
+      if (ok) { fast++; if (memcmp(&h, &m, 8) != 0) bad++; }
+    };
+    for (double v : specials) one(v);
+    for (int i = 0; i < 2000000; i++) {
+      const uint64_t b = rng();
+      double v; memcpy(&v, &b, 8);
+      one(v);
+      one(u(rng) * 1e7 - 5e6);
+    }
+    printf("half_exp: %ld fast of %d, %ld differ from the multiply\n", fast, 4000000 + 14, bad);
+    if (bad) return 1;
+  }
   for (int it = 0; it < n; it++) {
     const double w = 16 + std::floor(u(rng) * 200), h = 16 + std::floor(u(rng) * 200);
     // mostly around the canvas; some points on its borders, on the pixel grid, or far outside

@@ -272,3 +272,30 @@ def test_autotune_keeps_pixels_and_every_config_renders_the_same():
             assert not _diff(got, want), cfg
         with pytest.raises(bg.BLGpuError):
             rt.set_launch_config(bg.LaunchConfig(raster_block=96, edge_block=128))
+
+
+@pytest.mark.parametrize("variant", ["default", "avx2", "scalar"])
+def test_gradients_with_many_stops(runtimes, variant):
+    """Stop counts around the 32-stop chunks of the LUT builder, with repeated offsets and a first
+    stop at 0 (the SIMD builders skip it), each gradient filling a band of the canvas."""
+    rng = np.random.Generator(np.random.PCG64(77))
+    w, band = 300, 6
+    counts = [1, 2, 31, 32, 33, 34, 63, 64, 65, 100, 7]
+    sw = scenes.StreamWriter(w, band * len(counts))
+    sw.solid(0xFF202020)
+    sw.fill_all()
+    for i, n in enumerate(counts):
+        offs = np.sort(rng.uniform(0.0, 1.0, n))
+        if n > 3:
+            offs[0] = 0.0
+            offs[n // 2] = offs[n // 2 - 1]                 # repeated offset
+        cols = rng.integers(0, 2**32, n, dtype=np.uint64)
+        if i % 2:
+            cols |= np.uint64(0xFF000000)                   # opaque stops (the builders' opaque path)
+        stops = [(float(o), int(c)) for o, c in zip(offs, cols)]
+        sw.gradient(scenes.LINEAR, [3.0 + i, 0.0, w - 7.0, 1.0], i % 3, stops)
+        sw.fill_rect_i(0, band * i, w, band)
+    stream = sw.to_bytes()
+    got = bg.render_stream(runtimes(variant), stream)
+    want = oracle_lib.render(stream, variant)
+    assert not _diff(got, want), _diff(got, want)
