@@ -553,13 +553,56 @@ __device__ __forceinline__ double half_exp(double v, bool& ok) {
 }
 __device__ __forceinline__ Pt mid_exp(Pt a, Pt b, bool& ok) { return Pt{half_exp(a.x + b.x, ok), half_exp(a.y + b.y, ok)}; }
 
-// Monotonic curve with an explicit subdivision stack (FlattenMonoQuad / FlattenMonoCubic).
+// Subdivision stack storage. An entry is the right half of a split still to be flattened, without
+// its first point: that is the split point, which is also the last point of everything flattened
+// between the push and the pop (the left half's subtree ends there), so the pop takes it from the
+// current curve. 32 entries, as the reference's stack.
+constexpr int kStackLevels = 32;
+
 template<int DEG>
+struct LocalStack {
+  Pt e[kStackLevels][DEG];
+  // push(lvl, v): entry `lvl` (the stack held lvl entries); pop(lvl, v): takes entry `lvl` (the
+  // stack holds lvl entries afterwards).
+  __device__ __forceinline__ void push(int lvl, const Pt* v) {
+#pragma unroll
+    for (int k = 0; k < DEG; k++) e[lvl][k] = v[k];
+  }
+  __device__ __forceinline__ void pop(int lvl, Pt* v) {
+#pragma unroll
+    for (int k = 0; k < DEG; k++) v[k] = e[lvl][k];
+  }
+};
+
+// The same with the top entry held in registers: a pop returns it at once and reloads the entry
+// under it, whose load then overlaps the flattening of the popped part instead of stalling it.
+template<int DEG>
+struct CachedStack {
+  Pt top[DEG];
+  Pt e[kStackLevels][DEG];
+  __device__ __forceinline__ void push(int lvl, const Pt* v) {
+#pragma unroll
+    for (int k = 0; k < DEG; k++) {
+      if (lvl > 0) e[lvl - 1][k] = top[k];
+      top[k] = v[k];
+    }
+  }
+  __device__ __forceinline__ void pop(int lvl, Pt* v) {
+#pragma unroll
+    for (int k = 0; k < DEG; k++) {
+      v[k] = top[k];
+      if (lvl > 0) top[k] = e[lvl - 1][k];
+    }
+  }
+};
+
+// Monotonic curve with an explicit subdivision stack (FlattenMonoQuad / FlattenMonoCubic).
+template<int DEG, class S = LocalStack<DEG>>
 struct Mono {
   double tol_sq;
   Pt p[DEG + 1];
-  Pt stack[32 * (DEG + 1)];
-  int sp;
+  S stack;
+  int sp;                      // entries on the stack
 
   __device__ __forceinline__ void begin(const Pt* src, uint32_t sign) {
     sp = 0;
@@ -569,17 +612,17 @@ struct Mono {
   __device__ __forceinline__ Pt first() const { return p[0]; }
   __device__ __forceinline__ Pt last() const { return p[DEG]; }
   __device__ __forceinline__ bool can_pop() const { return sp != 0; }
-  __device__ __forceinline__ bool can_push() const { return sp != 32 * (DEG + 1); }
+  __device__ __forceinline__ bool can_push() const { return sp != kStackLevels; }
   __device__ __forceinline__ bool ltr() const { return p[0].x < p[DEG].x; }
-  __device__ void bound_ltr() {
+  __device__ __forceinline__ void bound_ltr() {
 #pragma unroll
     for (int i = 1; i < DEG; i++) { p[i].x = dclamp(p[i].x, p[0].x, p[DEG].x); p[i].y = dclamp(p[i].y, p[0].y, p[DEG].y); }
   }
-  __device__ void bound_rtl() {
+  __device__ __forceinline__ void bound_rtl() {
 #pragma unroll
     for (int i = 1; i < DEG; i++) { p[i].x = dclamp(p[i].x, p[DEG].x, p[0].x); p[i].y = dclamp(p[i].y, p[0].y, p[DEG].y); }
   }
-  __device__ bool is_flat(Step& s) const {
+  __device__ __forceinline__ bool is_flat(Step& s) const {
     if (DEG == 2) {
       Pt v1{p[1].x - p[0].x, p[1].y - p[0].y}, v2{p[2].x - p[0].x, p[2].y - p[0].y};
       double d = cross(v2, v1);
@@ -598,7 +641,7 @@ struct Mono {
     }
     return s.value <= s.limit;
   }
-  __device__ void split(Step& s) const {
+  __device__ __forceinline__ void split(Step& s) const {
     bool ok = true;
     if (DEG == 2) {
       s.p01 = mid_exp(p[0], p[1], ok); s.p12 = mid_exp(p[1], p[2], ok); s.p012 = mid_exp(s.p01, s.p12, ok);
@@ -614,34 +657,36 @@ struct Mono {
     }
   }
   __device__ __forceinline__ Pt step_mid(const Step& s) const { return DEG == 2 ? s.p012 : s.p0123; }
-  __device__ void push(const Step& s) {
+  __device__ __forceinline__ void push(const Step& s) {
+    Pt v[DEG];
     if (DEG == 2) {
-      stack[sp] = s.p012; stack[sp + 1] = s.p12; stack[sp + 2] = p[2];
-      sp += 3;
+      v[0] = s.p12; v[DEG - 1] = p[2];
+      stack.push(sp, v);
       p[1] = s.p01; p[2] = s.p012;
     }
     else {
-      stack[sp] = s.p0123; stack[sp + 1] = s.p123; stack[sp + 2] = s.p23; stack[sp + 3] = p[DEG];
-      sp += 4;
+      v[0] = s.p123; v[1] = s.p23; v[DEG - 1] = p[DEG];
+      stack.push(sp, v);
       p[1] = s.p01; p[2] = s.p012; p[DEG] = s.p0123;
     }
+    sp++;
   }
-  __device__ void discard_and_advance(const Step& s) {
+  __device__ __forceinline__ void discard_and_advance(const Step& s) {
     if (DEG == 2) { p[0] = s.p012; p[1] = s.p12; }
     else { p[0] = s.p0123; p[1] = s.p123; p[2] = s.p23; }
   }
-  __device__ void pop() {
-    sp -= DEG + 1;
-#pragma unroll
-    for (int i = 0; i <= DEG; i++) p[i] = stack[sp + i];
+  __device__ __forceinline__ void pop() {
+    sp--;
+    p[0] = p[DEG];
+    stack.pop(sp, p + 1);
   }
 };
 
 __device__ __forceinline__ double dx_div_dy(Pt a, Pt b) { return (b.x - a.x) / (b.y - a.y); }
 __device__ __forceinline__ double dy_div_dx(Pt a, Pt b) { return (b.y - a.y) / (b.x - a.x); }
 
-template<int DEG>
-__device__ void flatten_safe(Builder& eb, Mono<DEG>& mc, const Pt* src, uint32_t sign) {
+template<int DEG, class M>
+__device__ void flatten_safe(Builder& eb, M& mc, const Pt* src, uint32_t sign) {
   mc.begin(src, sign);
   if (mc.ltr()) mc.bound_ltr(); else mc.bound_rtl();
   eb.desc_open(trunc_i(mc.first().x), trunc_i(mc.first().y), sign);
@@ -656,8 +701,8 @@ __device__ void flatten_safe(Builder& eb, Mono<DEG>& mc, const Pt* src, uint32_t
   }
 }
 
-template<int DEG>
-__device__ void flatten_unsafe(Builder& eb, Mono<DEG>& mc, const Pt* src, uint32_t sign) {
+template<int DEG, class M>
+__device__ void flatten_unsafe(Builder& eb, M& mc, const Pt* src, uint32_t sign) {
   mc.begin(src, sign);
   double y_start = mc.first().y;
   double y_end = dmin(mc.last().y, eb.cy1);
@@ -979,9 +1024,9 @@ enum : int {
   kLsRIn           // right-to-left, inside (RTL_AddLine)
 };
 
-template<int DEG>
+template<int DEG, class S = LocalStack<DEG>>
 struct LaneCurve {
-  Mono<DEG> mc;
+  Mono<DEG, S> mc;
   Pt spline[DEG == 3 ? 25 : 7];
   int nout, piece, state;
   uint32_t any, sign, out;
@@ -989,7 +1034,7 @@ struct LaneCurve {
 
   // curve_to for a source holding exactly this one curve: p0 (with its clip flags) and
   // spline[1..DEG] set by the caller. Returns false when the curve has nothing to flatten.
-  __device__ bool begin_curve(Builder& eb, Pt p0, uint32_t p0_flags) {
+  __device__ __forceinline__ bool begin_curve(Builder& eb, Pt p0, uint32_t p0_flags) {
     mc.tol_sq = eb.tol_sq;
     uint32_t common = p0_flags, fl_any = p0_flags;
 #pragma unroll
@@ -1011,7 +1056,7 @@ struct LaneCurve {
 
   // Starts the next piece with work (pieces that finish at their start are skipped). Returns
   // false when the curve is done.
-  __device__ bool next_piece(Builder& eb, bool advance) {
+  __device__ __forceinline__ bool next_piece(Builder& eb, bool advance) {
     if (advance) piece += DEG;
     for (; piece < nout; piece += DEG) {
       start_piece(eb);
@@ -1020,7 +1065,7 @@ struct LaneCurve {
     return false;
   }
 
-  __device__ void finish(Builder& eb) {
+  __device__ __forceinline__ void finish(Builder& eb) {
     if (out && y_start < y_end) {
       if (out & CF_X0) eb.acc_left_s(y_start, y_end, sign);
       else eb.acc_right_s(y_start, y_end, sign);
@@ -1034,7 +1079,7 @@ struct LaneCurve {
     finish(eb);
   }
 
-  __device__ void start_piece(Builder& eb) {
+  __device__ __forceinline__ void start_piece(Builder& eb) {
     const Pt* sp = spline + piece;
     sign = sp[0].y > sp[DEG].y;
     mc.begin(sp, sign);
@@ -1083,7 +1128,7 @@ struct LaneCurve {
   }
 
   // One pass of the current loop's body.
-  __device__ void step(Builder& eb) {
+  __device__ __forceinline__ void step(Builder& eb) {
     switch (state) {
       case kLsLTop: out = mc.first().x >= eb.cx1; if (out) { exit_loop(eb, true); return; } break;
       case kLsLLeft: out = mc.first().y >= eb.cy1; if (out) { exit_loop(eb, false); return; } break;
@@ -1104,7 +1149,7 @@ struct LaneCurve {
     leaf(eb);
   }
 
-  __device__ void leaf(Builder& eb) {
+  __device__ __forceinline__ void leaf(Builder& eb) {
     const Pt a = mc.first(), b = mc.last();
     switch (state) {
       case kLsSafe:
@@ -1165,12 +1210,12 @@ struct LaneCurve {
     }
   }
 
-  __device__ void l_left_pop(Builder& eb) {           // LTR_BeforeX0_Pop
+  __device__ __forceinline__ void l_left_pop(Builder& eb) {           // LTR_BeforeX0_Pop
     state = kLsLLeft;
     if (!mc.can_pop()) { exit_loop(eb, false); return; }
     mc.pop();
   }
-  __device__ void l_left_clip(Builder& eb) {          // LTR_BeforeX0_Clip
+  __device__ __forceinline__ void l_left_clip(Builder& eb) {          // LTR_BeforeX0_Clip
     state = kLsLLeft;
     const Pt a = mc.first(), b = mc.last();
     const double yc = a.y + (eb.cx0 - a.x) * dy_div_dx(a, b);
@@ -1180,7 +1225,7 @@ struct LaneCurve {
     eb.desc_open(trunc_i(eb.cx0), trunc_i(yc), sign);
     l_add_line(eb);
   }
-  __device__ void l_add_line(Builder& eb) {           // LTR_AddLine
+  __device__ __forceinline__ void l_add_line(Builder& eb) {           // LTR_AddLine
     state = kLsLIn;
     const Pt a = mc.first(), b = mc.last();
     out = b.x > eb.cx1;
@@ -1205,12 +1250,12 @@ struct LaneCurve {
     if (!mc.can_pop()) { exit_loop(eb, true); return; }
     mc.pop();
   }
-  __device__ void r_right_pop(Builder& eb) {          // RTL_AfterX1_Pop
+  __device__ __forceinline__ void r_right_pop(Builder& eb) {          // RTL_AfterX1_Pop
     state = kLsRRight;
     if (!mc.can_pop()) { exit_loop(eb, true); return; }
     mc.pop();
   }
-  __device__ void r_right_clip(Builder& eb) {         // RTL_AfterX1_Clip
+  __device__ __forceinline__ void r_right_clip(Builder& eb) {         // RTL_AfterX1_Clip
     state = kLsRRight;
     const Pt a = mc.first(), b = mc.last();
     const double yc = a.y + (eb.cx1 - a.x) * dy_div_dx(a, b);
@@ -1220,7 +1265,7 @@ struct LaneCurve {
     eb.desc_open(trunc_i(eb.cx1), trunc_i(yc), sign);
     r_add_line(eb);
   }
-  __device__ void r_add_line(Builder& eb) {           // RTL_AddLine
+  __device__ __forceinline__ void r_add_line(Builder& eb) {           // RTL_AddLine
     state = kLsRIn;
     const Pt a = mc.first(), b = mc.last();
     out = b.x < eb.cx0;

@@ -331,14 +331,19 @@ __device__ __forceinline__ void finish_curve(FrameView& f, eb::Builder& b, uint3
   }
 }
 
+// The lanes' subdivision stacks live in local memory with the top entry in registers
+// (eb::CachedStack): the kernel is bound by the FP64 pipe and the latency of its stack, and needs
+// every resident warp, so the stacks stay out of shared memory.
+constexpr int kCurveThreads = 128;
+
 template<int DEG>
-__global__ void __launch_bounds__(128) edge_curves_kernel(FrameView f) {
+__global__ void __launch_bounds__(kCurveThreads) edge_curves_kernel(FrameView f) {
   const int lane = threadIdx.x & 31;
   const uint32_t n_cubic = min(f.work_counter[2], f.item_capacity);
   const uint32_t n_items = DEG == 3 ? n_cubic : min(f.work_counter[21], f.item_capacity - n_cubic);
   uint32_t* queue = f.work_counter + (DEG == 3 ? 3 : 22);
   eb::Builder b;
-  eb::LaneCurve<DEG> lc;
+  eb::LaneCurve<DEG, eb::CachedStack<DEG>> lc;
   bool busy = false, exhausted = false;
   uint32_t cur = 0, rows = 0;
 
@@ -1056,17 +1061,17 @@ int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, edge_curves_kernel<3>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, edge_curves_kernel<3>, kCurveThreads, 0);
     if (max_per_sm < 1) max_per_sm = 1;
   }
   const int per_sm = cfg.cubic_blocks_per_sm > 0 && cfg.cubic_blocks_per_sm < max_per_sm ? cfg.cubic_blocks_per_sm : max_per_sm;
   const uint32_t eb = cfg.edge_block == 64 || cfg.edge_block == 256 ? uint32_t(cfg.edge_block) : 128u;
   classify_kernel<<<cdiv(f.num_cmds, 128), 128, 0, st>>>(f);
   edge_items_kernel<<<cdiv(f.item_capacity ? f.item_capacity : 1, eb), eb, 0, st>>>(f);
-  uint32_t grid = cdiv(f.item_capacity ? f.item_capacity : 1, 128);
+  uint32_t grid = cdiv(f.item_capacity ? f.item_capacity : 1, kCurveThreads);
   uint32_t cubic_grid = uint32_t(sms * per_sm);
-  edge_curves_kernel<3><<<grid < cubic_grid ? grid : cubic_grid, 128, 0, st>>>(f);
-  edge_curves_kernel<2><<<sms, 128, 0, st>>>(f);
+  edge_curves_kernel<3><<<grid < cubic_grid ? grid : cubic_grid, kCurveThreads, 0, st>>>(f);
+  edge_curves_kernel<2><<<sms, kCurveThreads, 0, st>>>(f);
   return 4;
 }
 

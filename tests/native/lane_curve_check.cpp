@@ -1,6 +1,6 @@
 // Host build of the device edge builder (edge_build.cuh) checking that the lane-stepped curve
 // flattener (eb::LaneCurve, one subdivision step per call) emits exactly the segments, in the same
-// order, as the loop flattener (eb::curve_to) for random cubic, quadratic and conic curves around
+// order, as the loop flattener (eb::curve_to, with the plain local stack) for random cubic, quadratic and conic curves around
 // and across the clip box. Usage: lane_curve_check <seed> <curves>; exit status 0 when all match.
 #include <algorithm>
 #include <cmath>
@@ -42,7 +42,8 @@ static void init_builder(Builder& b, double w, double h, Out& o) {
   b.sink.init(o.segs.data(), o.meta.data(), &o.counter, 1u << 14, 7u);
 }
 
-template<int DEG>
+// S: the lane flattener's stack (the kernels use CachedStack, the top entry in registers).
+template<int DEG, class S>
 static bool same_segments(const double* xy, const uint8_t* cmd, int npts, bool conic, double w, double h) {
   Src src;
   src.xy = xy; src.cmd = cmd; src.affine = false;
@@ -59,7 +60,7 @@ static bool same_segments(const double* xy, const uint8_t* cmd, int npts, bool c
 
   Builder b2;
   init_builder(b2, w, h, o2);
-  LaneCurve<DEG> lc;
+  LaneCurve<DEG, S> lc;
   const Pt q0 = src.tf(0);
   lc.spline[1] = src.tf(1);
   if (DEG == 3) { lc.spline[2] = src.tf(2); lc.spline[3] = src.tf(3); }
@@ -107,6 +108,7 @@ int main(int argc, char** argv) {
     if (bad) return 1;
   }
   for (int it = 0; it < n; it++) {
+    const bool cached = (it & 4) != 0;           // half the curves with each stack
     const double w = 16 + std::floor(u(rng) * 200), h = 16 + std::floor(u(rng) * 200);
     // mostly around the canvas; some points on its borders, on the pixel grid, or far outside
     auto coord = [&](double lim) {
@@ -125,16 +127,16 @@ int main(int argc, char** argv) {
     bool ok;
     if (it % 3 == 0) {
       const uint8_t c[4] = {0, 4, 4, 4};
-      ok = same_segments<3>(xy, c, 4, false, w, h);
+      ok = cached ? same_segments<3, CachedStack<3>>(xy, c, 4, false, w, h) : same_segments<3, LocalStack<3>>(xy, c, 4, false, w, h);
     }
     else if (it % 3 == 1) {
       const uint8_t c[3] = {0, 2, 2};
-      ok = same_segments<2>(xy, c, 3, false, w, h);
+      ok = cached ? same_segments<2, CachedStack<2>>(xy, c, 3, false, w, h) : same_segments<2, LocalStack<2>>(xy, c, 3, false, w, h);
     }
     else {
       const uint8_t c[4] = {0, 3, 3, 3};
       const double cx[8] = {xy[0], xy[1], xy[2], xy[3], 1.0, 0.0, xy[4], xy[5]};
-      ok = same_segments<2>(cx, c, 4, true, w, h);
+      ok = cached ? same_segments<2, CachedStack<2>>(cx, c, 4, true, w, h) : same_segments<2, LocalStack<2>>(cx, c, 4, true, w, h);
     }
     if (!ok && ++fails <= 5) printf("mismatch: curve %d (kind %d)\n", it, it % 3);
   }
