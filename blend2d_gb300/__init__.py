@@ -29,6 +29,7 @@ ERROR_DEVICE = 0x00011000
 FORMAT_PRGB32 = 1
 IMAGE_DEVICE_MEMORY = 1
 FLUSH_SYNC = 0x80000000
+FLUSH_ASYNC = 0x1            # start rendering what is recorded and return (see include/blgpu.h)
 LUT_SSE2, LUT_AVX2, LUT_SCALAR = 0, 1, 2
 
 COMP_OP_SRC_OVER, COMP_OP_SRC_COPY = 0, 1
@@ -265,6 +266,7 @@ class Context:
         _check(self._lib.blgpu_context_create(ctypes.byref(h), runtime.handle), "blgpu_context_create")
         self.handle = h
         self._keep = []
+        self._inflight = []
         if target is not None:
             self.begin(target)
 
@@ -275,14 +277,22 @@ class Context:
         img, keep = make_image(target)
         self._img = img
         self._keep = [keep]
+        self._inflight = []
         self._call("blgpu_context_begin", ctypes.byref(img))
 
     def end(self):
         self._call("blgpu_context_end")
         self._keep = []
+        self._inflight = []
 
     def flush(self, flags: int = FLUSH_SYNC):
+        """FLUSH_SYNC renders and waits; FLUSH_ASYNC starts rendering and returns (the target
+        holds the result after the next FLUSH_SYNC or end())."""
         self._call("blgpu_context_flush", flags)
+        if flags & FLUSH_SYNC:
+            self._inflight = []
+        elif flags & FLUSH_ASYNC:
+            self._inflight.append(self._keep[1:])     # pattern images of frames still rendering
         self._keep = self._keep[:1]
 
     def close(self):

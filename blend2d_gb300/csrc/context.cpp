@@ -13,7 +13,9 @@
 #include <string.h>
 
 #include <deque>
+#include <condition_variable>
 #include <mutex>
+#include <thread>
 #include <new>
 #include <vector>
 
@@ -24,10 +26,72 @@
 
 using namespace blgpu;
 
+// A frame handed to the runtime's submission thread by an asynchronous flush, with the pattern
+// pixels its stream records brought along.
+struct AsyncSlot {
+  Frame frame;
+  std::deque<std::vector<uint32_t>> images;
+  bool in_flight = false;                    // guarded by BLGpuRuntime::queue_lock
+  BLGpuResult result = BLGPU_SUCCESS;
+};
+
 struct BLGpuRuntime {
   Runtime rt;
   Frame batch_frame;               // reused by blgpu_render_batch (its page-locked arrays persist)
   std::mutex batch_lock;
+  // One pipeline run at a time: the submission thread and every synchronous entry point that
+  // touches `rt` hold it.
+  std::mutex exec;
+  // Asynchronous flushes: frames run in submission order by one thread, so a frame's canvas
+  // upload always sees what the frames before it wrote back.
+  std::mutex queue_lock;
+  std::condition_variable queue_cv, done_cv;
+  std::deque<AsyncSlot*> queue;
+  std::thread worker;
+  bool stopping = false;
+
+  void submit(AsyncSlot* s) {
+    std::lock_guard<std::mutex> g(queue_lock);
+    s->in_flight = true;
+    queue.push_back(s);
+    if (!worker.joinable()) worker = std::thread([this] { work(); });
+    queue_cv.notify_one();
+  }
+  // Waits until `s` is no longer in flight; returns (and clears) its result.
+  BLGpuResult wait(AsyncSlot* s) {
+    std::unique_lock<std::mutex> g(queue_lock);
+    done_cv.wait(g, [&] { return !s->in_flight; });
+    BLGpuResult r = s->result;
+    s->result = BLGPU_SUCCESS;
+    return r;
+  }
+  void work() {
+    std::unique_lock<std::mutex> g(queue_lock);
+    for (;;) {
+      queue_cv.wait(g, [&] { return stopping || !queue.empty(); });
+      if (queue.empty()) return;             // stopping, nothing left
+      AsyncSlot* s = queue.front();
+      queue.pop_front();
+      g.unlock();
+      BLGpuResult r;
+      {
+        std::lock_guard<std::mutex> e(exec);
+        r = rt.run(s->frame);
+      }
+      g.lock();
+      s->result = r;
+      s->in_flight = false;
+      done_cv.notify_all();
+    }
+  }
+  void stop() {
+    {
+      std::lock_guard<std::mutex> g(queue_lock);
+      stopping = true;
+      queue_cv.notify_all();
+    }
+    if (worker.joinable()) worker.join();
+  }
 };
 
 namespace {
@@ -72,8 +136,11 @@ struct State {
 
 struct BLGpuContext {
   BLGpuRuntime* rt = nullptr;
-  Frame own_frame;
-  Frame* frame = &own_frame;
+  // Two recording buffers: while one frame renders asynchronously the next one is recorded.
+  AsyncSlot slots[2];
+  int cur = 0;
+  Frame* frame = &slots[0].frame;
+  std::deque<std::vector<uint32_t>>* stream_images = &slots[0].images;   // pattern pixels copied out of submitted streams
   bool bound = false;
   BLGpuImage target{};
   uint32_t canvas = 0;
@@ -82,7 +149,6 @@ struct BLGpuContext {
   std::vector<State> stack;
   uint64_t clear_style_gen = 0;
   uint32_t clear_style_index = 0;
-  std::deque<std::vector<uint32_t>> stream_images;   // pattern pixels copied out of submitted streams
 
   void reset_state() {
     s = State{};
@@ -286,25 +352,58 @@ struct BLGpuContext {
     h = image->height;
     bound = true;
     frame->clear();
-    stream_images.clear();
+    stream_images->clear();
     canvas = frame->add_canvas(target, true);
     reset_state();
     return BLGPU_SUCCESS;
   }
 
-  // Runs the recorded frame (canvas content uploaded unless the first command overwrites it).
+  // Waits for the frames this context submitted asynchronously; returns the first error.
+  BLGpuResult wait_async() {
+    BLGpuResult r0 = rt->wait(&slots[0]), r1 = rt->wait(&slots[1]);
+    return r0 ? r0 : r1;
+  }
+
+  // Runs the recorded frame (canvas content uploaded unless the first command overwrites it)
+  // after the ones submitted before it; returns the first error of any of them.
   BLGpuResult flush_frame() {
     if (!bound) return BLGPU_ERROR_INVALID_STATE;
-    BLGpuResult r = BLGPU_SUCCESS;
+    BLGpuResult r = frame == &slots[cur].frame ? wait_async() : BLGPU_SUCCESS;
     if (!frame->cmds.empty()) {
       mark_uploads(*frame);
-      r = rt->rt.run(*frame);
+      BLGpuResult rr;
+      {
+        std::lock_guard<std::mutex> e(rt->exec);
+        rr = rt->rt.run(*frame);
+      }
+      if (!r) r = rr;
     }
     frame->clear();
-    stream_images.clear();
+    stream_images->clear();
     canvas = frame->add_canvas(target, true);
     return r;
   }
+
+  // Hands the recorded frame to the runtime's submission thread and returns; recording goes on in
+  // the other buffer (after the frame that used it last has finished). An error of a frame run
+  // this way is returned by a later flush.
+  BLGpuResult flush_async() {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    if (frame != &slots[cur].frame) return flush_frame();   // an external frame (batch): run it now
+    if (frame->cmds.empty()) return BLGPU_SUCCESS;
+    mark_uploads(*frame);
+    rt->submit(&slots[cur]);
+    cur ^= 1;
+    BLGpuResult r = rt->wait(&slots[cur]);
+    frame = &slots[cur].frame;
+    stream_images = &slots[cur].images;
+    frame->clear();
+    stream_images->clear();
+    canvas = frame->add_canvas(target, true);
+    if (r) pending_error = r;
+    return BLGPU_SUCCESS;
+  }
+  BLGpuResult pending_error = BLGPU_SUCCESS;
 
   static void mark_uploads(Frame& fr) {
     for (size_t i = 0; i < fr.canvases.size(); i++) {
@@ -320,6 +419,8 @@ struct BLGpuContext {
   BLGpuResult end() {
     if (!bound) return BLGPU_ERROR_INVALID_STATE;
     BLGpuResult r = flush_frame();
+    if (!r) r = pending_error;
+    pending_error = BLGPU_SUCCESS;
     frame->clear();
     bound = false;
     return r;
@@ -544,9 +645,9 @@ BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
     off += sizeof(im);
     size_t n = size_t(im.width) * im.height;
     if (im.width > 65535 || im.height > 65535 || off + n * 4u > size) return BLGPU_ERROR_INVALID_VALUE;
-    stream_images.emplace_back(n ? n : 1);
-    memcpy(stream_images.back().data(), base + off, n * 4u);
-    images[i] = BLGpuImage{stream_images.back().data(), intptr_t(im.width) * 4, int32_t(im.width), int32_t(im.height),
+    stream_images->emplace_back(n ? n : 1);
+    memcpy(stream_images->back().data(), base + off, n * 4u);
+    images[i] = BLGpuImage{stream_images->back().data(), intptr_t(im.width) * 4, int32_t(im.width), int32_t(im.height),
                            BLGPU_FORMAT_PRGB32, 0};
     off += (n * 4u + 7u) & ~size_t(7);
   }
@@ -671,6 +772,7 @@ BLGPU_API BLGpuResult blgpu_runtime_create(BLGpuRuntime** out, const BLGpuRuntim
 
 BLGPU_API BLGpuResult blgpu_runtime_destroy(BLGpuRuntime* rt) {
   if (!rt) return BLGPU_ERROR_INVALID_VALUE;
+  rt->stop();
   rt->rt.destroy();
   delete rt;
   return BLGPU_SUCCESS;
@@ -678,6 +780,7 @@ BLGPU_API BLGpuResult blgpu_runtime_destroy(BLGpuRuntime* rt) {
 
 BLGPU_API BLGpuResult blgpu_runtime_get_stats(const BLGpuRuntime* rt, BLGpuStats* out) {
   if (!rt || !out) return BLGPU_ERROR_INVALID_VALUE;
+  std::lock_guard<std::mutex> e(const_cast<BLGpuRuntime*>(rt)->exec);
   *out = rt->rt.stats;
   out->last_cuda_error = last_cuda_error();
   return BLGPU_SUCCESS;
@@ -685,11 +788,13 @@ BLGPU_API BLGpuResult blgpu_runtime_get_stats(const BLGpuRuntime* rt, BLGpuStats
 
 BLGPU_API BLGpuResult blgpu_runtime_replay(BLGpuRuntime* rt, int use_graph) {
   if (!rt) return BLGPU_ERROR_INVALID_VALUE;
+  std::lock_guard<std::mutex> e(rt->exec);
   return rt->rt.replay(use_graph != 0);
 }
 
 BLGPU_API BLGpuResult blgpu_runtime_synchronize(BLGpuRuntime* rt) {
   if (!rt) return BLGPU_ERROR_INVALID_VALUE;
+  std::lock_guard<std::mutex> e(rt->exec);
   return rt->rt.synchronize();
 }
 
@@ -704,6 +809,7 @@ static void to_abi(const LaunchConfig& c, BLGpuLaunchConfig* out) {
 
 BLGPU_API BLGpuResult blgpu_runtime_get_launch_config(const BLGpuRuntime* rt, BLGpuLaunchConfig* out) {
   if (!rt || !out) return BLGPU_ERROR_INVALID_VALUE;
+  std::lock_guard<std::mutex> e(const_cast<BLGpuRuntime*>(rt)->exec);
   to_abi(rt->rt.cfg, out);
   return BLGPU_SUCCESS;
 }
@@ -720,6 +826,7 @@ BLGPU_API BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BL
   lc.fine_blocks_per_sm = c->fine_blocks_per_sm;
   lc.edge_block = c->edge_block;
   lc.cubic_blocks_per_sm = c->cubic_blocks_per_sm;
+  std::lock_guard<std::mutex> e(rt->exec);
   rt->rt.cfg = lc;
   rt->rt.graph_valid = false;
   return BLGPU_SUCCESS;
@@ -729,7 +836,11 @@ BLGPU_API BLGpuResult blgpu_runtime_autotune(BLGpuRuntime* rt, uint32_t trials, 
   if (!rt) return BLGPU_ERROR_INVALID_VALUE;
   LaunchConfig c;
   double ms = 0.0;
-  BLGpuResult r = rt->rt.autotune(int(trials), &c, &ms);
+  BLGpuResult r;
+  {
+    std::lock_guard<std::mutex> e(rt->exec);
+    r = rt->rt.autotune(int(trials), &c, &ms);
+  }
   if (best) to_abi(c, best);
   if (best_ms) *best_ms = ms;
   return r;
@@ -747,7 +858,7 @@ BLGPU_API BLGpuResult blgpu_context_create(BLGpuContext** out, BLGpuRuntime* rt)
 
 BLGPU_API BLGpuResult blgpu_context_destroy(BLGpuContext* ctx) {
   if (!ctx) return BLGPU_ERROR_INVALID_VALUE;
-  BLGpuResult r = ctx->bound ? ctx->end() : BLGPU_SUCCESS;
+  BLGpuResult r = ctx->bound ? ctx->end() : ctx->wait_async();
   delete ctx;
   return r;
 }
@@ -759,8 +870,14 @@ BLGPU_API BLGpuResult blgpu_context_end(BLGpuContext* ctx) { CTX_CALL(end()); }
 BLGPU_API BLGpuResult blgpu_context_flush(BLGpuContext* ctx, uint32_t flags) {
   if (!ctx) return BLGPU_ERROR_INVALID_VALUE;
   if (!ctx->bound) return BLGPU_ERROR_INVALID_STATE;
-  if (!(flags & BLGPU_FLUSH_SYNC)) return BLGPU_SUCCESS;
-  return ctx->flush_frame();
+  if (flags & BLGPU_FLUSH_SYNC) {
+    BLGpuResult r = ctx->flush_frame();
+    if (!r) r = ctx->pending_error;
+    ctx->pending_error = BLGPU_SUCCESS;
+    return r;
+  }
+  if (flags & BLGPU_FLUSH_ASYNC) return ctx->flush_async();
+  return BLGPU_SUCCESS;
 }
 BLGPU_API BLGpuResult blgpu_context_save(BLGpuContext* ctx) { CTX_CALL(save()); }
 BLGPU_API BLGpuResult blgpu_context_restore(BLGpuContext* ctx) { CTX_CALL(restore()); }
@@ -815,6 +932,7 @@ BLGPU_API BLGpuResult blgpu_render_batch(BLGpuRuntime* rt, const void* const* st
   }
   if (frame.cmds.empty()) return BLGPU_SUCCESS;
   BLGpuContext::mark_uploads(frame);
+  std::lock_guard<std::mutex> e(rt->exec);
   return rt->rt.run(frame);
 }
 
@@ -844,5 +962,6 @@ BLGPU_API BLGpuResult blgpu_render_stream_noalloc(BLGpuRuntime* rt, const void* 
   c.bound = false;
   if (r) return r;
   if (frame.cmds.empty()) return BLGPU_SUCCESS;
+  std::lock_guard<std::mutex> e(rt->exec);
   return rt->rt.run_noalloc(frame);
 }

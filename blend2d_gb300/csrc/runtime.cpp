@@ -39,11 +39,17 @@ static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1
 
 // --- Frame ------------------------------------------------------------------------------------
 
+// Generations are unique across all frames of the process: a context records into two frames in
+// turn, and a style registered in one must not look registered in the other.
+static std::atomic<uint64_t> g_frame_generation{1};
+
+uint64_t Frame::next_generation() { return g_frame_generation.fetch_add(1) + 1; }
+
 void Frame::clear() {
   cmds.clear(); styles.clear(); xforms.clear(); canvases.clear(); targets.clear();
   verts.clear(); path_cmds.clear(); lut_jobs.clear(); stops.clear(); images.clear();
   image_words = 0; lut_words = 0; tiles = 0; rows = 0;
-  generation++;
+  generation = next_generation();
 }
 
 static int band_height_for(int width) {

@@ -111,8 +111,9 @@ struct Frame {
   uint64_t image_words = 0;
   uint32_t lut_words = 0;
   uint32_t tiles = 0, rows = 0;
-  uint64_t generation = 1;  // bumped by clear(); per-frame registrations compare against it (0 = none)
+  uint64_t generation = next_generation();   // renewed by clear(); per-frame registrations compare against it
 
+  static uint64_t next_generation();
   void clear();
   // Adds a canvas (tile/row bases, band height) for `image`; returns its index.
   uint32_t add_canvas(const BLGpuImage& image, bool upload);

@@ -39,8 +39,17 @@ enum {
   BLGPU_IMAGE_DEVICE_MEMORY = 0x1u           /* pixel_data is a CUDA device pointer */
 };
 
-/* bl_context_flush flags (BLContextFlushFlags). */
-enum { BLGPU_FLUSH_SYNC = 0x80000000u };     /* BL_CONTEXT_FLUSH_SYNC */
+/* bl_context_flush flags (BLContextFlushFlags). SYNC renders everything recorded so far and waits
+   (the image holds the result when it returns). ASYNC is this backend's extension, the explicit
+   form of the reference's asynchronous context handing a full command batch to its workers
+   (rastercontext.cpp:1480-1492): the recorded frame starts rendering and the call returns at once;
+   recording continues into a second buffer, frames render in order, and the image holds the
+   result after the next SYNC flush or end(). An error of an asynchronous frame is returned there.
+   No flag (BL_CONTEXT_FLUSH_NO_FLAGS) does nothing, as in the reference. */
+enum {
+  BLGPU_FLUSH_ASYNC = 0x1u,
+  BLGPU_FLUSH_SYNC = 0x80000000u             /* BL_CONTEXT_FLUSH_SYNC */
+};
 
 /* Gradient LUT builder the backend reproduces (blend2d/pixelops/funcs.cpp:22-34). */
 enum {

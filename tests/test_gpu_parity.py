@@ -299,3 +299,50 @@ def test_gradients_with_many_stops(runtimes, variant):
     got = bg.render_stream(runtimes(variant), stream)
     want = oracle_lib.render(stream, variant)
     assert not _diff(got, want), _diff(got, want)
+
+
+def test_async_flush_pipelines_frames_with_the_same_pixels(runtimes):
+    """Two contexts alternate: each records a frame while the other's renders (FLUSH_ASYNC), with
+    mid-frame async flushes too; every image matches the synchronous render of its stream."""
+    import torch
+    rt = runtimes()
+    streams = [scenes.random_mix(seed, width=211, height=157, count=200).to_bytes() for seed in range(3100, 3106)]
+    want = [bg.render_stream(rt, s) for s in streams]
+    hosts = [torch.zeros((157, 211), dtype=torch.int32).pin_memory() for _ in range(2)]
+    ctxs = [bg.Context(rt) for _ in range(2)]
+    got = []
+    active = [None, None]
+    for i, s in enumerate(streams):
+        c = ctxs[i % 2]
+        if active[i % 2] is not None:
+            c.end()
+            got.append((active[i % 2], hosts[i % 2].numpy().view(np.uint32).copy()))
+        hosts[i % 2].zero_()
+        c.begin(hosts[i % 2])
+        c.submit_stream(s)
+        c.flush(bg.FLUSH_ASYNC)
+        c.flush(bg.FLUSH_ASYNC)                             # nothing recorded since: a no-op
+        active[i % 2] = i
+    for k in range(2):
+        ctxs[k].end()
+        got.append((active[k], hosts[k].numpy().view(np.uint32).copy()))
+    assert sorted(i for i, _ in got) == list(range(len(streams)))
+    for i, img in got:
+        assert not _diff(img, want[i]), (i, _diff(img, want[i]))
+    # a frame split by an async flush renders the same as in one piece
+    half = scenes.random_mix(3200, width=211, height=157, count=120)
+    host = torch.zeros((157, 211), dtype=torch.int32).pin_memory()
+    c = ctxs[0]
+    c.begin(host)
+    c.submit_stream(half.to_bytes())
+    c.flush(bg.FLUSH_ASYNC)
+    c.fill_rect_i(5, 7, 50, 40)
+    c.end()
+    ref = torch.zeros((157, 211), dtype=torch.int32).pin_memory()
+    c.begin(ref)
+    c.submit_stream(half.to_bytes())
+    c.fill_rect_i(5, 7, 50, 40)
+    c.end()
+    assert np.array_equal(host.numpy(), ref.numpy())
+    for c in ctxs:
+        c.close()
