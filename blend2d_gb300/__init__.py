@@ -72,7 +72,7 @@ class Pattern(ctypes.Structure):
 
 
 class LaunchConfig(ctypes.Structure):
-    _fields_ = [("raster_block", ctypes.c_int32), ("cover_blocks_per_sm", ctypes.c_int32),
+    _fields_ = [("cover_slots", ctypes.c_int32), ("cover_blocks_per_sm", ctypes.c_int32),
                 ("fine_blocks_per_sm", ctypes.c_int32), ("edge_block", ctypes.c_int32),
                 ("cubic_blocks_per_sm", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 

@@ -151,16 +151,20 @@ struct DevItem {
 #ifdef __CUDACC__
 // Tile columns whose cells a segment can touch within strip row `r` (pixel rows [4r, 4r + 3]):
 // the line's x at the strip's clipped y extent, one pixel of slack on both sides (the integer DDA
-// stays within a 24.8 unit of the exact line), plus the cell right of the last one (area).
-// `t_last` is the last such column; columns after it only see the segment's full row cover.
+// stays within a 24.8 unit of the exact line) and 16 units more for the FP32 evaluation (segments
+// are clipped to the canvas, so |dx|, |dy| < 2^24 are exact floats and the product and quotient
+// are off by a few units at most), clamped to the segment's own x extent, plus the cell right of
+// the last one (area). `t_last` is the last such column; columns after it only see the segment's
+// full row cover. A wider range only adds work items (whose cells the window clipping keeps
+// exact); FP32 keeps this off the FP64 pipe that 64-bit integer division would use.
 __device__ __forceinline__ void strip_tile_range(const DevSeg& g, int r, int& t0, int& t_last) {
   int ya = max(g.y0, (r << kStripShift) << 8);
   int yb = min(g.y1, ((r + 1) << kStripShift) << 8);
-  int64_t dy = int64_t(g.y1) - g.y0, dx = int64_t(g.x1) - g.x0;
-  int xa = g.x0 + int((dx * (ya - g.y0)) / dy);
-  int xb = g.x0 + int((dx * (yb - g.y0)) / dy);
-  int lo = max(min(xa, xb) - 256, min(g.x0, g.x1));
-  int hi = min(max(xa, xb) + 256, max(g.x0, g.x1));
+  const float slope = float(g.x1 - g.x0) / float(g.y1 - g.y0);
+  int xa = g.x0 + int(slope * float(ya - g.y0));
+  int xb = g.x0 + int(slope * float(yb - g.y0));
+  int lo = max(min(xa, xb) - (256 + 16), min(g.x0, g.x1));
+  int hi = min(max(xa, xb) + (256 + 16), max(g.x0, g.x1));
   t0 = (lo >> 8) >> kTileShift;
   t_last = ((hi >> 8) + 1) >> kTileShift;
 }
@@ -199,10 +203,9 @@ struct FrameView {
   uint32_t* slot_cmd;          // [num_cmdrows] command of each slot with segments
   uint32_t* slot_mask;         // [num_cmdrows + 1] 1 + index of the slot's masks, 0 = no segments
   uint32_t* mask_slot;         // [non-empty slots] slot of each compact mask index
-  uint32_t* cells;             // [non-empty slots][kStripRows * kTileW] cell sums of the coverage pass
-  uint4* entries;              // raster work: {segment, slot, mask index, x0 | row0 << 16}, by DDA kind
-  uint32_t* kind_info;         // [16]: entries per kind [0..5), cursors [5..10), offsets [10..16)
-  uint32_t mask_capacity;      // slots the cells/masks arrays hold
+  uint32_t* slot_first;        // [num_cmdrows + 1] first work item of each slot (exclusive scan of the counts)
+  uint2* entries;              // coverage work items {segment, mask index}, grouped by slot in slot order
+  uint32_t mask_capacity;      // slots the masks array holds
   uint8_t* masks;              // [non-empty slots][kStripRows * kTileW]: analytic masks from the coverage pass
   uint32_t* backdrop;          // [num_cmdrows][kStripRows]: coverage carried into the slot's tile
                                //   from segments entirely left of it (cover << 9 per row)

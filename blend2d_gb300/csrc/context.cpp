@@ -800,7 +800,7 @@ BLGPU_API BLGpuResult blgpu_runtime_synchronize(BLGpuRuntime* rt) {
 
 static void to_abi(const LaunchConfig& c, BLGpuLaunchConfig* out) {
   *out = BLGpuLaunchConfig{};
-  out->raster_block = c.raster_block;
+  out->cover_slots = c.cover_slots;
   out->cover_blocks_per_sm = c.cover_blocks_per_sm;
   out->fine_blocks_per_sm = c.fine_blocks_per_sm;
   out->edge_block = c.edge_block;
@@ -816,12 +816,12 @@ BLGPU_API BLGpuResult blgpu_runtime_get_launch_config(const BLGpuRuntime* rt, BL
 
 BLGPU_API BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BLGpuLaunchConfig* c) {
   if (!rt || !c) return BLGPU_ERROR_INVALID_VALUE;
-  if ((c->raster_block != 128 && c->raster_block != 256) ||
+  if ((c->cover_slots != 16 && c->cover_slots != 32 && c->cover_slots != 64) ||
       (c->edge_block != 64 && c->edge_block != 128 && c->edge_block != 256) ||
       c->cover_blocks_per_sm < 0 || c->fine_blocks_per_sm < 0 || c->cubic_blocks_per_sm < 0)
     return BLGPU_ERROR_INVALID_VALUE;
   LaunchConfig lc;
-  lc.raster_block = c->raster_block;
+  lc.cover_slots = c->cover_slots;
   lc.cover_blocks_per_sm = c->cover_blocks_per_sm;
   lc.fine_blocks_per_sm = c->fine_blocks_per_sm;
   lc.edge_block = c->edge_block;

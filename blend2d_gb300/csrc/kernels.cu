@@ -563,60 +563,44 @@ __global__ void cmd_tiles_kernel(FrameView f, uint32_t* cmdrow_counts_per_cmd, u
   for (uint32_t r = ty0; r <= ty1; r++) atomicAdd(&row_counts[cv.row_base + r], 1u);
 }
 
-// DDA path a segment takes through the reference rasterizer (prepare_ref's classification): the
-// coverage pass processes segments grouped by it so that a warp's lanes run the same code.
-__device__ __forceinline__ uint32_t dda_kind(const DevSeg& g) {
-  const int dx = g.x1 - g.x0, adx = dx < 0 ? -dx : dx, dy = g.y1 - g.y0;
-  if ((g.x0 >> 8) == (g.x1 >> 8) && ((g.y0 >> 8) == ((g.y1 - 1) >> 8) || adx == 0)) return 0u;
-  return dy >= adx ? (dx < 0 ? 2u : 1u) : (dx < 0 ? 4u : 3u);
-}
-
 // Segments per (command, strip row, tile column) slot: a segment belongs to every slot its cells
-// can touch within each strip row. Pass 0 counts the slots' segments, records each slot's command
-// and counts the work per DDA kind; tiles entirely right of a segment get its per-row cover in
-// their backdrop (added once, at the first tile right of it; a prefix over tile columns carries it
-// on). Pass 1 writes the raster work items, grouped by DDA kind.
+// can touch within each strip row. Pass 0 counts the slots' segments and records each slot's
+// command; tiles entirely right of a segment get its per-row cover in their backdrop (added once,
+// at the first tile right of it; a prefix over tile columns carries it on). Pass 1 writes the
+// (segment, mask index) work items, grouped by slot in slot order, so the items of consecutive
+// slots with segments are contiguous.
 __global__ void __launch_bounds__(256) seg_bin_kernel(FrameView f, int scatter) {
-  __shared__ uint32_t s_count[5], s_base[5];
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (threadIdx.x < 5) s_count[threadIdx.x] = 0;
-  uint32_t c = 0, ctx = 0xFFFFFFFFu;
-  if (s < f.num_segs) {
-    c = f.seg_meta[s] >> 1;
-    ctx = f.cmd_tile_x[c];
-  }
-  const bool valid = ctx != 0xFFFFFFFFu;
-  DevSeg g{};
-  uint32_t kind = 0, base = 0, sm = 0;
-  int tx0 = 0, tx1 = -1, ntx = 0, sr0 = 0, r0 = 0, r1 = -1, ey0 = 0, ey1 = 0;
-  if (valid) {
-    sm = 0u - (f.seg_meta[s] & 1u);
-    tx0 = int(ctx & 0xFFFFu); tx1 = int(ctx >> 16); ntx = tx1 - tx0 + 1;
-    const uint32_t yr = f.cmd_yr[c];
-    sr0 = int((yr & 0xFFFFu) >> kStripShift);
-    const int sr1 = int((yr >> 16) >> kStripShift);
-    g = f.segs[s];
-    kind = dda_kind(g);
-    ey0 = g.y0 >> 8; ey1 = (g.y1 - 1) >> 8;
-    r0 = max(ey0 >> kStripShift, sr0); r1 = min(ey1 >> kStripShift, sr1);
-    base = f.cmdrow_base[c];
-  }
-  __syncthreads();
-  // per strip row: slots [t0, t1] get the segment, the first tile right of it its cover
-  uint32_t n_entries = 0;
+  if (s >= f.num_segs) return;
+  const uint32_t c = f.seg_meta[s] >> 1;
+  const uint32_t ctx = f.cmd_tile_x[c];
+  if (ctx == 0xFFFFFFFFu) return;
+  const uint32_t sm = 0u - (f.seg_meta[s] & 1u);
+  const int tx0 = int(ctx & 0xFFFFu), tx1 = int(ctx >> 16), ntx = tx1 - tx0 + 1;
+  const uint32_t yr = f.cmd_yr[c];
+  const int sr0 = int((yr & 0xFFFFu) >> kStripShift), sr1 = int((yr >> 16) >> kStripShift);
+  const DevSeg g = f.segs[s];
+  const int ey0 = g.y0 >> 8, ey1 = (g.y1 - 1) >> 8;
+  const int r0 = max(ey0 >> kStripShift, sr0), r1 = min(ey1 >> kStripShift, sr1);
+  const uint32_t base = f.cmdrow_base[c];
   for (int r = r0; r <= r1; r++) {
     int t_first, t_last;
     strip_tile_range(g, r, t_first, t_last);
     const int t0 = max(t_first, tx0), t1 = min(t_last, tx1);
-    if (t1 >= t0) n_entries += uint32_t(t1 - t0 + 1);
-    if (scatter) continue;
     const uint32_t row_slot = base + uint32_t(r - sr0) * uint32_t(ntx);
     for (int t = t0; t <= t1; t++) {
       const uint32_t slot = row_slot + uint32_t(t - tx0);
-      atomicAdd(&f.cmdrow_counts[slot], 1u);
-      f.slot_cmd[slot] = c;
+      if (!scatter) {
+        atomicAdd(&f.cmdrow_counts[slot], 1u);
+        f.slot_cmd[slot] = c;
+      }
+      else {
+        const uint32_t pos = f.slot_first[slot] + atomicSub(&f.cmdrow_counts[slot], 1u) - 1u;
+        if (pos >= f.num_seglist) { atomicOr(&f.error_flags[0], 4u); continue; }
+        f.entries[pos] = make_uint2(s, f.slot_mask[slot] - 1u);
+      }
     }
-    if (t_last + 1 <= tx1) {
+    if (!scatter && t_last + 1 <= tx1) {
       uint32_t* bd = f.backdrop + size_t(row_slot + uint32_t(t_last + 1 - tx0)) * kStripRows;
       int ya = max(ey0, r << kStripShift), yb = min(ey1, (r << kStripShift) + kStripRows - 1);
       for (int y = ya; y <= yb; y++) {
@@ -624,26 +608,6 @@ __global__ void __launch_bounds__(256) seg_bin_kernel(FrameView f, int scatter) 
         uint32_t cov = (uint32_t(bot - top) ^ sm) - sm;
         atomicAdd(&bd[y & (kStripRows - 1)], cov << 9);
       }
-    }
-  }
-  // work per DDA kind, aggregated per block before it reaches the five global counters
-  const uint32_t local = n_entries ? atomicAdd(&s_count[kind], n_entries) : 0u;
-  __syncthreads();
-  if (threadIdx.x < 5 && s_count[threadIdx.x])
-    s_base[threadIdx.x] = atomicAdd(&f.kind_info[(scatter ? 5 : 0) + threadIdx.x], s_count[threadIdx.x]);
-  if (!scatter) return;                               // uniform over the block
-  __syncthreads();
-  if (!n_entries) return;
-  uint32_t pos = f.kind_info[10 + kind] + s_base[kind] + local;
-  if (pos + n_entries > f.num_seglist + 1u) { atomicOr(&f.error_flags[0], 4u); return; }
-  for (int r = r0; r <= r1; r++) {
-    int t_first, t_last;
-    strip_tile_range(g, r, t_first, t_last);
-    const int t0 = max(t_first, tx0), t1 = min(t_last, tx1);
-    const uint32_t row_slot = base + uint32_t(r - sr0) * uint32_t(ntx);
-    for (int t = t0; t <= t1; t++) {
-      const uint32_t slot = row_slot + uint32_t(t - tx0);
-      f.entries[pos++] = make_uint4(s, slot, f.slot_mask[slot] - 1u, uint32_t(t << kTileShift) | (uint32_t(r << kStripShift) << 16));
     }
   }
 }
@@ -667,13 +631,6 @@ __global__ void slot_compact_kernel(FrameView f) {
     f.slot_mask[i] = 0u;
   }
   if (i == f.num_cmdrows - 1) f.totals[5] = f.cmdrow_offsets[i] + (f.cmdrow_counts[i] ? 1u : 0u);
-}
-
-__global__ void kind_offsets_kernel(FrameView f) {
-  if (threadIdx.x || blockIdx.x) return;
-  uint32_t acc = 0;
-  for (int k = 0; k < 5; k++) { f.kind_info[10 + k] = acc; acc += f.kind_info[k]; }
-  f.kind_info[15] = acc;
 }
 
 // Prefix of the backdrop deltas over the tile columns of every (command, strip row, row).
@@ -721,60 +678,121 @@ __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// K3a - coverage, in two kernels. A slot is (analytic command, strip row, tile column): 4 rows x 32
-// pixels. `raster_kernel` takes one (segment, slot) work item per thread, in DDA-kind order so that
-// a warp's lanes follow the same path through the rasterizer, and adds the cells into the slot's
-// cell block in global memory (and its left-of-tile cover into the slot's backdrop). The sums are
-// modular u32, so the order of the atomic adds does not matter. `sweep_kernel` then turns each
-// slot's cells into 128 8-bit masks (8-lane shuffle prefix per row from the backdrop).
+// K3a - coverage. A slot is (analytic command, strip row, tile column): 4 rows x 32 pixels. One
+// block takes kCoverSlots consecutive slots with segments (by mask index), whose work items are
+// contiguous: it rasterizes them, a chunk at a time sorted by the DDA path the reference
+// rasterizer takes (so a warp's lanes follow the same path), into the slots' cells in shared memory
+// (atomicAdd: u32 sums commute) and their left-of-tile cover into the slots' backdrops, then one
+// warp per slot sweeps the cells (8-lane shuffle prefix per row from the backdrop) into 128 8-bit
+// masks.
 // ---------------------------------------------------------------------------------------------
 
 constexpr int kStripsPerTile = kTileH / kStripRows;
 constexpr int kFineWarps = kFineThreads / 32;
 constexpr int kSlotPixels = kStripRows * kTileW;
 
-__global__ void zero_cells_kernel(FrameView f) {
-  const uint32_t n = min(f.totals[5], f.mask_capacity) * uint32_t(kSlotPixels / 4);
-  uint4* cells = reinterpret_cast<uint4*>(f.cells);
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    cells[i] = make_uint4(0u, 0u, 0u, 0u);
+// DDA path a segment takes through the reference rasterizer (prepare's classification).
+__device__ __forceinline__ uint32_t dda_kind(const DevSeg& g) {
+  const int dx = g.x1 - g.x0, adx = dx < 0 ? -dx : dx, dy = g.y1 - g.y0;
+  if ((g.x0 >> 8) == (g.x1 >> 8) && ((g.y0 >> 8) == ((g.y1 - 1) >> 8) || adx == 0)) return 0u;
+  return dy >= adx ? (dx < 0 ? 2u : 1u) : (dx < 0 ? 4u : 3u);
 }
 
-__global__ void __launch_bounds__(256) raster_kernel(FrameView f) {
-  const uint32_t n = f.kind_info[15];
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const uint4 e = f.entries[i];
-    if (e.z >= f.mask_capacity) continue;
-    ras::WindowSink sink{f.cells + size_t(e.z) * kSlotPixels, f.backdrop + size_t(e.y) * kStripRows,
-                         int(e.w & 0xFFFFu)};
-    ras::segment_to_window(f.segs[e.x], f.seg_meta[e.x] & 1u, int(e.w >> 16), kStripRows, INT32_MAX, sink);
-  }
-}
+// K slots per group, 4 threads per slot; a round sorts and rasterizes up to 4 items per thread.
+template<int K>
+__global__ void __launch_bounds__(4 * K) coverage_kernel(FrameView f) {
+  constexpr int kCoverThreads = 4 * K;
+  constexpr int kCoverChunk = 4 * kCoverThreads;
+  __shared__ __align__(16) uint32_t cells[K][kSlotPixels];
+  __shared__ uint32_t bd[K][kStripRows];
+  __shared__ int2 org[K];                  // x of the slot's first column, its first row
+  __shared__ uint32_t meta[K];             // command flags << 16 | alpha
+  __shared__ uint2 items[kCoverChunk];
+  __shared__ uint32_t kcount[5], kbase[5];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t num_masks = min(f.totals[5], f.mask_capacity);
+  const uint32_t groups = (num_masks + K - 1) / K;
 
-__global__ void __launch_bounds__(256) sweep_kernel(FrameView f) {
-  const int lane = threadIdx.x & 31, prow = lane >> 3;
-  const uint32_t n = min(f.totals[5], f.mask_capacity);
-  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
-    const uint32_t slot = f.mask_slot[i];
-    const DevCmd& cmd = f.cmds[f.slot_cmd[slot]];
-    const uint32_t flags = cmd.flags, alpha = cmd.alpha;
-    const uint4 cv4 = reinterpret_cast<const uint4*>(f.cells + size_t(i) * kSlotPixels)[lane];
-    const uint32_t s4 = cv4.x + cv4.y + cv4.z + cv4.w;
-    uint32_t inc = s4;
-#pragma unroll
-    for (int o = 1; o < 8; o <<= 1) {
-      uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o, 8);
-      if ((lane & 7) >= o) inc += v;
+  for (uint32_t grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+    const uint32_t m0 = grp * K;
+    const int nk = int(min(uint32_t(K), num_masks - m0));
+    if (tid < nk) {
+      const uint32_t slot = f.mask_slot[m0 + tid];
+      const uint32_t c = f.slot_cmd[slot];
+      const uint32_t ctx = f.cmd_tile_x[c];
+      const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
+      const uint32_t local = slot - f.cmdrow_base[c];
+      const uint32_t sr = ((f.cmd_yr[c] & 0xFFFFu) >> kStripShift) + local / ntx;
+      org[tid] = make_int2(int(((ctx & 0xFFFFu) + local % ntx) << kTileShift), int(sr << kStripShift));
+      meta[tid] = (f.cmds[c].flags << 16) | f.cmds[c].alpha;
+      const uint4 b4 = *reinterpret_cast<const uint4*>(f.backdrop + size_t(slot) * kStripRows);
+      bd[tid][0] = b4.x; bd[tid][1] = b4.y; bd[tid][2] = b4.z; bd[tid][3] = b4.w;
     }
-    uint32_t cov = (256u << 9) + f.backdrop[size_t(slot) * kStripRows + prow] + inc - s4;
-    const uint32_t rule = (flags & 2u) ? 0x1FFu : 0xFFFFFFFFu;
-    uint32_t m;
-    cov += cv4.x; m = px::calc_mask(cov, rule, alpha);
-    cov += cv4.y; m |= px::calc_mask(cov, rule, alpha) << 8;
-    cov += cv4.z; m |= px::calc_mask(cov, rule, alpha) << 16;
-    cov += cv4.w; m |= px::calc_mask(cov, rule, alpha) << 24;
-    reinterpret_cast<uint32_t*>(f.masks + size_t(i) * kSlotPixels)[lane] = m;
+    for (int i = tid; i < K * kSlotPixels / 4; i += kCoverThreads)
+      reinterpret_cast<uint4*>(&cells[0][0])[i] = make_uint4(0u, 0u, 0u, 0u);
+    const uint32_t e0 = f.slot_first[f.mask_slot[m0]];
+    const uint32_t e1 = f.slot_first[f.mask_slot[m0 + uint32_t(nk) - 1u] + 1u];
+    __syncthreads();
+
+    for (uint32_t chunk = e0; chunk < e1; chunk += kCoverChunk) {
+      const int n = int(min(uint32_t(kCoverChunk), e1 - chunk));
+      if (tid < 5) kcount[tid] = 0;
+      __syncthreads();
+      // sort the chunk's items by DDA kind (counting sort through shared memory)
+      uint2 it[kCoverChunk / kCoverThreads];
+      uint32_t kind[kCoverChunk / kCoverThreads], pos[kCoverChunk / kCoverThreads];
+#pragma unroll
+      for (int q = 0; q < kCoverChunk / kCoverThreads; q++) {
+        const int i = tid + q * kCoverThreads;
+        if (i < n) {
+          it[q] = f.entries[chunk + uint32_t(i)];
+          kind[q] = dda_kind(f.segs[it[q].x]);
+          pos[q] = atomicAdd(&kcount[kind[q]], 1u);
+        }
+      }
+      __syncthreads();
+      if (tid == 0) {
+        uint32_t acc = 0;
+        for (int k = 0; k < 5; k++) { kbase[k] = acc; acc += kcount[k]; }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < kCoverChunk / kCoverThreads; q++) {
+        const int i = tid + q * kCoverThreads;
+        if (i < n) items[kbase[kind[q]] + pos[q]] = it[q];
+      }
+      __syncthreads();
+      for (int i = tid; i < n; i += kCoverThreads) {
+        const uint2 e = items[i];
+        const int j = int(e.y - m0);
+        ras::WindowSink sink{cells[j], bd[j], org[j].x};
+        ras::segment_to_window(f.segs[e.x], f.seg_meta[e.x] & 1u, org[j].y, kStripRows, INT32_MAX, sink);
+      }
+      __syncthreads();
+    }
+
+    // sweep: lane covers row lane / 8, columns (lane % 8) * 4 .. + 3 of the slot
+    const int prow = lane >> 3;
+    for (int j = warp; j < nk; j += kCoverThreads / 32) {
+      const uint32_t flags = meta[j] >> 16, alpha = meta[j] & 0xFFFFu;
+      const uint4 cv4 = *reinterpret_cast<const uint4*>(&cells[j][lane * 4]);
+      const uint32_t s4 = cv4.x + cv4.y + cv4.z + cv4.w;
+      uint32_t inc = s4;
+#pragma unroll
+      for (int o = 1; o < 8; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o, 8);
+        if ((lane & 7) >= o) inc += v;
+      }
+      uint32_t cov = (256u << 9) + bd[j][prow] + inc - s4;
+      const uint32_t rule = (flags & 2u) ? 0x1FFu : 0xFFFFFFFFu;
+      uint32_t m;
+      cov += cv4.x; m = px::calc_mask(cov, rule, alpha);
+      cov += cv4.y; m |= px::calc_mask(cov, rule, alpha) << 8;
+      cov += cv4.z; m |= px::calc_mask(cov, rule, alpha) << 16;
+      cov += cv4.w; m |= px::calc_mask(cov, rule, alpha) << 24;
+      reinterpret_cast<uint32_t*>(f.masks + size_t(m0 + uint32_t(j)) * kSlotPixels)[lane] = m;
+    }
+    __syncthreads();
   }
 }
 
@@ -1107,8 +1125,8 @@ int fine_grid_size(int blocks_per_sm) {
   return sms * (blocks_per_sm > 0 && blocks_per_sm < max_per_sm ? blocks_per_sm : max_per_sm);
 }
 
-// Coverage pass: compact the slots with segments, write the kind-ordered raster work, rasterize,
-// sweep. Called after the binning count pass and the backdrop prefix.
+// Coverage pass: compact the slots with segments, lay out their work items slot by slot,
+// rasterize and sweep. Called after the binning count pass and the backdrop prefix.
 int launch_coverage(const FrameView& f, const LaunchConfig& cfg, uint32_t* scan_tmp, cudaStream_t st) {
   if (!f.num_cmdrows) return 0;
   static int sms = 0;
@@ -1121,14 +1139,13 @@ int launch_coverage(const FrameView& f, const LaunchConfig& cfg, uint32_t* scan_
   slot_flags_kernel<<<cdiv(f.num_cmdrows, 256), 256, 0, st>>>(f); k++;
   k += exclusive_scan(f.cmdrow_offsets, f.cmdrow_offsets, f.num_cmdrows, scan_tmp, st);
   slot_compact_kernel<<<cdiv(f.num_cmdrows, 256), 256, 0, st>>>(f); k++;
-  kind_offsets_kernel<<<1, 32, 0, st>>>(f); k++;
+  k += exclusive_scan(f.cmdrow_counts, f.slot_first, f.num_cmdrows + 1, scan_tmp, st);
   k += launch_seg_bin(f, 1, st);
-  const int per_sm = cfg.cover_blocks_per_sm > 0 ? cfg.cover_blocks_per_sm : 8;
-  const int rb = cfg.raster_block == 128 ? 128 : 256;
-  zero_cells_kernel<<<sms * 4, 256, 0, st>>>(f); k++;
-  raster_kernel<<<sms * per_sm * (256 / rb), rb, 0, st>>>(f); k++;
-  sweep_kernel<<<sms * per_sm, 256, 0, st>>>(f); k++;
-  return k;
+  const int per_sm = cfg.cover_blocks_per_sm > 0 ? cfg.cover_blocks_per_sm : 16;
+  if (cfg.cover_slots == 16) coverage_kernel<16><<<sms * per_sm, 64, 0, st>>>(f);
+  else if (cfg.cover_slots == 64) coverage_kernel<64><<<sms * per_sm, 256, 0, st>>>(f);
+  else coverage_kernel<32><<<sms * per_sm, 128, 0, st>>>(f);
+  return k + 1;
 }
 
 int launch_row_states(const FrameView& f, cudaStream_t st) {

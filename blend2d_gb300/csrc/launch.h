@@ -11,7 +11,7 @@ namespace blgpu {
 
 // Launch shapes the autotuner chooses between (0 = the default for that field).
 struct LaunchConfig {
-  int raster_block = 256;         // threads per block of the raster kernel (128 or 256)
+  int cover_slots = 64;           // slots with segments per block of the coverage kernel (16, 32 or 64)
   int cover_blocks_per_sm = 0;    // coverage grid: blocks per SM (0 = as many as fit)
   int fine_blocks_per_sm = 0;     // composite grid: blocks per SM (0 = as many as fit)
   int edge_block = 128;           // threads per block of the per-item edge builder (64/128/256)

@@ -230,12 +230,11 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     v.tile_canvas = L.take<uint32_t>(fr.tiles + 1);
     // [0] work queue, [1] line items, [2] cubic curves, [3] their queue, [4..12) totals,
     // [12..16) error flags, [16..20) pixel ops (2 x u64), [21] quadratic / conic curves, [22] their
-    // queue, [32..48) raster work per DDA kind
+    // queue
     v.work_counter = L.take<uint32_t>(kCounterWords);
     v.totals = v.work_counter + 4;
     v.error_flags = v.work_counter + 12;
     v.pixel_ops = reinterpret_cast<unsigned long long*>(v.work_counter + 16);
-    v.kind_info = v.work_counter + 32;
     v.rs_count = L.take<uint32_t>(nc + 1);
     v.rs_base = L.take<uint32_t>(nc + 1);
     scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, fr.rows + 1)));
@@ -412,17 +411,17 @@ int Runtime::enqueue_render_half(cudaStream_t st, bool timed) {
 }
 
 // Buffers sized by the counting half's totals. Slots with segments are at most min(slots, raster
-// work items), and each has one block of cells and one block of masks.
+// work items), and each has one block of masks.
 static void plan_dynamic(Layout& L, FrameView& v, const FrameTotals& t) {
   const uint32_t slots = std::min(t.cmdrows, t.seglist);
   v.cmdrow_counts = L.take<uint32_t>(t.cmdrows + 1);
   v.cmdrow_offsets = L.take<uint32_t>(t.cmdrows + 1 + scan_temp_words(t.cmdrows + 1));
   v.slot_cmd = L.take<uint32_t>(t.cmdrows + 1);
   v.slot_mask = L.take<uint32_t>(t.cmdrows + 1);
+  v.slot_first = L.take<uint32_t>(t.cmdrows + 2);
   v.backdrop = L.take<uint32_t>((size_t(t.cmdrows) + 1) * kStripRows);
-  v.entries = L.take<uint4>(size_t(t.seglist) + 1);
+  v.entries = L.take<uint2>(size_t(t.seglist) + 1);
   v.mask_slot = L.take<uint32_t>(size_t(slots) + 1);
-  v.cells = L.take<uint32_t>((size_t(slots) + 1) * kStripRows * kTileW);
   v.masks = L.take<uint8_t>((size_t(slots) + 1) * kStripRows * kTileW);
   v.row_cmds = L.take<uint32_t>(t.row_entries + 1);
   v.row_states = L.take<float4>(t.row_states + 1);
@@ -566,7 +565,6 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     v.totals = v.work_counter + 4;
     v.error_flags = v.work_counter + 12;
     v.pixel_ops = reinterpret_cast<unsigned long long*>(v.work_counter + 16);
-    v.kind_info = v.work_counter + 32;
     v.rs_count = L.take<uint32_t>(nc + 1);
     v.rs_base = L.take<uint32_t>(nc + 1);
     a_scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, fr.rows + 1)));
@@ -743,15 +741,15 @@ BLGpuResult Runtime::autotune(int trials, LaunchConfig* best_out, double* best_m
   LaunchConfig best = cfg;
   double best_ms = 0.0;
   if (!r) r = measure(best, best_ms);
-  const int raster_blocks[] = {128, 256};
+  const int cover_slots[] = {16, 32, 64};
   const int blocks[] = {0, 1, 2, 3};
   const int edge_blocks[] = {64, 128, 256};
   for (int field = 0; field < 5 && !r; field++) {
-    const int* vals = field == 0 ? raster_blocks : (field == 3 ? edge_blocks : blocks);
-    const int nvals = field == 0 ? 2 : (field == 3 ? 3 : 4);
+    const int* vals = field == 0 ? cover_slots : (field == 3 ? edge_blocks : blocks);
+    const int nvals = field == 0 ? 3 : (field == 3 ? 3 : 4);
     for (int k = 0; k < nvals && !r; k++) {
       LaunchConfig c = best;
-      int* slot = field == 0 ? &c.raster_block : field == 1 ? &c.cover_blocks_per_sm : field == 2 ? &c.fine_blocks_per_sm
+      int* slot = field == 0 ? &c.cover_slots : field == 1 ? &c.cover_blocks_per_sm : field == 2 ? &c.fine_blocks_per_sm
                 : field == 3 ? &c.edge_block : &c.cubic_blocks_per_sm;
       if (*slot == vals[k]) continue;
       *slot = vals[k];

@@ -118,7 +118,7 @@ typedef struct BLGpuStats {
  * band geometry are fixed by the pipeline (32-pixel tile columns matching a warp's lanes, the
  * reference's band heights), so the tunable parameters are how work is grouped and gridded. */
 typedef struct BLGpuLaunchConfig {
-  int32_t raster_block;         /* threads per block of the coverage pass's raster kernel: 128 or 256 */
+  int32_t cover_slots;          /* slots (command x 4-row strip x 32-px tile column) per coverage block: 16, 32 or 64 */
   int32_t cover_blocks_per_sm;  /* coverage pass grid */
   int32_t fine_blocks_per_sm;   /* composite pass grid */
   int32_t edge_block;           /* threads per block of the per-item edge builder: 64, 128 or 256 */

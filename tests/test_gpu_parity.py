@@ -263,15 +263,15 @@ def test_autotune_keeps_pixels_and_every_config_renders_the_same():
         bg.render_stream(rt, stream, dev)
         best, ms = rt.autotune(trials=2)
         torch.cuda.synchronize()
-        assert ms > 0 and best.raster_block in (128, 256) and best.edge_block in (64, 128, 256)
+        assert ms > 0 and best.cover_slots in (16, 32, 64) and best.edge_block in (64, 128, 256)
         assert not _diff(dev.cpu().numpy().view(np.uint32), want)       # tuning left the pixels alone
-        for cfg in [dict(raster_block=128, edge_block=64, fine_blocks_per_sm=1, cover_blocks_per_sm=1, cubic_blocks_per_sm=1),
-                    dict(raster_block=256, edge_block=256, fine_blocks_per_sm=0, cover_blocks_per_sm=0, cubic_blocks_per_sm=0)]:
+        for cfg in [dict(cover_slots=16, edge_block=64, fine_blocks_per_sm=1, cover_blocks_per_sm=1, cubic_blocks_per_sm=1),
+                    dict(cover_slots=32, edge_block=256, fine_blocks_per_sm=0, cover_blocks_per_sm=0, cubic_blocks_per_sm=0)]:
             rt.set_launch_config(bg.LaunchConfig(**cfg))
             got = bg.render_stream(rt, stream)
             assert not _diff(got, want), cfg
         with pytest.raises(bg.BLGpuError):
-            rt.set_launch_config(bg.LaunchConfig(raster_block=96, edge_block=128))
+            rt.set_launch_config(bg.LaunchConfig(cover_slots=24, edge_block=128))
 
 
 @pytest.mark.parametrize("variant", ["default", "avx2", "scalar"])
