@@ -215,10 +215,13 @@ struct FrameView {
   uint32_t* tile_order;        // tile processing order for the persistent fine kernel
   uint32_t* tile_canvas;       // canvas index per global tile
   uint32_t* work_counter;      // [0] fine work queue, [1] items, [2] cubics, [3] their queue, [21] quads, [22] their queue
-  uint32_t* totals;            // [8] segments, seglist bound, (cmd,strip) slots, row entries, gradient rows
+  uint32_t* totals;            // [8] segments, seglist bound, (cmd,strip) slots, row entries, gradient rows,
+                               //   slots with segments, conic row runs
   uint32_t* rs_count;          // [num_cmds + 1] gradient row states per command (radial/conic styles)
   uint32_t* rs_base;           // exclusive scan of rs_count
   float4* row_states;          // per (command, row): the fetcher's row values f0, f1, f2
+  uint32_t* rb_count;          // [num_cmds + 1] conic styles: runs of rows sharing one fetcher start
+  uint32_t* rb_base;           // exclusive scan of rb_count
   uint32_t* error_flags;
   unsigned long long* pixel_ops;   // [2] composited pixels (mask != 0), of which pattern-fetched
   uint32_t num_cmds;
@@ -230,6 +233,7 @@ struct FrameView {
   uint32_t num_cmdrows;
   uint32_t num_seglist;
   uint32_t num_row_states;
+  uint32_t num_row_runs;       // conic row runs (sum of rb_count)
 };
 
 }  // namespace blgpu

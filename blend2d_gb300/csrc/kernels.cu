@@ -547,9 +547,15 @@ __global__ void cmd_tiles_kernel(FrameView f, uint32_t* cmdrow_counts_per_cmd, u
     f.cmd_yr[c] = 0x0000FFFFu;
     cmdrow_counts_per_cmd[c] = 0;
     f.rs_count[c] = 0;
+    f.rb_count[c] = 0;
     return;
   }
-  f.rs_count[c] = px::has_row_table(f.styles[cmd.style].fetch) ? uint32_t(y1 - y0 + 1) : 0u;
+  const uint32_t fetch = f.styles[cmd.style].fetch;
+  f.rs_count[c] = px::has_row_table(fetch) ? uint32_t(y1 - y0 + 1) : 0u;
+  // conic row runs: the reference restarts the fetcher at each band of an analytic fill, once for
+  // a box fill
+  f.rb_count[c] = fetch != kFetchConic ? 0u
+                : cmd.kind == kFillAnalytic ? uint32_t(y1 / cv.band_height - y0 / cv.band_height + 1) : 1u;
   f.cmd_xr[c] = uint32_t(x0) | (uint32_t(x1) << 16);
   f.cmd_yr[c] = uint32_t(y0) | (uint32_t(y1) << 16);
   uint32_t tx0 = uint32_t(x0) >> kTileShift, tx1 = uint32_t(x1) >> kTileShift;
@@ -804,7 +810,7 @@ __global__ void __launch_bounds__(4 * K) coverage_kernel(FrameView f) {
 // lane from the coverage pass, box fills compute theirs, then fetch + SrcOver/SrcCopy.
 // ---------------------------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
+__global__ void __launch_bounds__(kFineThreads, 4) fine_kernel(FrameView f) {
   const int lane = threadIdx.x & 31;
   const int prow = lane >> 3;            // row within the strip
   const int pcol = (lane & 7) * 4;       // first of this lane's 4 columns
@@ -939,16 +945,35 @@ __global__ void __launch_bounds__(kFineThreads) fine_kernel(FrameView f) {
             rs = px::row_state(st, y, fetch_y0);
           }
           uint32_t n = 0;
-          // one copy of the fetch + composite code: the 4 pixels rotate through slot 0
-#pragma unroll 1
-          for (int k = 0; k < 4; k++) {
-            if (m[0] && xp + k < cv.w) {
-              uint32_t sv = px::fetch(st, rs, xp + k, f.luts, f.images);
-              pix[0] = px::composite(pix[0], sv, m[0], src_copy);
-              n++;
+          if (px::is_gradient(st.fetch)) {
+            // the 4 pixels' LUT indices first, so their 4 table loads are in flight together
+            const uint32_t* lut = f.luts + st.lut_offset;
+            uint32_t sv[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+              const bool on = m[k] && xp + k < cv.w;
+              sv[k] = on ? __ldg(lut + px::gradient_index(st, rs, xp + k)) : 0u;
             }
-            uint32_t tp = pix[0]; pix[0] = pix[1]; pix[1] = pix[2]; pix[2] = pix[3]; pix[3] = tp;
-            uint32_t tm = m[0]; m[0] = m[1]; m[1] = m[2]; m[2] = m[3]; m[3] = tm;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+              if (m[k] && xp + k < cv.w) {
+                pix[k] = px::composite(pix[k], sv[k], m[k], src_copy);
+                n++;
+              }
+            }
+          }
+          else {
+            // one copy of the fetch + composite code: the 4 pixels rotate through slot 0
+#pragma unroll 1
+            for (int k = 0; k < 4; k++) {
+              if (m[0] && xp + k < cv.w) {
+                uint32_t sv = px::fetch(st, rs, xp + k, f.luts, f.images);
+                pix[0] = px::composite(pix[0], sv, m[0], src_copy);
+                n++;
+              }
+              uint32_t tp = pix[0]; pix[0] = pix[1]; pix[1] = pix[2]; pix[2] = pix[3]; pix[3] = tp;
+              uint32_t tm = m[0]; m[0] = m[1]; m[1] = m[2]; m[2] = m[3]; m[3] = tm;
+            }
           }
           ops += n;
           pat_ops += st.fetch >= kFetchPatAlignedPad ? n : 0u;
@@ -985,8 +1010,42 @@ __global__ void row_state_kernel(FrameView f, uint32_t total) {
   const int y = int(f.cmd_yr[c] & 0xFFFFu) + int(t - f.rs_base[c]);
   // the row the reference initialized its fetcher at (start of the band for analytic fills)
   int fetch_y0 = cmd.kind == kFillAnalytic ? max(cmd.box[1], (y / cv.band_height) * cv.band_height) : cmd.fetch_y0;
-  px::RowState rs = px::row_state(f.styles[cmd.style], y, fetch_y0);
+  const DevStyle& st = f.styles[cmd.style];
+  if (st.fetch == kFetchConic) return;            // conic_rows_kernel
+  px::RowState rs = px::row_state(st, y, fetch_y0);
   f.row_states[t] = make_float4(rs.f0, rs.f1, rs.f2, 0.0f);
+}
+
+// Conic row values, one thread per run of rows sharing a fetcher start: the reference steps the
+// fetcher's FP64 position row by row from there, so a run is one sequential chain (a thread per
+// row would repeat the chain's prefix in every row; the FP64 pipe is the scarce one).
+__global__ void conic_rows_kernel(FrameView f, uint32_t total) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  uint32_t lo = 0, hi = f.num_cmds - 1;       // last command whose first run is <= t
+  while (lo < hi) { uint32_t mid = (lo + hi + 1) >> 1; if (f.rb_base[mid] <= t) lo = mid; else hi = mid - 1; }
+  const uint32_t c = lo;
+  const DevCmd& cmd = f.cmds[c];
+  const DevCanvas& cv = f.canvases[cmd.canvas];
+  const DevStyle& st = f.styles[cmd.style];
+  const int y0 = int(f.cmd_yr[c] & 0xFFFFu), y1 = int(f.cmd_yr[c] >> 16);
+  int ya = y0, yb = y1, fs = cmd.fetch_y0;
+  if (cmd.kind == kFillAnalytic) {
+    const int band = y0 / cv.band_height + int(t - f.rb_base[c]);
+    ya = max(y0, band * cv.band_height);
+    yb = min(y1, band * cv.band_height + cv.band_height - 1);
+    fs = max(cmd.box[1], band * cv.band_height);
+  }
+  double tx = st.con_tx + st.con_yx * double(fs);
+  double ty = st.con_ty + st.con_yy * double(fs);
+  int cur = fs;
+  float4* out = f.row_states + f.rs_base[c] + uint32_t(ya - y0);
+  for (int y = ya; y <= yb; y++) {
+    for (; cur < y; cur++) { tx += st.con_yx; ty += st.con_yy; }
+    const float ay = float(ty);
+    const uint32_t byb = uint32_t(int32_t(__float_as_uint(ay)) >> 31) & __float_as_uint(st.con_n1);
+    *out++ = make_float4(float(tx), fabsf(ay), __uint_as_float(byb), 0.0f);
+  }
 }
 
 // Tile/row bookkeeping: canvas of every global tile and tile row, identity processing order.
@@ -1151,7 +1210,9 @@ int launch_coverage(const FrameView& f, const LaunchConfig& cfg, uint32_t* scan_
 int launch_row_states(const FrameView& f, cudaStream_t st) {
   if (!f.num_row_states) return 0;
   row_state_kernel<<<cdiv(f.num_row_states, 128), 128, 0, st>>>(f, f.num_row_states);
-  return 1;
+  if (!f.num_row_runs) return 1;
+  conic_rows_kernel<<<cdiv(f.num_row_runs, 64), 64, 0, st>>>(f, f.num_row_runs);
+  return 2;
 }
 
 // work_counter must be zero on entry.

@@ -174,25 +174,24 @@ __device__ RowState row_state(const DevStyle& st, int y, int fetch_y0) {
   return r;
 }
 
-__device__ __forceinline__ uint32_t fetch(const DevStyle& st, const RowState& r, int x,
-                                          const uint32_t* __restrict__ luts, const uint32_t* __restrict__ images) {
+__device__ __forceinline__ bool is_gradient(uint32_t fetch) { return fetch >= kFetchLinearPad && fetch <= kFetchConic; }
+
+// LUT index of pixel x of a gradient fetcher (linear, radial or conic): the fetchers' per-pixel
+// arithmetic up to the table lookup.
+__device__ __forceinline__ uint32_t gradient_index(const DevStyle& st, const RowState& r, int x) {
   switch (st.fetch) {
-    case kFetchSolid:
-      return st.solid;
     case kFetchLinearPad: case kFetchLinearRoR: {
       uint64_t pt = r.a64 + uint64_t(uint32_t(x)) * st.lin_dt;
-      uint32_t idx = grad_index(uint32_t(pt >> 32), st.fetch == kFetchLinearPad, st.maxi, st.rori);
-      return __ldg(luts + st.lut_offset + idx);
+      return grad_index(uint32_t(pt >> 32), st.fetch == kFetchLinearPad, st.maxi, st.rori);
     }
     case kFetchRadialPad: case kFetchRadialRoR: {
       float xf = float(x);
       float sq_x = xf * xf;
       float a = sqrtf(fabsf(sq_x * st.rad_ddd + (xf * r.f2 + r.f1)));
       float v = (xf * st.rad_bd + r.f0) + a;
-      uint32_t idx = grad_index(uint32_t(trunc_f(v)), st.fetch == kFetchRadialPad, st.maxi, st.rori);
-      return __ldg(luts + st.lut_offset + idx);
+      return grad_index(uint32_t(trunc_f(v)), st.fetch == kFetchRadialPad, st.maxi, st.rori);
     }
-    case kFetchConic: {
+    default: {    // kFetchConic
       float xf = float(x) * st.con_xx + r.f0;
       float ax = fabsf(xf);
       float ay = r.f1;
@@ -208,9 +207,18 @@ __device__ __forceinline__ uint32_t fetch(const DevStyle& st, const RowState& r,
       v = fabsf(v - __uint_as_float(uint32_t(int32_t(__float_as_uint(xf)) >> 31) & __float_as_uint(st.con_n2)));
       v = fabsf(v - r.f2) + st.con_offset;
       int32_t ni = nearby_f(v);
-      uint32_t idx = uint32_t(ni < st.con_maxi ? ni : st.con_maxi) & uint32_t(st.con_rori);
-      return __ldg(luts + st.lut_offset + idx);
+      return uint32_t(ni < st.con_maxi ? ni : st.con_maxi) & uint32_t(st.con_rori);
     }
+  }
+}
+
+__device__ __forceinline__ uint32_t fetch(const DevStyle& st, const RowState& r, int x,
+                                          const uint32_t* __restrict__ luts, const uint32_t* __restrict__ images) {
+  switch (st.fetch) {
+    case kFetchSolid:
+      return st.solid;
+    case kFetchLinearPad: case kFetchLinearRoR: case kFetchRadialPad: case kFetchRadialRoR: case kFetchConic:
+      return __ldg(luts + st.lut_offset + gradient_index(st, r, x));
     case kFetchPatAlignedPad: case kFetchPatAlignedRepeat: case kFetchPatAlignedRoR: {
       uint32_t kind = st.fetch - kFetchPatAlignedPad;
       int cx = pat_col(st, x, kind);

@@ -237,6 +237,8 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     v.pixel_ops = reinterpret_cast<unsigned long long*>(v.work_counter + 16);
     v.rs_count = L.take<uint32_t>(nc + 1);
     v.rs_base = L.take<uint32_t>(nc + 1);
+    v.rb_count = L.take<uint32_t>(nc + 1);
+    v.rb_base = L.take<uint32_t>(nc + 1);
     scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, fr.rows + 1)));
     return staged_end;
   };
@@ -386,6 +388,8 @@ int Runtime::enqueue_count_half(cudaStream_t st) {
   k += launch_total(f.row_counts, f.row_offsets, f.num_rows, f.totals + 3, st);
   k += exclusive_scan(f.rs_count, f.rs_base, f.num_cmds, scan_tmp, st);
   k += launch_total(f.rs_count, f.rs_base, f.num_cmds, f.totals + 4, st);
+  k += exclusive_scan(f.rb_count, f.rb_base, f.num_cmds, scan_tmp, st);
+  k += launch_total(f.rb_count, f.rb_base, f.num_cmds, f.totals + 6, st);
   return k;
 }
 
@@ -430,6 +434,7 @@ static void plan_dynamic(Layout& L, FrameView& v, const FrameTotals& t) {
   v.num_cmdrows = t.cmdrows;
   v.num_seglist = t.seglist;
   v.num_row_states = t.row_states;
+  v.num_row_runs = t.row_runs;
 }
 
 BLGpuResult Runtime::download() {
@@ -481,6 +486,7 @@ BLGpuResult Runtime::run(const Frame& fr) {
   totals.cmdrows = host_totals[2];
   totals.row_entries = host_totals[3];
   totals.row_states = host_totals[4];
+  totals.row_runs = host_totals[6];
 
   // Dynamic buffers.
   Layout measure;
@@ -567,6 +573,8 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     v.pixel_ops = reinterpret_cast<unsigned long long*>(v.work_counter + 16);
     v.rs_count = L.take<uint32_t>(nc + 1);
     v.rs_base = L.take<uint32_t>(nc + 1);
+    v.rb_count = L.take<uint32_t>(nc + 1);
+    v.rb_base = L.take<uint32_t>(nc + 1);
     a_scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, fr.rows + 1)));
   };
   Layout L;
@@ -632,6 +640,7 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     t.cmdrows = host_totals[2];
     t.row_entries = host_totals[3];
     t.row_states = host_totals[4];
+    t.row_runs = host_totals[6];
     if (t.segs > view.seg_capacity) { r = BLGPU_ERROR_DATA_TOO_LARGE; break; }
     Layout D;
     D.base = static_cast<char*>(arena);

@@ -123,7 +123,7 @@ struct Frame {
 
 // Sizes produced by the counting half of the pipeline, cached for replay.
 struct FrameTotals {
-  uint32_t segs = 0, seglist = 0, cmdrows = 0, row_entries = 0, row_states = 0;
+  uint32_t segs = 0, seglist = 0, cmdrows = 0, row_entries = 0, row_states = 0, row_runs = 0;
 };
 
 constexpr int kCounterWords = 48;
