@@ -81,6 +81,7 @@ struct alignas(16) DevStyle {
   int32_t af_ox, af_oy, af_rx, af_ry;
   int32_t af_minx, af_miny, af_maxx, af_maxy;
   int32_t af_corx, af_cory, af_tw, af_th;
+  int32_t af_tw_m, af_tw_s, af_th_m, af_th_s;   // div_magic of af_tw / af_th (divmagic.h)
 };
 
 struct alignas(16) DevXform {

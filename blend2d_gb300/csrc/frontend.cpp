@@ -1,6 +1,7 @@
 // frontend.cpp - host front end: fetch-data setup and numeric helpers (see frontend.h).
 // Compiled with -ffp-contract=off: every expression is evaluated unfused, in source order.
 #include "frontend.h"
+#include "divmagic.h"
 
 #include <math.h>
 #include <string.h>
@@ -430,6 +431,8 @@ static bool pattern_affine(DevStyle& d, uint32_t extend, uint32_t quality, const
   }
   d.af_rx = rx; d.af_ry = ry; d.af_ox = ox; d.af_oy = oy;
   d.af_tw = int32_t(tw_d); d.af_th = int32_t(th_d);
+  const DivMagic mw = div_magic(d.af_tw), mh = div_magic(d.af_th);
+  d.af_tw_m = mw.m; d.af_tw_s = mw.s; d.af_th_m = mh.m; d.af_th_s = mh.s;
   return true;
 }
 

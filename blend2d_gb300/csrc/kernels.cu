@@ -962,6 +962,52 @@ __global__ void __launch_bounds__(kFineThreads, 4) fine_kernel(FrameView f) {
               }
             }
           }
+          else if (st.fetch == kFetchPatAffineNN || st.fetch == kFetchPatAffineBI) {
+            // affine patterns two pixels at a time, so their texel loads are in flight together
+            // (the arithmetic is px::fetch's, unchanged)
+            const bool bi = st.fetch == kFetchPatAffineBI;
+            const uint32_t* img = f.images + st.src_offset;
+#pragma unroll
+            for (int k0 = 0; k0 < 4; k0 += 2) {
+              uint32_t tex[2][4], wxs[2], wys[2];
+              bool on[2];
+#pragma unroll
+              for (int h = 0; h < 2; h++) {
+                const int k = k0 + h;
+                on[h] = m[k] && xp + k < cv.w;
+                uint64_t pxv, pyv;
+                px::af_normalize(st, rs.a64 + st.af_xx * uint64_t(uint32_t(xp + k)),
+                                 rs.b64 + st.af_xy * uint64_t(uint32_t(xp + k)), pxv, pyv);
+                uint32_t x0, y0, x1, y1;
+                px::af_index(st, pxv, pyv, 0, x0, y0);
+                px::af_index(st, pxv, pyv, 1, x1, y1);
+                wxs[h] = uint32_t(pxv & 0xFFFFFFFFu) >> 24;
+                wys[h] = uint32_t(pyv & 0xFFFFFFFFu) >> 24;
+                const uint32_t* l0 = img + int64_t(y0) * st.src_stride;
+                const uint32_t* l1 = img + int64_t(y1) * st.src_stride;
+                tex[h][0] = on[h] ? __ldg(l0 + x0) : 0u;
+                tex[h][1] = on[h] && bi ? __ldg(l1 + x0) : 0u;
+                tex[h][2] = on[h] && bi ? __ldg(l0 + x1) : 0u;
+                tex[h][3] = on[h] && bi ? __ldg(l1 + x1) : 0u;
+              }
+#pragma unroll
+              for (int h = 0; h < 2; h++) {
+                const int k = k0 + h;
+                if (!on[h]) continue;
+                uint32_t sv = tex[h][0];
+                if (bi) {
+                  const uint32_t wx = wxs[h], wy = wys[h], ix = 256 - wx, iy = 256 - wy;
+                  uint64_t p0 = px::unpack(tex[h][0]) * iy + px::unpack(tex[h][1]) * wy;
+                  uint64_t p1 = px::unpack(tex[h][2]) * iy + px::unpack(tex[h][3]) * wy;
+                  p0 = px::div256(p0) * ix;
+                  p1 = px::div256(p1) * wx;
+                  sv = px::pack(px::div256(p0 + p1));
+                }
+                pix[k] = px::composite(pix[k], sv, m[k], src_copy);
+                n++;
+              }
+            }
+          }
           else {
             // one copy of the fetch + composite code: the 4 pixels rotate through slot 0
 #pragma unroll 1

@@ -12,6 +12,7 @@
 #pragma once
 
 #include "blgpu_internal.h"
+#include "divmagic.h"
 
 namespace blgpu {
 namespace px {
@@ -97,8 +98,8 @@ __device__ __forceinline__ int pat_col(const DevStyle& st, int x, uint32_t kind)
 }
 
 __device__ __forceinline__ void af_normalize(const DevStyle& s, uint64_t vx, uint64_t vy, uint64_t& ox, uint64_t& oy) {
-  uint32_t x = uint32_t(int32_t(vx >> 32) % s.af_tw);
-  uint32_t y = uint32_t(int32_t(vy >> 32) % s.af_th);
+  uint32_t x = uint32_t(smod_magic(int32_t(vx >> 32), s.af_tw, DivMagic{s.af_tw_m, s.af_tw_s}));
+  uint32_t y = uint32_t(smod_magic(int32_t(vy >> 32), s.af_th, DivMagic{s.af_th_m, s.af_th_s}));
   if (int32_t(x) < 0) x += uint32_t(s.af_rx);
   if (int32_t(y) < 0) y += uint32_t(s.af_ry);
   if (int32_t(x) > s.af_ox) x -= uint32_t(s.af_rx);
