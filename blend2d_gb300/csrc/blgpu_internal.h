@@ -213,6 +213,8 @@ struct FrameView {
   uint32_t* row_counts;        // [num_rows + 1]
   uint32_t* row_offsets;
   uint32_t* row_cmds;          // command indices grouped by tile row, painter's order
+  uint32_t* row_copies;        // [num_rows] SrcCopy commands in each tile row's list
+  uint32_t* strip_start;       // [num_tiles * strips per tile] first list entry the composite needs (occlusion)
   uint32_t* tile_order;        // tile processing order for the persistent fine kernel
   uint32_t* tile_canvas;       // canvas index per global tile
   uint32_t* work_counter;      // [0] fine work queue, [1] items, [2] cubics, [3] their queue, [21] quads, [22] their queue

@@ -669,18 +669,23 @@ __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
   const DevCanvas cv = f.canvases[row_canvas[row]];
   uint32_t r = row - cv.row_base;
   uint32_t out = f.row_offsets[row];
+  uint32_t copies = 0;
   for (uint32_t base = 0; base < cv.cmd_count; base += blockDim.x) {
     uint32_t c = cv.cmd_first + base + threadIdx.x;
     uint32_t flag = 0;
     if (base + threadIdx.x < cv.cmd_count) {
       uint32_t ty = f.cmd_tile_y[c];
       flag = (ty != 0xFFFFFFFFu && (ty & 0xFFFFu) <= r && (ty >> 16) >= r) ? 1u : 0u;
+      copies += flag & f.cmds[c].flags;               // bit 0: SrcCopy
     }
     uint32_t total;
     uint32_t pos = block_exclusive_scan(flag, smem, total);
     if (flag) f.row_cmds[out + pos] = c;
     out += total;
   }
+  uint32_t total_copies;
+  block_exclusive_scan(copies, smem, total_copies);
+  if (threadIdx.x == 0) f.row_copies[row] = total_copies;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -810,6 +815,116 @@ __global__ void __launch_bounds__(4 * K) coverage_kernel(FrameView f) {
 // lane from the coverage pass, box fills compute theirs, then fetch + SrcOver/SrcCopy.
 // ---------------------------------------------------------------------------------------------
 
+// The lane's 4 masks of command `ci` in its strip: analytic commands from the slot's masks (or the
+// backdrop alone when no segment reaches the slot: `mw` is then the row's backdrop), boxes from
+// their rectangles.
+__device__ __forceinline__ void strip_masks(const FrameView& f, uint32_t ckind, uint32_t ci, uint32_t cmeta,
+                                            uint32_t cnseg, uint32_t mw, int xp, int y, uint32_t m[4]) {
+  const uint32_t alpha = cmeta & 0xFFFFu;
+  if (ckind == kFillAnalytic) {
+    if (cnseg) {
+      m[0] = mw & 0xFFu; m[1] = (mw >> 8) & 0xFFu; m[2] = (mw >> 16) & 0xFFu; m[3] = mw >> 24;
+    }
+    else {
+      // no segment reaches this slot: every pixel of a row has the row's carried-in coverage
+      const uint32_t rule = ((cmeta >> 16) & 2u) ? 0x1FFu : 0xFFFFFFFFu;
+      m[0] = px::calc_mask((256u << 9) + mw, rule, alpha);
+      m[1] = m[2] = m[3] = m[0];
+    }
+  }
+  else {
+    const DevCmd& cmd = f.cmds[ci];
+    if (ckind == kFillBoxA) {
+      bool in_y = y >= cmd.box[1] && y < cmd.box[3];
+#pragma unroll
+      for (int k = 0; k < 4; k++) m[k] = (in_y && xp + k >= cmd.box[0] && xp + k < cmd.box[2]) ? alpha : 0u;
+    }
+    else {
+#pragma unroll
+      for (int k = 0; k < 4; k++) m[k] = px::box_u_mask(cmd.box, alpha, xp + k, y);
+    }
+  }
+}
+
+// Slot of analytic command c in strip row `strip_row`, tile column tx, and its mask index + 1
+// (0: no segment reaches it).
+__device__ __forceinline__ uint32_t strip_slot(const FrameView& f, uint32_t c, uint32_t strip_row, int tx, uint32_t& nseg) {
+  const uint32_t ctx = f.cmd_tile_x[c];
+  const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
+  const uint32_t slot = f.cmdrow_base[c] + (strip_row - ((f.cmd_yr[c] & 0xFFFFu) >> kStripShift)) * ntx + (uint32_t(tx) - (ctx & 0xFFFFu));
+  nseg = f.slot_mask[slot];
+  return slot;
+}
+
+// Occlusion, per strip: a SrcCopy command whose mask is 255 on every pixel of the strip writes its
+// source there whatever is below (CompOp_SrcCopy with m = 255 gives the source exactly), so the
+// composite pass can start at the last such command of the strip's list. Looked for from the end
+// of the list, in rows with SrcCopy commands besides a first clear; 0 elsewhere.
+__global__ void __launch_bounds__(kFineThreads) cull_kernel(FrameView f) {
+  const int lane = threadIdx.x & 31;
+  const int prow = lane >> 3;
+  const int pcol = (lane & 7) * 4;
+  const uint32_t num_units = f.num_tiles * kStripsPerTile;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t unit = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); unit < num_units; unit += warps) {
+    const uint32_t tile = f.tile_order[unit / kStripsPerTile];
+    const int strip = int(unit % kStripsPerTile);
+    const DevCanvas cv = f.canvases[f.tile_canvas[tile]];
+    const uint32_t local = tile - cv.tile_base;
+    const int tx = int(local % uint32_t(cv.tiles_x)), ty = int(local / uint32_t(cv.tiles_x));
+    const int x_base = tx * kTileW;
+    const int row0 = ty * kTileH + strip * kStripRows;
+    const uint32_t row_id = cv.row_base + uint32_t(ty);
+    if (row0 >= cv.h || f.row_copies[row_id] < 2) {
+      if (lane == 0) f.strip_start[unit] = 0;
+      continue;
+    }
+    const uint32_t strip_row = uint32_t(row0) >> kStripShift;
+    const int row1 = min(row0 + kStripRows, cv.h) - 1;
+    const int y = row0 + prow, xp = x_base + pcol;
+    const bool row_ok = y < cv.h;
+    const uint32_t list_first = f.row_offsets[row_id];
+    const uint32_t list_count = f.row_counts[row_id];
+    const uint32_t strip_y = uint32_t(row0) | (uint32_t(row1) << 16);
+    const uint32_t strip_x = uint32_t(x_base) | (uint32_t(min(x_base + kTileW, cv.w) - 1) << 16);
+    uint32_t start = 0;
+    for (int cb = int((list_count - 1u) & ~31u); cb >= 0; cb -= 32) {
+      uint32_t c = 0;
+      bool cand = false;
+      if (uint32_t(cb + lane) < list_count) {
+        c = f.row_cmds[list_first + uint32_t(cb + lane)];
+        const uint32_t bx = f.cmd_xr[c], by = f.cmd_yr[c];
+        cand = (bx & 0xFFFFu) <= (strip_x & 0xFFFFu) && (bx >> 16) >= (strip_x >> 16) &&
+               (by & 0xFFFFu) <= (strip_y & 0xFFFFu) && (by >> 16) >= (strip_y >> 16) &&
+               (f.cmds[c].flags & 1u) && f.cmds[c].alpha == 255u;
+      }
+      uint32_t todo = __ballot_sync(0xFFFFFFFFu, cand);
+      bool found = false;
+      while (todo) {
+        const int bit = 31 - __clz(todo);
+        todo &= ~(1u << bit);
+        const uint32_t ci = __shfl_sync(0xFFFFFFFFu, c, bit);
+        const uint32_t ckind = f.cmds[ci].kind;
+        const uint32_t cmeta = (f.cmds[ci].flags << 16) | f.cmds[ci].alpha;
+        uint32_t cnseg = 0, mw = 0;
+        if (ckind == kFillAnalytic) {
+          const uint32_t slot = strip_slot(f, ci, strip_row, tx, cnseg);
+          mw = cnseg ? reinterpret_cast<const uint32_t*>(f.masks + size_t(cnseg - 1u) * kSlotPixels)[lane]
+                     : f.backdrop[size_t(slot) * kStripRows + prow];
+        }
+        uint32_t m[4];
+        strip_masks(f, ckind, ci, cmeta, cnseg, mw, xp, y, m);
+        bool full = true;
+#pragma unroll
+        for (int k = 0; k < 4; k++) full &= !(row_ok && xp + k < cv.w) || m[k] == 255u;
+        if (__all_sync(0xFFFFFFFFu, full)) { start = uint32_t(cb + bit); found = true; break; }
+      }
+      if (found) break;
+    }
+    if (lane == 0) f.strip_start[unit] = start;
+  }
+}
+
 __global__ void __launch_bounds__(kFineThreads, 4) fine_kernel(FrameView f) {
   const int lane = threadIdx.x & 31;
   const int prow = lane >> 3;            // row within the strip
@@ -853,11 +968,13 @@ __global__ void __launch_bounds__(kFineThreads, 4) fine_kernel(FrameView f) {
     const uint32_t strip_y = uint32_t(row0) | (uint32_t(row1) << 16);
     const uint32_t strip_x = uint32_t(x_base) | (uint32_t(min(x_base + kTileW, cv.w) - 1) << 16);
 
-    for (uint32_t base = 0; base < list_count; base += 32) {
+    const uint32_t start = f.strip_start[unit];      // cull_kernel
+
+    for (uint32_t base = start & ~31u; base < list_count; base += 32) {
       // commands of this chunk whose pixel bbox overlaps the strip, in painter's order
       uint32_t c = 0;
       bool hit = false;
-      if (base + lane < list_count) {
+      if (base + lane < list_count && base + lane >= start) {
         c = f.row_cmds[list_first + base + lane];
         uint32_t bx = f.cmd_xr[c], by = f.cmd_yr[c];
         hit = (bx & 0xFFFFu) <= (strip_x >> 16) && (bx >> 16) >= (strip_x & 0xFFFFu) &&
@@ -872,12 +989,7 @@ __global__ void __launch_bounds__(kFineThreads, 4) fine_kernel(FrameView f) {
         const DevCmd& hc = f.cmds[c];
         kind = hc.kind;
         meta = (hc.flags << 16) | hc.alpha;
-        if (kind == kFillAnalytic) {
-          const uint32_t ctx = f.cmd_tile_x[c];
-          const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
-          slot = f.cmdrow_base[c] + (strip_row - ((f.cmd_yr[c] & 0xFFFFu) >> kStripShift)) * ntx + (uint32_t(tx) - (ctx & 0xFFFFu));
-          nseg = f.slot_mask[slot];                    // 1 + mask index, 0 = no segment reaches the slot
-        }
+        if (kind == kFillAnalytic) slot = strip_slot(f, c, strip_row, tx, nseg);
       }
       uint32_t todo = ballot;
       // the first command's mask word, then each next one's while the current one composites
@@ -904,31 +1016,8 @@ __global__ void __launch_bounds__(kFineThreads, 4) fine_kernel(FrameView f) {
                          : f.backdrop[size_t(s1) * kStripRows + prow];
           bit = nb;
         }
-        const uint32_t alpha = cmeta & 0xFFFFu;
         uint32_t m[4];
-        if (ckind == kFillAnalytic) {
-          if (cnseg) {
-            m[0] = mw & 0xFFu; m[1] = (mw >> 8) & 0xFFu; m[2] = (mw >> 16) & 0xFFu; m[3] = mw >> 24;
-          }
-          else {
-            // no segment reaches this slot: every pixel of a row has the row's carried-in coverage
-            const uint32_t rule = ((cmeta >> 16) & 2u) ? 0x1FFu : 0xFFFFFFFFu;
-            m[0] = px::calc_mask((256u << 9) + mw, rule, alpha);
-            m[1] = m[2] = m[3] = m[0];
-          }
-        }
-        else {
-          const DevCmd& cmd = f.cmds[ci];
-          if (ckind == kFillBoxA) {
-            bool in_y = y >= cmd.box[1] && y < cmd.box[3];
-#pragma unroll
-            for (int k = 0; k < 4; k++) m[k] = (in_y && xp + k >= cmd.box[0] && xp + k < cmd.box[2]) ? alpha : 0u;
-          }
-          else {
-#pragma unroll
-            for (int k = 0; k < 4; k++) m[k] = px::box_u_mask(cmd.box, alpha, xp + k, y);
-          }
-        }
+        strip_masks(f, ckind, ci, cmeta, cnseg, mw, xp, y, m);
 
         if (row_ok && (m[0] | m[1] | m[2] | m[3])) {
           const DevCmd& cmd = f.cmds[ci];
@@ -958,52 +1047,6 @@ __global__ void __launch_bounds__(kFineThreads, 4) fine_kernel(FrameView f) {
             for (int k = 0; k < 4; k++) {
               if (m[k] && xp + k < cv.w) {
                 pix[k] = px::composite(pix[k], sv[k], m[k], src_copy);
-                n++;
-              }
-            }
-          }
-          else if (st.fetch == kFetchPatAffineNN || st.fetch == kFetchPatAffineBI) {
-            // affine patterns two pixels at a time, so their texel loads are in flight together
-            // (the arithmetic is px::fetch's, unchanged)
-            const bool bi = st.fetch == kFetchPatAffineBI;
-            const uint32_t* img = f.images + st.src_offset;
-#pragma unroll
-            for (int k0 = 0; k0 < 4; k0 += 2) {
-              uint32_t tex[2][4], wxs[2], wys[2];
-              bool on[2];
-#pragma unroll
-              for (int h = 0; h < 2; h++) {
-                const int k = k0 + h;
-                on[h] = m[k] && xp + k < cv.w;
-                uint64_t pxv, pyv;
-                px::af_normalize(st, rs.a64 + st.af_xx * uint64_t(uint32_t(xp + k)),
-                                 rs.b64 + st.af_xy * uint64_t(uint32_t(xp + k)), pxv, pyv);
-                uint32_t x0, y0, x1, y1;
-                px::af_index(st, pxv, pyv, 0, x0, y0);
-                px::af_index(st, pxv, pyv, 1, x1, y1);
-                wxs[h] = uint32_t(pxv & 0xFFFFFFFFu) >> 24;
-                wys[h] = uint32_t(pyv & 0xFFFFFFFFu) >> 24;
-                const uint32_t* l0 = img + int64_t(y0) * st.src_stride;
-                const uint32_t* l1 = img + int64_t(y1) * st.src_stride;
-                tex[h][0] = on[h] ? __ldg(l0 + x0) : 0u;
-                tex[h][1] = on[h] && bi ? __ldg(l1 + x0) : 0u;
-                tex[h][2] = on[h] && bi ? __ldg(l0 + x1) : 0u;
-                tex[h][3] = on[h] && bi ? __ldg(l1 + x1) : 0u;
-              }
-#pragma unroll
-              for (int h = 0; h < 2; h++) {
-                const int k = k0 + h;
-                if (!on[h]) continue;
-                uint32_t sv = tex[h][0];
-                if (bi) {
-                  const uint32_t wx = wxs[h], wy = wys[h], ix = 256 - wx, iy = 256 - wy;
-                  uint64_t p0 = px::unpack(tex[h][0]) * iy + px::unpack(tex[h][1]) * wy;
-                  uint64_t p1 = px::unpack(tex[h][2]) * iy + px::unpack(tex[h][3]) * wy;
-                  p0 = px::div256(p0) * ix;
-                  p1 = px::div256(p1) * wx;
-                  sv = px::pack(px::div256(p0 + p1));
-                }
-                pix[k] = px::composite(pix[k], sv, m[k], src_copy);
                 n++;
               }
             }
@@ -1267,8 +1310,9 @@ int launch_fine(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   int grid = fine_grid_size(cfg.fine_blocks_per_sm);
   uint32_t max_blocks = (f.num_tiles * kStripsPerTile + kFineWarps - 1) / kFineWarps;
   if (uint32_t(grid) > max_blocks) grid = int(max_blocks);
+  cull_kernel<<<grid, kFineThreads, 0, st>>>(f);
   fine_kernel<<<grid, kFineThreads, 0, st>>>(f);
-  return 1;
+  return 2;
 }
 
 }  // namespace blgpu

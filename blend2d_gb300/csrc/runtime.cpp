@@ -225,6 +225,8 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     v.cmdrow_base = L.take<uint32_t>(nc + 1);
     v.row_counts = L.take<uint32_t>(fr.rows + 1);
     v.row_offsets = L.take<uint32_t>(fr.rows + 1);
+    v.row_copies = L.take<uint32_t>(fr.rows + 1);
+    v.strip_start = L.take<uint32_t>((size_t(fr.tiles) + 1) * (kTileH / kStripRows));
     row_canvas = L.take<uint32_t>(fr.rows + 1);
     v.tile_order = L.take<uint32_t>(fr.tiles + 1);
     v.tile_canvas = L.take<uint32_t>(fr.tiles + 1);
@@ -564,6 +566,8 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     v.cmdrow_base = L.take<uint32_t>(nc + 1);
     v.row_counts = L.take<uint32_t>(fr.rows + 1);
     v.row_offsets = L.take<uint32_t>(fr.rows + 1);
+    v.row_copies = L.take<uint32_t>(fr.rows + 1);
+    v.strip_start = L.take<uint32_t>((size_t(fr.tiles) + 1) * (kTileH / kStripRows));
     a_row_canvas = L.take<uint32_t>(fr.rows + 1);
     v.tile_order = L.take<uint32_t>(fr.tiles + 1);
     v.tile_canvas = L.take<uint32_t>(fr.tiles + 1);
