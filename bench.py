@@ -60,8 +60,8 @@ def parse_args(argv=None):
     ap.add_argument("--mode", default="frame", choices=["frame", "batch", "serving"],
                     help="frame: one canvas per step (default); batch: many canvases in one pipeline vs one "
                          "pipeline per canvas; serving: Poisson arrivals through the continuous-batching server")
-    ap.add_argument("--batch-count", type=int, default=1024, help="canvases of the batched workload")
-    ap.add_argument("--batch-scale", type=float, default=0.02, help="path-count scale of the batched workload")
+    ap.add_argument("--batch-count", type=int, default=4096, help="canvases of the batched workload")
+    ap.add_argument("--batch-scale", type=float, default=1.0, help="path-count scale of the batched workload (1.0: 10-5000 paths per canvas)")
     ap.add_argument("--serve-requests", type=int, default=48, help="requests per arrival-rate point")
     ap.add_argument("--serve-scale", type=float, default=0.05, help="path-count scale of the serving requests")
     ap.add_argument("--serve-rates", default="20,60,200", help="arrival rates (requests/s) to sweep")

@@ -204,6 +204,7 @@ struct FrameView {
   uint32_t* slot_cmd;          // [num_cmdrows] command of each slot with segments
   uint32_t* slot_mask;         // [num_cmdrows + 1] 1 + index of the slot's masks, 0 = no segments
   uint32_t* mask_slot;         // [non-empty slots] slot of each compact mask index
+  uint4* mask_info;            // [non-empty slots] {x of the slot's first column, its first row, flags << 16 | alpha, slot}
   uint32_t* slot_first;        // [num_cmdrows + 1] first work item of each slot (exclusive scan of the counts)
   uint2* entries;              // coverage work items {segment, mask index}, grouped by slot in slot order
   uint32_t mask_capacity;      // slots the masks array holds

@@ -632,6 +632,14 @@ __global__ void slot_compact_kernel(FrameView f) {
     const uint32_t idx = f.cmdrow_offsets[i];
     f.slot_mask[i] = idx + 1u;
     f.mask_slot[idx] = i;
+    // what the coverage pass needs of the slot, gathered here where every slot is independent
+    const uint32_t c = f.slot_cmd[i];
+    const uint32_t ctx = f.cmd_tile_x[c];
+    const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
+    const uint32_t local = i - f.cmdrow_base[c];
+    const uint32_t sr = ((f.cmd_yr[c] & 0xFFFFu) >> kStripShift) + local / ntx;
+    f.mask_info[idx] = make_uint4(((ctx & 0xFFFFu) + local % ntx) << kTileShift, sr << kStripShift,
+                                  (f.cmds[c].flags << 16) | f.cmds[c].alpha, i);
   }
   else {
     f.slot_mask[i] = 0u;
@@ -728,14 +736,10 @@ __global__ void __launch_bounds__(4 * K) coverage_kernel(FrameView f) {
     const uint32_t m0 = grp * K;
     const int nk = int(min(uint32_t(K), num_masks - m0));
     if (tid < nk) {
-      const uint32_t slot = f.mask_slot[m0 + tid];
-      const uint32_t c = f.slot_cmd[slot];
-      const uint32_t ctx = f.cmd_tile_x[c];
-      const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
-      const uint32_t local = slot - f.cmdrow_base[c];
-      const uint32_t sr = ((f.cmd_yr[c] & 0xFFFFu) >> kStripShift) + local / ntx;
-      org[tid] = make_int2(int(((ctx & 0xFFFFu) + local % ntx) << kTileShift), int(sr << kStripShift));
-      meta[tid] = (f.cmds[c].flags << 16) | f.cmds[c].alpha;
+      const uint4 info = f.mask_info[m0 + tid];
+      const uint32_t slot = info.w;
+      org[tid] = make_int2(int(info.x), int(info.y));
+      meta[tid] = info.z;
       const uint4 b4 = *reinterpret_cast<const uint4*>(f.backdrop + size_t(slot) * kStripRows);
       bd[tid][0] = b4.x; bd[tid][1] = b4.y; bd[tid][2] = b4.z; bd[tid][3] = b4.w;
     }
