@@ -357,7 +357,7 @@ def run_ours(args) -> int:
                 "frames_in_flight": 2, "one_at_a_time_ms_per_step": round(e2e_seq_s * 1e3 / args.steps, 3)},
         "gpu_launches": launches,
         "clocks": clock_info,
-        "roofline": {"bound": "hbm", "kernel": "fine stage (coverage: raster_kernel + sweep_kernel; composite: fine_kernel)",
+        "roofline": {"bound": "hbm", "kernel": "fine stage (coverage: coverage_kernel; composite: cull_kernel + fine_kernel)",
                      "achieved": round(achieved, 2), "peak": peak,
                      "peak_kind": f"of {peak_kind}", "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": traffic, "traffic_source": traffic_src,
