@@ -171,6 +171,16 @@ __device__ __forceinline__ void strip_tile_range(const DevSeg& g, int r, int& t0
 }
 #endif
 
+// One monotonic piece of a curve, split off by curve_split_kernel and flattened by
+// edge_pieces_kernel: its DEG + 1 points (transformed, 24.8 scale), its command and its curve's
+// clip flags (0: the curve lies inside the clip box).
+struct alignas(16) DevPiece {
+  double2 p[4];
+  uint32_t cmd;
+  uint32_t any;
+  uint32_t pad[2];
+};
+
 // Device-side view of a frame (pointers into one device arena).
 struct FrameView {
   const DevCmd* cmds;
@@ -188,6 +198,8 @@ struct FrameView {
   // K1
   DevItem* items;              // lines and curves of every analytic command (any order)
   DevItem* curve_items;        // cubic curves from the front, quadratic / conic curves from the back
+  DevPiece* pieces;            // their monotonic pieces, cubic from the front, quadratic from the back
+  uint32_t piece_capacity;
   int4* cmd_bbox;              // [num_cmds] 24.8 bbox of the emitted segments: xmin, ymin, xmax, ymax
   DevSeg* segs;                // emitted segments (any order)
   uint32_t* seg_meta;          // cmd << 1 | sign
@@ -218,7 +230,8 @@ struct FrameView {
   uint32_t* strip_start;       // [num_tiles * strips per tile] first list entry the composite needs (occlusion)
   uint32_t* tile_order;        // tile processing order for the persistent fine kernel
   uint32_t* tile_canvas;       // canvas index per global tile
-  uint32_t* work_counter;      // [0] fine work queue, [1] items, [2] cubics, [3] their queue, [21] quads, [22] their queue
+  uint32_t* work_counter;      // [0] fine work queue, [1] items, [2] cubics, [3] their queue, [21] quads, [22] their queue,
+                               //   [23] cubic pieces, [24] their queue, [25] quadratic pieces, [26] their queue
   uint32_t* totals;            // [8] segments, seglist bound, (cmd,strip) slots, row entries, gradient rows,
                                //   slots with segments, conic row runs
   uint32_t* rs_count;          // [num_cmds + 1] gradient row states per command (radial/conic styles)

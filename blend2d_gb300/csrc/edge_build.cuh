@@ -1032,9 +1032,11 @@ struct LaneCurve {
   uint32_t any, sign, out;
   double y_start, y_end;
 
-  // curve_to for a source holding exactly this one curve: p0 (with its clip flags) and
-  // spline[1..DEG] set by the caller. Returns false when the curve has nothing to flatten.
-  __device__ __forceinline__ bool begin_curve(Builder& eb, Pt p0, uint32_t p0_flags) {
+  // curve_to for a source holding exactly this one curve, up to the flattening: p0 (with its clip
+  // flags) and spline[1..DEG] set by the caller. A curve entirely on one side of the clip box is
+  // done here; otherwise its monotonic pieces are left in spline[0..nout] (`any`: the curve's clip
+  // flags). Returns false when there is nothing to flatten.
+  __device__ __forceinline__ bool prepare(Builder& eb, Pt p0, uint32_t p0_flags) {
     mc.tol_sq = eb.tol_sq;
     uint32_t common = p0_flags, fl_any = p0_flags;
 #pragma unroll
@@ -1050,6 +1052,23 @@ struct LaneCurve {
     nout = DEG == 3 ? split_cubic(spline) : split_quad(spline);
     if (nout == 0) nout = DEG;
     any = fl_any;
+    return true;
+  }
+
+  // The whole curve: prepare, then the first piece with work.
+  __device__ __forceinline__ bool begin_curve(Builder& eb, Pt p0, uint32_t p0_flags) {
+    if (!prepare(eb, p0, p0_flags)) return false;
+    piece = 0;
+    return next_piece(eb, false);
+  }
+
+  // One monotonic piece prepared earlier (its DEG + 1 points and its curve's clip flags).
+  __device__ __forceinline__ bool begin_piece(Builder& eb, const Pt* pts, uint32_t any_flags) {
+    mc.tol_sq = eb.tol_sq;
+#pragma unroll
+    for (int i = 0; i <= DEG; i++) spline[i] = pts[i];
+    nout = DEG;
+    any = any_flags;
     piece = 0;
     return next_piece(eb, false);
   }

@@ -311,12 +311,8 @@ __global__ void classify_kernel(FrameView f) {
   });
 }
 
-// Curves (classify's curve list: cubics from the front, quadratic and conic curves from the
-// back), flattened per lane: every lane advances its own curve by one subdivision step per
-// iteration of a warp-wide loop (eb::LaneCurve) and takes the next curve from the list as soon as
-// its current one is done, so the lanes stay busy whatever the curves' subdivision depths and
-// clipping paths. Each curve is built by its own builder, as curve_to builds it
-// (edgebuilder_p.h:1618-2022) when the source holds just that curve.
+// The end of a curve's or piece's builder: border runs emitted, segments flushed, the command's
+// bbox, status and binning bound updated.
 __device__ __forceinline__ void finish_curve(FrameView& f, eb::Builder& b, uint32_t cmd, uint32_t& rows) {
   b.done();
   b.sink.flush();
@@ -332,25 +328,104 @@ __device__ __forceinline__ void finish_curve(FrameView& f, eb::Builder& b, uint3
 }
 
 // The lanes' subdivision stacks live in local memory with the top entry in registers
-// (eb::CachedStack): the kernel is bound by the FP64 pipe and the latency of its stack, and needs
-// every resident warp, so the stacks stay out of shared memory.
+// (eb::CachedStack): the piece kernel is bound by the FP64 pipe and the latency of its stack, and
+// needs every resident warp, so the stacks stay out of shared memory.
 constexpr int kCurveThreads = 128;
+constexpr int kPieceRefillLanes = 16;
 
+// Curves in two kernels. curve_split_kernel<DEG>: one thread per curve of the curve list does
+// curve_to's set-up (transform, clip flags, a curve entirely on one side of the clip box, the split
+// into monotonic pieces: the divergent, FP64-heavy part) with every lane converged on it, and
+// writes the pieces. edge_pieces_kernel<DEG> flattens the pieces lane-scheduled, so taking a new
+// piece is cheap and the lanes' subdivision steps stay together. A piece is built by its own
+// builder: the border runs a curve accumulates are vertical lines at the clip box's x0/x1 whose
+// cells add up the same whether the runs of consecutive pieces are merged or not.
 template<int DEG>
-__global__ void __launch_bounds__(kCurveThreads) edge_curves_kernel(FrameView f) {
+__global__ void __launch_bounds__(128) curve_split_kernel(FrameView f) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const uint32_t n_cubic = min(f.work_counter[2], f.item_capacity);
   const uint32_t n_items = DEG == 3 ? n_cubic : min(f.work_counter[21], f.item_capacity - n_cubic);
-  uint32_t* queue = f.work_counter + (DEG == 3 ? 3 : 22);
+  uint32_t rows = 0, npieces = 0, cmd_i = 0;
+  eb::Pt spline[DEG == 3 ? 25 : 7];
+  uint32_t any = 0;
+  if (t < n_items) {
+    const DevItem it = f.curve_items[DEG == 3 ? t : f.item_capacity - 1u - t];
+    const DevCmd& cmd = f.cmds[it.cmd];
+    const DevXform& xf = f.xforms[cmd.xform];
+    eb::Builder b;
+    init_builder(b, f.canvases[cmd.canvas]);
+    b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, it.cmd);
+    eb::Src src;
+    src.xy = f.verts + 2ull * cmd.geom_first;
+    src.affine = xf.affine != 0;
+    src.m00 = xf.m[0]; src.m01 = xf.m[1]; src.m10 = xf.m[2]; src.m11 = xf.m[3]; src.m20 = xf.m[4]; src.m21 = xf.m[5];
+    const eb::Pt p0 = src.tf(int(it.a));
+    spline[1] = src.tf(int(it.b));
+    if (DEG == 3) { spline[2] = src.tf(int(it.b) + 1); spline[DEG] = src.tf(int(it.b) + 2); }
+    else spline[DEG] = src.tf(int(it.b) + (it.kind == kItemConic ? 2 : 1));
+    cmd_i = it.cmd;
+    // curve_to's set-up (LaneCurve::prepare, restated on this thread's own spline)
+    const uint32_t p0_flags = b.fxy(p0);
+    uint32_t common = p0_flags;
+    any = p0_flags;
+#pragma unroll
+    for (int i = 1; i <= DEG; i++) { const uint32_t fl = b.fxy(spline[i]); common &= fl; any |= fl; }
+    if (common) {
+      if (!(common & (eb::CF_Y0 | eb::CF_Y1))) {
+        const double y0 = eb::dclamp(p0.y, b.cy0, b.cy1), y1 = eb::dclamp(spline[DEG].y, b.cy0, b.cy1);
+        if (common & eb::CF_X0) b.acc_left(y0, y1); else b.acc_right(y0, y1);
+      }
+      finish_curve(f, b, it.cmd, rows);
+    }
+    else {
+      spline[0] = p0;
+      int nout = DEG == 3 ? eb::split_cubic(spline) : eb::split_quad(spline);
+      if (nout == 0) nout = DEG;
+      npieces = uint32_t(nout / DEG);
+    }
+  }
+  // one atomic per warp for the pieces of its curves
+  uint32_t incl = npieces;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+  uint32_t base = 0;
+  if (lane == 31 && total) base = atomicAdd(f.work_counter + (DEG == 3 ? 23 : 25), total);
+  base = __shfl_sync(0xFFFFFFFFu, base, 31) + incl - npieces;
+  for (uint32_t k = 0; k < npieces; k++) {
+    const uint32_t idx = base + k;
+    if (idx >= f.piece_capacity) break;
+    DevPiece pc;
+#pragma unroll
+    for (int i = 0; i <= DEG; i++) pc.p[i] = make_double2(spline[k * DEG + i].x, spline[k * DEG + i].y);
+    pc.cmd = cmd_i;
+    pc.any = any;
+    f.pieces[DEG == 3 ? idx : f.piece_capacity - 1u - idx] = pc;
+  }
+  rows = __reduce_add_sync(0xFFFFFFFFu, rows);
+  if (lane == 0 && rows) atomicAdd(f.totals + 1, rows);
+}
+
+template<int DEG>
+__global__ void __launch_bounds__(kCurveThreads) edge_pieces_kernel(FrameView f) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t n_cubic = min(f.work_counter[23], f.piece_capacity);
+  const uint32_t n_items = DEG == 3 ? n_cubic : min(f.work_counter[25], f.piece_capacity - n_cubic);
+  uint32_t* queue = f.work_counter + (DEG == 3 ? 24 : 26);
   eb::Builder b;
   eb::LaneCurve<DEG, eb::CachedStack<DEG>> lc;
   bool busy = false, exhausted = false;
   uint32_t cur = 0, rows = 0;
 
   for (;;) {
-    // hand the next curves of the list to the idle lanes (one atomic per warp)
+    // hand the next pieces of the list to the idle lanes (one atomic per warp), once enough lanes
+    // are idle that the set-up's FP64 instructions serve several pieces at once
     const uint32_t want = __ballot_sync(0xFFFFFFFFu, !busy && !exhausted);
-    if (want) {
+    if (want && (__popc(want) >= kPieceRefillLanes || !__any_sync(0xFFFFFFFFu, busy))) {
       const int leader = __ffs(want) - 1;
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(queue, uint32_t(__popc(want)));
@@ -361,21 +436,14 @@ __global__ void __launch_bounds__(kCurveThreads) edge_curves_kernel(FrameView f)
           exhausted = true;
         }
         else {
-          const DevItem it = f.curve_items[DEG == 3 ? t : f.item_capacity - 1u - t];
-          const DevCmd& cmd = f.cmds[it.cmd];
-          const DevXform& xf = f.xforms[cmd.xform];
-          init_builder(b, f.canvases[cmd.canvas]);
-          b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, it.cmd);
-          eb::Src src;
-          src.xy = f.verts + 2ull * cmd.geom_first;
-          src.affine = xf.affine != 0;
-          src.m00 = xf.m[0]; src.m01 = xf.m[1]; src.m10 = xf.m[2]; src.m11 = xf.m[3]; src.m20 = xf.m[4]; src.m21 = xf.m[5];
-          const eb::Pt p0 = src.tf(int(it.a));
-          lc.spline[1] = src.tf(int(it.b));
-          if (DEG == 3) { lc.spline[2] = src.tf(int(it.b) + 1); lc.spline[DEG] = src.tf(int(it.b) + 2); }
-          else lc.spline[DEG] = src.tf(int(it.b) + (it.kind == kItemConic ? 2 : 1));
-          cur = it.cmd;
-          busy = lc.begin_curve(b, p0, b.fxy(p0));
+          const DevPiece pc = f.pieces[DEG == 3 ? t : f.piece_capacity - 1u - t];
+          cur = pc.cmd;
+          init_builder(b, f.canvases[f.cmds[cur].canvas]);
+          b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, cur);
+          eb::Pt pts[DEG + 1];
+#pragma unroll
+          for (int i = 0; i <= DEG; i++) pts[i] = eb::Pt{pc.p[i].x, pc.p[i].y};
+          busy = lc.begin_piece(b, pts, pc.any);
           if (!busy) finish_curve(f, b, cur, rows);
         }
       }
@@ -1231,18 +1299,22 @@ int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, edge_curves_kernel<3>, kCurveThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, edge_pieces_kernel<3>, kCurveThreads, 0);
     if (max_per_sm < 1) max_per_sm = 1;
   }
   const int per_sm = cfg.cubic_blocks_per_sm > 0 && cfg.cubic_blocks_per_sm < max_per_sm ? cfg.cubic_blocks_per_sm : max_per_sm;
   const uint32_t eb = cfg.edge_block == 64 || cfg.edge_block == 256 ? uint32_t(cfg.edge_block) : 128u;
   classify_kernel<<<cdiv(f.num_cmds, 128), 128, 0, st>>>(f);
   edge_items_kernel<<<cdiv(f.item_capacity ? f.item_capacity : 1, eb), eb, 0, st>>>(f);
-  uint32_t grid = cdiv(f.item_capacity ? f.item_capacity : 1, kCurveThreads);
-  uint32_t cubic_grid = uint32_t(sms * per_sm);
-  edge_curves_kernel<3><<<grid < cubic_grid ? grid : cubic_grid, kCurveThreads, 0, st>>>(f);
-  edge_curves_kernel<2><<<sms, kCurveThreads, 0, st>>>(f);
-  return 4;
+  const uint32_t cubic_grid = uint32_t(sms * per_sm);
+  const uint32_t split_grid = cdiv(f.item_capacity ? f.item_capacity : 1, 128);
+  curve_split_kernel<3><<<split_grid, 128, 0, st>>>(f);
+  curve_split_kernel<2><<<split_grid, 128, 0, st>>>(f);
+  const uint32_t pgrid = cdiv(f.piece_capacity ? f.piece_capacity : 1, kCurveThreads);
+  const uint32_t pieces_grid = pgrid < cubic_grid ? pgrid : cubic_grid;
+  edge_pieces_kernel<3><<<pieces_grid, kCurveThreads, 0, st>>>(f);
+  edge_pieces_kernel<2><<<pieces_grid, kCurveThreads, 0, st>>>(f);
+  return 6;
 }
 
 int launch_cmd_tiles(const FrameView& f, uint32_t* cmdrow_counts_per_cmd, cudaStream_t st) {

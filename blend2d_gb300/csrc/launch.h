@@ -15,7 +15,7 @@ struct LaunchConfig {
   int cover_blocks_per_sm = 0;    // coverage grid: blocks per SM (0 = as many as fit)
   int fine_blocks_per_sm = 0;     // composite grid: blocks per SM (0 = as many as fit)
   int edge_block = 128;           // threads per block of the per-item edge builder (64/128/256)
-  int cubic_blocks_per_sm = 0;    // lane-scheduled cubic flattener: blocks per SM
+  int cubic_blocks_per_sm = 3;    // lane-scheduled curve-piece flattener: blocks per SM (0 = as many as fit)
 };
 
 int exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* tmp, cudaStream_t st);

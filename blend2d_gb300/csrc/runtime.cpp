@@ -192,6 +192,8 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   // Items: at most one per vertex (a line or curve consumes at least one; a closing line takes
   // the place of the figure's move-to).
   const uint32_t item_capacity = uint32_t(std::min<size_t>(fr.verts.size() + 1, 0xFFFFFFF0u));
+  // a cubic (3 vertices) splits into at most 8 monotonic pieces, a quadratic (2) into at most 3
+  const uint32_t piece_capacity = uint32_t(std::min<size_t>(fr.verts.size() / 2 * 3 + 64, 0xFFFFFFF0u));
 
   // Plan: [staged inputs][luts][canvases][work arrays]
   auto plan = [&](Layout& L, FrameView& v, std::vector<uint32_t*>* cpix) -> size_t {
@@ -216,6 +218,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     }
     v.items = L.take<DevItem>(item_capacity);
     v.curve_items = L.take<DevItem>(item_capacity);
+    v.pieces = L.take<DevPiece>(piece_capacity);
     v.cmd_bbox = L.take<int4>(nc);
     v.cmd_tile_x = L.take<uint32_t>(nc);
     v.cmd_tile_y = L.take<uint32_t>(nc);
@@ -352,6 +355,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   v.seg_meta = reinterpret_cast<uint32_t*>(static_cast<char*>(seg_buf.ptr) + sizeof(DevSeg) * size_t(seg_capacity));
   v.seg_capacity = seg_capacity;
   v.item_capacity = item_capacity;
+  v.piece_capacity = piece_capacity;
   v.num_cmds = nc;
   v.num_canvases = ncv;
   v.num_tiles = fr.tiles;
@@ -539,6 +543,7 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
   BLGPU_CHECK(noalloc_arena(device, &arena));
   const uint32_t nc = uint32_t(fr.cmds.size());
   const uint32_t item_capacity = uint32_t(std::min<size_t>(fr.verts.size() / 2 + 1, 0xFFFFFFF0u));   // <= one per vertex
+  const uint32_t piece_capacity = uint32_t(std::min<size_t>(fr.verts.size() / 2 * 3 + 64, 0xFFFFFFF0u));
 
   FrameView v{};
   uint32_t* a_cmdrow_per_cmd = nullptr;
@@ -558,6 +563,7 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     v.luts = L.take<uint32_t>(fr.lut_words);
     v.items = L.take<DevItem>(item_capacity);
     v.curve_items = L.take<DevItem>(item_capacity);
+    v.pieces = L.take<DevPiece>(piece_capacity);
     v.cmd_bbox = L.take<int4>(nc);
     v.cmd_tile_x = L.take<uint32_t>(nc);
     v.cmd_tile_y = L.take<uint32_t>(nc);
@@ -594,6 +600,7 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
   v.seg_meta = reinterpret_cast<uint32_t*>(static_cast<char*>(arena) + fixed_end + sizeof(DevSeg) * size_t(v.seg_capacity));
   const size_t dyn_begin = fixed_end + seg_bytes;
   v.item_capacity = item_capacity;
+  v.piece_capacity = piece_capacity;
   v.num_cmds = nc;
   v.num_canvases = 1;
   v.num_tiles = fr.tiles;
