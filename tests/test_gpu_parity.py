@@ -346,3 +346,40 @@ def test_async_flush_pipelines_frames_with_the_same_pixels(runtimes):
     assert np.array_equal(host.numpy(), ref.numpy())
     for c in ctxs:
         c.close()
+
+
+def test_two_threads_record_and_flush_async(runtimes):
+    """Two host threads, a context each on one runtime, record and flush asynchronously at the same
+    time (the bench's e2e arm); every frame matches its synchronous render."""
+    import threading
+    import torch
+    rt = runtimes()
+    streams = [scenes.random_mix(seed, width=173, height=141, count=250).to_bytes() for seed in range(3300, 3308)]
+    want = [bg.render_stream(rt, s) for s in streams]
+    results, errors = {}, []
+
+    def worker(k):
+        try:
+            ctx = bg.Context(rt)
+            hosts = [torch.zeros((141, 173), dtype=torch.int32).pin_memory() for _ in range(2)]
+            for rep in range(3):
+                for j, i in enumerate(range(k, len(streams), 2)):
+                    host = hosts[j % 2]
+                    ctx.begin(host)
+                    ctx.submit_stream(streams[i])
+                    ctx.flush(bg.FLUSH_ASYNC)
+                    ctx.end()
+                    results[(rep, i)] = host.numpy().view(np.uint32).copy()
+            ctx.close()
+        except Exception as e:
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(k,)) for k in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    assert len(results) == 3 * len(streams)
+    for (rep, i), img in results.items():
+        assert not _diff(img, want[i]), (rep, i, _diff(img, want[i]))
