@@ -1292,16 +1292,28 @@ int launch_lut(const FrameView& f, cudaStream_t st) {
   return 1;
 }
 
+// Device properties the launch shapes depend on, queried once (thread-safe static
+// initialization: the runtime's two pipeline lanes launch from two threads).
+static int device_sms() {
+  static const int v = [] {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+  }();
+  return v;
+}
+template<typename K>
+static int max_blocks_per_sm(K kernel, int threads) {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, 0);
+  return n > 0 ? n : 1;
+}
+
 int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   if (!f.num_cmds) return 0;
-  static int sms = 0, max_per_sm = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, edge_pieces_kernel<3>, kCurveThreads, 0);
-    if (max_per_sm < 1) max_per_sm = 1;
-  }
+  const int sms = device_sms();
+  static const int max_per_sm = max_blocks_per_sm(edge_pieces_kernel<3>, kCurveThreads);
   const int per_sm = cfg.cubic_blocks_per_sm > 0 && cfg.cubic_blocks_per_sm < max_per_sm ? cfg.cubic_blocks_per_sm : max_per_sm;
   const uint32_t eb = cfg.edge_block == 64 || cfg.edge_block == 256 ? uint32_t(cfg.edge_block) : 128u;
   classify_kernel<<<cdiv(f.num_cmds, 128), 128, 0, st>>>(f);
@@ -1338,14 +1350,8 @@ int launch_rows_and_tiles(const FrameView& f, uint32_t* row_canvas, cudaStream_t
 }
 
 int fine_grid_size(int blocks_per_sm) {
-  static int sms = 0, max_per_sm = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, fine_kernel, kFineThreads, 0);
-    if (max_per_sm < 1) max_per_sm = 1;
-  }
+  const int sms = device_sms();
+  static const int max_per_sm = max_blocks_per_sm(fine_kernel, kFineThreads);
   return sms * (blocks_per_sm > 0 && blocks_per_sm < max_per_sm ? blocks_per_sm : max_per_sm);
 }
 
@@ -1353,12 +1359,7 @@ int fine_grid_size(int blocks_per_sm) {
 // rasterize and sweep. Called after the binning count pass and the backdrop prefix.
 int launch_coverage(const FrameView& f, const LaunchConfig& cfg, uint32_t* scan_tmp, cudaStream_t st) {
   if (!f.num_cmdrows) return 0;
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  }
+  const int sms = device_sms();
   int k = 0;
   slot_flags_kernel<<<cdiv(f.num_cmdrows, 256), 256, 0, st>>>(f); k++;
   k += exclusive_scan(f.cmdrow_offsets, f.cmdrow_offsets, f.num_cmdrows, scan_tmp, st);
