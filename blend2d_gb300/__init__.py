@@ -74,7 +74,8 @@ class Pattern(ctypes.Structure):
 class LaunchConfig(ctypes.Structure):
     _fields_ = [("cover_slots", ctypes.c_int32), ("cover_blocks_per_sm", ctypes.c_int32),
                 ("fine_blocks_per_sm", ctypes.c_int32), ("edge_block", ctypes.c_int32),
-                ("cubic_blocks_per_sm", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("cubic_blocks_per_sm", ctypes.c_int32), ("no_occlusion_cull", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}

@@ -1367,8 +1367,11 @@ int launch_coverage(const FrameView& f, const LaunchConfig& cfg, uint32_t* scan_
   k += exclusive_scan(f.cmdrow_counts, f.slot_first, f.num_cmdrows + 1, scan_tmp, st);
   k += launch_seg_bin(f, 1, st);
   const int per_sm = cfg.cover_blocks_per_sm > 0 ? cfg.cover_blocks_per_sm : 16;
-  if (cfg.cover_slots == 16) coverage_kernel<16><<<sms * per_sm, 64, 0, st>>>(f);
-  else if (cfg.cover_slots == 64) coverage_kernel<64><<<sms * per_sm, 256, 0, st>>>(f);
+  // by frame: scenes of long edges (many strip rows per segment) have few work items per slot,
+  // where smaller groups keep more of them in flight per SM
+  const int slots = cfg.cover_slots ? cfg.cover_slots : (f.num_seglist > 16u * f.num_segs ? 32 : 64);
+  if (slots == 16) coverage_kernel<16><<<sms * per_sm, 64, 0, st>>>(f);
+  else if (slots == 64) coverage_kernel<64><<<sms * per_sm, 256, 0, st>>>(f);
   else coverage_kernel<32><<<sms * per_sm, 128, 0, st>>>(f);
   return k + 1;
 }
@@ -1387,9 +1390,14 @@ int launch_fine(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   int grid = fine_grid_size(cfg.fine_blocks_per_sm);
   uint32_t max_blocks = (f.num_tiles * kStripsPerTile + kFineWarps - 1) / kFineWarps;
   if (uint32_t(grid) > max_blocks) grid = int(max_blocks);
-  cull_kernel<<<grid, kFineThreads, 0, st>>>(f);
+  if (cfg.no_occlusion_cull) {
+    cudaMemsetAsync(f.strip_start, 0, sizeof(uint32_t) * size_t(f.num_tiles) * kStripsPerTile, st);
+  }
+  else {
+    cull_kernel<<<grid, kFineThreads, 0, st>>>(f);
+  }
   fine_kernel<<<grid, kFineThreads, 0, st>>>(f);
-  return 2;
+  return cfg.no_occlusion_cull ? 1 : 2;
 }
 
 }  // namespace blgpu

@@ -11,11 +11,12 @@ namespace blgpu {
 
 // Launch shapes the autotuner chooses between (0 = the default for that field).
 struct LaunchConfig {
-  int cover_slots = 64;           // slots with segments per block of the coverage kernel (16, 32 or 64)
+  int cover_slots = 0;            // slots with segments per coverage block (16, 32 or 64; 0 = by frame)
   int cover_blocks_per_sm = 0;    // coverage grid: blocks per SM (0 = as many as fit)
   int fine_blocks_per_sm = 0;     // composite grid: blocks per SM (0 = as many as fit)
   int edge_block = 128;           // threads per block of the per-item edge builder (64/128/256)
   int cubic_blocks_per_sm = 3;    // lane-scheduled curve-piece flattener: blocks per SM (0 = as many as fit)
+  int no_occlusion_cull = 0;      // 1: the composite starts every strip at its first command
 };
 
 int exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* tmp, cudaStream_t st);

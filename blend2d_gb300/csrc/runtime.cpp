@@ -762,12 +762,12 @@ BLGpuResult Runtime::autotune(int trials, LaunchConfig* best_out, double* best_m
   LaunchConfig best = cfg;
   double best_ms = 0.0;
   if (!r) r = measure(best, best_ms);
-  const int cover_slots[] = {16, 32, 64};
+  const int cover_slots[] = {0, 16, 32, 64};
   const int blocks[] = {0, 1, 2, 3};
   const int edge_blocks[] = {64, 128, 256};
   for (int field = 0; field < 5 && !r; field++) {
     const int* vals = field == 0 ? cover_slots : (field == 3 ? edge_blocks : blocks);
-    const int nvals = field == 0 ? 3 : (field == 3 ? 3 : 4);
+    const int nvals = field == 0 ? 4 : (field == 3 ? 3 : 4);
     for (int k = 0; k < nvals && !r; k++) {
       LaunchConfig c = best;
       int* slot = field == 0 ? &c.cover_slots : field == 1 ? &c.cover_blocks_per_sm : field == 2 ? &c.fine_blocks_per_sm

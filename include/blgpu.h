@@ -118,12 +118,14 @@ typedef struct BLGpuStats {
  * band geometry are fixed by the pipeline (32-pixel tile columns matching a warp's lanes, the
  * reference's band heights), so the tunable parameters are how work is grouped and gridded. */
 typedef struct BLGpuLaunchConfig {
-  int32_t cover_slots;          /* slots (command x 4-row strip x 32-px tile column) per coverage block: 16, 32 or 64 */
+  int32_t cover_slots;          /* slots (command x 4-row strip x 32-px tile column) per coverage block: 16, 32 or 64; 0 = chosen per frame */
   int32_t cover_blocks_per_sm;  /* coverage pass grid */
   int32_t fine_blocks_per_sm;   /* composite pass grid */
   int32_t edge_block;           /* threads per block of the per-item edge builder: 64, 128 or 256 */
-  int32_t cubic_blocks_per_sm;  /* lane-scheduled cubic flattener grid */
-  int32_t reserved[3];
+  int32_t cubic_blocks_per_sm;  /* lane-scheduled curve-piece flattener grid */
+  int32_t no_occlusion_cull;    /* 1: composite every command of every strip (pixel-op counts of the
+                                   reference's work; same pixels) */
+  int32_t reserved[2];
 } BLGpuLaunchConfig;
 
 /* --- runtime (device, stream, memory) --------------------------------------------------- */

@@ -263,7 +263,7 @@ def test_autotune_keeps_pixels_and_every_config_renders_the_same():
         bg.render_stream(rt, stream, dev)
         best, ms = rt.autotune(trials=2)
         torch.cuda.synchronize()
-        assert ms > 0 and best.cover_slots in (16, 32, 64) and best.edge_block in (64, 128, 256)
+        assert ms > 0 and best.cover_slots in (0, 16, 32, 64) and best.edge_block in (64, 128, 256)
         assert not _diff(dev.cpu().numpy().view(np.uint32), want)       # tuning left the pixels alone
         for cfg in [dict(cover_slots=16, edge_block=64, fine_blocks_per_sm=1, cover_blocks_per_sm=1, cubic_blocks_per_sm=1),
                     dict(cover_slots=32, edge_block=256, fine_blocks_per_sm=0, cover_blocks_per_sm=0, cubic_blocks_per_sm=0)]:
@@ -383,3 +383,20 @@ def test_two_threads_record_and_flush_async(runtimes):
     assert len(results) == 3 * len(streams)
     for (rep, i), img in results.items():
         assert not _diff(img, want[i]), (rep, i, _diff(img, want[i]))
+
+
+def test_occlusion_cull_keeps_pixels_and_skips_work():
+    """SrcCopy quads over each other: the composite with occlusion culling gives the pixels of the
+    composite without it (and of the oracle) while compositing fewer pixel-ops."""
+    stream = scenes.patterns(count=300, width=512, height=512).to_bytes()
+    with bg.Runtime(0) as rt:
+        culled = bg.render_stream(rt, stream)
+        ops_culled = rt.stats().pixel_ops
+        cfg = rt.launch_config()
+        rt.set_launch_config(bg.LaunchConfig(**{**cfg.as_dict(), "no_occlusion_cull": 1}))
+        full = bg.render_stream(rt, stream)
+        ops_full = rt.stats().pixel_ops
+    assert np.array_equal(culled, full)
+    assert ops_culled < ops_full
+    want = oracle_lib.render(stream)
+    assert not _diff(culled, want), _diff(culled, want)
