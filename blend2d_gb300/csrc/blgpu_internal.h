@@ -46,7 +46,8 @@ enum FetchKind : uint32_t {
   kFetchPatAffineNN, kFetchPatAffineBI
 };
 
-enum LutVariant : uint32_t { kLutSSE2 = 0, kLutAVX2 = 1, kLutScalar = 2 };
+enum LutVariant : uint32_t { kLutSSE2 = 0, kLutAVX2 = 1, kLutScalar = 2,
+                             kLut64 = 3 };   // kLut64: the 64-bit LUT of dithered gradients (interpolate_prgb64)
 
 // Fetch parameters of one style, set up on the host exactly like the reference's
 // Pipeline::FetchUtils (blend2d/pipeline/pipedefs.cpp).
@@ -75,7 +76,8 @@ struct alignas(16) DevStyle {
   int32_t pat_tx, pat_ty, pat_rx, pat_ry;
   uint32_t pat_wa, pat_wb, pat_wc, pat_wd;
   uint32_t ext_y;          // vertical extend: 0 pad, 1 repeat, 2 reflect
-  uint32_t pad2[3];
+  uint32_t dither;         // gradient quality DITHER: 64-bit LUT (2 words per entry) + ordered dither
+  uint32_t pad2[2];
   // pattern affine (32.32 fixed point)
   uint64_t af_xx, af_xy, af_yx, af_yy, af_tx, af_ty;
   int32_t af_ox, af_oy, af_rx, af_ry;

@@ -190,17 +190,18 @@ struct BLGpuContext {
     if (cs.frame_gen == frame->generation) return cs.frame_index;
     DevStyle d = cs.hs.dev;
     if (d.lut_size) {
+      if (d.dither) frame->lut_words = (frame->lut_words + 1u) & ~1u;   // 8-byte aligned entries
       DevLutJob job{};
       job.style = uint32_t(frame->styles.size());
       job.stop_first = uint32_t(frame->stops.size());
       job.stop_count = uint32_t(cs.hs.stops.size());
       job.lut_offset = frame->lut_words;
       job.lut_size = d.lut_size;
-      job.variant = rt->rt.lut_variant;
+      job.variant = d.dither ? uint32_t(kLut64) : rt->rt.lut_variant;
       frame->stops.append(cs.hs.stops.data(), cs.hs.stops.size());
       frame->lut_jobs.push_back(job);
       d.lut_offset = frame->lut_words;
-      frame->lut_words += d.lut_size;
+      frame->lut_words += d.dither ? 2u * d.lut_size : d.lut_size;
     }
     if (cs.has_image) d.src_offset += frame->add_image(cs.image);
     frame->styles.push_back(d);
@@ -463,7 +464,6 @@ struct BLGpuContext {
         return value > 0 ? BLGPU_ERROR_INVALID_VALUE : BLGPU_SUCCESS;
       case kHintGradientQuality:
         if (value > kGradientQualityDither) return BLGPU_ERROR_INVALID_VALUE;
-        if (value == kGradientQualityDither) return BLGPU_ERROR_NOT_IMPLEMENTED;
         s.gradient_quality = value;
         return BLGPU_SUCCESS;
       case kHintPatternQuality:
@@ -512,7 +512,7 @@ struct BLGpuContext {
     d.stop_count = g->stop_count;
     d.transform = g->transform;
     reset_style_slot();
-    style_gradient(s.style.hs, d, s.final_t);
+    style_gradient(s.style.hs, d, s.final_t, s.gradient_quality);
     return BLGPU_SUCCESS;
   }
 

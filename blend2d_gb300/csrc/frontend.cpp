@@ -268,7 +268,8 @@ static bool init_conic(DevStyle& d, const double* v, const Mat& t) {   // pipede
 
 // init_non_solid_fetch_data, gradient branch (blend2d/raster/rastercontext.cpp:423-478) with
 // GradientInternal::ensure_info (blend2d/core/gradient.cpp:202-287).
-void style_gradient(HostStyle& s, const GradientDesc& g, const Mat& final_transform) {
+// `quality`: BLGradientQuality captured when the style is set (rastercontext.cpp:454-466).
+void style_gradient(HostStyle& s, const GradientDesc& g, const Mat& final_transform, uint32_t quality) {
   // reset in place: the stop vector keeps its capacity from style to style
   std::vector<DevStop> stops = std::move(s.stops);
   s.nop = true;
@@ -308,6 +309,10 @@ void style_gradient(HostStyle& s, const GradientDesc& g, const Mat& final_transf
     s.dev.fetch = kFetchSolid;
     s.dev.solid = premultiply(rgba32_of(stops[n - 1].rgba64));
     return;
+  }
+  if (quality >= 2u) {            // DITHER: lut_size(true) (gradient_p.h:113-120), 64-bit LUT
+    lut_size = lut_size * 2u < 1024u ? lut_size * 2u : 1024u;
+    s.dev.dither = 1u;
   }
   s.dev.lut_size = lut_size;
   bool ok = g.type == 0 ? init_linear(s.dev, g.values, g.extend, tf)

@@ -54,7 +54,7 @@ struct PatternDesc {
 };
 
 void style_solid(HostStyle& s, uint32_t argb32);
-void style_gradient(HostStyle& s, const GradientDesc& g, const Mat& final_transform);
+void style_gradient(HostStyle& s, const GradientDesc& g, const Mat& final_transform, uint32_t quality = 0);
 void style_pattern(HostStyle& s, const PatternDesc& p, uint32_t pattern_quality, const Mat& final_transform);
 
 int default_band_height(int width);

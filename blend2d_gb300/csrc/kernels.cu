@@ -117,6 +117,120 @@ __device__ uint32_t lut_eval_scalar(const LutSpan* sp, int nspans, uint32_t e, u
   return val;
 }
 
+// 64-bit LUT of dithered gradients: interpolate_prgb64 (interpolation.cpp:161-288). Same span walk
+// as the scalar 32-bit builder (a span covers (p1 >> 8) - (p0 >> 8) + 1 entries, its first entry is
+// premultiplied c0, later ones step 16.15 fixed-point positions), with 16-bit channels and
+// premultiplication by udiv65535 (scalar_p.h:37, :179-222).
+struct LutSpan64 {
+  uint32_t start, count;
+  uint64_t c0, c1;
+  uint32_t inc[4];         // r, g, b, a
+};
+
+__device__ __forceinline__ uint32_t udiv65535(uint32_t x) { return ((x + 0x8000u) + ((x + 0x8000u) >> 16)) >> 16; }
+
+__device__ __forceinline__ uint64_t premul64(uint64_t c) {
+  const uint32_t a = uint32_t(c >> 48);
+  const uint32_t r = udiv65535((uint32_t(c >> 32) & 0xFFFFu) * a);
+  const uint32_t g = udiv65535((uint32_t(c >> 16) & 0xFFFFu) * a);
+  const uint32_t b = udiv65535((uint32_t(c) & 0xFFFFu) * a);
+  return (uint64_t(a) << 48) | (uint64_t(r) << 32) | (uint64_t(g) << 16) | uint64_t(b);
+}
+
+constexpr uint32_t kLut64Shift = 15, kLut64Mask = 0xFFFFu << 15;
+
+__device__ uint64_t lut_eval64(const LutSpan64* sp, int nspans, uint32_t e, uint64_t val) {
+  for (int k = 0; k < nspans; k++) {
+    const LutSpan64& q = sp[k];
+    if (e >= q.start && e < q.start + q.count) {
+      if (q.c0 == q.c1 || e == q.start) val = premul64(q.c0);
+      else {
+        const uint32_t j = e - q.start, half = 1u << (kLut64Shift - 1);
+        const uint32_t r_pos = uint32_t((q.c0 >> (32 - kLut64Shift)) & kLut64Mask) + half + j * q.inc[0];
+        const uint32_t g_pos = uint32_t((q.c0 >> (16 - kLut64Shift)) & kLut64Mask) + half + j * q.inc[1];
+        const uint32_t b_pos = uint32_t((q.c0 << kLut64Shift) & kLut64Mask) + half + j * q.inc[2];
+        if (((q.c0 & q.c1) >> 48) == 0xFFFFu) {
+          val = (uint64_t(r_pos & kLut64Mask) << (32 - kLut64Shift)) | (uint64_t(g_pos & kLut64Mask) << (16 - kLut64Shift)) |
+                (uint64_t(b_pos & kLut64Mask) >> kLut64Shift) | 0xFFFF000000000000ull;
+        }
+        else {
+          const uint32_t a_pos = uint32_t((q.c0 >> (48 - kLut64Shift)) & kLut64Mask) + half + j * q.inc[3];
+          const uint32_t ca = a_pos >> kLut64Shift;
+          const uint32_t cr = udiv65535((r_pos >> kLut64Shift) * ca);
+          const uint32_t cg = udiv65535((g_pos >> kLut64Shift) * ca);
+          const uint32_t cb = udiv65535((b_pos >> kLut64Shift) * ca);
+          val = (uint64_t(ca) << 48) | (uint64_t(cr) << 32) | (uint64_t(cg) << 16) | uint64_t(cb);
+        }
+      }
+    }
+  }
+  return val;
+}
+
+// Warp-wide build of one 64-bit LUT, 32 stops per chunk like the 32-bit scalar path below.
+__device__ void lut_build64(const DevLutJob& job, const DevStop* s, uint64_t* lut, LutSpan64* spans, int lane) {
+  const uint32_t n = job.stop_count;
+  const uint64_t first_c = s[0].rgba64;
+  const double fWidth = double(int32_t(job.lut_size - 1u) << 8);
+  uint32_t car_u0 = 0, span_end = 0;
+  uint64_t car_c = first_c;
+  bool first_chunk = true;
+  for (uint32_t si = 0; si < n; si += 32) {
+    const uint32_t k = si + uint32_t(lane);
+    const int ns = int(min(32u, n - si));
+    uint64_t c1 = 0;
+    uint32_t u1 = 0;
+    if (k < n) {
+      c1 = s[k].rgba64;
+      u1 = uint32_t(round_to_int(s[k].offset * fWidth));
+    }
+    uint32_t u0 = __shfl_up_sync(0xFFFFFFFFu, u1, 1);
+    uint64_t c0 = __shfl_up_sync(0xFFFFFFFFu, c1, 1);
+    if (lane == 0) { u0 = car_u0; c0 = car_c; }
+    if (lane < ns) {
+      LutSpan64 sp;
+      const uint32_t i = (u1 >> 8) - (u0 >> 8);
+      if (i == 0) c0 = c1;
+      sp.start = u0 >> 8;
+      sp.count = i + 1u;
+      sp.c0 = c0;
+      sp.c1 = c1;
+      if (c0 != c1 && sp.count > 1) {
+        const int32_t div = int32_t(sp.count - 1u);
+        sp.inc[0] = uint32_t(int32_t(uint32_t((c1 >> (32 - kLut64Shift)) & kLut64Mask) -
+                                     uint32_t((c0 >> (32 - kLut64Shift)) & kLut64Mask)) / div);
+        sp.inc[1] = uint32_t(int32_t(uint32_t((c1 >> (16 - kLut64Shift)) & kLut64Mask) -
+                                     uint32_t((c0 >> (16 - kLut64Shift)) & kLut64Mask)) / div);
+        sp.inc[2] = uint32_t(int32_t(uint32_t((c1 << kLut64Shift) & kLut64Mask) -
+                                     uint32_t((c0 << kLut64Shift) & kLut64Mask)) / div);
+        sp.inc[3] = uint32_t(int32_t(uint32_t((c1 >> (48 - kLut64Shift)) & kLut64Mask) -
+                                     uint32_t((c0 >> (48 - kLut64Shift)) & kLut64Mask)) / div);
+      }
+      spans[lane] = sp;
+    }
+    car_u0 = __shfl_sync(0xFFFFFFFFu, u1, ns - 1);
+    car_c = __shfl_sync(0xFFFFFFFFu, c1, ns - 1);
+    __syncwarp();
+    span_end = spans[ns - 1].start + spans[ns - 1].count;
+    for (uint32_t e = uint32_t(lane); e < job.lut_size; e += 32) {
+      const uint64_t v = first_chunk ? 0ull : lut[e];
+      lut[e] = lut_eval64(spans, ns, e, v);
+    }
+    first_chunk = false;
+    __syncwarp();
+  }
+  // the trailing fill is the last stop's colour; entry 0 is the first stop's
+  for (uint32_t e = uint32_t(lane); e < job.lut_size; e += 32) {
+    uint64_t v = first_chunk ? 0ull : lut[e];
+    if (n == 1) v = premul64(first_c);
+    else {
+      if (e >= span_end) v = premul64(car_c);
+      if (e == 0) v = premul64(first_c);
+    }
+    lut[e] = v;
+  }
+}
+
 // One warp per LUT. The span table is built 32 stops at a time, one stop per lane: a span depends
 // only on its stop and the one before it (position and colour, passed up one lane; the previous
 // chunk's last stop is carried), so the FP64 stop positions and increments of a chunk are computed
@@ -128,12 +242,17 @@ constexpr int kLutWarps = 8;
 __global__ void __launch_bounds__(32 * kLutWarps) lut_kernel(const DevLutJob* jobs, const DevStop* stops, uint32_t* luts,
                                                              uint32_t num_jobs) {
   __shared__ LutSpan spans_all[kLutWarps][32];
+  __shared__ LutSpan64 spans64_all[kLutWarps][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t jid = blockIdx.x * kLutWarps + uint32_t(warp);
   if (jid >= num_jobs) return;                         // whole warps leave together
   LutSpan* spans = spans_all[warp];
   const DevLutJob job = jobs[jid];
   const DevStop* s = stops + job.stop_first;
+  if (job.variant == kLut64) {                         // offset is even: 8-byte aligned entries
+    lut_build64(job, s, reinterpret_cast<uint64_t*>(luts + job.lut_offset), spans64_all[warp], lane);
+    return;
+  }
   const uint32_t n = job.stop_count;
   const bool scalar = job.variant == kLutScalar;
   const bool avx2 = job.variant == kLutAVX2;
@@ -1110,10 +1229,24 @@ __global__ void __launch_bounds__(kFineThreads, 4) fine_kernel(FrameView f) {
             // the 4 pixels' LUT indices first, so their 4 table loads are in flight together
             const uint32_t* lut = f.luts + st.lut_offset;
             uint32_t sv[4];
+            if (!st.dither) {
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-              const bool on = m[k] && xp + k < cv.w;
-              sv[k] = on ? __ldg(lut + px::gradient_index(st, rs, xp + k)) : 0u;
+              for (int k = 0; k < 4; k++) {
+                const bool on = m[k] && xp + k < cv.w;
+                sv[k] = on ? __ldg(lut + px::gradient_index(st, rs, xp + k)) : 0u;
+              }
+            }
+            else {
+              // 64-bit entries (lut_offset is even) + the ordered-dither threshold of each pixel
+              uint2 e[4];
+#pragma unroll
+              for (int k = 0; k < 4; k++) {
+                const bool on = m[k] && xp + k < cv.w;
+                e[k] = on ? __ldg(reinterpret_cast<const uint2*>(lut) + px::gradient_index(st, rs, xp + k))
+                          : make_uint2(0u, 0u);
+              }
+#pragma unroll
+              for (int k = 0; k < 4; k++) sv[k] = px::dither_pixel(e[k], px::dither_threshold(xp + k, y));
             }
 #pragma unroll
             for (int k = 0; k < 4; k++) {

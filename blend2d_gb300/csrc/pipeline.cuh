@@ -177,6 +177,30 @@ __device__ RowState row_state(const DevStyle& st, int y, int fetch_y0) {
 
 __device__ __forceinline__ bool is_gradient(uint32_t fetch) { return fetch >= kFetchLinearPad && fetch <= kFetchConic; }
 
+// Threshold of the 16x16 ordered-dither matrix (bayer_matrix_16x16, tables_p.h:449-473) at canvas
+// pixel (x, y), from the matrix's recursive construction instead of a table: the index interleaves
+// the bits of row and column, lowest bits most significant, each pair weighted by the 2x2 pattern
+// {{0, 3}, {2, 1}} (= 2 * (r ^ c) + c); the entry scales the index from [0, 256) to [0, 255],
+// rounding half down.
+__device__ __forceinline__ uint32_t dither_threshold(int x, int y) {
+  uint32_t c = __brev(uint32_t(x) & 15u) >> 28;               // bit k of x -> bit 3 - k
+  uint32_t v = __brev((uint32_t(x) ^ uint32_t(y)) & 15u) >> 28;
+  c = (c | (c << 2)) & 0x33u; c = (c | (c << 1)) & 0x55u;      // bit j -> bit 2j
+  v = (v | (v << 2)) & 0x33u; v = (v | (v << 1)) & 0x55u;
+  return (((v << 1) | c) * 255u + 127u) >> 8;
+}
+
+// FetchGradientBase<DITHER>::fetch_pixel (fetchgeneric_p.h:922-933): a 64-bit premultiplied LUT
+// entry (lo = g << 16 | b, hi = a << 16 | r) plus the threshold, down to 8 bits, each colour
+// channel clamped to alpha.
+__device__ __forceinline__ uint32_t dither_pixel(uint2 v, uint32_t dd) {
+  const uint32_t a = v.y >> 24;
+  const uint32_t r = min(((v.y & 0xFFFFu) + dd) >> 8, a);
+  const uint32_t g = min(((v.x >> 16) + dd) >> 8, a);
+  const uint32_t b = min(((v.x & 0xFFFFu) + dd) >> 8, a);
+  return (a << 24) | (r << 16) | (g << 8) | b;
+}
+
 // LUT index of pixel x of a gradient fetcher (linear, radial or conic): the fetchers' per-pixel
 // arithmetic up to the table lookup.
 __device__ __forceinline__ uint32_t gradient_index(const DevStyle& st, const RowState& r, int x) {
@@ -219,6 +243,7 @@ __device__ __forceinline__ uint32_t fetch(const DevStyle& st, const RowState& r,
     case kFetchSolid:
       return st.solid;
     case kFetchLinearPad: case kFetchLinearRoR: case kFetchRadialPad: case kFetchRadialRoR: case kFetchConic:
+      // 32-bit LUT only: the fine stage fetches gradients (dithered ones too) on its own path
       return __ldg(luts + st.lut_offset + gradient_index(st, r, x));
     case kFetchPatAlignedPad: case kFetchPatAlignedRepeat: case kFetchPatAlignedRoR: {
       uint32_t kind = st.fetch - kFetchPatAlignedPad;

@@ -53,6 +53,7 @@ NON_ZERO, EVEN_ODD = 0, 1
 LINEAR, RADIAL, CONIC = 0, 1, 2
 PAD, REPEAT, REFLECT = 0, 1, 2
 HINT_GRADIENT_QUALITY, HINT_PATTERN_QUALITY = 1, 2
+GRADIENT_NEAREST, GRADIENT_SMOOTH, GRADIENT_DITHER = 0, 1, 2        # BLGradientQuality
 NEAREST, BILINEAR = 0, 1
 P_MOVE, P_ON, P_QUAD, P_CONIC, P_CUBIC, P_CLOSE = 0, 1, 2, 3, 4, 5
 
@@ -299,15 +300,18 @@ def polygons(seed: int = 1, width: int = 512, height: int = 512, count: int = 20
     return sw
 
 
-def curves(seed: int = 2, width: int = 1920, height: int = 1080, count: int = 20000) -> StreamWriter:
+def curves(seed: int = 2, width: int = 1920, height: int = 1080, count: int = 20000,
+           dither: bool = False) -> StreamWriter:
     """Closed cubic paths (4-12 segments, bbox side log-uniform 8-256 px, partly outside the
     canvas), NonZero/EvenOdd 50/50, linear/radial/conic gradients with 2-8 stops and
-    pad/repeat/reflect extend, SrcOver."""
+    pad/repeat/reflect extend, SrcOver. `dither`: gradient quality DITHER for every gradient."""
     rng = np.random.Generator(np.random.PCG64(seed))
     sw = StreamWriter(width, height)
     sw.solid(0xFF000000)
     sw.fill_all()
     sw.comp_op(SRC_OVER)
+    if dither:
+        sw.hint(HINT_GRADIENT_QUALITY, GRADIENT_DITHER)
     for i in range(count):
         side = float(_log_uniform(rng, 8.0, 256.0))
         x0 = float(rng.uniform(-side * 0.5, width - side * 0.5))
@@ -409,9 +413,10 @@ def serving_requests(seed: int = 5, count: int = 32, min_side: int = 64, max_sid
 def random_mix(seed: int, width: int = 257, height: int = 257, count: int = 200,
                styles=("solid", "linear", "radial", "conic", "pattern_nn", "pattern_bi"),
                commands=("rect_i", "rect_d", "box_d", "polygon", "path_quad", "path_cubic"),
-               transforms: bool = True, alphas: bool = True) -> StreamWriter:
+               transforms: bool = True, alphas: bool = True, dither: bool = False) -> StreamWriter:
     """Mixed commands/styles/comp-ops over a canvas slightly larger than the shapes' range
-    (coordinates span -30 .. size+30 like the reference tester, so clipping is exercised)."""
+    (coordinates span -30 .. size+30 like the reference tester, so clipping is exercised).
+    `dither`: each gradient is set with gradient quality DITHER (2 in 3) or NEAREST."""
     rng = np.random.Generator(np.random.PCG64(seed))
     sw = StreamWriter(width, height)
     for _ in range(3):
@@ -442,6 +447,8 @@ def random_mix(seed: int, width: int = 257, height: int = 257, count: int = 200,
         if style == "solid":
             sw.solid(int(rng.integers(0, 2**32, dtype=np.uint64)))
         elif style in ("linear", "radial", "conic"):
+            if dither:
+                sw.hint(HINT_GRADIENT_QUALITY, GRADIENT_DITHER if rng.integers(0, 3) else GRADIENT_NEAREST)
             side = float(rng.uniform(20, max(20, width, height)))
             x0, y0 = float(rng.uniform(lo_x, max(lo_x, hi_x - side))), float(rng.uniform(lo_y, max(lo_y, hi_y - side)))
             _gradient_style(rng, sw, x0, y0, side, kind={"linear": LINEAR, "radial": RADIAL, "conic": CONIC}[style])

@@ -429,8 +429,16 @@ static void set_style_gradient(OCtx* c, const uint8_t* p) {
       st->solid = o_premultiply(c32);
       goto done;
     }
+    if (c->s.gradient_quality >= 2u) {
+      /* BL_GRADIENT_QUALITY_DITHER: lut_size(true) (gradient_p.h:113-120), ensure_lut64 */
+      lut_size = lut_size * 2u < 1024u ? lut_size * 2u : 1024u;
+      st->dither = 1;
+      b2d_oracle_build_lut64(st->lut64, lut_size, stops, (size_t)n);
+    }
+    else {
+      b2d_oracle_build_lut(st->lut, lut_size, stops, (size_t)n, c->lut_variant);
+    }
     st->lut_size = lut_size;
-    b2d_oracle_build_lut(st->lut, lut_size, stops, (size_t)n, c->lut_variant);
     if (!o_init_gradient(st, g.type, g.extend_mode, g.values, &tf)) st->nop = 1;
   }
 done:

@@ -46,6 +46,8 @@ int b2d_oracle_render(const uint8_t* stream, size_t size, uint32_t* out_pixels,
 
 /* Builds a gradient LUT of `lut_size` entries from `n` stops {double offset; uint64 rgba64}. */
 void b2d_oracle_build_lut(uint32_t* lut, uint32_t lut_size, const void* stops, size_t n, uint32_t variant);
+/* The 64-bit (premultiplied RGBA64) LUT of dithered gradients (interpolate_prgb64). */
+void b2d_oracle_build_lut64(uint64_t* lut, uint32_t lut_size, const void* stops, size_t n);
 
 /* Analytic-rasterizer known-answer support: rasterizes one 24.8 line into a dense cell grid
  * [rows x (width+2)] using banded rasterization with `band_height`, starting at row 0. */

@@ -144,6 +144,8 @@ typedef struct OStyle {
   /* gradient */
   uint32_t lut[1024];
   uint32_t lut_size;
+  int dither;                  /* BL_GRADIENT_QUALITY_DITHER: 64-bit LUT + ordered dither */
+  uint64_t lut64[1024];
   uint64_t lin_pt0, lin_dt, lin_dy;
   uint32_t maxi, rori;
   double rad_tx, rad_ty, rad_yx, rad_yy, rad_b0, rad_by, rad_dd0, rad_ddy, rad_inv2a, rad_amul4, rad_sq_inv2a, rad_sq_fr;

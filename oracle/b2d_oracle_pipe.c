@@ -52,6 +52,9 @@ static inline uint32_t op_src_copy_m(uint32_t d, uint32_t s, uint32_t m) {
 typedef struct {
   const OStyle* s;
   uint32_t solid;
+  /* dithered gradients (FetchGradientBase<DITHER>, fetchgeneric_p.h:899-934): matrix row and
+     column of the next fetched pixel */
+  uint32_t dm_y, dm_x;
   /* linear */
   uint64_t pt, py;
   /* radial */
@@ -73,7 +76,36 @@ typedef struct {
   uint64_t tx, ty, px, py_;
 } OFetch;
 
-static inline uint32_t lut_fetch(const OFetch* f, uint32_t idx) { return f->s->lut[idx]; }
+/* 16x16 ordered-dither matrix of the reference (its bayer_matrix_16x16, tables_p.h:449-473),
+ * restated from its recursive construction: the index interleaves the bits of the row and column,
+ * low bits most significant, each pair weighted by the 2x2 pattern {{0, 3}, {2, 1}}; the entry is
+ * the index scaled from [0, 256) to [0, 255] rounding half down. */
+static uint8_t o_dither[16][16];
+static int o_dither_ready;
+static void o_dither_init(void) {
+  static const uint32_t p2[2][2] = {{0, 3}, {2, 1}};
+  for (uint32_t r = 0; r < 16; r++) {
+    for (uint32_t c = 0; c < 16; c++) {
+      uint32_t b = 0;
+      for (uint32_t k = 0; k < 4; k++) b += p2[(r >> k) & 1u][(c >> k) & 1u] << (2u * (3u - k));
+      o_dither[r][c] = (uint8_t)((b * 255u + 127u) >> 8);
+    }
+  }
+  o_dither_ready = 1;
+}
+
+static inline uint32_t lut_fetch(OFetch* f, uint32_t idx) {
+  if (!f->s->dither) return f->s->lut[idx];
+  /* FetchGradientBase<DITHER>::fetch_pixel (fetchgeneric_p.h:922-933) */
+  uint64_t v = f->s->lut64[idx];
+  uint32_t dd = o_dither[f->dm_y][f->dm_x];
+  uint32_t a = (uint32_t)(v >> 48) >> 8;
+  uint32_t r = ((uint32_t)(v >> 32) & 0xFFFFu) + dd; r >>= 8; if (r > a) r = a;
+  uint32_t g = ((uint32_t)(v >> 16) & 0xFFFFu) + dd; g >>= 8; if (g > a) g = a;
+  uint32_t b = ((uint32_t)v & 0xFFFFu) + dd; b >>= 8; if (b > a) b = a;
+  f->dm_x = (f->dm_x + 1u) & 15u;
+  return (a << 24) | (r << 16) | (g << 8) | b;
+}
 
 /* --- pattern vertical context (fetchgeneric_p.h:78-155) --- */
 static void vctx_init(OFetch* f, uint32_t y_pos) {
@@ -229,6 +261,7 @@ static void conic_begin_scanline(OFetch* f) {
 
 static void fetch_span_init_y(OFetch* f, uint32_t y) {
   const OStyle* s = f->s;
+  f->dm_y = y & 15u;           /* _init_gradient_base: pixel origin (0, 0) */
   switch (s->fetch_type) {
     case O_FT_SOLID: f->solid = s->solid; break;
     case O_FT_LINEAR_PAD: case O_FT_LINEAR_ROR:
@@ -260,6 +293,7 @@ static void fxfy_init_acc(OFetch* f) {
 
 static void fetch_span_start_x(OFetch* f, uint32_t x) {
   const OStyle* s = f->s;
+  f->dm_x = x & 15u;           /* _initGradientX */
   switch (s->fetch_type) {
     case O_FT_SOLID: break;
     case O_FT_LINEAR_PAD: case O_FT_LINEAR_ROR: f->pt = f->py + (uint64_t)x * s->lin_dt; break;
@@ -286,8 +320,8 @@ static void fetch_span_start_x(OFetch* f, uint32_t x) {
 }
 
 static void fetch_span_advance_x(OFetch* f, uint32_t x, uint32_t diff) {
-  (void)x;
   const OStyle* s = f->s;
+  f->dm_x = x & 15u;           /* _initGradientX */
   switch (s->fetch_type) {
     case O_FT_SOLID: break;
     case O_FT_LINEAR_PAD: case O_FT_LINEAR_ROR: f->pt += (uint64_t)diff * s->lin_dt; break;
@@ -305,6 +339,7 @@ static void fetch_span_advance_x(OFetch* f, uint32_t x, uint32_t diff) {
 
 static void fetch_advance_y(OFetch* f) {
   const OStyle* s = f->s;
+  f->dm_y = (f->dm_y + 1u) & 15u;   /* _advanceGradientY */
   switch (s->fetch_type) {
     case O_FT_SOLID: break;
     case O_FT_LINEAR_PAD: case O_FT_LINEAR_ROR: f->py += s->lin_dy; break;
@@ -419,6 +454,7 @@ static void fetch_rect_init(OFetch* f, uint32_t x, uint32_t y, uint32_t w) {
   (void)w;
   switch (s->fetch_type) {
     case O_FT_LINEAR_PAD: case O_FT_LINEAR_ROR:
+      f->dm_y = y & 15u;
       f->pt = 0; f->py = s->lin_pt0; f->py += (uint64_t)y * s->lin_dy + (uint64_t)x * s->lin_dt; break;
     case O_FT_PAT_ALIGNED_PAD: case O_FT_PAT_ALIGNED_REPEAT: case O_FT_PAT_ALIGNED_ROR:
     case O_FT_PAT_FXFY_PAD: case O_FT_PAT_FXFY_ROR: {
@@ -446,7 +482,7 @@ static void fetch_rect_init(OFetch* f, uint32_t x, uint32_t y, uint32_t w) {
 static void fetch_rect_start_x(OFetch* f, uint32_t x) {
   const OStyle* s = f->s;
   switch (s->fetch_type) {
-    case O_FT_LINEAR_PAD: case O_FT_LINEAR_ROR: f->pt = f->py; break;
+    case O_FT_LINEAR_PAD: case O_FT_LINEAR_ROR: f->dm_x = x & 15u; f->pt = f->py; break;
     case O_FT_PAT_ALIGNED_PAD: case O_FT_PAT_ALIGNED_REPEAT: case O_FT_PAT_ALIGNED_ROR:
       f->hx = f->htx; break;
     case O_FT_PAT_FXFY_PAD: case O_FT_PAT_FXFY_ROR:
@@ -891,6 +927,94 @@ SolidLoop:
             cp = ((cp + ((cp & 0xFF00FF00u) >> 8)) & 0xFF00FF00u) >> 8;
             cg = ((cg + ((cg & 0xFF00FF00u) >> 8)) & 0xFF00FF00u);
             cp += cg + ca;
+            *span++ = cp;
+          } while (--i);
+        }
+      }
+      c0 = c1;
+    }
+  } while (++si < s_size);
+
+  i = (uint32_t)((d + d_size + 1) - span);
+  if (i != 0) goto SolidInit;
+  d[0] = cp_first;
+}
+
+/* Scalar::udiv65535 and cvt_prgb64_8888_from_argb64_8888 (scalar_p.h:37, :179-222): every
+ * channel of an RGBA64 colour times its alpha, divided by 65535 with rounding. */
+static inline uint32_t udiv65535(uint32_t x) { return ((x + 0x8000u) + ((x + 0x8000u) >> 16)) >> 16; }
+static inline uint64_t premul64(uint64_t c) {
+  uint32_t a = (uint32_t)(c >> 48);
+  uint32_t r = udiv65535(((uint32_t)(c >> 32) & 0xFFFFu) * a);
+  uint32_t g = udiv65535(((uint32_t)(c >> 16) & 0xFFFFu) * a);
+  uint32_t b = udiv65535(((uint32_t)c & 0xFFFFu) * a);
+  return ((uint64_t)a << 48) | ((uint64_t)r << 32) | ((uint64_t)g << 16) | b;
+}
+
+/* interpolate_prgb64 (interpolation.cpp:161-288). */
+void b2d_oracle_build_lut64(uint64_t* d, uint32_t d_size, const void* stops, size_t s_size) {
+  const OStop* s = (const OStop*)stops;
+  if (!o_dither_ready) o_dither_init();
+  uint64_t* span = d;
+  uint32_t i = d_size;
+  uint64_t c0 = s[0].rgba, c1 = c0;
+  uint32_t p0 = 0, p1;
+  size_t si = 0;
+  d_size--;
+  double fWidth = (double)((int32_t)d_size << 8);
+  uint64_t cp = premul64(c0);
+  uint64_t cp_first = cp;
+
+  if (s_size == 1) goto SolidLoop;
+
+  do {
+    c1 = s[si].rgba;
+    p1 = (uint32_t)o_round_to_int(s[si].offset * fWidth);
+    span = d + (p0 >> 8);
+    i = (p1 >> 8) - (p0 >> 8);
+    if (i == 0) c0 = c1;
+    p0 = p1;
+    i++;
+SolidInit:
+    cp = premul64(c0);
+    if (c0 == c1) {
+SolidLoop:
+      do { *span++ = cp; } while (--i);
+    }
+    else {
+      *span++ = cp;
+      if (--i) {
+        const uint32_t kShift = 15, kMask = 0xFFFFu << 15;
+        uint32_t r_pos = (uint32_t)((c0 >> (32 - kShift)) & kMask);
+        uint32_t g_pos = (uint32_t)((c0 >> (16 - kShift)) & kMask);
+        uint32_t b_pos = (uint32_t)((c0 << kShift) & kMask);
+        uint32_t r_inc = (uint32_t)((c1 >> (32 - kShift)) & kMask);
+        uint32_t g_inc = (uint32_t)((c1 >> (16 - kShift)) & kMask);
+        uint32_t b_inc = (uint32_t)((c1 << kShift) & kMask);
+        r_inc = (uint32_t)((int32_t)(r_inc - r_pos) / (int32_t)i);
+        g_inc = (uint32_t)((int32_t)(g_inc - g_pos) / (int32_t)i);
+        b_inc = (uint32_t)((int32_t)(b_inc - b_pos) / (int32_t)i);
+        r_pos += 1u << (kShift - 1); g_pos += 1u << (kShift - 1); b_pos += 1u << (kShift - 1);
+        if (((c0 & c1) & 0xFFFF000000000000ull) == 0xFFFF000000000000ull) {
+          do {
+            r_pos += r_inc; g_pos += g_inc; b_pos += b_inc;
+            cp = ((uint64_t)(r_pos & kMask) << (32 - kShift)) | ((uint64_t)(g_pos & kMask) << (16 - kShift)) |
+                 ((uint64_t)(b_pos & kMask) >> kShift) | 0xFFFF000000000000ull;
+            *span++ = cp;
+          } while (--i);
+        }
+        else {
+          uint32_t a_pos = (uint32_t)((c0 >> (48 - kShift)) & kMask);
+          uint32_t a_inc = (uint32_t)((c1 >> (48 - kShift)) & kMask);
+          a_inc = (uint32_t)((int32_t)(a_inc - a_pos) / (int32_t)i);
+          a_pos += 1u << (kShift - 1);
+          do {
+            a_pos += a_inc; r_pos += r_inc; g_pos += g_inc; b_pos += b_inc;
+            uint32_t ca = a_pos >> kShift;
+            uint32_t cr = udiv65535((r_pos >> kShift) * ca);
+            uint32_t cg = udiv65535((g_pos >> kShift) * ca);
+            uint32_t cb = udiv65535((b_pos >> kShift) * ca);
+            cp = ((uint64_t)ca << 48) | ((uint64_t)cr << 32) | ((uint64_t)cg << 16) | cb;
             *span++ = cp;
           } while (--i);
         }

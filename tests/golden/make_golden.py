@@ -4,7 +4,8 @@ Run in a checkout that has the reference sources (default /root/reference); it b
 reference with oracle/ref.mk (no CMake) into oracle/_ref/ and records:
 
   * scenes  - sha256 of the PRGB32 pixels the reference renders for seeded command streams
-              (blend2d_gb300.scenes), for the stock no-JIT x86-64 build ("default", SSE2 LUT
+              (blend2d_gb300.scenes; the mix_dither / curves_dither scenes use gradient quality
+              DITHER, whose 64-bit LUT has a single builder), for the stock no-JIT x86-64 build ("default", SSE2 LUT
               builder) and, for a subset, the portable-LUT build ("scalar");
   * luts    - sha256 of the gradient LUTs produced by the reference's three builders
               (interpolate_prgb32 / _sse2 / _avx2) for random stop arrays;
@@ -54,6 +55,9 @@ def scene_catalog(full: bool):
         cat.append((f"mix_notf_{s}", f"scenes.random_mix({100 + s}, count=400, transforms=False, alphas=False)", ("default",)))
     cat.append(("mix_wide", "scenes.random_mix(200, width=1031, height=77, count=300)", ("default",)))
     cat.append(("mix_tall", "scenes.random_mix(201, width=61, height=1500, count=300)", ("default",)))
+    for s in range(6):
+        cat.append((f"mix_dither_{s}", f"scenes.random_mix({300 + s}, dither=True)", ("default",) if s % 2 else ("default", "scalar")))
+    cat.append(("curves_dither", "scenes.curves(count=600, width=640, height=360, dither=True)", ("default",)))
     for i in range(6):
         cat.append((f"batch_{i}", f"scenes.batch_canvases(seed=4, count=6, max_side=640, max_paths=400)[{i}]", ("default",)))
     if full:

@@ -62,6 +62,19 @@ def test_random_mix_vs_oracle(runtimes, seed, w, h, variant):
     assert not _diff(got, want), _diff(got, want)
 
 
+@pytest.mark.parametrize("seed,w,h,variant", [(s, w, h, v) for s, (w, h), v in
+                                               zip(range(1100, 1112), [(257, 257), (33, 97), (400, 150), (1, 1),
+                                                                       (129, 129), (640, 31)] * 2,
+                                                   ["default", "avx2", "scalar"] * 4)])
+def test_dithered_gradients_vs_oracle(runtimes, seed, w, h, variant):
+    """Gradient quality DITHER (2 gradients in 3; the others NEAREST, whose LUT builder depends on
+    the variant): the 64-bit LUT and the ordered-dither threshold of every pixel."""
+    stream = scenes.random_mix(seed, width=w, height=h, count=150, dither=True).to_bytes()
+    got = bg.render_stream(runtimes(variant), stream)
+    want = oracle_lib.render(stream, variant)
+    assert not _diff(got, want), _diff(got, want)
+
+
 @pytest.mark.parametrize("seed", range(6))
 def test_edge_cases_vs_oracle(runtimes, seed):
     stream = scenes.edge_cases(seed=seed, width=131 + 17 * seed, height=97 + 5 * seed).to_bytes()
@@ -274,16 +287,20 @@ def test_autotune_keeps_pixels_and_every_config_renders_the_same():
             rt.set_launch_config(bg.LaunchConfig(cover_slots=24, edge_block=128))
 
 
-@pytest.mark.parametrize("variant", ["default", "avx2", "scalar"])
-def test_gradients_with_many_stops(runtimes, variant):
+@pytest.mark.parametrize("variant,dither", [("default", False), ("avx2", False), ("scalar", False),
+                                            ("default", True)])
+def test_gradients_with_many_stops(runtimes, variant, dither):
     """Stop counts around the 32-stop chunks of the LUT builder, with repeated offsets and a first
-    stop at 0 (the SIMD builders skip it), each gradient filling a band of the canvas."""
+    stop at 0 (the SIMD builders skip it), each gradient filling a band of the canvas; with
+    `dither`, the 64-bit LUT builder of gradient quality DITHER."""
     rng = np.random.Generator(np.random.PCG64(77))
     w, band = 300, 6
     counts = [1, 2, 31, 32, 33, 34, 63, 64, 65, 100, 7]
     sw = scenes.StreamWriter(w, band * len(counts))
     sw.solid(0xFF202020)
     sw.fill_all()
+    if dither:
+        sw.hint(scenes.HINT_GRADIENT_QUALITY, scenes.GRADIENT_DITHER)
     for i, n in enumerate(counts):
         offs = np.sort(rng.uniform(0.0, 1.0, n))
         if n > 3:
