@@ -47,6 +47,21 @@ OP_FILL_POLYGON_D = 16
 OP_FILL_PATH_D = 17
 OP_SAVE = 18
 OP_RESTORE = 19
+OP_SET_STROKE_WIDTH = 20
+OP_SET_STROKE_MITER_LIMIT = 21
+OP_SET_STROKE_JOIN = 22
+OP_SET_STROKE_CAPS = 23
+OP_SET_STROKE_TRANSFORM_ORDER = 24
+OP_SET_STROKE_ALPHA = 25
+OP_STROKE_STYLE_RGBA32 = 26
+OP_STROKE_STYLE_GRADIENT = 27
+OP_STROKE_STYLE_PATTERN = 28
+OP_STROKE_PATH_D = 29
+OP_STROKE_POLYLINE_D = 30
+OP_STROKE_POLYGON_D = 31
+OP_STROKE_BOX_D = 32
+OP_STROKE_RECT_D = 33
+OP_STROKE_LINE_D = 34
 
 SRC_OVER, SRC_COPY = 0, 1
 NON_ZERO, EVEN_ODD = 0, 1
@@ -56,6 +71,9 @@ HINT_GRADIENT_QUALITY, HINT_PATTERN_QUALITY = 1, 2
 GRADIENT_NEAREST, GRADIENT_SMOOTH, GRADIENT_DITHER = 0, 1, 2        # BLGradientQuality
 NEAREST, BILINEAR = 0, 1
 P_MOVE, P_ON, P_QUAD, P_CONIC, P_CUBIC, P_CLOSE = 0, 1, 2, 3, 4, 5
+JOIN_MITER_CLIP, JOIN_MITER_BEVEL, JOIN_MITER_ROUND, JOIN_BEVEL, JOIN_ROUND = 0, 1, 2, 3, 4     # BLStrokeJoin
+CAP_BUTT, CAP_SQUARE, CAP_ROUND, CAP_ROUND_REV, CAP_TRIANGLE, CAP_TRIANGLE_REV = 0, 1, 2, 3, 4, 5  # BLStrokeCap
+TRANSFORM_ORDER_AFTER, TRANSFORM_ORDER_BEFORE = 0, 1                                          # BLStrokeTransformOrder
 
 
 def rgba64_from_rgba32(c: int) -> int:
@@ -109,19 +127,54 @@ class StreamWriter:
     def solid(self, argb32: int):
         self._rec(OP_STYLE_RGBA32, struct.pack("<II", int(argb32) & 0xFFFFFFFF, 0))
 
-    def gradient(self, gtype: int, values, extend: int, stops, transform=None):
+    @staticmethod
+    def _gradient_payload(gtype, values, extend, stops, transform):
         vals = list(values) + [0.0] * (6 - len(values))
         tr = list(transform) if transform is not None else [1.0, 0.0, 0.0, 1.0, 0.0, 0.0]
         payload = struct.pack("<IIII6d6d", gtype, extend, len(stops), 1 if transform is not None else 0, *vals, *tr)
         for off, argb in stops:
             payload += struct.pack("<dQ", float(off), rgba64_from_rgba32(int(argb)))
-        self._rec(OP_STYLE_GRADIENT, payload)
+        return payload
 
-    def pattern(self, image_index: int, extend: int = PAD, area=None, transform=None):
+    @staticmethod
+    def _pattern_payload(image_index, extend, area, transform):
         ar = list(area) if area is not None else [0, 0, 0, 0]
         tr = list(transform) if transform is not None else [1.0, 0.0, 0.0, 1.0, 0.0, 0.0]
-        self._rec(OP_STYLE_PATTERN, struct.pack("<II4iII6d", image_index, extend, *ar,
-                                                1 if transform is not None else 0, 0, *tr))
+        return struct.pack("<II4iII6d", image_index, extend, *ar, 1 if transform is not None else 0, 0, *tr)
+
+    def gradient(self, gtype: int, values, extend: int, stops, transform=None):
+        self._rec(OP_STYLE_GRADIENT, self._gradient_payload(gtype, values, extend, stops, transform))
+
+    def pattern(self, image_index: int, extend: int = PAD, area=None, transform=None):
+        self._rec(OP_STYLE_PATTERN, self._pattern_payload(image_index, extend, area, transform))
+
+    # -- stroke state (the stroke style slot and BLStrokeOptions) -------------------------------
+    def stroke_solid(self, argb32: int):
+        self._rec(OP_STROKE_STYLE_RGBA32, struct.pack("<II", int(argb32) & 0xFFFFFFFF, 0))
+
+    def stroke_gradient(self, gtype: int, values, extend: int, stops, transform=None):
+        self._rec(OP_STROKE_STYLE_GRADIENT, self._gradient_payload(gtype, values, extend, stops, transform))
+
+    def stroke_pattern(self, image_index: int, extend: int = PAD, area=None, transform=None):
+        self._rec(OP_STROKE_STYLE_PATTERN, self._pattern_payload(image_index, extend, area, transform))
+
+    def stroke_alpha(self, a: float):
+        self._rec(OP_SET_STROKE_ALPHA, struct.pack("<d", a))
+
+    def stroke_width(self, w: float):
+        self._rec(OP_SET_STROKE_WIDTH, struct.pack("<d", w))
+
+    def stroke_miter_limit(self, m: float):
+        self._rec(OP_SET_STROKE_MITER_LIMIT, struct.pack("<d", m))
+
+    def stroke_join(self, join: int):
+        self._rec(OP_SET_STROKE_JOIN, struct.pack("<II", join, 0))
+
+    def stroke_caps(self, start: int, end: int):
+        self._rec(OP_SET_STROKE_CAPS, struct.pack("<II", start, end))
+
+    def stroke_transform_order(self, order: int):
+        self._rec(OP_SET_STROKE_TRANSFORM_ORDER, struct.pack("<II", order, 0))
 
     def clear_all(self):
         self._rec(OP_CLEAR_ALL)
@@ -154,6 +207,37 @@ class StreamWriter:
         assert len(cmds) == xy.shape[0]
         pad = (-len(cmds)) % 8
         self._rec(OP_FILL_PATH_D, struct.pack("<II", len(cmds), 0) + cmds + b"\0" * pad + xy.tobytes())
+        self.fill_count += 1
+
+    # -- strokes --------------------------------------------------------------------------------
+    def stroke_path(self, cmds, xy: np.ndarray):
+        cmds = bytes(bytearray(cmds))
+        xy = np.ascontiguousarray(xy, dtype="<f8").reshape(-1, 2)
+        assert len(cmds) == xy.shape[0]
+        pad = (-len(cmds)) % 8
+        self._rec(OP_STROKE_PATH_D, struct.pack("<II", len(cmds), 0) + cmds + b"\0" * pad + xy.tobytes())
+        self.fill_count += 1
+
+    def stroke_polyline(self, xy: np.ndarray):
+        xy = np.ascontiguousarray(xy, dtype="<f8").reshape(-1, 2)
+        self._rec(OP_STROKE_POLYLINE_D, struct.pack("<II", xy.shape[0], 0) + xy.tobytes())
+        self.fill_count += 1
+
+    def stroke_polygon(self, xy: np.ndarray):
+        xy = np.ascontiguousarray(xy, dtype="<f8").reshape(-1, 2)
+        self._rec(OP_STROKE_POLYGON_D, struct.pack("<II", xy.shape[0], 0) + xy.tobytes())
+        self.fill_count += 1
+
+    def stroke_box_d(self, x0, y0, x1, y1):
+        self._rec(OP_STROKE_BOX_D, struct.pack("<4d", x0, y0, x1, y1))
+        self.fill_count += 1
+
+    def stroke_rect_d(self, x, y, w, h):
+        self._rec(OP_STROKE_RECT_D, struct.pack("<4d", x, y, w, h))
+        self.fill_count += 1
+
+    def stroke_line_d(self, x0, y0, x1, y1):
+        self._rec(OP_STROKE_LINE_D, struct.pack("<4d", x0, y0, x1, y1))
         self.fill_count += 1
 
     def save(self):
@@ -521,10 +605,148 @@ def conic_paths(seed: int = 8, width: int = 300, height: int = 200, count: int =
     return sw
 
 
+def _stroke_figure(rng, x0, y0, side, closed: bool, curves: bool):
+    """One figure for stroking: lines, quads and cubics with control points in the bbox, some
+    points repeated or collinear (the stroker's degenerate branches)."""
+    n = int(rng.integers(1, 7))
+    pts = lambda k: rng.uniform(0.0, side, (k, 2)) + np.array([x0, y0])
+    p0 = pts(1)[0]
+    cmds, xy = [P_MOVE], [p0]
+    cur = p0
+    for _ in range(n):
+        kind = int(rng.integers(0, 3)) if curves else 0
+        r = float(rng.random())
+        if kind == 0:
+            q = pts(1)[0]
+            if r < 0.08:
+                q = cur.copy()                                     # zero-length line
+            elif r < 0.16:
+                q = cur + (cur - xy[-2] if len(xy) > 1 else np.array([3.0, 0.0]))   # collinear
+            cmds.append(P_ON); xy.append(q); cur = q
+        elif kind == 1:
+            c, q = pts(2)
+            if r < 0.15:
+                c = cur + (q - cur) * float(rng.uniform(-0.5, 1.5))       # collinear (cusp when outside)
+            cmds += [P_QUAD, P_ON]; xy += [c, q]; cur = q
+        else:
+            c1, c2, q = pts(3)
+            if r < 0.1:
+                t = rng.uniform(-0.5, 1.5, 2)
+                c1, c2 = cur + (q - cur) * t[0], cur + (q - cur) * t[1]   # flat cubic
+            elif r < 0.2:
+                c1, c2 = c2.copy(), c1.copy()
+                c2 = c1.copy()                                     # cusp-prone: equal controls
+            cmds += [P_CUBIC, P_CUBIC, P_ON]; xy += [c1, c2, q]; cur = q
+    if closed:
+        cmds.append(P_CLOSE); xy.append(np.array([np.nan, np.nan]))
+    return cmds, xy
+
+
+def strokes(seed: int = 9, width: int = 640, height: int = 480, count: int = 400, curves: bool = True,
+            max_width: float = 24.0) -> StreamWriter:
+    """Stroked geometry: open and closed paths (lines, quads, cubics, degenerate segments),
+    polylines, polygons, boxes, rects and lines, with every join, both caps drawn from all six,
+    miter limits 1-10, widths log-uniform 0.5..max_width, solid/gradient/pattern stroke styles,
+    stroke alpha, SrcOver/SrcCopy, rotated and scaled transforms in both transform orders."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sw = StreamWriter(width, height)
+    sw.solid(0xFF101010)
+    sw.fill_all()
+    sw.add_image(premultiplied_noise(rng, 64, 48))
+    for i in range(count):
+        side = float(_log_uniform(rng, 8.0, 200.0))
+        x0 = float(rng.uniform(-side * 0.3, max(-side * 0.3, width - side * 0.7)))
+        y0 = float(rng.uniform(-side * 0.3, max(-side * 0.3, height - side * 0.7)))
+        sw.stroke_width(float(_log_uniform(rng, 0.5, max_width)))
+        sw.stroke_join(int(rng.integers(0, 5)))
+        sw.stroke_caps(int(rng.integers(0, 6)), int(rng.integers(0, 6)))
+        sw.stroke_miter_limit(float(rng.uniform(1.0, 10.0)))
+        sw.comp_op(SRC_COPY if rng.random() < 0.15 else SRC_OVER)
+        r = float(rng.random())
+        if r < 0.6:
+            sw.stroke_solid(int(rng.integers(0, 2**32, dtype=np.uint64)) | (0xFF000000 if rng.random() < 0.5 else 0))
+        elif r < 0.85:
+            kind = int(rng.integers(0, 3))
+            stops = _random_stops(rng, int(rng.integers(2, 6)))
+            if kind == LINEAR:
+                p = rng.uniform(0, side, 4) + np.array([x0, y0, x0, y0])
+                sw.stroke_gradient(LINEAR, p.tolist(), int(rng.integers(0, 3)), stops)
+            elif kind == RADIAL:
+                c = rng.uniform(0, side, 2) + np.array([x0, y0])
+                sw.stroke_gradient(RADIAL, [c[0], c[1], c[0], c[1], side * 0.5, 0.0], int(rng.integers(0, 3)), stops)
+            else:
+                c = rng.uniform(0, side, 2) + np.array([x0, y0])
+                sw.stroke_gradient(CONIC, [c[0], c[1], float(rng.uniform(0, 2 * math.pi)), 1.0], 0, stops)
+        else:
+            sw.hint(HINT_PATTERN_QUALITY, int(rng.integers(0, 2)))
+            sw.stroke_pattern(0, int(rng.integers(0, 3)), transform=[1.0, 0.0, 0.0, 1.0, x0, y0])
+        if rng.random() < 0.1:
+            sw.stroke_alpha(float(rng.uniform(0.2, 1.0)))
+        elif rng.random() < 0.1:
+            sw.stroke_alpha(1.0)
+        t = float(rng.random())
+        if t < 0.2:
+            a = float(rng.uniform(-0.6, 0.6))
+            sc = float(_log_uniform(rng, 0.5, 2.0))
+            sn, c = _sincos(a)
+            sw.transform([c * sc, sn * sc, -sn * sc * 0.8, c * sc * 0.8, 15.0, -7.5])
+            sw.stroke_transform_order(int(rng.integers(0, 2)))
+        elif t < 0.3:
+            sw.transform([1.5, 0.0, 0.0, 0.75, -10.0, 20.0])
+        elif t < 0.5:
+            sw.reset_transform()
+        g = float(rng.random())
+        if g < 0.45:
+            cmds, xy = [], []
+            for f in range(int(rng.integers(1, 3))):
+                fc, fxy = _stroke_figure(rng, x0, y0, side, closed=rng.random() < 0.4, curves=curves)
+                cmds += fc; xy += fxy
+            sw.stroke_path(cmds, np.array(xy))
+        elif g < 0.65:
+            k = int(rng.integers(2, 10))
+            sw.stroke_polyline(rng.uniform(0, side, (k, 2)) + np.array([x0, y0]))
+        elif g < 0.8:
+            k = int(rng.integers(3, 10))
+            sw.stroke_polygon(rng.uniform(0, side, (k, 2)) + np.array([x0, y0]))
+        elif g < 0.88:
+            sw.stroke_box_d(x0, y0, x0 + side * float(rng.random()), y0 + side * float(rng.random()))
+        elif g < 0.94:
+            sw.stroke_rect_d(x0, y0, side * float(rng.random()), side * float(rng.random()))
+        else:
+            p = rng.uniform(0, side, 4) + np.array([x0, y0, x0, y0])
+            sw.stroke_line_d(*p.tolist())
+    return sw
+
+
+def stroked_paths(seed: int = 10, width: int = 1920, height: int = 1080, count: int = 20000) -> StreamWriter:
+    """Stroking benchmark: `count` open cubic paths (2-6 segments, bbox side log-uniform 8-256 px)
+    stroked with widths log-uniform 1-16 px, round/miter/bevel joins and butt/square/round caps,
+    solid colours, SrcOver, identity transform."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sw = StreamWriter(width, height)
+    sw.solid(0xFF000000)
+    sw.fill_all()
+    for i in range(count):
+        side = float(_log_uniform(rng, 8.0, 256.0))
+        x0 = float(rng.uniform(-side * 0.5, width - side * 0.5))
+        y0 = float(rng.uniform(-side * 0.5, height - side * 0.5))
+        sw.stroke_width(float(_log_uniform(rng, 1.0, 16.0)))
+        sw.stroke_join((JOIN_ROUND, JOIN_MITER_CLIP, JOIN_BEVEL)[i % 3])
+        cap = (CAP_BUTT, CAP_SQUARE, CAP_ROUND)[(i // 3) % 3]
+        sw.stroke_caps(cap, cap)
+        sw.stroke_solid(int(rng.integers(0, 2**32, dtype=np.uint64)))
+        nseg = int(rng.integers(2, 7))
+        pts = rng.uniform(0.0, side, (3 * nseg + 1, 2)) + np.array([x0, y0])
+        cmds = [P_MOVE] + [P_CUBIC, P_CUBIC, P_ON] * nseg
+        sw.stroke_path(cmds, pts)
+    return sw
+
+
 WORKLOADS = {
     "polygons": polygons,
     "curves": curves,
     "patterns": patterns,
+    "strokes": stroked_paths,
 }
 
 

@@ -63,6 +63,22 @@ enum {
   BLGPU_OP_FILL_PATH_D = 17,       /* u32 n, u32 pad, u8 cmd[n] (pad 8), f64 xy[2n] bl_context_fill_path_d */
   BLGPU_OP_SAVE = 18,              /* -                                            bl_context_save */
   BLGPU_OP_RESTORE = 19,           /* -                                            bl_context_restore */
+  /* stroking (stroke style slot, stroke options; rastercontext.cpp:2059-2165, :3794-3870) */
+  BLGPU_OP_SET_STROKE_WIDTH = 20,  /* f64 width                                    bl_context_set_stroke_width */
+  BLGPU_OP_SET_STROKE_MITER_LIMIT = 21, /* f64 miter_limit                         bl_context_set_stroke_miter_limit */
+  BLGPU_OP_SET_STROKE_JOIN = 22,   /* u32 join, u32 pad                            bl_context_set_stroke_join */
+  BLGPU_OP_SET_STROKE_CAPS = 23,   /* u32 start_cap, u32 end_cap                   bl_context_set_stroke_cap x2 */
+  BLGPU_OP_SET_STROKE_TRANSFORM_ORDER = 24, /* u32 order, u32 pad                  bl_context_set_stroke_transform_order */
+  BLGPU_OP_SET_STROKE_ALPHA = 25,  /* f64 alpha                                    bl_context_set_stroke_alpha */
+  BLGPU_OP_STROKE_STYLE_RGBA32 = 26,   /* u32 argb32, u32 pad                      bl_context_set_stroke_style_rgba32 */
+  BLGPU_OP_STROKE_STYLE_GRADIENT = 27, /* BLGpuStreamGradient + stops[]            bl_context_set_stroke_style(BLGradient) */
+  BLGPU_OP_STROKE_STYLE_PATTERN = 28,  /* BLGpuStreamPattern                       bl_context_set_stroke_style(BLPattern) */
+  BLGPU_OP_STROKE_PATH_D = 29,     /* u32 n, u32 pad, u8 cmd[n] (pad 8), f64 xy[2n] bl_context_stroke_path_d */
+  BLGPU_OP_STROKE_POLYLINE_D = 30, /* u32 n, u32 pad, f64 xy[2n]                   stroke_geometry(POLYLINED) */
+  BLGPU_OP_STROKE_POLYGON_D = 31,  /* u32 n, u32 pad, f64 xy[2n]                   stroke_geometry(POLYGOND) */
+  BLGPU_OP_STROKE_BOX_D = 32,      /* f64 x0, y0, x1, y1                           stroke_geometry(BOXD) */
+  BLGPU_OP_STROKE_RECT_D = 33,     /* f64 x, y, w, h                               stroke_geometry(RECTD) */
+  BLGPU_OP_STROKE_LINE_D = 34,     /* f64 x0, y0, x1, y1                           stroke_geometry(LINE) */
   BLGPU_OP_COUNT
 };
 

@@ -11,6 +11,7 @@
  *   band height          blend2d/raster/rastercontext.cpp:4154-4193
  */
 #include "b2d_oracle_p.h"
+#include "b2d_oracle_stroke.h"
 #include "blgpu_stream.h"
 
 /* ============================================================================================
@@ -330,7 +331,11 @@ typedef struct {
   OMat user, final_t, final_fixed;
   int final_type, final_fixed_type;
   int integral_translation, tx_i, ty_i;
-  OStyle style;
+  OStyle style;                       /* BL_CONTEXT_STYLE_SLOT_FILL */
+  OStyle stroke_style;                /* BL_CONTEXT_STYLE_SLOT_STROKE */
+  double stroke_alpha;
+  uint32_t stroke_alpha_i;
+  OStrokeOpts stroke;
 } OState;
 
 typedef struct {
@@ -372,18 +377,20 @@ static void on_transform_changed(OCtx* c) {   /* rastercontext.cpp:741-800 */
   }
 }
 
-static void set_style_solid(OCtx* c, uint32_t rgba32) {
-  OStyle* st = &c->s.style;
+static inline OStyle* slot_style(OCtx* c, int slot) { return slot ? &c->s.stroke_style : &c->s.style; }
+
+static void set_style_solid(OCtx* c, int slot, uint32_t rgba32) {
+  OStyle* st = slot_style(c, slot);
   st->nop = 0;
   st->fetch_type = O_FT_SOLID;
   st->solid = o_premultiply(rgba32);
   st->format = rgba32 == 0 ? O_FMT_ZERO32 : (rgba32 >= 0xFF000000u ? O_FMT_FRGB32 : O_FMT_PRGB32);
 }
 
-static void set_style_gradient(OCtx* c, const uint8_t* p) {
+static void set_style_gradient(OCtx* c, int slot, const uint8_t* p) {
   BLGpuStreamGradient g;
   memcpy(&g, p, sizeof(g));
-  OStyle* st = &c->s.style;
+  OStyle* st = slot_style(c, slot);
   memset(st, 0, sizeof(*st));
   BLGpuStreamGradientStop* raw = (BLGpuStreamGradientStop*)malloc(sizeof(BLGpuStreamGradientStop) * (g.stop_count + 1));
   memcpy(raw, p + sizeof(g), sizeof(BLGpuStreamGradientStop) * g.stop_count);
@@ -446,10 +453,10 @@ done:
   free(stops);
 }
 
-static void set_style_pattern(OCtx* c, const uint8_t* p) {
+static void set_style_pattern(OCtx* c, int slot, const uint8_t* p) {
   BLGpuStreamPattern pt;
   memcpy(&pt, p, sizeof(pt));
-  OStyle* st = &c->s.style;
+  OStyle* st = slot_style(c, slot);
   memset(st, 0, sizeof(*st));
   int iw = c->iw[pt.image_index], ih = c->ih[pt.image_index];
   int ax = 0, ay = 0, aw = iw, ah = ih;
@@ -468,18 +475,21 @@ static void set_style_pattern(OCtx* c, const uint8_t* p) {
 }
 
 /* Resolve the fill: returns 0 for NOP, else sets comp-op (0/1) and alpha. */
-static int resolve_fill(OCtx* c, int* comp_op, uint32_t* alpha) {
+static int resolve_slot(OCtx* c, int slot, int* comp_op, uint32_t* alpha) {
   OState* s = &c->s;
-  if (s->global_alpha_i == 0 || s->fill_alpha_i == 0 || s->style.nop) return 0;
+  const OStyle* st = slot_style(c, slot);
+  uint32_t a = slot ? s->stroke_alpha_i : s->fill_alpha_i;
+  if (s->global_alpha_i == 0 || a == 0 || st->nop) return 0;
   int op = s->comp_op;
   if (op == 0) {   /* SrcOver simplification for a PRGB32 destination */
-    if (s->style.format == O_FMT_ZERO32) return 0;        /* DstCopy */
-    if (s->style.format == O_FMT_FRGB32) op = 1;          /* SrcCopy */
+    if (st->format == O_FMT_ZERO32) return 0;             /* DstCopy */
+    if (st->format == O_FMT_FRGB32) op = 1;               /* SrcCopy */
   }
   *comp_op = op;
-  *alpha = s->fill_alpha_i;
+  *alpha = a;
   return 1;
 }
+static int resolve_fill(OCtx* c, int* comp_op, uint32_t* alpha) { return resolve_slot(c, 0, comp_op, alpha); }
 
 static void fill_box_a(OCtx* c, int x0, int y0, int x1, int y1) {
   if (c->stats) c->stats->fill_calls++;
@@ -530,6 +540,137 @@ static void fill_box_d(OCtx* c, double bx0, double by0, double bx1, double by1) 
   }
 }
 
+/* --- stroking -------------------------------------------------------------------------------
+ * stroke_unclipped_geometry / stroke_unclipped_path<kSync> (rastercontext.cpp:3180-3234) with
+ * add_stroked_path_edges (rastercontextops_p.h:95-140) and stroke_geometry_sink
+ * (rastercontextops.cpp:61-74): the outline of every figure goes into one edge builder - A and C
+ * as open paths, B reversed (closed when it ends with CLOSE) - and the edges are filled non-zero
+ * with the stroke style. A stroke that fails (invalid geometry) fills nothing. */
+
+typedef struct { OCtx* c; OMat m; int ttype; OPath rev; int failed; } OStrokeEdges;
+
+/* EdgeSourceReversePathFromStrokeSink (edgebuilder_p.h:287-405) as a forward path: the last
+ * on-point first, then every segment backwards. Returns the closed flag (must_close). */
+static int reverse_stroke_path(const OPath* b, OPath* out) {
+  out->n = 0;
+  size_t n = b->n;
+  int must_close = n > 0 && b->cmd[n - 1] == 5;
+  n -= (size_t)must_close;
+  if (n == 0 || b->cmd[n - 1] != 1) return must_close;          /* begin(): needs an on-point */
+  size_t i = n - 1;
+  o_path_reserve(out, n);
+  out->cmd[out->n] = 0; out->vtx[out->n++] = b->vtx[i];
+  while (i > 0) {
+    uint8_t k = b->cmd[i - 1];
+    if (k <= 1) { out->cmd[out->n] = 1; out->vtx[out->n++] = b->vtx[i - 1]; i -= 1; }
+    else if (k == 2 && i >= 2) {
+      out->cmd[out->n] = 2; out->vtx[out->n++] = b->vtx[i - 1];
+      out->cmd[out->n] = 1; out->vtx[out->n++] = b->vtx[i - 2];
+      i -= 2;
+    }
+    else if (k == 4 && i >= 3) {
+      out->cmd[out->n] = 4; out->vtx[out->n++] = b->vtx[i - 1];
+      out->cmd[out->n] = 4; out->vtx[out->n++] = b->vtx[i - 2];
+      out->cmd[out->n] = 1; out->vtx[out->n++] = b->vtx[i - 3];
+      i -= 3;
+    }
+    else break;
+  }
+  return must_close;
+}
+
+static int stroke_edges_sink(const OPath* a, const OPath* b, const OPath* cpath, void* user) {
+  OStrokeEdges* se = (OStrokeEdges*)user;
+  OEdgeBuilder* eb = &se->c->eb;
+  if (o_eb_add_path_ex(eb, a->cmd, (const double*)a->vtx, a->n, &se->m, se->ttype, 0)) return 2;
+  int closed = reverse_stroke_path(b, &se->rev);
+  if (o_eb_add_path_ex(eb, se->rev.cmd, (const double*)se->rev.vtx, se->rev.n, &se->m, se->ttype, closed)) return 2;
+  if (cpath->n && o_eb_add_path_ex(eb, cpath->cmd, (const double*)cpath->vtx, cpath->n, &se->m, se->ttype, 0)) return 2;
+  return 0;
+}
+
+static void stroke_op(OCtx* c, uint32_t op, const uint8_t* p) {
+  OState* s = &c->s;
+  int cop; uint32_t alpha;
+  /* the input path (BLPath::add_geometry, path.cpp:1335-1660; direction CW) */
+  OPath in;
+  memset(&in, 0, sizeof(in));
+  uint32_t n = 0;
+  if (op == BLGPU_OP_STROKE_PATH_D || op == BLGPU_OP_STROKE_POLYLINE_D || op == BLGPU_OP_STROKE_POLYGON_D) {
+    memcpy(&n, p, 4);
+    if (c->stats) c->stats->input_vertices += n;
+  }
+  if (!resolve_slot(c, 1, &cop, &alpha)) return;
+  switch (op) {
+    case BLGPU_OP_STROKE_PATH_D: {
+      if (n == 0) return;
+      o_path_reserve(&in, n);
+      memcpy(in.cmd, p + 8, n);
+      memcpy(in.vtx, p + 8 + ((n + 7u) & ~7u), sizeof(double) * 2 * n);
+      in.n = n;
+      break;
+    }
+    case BLGPU_OP_STROKE_POLYLINE_D: case BLGPU_OP_STROKE_POLYGON_D: {
+      if (n == 0) return;
+      o_path_reserve(&in, n + 1);
+      memcpy(in.vtx, p + 8, sizeof(double) * 2 * n);
+      for (uint32_t i = 0; i < n; i++) in.cmd[i] = i ? 1 : 0;
+      in.n = n;
+      if (op == BLGPU_OP_STROKE_POLYGON_D) { in.cmd[n] = 5; in.vtx[n].x = NAN; in.vtx[n].y = NAN; in.n = n + 1; }
+      break;
+    }
+    case BLGPU_OP_STROKE_LINE_D: {
+      double v[4]; memcpy(v, p, sizeof(v));
+      o_path_reserve(&in, 2);
+      in.cmd[0] = 0; in.vtx[0].x = v[0]; in.vtx[0].y = v[1];
+      in.cmd[1] = 1; in.vtx[1].x = v[2]; in.vtx[1].y = v[3];
+      in.n = 2;
+      break;
+    }
+    default: {   /* BOX_D, RECT_D: PathAppender::add_box (path_p.h:420-442) */
+      double v[4]; memcpy(v, p, sizeof(v));
+      double x0 = v[0], y0 = v[1], x1 = v[2], y1 = v[3];
+      if (op == BLGPU_OP_STROKE_RECT_D) { x1 = v[2] + v[0]; y1 = v[3] + v[1]; }
+      o_path_reserve(&in, 5);
+      static const uint8_t box_cmd[5] = { 0, 1, 1, 1, 5 };
+      memcpy(in.cmd, box_cmd, 5);
+      in.vtx[0].x = x0; in.vtx[0].y = y0; in.vtx[1].x = x1; in.vtx[1].y = y0;
+      in.vtx[2].x = x1; in.vtx[2].y = y1; in.vtx[3].x = x0; in.vtx[3].y = y1;
+      in.vtx[4].x = NAN; in.vtx[4].y = NAN;
+      in.n = 5;
+      break;
+    }
+  }
+  OStrokeEdges se;
+  memset(&se, 0, sizeof(se));
+  se.c = c;
+  se.m = s->final_fixed;             /* final_transform_fixed(origin_fixed), origin (0, 0) */
+  se.ttype = s->final_fixed_type;
+  if (s->stroke.transform_order != 0) {
+    /* BEFORE: the path is transformed by the user transform without its translation
+     * (DirectStateAccessor::user_transform, rastercontext.cpp:168-171) first; the edges then use
+     * the meta transform (identity here, scaled to 24.8) with the final transform's origin. */
+    OMat lin = s->user;
+    lin.m20 = 0.0; lin.m21 = 0.0;
+    for (size_t i = 0; i < in.n; i++) in.vtx[i] = o_mat_map(&lin, in.vtx[i].x, in.vtx[i].y);
+    OMat meta = { 256.0, 0.0, 0.0, 256.0, s->final_fixed.m20, s->final_fixed.m21 };
+    se.m = meta;
+    se.ttype = O_TT_SCALE;
+  }
+  OPath a, b, cp;
+  memset(&a, 0, sizeof(a)); memset(&b, 0, sizeof(b)); memset(&cp, 0, sizeof(cp));
+  o_storage_clear(&c->storage);
+  o_eb_begin(&c->eb);
+  int rc = o_stroke_path(in.cmd, (const double*)in.vtx, in.n, &s->stroke, 0.05, 0.414213562,
+                         &a, &b, &cp, stroke_edges_sink, &se);
+  if (rc == 0) {
+    o_eb_done(&c->eb);
+    c->fc.style = &s->stroke_style; c->fc.comp_op = cop; c->fc.alpha = alpha;
+    fill_edges(c, 0 /* NON_ZERO */);
+  }
+  o_path_free(&a); o_path_free(&b); o_path_free(&cp); o_path_free(&se.rev); o_path_free(&in);
+}
+
 static int replay(OCtx* c, const uint8_t* base, size_t size, size_t off) {
   while (off + 8 <= size) {
     uint32_t op, len;
@@ -553,6 +694,7 @@ static int replay(OCtx* c, const uint8_t* base, size_t size, size_t off) {
         s->global_alpha = a;
         s->global_alpha_i = (uint32_t)o_round_to_int(ia);
         s->fill_alpha_i = (uint32_t)o_round_to_int(ia * s->fill_alpha);
+        s->stroke_alpha_i = (uint32_t)o_round_to_int(ia * s->stroke_alpha);
         break;
       }
       case BLGPU_OP_SET_FILL_ALPHA: {
@@ -581,9 +723,34 @@ static int replay(OCtx* c, const uint8_t* base, size_t size, size_t off) {
         on_transform_changed(c);
         break;
       }
-      case BLGPU_OP_STYLE_RGBA32: { uint32_t v; memcpy(&v, p, 4); set_style_solid(c, v); break; }
-      case BLGPU_OP_STYLE_GRADIENT: set_style_gradient(c, p); break;
-      case BLGPU_OP_STYLE_PATTERN: set_style_pattern(c, p); break;
+      case BLGPU_OP_STYLE_RGBA32: { uint32_t v; memcpy(&v, p, 4); set_style_solid(c, 0, v); break; }
+      case BLGPU_OP_STYLE_GRADIENT: set_style_gradient(c, 0, p); break;
+      case BLGPU_OP_STYLE_PATTERN: set_style_pattern(c, 0, p); break;
+      case BLGPU_OP_STROKE_STYLE_RGBA32: { uint32_t v; memcpy(&v, p, 4); set_style_solid(c, 1, v); break; }
+      case BLGPU_OP_STROKE_STYLE_GRADIENT: set_style_gradient(c, 1, p); break;
+      case BLGPU_OP_STROKE_STYLE_PATTERN: set_style_pattern(c, 1, p); break;
+      case BLGPU_OP_SET_STROKE_ALPHA: {      /* set_style_alpha (rastercontext.cpp:1920-1939) */
+        double a; memcpy(&a, p, 8);
+        if (isnan(a)) break;
+        a = o_clamp(a, 0.0, 1.0);
+        s->stroke_alpha = a;
+        s->stroke_alpha_i = (uint32_t)o_round_to_int(s->global_alpha * 255.0 * a);
+        break;
+      }
+      case BLGPU_OP_SET_STROKE_WIDTH: memcpy(&s->stroke.width, p, 8); break;
+      case BLGPU_OP_SET_STROKE_MITER_LIMIT: memcpy(&s->stroke.miter_limit, p, 8); break;
+      case BLGPU_OP_SET_STROKE_JOIN: { uint32_t v; memcpy(&v, p, 4); if (v <= 4u) s->stroke.join = v; break; }
+      case BLGPU_OP_SET_STROKE_CAPS: {
+        uint32_t v[2]; memcpy(v, p, 8);
+        if (v[0] <= 5u) s->stroke.start_cap = v[0];
+        if (v[1] <= 5u) s->stroke.end_cap = v[1];
+        break;
+      }
+      case BLGPU_OP_SET_STROKE_TRANSFORM_ORDER: { uint32_t v; memcpy(&v, p, 4); if (v <= 1u) s->stroke.transform_order = v; break; }
+      case BLGPU_OP_STROKE_PATH_D: case BLGPU_OP_STROKE_POLYLINE_D: case BLGPU_OP_STROKE_POLYGON_D:
+      case BLGPU_OP_STROKE_BOX_D: case BLGPU_OP_STROKE_RECT_D: case BLGPU_OP_STROKE_LINE_D:
+        stroke_op(c, op, p);
+        break;
 
       case BLGPU_OP_CLEAR_ALL: {
         OStyle clear_style;
@@ -732,7 +899,10 @@ int b2d_oracle_render(const uint8_t* stream, size_t size, uint32_t* out, const B
   OMat id = { 1, 0, 0, 1, 0, 0 };
   c.s.user = id;
   on_transform_changed(&c);
-  set_style_solid(&c, 0xFF000000u);
+  set_style_solid(&c, 0, 0xFF000000u);
+  set_style_solid(&c, 1, 0xFF000000u);
+  c.s.stroke_alpha = 1.0; c.s.stroke_alpha_i = 255;
+  c.s.stroke.width = 1.0; c.s.stroke.miter_limit = 4.0;   /* bl_stroke_options_init (path.cpp:186-190) */
 
   int bh = (opt && opt->band_height) ? (int)opt->band_height : default_band_height(c.w);
   o_storage_init(&c.storage, c.w, c.h, bh);

@@ -1152,10 +1152,17 @@ int o_eb_add_poly(OEdgeBuilder* eb, const double* xy, size_t n, const OMat* m, i
 }
 
 int o_eb_add_path(OEdgeBuilder* eb, const uint8_t* cmd, const double* xy, size_t n, const OMat* m, int ttype) {
+  return o_eb_add_path_ex(eb, cmd, xy, n, m, ttype, 1);
+}
+
+/* add_path(view, closed, transform, type) (edgebuilder_p.h:990-1002): `closed` = 0 leaves figures
+ * without a CLOSE command open (the stroker's A and C paths). */
+int o_eb_add_path_ex(OEdgeBuilder* eb, const uint8_t* cmd, const double* xy, size_t n, const OMat* m, int ttype,
+                     int closed) {
   OSrc s;
   memset(&s, 0, sizeof(s));
   s.is_path = 1; s.xy = xy; s.cmd = cmd; s.i = 0; s.n = (long)n; s.m = *m; s.affine = ttype > O_TT_SCALE;
-  return eb_add_from_source(eb, &s, 1);
+  return eb_add_from_source(eb, &s, closed);
 }
 
 /* ============================================================================================

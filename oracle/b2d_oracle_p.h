@@ -113,6 +113,8 @@ void o_eb_begin(OEdgeBuilder* eb);
 /* Polygon / path edge building (edgebuilder_p.h:959-1070). Returns 0 or an error. */
 int o_eb_add_poly(OEdgeBuilder* eb, const double* xy, size_t n, const OMat* m, int ttype);
 int o_eb_add_path(OEdgeBuilder* eb, const uint8_t* cmd, const double* xy, size_t n, const OMat* m, int ttype);
+int o_eb_add_path_ex(OEdgeBuilder* eb, const uint8_t* cmd, const double* xy, size_t n, const OMat* m, int ttype,
+                     int closed);
 int o_eb_done(OEdgeBuilder* eb);
 
 /* --- analytic fill --------------------------------------------------------------------- */

@@ -66,6 +66,53 @@ static void parse_header(Stream& s) {
 template<typename T>
 static T rd(const uint8_t* p) { T v; memcpy(&v, p, sizeof(T)); return v; }
 
+static BLGradient make_gradient(const uint8_t* p) {
+  BLGpuStreamGradient g = rd<BLGpuStreamGradient>(p);
+  std::vector<BLGradientStop> stops(g.stop_count);
+  for (uint32_t i = 0; i < g.stop_count; i++) {
+    BLGpuStreamGradientStop st = rd<BLGpuStreamGradientStop>(p + sizeof(g) + i * sizeof(st));
+    stops[i] = BLGradientStop(st.offset, BLRgba64(st.rgba64));
+  }
+  BLGradient grad;
+  if (g.type == BLGPU_GRADIENT_LINEAR)
+    grad.create(BLLinearGradientValues(g.values[0], g.values[1], g.values[2], g.values[3]), BLExtendMode(g.extend_mode));
+  else if (g.type == BLGPU_GRADIENT_RADIAL)
+    grad.create(BLRadialGradientValues(g.values[0], g.values[1], g.values[2], g.values[3], g.values[4], g.values[5]), BLExtendMode(g.extend_mode));
+  else
+    grad.create(BLConicGradientValues(g.values[0], g.values[1], g.values[2], g.values[3]), BLExtendMode(g.extend_mode));
+  grad.assign_stops(stops.data(), stops.size());
+  if (g.has_transform)
+    grad.set_transform(BLMatrix2D(g.transform[0], g.transform[1], g.transform[2], g.transform[3], g.transform[4], g.transform[5]));
+  return grad;
+}
+
+static BLPattern make_pattern(const Stream& s, const uint8_t* p) {
+  BLGpuStreamPattern pt = rd<BLGpuStreamPattern>(p);
+  const BLImage& src = s.images[pt.image_index];
+  BLPattern pat;
+  if (pt.area[2] > 0)
+    pat.create(src, BLRectI(pt.area[0], pt.area[1], pt.area[2], pt.area[3]), BLExtendMode(pt.extend_mode));
+  else
+    pat.create(src, BLExtendMode(pt.extend_mode));
+  if (pt.has_transform)
+    pat.set_transform(BLMatrix2D(pt.transform[0], pt.transform[1], pt.transform[2], pt.transform[3], pt.transform[4], pt.transform[5]));
+  return pat;
+}
+
+// u32 n, u32 pad, u8 cmd[n] (padded to 8), f64 xy[2n]
+static BLPath read_path(const uint8_t* p) {
+  uint32_t n = rd<uint32_t>(p);
+  const uint8_t* cmds = p + 8;
+  const uint8_t* xy = cmds + ((n + 7u) & ~7u);
+  BLPath path;
+  uint8_t* cmd_out;
+  BLPoint* vtx_out;
+  path.modify_op(BL_MODIFY_OP_ASSIGN_GROW, n, &cmd_out, &vtx_out);
+  memcpy(cmd_out, cmds, n);
+  memcpy(vtx_out, xy, size_t(n) * sizeof(BLPoint));
+  return path;
+}
+
 static void replay(const Stream& s, BLImage& img, uint32_t threads) {
   BLImageData d;
   img.make_mutable(&d);
@@ -100,39 +147,32 @@ static void replay(const Stream& s, BLImage& img, uint32_t threads) {
       }
       case BLGPU_OP_RESET_TRANSFORM: ctx.reset_transform(); break;
       case BLGPU_OP_STYLE_RGBA32: ctx.set_fill_style(BLRgba32(rd<uint32_t>(p))); break;
-      case BLGPU_OP_STYLE_GRADIENT: {
-        BLGpuStreamGradient g = rd<BLGpuStreamGradient>(p);
-        std::vector<BLGradientStop> stops(g.stop_count);
-        for (uint32_t i = 0; i < g.stop_count; i++) {
-          BLGpuStreamGradientStop st = rd<BLGpuStreamGradientStop>(p + sizeof(g) + i * sizeof(st));
-          stops[i] = BLGradientStop(st.offset, BLRgba64(st.rgba64));
-        }
-        BLGradient grad;
-        if (g.type == BLGPU_GRADIENT_LINEAR)
-          grad.create(BLLinearGradientValues(g.values[0], g.values[1], g.values[2], g.values[3]), BLExtendMode(g.extend_mode));
-        else if (g.type == BLGPU_GRADIENT_RADIAL)
-          grad.create(BLRadialGradientValues(g.values[0], g.values[1], g.values[2], g.values[3], g.values[4], g.values[5]), BLExtendMode(g.extend_mode));
-        else
-          grad.create(BLConicGradientValues(g.values[0], g.values[1], g.values[2], g.values[3]), BLExtendMode(g.extend_mode));
-        grad.assign_stops(stops.data(), stops.size());
-        if (g.has_transform)
-          grad.set_transform(BLMatrix2D(g.transform[0], g.transform[1], g.transform[2], g.transform[3], g.transform[4], g.transform[5]));
-        ctx.set_fill_style(grad);
+      case BLGPU_OP_STYLE_GRADIENT: ctx.set_fill_style(make_gradient(p)); break;
+      case BLGPU_OP_STYLE_PATTERN: ctx.set_fill_style(make_pattern(s, p)); break;
+      case BLGPU_OP_STROKE_STYLE_RGBA32: ctx.set_stroke_style(BLRgba32(rd<uint32_t>(p))); break;
+      case BLGPU_OP_STROKE_STYLE_GRADIENT: ctx.set_stroke_style(make_gradient(p)); break;
+      case BLGPU_OP_STROKE_STYLE_PATTERN: ctx.set_stroke_style(make_pattern(s, p)); break;
+      case BLGPU_OP_SET_STROKE_ALPHA: ctx.set_stroke_alpha(rd<double>(p)); break;
+      case BLGPU_OP_SET_STROKE_WIDTH: ctx.set_stroke_width(rd<double>(p)); break;
+      case BLGPU_OP_SET_STROKE_MITER_LIMIT: ctx.set_stroke_miter_limit(rd<double>(p)); break;
+      case BLGPU_OP_SET_STROKE_JOIN: ctx.set_stroke_join(BLStrokeJoin(rd<uint32_t>(p))); break;
+      case BLGPU_OP_SET_STROKE_CAPS:
+        ctx.set_stroke_cap(BL_STROKE_CAP_POSITION_START, BLStrokeCap(rd<uint32_t>(p)));
+        ctx.set_stroke_cap(BL_STROKE_CAP_POSITION_END, BLStrokeCap(rd<uint32_t>(p + 4)));
+        break;
+      case BLGPU_OP_SET_STROKE_TRANSFORM_ORDER: ctx.set_stroke_transform_order(BLStrokeTransformOrder(rd<uint32_t>(p))); break;
+      case BLGPU_OP_STROKE_PATH_D: ctx.stroke_path(read_path(p)); break;
+      case BLGPU_OP_STROKE_POLYLINE_D: case BLGPU_OP_STROKE_POLYGON_D: {
+        uint32_t n = rd<uint32_t>(p);
+        pts.resize(n);
+        memcpy(pts.data(), p + 8, size_t(n) * sizeof(BLPoint));
+        if (op == BLGPU_OP_STROKE_POLYLINE_D) ctx.stroke_polyline(pts.data(), n);
+        else ctx.stroke_polygon(pts.data(), n);
         break;
       }
-      case BLGPU_OP_STYLE_PATTERN: {
-        BLGpuStreamPattern pt = rd<BLGpuStreamPattern>(p);
-        const BLImage& src = s.images[pt.image_index];
-        BLPattern pat;
-        if (pt.area[2] > 0)
-          pat.create(src, BLRectI(pt.area[0], pt.area[1], pt.area[2], pt.area[3]), BLExtendMode(pt.extend_mode));
-        else
-          pat.create(src, BLExtendMode(pt.extend_mode));
-        if (pt.has_transform)
-          pat.set_transform(BLMatrix2D(pt.transform[0], pt.transform[1], pt.transform[2], pt.transform[3], pt.transform[4], pt.transform[5]));
-        ctx.set_fill_style(pat);
-        break;
-      }
+      case BLGPU_OP_STROKE_BOX_D: { double b[4]; memcpy(b, p, sizeof(b)); ctx.stroke_box(BLBox(b[0], b[1], b[2], b[3])); break; }
+      case BLGPU_OP_STROKE_RECT_D: { double r[4]; memcpy(r, p, sizeof(r)); ctx.stroke_rect(BLRect(r[0], r[1], r[2], r[3])); break; }
+      case BLGPU_OP_STROKE_LINE_D: { double l[4]; memcpy(l, p, sizeof(l)); ctx.stroke_line(BLLine(l[0], l[1], l[2], l[3])); break; }
       case BLGPU_OP_CLEAR_ALL: ctx.clear_all(); break;
       case BLGPU_OP_FILL_ALL: ctx.fill_all(); break;
       case BLGPU_OP_FILL_RECT_I: {
@@ -160,19 +200,7 @@ static void replay(const Stream& s, BLImage& img, uint32_t threads) {
         ctx.fill_polygon(pts.data(), n);
         break;
       }
-      case BLGPU_OP_FILL_PATH_D: {
-        uint32_t n = rd<uint32_t>(p);
-        const uint8_t* cmds = p + 8;
-        const uint8_t* xy = cmds + ((n + 7u) & ~7u);
-        BLPath path;
-        uint8_t* cmd_out;
-        BLPoint* vtx_out;
-        path.modify_op(BL_MODIFY_OP_ASSIGN_GROW, n, &cmd_out, &vtx_out);
-        memcpy(cmd_out, cmds, n);
-        memcpy(vtx_out, xy, size_t(n) * sizeof(BLPoint));
-        ctx.fill_path(path);
-        break;
-      }
+      case BLGPU_OP_FILL_PATH_D: ctx.fill_path(read_path(p)); break;
       case BLGPU_OP_SAVE: ctx.save(); break;
       case BLGPU_OP_RESTORE: ctx.restore(); break;
       default:
