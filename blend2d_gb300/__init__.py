@@ -24,6 +24,7 @@ ERROR_INVALID_STATE = 0x00010002
 ERROR_NOT_IMPLEMENTED = 0x00010007
 ERROR_NO_STATES_TO_RESTORE = 0x00010038
 ERROR_DATA_TOO_LARGE = 0x00010032
+ERROR_INVALID_GEOMETRY = 0x00010034
 ERROR_DEVICE = 0x00011000
 
 FORMAT_PRGB32 = 1
@@ -69,6 +70,11 @@ class Gradient(ctypes.Structure):
 class Pattern(ctypes.Structure):
     _fields_ = [("image", ctypes.POINTER(Image)), ("area", ctypes.c_int32 * 4), ("extend_mode", ctypes.c_uint32),
                 ("transform", ctypes.POINTER(ctypes.c_double))]
+
+
+class StrokeOptions(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_double), ("miter_limit", ctypes.c_double), ("join", ctypes.c_uint32),
+                ("start_cap", ctypes.c_uint32), ("end_cap", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class LaunchConfig(ctypes.Structure):
@@ -125,6 +131,24 @@ _SIGNATURES = {
     "blgpu_context_fill_box_d": [_P, _D, _D, _D, _D],
     "blgpu_context_fill_polygon_d": [_P, _P, ctypes.c_size_t],
     "blgpu_context_fill_path_d": [_P, _P, _P, ctypes.c_size_t],
+    "blgpu_context_set_stroke_style_rgba32": [_P, _U32],
+    "blgpu_context_set_stroke_style_gradient": [_P, ctypes.POINTER(Gradient)],
+    "blgpu_context_set_stroke_style_pattern": [_P, ctypes.POINTER(Pattern)],
+    "blgpu_context_set_stroke_alpha": [_P, _D],
+    "blgpu_context_set_stroke_width": [_P, _D],
+    "blgpu_context_set_stroke_miter_limit": [_P, _D],
+    "blgpu_context_set_stroke_join": [_P, _U32],
+    "blgpu_context_set_stroke_cap": [_P, _U32, _U32],
+    "blgpu_context_set_stroke_caps": [_P, _U32],
+    "blgpu_context_set_stroke_transform_order": [_P, _U32],
+    "blgpu_context_stroke_path_d": [_P, _P, _P, ctypes.c_size_t],
+    "blgpu_context_stroke_polyline_d": [_P, _P, ctypes.c_size_t],
+    "blgpu_context_stroke_polygon_d": [_P, _P, ctypes.c_size_t],
+    "blgpu_context_stroke_box_d": [_P, _D, _D, _D, _D],
+    "blgpu_context_stroke_rect_d": [_P, _D, _D, _D, _D],
+    "blgpu_context_stroke_line_d": [_P, _D, _D, _D, _D],
+    "blgpu_stroke_outline_d": [_P, _P, ctypes.c_size_t, ctypes.POINTER(StrokeOptions), _P, _P, ctypes.c_size_t,
+                               ctypes.POINTER(ctypes.c_size_t)],
     "blgpu_context_submit_stream": [_P, ctypes.c_char_p, ctypes.c_size_t],
     "blgpu_render_batch": [_P, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(Image),
                            _U32],
@@ -318,22 +342,58 @@ class Context:
     def reset_transform(self): self._call("blgpu_context_reset_transform")
     def set_fill_style_rgba32(self, argb32): self._call("blgpu_context_set_fill_style_rgba32", argb32 & 0xFFFFFFFF)
 
-    def set_fill_style_gradient(self, type, values, stops, extend_mode=EXTEND_PAD, transform=None):
+    def set_fill_style_gradient(self, type, values, stops, extend_mode=EXTEND_PAD, transform=None, _slot="fill"):
         """stops: iterable of (offset, rgba64)."""
         st = (GradientStop * max(len(stops), 1))(*[GradientStop(float(o), int(c)) for o, c in stops])
         vals = list(values) + [0.0] * (6 - len(values))
         m = _mat(transform)
         g = Gradient(type, extend_mode, (ctypes.c_double * 6)(*vals), st, len(stops),
                      ctypes.cast(m, ctypes.POINTER(ctypes.c_double)) if m is not None else None)
-        self._call("blgpu_context_set_fill_style_gradient", ctypes.byref(g))
+        self._call(f"blgpu_context_set_{_slot}_style_gradient", ctypes.byref(g))
 
-    def set_fill_style_pattern(self, image, area=(0, 0, 0, 0), extend_mode=EXTEND_REPEAT, transform=None):
+    def set_fill_style_pattern(self, image, area=(0, 0, 0, 0), extend_mode=EXTEND_REPEAT, transform=None, _slot="fill"):
         img, keep = make_image(image)
         self._keep.append((img, keep))
         m = _mat(transform)
         p = Pattern(ctypes.pointer(img), (ctypes.c_int32 * 4)(*area), extend_mode,
                     ctypes.cast(m, ctypes.POINTER(ctypes.c_double)) if m is not None else None)
-        self._call("blgpu_context_set_fill_style_pattern", ctypes.byref(p))
+        self._call(f"blgpu_context_set_{_slot}_style_pattern", ctypes.byref(p))
+
+    # -- stroking (the stroke style slot and BLStrokeOptions) --------------------------------------
+    def set_stroke_style_rgba32(self, argb32: int): self._call("blgpu_context_set_stroke_style_rgba32", argb32)
+
+    def set_stroke_style_gradient(self, type, values, stops, extend_mode=EXTEND_PAD, transform=None):
+        self.set_fill_style_gradient(type, values, stops, extend_mode, transform, _slot="stroke")
+
+    def set_stroke_style_pattern(self, image, area=(0, 0, 0, 0), extend_mode=EXTEND_REPEAT, transform=None):
+        self.set_fill_style_pattern(image, area, extend_mode, transform, _slot="stroke")
+
+    def set_stroke_alpha(self, a: float): self._call("blgpu_context_set_stroke_alpha", a)
+    def set_stroke_width(self, w: float): self._call("blgpu_context_set_stroke_width", w)
+    def set_stroke_miter_limit(self, m: float): self._call("blgpu_context_set_stroke_miter_limit", m)
+    def set_stroke_join(self, join: int): self._call("blgpu_context_set_stroke_join", join)
+    def set_stroke_cap(self, position: int, cap: int): self._call("blgpu_context_set_stroke_cap", position, cap)
+    def set_stroke_caps(self, cap: int): self._call("blgpu_context_set_stroke_caps", cap)
+    def set_stroke_transform_order(self, order: int): self._call("blgpu_context_set_stroke_transform_order", order)
+
+    def stroke_path_d(self, cmds, xy):
+        c = np.ascontiguousarray(cmds, dtype=np.uint8)
+        a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
+        if c.shape[0] != a.shape[0]:
+            raise ValueError("one command per vertex")
+        self._call("blgpu_context_stroke_path_d", c.ctypes.data, a.ctypes.data, a.shape[0])
+
+    def stroke_polyline_d(self, xy):
+        a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
+        self._call("blgpu_context_stroke_polyline_d", a.ctypes.data, a.shape[0])
+
+    def stroke_polygon_d(self, xy):
+        a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
+        self._call("blgpu_context_stroke_polygon_d", a.ctypes.data, a.shape[0])
+
+    def stroke_box_d(self, x0, y0, x1, y1): self._call("blgpu_context_stroke_box_d", x0, y0, x1, y1)
+    def stroke_rect_d(self, x, y, w, h): self._call("blgpu_context_stroke_rect_d", x, y, w, h)
+    def stroke_line_d(self, x0, y0, x1, y1): self._call("blgpu_context_stroke_line_d", x0, y0, x1, y1)
 
     def clear_all(self): self._call("blgpu_context_clear_all")
     def fill_all(self): self._call("blgpu_context_fill_all")
@@ -354,6 +414,26 @@ class Context:
 
     def submit_stream(self, stream: bytes):
         self._call("blgpu_context_submit_stream", stream, len(stream))
+
+
+def stroke_outline(cmds, xy, width=1.0, miter_limit=4.0, join=0, start_cap=0, end_cap=0):
+    """The outline a stroke of the path fills non-zero (host-side, no device): (cmds, xy)."""
+    lib = load_library()
+    c = np.ascontiguousarray(cmds, dtype=np.uint8)
+    a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
+    opt = StrokeOptions(width, miter_limit, join, start_cap, end_cap, 0)
+    n = ctypes.c_size_t(0)
+    cap = max(64, 16 * c.shape[0])
+    while True:
+        oc = np.zeros(cap, dtype=np.uint8)
+        ox = np.zeros((cap, 2), dtype=np.float64)
+        r = lib.blgpu_stroke_outline_d(c.ctypes.data, a.ctypes.data, c.shape[0], ctypes.byref(opt),
+                                       oc.ctypes.data, ox.ctypes.data, cap, ctypes.byref(n))
+        if r == ERROR_DATA_TOO_LARGE:
+            cap = n.value
+            continue
+        _check(r, "blgpu_stroke_outline_d")
+        return oc[: n.value].copy(), ox[: n.value].copy()
 
 
 def stream_size(stream: bytes) -> tuple[int, int]:

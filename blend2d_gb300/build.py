@@ -24,7 +24,7 @@ LIB = os.path.join(BUILD, "libblgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["kernels.cu", "noalloc.cu"]
-HOST_SOURCES = ["frontend.cpp", "runtime.cpp", "context.cpp"]
+HOST_SOURCES = ["frontend.cpp", "runtime.cpp", "context.cpp", "stroke.cpp"]
 
 
 def nvcc() -> str:

@@ -23,6 +23,7 @@
 #include "blgpu_stream.h"
 #include "frontend.h"
 #include "runtime.h"
+#include "stroke.h"
 
 using namespace blgpu;
 
@@ -127,9 +128,15 @@ struct State {
   int final_type = kTTIdentity, final_fixed_type = kTTScale;
   bool integral_translation = true;
   int tx_i = 0, ty_i = 0;
-  CtxStyle style;
+  CtxStyle style;               // BL_CONTEXT_STYLE_SLOT_FILL
+  CtxStyle stroke_style;        // BL_CONTEXT_STYLE_SLOT_STROKE
+  double stroke_alpha = 1.0;
+  uint32_t stroke_alpha_i = 255;
+  StrokeParams stroke;
   uint64_t xform_gen = 0;       // frame generation of xform_index
   uint32_t xform_index = 0;
+  uint64_t meta_xform_gen = 0;  // frame generation of meta_xform_index
+  uint32_t meta_xform_index = 0;
 };
 
 }  // namespace
@@ -155,6 +162,7 @@ struct BLGpuContext {
     stack.clear();
     on_transform_changed();
     style_solid(s.style.hs, 0xFF000000u);
+    style_solid(s.stroke_style.hs, 0xFF000000u);
   }
 
   // rastercontext.cpp:741-800
@@ -169,6 +177,7 @@ struct BLGpuContext {
     s.final_fixed_type = s.final_type > kTTScale ? s.final_type : int(kTTScale);
     s.integral_translation = false;
     s.xform_gen = 0;
+    s.meta_xform_gen = 0;
     if (s.final_type <= kTTTranslate) {
       double mn = floor(double(INT32_MIN + 1) * 256.0);
       double mx = floor(double(INT32_MAX - 1 - (w > h ? w : h)) * 256.0);
@@ -234,6 +243,21 @@ struct BLGpuContext {
     return s.xform_index;
   }
 
+  // The edge transform of a stroke in transform order BEFORE: the meta transform (identity) in
+  // 24.8 with the final transform's origin (DirectStateAccessor::meta_transform_fixed,
+  // rastercontext.cpp:179-182), a scale-type transform.
+  uint32_t register_meta_xform() {
+    if (s.meta_xform_gen == frame->generation) return s.meta_xform_index;
+    DevXform x{};
+    x.m[0] = 256.0; x.m[1] = 0.0; x.m[2] = 0.0; x.m[3] = 256.0;
+    x.m[4] = s.final_fixed.m20; x.m[5] = s.final_fixed.m21;
+    x.affine = 0u;
+    frame->xforms.push_back(x);
+    s.meta_xform_gen = frame->generation;
+    s.meta_xform_index = uint32_t(frame->xforms.size() - 1);
+    return s.meta_xform_index;
+  }
+
   DevCmd& push_cmd(uint32_t kind, uint32_t style, bool src_copy, uint32_t alpha) {
     DevCmd c{};
     c.kind = kind;
@@ -250,17 +274,20 @@ struct BLGpuContext {
 
   struct Fill { uint32_t style; bool src_copy; uint32_t alpha; };
 
-  // Returns false for a NOP fill (no alpha, no style, or a comp-op that simplifies to DstCopy).
-  bool resolve_fill(Fill& f) {
-    if (s.global_alpha_i == 0 || s.fill_alpha_i == 0 || s.style.hs.nop) return false;
+  // Returns false for a NOP fill or stroke (no alpha, no style, or a comp-op that simplifies to
+  // DstCopy) of the fill (slot 0) or stroke (slot 1) style.
+  bool resolve_fill(Fill& f, uint32_t slot = 0) {
+    CtxStyle& cs = slot_style(slot);
+    uint32_t alpha = slot ? s.stroke_alpha_i : s.fill_alpha_i;
+    if (s.global_alpha_i == 0 || alpha == 0 || cs.hs.nop) return false;
     uint32_t op = s.comp_op;
     if (op == kCompOpSrcOver) {
-      if (s.style.hs.format == kFmtZERO32) return false;
-      if (s.style.hs.format == kFmtFRGB32) op = kCompOpSrcCopy;
+      if (cs.hs.format == kFmtZERO32) return false;
+      if (cs.hs.format == kFmtFRGB32) op = kCompOpSrcCopy;
     }
     f.src_copy = op == kCompOpSrcCopy;
-    f.alpha = s.fill_alpha_i;
-    f.style = register_style(s.style);
+    f.alpha = alpha;
+    f.style = register_style(cs);
     return true;
   }
 
@@ -447,6 +474,34 @@ struct BLGpuContext {
     s.global_alpha = a;
     s.global_alpha_i = uint32_t(round_to_int(ia));
     s.fill_alpha_i = uint32_t(round_to_int(ia * s.fill_alpha));
+    s.stroke_alpha_i = uint32_t(round_to_int(ia * s.stroke_alpha));
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult set_stroke_alpha(double a) {   // set_style_alpha(STROKE) (rastercontext.cpp:1920-1939)
+    if (isnan(a)) return BLGPU_ERROR_INVALID_VALUE;
+    a = a < 0.0 ? 0.0 : (a > 1.0 ? 1.0 : a);
+    s.stroke_alpha = a;
+    s.stroke_alpha_i = uint32_t(round_to_int(s.global_alpha * 255.0 * a));
+    return BLGPU_SUCCESS;
+  }
+
+  // Stroke options (rastercontext.cpp:2059-2165): values outside the enums are rejected.
+  BLGpuResult set_stroke_width(double v) { s.stroke.width = v; return BLGPU_SUCCESS; }
+  BLGpuResult set_stroke_miter_limit(double v) { s.stroke.miter_limit = v; return BLGPU_SUCCESS; }
+  BLGpuResult set_stroke_join(uint32_t v) {
+    if (v > 4u) return BLGPU_ERROR_INVALID_VALUE;
+    s.stroke.join = v;
+    return BLGPU_SUCCESS;
+  }
+  BLGpuResult set_stroke_cap(uint32_t position, uint32_t cap) {
+    if (position > 1u || cap > 5u) return BLGPU_ERROR_INVALID_VALUE;
+    (position ? s.stroke.end_cap : s.stroke.start_cap) = cap;
+    return BLGPU_SUCCESS;
+  }
+  BLGpuResult set_stroke_transform_order(uint32_t v) {
+    if (v > 1u) return BLGPU_ERROR_INVALID_VALUE;
+    s.stroke.transform_order = v;
     return BLGPU_SUCCESS;
   }
 
@@ -488,21 +543,23 @@ struct BLGpuContext {
     return BLGPU_SUCCESS;
   }
 
-  // A new fill style: the previous one's registration is dropped, its stop storage reused.
-  void reset_style_slot() {
-    s.style.has_image = false;
-    s.style.image = BLGpuImage{};
-    s.style.frame_gen = 0;
-    s.style.frame_index = 0;
+  // A new style in a slot: the previous one's registration is dropped, its stop storage reused.
+  static void reset_style_slot(CtxStyle& cs) {
+    cs.has_image = false;
+    cs.image = BLGpuImage{};
+    cs.frame_gen = 0;
+    cs.frame_index = 0;
   }
+  CtxStyle& slot_style(uint32_t slot) { return slot ? s.stroke_style : s.style; }
 
-  BLGpuResult set_style_rgba32(uint32_t c) {
-    reset_style_slot();
-    style_solid(s.style.hs, c);
+  BLGpuResult set_style_rgba32(uint32_t c, uint32_t slot = 0) {
+    CtxStyle& cs = slot_style(slot);
+    reset_style_slot(cs);
+    style_solid(cs.hs, c);
     return BLGPU_SUCCESS;
   }
 
-  BLGpuResult set_style_gradient(const BLGpuGradient* g) {
+  BLGpuResult set_style_gradient(const BLGpuGradient* g, uint32_t slot = 0) {
     if (!g || g->type > 2 || g->extend_mode > 2 || (g->stop_count && !g->stops)) return BLGPU_ERROR_INVALID_VALUE;
     GradientDesc d;
     d.type = g->type;
@@ -511,12 +568,13 @@ struct BLGpuContext {
     d.stops = reinterpret_cast<const DevStop*>(g->stops);
     d.stop_count = g->stop_count;
     d.transform = g->transform;
-    reset_style_slot();
-    style_gradient(s.style.hs, d, s.final_t, s.gradient_quality);
+    CtxStyle& cs = slot_style(slot);
+    reset_style_slot(cs);
+    style_gradient(cs.hs, d, s.final_t, s.gradient_quality);
     return BLGPU_SUCCESS;
   }
 
-  BLGpuResult set_style_pattern(const BLGpuPattern* p) {
+  BLGpuResult set_style_pattern(const BLGpuPattern* p, uint32_t slot = 0) {
     if (!p || !p->image) return BLGPU_ERROR_INVALID_VALUE;
     const BLGpuImage& im = *p->image;
     if (im.format != BLGPU_FORMAT_PRGB32 || im.width < 0 || im.height < 0 || (im.width && !im.pixel_data) ||
@@ -535,11 +593,12 @@ struct BLGpuContext {
     memcpy(d.area, p->area, sizeof(d.area));
     d.extend = p->extend_mode;
     d.transform = p->transform;
-    reset_style_slot();
-    style_pattern(s.style.hs, d, s.pattern_quality, s.final_t);
-    if (!s.style.hs.nop) {
-      s.style.has_image = true;
-      s.style.image = im;
+    CtxStyle& cs = slot_style(slot);
+    reset_style_slot(cs);
+    style_pattern(cs.hs, d, s.pattern_quality, s.final_t);
+    if (!cs.hs.nop) {
+      cs.has_image = true;
+      cs.image = im;
     }
     return BLGPU_SUCCESS;
   }
@@ -605,6 +664,73 @@ struct BLGpuContext {
     if (n == 0) return BLGPU_SUCCESS;
     fill_analytic(f, xy, cmds, n, s.fill_rule, register_xform());
     return BLGPU_SUCCESS;
+  }
+
+  // --- strokes ----------------------------------------------------------------------------
+  // stroke_unclipped_geometry / stroke_unclipped_path<kSync> (rastercontext.cpp:3180-3234) with
+  // add_stroked_path_edges (rastercontextops_p.h:95-140): the outline is built here and recorded
+  // as a non-zero analytic fill with the stroke style; the device builds its edges.
+  std::vector<uint8_t> stroke_in_cmds, stroke_cmds;
+  std::vector<double> stroke_in_xy, stroke_poly_xy, stroke_xy;
+
+  BLGpuResult stroke_path(const uint8_t* cmds, const double* xy, size_t n) {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    if (n && (!xy || !cmds)) return BLGPU_ERROR_INVALID_VALUE;
+    if (n > 0x3FFFFFFFu) return BLGPU_ERROR_INVALID_VALUE;
+    Fill f;
+    if (n == 0 || !resolve_fill(f, 1)) return BLGPU_SUCCESS;
+    uint32_t xform;
+    if (s.stroke.transform_order != 0) {
+      // BEFORE: the path is mapped by the user transform without its translation first
+      // (DirectStateAccessor::user_transform, rastercontext.cpp:168-171).
+      const Mat& u = s.user;
+      stroke_in_xy.resize(2 * n);
+      for (size_t i = 0; i < n; i++) {
+        double x = xy[2 * i], y = xy[2 * i + 1];
+        stroke_in_xy[2 * i] = x * u.m00 + y * u.m10 + 0.0;
+        stroke_in_xy[2 * i + 1] = x * u.m01 + y * u.m11 + 0.0;
+      }
+      xy = stroke_in_xy.data();
+      xform = register_meta_xform();
+    }
+    else {
+      xform = register_xform();
+    }
+    stroke_cmds.clear();
+    stroke_xy.clear();
+    BLGpuResult r = stroke_outline(cmds, xy, n, s.stroke, stroke_cmds, stroke_xy);
+    if (r) return r;
+    if (stroke_cmds.empty()) return BLGPU_SUCCESS;
+    fill_analytic(f, stroke_xy.data(), stroke_cmds.data(), stroke_cmds.size(), 0 /* NON_ZERO */, xform);
+    return BLGPU_SUCCESS;
+  }
+
+  // BLPath::add_geometry (path.cpp:1335-1660, direction CW) for the simple geometry types.
+  BLGpuResult stroke_poly(const double* xy, size_t n, bool closed) {
+    if (n && !xy) return BLGPU_ERROR_INVALID_VALUE;
+    if (n > 0x3FFFFFFEu) return BLGPU_ERROR_INVALID_VALUE;
+    if (n == 0) return bound ? BLGPU_SUCCESS : BLGPU_ERROR_INVALID_STATE;
+    stroke_in_cmds.assign(n, uint8_t(1));
+    stroke_in_cmds[0] = 0;
+    stroke_poly_xy.assign(xy, xy + 2 * n);
+    if (closed) {
+      stroke_in_cmds.push_back(5);
+      stroke_poly_xy.push_back(NAN);
+      stroke_poly_xy.push_back(NAN);
+    }
+    return stroke_path(stroke_in_cmds.data(), stroke_poly_xy.data(), stroke_in_cmds.size());
+  }
+
+  BLGpuResult stroke_box(double x0, double y0, double x1, double y1) {
+    const uint8_t c[5] = {0, 1, 1, 1, 5};
+    const double v[10] = {x0, y0, x1, y0, x1, y1, x0, y1, NAN, NAN};
+    return stroke_path(c, v, 5);
+  }
+
+  BLGpuResult stroke_line(double x0, double y0, double x1, double y1) {
+    const uint8_t c[2] = {0, 1};
+    const double v[4] = {x0, y0, x1, y1};
+    return stroke_path(c, v, 2);
   }
 
   BLGpuResult save() { stack.push_back(s); return BLGPU_SUCCESS; }
@@ -675,7 +801,7 @@ BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
       case BLGPU_OP_SET_TRANSFORM: { if (!need(48)) return BLGPU_ERROR_INVALID_VALUE; double m[6]; memcpy(m, p, 48); set_transform(m); break; }
       case BLGPU_OP_RESET_TRANSFORM: reset_transform(); break;
       case BLGPU_OP_STYLE_RGBA32: { if (!need(4)) return BLGPU_ERROR_INVALID_VALUE; uint32_t v; memcpy(&v, p, 4); set_style_rgba32(v); break; }
-      case BLGPU_OP_STYLE_GRADIENT: {
+      case BLGPU_OP_STYLE_GRADIENT: case BLGPU_OP_STROKE_STYLE_GRADIENT: {
         BLGpuStreamGradient g;
         if (!need(sizeof(g))) return BLGPU_ERROR_INVALID_VALUE;
         memcpy(&g, p, sizeof(g));
@@ -693,10 +819,10 @@ BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
         gg.stops = reinterpret_cast<const BLGpuGradientStop*>(sp);
         gg.stop_count = g.stop_count;
         gg.transform = g.has_transform ? g.transform : nullptr;
-        r = set_style_gradient(&gg);
+        r = set_style_gradient(&gg, op == BLGPU_OP_STROKE_STYLE_GRADIENT ? 1u : 0u);
         break;
       }
-      case BLGPU_OP_STYLE_PATTERN: {
+      case BLGPU_OP_STYLE_PATTERN: case BLGPU_OP_STROKE_STYLE_PATTERN: {
         BLGpuStreamPattern pt;
         if (!need(sizeof(pt))) return BLGPU_ERROR_INVALID_VALUE;
         memcpy(&pt, p, sizeof(pt));
@@ -706,7 +832,7 @@ BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
         memcpy(pp.area, pt.area, sizeof(pp.area));
         pp.extend_mode = pt.extend_mode;
         pp.transform = pt.has_transform ? pt.transform : nullptr;
-        r = set_style_pattern(&pp);
+        r = set_style_pattern(&pp, op == BLGPU_OP_STROKE_STYLE_PATTERN ? 1u : 0u);
         break;
       }
       case BLGPU_OP_CLEAR_ALL: r = clear_all(); break;
@@ -744,10 +870,47 @@ BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
         r = fill_path(p + 8, aligned_doubles(p + 8 + cmd_bytes, size_t(n) * 2), n);
         break;
       }
+      case BLGPU_OP_STROKE_STYLE_RGBA32: { if (!need(4)) return BLGPU_ERROR_INVALID_VALUE; uint32_t v; memcpy(&v, p, 4); set_style_rgba32(v, 1); break; }
+      case BLGPU_OP_SET_STROKE_ALPHA: { if (!need(8)) return BLGPU_ERROR_INVALID_VALUE; double a; memcpy(&a, p, 8); set_stroke_alpha(a); break; }
+      case BLGPU_OP_SET_STROKE_WIDTH: { if (!need(8)) return BLGPU_ERROR_INVALID_VALUE; double v; memcpy(&v, p, 8); set_stroke_width(v); break; }
+      case BLGPU_OP_SET_STROKE_MITER_LIMIT: { if (!need(8)) return BLGPU_ERROR_INVALID_VALUE; double v; memcpy(&v, p, 8); set_stroke_miter_limit(v); break; }
+      case BLGPU_OP_SET_STROKE_JOIN: { if (!need(4)) return BLGPU_ERROR_INVALID_VALUE; uint32_t v; memcpy(&v, p, 4); set_stroke_join(v); break; }
+      case BLGPU_OP_SET_STROKE_CAPS: {
+        if (!need(8)) return BLGPU_ERROR_INVALID_VALUE;
+        uint32_t v[2]; memcpy(v, p, 8);
+        set_stroke_cap(0, v[0]);
+        set_stroke_cap(1, v[1]);
+        break;
+      }
+      case BLGPU_OP_SET_STROKE_TRANSFORM_ORDER: { if (!need(4)) return BLGPU_ERROR_INVALID_VALUE; uint32_t v; memcpy(&v, p, 4); set_stroke_transform_order(v); break; }
+      case BLGPU_OP_STROKE_PATH_D: {
+        if (!need(8)) return BLGPU_ERROR_INVALID_VALUE;
+        uint32_t n; memcpy(&n, p, 4);
+        size_t cmd_bytes = (size_t(n) + 7u) & ~size_t(7);
+        if (!need(8 + cmd_bytes + size_t(n) * 16)) return BLGPU_ERROR_INVALID_VALUE;
+        r = stroke_path(p + 8, aligned_doubles(p + 8 + cmd_bytes, size_t(n) * 2), n);
+        break;
+      }
+      case BLGPU_OP_STROKE_POLYLINE_D: case BLGPU_OP_STROKE_POLYGON_D: {
+        if (!need(8)) return BLGPU_ERROR_INVALID_VALUE;
+        uint32_t n; memcpy(&n, p, 4);
+        if (!need(8 + size_t(n) * 16)) return BLGPU_ERROR_INVALID_VALUE;
+        r = stroke_poly(aligned_doubles(p + 8, size_t(n) * 2), n, op == BLGPU_OP_STROKE_POLYGON_D);
+        break;
+      }
+      case BLGPU_OP_STROKE_BOX_D: case BLGPU_OP_STROKE_RECT_D: case BLGPU_OP_STROKE_LINE_D: {
+        if (!need(32)) return BLGPU_ERROR_INVALID_VALUE;
+        double q[4]; memcpy(q, p, 32);
+        if (op == BLGPU_OP_STROKE_BOX_D) r = stroke_box(q[0], q[1], q[2], q[3]);
+        else if (op == BLGPU_OP_STROKE_RECT_D) r = stroke_box(q[0], q[1], q[2] + q[0], q[3] + q[1]);
+        else r = stroke_line(q[0], q[1], q[2], q[3]);
+        break;
+      }
       case BLGPU_OP_SAVE: save(); break;
       case BLGPU_OP_RESTORE: restore(); break;
       default: return BLGPU_ERROR_INVALID_VALUE;
     }
+    if (r == BLGPU_ERROR_INVALID_GEOMETRY) r = BLGPU_SUCCESS;   // a failed stroke draws nothing; replay goes on
     if (r) return r;
   }
   return BLGPU_SUCCESS;
@@ -901,6 +1064,50 @@ BLGPU_API BLGpuResult blgpu_context_fill_rect_d(BLGpuContext* ctx, double x, dou
 BLGPU_API BLGpuResult blgpu_context_fill_box_d(BLGpuContext* ctx, double x0, double y0, double x1, double y1) { CTX_CALL(fill_box(x0, y0, x1, y1)); }
 BLGPU_API BLGpuResult blgpu_context_fill_polygon_d(BLGpuContext* ctx, const double* xy, size_t n) { CTX_CALL(fill_polygon(xy, n)); }
 BLGPU_API BLGpuResult blgpu_context_fill_path_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n) { CTX_CALL(fill_path(cmds, xy, n)); }
+BLGPU_API BLGpuResult blgpu_context_set_stroke_style_rgba32(BLGpuContext* ctx, uint32_t c) { CTX_CALL(set_style_rgba32(c, 1)); }
+BLGPU_API BLGpuResult blgpu_context_set_stroke_style_gradient(BLGpuContext* ctx, const BLGpuGradient* g) { CTX_CALL(set_style_gradient(g, 1)); }
+BLGPU_API BLGpuResult blgpu_context_set_stroke_style_pattern(BLGpuContext* ctx, const BLGpuPattern* p) { CTX_CALL(set_style_pattern(p, 1)); }
+BLGPU_API BLGpuResult blgpu_context_set_stroke_alpha(BLGpuContext* ctx, double a) { CTX_CALL(set_stroke_alpha(a)); }
+BLGPU_API BLGpuResult blgpu_context_set_stroke_width(BLGpuContext* ctx, double w) { CTX_CALL(set_stroke_width(w)); }
+BLGPU_API BLGpuResult blgpu_context_set_stroke_miter_limit(BLGpuContext* ctx, double m) { CTX_CALL(set_stroke_miter_limit(m)); }
+BLGPU_API BLGpuResult blgpu_context_set_stroke_join(BLGpuContext* ctx, uint32_t join) { CTX_CALL(set_stroke_join(join)); }
+BLGPU_API BLGpuResult blgpu_context_set_stroke_cap(BLGpuContext* ctx, uint32_t position, uint32_t cap) { CTX_CALL(set_stroke_cap(position, cap)); }
+BLGPU_API BLGpuResult blgpu_context_set_stroke_caps(BLGpuContext* ctx, uint32_t cap) {
+  if (!ctx) return BLGPU_ERROR_INVALID_VALUE;
+  if (cap > 5u) return BLGPU_ERROR_INVALID_VALUE;
+  ctx->set_stroke_cap(0, cap);
+  return ctx->set_stroke_cap(1, cap);
+}
+BLGPU_API BLGpuResult blgpu_context_set_stroke_transform_order(BLGpuContext* ctx, uint32_t order) { CTX_CALL(set_stroke_transform_order(order)); }
+BLGPU_API BLGpuResult blgpu_context_stroke_path_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n) { CTX_CALL(stroke_path(cmds, xy, n)); }
+BLGPU_API BLGpuResult blgpu_context_stroke_polyline_d(BLGpuContext* ctx, const double* xy, size_t n) { CTX_CALL(stroke_poly(xy, n, false)); }
+BLGPU_API BLGpuResult blgpu_context_stroke_polygon_d(BLGpuContext* ctx, const double* xy, size_t n) { CTX_CALL(stroke_poly(xy, n, true)); }
+BLGPU_API BLGpuResult blgpu_context_stroke_box_d(BLGpuContext* ctx, double x0, double y0, double x1, double y1) { CTX_CALL(stroke_box(x0, y0, x1, y1)); }
+BLGPU_API BLGpuResult blgpu_context_stroke_rect_d(BLGpuContext* ctx, double x, double y, double w, double h) { CTX_CALL(stroke_box(x, y, w + x, h + y)); }
+BLGPU_API BLGpuResult blgpu_context_stroke_line_d(BLGpuContext* ctx, double x0, double y0, double x1, double y1) { CTX_CALL(stroke_line(x0, y0, x1, y1)); }
+BLGPU_API BLGpuResult blgpu_stroke_outline_d(const uint8_t* cmds, const double* xy, size_t n, const BLGpuStrokeOptions* options,
+                                             uint8_t* out_cmds, double* out_xy, size_t capacity, size_t* out_n) {
+  if (!options || !out_n || (n && (!cmds || !xy)) || (capacity && (!out_cmds || !out_xy))) return BLGPU_ERROR_INVALID_VALUE;
+  if (options->join > 4u || options->start_cap > 5u || options->end_cap > 5u) return BLGPU_ERROR_INVALID_VALUE;
+  StrokeParams p;
+  p.width = options->width;
+  p.miter_limit = options->miter_limit;
+  p.join = options->join;
+  p.start_cap = options->start_cap;
+  p.end_cap = options->end_cap;
+  std::vector<uint8_t> oc;
+  std::vector<double> ox;
+  *out_n = 0;
+  BLGpuResult r = stroke_outline(cmds, xy, n, p, oc, ox);
+  if (r) return r;
+  *out_n = oc.size();
+  if (oc.size() > capacity) return BLGPU_ERROR_DATA_TOO_LARGE;
+  if (!oc.empty()) {
+    memcpy(out_cmds, oc.data(), oc.size());
+    memcpy(out_xy, ox.data(), ox.size() * sizeof(double));
+  }
+  return BLGPU_SUCCESS;
+}
 BLGPU_API BLGpuResult blgpu_context_submit_stream(BLGpuContext* ctx, const void* stream, size_t size) {
   CTX_CALL(submit_stream(static_cast<const uint8_t*>(stream), size));
 }

@@ -30,6 +30,7 @@ enum {
   BLGPU_ERROR_NOT_IMPLEMENTED = 0x00010007u, /* BL_ERROR_NOT_IMPLEMENTED */
   BLGPU_ERROR_NO_STATES_TO_RESTORE = 0x00010038u, /* BL_ERROR_NO_STATES_TO_RESTORE */
   BLGPU_ERROR_DATA_TOO_LARGE = 0x00010032u,   /* BL_ERROR_DATA_TOO_LARGE */
+  BLGPU_ERROR_INVALID_GEOMETRY = 0x00010034u, /* BL_ERROR_INVALID_GEOMETRY */
   BLGPU_ERROR_DEVICE = 0x00011000u           /* CUDA failure (no reference counterpart) */
 };
 
@@ -172,6 +173,46 @@ BLGpuResult blgpu_context_fill_rect_d(BLGpuContext* ctx, double x, double y, dou
 BLGpuResult blgpu_context_fill_box_d(BLGpuContext* ctx, double x0, double y0, double x1, double y1);  /* fill_geometry(BOXD) */
 BLGpuResult blgpu_context_fill_polygon_d(BLGpuContext* ctx, const double* xy, size_t n);              /* fill_geometry(POLYGOND) */
 BLGpuResult blgpu_context_fill_path_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n); /* bl_context_fill_path_d */
+
+/* Stroking (rastercontext.cpp:2059-2165 options, :3794-3870 operations). The stroke has its own
+ * style slot and alpha; the outline of the stroked geometry (pathstroke.cpp) is filled non-zero.
+ * Joins: BLStrokeJoin 0..4; caps: BLStrokeCap 0..5 at position 0 (start) / 1 (end); transform
+ * order: 0 AFTER (stroke in user space), 1 BEFORE. A path the stroker rejects draws nothing and
+ * returns BLGPU_ERROR_INVALID_GEOMETRY. */
+BLGpuResult blgpu_context_set_stroke_style_rgba32(BLGpuContext* ctx, uint32_t argb32);           /* bl_context_set_stroke_style_rgba32 */
+BLGpuResult blgpu_context_set_stroke_style_gradient(BLGpuContext* ctx, const BLGpuGradient* g);  /* bl_context_set_stroke_style(BLGradient) */
+BLGpuResult blgpu_context_set_stroke_style_pattern(BLGpuContext* ctx, const BLGpuPattern* p);    /* bl_context_set_stroke_style(BLPattern) */
+BLGpuResult blgpu_context_set_stroke_alpha(BLGpuContext* ctx, double alpha);        /* bl_context_set_stroke_alpha */
+BLGpuResult blgpu_context_set_stroke_width(BLGpuContext* ctx, double width);        /* bl_context_set_stroke_width */
+BLGpuResult blgpu_context_set_stroke_miter_limit(BLGpuContext* ctx, double limit);  /* bl_context_set_stroke_miter_limit */
+BLGpuResult blgpu_context_set_stroke_join(BLGpuContext* ctx, uint32_t join);        /* bl_context_set_stroke_join */
+BLGpuResult blgpu_context_set_stroke_cap(BLGpuContext* ctx, uint32_t position, uint32_t cap); /* bl_context_set_stroke_cap */
+BLGpuResult blgpu_context_set_stroke_caps(BLGpuContext* ctx, uint32_t cap);         /* bl_context_set_stroke_caps */
+BLGpuResult blgpu_context_set_stroke_transform_order(BLGpuContext* ctx, uint32_t order); /* bl_context_set_stroke_transform_order */
+BLGpuResult blgpu_context_stroke_path_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n); /* bl_context_stroke_path_d */
+BLGpuResult blgpu_context_stroke_polyline_d(BLGpuContext* ctx, const double* xy, size_t n);   /* stroke_geometry(POLYLINED) */
+BLGpuResult blgpu_context_stroke_polygon_d(BLGpuContext* ctx, const double* xy, size_t n);    /* stroke_geometry(POLYGOND) */
+BLGpuResult blgpu_context_stroke_box_d(BLGpuContext* ctx, double x0, double y0, double x1, double y1); /* stroke_geometry(BOXD) */
+BLGpuResult blgpu_context_stroke_rect_d(BLGpuContext* ctx, double x, double y, double w, double h);    /* stroke_geometry(RECTD) */
+BLGpuResult blgpu_context_stroke_line_d(BLGpuContext* ctx, double x0, double y0, double x1, double y1); /* stroke_geometry(LINE) */
+
+/* BLStrokeOptions without the dash array (core/path.h:330-352). */
+typedef struct BLGpuStrokeOptions {
+  double width;
+  double miter_limit;
+  uint32_t join;
+  uint32_t start_cap;
+  uint32_t end_cap;
+  uint32_t reserved;
+} BLGpuStrokeOptions;
+
+/* The outline a stroke fills (non-zero), in user space: per closed figure of the input its two
+ * offset figures, per open figure one loop (offset, end cap, reversed inner offset, start cap).
+ * Host-only; needs no device. *out_n receives the vertex count; BLGPU_ERROR_DATA_TOO_LARGE when
+ * it exceeds `capacity` (nothing written). Counterpart of bl_path_add_stroked_path
+ * (core/path.h:1232), whose figures are the same segments in a different arrangement. */
+BLGpuResult blgpu_stroke_outline_d(const uint8_t* cmds, const double* xy, size_t n, const BLGpuStrokeOptions* options,
+                                   uint8_t* out_cmds, double* out_xy, size_t capacity, size_t* out_n);
 
 /* Replays a serialized command stream (include/blgpu_stream.h) into the context; the stream's
  * canvas size must match the bound image. */

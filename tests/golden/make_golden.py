@@ -5,7 +5,8 @@ reference with oracle/ref.mk (no CMake) into oracle/_ref/ and records:
 
   * scenes  - sha256 of the PRGB32 pixels the reference renders for seeded command streams
               (blend2d_gb300.scenes; the mix_dither / curves_dither scenes use gradient quality
-              DITHER, whose 64-bit LUT has a single builder), for the stock no-JIT x86-64 build ("default", SSE2 LUT
+              DITHER, whose 64-bit LUT has a single builder; strokes_* / stroked_paths_* stroke
+              paths, polylines, polygons, boxes, rects and lines), for the stock no-JIT x86-64 build ("default", SSE2 LUT
               builder) and, for a subset, the portable-LUT build ("scalar");
   * luts    - sha256 of the gradient LUTs produced by the reference's three builders
               (interpolate_prgb32 / _sse2 / _avx2) for random stop arrays;
@@ -58,6 +59,12 @@ def scene_catalog(full: bool):
     for s in range(6):
         cat.append((f"mix_dither_{s}", f"scenes.random_mix({300 + s}, dither=True)", ("default",) if s % 2 else ("default", "scalar")))
     cat.append(("curves_dither", "scenes.curves(count=600, width=640, height=360, dither=True)", ("default",)))
+    for s in range(6):
+        cat.append((f"strokes_{s}", f"scenes.strokes(seed={20 + s}, count=250)", ("default",)))
+    cat.append(("strokes_wide", "scenes.strokes(seed=30, count=300, max_width=90.0)", ("default",)))
+    cat.append(("strokes_lines", "scenes.strokes(seed=31, count=300, curves=False)", ("default",)))
+    cat.append(("strokes_small", "scenes.strokes(seed=32, width=61, height=97, count=60)", ("default",)))
+    cat.append(("stroked_paths_2k", "scenes.stroked_paths(count=2000)", ("default",)))
     for i in range(6):
         cat.append((f"batch_{i}", f"scenes.batch_canvases(seed=4, count=6, max_side=640, max_paths=400)[{i}]", ("default",)))
     if full:

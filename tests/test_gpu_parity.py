@@ -417,3 +417,65 @@ def test_occlusion_cull_keeps_pixels_and_skips_work():
     assert ops_culled < ops_full
     want = oracle_lib.render(stream)
     assert not _diff(culled, want), _diff(culled, want)
+
+
+# --- stroking ---------------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("seed,variant", [(s, v) for s, v in zip(range(1200, 1212), ["default", "avx2", "scalar"] * 4)])
+def test_strokes_vs_oracle(runtimes, seed, variant):
+    """Stroked paths, polylines, polygons, boxes, rects and lines with every join and cap, both
+    transform orders, solid / gradient / pattern stroke styles (host stroker, device fill)."""
+    sw = scenes.strokes(seed=seed, count=120, width=(257, 64, 400)[seed % 3], height=(193, 301, 90)[seed % 3],
+                        max_width=(24.0, 6.0, 60.0, 12.0)[seed % 4], curves=seed % 5 != 4)
+    stream = sw.to_bytes()
+    got = bg.render_stream(runtimes(variant), stream)
+    want = oracle_lib.render(stream, variant)
+    assert not _diff(got, want), _diff(got, want)
+
+
+def test_stroke_context_calls_match_stream(runtimes):
+    """The stroke entry points and stroke state of the C ABI against the same operations replayed
+    from a stream (and the oracle)."""
+    w, h = 220, 160
+    sw = scenes.StreamWriter(w, h)
+    out = np.zeros((h, w), dtype=np.uint32)
+    ctx = bg.Context(runtimes(), out)
+    sw.solid(0xFF202020); sw.fill_all()
+    ctx.set_fill_style_rgba32(0xFF202020); ctx.fill_all()
+    sw.stroke_solid(0xFFFFCC00); ctx.set_stroke_style_rgba32(0xFFFFCC00)
+    sw.stroke_width(7.5); ctx.set_stroke_width(7.5)
+    sw.stroke_join(scenes.JOIN_ROUND); ctx.set_stroke_join(scenes.JOIN_ROUND)
+    sw.stroke_caps(scenes.CAP_ROUND, scenes.CAP_TRIANGLE)
+    ctx.set_stroke_cap(0, scenes.CAP_ROUND); ctx.set_stroke_cap(1, scenes.CAP_TRIANGLE)
+    pl = np.array([[10.0, 20.0], [80.0, 30.0], [40.0, 90.0], [120.0, 70.0]])
+    sw.stroke_polyline(pl); ctx.stroke_polyline_d(pl)
+    sw.stroke_join(scenes.JOIN_MITER_CLIP); ctx.set_stroke_join(scenes.JOIN_MITER_CLIP)
+    sw.stroke_miter_limit(2.5); ctx.set_stroke_miter_limit(2.5)
+    sw.stroke_polygon(pl + 80.0); ctx.stroke_polygon_d(pl + 80.0)
+    sw.stroke_alpha(0.6); ctx.set_stroke_alpha(0.6)
+    sw.stroke_box_d(150.0, 10.0, 210.0, 60.0); ctx.stroke_box_d(150.0, 10.0, 210.0, 60.0)
+    sw.stroke_rect_d(15.0, 110.0, 60.0, 35.0); ctx.stroke_rect_d(15.0, 110.0, 60.0, 35.0)
+    sw.stroke_caps(scenes.CAP_SQUARE, scenes.CAP_SQUARE); ctx.set_stroke_caps(scenes.CAP_SQUARE)
+    sw.stroke_line_d(100.0, 150.0, 200.0, 100.0); ctx.stroke_line_d(100.0, 150.0, 200.0, 100.0)
+    m = [1.2, 0.3, -0.2, 0.9, 10.0, 5.0]
+    sw.transform(m); ctx.set_transform(m)
+    sw.stroke_transform_order(scenes.TRANSFORM_ORDER_BEFORE); ctx.set_stroke_transform_order(scenes.TRANSFORM_ORDER_BEFORE)
+    stops = [(0.0, 0xFF00FFFF), (1.0, 0xFFFF00FF)]
+    sw.stroke_gradient(scenes.LINEAR, [0.0, 0.0, 150.0, 100.0], scenes.PAD, stops)
+    ctx.set_stroke_style_gradient(bg.GRADIENT_LINEAR, [0.0, 0.0, 150.0, 100.0],
+                                  [(o, scenes.rgba64_from_rgba32(c)) for o, c in stops], bg.EXTEND_PAD)
+    path_c = [0, 4, 4, 1, 2, 1]
+    path_xy = np.array([[20.0, 40.0], [60.0, -10.0], [90.0, 90.0], [130.0, 40.0], [150.0, 0.0], [170.0, 60.0]])
+    sw.stroke_path(path_c, path_xy); ctx.stroke_path_d(path_c, path_xy)
+    ctx.end()
+    stream = sw.to_bytes()
+    via_stream = bg.render_stream(runtimes(), stream)
+    assert not _diff(out, via_stream), _diff(out, via_stream)
+    want = oracle_lib.render(stream)
+    assert not _diff(out, want), _diff(out, want)
+    with pytest.raises(bg.BLGpuError):
+        ctx2 = bg.Context(runtimes(), np.zeros((8, 8), dtype=np.uint32))
+        try:
+            ctx2.stroke_path_d([1, 1], np.array([[0.0, 0.0], [4.0, 4.0]]))   # no MOVE: invalid geometry
+        finally:
+            ctx2.end()
