@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 fill pipeline on the curves-and-gradients workload.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload curves|polygons|patterns]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload curves|polygons|patterns|strokes]
                     [--impl ours|reference] [--cpu-seconds S]
 
 Workload (default): one 1920x1080 PRGB32 canvas cleared to opaque black, 20,000 closed paths of
@@ -44,6 +44,7 @@ WORKLOADS = {   # name -> (config label, seed)
     "curves": ("curves_gradients_1920x1080_20000_cubic_paths", 2),
     "polygons": ("polygons_512x512_2000_solid", 1),
     "patterns": ("patterns_4096x4096_50000_affine_quads", 3),
+    "strokes": ("strokes_1920x1080_20000_stroked_cubic_paths", 10),
 }
 FALLBACK_HBM_GBS = 6800.0
 L2_FLUSH_BYTES = 256 << 20
@@ -71,7 +72,7 @@ def parse_args(argv=None):
 
 def make_stream(workload: str) -> tuple[bytes, int, int, int]:
     from blend2d_gb300 import scenes
-    sw = getattr(scenes, workload)()
+    sw = scenes.WORKLOADS[workload]()
     return sw.to_bytes(), sw.width, sw.height, sw.fill_count
 
 

@@ -23,7 +23,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libblgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["kernels.cu", "noalloc.cu"]
+CUDA_SOURCES = ["kernels.cu", "noalloc.cu", "stroke.cu"]
 HOST_SOURCES = ["frontend.cpp", "runtime.cpp", "context.cpp", "stroke.cpp"]
 
 

@@ -183,6 +183,21 @@ struct alignas(16) DevPiece {
   uint32_t pad[2];
 };
 
+// One figure of a stroked path: commands [first, end) of the frame's stroke input (the extent the
+// reference's stroker walks), the stroke command whose outline it adds to, and its options.
+struct DevStrokeFig {
+  uint32_t first, end;
+  uint32_t cmd;            // DevCmd index
+  uint32_t cmd_figs;       // on the command's first figure: its figure count; else 0
+  uint32_t param;          // stroke parameter index
+};
+
+// Width, miter limit, join and caps of a stroke (BLStrokeOptions without the dash array).
+struct DevStrokeParams {
+  double width, miter_limit;
+  uint32_t join, start_cap, end_cap, pad;
+};
+
 // Device-side view of a frame (pointers into one device arena).
 struct FrameView {
   const DevCmd* cmds;
@@ -248,6 +263,19 @@ struct FrameView {
   uint32_t num_tiles;
   uint32_t num_rows;
   uint32_t num_lut_jobs;
+  // Stroking: the stroke input paths, one thread per figure counts (stroke_counts: total, A, B,
+  // C | closed << 30 | B taken << 31) and then writes the figure's outline at
+  // verts / path_cmds[stroke_vert_base + stroke_offsets[fig]].
+  const DevStrokeFig* stroke_figs;
+  const DevStrokeParams* stroke_params;
+  const double* stroke_xy;
+  const uint8_t* stroke_cmds;
+  uint4* stroke_counts;
+  uint32_t* stroke_totals;
+  uint32_t* stroke_offsets;   // num_stroke_figs + 1 (the last one: the outline's size)
+  uint32_t* stroke_scan_tmp;
+  uint32_t num_stroke_figs;
+  uint32_t stroke_vert_base;
   uint32_t num_segs;
   uint32_t num_cmdrows;
   uint32_t num_seglist;

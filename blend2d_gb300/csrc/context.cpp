@@ -668,10 +668,12 @@ struct BLGpuContext {
 
   // --- strokes ----------------------------------------------------------------------------
   // stroke_unclipped_geometry / stroke_unclipped_path<kSync> (rastercontext.cpp:3180-3234) with
-  // add_stroked_path_edges (rastercontextops_p.h:95-140): the outline is built here and recorded
-  // as a non-zero analytic fill with the stroke style; the device builds its edges.
-  std::vector<uint8_t> stroke_in_cmds, stroke_cmds;
-  std::vector<double> stroke_in_xy, stroke_poly_xy, stroke_xy;
+  // add_stroked_path_edges (rastercontextops_p.h:95-140): the path is recorded with its figures
+  // and stroke options; the device strokes every figure into the command's outline, which is then
+  // filled non-zero with the stroke style like an analytic fill's path.
+  std::vector<uint32_t> stroke_ranges;
+  std::vector<uint8_t> stroke_in_cmds;
+  std::vector<double> stroke_in_xy, stroke_poly_xy;
 
   BLGpuResult stroke_path(const uint8_t* cmds, const double* xy, size_t n) {
     if (!bound) return BLGPU_ERROR_INVALID_STATE;
@@ -679,6 +681,10 @@ struct BLGpuContext {
     if (n > 0x3FFFFFFFu) return BLGPU_ERROR_INVALID_VALUE;
     Fill f;
     if (n == 0 || !resolve_fill(f, 1)) return BLGPU_SUCCESS;
+    stroke_ranges.clear();
+    BLGpuResult r = stroke_figures(cmds, n, stroke_ranges);
+    if (r) return r;
+    if (stroke_ranges.empty()) return BLGPU_SUCCESS;
     uint32_t xform;
     if (s.stroke.transform_order != 0) {
       // BEFORE: the path is mapped by the user transform without its translation first
@@ -696,12 +702,22 @@ struct BLGpuContext {
     else {
       xform = register_xform();
     }
-    stroke_cmds.clear();
-    stroke_xy.clear();
-    BLGpuResult r = stroke_outline(cmds, xy, n, s.stroke, stroke_cmds, stroke_xy);
-    if (r) return r;
-    if (stroke_cmds.empty()) return BLGPU_SUCCESS;
-    fill_analytic(f, stroke_xy.data(), stroke_cmds.data(), stroke_cmds.size(), 0 /* NON_ZERO */, xform);
+    DevCmd& c = push_cmd(kFillAnalytic, f.style, f.src_copy, f.alpha);   // non-zero
+    c.geom = kGeomPath;
+    c.geom_first = 0;                  // the outline's range is set on the device
+    c.geom_count = 0;
+    c.xform = xform;
+    const uint32_t cmd_index = uint32_t(frame->cmds.size() - 1);
+    const uint32_t base = uint32_t(frame->stroke_cmds.size());
+    frame->stroke_cmds.append(cmds, n);
+    frame->stroke_xy.append(xy, 2 * n);
+    DevStrokeParams sp{s.stroke.width, s.stroke.miter_limit, s.stroke.join, s.stroke.start_cap, s.stroke.end_cap, 0u};
+    const uint32_t param = uint32_t(frame->stroke_params.size());
+    frame->stroke_params.push_back(sp);
+    const uint32_t figs = uint32_t(stroke_ranges.size() / 2);
+    for (uint32_t k = 0; k < figs; k++)
+      frame->stroke_figs.push_back(DevStrokeFig{base + stroke_ranges[2 * k], base + stroke_ranges[2 * k + 1], cmd_index,
+                                                k == 0 ? figs : 0u, param});
     return BLGPU_SUCCESS;
   }
 

@@ -1,4 +1,4 @@
-// launch.h - host entry points of the device pipeline (implemented in kernels.cu). Each returns
+// launch.h - host entry points of the device pipeline (kernels.cu, stroke.cu). Each returns
 // the number of kernels it launched on `st`.
 #pragma once
 
@@ -34,5 +34,8 @@ int launch_row_states(const FrameView& f, cudaStream_t st);
 int launch_backdrop_prefix(const FrameView& f, cudaStream_t st);
 int launch_coverage(const FrameView& f, const LaunchConfig& cfg, uint32_t* scan_tmp, cudaStream_t st);
 int fine_grid_size(int blocks_per_sm);
+// Stroking: per-figure outline sizes and their exclusive scan (stroke_offsets), then the outlines.
+int launch_stroke_count(const FrameView& f, cudaStream_t st);
+int launch_stroke_emit(const FrameView& f, cudaStream_t st);
 
 }  // namespace blgpu

@@ -48,6 +48,7 @@ uint64_t Frame::next_generation() { return g_frame_generation.fetch_add(1) + 1; 
 void Frame::clear() {
   cmds.clear(); styles.clear(); xforms.clear(); canvases.clear(); targets.clear();
   verts.clear(); path_cmds.clear(); lut_jobs.clear(); stops.clear(); images.clear();
+  stroke_figs.clear(); stroke_params.clear(); stroke_xy.clear(); stroke_cmds.clear();
   image_words = 0; lut_words = 0; tiles = 0; rows = 0;
   generation = next_generation();
 }
@@ -185,15 +186,74 @@ static bool device_target_direct(const BLGpuImage& im) {
          (im.stride & 15) == 0 && im.stride >= intptr_t(im.width) * 4;
 }
 
+// Stroke sizing: the stroke inputs go to the device and the count pass runs once, so the frame's
+// vertex arrays can be planned with room for the outlines (their size comes back to the host).
+// The pipeline writes the outlines (and, on a replay, counts again).
+BLGpuResult Runtime::prepare_strokes(const Frame& fr, FrameView& v, uint32_t& outline_verts) {
+  outline_verts = 0;
+  const uint32_t nf = uint32_t(fr.stroke_figs.size());
+  v.num_stroke_figs = nf;
+  v.stroke_vert_base = uint32_t(fr.verts.size() / 2);
+  if (!nf) return BLGPU_SUCCESS;
+  auto plan = [&](Layout& L) {
+    v.stroke_figs = L.take<DevStrokeFig>(nf);
+    v.stroke_params = L.take<DevStrokeParams>(fr.stroke_params.size());
+    v.stroke_xy = L.take<double>(fr.stroke_xy.size());
+    v.stroke_cmds = L.take<uint8_t>(fr.stroke_cmds.size());
+    v.stroke_counts = L.take<uint4>(nf);
+    v.stroke_totals = L.take<uint32_t>(nf + 1);
+    v.stroke_offsets = L.take<uint32_t>(nf + 1);
+    v.stroke_scan_tmp = L.take<uint32_t>(scan_temp_words(nf + 1));
+  };
+  Layout measure;
+  plan(measure);
+  if (measure.off > stroke_buf.size) {
+    graph_valid = false;
+    BLGPU_CHECK(cudaStreamSynchronize(stream));
+    BLGPU_CHECK(stroke_buf.reserve(measure.off));
+  }
+  Layout L;
+  L.base = static_cast<char*>(stroke_buf.ptr);
+  plan(L);
+  auto put = [&](const void* dst, const void* src, size_t bytes) -> cudaError_t {
+    if (!bytes) return cudaSuccess;
+    h2d_bytes += bytes;
+    return cudaMemcpyAsync(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice, stream);
+  };
+  BLGPU_CHECK(put(v.stroke_figs, fr.stroke_figs.data(), sizeof(DevStrokeFig) * nf));
+  BLGPU_CHECK(put(v.stroke_params, fr.stroke_params.data(), sizeof(DevStrokeParams) * fr.stroke_params.size()));
+  BLGPU_CHECK(put(v.stroke_xy, fr.stroke_xy.data(), sizeof(double) * fr.stroke_xy.size()));
+  BLGPU_CHECK(put(v.stroke_cmds, fr.stroke_cmds.data(), fr.stroke_cmds.size()));
+  launch_stroke_count(v, stream);
+  BLGPU_CHECK(cudaGetLastError());
+  BLGPU_CHECK(cudaMemcpyAsync(host_totals + 16, v.stroke_offsets + nf, 4, cudaMemcpyDeviceToHost, stream));
+  d2h_bytes += 4;
+  BLGPU_CHECK(cudaStreamSynchronize(stream));
+  if (host_totals[16] > 0x3FFFFFFFu) return BLGPU_ERROR_DATA_TOO_LARGE;
+  outline_verts = host_totals[16];
+  strokes_counted = true;
+  return BLGPU_SUCCESS;
+}
+
 BLGpuResult Runtime::upload(const Frame& fr) {
   const uint32_t nc = uint32_t(fr.cmds.size());
   const uint32_t ncv = uint32_t(fr.canvases.size());
+  h2d_bytes = 0;
+  d2h_bytes = 0;
+
+  FrameView v{};
+  uint32_t outline_verts = 0;
+  strokes_counted = false;
+  BLGpuResult sr = prepare_strokes(fr, v, outline_verts);
+  if (sr) return sr;
+  const size_t vert_words = fr.verts.size() + 2 * size_t(outline_verts);   // doubles
+  const size_t cmd_bytes = fr.path_cmds.size() + size_t(outline_verts);
 
   // Items: at most one per vertex (a line or curve consumes at least one; a closing line takes
   // the place of the figure's move-to).
-  const uint32_t item_capacity = uint32_t(std::min<size_t>(fr.verts.size() + 1, 0xFFFFFFF0u));
+  const uint32_t item_capacity = uint32_t(std::min<size_t>(vert_words + 1, 0xFFFFFFF0u));
   // a cubic (3 vertices) splits into at most 8 monotonic pieces, a quadratic (2) into at most 3
-  const uint32_t piece_capacity = uint32_t(std::min<size_t>(fr.verts.size() / 2 * 3 + 64, 0xFFFFFFF0u));
+  const uint32_t piece_capacity = uint32_t(std::min<size_t>(vert_words / 2 * 3 + 64, 0xFFFFFFF0u));
 
   // Plan: [staged inputs][luts][canvases][work arrays]
   auto plan = [&](Layout& L, FrameView& v, std::vector<uint32_t*>* cpix) -> size_t {
@@ -202,8 +262,8 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     v.styles = L.take<DevStyle>(fr.styles.size());
     v.xforms = L.take<DevXform>(fr.xforms.size());
     v.canvases = L.take<DevCanvas>(ncv);
-    v.verts = L.take<double>(fr.verts.size());
-    v.path_cmds = L.take<uint8_t>(fr.path_cmds.size());
+    v.verts = L.take<double>(vert_words);
+    v.path_cmds = L.take<uint8_t>(cmd_bytes);
     v.lut_jobs = L.take<DevLutJob>(fr.lut_jobs.size());
     v.stops = L.take<DevStop>(fr.stops.size());
     v.images = L.take<uint32_t>(fr.image_words);
@@ -248,7 +308,6 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     return staged_end;
   };
 
-  FrameView v{};
   Layout measure;
   plan(measure, v, nullptr);
   size_t total = measure.off;
@@ -287,8 +346,6 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   }
   char* hs = static_cast<char*>(host_staging);
   size_t hs_off = 0;
-  h2d_bytes = 0;
-  d2h_bytes = 0;
   auto put = [&](const void* dev_ptr, const void* src, size_t bytes, bool src_pinned) -> cudaError_t {
     if (!bytes) return cudaSuccess;
     h2d_bytes += bytes;
@@ -344,7 +401,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
 
   // Segment array: kept across frames, sized from the vertex count at first and from the actual
   // count whenever a frame overflows it (run() then repeats the counting half).
-  size_t want_segs = std::max<size_t>(size_t(seg_capacity), fr.verts.size() * 2 + 65536);
+  size_t want_segs = std::max<size_t>(size_t(seg_capacity), vert_words * 2 + 65536);
   want_segs = std::min<size_t>(want_segs, 0xFFFFFFF0u);
   if (want_segs > seg_capacity) {
     graph_valid = false;
@@ -385,6 +442,11 @@ int Runtime::enqueue_count_half(cudaStream_t st) {
     cudaStreamWaitEvent(side, fork_ev, 0);
     k += launch_lut(f, side);
     cudaEventRecord(join_ev, side);
+  }
+  if (f.num_stroke_figs) {
+    if (!strokes_counted) k += launch_stroke_count(f, st);
+    strokes_counted = false;      // a replay of this frame counts again
+    k += launch_stroke_emit(f, st);
   }
   k += launch_edges(f, cfg, st);
   k += launch_cmd_tiles(f, cmdrow_per_cmd, st);
@@ -513,7 +575,7 @@ BLGpuResult Runtime::run(const Frame& fr) {
   BLGPU_CHECK(cudaStreamSynchronize(stream));
   has_frame = true;
   read_pixel_ops();
-  stats.input_vertices = uint64_t(fr.verts.size() / 2);
+  stats.input_vertices = uint64_t((fr.verts.size() + fr.stroke_xy.size()) / 2);
   stats.h2d_bytes = h2d_bytes;
   stats.d2h_bytes = d2h_bytes + 16;
 
@@ -537,6 +599,8 @@ BLGpuResult Runtime::run(const Frame& fr) {
 // (noalloc.h): no allocating call at all. Inputs are copied straight from the frame's host vectors.
 // The runtime's own frame (kept for replay) is left untouched.
 BLGpuResult Runtime::run_noalloc(const Frame& fr) {
+  // stroke outlines are sized on the device first; that needs buffers this path does not have
+  if (!fr.stroke_figs.empty()) return BLGPU_ERROR_NOT_IMPLEMENTED;
   BLGPU_CHECK(cudaSetDevice(device));
   if (fr.canvases.size() != 1 || !device_target_direct(fr.targets[0].image)) return BLGPU_ERROR_INVALID_VALUE;
   void* arena = nullptr;

@@ -97,6 +97,7 @@ struct Frame {
   explicit Frame(bool pinned_memory = true) {
     cmds.pinned = styles.pinned = xforms.pinned = verts.pinned = path_cmds.pinned = lut_jobs.pinned = stops.pinned =
         pinned_memory;
+    stroke_figs.pinned = stroke_params.pinned = stroke_xy.pinned = stroke_cmds.pinned = pinned_memory;
   }
   HostArray<DevCmd> cmds;
   HostArray<DevStyle> styles;
@@ -107,6 +108,12 @@ struct Frame {
   HostArray<uint8_t> path_cmds;
   HostArray<DevLutJob> lut_jobs;
   HostArray<DevStop> stops;
+  // stroke input paths (user space, or mapped by the user transform's linear part for transform
+  // order BEFORE), their figures and parameters
+  HostArray<DevStrokeFig> stroke_figs;
+  HostArray<DevStrokeParams> stroke_params;
+  HostArray<double> stroke_xy;
+  HostArray<uint8_t> stroke_cmds;
   std::vector<FrameImage> images;
   uint64_t image_words = 0;
   uint32_t lut_words = 0;
@@ -145,6 +152,8 @@ struct Runtime {
   DeviceBuffer in_buf;      // uploaded frame data + canvases + fixed-size work arrays
   DeviceBuffer dyn_buf;     // sizes known after the counting pass (segment and command lists)
   DeviceBuffer seg_buf;     // segments + their metadata, appended by the edge builders
+  DeviceBuffer stroke_buf;  // stroke inputs, per-figure outline counts and offsets
+  bool strokes_counted = false;   // the upload's sizing pass left this frame's counts in place
   uint32_t seg_capacity = 0;
   void* host_staging = nullptr;
   size_t host_staging_size = 0;
@@ -189,6 +198,7 @@ struct Runtime {
  private:
   int enqueue_count_half(cudaStream_t st);
   int enqueue_render_half(cudaStream_t st, bool timed);
+  BLGpuResult prepare_strokes(const Frame& fr, FrameView& v, uint32_t& outline_verts);
   BLGpuResult upload(const Frame& fr);
   BLGpuResult download();
   BLGpuResult reserve_segments(uint32_t count);

@@ -1,5 +1,6 @@
-// Path stroking on the recording thread: a stroke becomes the non-zero fill of its outline, which
-// the device pipeline then builds, rasterizes and composites like any analytic fill.
+// Path stroking. The stroker itself (stroke_core.h) runs on the device, one thread per figure;
+// the recording thread only splits a stroked path into the figures the reference's stroker visits
+// and validates it.
 #pragma once
 
 #include <cstddef>
@@ -21,17 +22,15 @@ struct StrokeParams {
   uint32_t transform_order = 0;   // BLStrokeTransformOrder, AFTER
 };
 
-// BLApproximationOptions defaults (blend2d/core/path_p.h:89-98) the stroker reads.
-constexpr double kSimplifyTolerance = 0.05;
-constexpr double kOffsetParameter = 0.414213562;
+// The figures PathStroker::stroke (pathstroke.cpp:224-487) strokes, as [first, end) command
+// ranges appended to `ranges` (figures with a move only are left out: they stroke to nothing).
+// Returns BLGPU_ERROR_INVALID_GEOMETRY where the reference's stroke fails (a command other than
+// a move or close between figures, a curve running past the path's end): it then draws nothing.
+BLGpuResult stroke_figures(const uint8_t* cmds, size_t n, std::vector<uint32_t>& ranges);
 
-// Strokes the path (BLPathCmd bytes + vertices) and appends its outline to `cmds`/`xy` as
-// implicitly closed figures for a non-zero fill: per closed input figure its two offset paths
-// (A, and B reversed); per open figure one loop A + end cap + reversed B + start cap. The
-// segments are exactly those the reference's stroke sink hands its edge builder
-// (rastercontextops.cpp:61-74): an open A or C path ends where the next part starts, and the
-// zero-length closing line of the joined loop adds nothing. Returns BLGPU_SUCCESS, or
-// BLGPU_ERROR_INVALID_GEOMETRY with nothing appended (the reference then fills nothing).
+// The outline a stroke fills non-zero, on the host with the same stroker: per closed figure its
+// two offset figures, per open figure one loop (see stroke_core.h). Used by
+// blgpu_stroke_outline_d; rendering strokes the figures on the device.
 BLGpuResult stroke_outline(const uint8_t* cmds, const double* xy, size_t n, const StrokeParams& p,
                            std::vector<uint8_t>& out_cmds, std::vector<double>& out_xy);
 

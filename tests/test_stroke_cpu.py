@@ -88,3 +88,40 @@ def test_invalid_geometry_is_rejected_with_nothing_drawn():
     # a figure with a single point has no direction and strokes to nothing
     oc, _ = bg.stroke_outline([0], np.array([[3.0, 4.0]]))
     assert len(oc) == 0
+
+
+@pytest.mark.parametrize("join", range(5))
+def test_long_figures_through_the_vertex_window(join):
+    """Figures far longer than the stroker's window of patchable vertices: closed polygons whose
+    closing join moves the figure's first vertex after it was handed out, open polylines, and
+    cubic chains."""
+    rng = np.random.Generator(np.random.PCG64(700 + join))
+    w, h = 300, 220
+    ss, sf = scenes.StreamWriter(w, h), scenes.StreamWriter(w, h)
+    for sw in (ss, sf):
+        sw.solid(0xFF000000)
+        sw.fill_all()
+    for k in range(6):
+        npts = int(rng.integers(40, 160))
+        ang = np.sort(rng.uniform(0, 2 * np.pi, npts))
+        rad = rng.uniform(30, 100, npts)
+        xy = np.stack([150 + rad * np.cos(ang), 110 + rad * np.sin(ang)], axis=1)
+        if k % 3 == 0:
+            cmds = [0] + [1] * (npts - 1) + [5]
+            xy = np.vstack([xy, [np.nan, np.nan]])
+        elif k % 3 == 1:
+            cmds = [0] + [1] * (npts - 1)
+        else:
+            m = (npts - 1) // 3
+            cmds = [0] + [4, 4, 1] * m
+            xy = xy[: 1 + 3 * m]
+        width = float(rng.uniform(1.0, 14.0))
+        caps = int(rng.integers(0, 6)), int(rng.integers(0, 6))
+        col = int(rng.integers(0, 2**32, dtype=np.uint64))
+        ss.stroke_width(width); ss.stroke_join(join); ss.stroke_caps(*caps); ss.stroke_miter_limit(8.0)
+        ss.stroke_solid(col)
+        ss.stroke_path(cmds, xy)
+        oc, ox = bg.stroke_outline(cmds, xy, width, 8.0, join, *caps)
+        sf.solid(col)
+        sf.fill_path(oc, ox)
+    assert int((ol.render(ss.to_bytes()) != ol.render(sf.to_bytes())).sum()) == 0
