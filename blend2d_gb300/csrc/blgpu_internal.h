@@ -267,6 +267,7 @@ struct FrameView {
   // C | closed << 30 | B taken << 31) and then writes the figure's outline at
   // verts / path_cmds[stroke_vert_base + stroke_offsets[fig]].
   const DevStrokeFig* stroke_figs;
+  const uint32_t* stroke_order;   // thread -> figure: figures with alike work side by side
   const DevStrokeParams* stroke_params;
   const double* stroke_xy;
   const uint8_t* stroke_cmds;

@@ -195,8 +195,26 @@ BLGpuResult Runtime::prepare_strokes(const Frame& fr, FrameView& v, uint32_t& ou
   v.num_stroke_figs = nf;
   v.stroke_vert_base = uint32_t(fr.verts.size() / 2);
   if (!nf) return BLGPU_SUCCESS;
+  // Thread order: a counting sort by vertex count (larger first), join and caps, so a warp's
+  // figures run the same branches and loops of similar length (the stroker is FP64-bound and a
+  // warp's FP64 instruction costs the same for one lane as for 32).
+  stroke_order.resize(nf);
+  {
+    constexpr uint32_t kBuckets = 64u * 8u * 64u;
+    std::vector<uint32_t> keys(nf), start(kBuckets + 1, 0u);
+    for (uint32_t i = 0; i < nf; i++) {
+      const DevStrokeFig& fg = fr.stroke_figs[i];
+      const DevStrokeParams& sp = fr.stroke_params[fg.param];
+      const uint32_t nv = std::min<uint32_t>(fg.end - fg.first, 63u);
+      keys[i] = ((63u - nv) << 9) | ((sp.join & 7u) << 6) | ((sp.start_cap * 6u + sp.end_cap) & 63u);
+      start[keys[i] + 1]++;
+    }
+    for (uint32_t k = 0; k < kBuckets; k++) start[k + 1] += start[k];
+    for (uint32_t i = 0; i < nf; i++) stroke_order[start[keys[i]]++] = i;
+  }
   auto plan = [&](Layout& L) {
     v.stroke_figs = L.take<DevStrokeFig>(nf);
+    v.stroke_order = L.take<uint32_t>(nf);
     v.stroke_params = L.take<DevStrokeParams>(fr.stroke_params.size());
     v.stroke_xy = L.take<double>(fr.stroke_xy.size());
     v.stroke_cmds = L.take<uint8_t>(fr.stroke_cmds.size());
@@ -221,6 +239,7 @@ BLGpuResult Runtime::prepare_strokes(const Frame& fr, FrameView& v, uint32_t& ou
     return cudaMemcpyAsync(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice, stream);
   };
   BLGPU_CHECK(put(v.stroke_figs, fr.stroke_figs.data(), sizeof(DevStrokeFig) * nf));
+  BLGPU_CHECK(put(v.stroke_order, stroke_order.data(), sizeof(uint32_t) * nf));
   BLGPU_CHECK(put(v.stroke_params, fr.stroke_params.data(), sizeof(DevStrokeParams) * fr.stroke_params.size()));
   BLGPU_CHECK(put(v.stroke_xy, fr.stroke_xy.data(), sizeof(double) * fr.stroke_xy.size()));
   BLGPU_CHECK(put(v.stroke_cmds, fr.stroke_cmds.data(), fr.stroke_cmds.size()));

@@ -154,6 +154,7 @@ struct Runtime {
   DeviceBuffer seg_buf;     // segments + their metadata, appended by the edge builders
   DeviceBuffer stroke_buf;  // stroke inputs, per-figure outline counts and offsets
   bool strokes_counted = false;   // the upload's sizing pass left this frame's counts in place
+  std::vector<uint32_t> stroke_order;   // thread -> figure order of the frame being uploaded
   uint32_t seg_capacity = 0;
   void* host_staging = nullptr;
   size_t host_staging_size = 0;

@@ -1,4 +1,5 @@
-// Device stroking: one thread per figure of every stroke command in the frame. The first kernel
+// Device stroking: one thread per figure of every stroke command in the frame (threads take the
+// figures in an order that puts figures with alike control flow side by side). The first kernel
 // runs the stroker to count the figure's outline vertices, an exclusive scan places the figures'
 // outlines after the frame's recorded vertices, and the second kernel runs the stroker again to
 // write them; the stroke command then reads its outline like any analytic fill's path.
@@ -13,8 +14,9 @@ namespace {
 constexpr int kStrokeThreads = 64;
 
 __global__ void __launch_bounds__(kStrokeThreads) stroke_count_kernel(FrameView f) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= f.num_stroke_figs) return;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= f.num_stroke_figs) return;
+  const uint32_t i = f.stroke_order[t];
   const DevStrokeFig fg = f.stroke_figs[i];
   const DevStrokeParams dp = f.stroke_params[fg.param];
   const sk::Params p{dp.width, dp.miter_limit, dp.join, dp.start_cap, dp.end_cap, 0u};
@@ -26,8 +28,9 @@ __global__ void __launch_bounds__(kStrokeThreads) stroke_count_kernel(FrameView 
 }
 
 __global__ void __launch_bounds__(kStrokeThreads) stroke_emit_kernel(FrameView f) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= f.num_stroke_figs) return;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= f.num_stroke_figs) return;
+  const uint32_t i = f.stroke_order[t];
   const DevStrokeFig fg = f.stroke_figs[i];
   const uint32_t off = f.stroke_offsets[i];
   const uint32_t vb = f.stroke_vert_base + off;
