@@ -137,6 +137,7 @@ struct QuadPieces {
   const double* t_end;
   V in[3], piece[3], i01, i12;
 
+  SK_HD QuadPieces() : t(nullptr), t_end(nullptr) {}
   SK_HD QuadPieces(const V* q, const double* ts, uint32_t n) : t(ts), t_end(ts + n) {
     in[0] = q[0]; in[1] = q[1]; in[2] = q[2];
     double u = *t++;
@@ -608,41 +609,167 @@ class FigureStroker {
     b.quad_to(q1 - k1, q2 - k2);
   }
 
-  SK_HD void offset_quad(const V* q) {           // offset_quad (:860-883)
-    double ts[3];
-    uint32_t tn = quad_offset_cusps(q, d_[0], ts);
-    ts[tn++] = 1.0;
-    QuadPieces it(q, ts, tn);
-    do {
-      for (;;) {
-        double t = quad_angle_step(it.piece, kOffsetParameter);
-        if (!(t > kOffsetQuadEpsilonT && t < 1.0 - kOffsetQuadEpsilonT)) t = 1.0;
-        V head[3];
-        quad_split(it.piece, head, it.piece, t);
-        offset_quad_piece(head[0], head[1], head[2]);
-        if (t == 1.0) break;
-      }
-    } while (it.next());
+  // --- offsetting, one piece per step ------------------------------------------------------
+  // offset_quad (:860-883) and approximate_cubic_with_quads (bezier_p.h:943-982) unrolled into a
+  // state the figure loop advances by one offset quad piece per iteration, so the lanes of a warp,
+  // each on its own figure, issue the piece arithmetic together however many t-steps, quads and
+  // pieces their curves need.
+  bool cubic_ = false, pieces_ = false;
+  uint32_t qn_ = 0, qe_ = 0;                   // quads of the current step start at q_[qn_], end at qe_
+  double t_ = 0.0;                             // the cubic's next t-step
+  V w_[7];                                     // the cubic's remainder in w_[3..6]
+  V q_[5];
+  double ts_[3];
+  QuadPieces it_;
+
+  SK_HD bool offsetting() const { return pieces_ || qn_ < qe_ || cubic_; }
+
+  SK_HD void begin_quad(const V* q) {
+    q_[0] = q[0]; q_[1] = q[1]; q_[2] = q[2];
+    qn_ = 0; qe_ = 2;
+    cubic_ = false; pieces_ = false;
   }
 
-  SK_HD void offset_cubic(const V* c) {          // approximate_cubic_with_quads (bezier_p.h:943-982)
+  SK_HD void begin_cubic(const V* c) {
     double tol = 54.0 * kSimplifyTolerance;
-    double t = sk_pow(tol * tol / mag_sq(cubic_identity(c)), 1.0 / 6.0);
-    V w[7];
-    w[3] = c[0]; w[4] = c[1]; w[5] = c[2]; w[6] = c[3];
-    for (;;) {
-      V q[5];
-      t = t < 1.0 ? t : 1.0;
-      if (t >= 0.999) t = 1.0;
-      cubic_split(w + 3, w, w + 3, t);
-      cubic_two_quads(w, q);
-      offset_quad(q);
-      offset_quad(q + 2);
-      if (t >= 1.0) return;
-      double prev = t;
-      t = t / (1.0 - t);
-      if (prev - t < 1e-3) t += 0.01;
+    t_ = sk_pow(tol * tol / mag_sq(cubic_identity(c)), 1.0 / 6.0);
+    w_[3] = c[0]; w_[4] = c[1]; w_[5] = c[2]; w_[6] = c[3];
+    qn_ = qe_ = 0;
+    cubic_ = true; pieces_ = false;
+  }
+
+  SK_HD void offset_step() {
+    if (!pieces_) {
+      if (qn_ >= qe_) {                          // the cubic's next t-step: two quads
+        t_ = t_ < 1.0 ? t_ : 1.0;
+        if (t_ >= 0.999) t_ = 1.0;
+        cubic_split(w_ + 3, w_, w_ + 3, t_);
+        cubic_two_quads(w_, q_);
+        qn_ = 0; qe_ = 4;
+        if (t_ >= 1.0) cubic_ = false;
+        else {
+          double prev = t_;
+          t_ = t_ / (1.0 - t_);
+          if (prev - t_ < 1e-3) t_ += 0.01;
+        }
+      }
+      // the next quad, cut at its offset's cusps
+      const V* q = q_ + qn_;
+      qn_ += 2;
+      uint32_t tn = quad_offset_cusps(q, d_[0], ts_);
+      ts_[tn++] = 1.0;
+      it_ = QuadPieces(q, ts_, tn);
+      pieces_ = true;
     }
+    double t = quad_angle_step(it_.piece, kOffsetParameter);
+    if (!(t > kOffsetQuadEpsilonT && t < 1.0 - kOffsetQuadEpsilonT)) t = 1.0;
+    V head[3];
+    quad_split(it_.piece, head, it_.piece, t);
+    offset_quad_piece(head[0], head[1], head[2]);
+    if (t == 1.0 && !it_.next()) pieces_ = false;
+  }
+
+  // --- input commands, one per step ----------------------------------------------------------
+  bool cusp_pending_ = false;                  // the second half of a cubic split at its cusp
+  V cusp_half_[4];
+
+  SK_HD void line_step(V p1) {
+    V v1 = p1 - p0_;
+    if (mag_sq(v1) < kLengthEpsilonSq) return;
+    V n1 = unit_normal(v1);
+    if (!open_) start_with_line(p1, n1);
+    else line_to(p1, n1);
+  }
+
+  // Starts offsetting the cubic p[0..3]; `cusp_join` for the half after a cusp.
+  SK_HD void cubic_step(const V* p, bool after_cusp) {
+    V v1 = p[1] - p0_;
+    if (is_zero(v1)) v1 = p[2] - p0_;
+    V n1 = unit_normal(v1);
+    if (!open_) start_with_curve(n1);
+    else if (!after_cusp) curve_join(n1);
+    else cusp_curve_join(n1);
+    begin_cubic(p);
+  }
+
+  // One command of the figure (PathStroker::stroke's loop body, pathstroke.cpp:266-456); false
+  // where that loop ends. Curves leave their offsetting to offset_step.
+  SK_HD bool command_step(const uint8_t* cmd, const V* vtx, uint32_t& i, uint32_t end) {
+    if (i >= end) return false;
+    const uint8_t c = cmd[i];
+    const V p1 = vtx[i];
+    if (c == kOn) {
+      i++;
+      line_step(p1);
+      return true;
+    }
+    if (c == kQuad) {
+      i += 2;
+      const V* q = vtx + i - 3;                  // starts at the input's previous vertex
+      V p2 = q[2];
+      V v2 = p2 - p1;
+      V v1 = p1 - p0_;
+      V n1 = unit_normal(v1);
+      if (sk_fabs(cross(v2, v1)) <= kCollinearityEpsilon) {
+        if (dot(-v1, v2) > 0.0) {                // control point outside: a cusp
+          double r1 = dot(p1 - p0_, v1);
+          double r2 = dot(p2 - p0_, v1);
+          double t = r1 / (2.0 * r1 - r2);
+          if (t > 0.0 && t < 1.0) {
+            V poly[2] = {quad_point(q, t), p2};
+            poly_to(poly, 2);
+            return true;
+          }
+        }
+        line_step(p2);
+        return true;
+      }
+      if (mag_sq(v1) < kLengthEpsilonSq || mag_sq(v2) < kLengthEpsilonSq) { line_step(p2); return true; }
+      if (!open_) start_with_curve(n1);
+      else curve_join(n1);
+      begin_quad(q);
+      return true;
+    }
+    if (c == kCubic) {
+      i += 3;
+      V p[7] = {};
+      p[0] = p0_; p[1] = vtx[i - 3]; p[2] = vtx[i - 2]; p[3] = vtx[i - 1];
+      if (cubic_is_flat(p, kDegenerateFlatness)) {
+        double dot1 = dot(p[0] - p[1], p[3] - p[1]);
+        double dot2 = dot(p[0] - p[2], p[3] - p[2]);
+        if (!(dot1 < 0.0) || !(dot2 < 0.0)) {    // flat with the controls outside: cusps
+          V r = cubic_start_dir(p);
+          double r1 = dot(p[1] - p[0], r), r2 = dot(p[2] - p[0], r), r3 = dot(p[3] - p[0], r);
+          double aa = 1.0 / (3.0 * r1 - 3.0 * r2 + r3);
+          double bb = 2.0 * r1 - r2;
+          double sq = sk_sqrt(r2 * (r2 - r1) - r1 * (r3 - r1));
+          double t1 = aa * (bb - sq), t2 = aa * (bb + sq);
+          V poly[3];
+          uint32_t poly_n = 0;
+          if (t1 > kCuspTThreshold && t1 < 1.0 - kCuspTThreshold) poly[poly_n++] = cubic_point(p, t1);
+          if (t2 > kCuspTThreshold && t2 < 1.0 - kCuspTThreshold) poly[poly_n++] = cubic_point(p, t2);
+          if (poly_n == 0) { line_step(p[3]); return true; }
+          poly[poly_n++] = p[3];
+          poly_to(poly, poly_n);
+          return true;
+        }
+        line_step(p[3]);
+        return true;
+      }
+      double tc, tl;
+      cubic_inflections(p, tc, tl);
+      if (tl == 0.0 && tc > 0.0 && tc < 1.0) {   // a cusp: the two halves, joined round
+        cubic_halve(p, p, p + 3);
+        cusp_half_[0] = p[3]; cusp_half_[1] = p[4]; cusp_half_[2] = p[5]; cusp_half_[3] = p[6];
+        cusp_pending_ = true;
+      }
+      cubic_step(p, false);
+      return true;
+    }
+    if (closed_ || c != kClose) return false;
+    closed_ = true;
+    line_step(p_start_);
+    return true;
   }
 
   template <class S>
@@ -662,119 +789,18 @@ class FigureStroker {
   }
 };
 
-// The body of PathStroker::stroke's figure loop (pathstroke.cpp:256-478).
+// The figure loop of PathStroker::stroke (pathstroke.cpp:256-478), one unit of work per iteration.
 template <class SinkA, class SinkB>
 SK_HD FigureCounts FigureStroker<SinkA, SinkB>::run(const uint8_t* cmd, const V* vtx, uint32_t first, uint32_t end) {
   FigureCounts out;
-  V poly[4];
-  uint32_t poly_n = 0;
   uint32_t i = first;
   p0_ = vtx[i];
   p_start_ = p0_;
   i++;
-  while (i < end) {
-    uint8_t c = cmd[i];
-    V p1 = vtx[i], v1, n1;
-    if (c == kOn) {
-      i++;
-    line:
-      v1 = p1 - p0_;
-      if (mag_sq(v1) < kLengthEpsilonSq) continue;
-      n1 = unit_normal(v1);
-      if (!open_) { start_with_line(p1, n1); continue; }
-      for (;;) {                                 // a run of lines
-        line_to(p1, n1);
-        if (i >= end) break;
-        c = cmd[i];
-        p1 = vtx[i];
-        if (c != kOn) break;
-        i++;
-        v1 = p1 - p0_;
-        if (mag_sq(v1) < kLengthEpsilonSq) break;
-        n1 = unit_normal(v1);
-      }
-      continue;
-    poly:
-      poly_to(poly, poly_n);
-      continue;
-    }
-    else if (c == kQuad) {
-      i += 2;
-      const V* q = vtx + i - 3;                  // starts at the input's previous vertex
-      V p2 = q[2];
-      V v2 = p2 - p1;
-      v1 = p1 - p0_;
-      n1 = unit_normal(v1);
-      if (sk_fabs(cross(v2, v1)) <= kCollinearityEpsilon) {
-        if (dot(-v1, v2) > 0.0) {                // control point outside: a cusp
-          double r1 = dot(p1 - p0_, v1);
-          double r2 = dot(p2 - p0_, v1);
-          double t = r1 / (2.0 * r1 - r2);
-          if (t > 0.0 && t < 1.0) {
-            poly[0] = quad_point(q, t);
-            poly[1] = p2;
-            poly_n = 2;
-            goto poly;
-          }
-        }
-        p1 = p2;
-        goto line;
-      }
-      if (mag_sq(v1) < kLengthEpsilonSq || mag_sq(v2) < kLengthEpsilonSq) { p1 = p2; goto line; }
-      if (!open_) start_with_curve(n1);
-      else curve_join(n1);
-      offset_quad(q);
-    }
-    else if (c == kCubic) {
-      i += 3;
-      V p[7] = {};
-      p[0] = p0_; p[1] = vtx[i - 3]; p[2] = vtx[i - 2]; p[3] = vtx[i - 1];
-      int cusp = 0;
-      if (cubic_is_flat(p, kDegenerateFlatness)) {
-        double dot1 = dot(p[0] - p[1], p[3] - p[1]);
-        double dot2 = dot(p[0] - p[2], p[3] - p[2]);
-        if (!(dot1 < 0.0) || !(dot2 < 0.0)) {    // flat with the controls outside: cusps
-          V r = cubic_start_dir(p);
-          double r1 = dot(p[1] - p[0], r), r2 = dot(p[2] - p[0], r), r3 = dot(p[3] - p[0], r);
-          double aa = 1.0 / (3.0 * r1 - 3.0 * r2 + r3);
-          double bb = 2.0 * r1 - r2;
-          double s = sk_sqrt(r2 * (r2 - r1) - r1 * (r3 - r1));
-          double t1 = aa * (bb - s), t2 = aa * (bb + s);
-          poly_n = 0;
-          if (t1 > kCuspTThreshold && t1 < 1.0 - kCuspTThreshold) poly[poly_n++] = cubic_point(p, t1);
-          if (t2 > kCuspTThreshold && t2 < 1.0 - kCuspTThreshold) poly[poly_n++] = cubic_point(p, t2);
-          if (poly_n == 0) { p1 = p[3]; goto line; }
-          poly[poly_n++] = p[3];
-          goto poly;
-        }
-        p1 = p[3];
-        goto line;
-      }
-      double tc, tl;
-      cubic_inflections(p, tc, tl);
-      if (tl == 0.0 && tc > 0.0 && tc < 1.0) {   // a cusp: the two halves, joined round
-        cubic_halve(p, p, p + 3);
-        cusp = 1;
-      }
-      for (;;) {
-        v1 = p[1] - p0_;
-        if (is_zero(v1)) v1 = p[2] - p0_;
-        n1 = unit_normal(v1);
-        if (!open_) start_with_curve(n1);
-        else if (cusp >= 0) curve_join(n1);
-        else cusp_curve_join(n1);
-        offset_cubic(p);
-        if (cusp <= 0) break;
-        cusp = -1;
-        p[0] = p[3]; p[1] = p[4]; p[2] = p[5]; p[3] = p[6];
-      }
-    }
-    else {
-      if (closed_ || c != kClose) break;
-      closed_ = true;
-      p1 = p_start_;
-      goto line;
-    }
+  for (;;) {
+    if (offsetting()) offset_step();
+    else if (cusp_pending_) { cusp_pending_ = false; cubic_step(cusp_half_, true); }
+    else if (!command_step(cmd, vtx, i, end)) break;
   }
   if (!open_) return out;
   out.closed = closed_;
