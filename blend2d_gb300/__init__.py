@@ -147,6 +147,11 @@ _SIGNATURES = {
     "blgpu_context_stroke_box_d": [_P, _D, _D, _D, _D],
     "blgpu_context_stroke_rect_d": [_P, _D, _D, _D, _D],
     "blgpu_context_stroke_line_d": [_P, _D, _D, _D, _D],
+    "blgpu_context_blit_image_i": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(Image), _P],
+    "blgpu_context_blit_image_d": [_P, _D, _D, ctypes.POINTER(Image), _P],
+    "blgpu_context_blit_scaled_image_i": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                          ctypes.POINTER(Image), _P],
+    "blgpu_context_blit_scaled_image_d": [_P, _D, _D, _D, _D, ctypes.POINTER(Image), _P],
     "blgpu_stroke_outline_d": [_P, _P, ctypes.c_size_t, ctypes.POINTER(StrokeOptions), _P, _P, ctypes.c_size_t,
                                ctypes.POINTER(ctypes.c_size_t)],
     "blgpu_context_submit_stream": [_P, ctypes.c_char_p, ctypes.c_size_t],
@@ -390,6 +395,22 @@ class Context:
     def stroke_polygon_d(self, xy):
         a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
         self._call("blgpu_context_stroke_polygon_d", a.ctypes.data, a.shape[0])
+
+    # -- image blits -----------------------------------------------------------------------------------
+    def _blit(self, name, args, image, area):
+        img, keep = make_image(image)
+        self._keep.append((img, keep))
+        ar = (ctypes.c_int32 * 4)(*area) if area is not None else None
+        self._call(name, *args, ctypes.byref(img), ctypes.cast(ar, _P) if ar is not None else None)
+
+    def blit_image_i(self, x, y, image, area=None): self._blit("blgpu_context_blit_image_i", (x, y), image, area)
+    def blit_image_d(self, x, y, image, area=None): self._blit("blgpu_context_blit_image_d", (x, y), image, area)
+
+    def blit_scaled_image_i(self, x, y, w, h, image, area=None):
+        self._blit("blgpu_context_blit_scaled_image_i", (x, y, w, h), image, area)
+
+    def blit_scaled_image_d(self, x, y, w, h, image, area=None):
+        self._blit("blgpu_context_blit_scaled_image_d", (x, y, w, h), image, area)
 
     def stroke_box_d(self, x0, y0, x1, y1): self._call("blgpu_context_stroke_box_d", x0, y0, x1, y1)
     def stroke_rect_d(self, x, y, w, h): self._call("blgpu_context_stroke_rect_d", x, y, w, h)

@@ -749,6 +749,131 @@ struct BLGpuContext {
     return stroke_path(c, v, 2);
   }
 
+  // --- image blits (rastercontext.cpp:3941-4160) -----------------------------------------------
+  // A blit composites the image (or its area) with the global alpha only, through the blit
+  // fetchers: aligned, fractional (bilinear or nearest by the pattern quality) or affine with
+  // REFLECT extend, over a box fill.
+  CtxStyle blit_style;
+
+  static bool valid_image(const BLGpuImage* im) {
+    return im && im->format == BLGPU_FORMAT_PRGB32 && im->width >= 0 && im->height >= 0 &&
+           (im->width == 0 || im->pixel_data) && im->stride >= intptr_t(im->width) * 4;
+  }
+
+  // check_image_area (rastercontext.cpp:2305-2319): false for an area outside the image.
+  static bool image_area(const BLGpuImage& im, const int32_t* area, int out[4]) {
+    out[0] = 0; out[1] = 0; out[2] = im.width; out[3] = im.height;
+    if (area) {
+      unsigned max_w = unsigned(im.width) - unsigned(area[0]);
+      unsigned max_h = unsigned(im.height) - unsigned(area[1]);
+      if ((max_w > unsigned(im.width)) | (unsigned(area[2]) > max_w) | (max_h > unsigned(im.height)) |
+          (unsigned(area[3]) > max_h))
+        return false;
+      out[0] = area[0]; out[1] = area[1]; out[2] = area[2]; out[3] = area[3];
+    }
+    return true;
+  }
+
+  // resolve_blit_op (rastercontext.cpp:1331-1342) for a PRGB32 image: the comp-op as set, the
+  // global alpha; false when the global alpha is zero.
+  bool resolve_blit(Fill& f, const BLGpuImage& im) {
+    if (s.global_alpha_i == 0 || blit_style.hs.nop) return false;
+    f.src_copy = s.comp_op == kCompOpSrcCopy;
+    f.alpha = s.global_alpha_i;
+    blit_style.has_image = true;
+    blit_style.image = im;
+    blit_style.frame_gen = 0;
+    f.style = register_style(blit_style);
+    return true;
+  }
+
+  BLGpuResult blit_image_d(double x, double y, const BLGpuImage* img, const int32_t* area) {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    if (!valid_image(img)) return BLGPU_ERROR_INVALID_VALUE;
+    int src[4];
+    if (!image_area(*img, area, src)) return BLGPU_ERROR_INVALID_VALUE;
+    if (s.global_alpha_i == 0) return BLGPU_SUCCESS;
+    Fill f;
+    if (s.final_type <= kTTTranslate) {
+      const Mat& t = s.final_fixed;
+      double sx = x * t.m00 + t.m20;
+      double sy = y * t.m11 + t.m21;
+      double cx1 = double(w) * 256.0, cy1 = double(h) * 256.0;
+      double dx0 = sx < 0.0 ? 0.0 : sx;
+      double dy0 = sy < 0.0 ? 0.0 : sy;
+      double ex = sx + double(src[2]) * t.m00, ey = sy + double(src[3]) * t.m11;
+      double dx1 = cx1 < ex ? cx1 : ex;
+      double dy1 = cy1 < ey ? cy1 : ey;
+      if (!((dx0 < dx1) & (dy0 < dy1))) return BLGPU_SUCCESS;
+      int ix0 = trunc_to_int(dx0), iy0 = trunc_to_int(dy0), ix1 = trunc_to_int(dx1), iy1 = trunc_to_int(dy1);
+      if (!((ix0 < ix1) & (iy0 < iy1))) return BLGPU_SUCCESS;
+      int64_t fx = floor_to_int64(sx), fy = floor_to_int64(sy);
+      if (!((fx | fy) & 0xFF)) {
+        // pixel aligned: the source area follows the clipped destination box
+        int x0 = ix0 >> 8, y0 = iy0 >> 8, x1 = (ix1 + 0xFF) >> 8, y1 = (iy1 + 0xFF) >> 8;
+        int tx = int(fx >> 8), ty = int(fy >> 8);
+        src[0] += x0 - tx; src[1] += y0 - ty;
+        src[2] = x1 - x0; src[3] = y1 - y0;
+        style_blit_aligned(blit_style.hs, 0, img->width, src, x0, y0);
+      }
+      else {
+        style_blit_fx_fy(blit_style.hs, 0, img->width, src, s.pattern_quality, fx, fy);
+      }
+      if (!resolve_blit(f, *img)) return BLGPU_SUCCESS;
+      fill_clipped_box_f(f, ix0, iy0, ix1, iy1);
+      return BLGPU_SUCCESS;
+    }
+    Mat ft = s.final_t;
+    ft.m20 += x * ft.m00 + y * ft.m10;       // BLMatrix2D::translate
+    ft.m21 += x * ft.m01 + y * ft.m11;
+    style_blit_affine(blit_style.hs, 0, img->width, src, s.pattern_quality, ft);
+    if (!resolve_blit(f, *img)) return BLGPU_SUCCESS;
+    fill_box_d(f, x, y, x + double(src[2]), y + double(src[3]));
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult blit_image_i(int32_t x, int32_t y, const BLGpuImage* img, const int32_t* area) {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    if (!valid_image(img)) return BLGPU_ERROR_INVALID_VALUE;
+    if (!s.integral_translation) return blit_image_d(double(x), double(y), img, area);
+    // translate_and_clip_rect_to_blit_i (rastercontext.cpp:922-990)
+    int src[4];
+    if (!image_area(*img, area, src)) return BLGPU_ERROR_INVALID_VALUE;
+    int64_t dx = int64_t(x) + s.tx_i, dy = int64_t(y) + s.ty_i;
+    int64_t x0 = dx, y0 = dy, x1 = x0 + src[2], y1 = y0 + src[3];
+    x0 = x0 < 0 ? 0 : x0; y0 = y0 < 0 ? 0 : y0;
+    x1 = x1 > w ? w : x1; y1 = y1 > h ? h : y1;
+    if ((x0 >= x1) | (y0 >= y1)) return BLGPU_SUCCESS;
+    src[0] += int(x0 - dx); src[1] += int(y0 - dy);
+    src[2] = int(x1 - x0); src[3] = int(y1 - y0);
+    if (s.global_alpha_i == 0) return BLGPU_SUCCESS;
+    style_blit_aligned(blit_style.hs, 0, img->width, src, int(x0), int(y0));
+    Fill f;
+    if (!resolve_blit(f, *img)) return BLGPU_SUCCESS;
+    fill_box_a(f, int(x0), int(y0), int(x1), int(y1));
+    return BLGPU_SUCCESS;
+  }
+
+  // blit_scaled_image_d / _i (rastercontext.cpp:4073-4160)
+  BLGpuResult blit_scaled_image(double rx, double ry, double rw, double rh, const BLGpuImage* img, const int32_t* area,
+                                bool integral) {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    if (!valid_image(img)) return BLGPU_ERROR_INVALID_VALUE;
+    int src[4];
+    if (!image_area(*img, area, src)) return BLGPU_ERROR_INVALID_VALUE;
+    if ((rw == double(src[2])) & (rh == double(src[3])))
+      return integral ? blit_image_i(int32_t(rx), int32_t(ry), img, area) : blit_image_d(rx, ry, img, area);
+    if (s.global_alpha_i == 0) return BLGPU_SUCCESS;
+    Mat sc{rw / double(src[2]), 0.0, 0.0, rh / double(src[3]), rx, ry};
+    Mat ft;
+    mat_multiply(ft, sc, s.final_t);
+    style_blit_affine(blit_style.hs, 0, img->width, src, s.pattern_quality, ft);
+    Fill f;
+    if (!resolve_blit(f, *img)) return BLGPU_SUCCESS;
+    fill_box_d(f, rx, ry, rx + rw, ry + rh);
+    return BLGPU_SUCCESS;
+  }
+
   BLGpuResult save() { stack.push_back(s); return BLGPU_SUCCESS; }
   BLGpuResult restore() {
     if (stack.empty()) return BLGPU_ERROR_NO_STATES_TO_RESTORE;
@@ -920,6 +1045,20 @@ BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
         if (op == BLGPU_OP_STROKE_BOX_D) r = stroke_box(q[0], q[1], q[2], q[3]);
         else if (op == BLGPU_OP_STROKE_RECT_D) r = stroke_box(q[0], q[1], q[2] + q[0], q[3] + q[1]);
         else r = stroke_line(q[0], q[1], q[2], q[3]);
+        break;
+      }
+      case BLGPU_OP_BLIT_IMAGE_I: case BLGPU_OP_BLIT_IMAGE_D:
+      case BLGPU_OP_BLIT_SCALED_IMAGE_I: case BLGPU_OP_BLIT_SCALED_IMAGE_D: {
+        BLGpuStreamBlit b;
+        if (!need(sizeof(b))) return BLGPU_ERROR_INVALID_VALUE;
+        memcpy(&b, p, sizeof(b));
+        if (b.image_index >= hdr.image_count) return BLGPU_ERROR_INVALID_VALUE;
+        const BLGpuImage* im = &images[b.image_index];
+        const int32_t* ar = b.has_area ? b.area : nullptr;
+        if (op == BLGPU_OP_BLIT_IMAGE_I) r = blit_image_i(int32_t(b.rect[0]), int32_t(b.rect[1]), im, ar);
+        else if (op == BLGPU_OP_BLIT_IMAGE_D) r = blit_image_d(b.rect[0], b.rect[1], im, ar);
+        else r = blit_scaled_image(b.rect[0], b.rect[1], b.rect[2], b.rect[3], im, ar, op == BLGPU_OP_BLIT_SCALED_IMAGE_I);
+        if (r == BLGPU_ERROR_INVALID_VALUE) r = BLGPU_SUCCESS;   // an area outside the image draws nothing
         break;
       }
       case BLGPU_OP_SAVE: save(); break;
@@ -1123,6 +1262,20 @@ BLGPU_API BLGpuResult blgpu_stroke_outline_d(const uint8_t* cmds, const double* 
     memcpy(out_xy, ox.data(), ox.size() * sizeof(double));
   }
   return BLGPU_SUCCESS;
+}
+BLGPU_API BLGpuResult blgpu_context_blit_image_i(BLGpuContext* ctx, int32_t x, int32_t y, const BLGpuImage* image, const int32_t* area) {
+  CTX_CALL(blit_image_i(x, y, image, area));
+}
+BLGPU_API BLGpuResult blgpu_context_blit_image_d(BLGpuContext* ctx, double x, double y, const BLGpuImage* image, const int32_t* area) {
+  CTX_CALL(blit_image_d(x, y, image, area));
+}
+BLGPU_API BLGpuResult blgpu_context_blit_scaled_image_i(BLGpuContext* ctx, int32_t x, int32_t y, int32_t w, int32_t h,
+                                                        const BLGpuImage* image, const int32_t* area) {
+  CTX_CALL(blit_scaled_image(double(x), double(y), double(w), double(h), image, area, true));
+}
+BLGPU_API BLGpuResult blgpu_context_blit_scaled_image_d(BLGpuContext* ctx, double x, double y, double w, double h,
+                                                        const BLGpuImage* image, const int32_t* area) {
+  CTX_CALL(blit_scaled_image(x, y, w, h, image, area, false));
 }
 BLGPU_API BLGpuResult blgpu_context_submit_stream(BLGpuContext* ctx, const void* stream, size_t size) {
   CTX_CALL(submit_stream(static_cast<const uint8_t*>(stream), size));

@@ -442,6 +442,43 @@ static bool pattern_affine(DevStyle& d, uint32_t extend, uint32_t quality, const
 }
 
 // init_non_solid_fetch_data, pattern branch (blend2d/raster/rastercontext.cpp:377-421).
+// Image blits (rastercontext.cpp:3941-4160): the image area as the style's source, then the
+// fetcher the blit sets up. Returns false (style NOP) for an empty area or a singular transform.
+static bool blit_source(HostStyle& s, int image, int img_w, const int area[4]) {
+  s.nop = true;
+  s.dev = DevStyle{};
+  s.image = -1;
+  s.stops.clear();
+  s.format = kFmtPRGB32;
+  if (area[2] <= 0 || area[3] <= 0) return false;
+  s.image = image;
+  s.dev.src_offset = uint64_t(uint32_t(area[1])) * uint64_t(img_w) + uint64_t(uint32_t(area[0]));
+  s.dev.src_w = area[2]; s.dev.src_h = area[3]; s.dev.src_stride = img_w;
+  return true;
+}
+
+// init_pattern_blit (pipedefs_p.h:1070-1076): pixel (x, y) reads the area's (x - x0, y - y0), never
+// outside it, which the aligned fetcher with pad extend and translation -x0, -y0 does.
+void style_blit_aligned(HostStyle& s, int image, int img_w, const int area[4], int x0, int y0) {
+  if (!blit_source(s, image, img_w, area)) return;
+  pattern_simple(s.dev, 0u, -x0, -y0, false, false);
+  s.nop = false;
+}
+
+// setup_pattern_fx_fy with the blit extend (REFLECT, rastercontext_p.h:51).
+void style_blit_fx_fy(HostStyle& s, int image, int img_w, const int area[4], uint32_t quality, int64_t tx64, int64_t ty64) {
+  if (!blit_source(s, image, img_w, area)) return;
+  pattern_fx_fy(s.dev, 2u, quality, tx64, ty64);
+  s.nop = false;
+}
+
+// setup_pattern_affine with the blit extend.
+void style_blit_affine(HostStyle& s, int image, int img_w, const int area[4], uint32_t quality, const Mat& t) {
+  if (!blit_source(s, image, img_w, area)) return;
+  if (!pattern_affine(s.dev, 2u, quality, t)) { s.nop = true; return; }
+  s.nop = false;
+}
+
 void style_pattern(HostStyle& s, const PatternDesc& p, uint32_t quality, const Mat& final_transform) {
   s.nop = true;
   s.dev = DevStyle{};

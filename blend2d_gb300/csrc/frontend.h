@@ -56,6 +56,10 @@ struct PatternDesc {
 void style_solid(HostStyle& s, uint32_t argb32);
 void style_gradient(HostStyle& s, const GradientDesc& g, const Mat& final_transform, uint32_t quality = 0);
 void style_pattern(HostStyle& s, const PatternDesc& p, uint32_t pattern_quality, const Mat& final_transform);
+// Blit fetchers over the image area {x, y, w, h} (image = frame image index).
+void style_blit_aligned(HostStyle& s, int image, int img_w, const int area[4], int x0, int y0);
+void style_blit_fx_fy(HostStyle& s, int image, int img_w, const int area[4], uint32_t quality, int64_t tx64, int64_t ty64);
+void style_blit_affine(HostStyle& s, int image, int img_w, const int area[4], uint32_t quality, const Mat& t);
 
 int default_band_height(int width);
 

@@ -62,6 +62,10 @@ OP_STROKE_POLYGON_D = 31
 OP_STROKE_BOX_D = 32
 OP_STROKE_RECT_D = 33
 OP_STROKE_LINE_D = 34
+OP_BLIT_IMAGE_I = 35
+OP_BLIT_IMAGE_D = 36
+OP_BLIT_SCALED_IMAGE_I = 37
+OP_BLIT_SCALED_IMAGE_D = 38
 
 SRC_OVER, SRC_COPY = 0, 1
 NON_ZERO, EVEN_ODD = 0, 1
@@ -239,6 +243,25 @@ class StreamWriter:
     def stroke_line_d(self, x0, y0, x1, y1):
         self._rec(OP_STROKE_LINE_D, struct.pack("<4d", x0, y0, x1, y1))
         self.fill_count += 1
+
+    # -- image blits ----------------------------------------------------------------------------
+    def _blit(self, op, rect, image_index, area):
+        r = [float(v) for v in rect] + [0.0] * (4 - len(rect))
+        ar = list(area) if area is not None else [0, 0, 0, 0]
+        self._rec(op, struct.pack("<4dII4i", *r, image_index, 1 if area is not None else 0, *ar))
+        self.fill_count += 1
+
+    def blit_image_i(self, x, y, image_index, area=None):
+        self._blit(OP_BLIT_IMAGE_I, [int(x), int(y)], image_index, area)
+
+    def blit_image_d(self, x, y, image_index, area=None):
+        self._blit(OP_BLIT_IMAGE_D, [x, y], image_index, area)
+
+    def blit_scaled_image_i(self, x, y, w, h, image_index, area=None):
+        self._blit(OP_BLIT_SCALED_IMAGE_I, [int(x), int(y), int(w), int(h)], image_index, area)
+
+    def blit_scaled_image_d(self, x, y, w, h, image_index, area=None):
+        self._blit(OP_BLIT_SCALED_IMAGE_D, [x, y, w, h], image_index, area)
 
     def save(self):
         self._rec(OP_SAVE)
@@ -715,6 +738,60 @@ def strokes(seed: int = 9, width: int = 640, height: int = 480, count: int = 400
         else:
             p = rng.uniform(0, side, 4) + np.array([x0, y0, x0, y0])
             sw.stroke_line_d(*p.tolist())
+    return sw
+
+
+def blits(seed: int = 40, width: int = 320, height: int = 240, count: int = 150) -> StreamWriter:
+    """Image blits: integer and fractional origins, scaled rectangles, image areas (some outside the
+    image, which the reference rejects), partly clipped, with translations, rotations and scales,
+    nearest and bilinear quality, SrcOver/SrcCopy and global alpha."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sw = StreamWriter(width, height)
+    sw.solid(0xFF303030)
+    sw.fill_all()
+    for _ in range(3):
+        sw.add_image(premultiplied_noise(rng, int(rng.integers(1, 90)), int(rng.integers(1, 70))))
+    sizes = [im.shape for im in sw.images]
+    for i in range(count):
+        idx = int(rng.integers(0, len(sizes)))
+        ih, iw = sizes[idx]
+        area = None
+        if rng.random() < 0.4:
+            ax, ay = int(rng.integers(0, iw)), int(rng.integers(0, ih))
+            # non-empty: the reference divides by the area's size in its pattern set-up
+            area = [ax, ay, int(rng.integers(1, iw - ax + 1)), int(rng.integers(1, ih - ay + 1))]
+            if rng.random() < 0.1:
+                area[2] += 1                                   # outside the image: rejected
+        sw.comp_op(SRC_COPY if rng.random() < 0.2 else SRC_OVER)
+        sw.hint(HINT_PATTERN_QUALITY, int(rng.integers(0, 2)))
+        if rng.random() < 0.15:
+            sw.global_alpha(float(rng.uniform(0.1, 1.0)))
+        elif rng.random() < 0.15:
+            sw.global_alpha(1.0)
+        t = float(rng.random())
+        if t < 0.15:
+            a = float(rng.uniform(-0.7, 0.7))
+            sn, c = _sincos(a)
+            sc = float(_log_uniform(rng, 0.5, 2.0))
+            sw.transform([c * sc, sn * sc, -sn * sc, c * sc, float(rng.uniform(-20, 40)), float(rng.uniform(-20, 40))])
+        elif t < 0.3:
+            sw.transform([1.0, 0.0, 0.0, 1.0, float(rng.integers(-30, 30)), float(rng.integers(-30, 30))])
+        elif t < 0.4:
+            sw.transform([1.0, 0.0, 0.0, 1.0, float(rng.uniform(-30, 30)), float(rng.uniform(-30, 30))])
+        elif t < 0.5:
+            sw.transform([1.5, 0.0, 0.0, 0.75, 5.0, -3.0])
+        elif t < 0.7:
+            sw.reset_transform()
+        x, y = float(rng.uniform(-60, width)), float(rng.uniform(-60, height))
+        k = float(rng.random())
+        if k < 0.35:
+            sw.blit_image_i(int(x), int(y), idx, area)
+        elif k < 0.65:
+            sw.blit_image_d(x if rng.random() < 0.7 else float(int(x)), y, idx, area)
+        elif k < 0.85:
+            sw.blit_scaled_image_d(x, y, float(rng.uniform(1, 200)), float(rng.uniform(1, 150)), idx, area)
+        else:
+            sw.blit_scaled_image_i(int(x), int(y), int(rng.integers(1, 200)), int(rng.integers(1, 150)), idx, area)
     return sw
 
 

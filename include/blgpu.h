@@ -196,6 +196,18 @@ BLGpuResult blgpu_context_stroke_box_d(BLGpuContext* ctx, double x0, double y0, 
 BLGpuResult blgpu_context_stroke_rect_d(BLGpuContext* ctx, double x, double y, double w, double h);    /* stroke_geometry(RECTD) */
 BLGpuResult blgpu_context_stroke_line_d(BLGpuContext* ctx, double x0, double y0, double x1, double y1); /* stroke_geometry(LINE) */
 
+/* Image blits (rastercontext.cpp:3941-4160): the image (PRGB32; `area` = {x, y, w, h} or NULL for
+ * all of it) composited with the comp-op and the global alpha (not the fill alpha) at the origin,
+ * or scaled into the rectangle, through the current transform; the pattern quality hint picks
+ * nearest or bilinear where the image is not pixel aligned. An area outside the image returns
+ * BLGPU_ERROR_INVALID_VALUE. */
+BLGpuResult blgpu_context_blit_image_i(BLGpuContext* ctx, int32_t x, int32_t y, const BLGpuImage* image, const int32_t* area); /* bl_context_blit_image_i */
+BLGpuResult blgpu_context_blit_image_d(BLGpuContext* ctx, double x, double y, const BLGpuImage* image, const int32_t* area);   /* bl_context_blit_image_d */
+BLGpuResult blgpu_context_blit_scaled_image_i(BLGpuContext* ctx, int32_t x, int32_t y, int32_t w, int32_t h,
+                                              const BLGpuImage* image, const int32_t* area);                                  /* bl_context_blit_scaled_image_i */
+BLGpuResult blgpu_context_blit_scaled_image_d(BLGpuContext* ctx, double x, double y, double w, double h,
+                                              const BLGpuImage* image, const int32_t* area);                                  /* bl_context_blit_scaled_image_d */
+
 /* BLStrokeOptions without the dash array (core/path.h:330-352). */
 typedef struct BLGpuStrokeOptions {
   double width;

@@ -79,6 +79,11 @@ enum {
   BLGPU_OP_STROKE_BOX_D = 32,      /* f64 x0, y0, x1, y1                           stroke_geometry(BOXD) */
   BLGPU_OP_STROKE_RECT_D = 33,     /* f64 x, y, w, h                               stroke_geometry(RECTD) */
   BLGPU_OP_STROKE_LINE_D = 34,     /* f64 x0, y0, x1, y1                           stroke_geometry(LINE) */
+  /* image blits (rastercontext.cpp:3941-4160); the image is one of the stream's images */
+  BLGPU_OP_BLIT_IMAGE_I = 35,      /* BLGpuStreamBlit (x, y as integers)           bl_context_blit_image_i */
+  BLGPU_OP_BLIT_IMAGE_D = 36,      /* BLGpuStreamBlit (x, y)                       bl_context_blit_image_d */
+  BLGPU_OP_BLIT_SCALED_IMAGE_I = 37, /* BLGpuStreamBlit (x, y, w, h as integers)   bl_context_blit_scaled_image_i */
+  BLGPU_OP_BLIT_SCALED_IMAGE_D = 38, /* BLGpuStreamBlit (x, y, w, h)               bl_context_blit_scaled_image_d */
   BLGPU_OP_COUNT
 };
 
@@ -121,5 +126,14 @@ typedef struct BLGpuStreamPattern {
   uint32_t reserved;
   double transform[6];   /* pattern transform (BLPattern::set_transform) when has_transform */
 } BLGpuStreamPattern;
+
+/* Payload of the blit records: the destination point (or rectangle) and the source area of one
+ * of the stream's images (has_area = 0: the whole image). */
+typedef struct BLGpuStreamBlit {
+  double rect[4];        /* x, y[, w, h]; integral values for the _I records */
+  uint32_t image_index;
+  uint32_t has_area;
+  int32_t area[4];       /* x, y, w, h */
+} BLGpuStreamBlit;
 
 #endif /* BLGPU_STREAM_H_INCLUDED */

@@ -671,6 +671,113 @@ static void stroke_op(OCtx* c, uint32_t op, const uint8_t* p) {
   o_path_free(&a); o_path_free(&b); o_path_free(&cp); o_path_free(&se.rev); o_path_free(&in);
 }
 
+/* --- image blits (rastercontext.cpp:3941-4160) ----------------------------------------------
+ * The image area composited with the comp-op and the global alpha through the blit fetchers. The
+ * aligned blit (FetchPatternAlignedBlit, fetchgeneric_p.h:471-534: pixel (x, y) reads the area's
+ * (x - x0, y - y0)) is the aligned pad fetcher translated by -x0, -y0: inside the blit box the two
+ * read the same pixels. */
+
+/* check_image_area (rastercontext.cpp:2305-2319) */
+static int o_image_area(int iw, int ih, const BLGpuStreamBlit* b, int out[4]) {
+  out[0] = 0; out[1] = 0; out[2] = iw; out[3] = ih;
+  if (b->has_area) {
+    unsigned max_w = (unsigned)iw - (unsigned)b->area[0];
+    unsigned max_h = (unsigned)ih - (unsigned)b->area[1];
+    if ((max_w > (unsigned)iw) | ((unsigned)b->area[2] > max_w) | (max_h > (unsigned)ih) | ((unsigned)b->area[3] > max_h))
+      return 0;
+    memcpy(out, b->area, sizeof(int) * 4);
+  }
+  return 1;
+}
+
+static int o_blit_source(OCtx* c, OStyle* st, uint32_t image_index, const int a[4]) {
+  memset(st, 0, sizeof(*st));
+  st->format = O_FMT_PRGB32;
+  if (a[2] <= 0 || a[3] <= 0) { st->nop = 1; return 0; }
+  int iw = c->iw[image_index];
+  st->src = c->images[image_index] + (intptr_t)a[1] * iw + a[0];
+  st->src_w = a[2]; st->src_h = a[3]; st->src_stride = iw;
+  return 1;
+}
+
+static void blit_op(OCtx* c, uint32_t op, const uint8_t* p) {
+  OState* s = &c->s;
+  BLGpuStreamBlit b;
+  memcpy(&b, p, sizeof(b));
+  int iw = c->iw[b.image_index], ih = c->ih[b.image_index];
+  int src[4];
+  if (op == BLGPU_OP_BLIT_SCALED_IMAGE_I || op == BLGPU_OP_BLIT_SCALED_IMAGE_D) {
+    if (!o_image_area(iw, ih, &b, src)) return;
+    if ((b.rect[2] == (double)src[2]) & (b.rect[3] == (double)src[3]))
+      op = op == BLGPU_OP_BLIT_SCALED_IMAGE_I ? BLGPU_OP_BLIT_IMAGE_I : BLGPU_OP_BLIT_IMAGE_D;
+  }
+  if (op == BLGPU_OP_BLIT_IMAGE_I && !s->integral_translation) op = BLGPU_OP_BLIT_IMAGE_D;
+  if (!o_image_area(iw, ih, &b, src)) return;
+  OStyle* st = (OStyle*)malloc(sizeof(OStyle));
+  c->fc.style = st; c->fc.comp_op = s->comp_op; c->fc.alpha = s->global_alpha_i;
+  if (op == BLGPU_OP_BLIT_IMAGE_I) {
+    /* translate_and_clip_rect_to_blit_i (rastercontext.cpp:922-990) */
+    int64_t dx = (int64_t)(int32_t)b.rect[0] + s->tx_i, dy = (int64_t)(int32_t)b.rect[1] + s->ty_i;
+    int64_t x0 = dx, y0 = dy, x1 = x0 + src[2], y1 = y0 + src[3];
+    x0 = x0 < 0 ? 0 : x0; y0 = y0 < 0 ? 0 : y0;
+    x1 = x1 > c->w ? c->w : x1; y1 = y1 > c->h ? c->h : y1;
+    if ((x0 < x1) & (y0 < y1) & (s->global_alpha_i != 0)) {
+      src[0] += (int)(x0 - dx); src[1] += (int)(y0 - dy);
+      src[2] = (int)(x1 - x0); src[3] = (int)(y1 - y0);
+      if (o_blit_source(c, st, b.image_index, src)) {
+        o_init_pattern_simple(st, 0, -(int)x0, -(int)y0, 0, 0);
+        fill_box_a(c, (int)x0, (int)y0, (int)x1, (int)y1);
+      }
+    }
+  }
+  else if (op == BLGPU_OP_BLIT_IMAGE_D && s->final_type <= O_TT_TRANSLATE) {
+    const OMat* t = &s->final_fixed;
+    double sx = b.rect[0] * t->m00 + t->m20, sy = b.rect[1] * t->m11 + t->m21;
+    double dx0 = o_max(sx, 0.0), dy0 = o_max(sy, 0.0);
+    double dx1 = o_min(sx + (double)src[2] * t->m00, (double)c->w * 256.0);
+    double dy1 = o_min(sy + (double)src[3] * t->m11, (double)c->h * 256.0);
+    if (s->global_alpha_i != 0 && ((dx0 < dx1) & (dy0 < dy1))) {
+      int ix0 = o_trunc_to_int(dx0), iy0 = o_trunc_to_int(dy0), ix1 = o_trunc_to_int(dx1), iy1 = o_trunc_to_int(dy1);
+      if ((ix0 < ix1) & (iy0 < iy1)) {
+        int64_t fx = o_floor_to_int64(sx), fy = o_floor_to_int64(sy);
+        int ok;
+        if (!((fx | fy) & 0xFF)) {
+          int x0 = ix0 >> 8, y0 = iy0 >> 8, x1 = (ix1 + 0xFF) >> 8, y1 = (iy1 + 0xFF) >> 8;
+          int tx = (int)(fx >> 8), ty = (int)(fy >> 8);
+          src[0] += x0 - tx; src[1] += y0 - ty; src[2] = x1 - x0; src[3] = y1 - y0;
+          ok = o_blit_source(c, st, b.image_index, src);
+          if (ok) o_init_pattern_simple(st, 0, -x0, -y0, 0, 0);
+        }
+        else {
+          ok = o_blit_source(c, st, b.image_index, src);
+          if (ok) o_init_pattern_fx_fy(st, 2 /* REFLECT */, s->pattern_quality, fx, fy);
+        }
+        if (ok) fill_clipped_box_f(c, ix0, iy0, ix1, iy1);
+      }
+    }
+  }
+  else if (s->global_alpha_i != 0) {
+    /* affine: BLMatrix2D::translate for a blit, the rectangle's scale x final transform for a
+     * scaled blit (TransformInternal::multiply, matrix_p.h:57-64) */
+    OMat ft;
+    double bx0 = b.rect[0], by0 = b.rect[1], bx1, by1;
+    if (op == BLGPU_OP_BLIT_IMAGE_D) {
+      ft = s->final_t;
+      ft.m20 += b.rect[0] * ft.m00 + b.rect[1] * ft.m10;
+      ft.m21 += b.rect[0] * ft.m01 + b.rect[1] * ft.m11;
+      bx1 = b.rect[0] + (double)src[2]; by1 = b.rect[1] + (double)src[3];
+    }
+    else {
+      OMat sc = { b.rect[2] / (double)src[2], 0.0, 0.0, b.rect[3] / (double)src[3], b.rect[0], b.rect[1] };
+      o_mat_multiply(&ft, &sc, &s->final_t);
+      bx1 = b.rect[0] + b.rect[2]; by1 = b.rect[1] + b.rect[3];
+    }
+    if (o_blit_source(c, st, b.image_index, src) && o_init_pattern_affine(st, 2 /* REFLECT */, s->pattern_quality, &ft))
+      fill_box_d(c, bx0, by0, bx1, by1);
+  }
+  free(st);
+}
+
 static int replay(OCtx* c, const uint8_t* base, size_t size, size_t off) {
   while (off + 8 <= size) {
     uint32_t op, len;
@@ -750,6 +857,10 @@ static int replay(OCtx* c, const uint8_t* base, size_t size, size_t off) {
       case BLGPU_OP_STROKE_PATH_D: case BLGPU_OP_STROKE_POLYLINE_D: case BLGPU_OP_STROKE_POLYGON_D:
       case BLGPU_OP_STROKE_BOX_D: case BLGPU_OP_STROKE_RECT_D: case BLGPU_OP_STROKE_LINE_D:
         stroke_op(c, op, p);
+        break;
+      case BLGPU_OP_BLIT_IMAGE_I: case BLGPU_OP_BLIT_IMAGE_D:
+      case BLGPU_OP_BLIT_SCALED_IMAGE_I: case BLGPU_OP_BLIT_SCALED_IMAGE_D:
+        blit_op(c, op, p);
         break;
 
       case BLGPU_OP_CLEAR_ALL: {

@@ -201,6 +201,30 @@ static void replay(const Stream& s, BLImage& img, uint32_t threads) {
         break;
       }
       case BLGPU_OP_FILL_PATH_D: ctx.fill_path(read_path(p)); break;
+      case BLGPU_OP_BLIT_IMAGE_I: case BLGPU_OP_BLIT_IMAGE_D:
+      case BLGPU_OP_BLIT_SCALED_IMAGE_I: case BLGPU_OP_BLIT_SCALED_IMAGE_D: {
+        BLGpuStreamBlit b = rd<BLGpuStreamBlit>(p);
+        const BLImage& im = s.images[b.image_index];
+        BLRectI area(b.area[0], b.area[1], b.area[2], b.area[3]);
+        const BLRectI* ap = b.has_area ? &area : nullptr;
+        if (op == BLGPU_OP_BLIT_IMAGE_I) {
+          BLPointI o(int(b.rect[0]), int(b.rect[1]));
+          bl_context_blit_image_i(&ctx, &o, &im, ap);
+        }
+        else if (op == BLGPU_OP_BLIT_IMAGE_D) {
+          BLPoint o(b.rect[0], b.rect[1]);
+          bl_context_blit_image_d(&ctx, &o, &im, ap);
+        }
+        else if (op == BLGPU_OP_BLIT_SCALED_IMAGE_I) {
+          BLRectI r(int(b.rect[0]), int(b.rect[1]), int(b.rect[2]), int(b.rect[3]));
+          bl_context_blit_scaled_image_i(&ctx, &r, &im, ap);
+        }
+        else {
+          BLRect r(b.rect[0], b.rect[1], b.rect[2], b.rect[3]);
+          bl_context_blit_scaled_image_d(&ctx, &r, &im, ap);
+        }
+        break;
+      }
       case BLGPU_OP_SAVE: ctx.save(); break;
       case BLGPU_OP_RESTORE: ctx.restore(); break;
       default:

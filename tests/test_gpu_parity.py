@@ -479,3 +479,49 @@ def test_stroke_context_calls_match_stream(runtimes):
             ctx2.stroke_path_d([1, 1], np.array([[0.0, 0.0], [4.0, 4.0]]))   # no MOVE: invalid geometry
         finally:
             ctx2.end()
+
+
+# --- image blits ----------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("seed", range(1300, 1306))
+def test_blits_vs_oracle(runtimes, seed):
+    """Integer / fractional / scaled / transformed blits of image areas, clipped, both qualities."""
+    sw = scenes.blits(seed=seed, count=150, width=(320, 61, 500)[seed % 3], height=(240, 203, 90)[seed % 3])
+    stream = sw.to_bytes()
+    got = bg.render_stream(runtimes(), stream)
+    want = oracle_lib.render(stream)
+    assert not _diff(got, want), _diff(got, want)
+
+
+def test_blit_context_calls_match_stream(runtimes):
+    rng = np.random.default_rng(9)
+    w, h = 160, 120
+    img = scenes.premultiplied_noise(rng, 37, 23)
+    sw = scenes.StreamWriter(w, h)
+    sw.add_image(img)
+    out = np.zeros((h, w), dtype=np.uint32)
+    ctx = bg.Context(runtimes(), out)
+    sw.solid(0xFF102030); sw.fill_all()
+    ctx.set_fill_style_rgba32(0xFF102030); ctx.fill_all()
+    sw.blit_image_i(10, 12, 0); ctx.blit_image_i(10, 12, img)
+    sw.blit_image_i(140, 100, 0, [3, 4, 20, 15]); ctx.blit_image_i(140, 100, img, [3, 4, 20, 15])
+    sw.blit_image_d(30.25, 60.5, 0); ctx.blit_image_d(30.25, 60.5, img)
+    sw.hint(scenes.HINT_PATTERN_QUALITY, scenes.NEAREST); ctx.set_hint(2, 0)
+    sw.blit_image_d(80.75, 5.125, 0, [1, 1, 30, 20]); ctx.blit_image_d(80.75, 5.125, img, [1, 1, 30, 20])
+    sw.hint(scenes.HINT_PATTERN_QUALITY, scenes.BILINEAR); ctx.set_hint(2, 1)
+    sw.global_alpha(0.6); ctx.set_global_alpha(0.6)
+    sw.blit_scaled_image_d(90.0, 50.0, 60.5, 40.25, 0); ctx.blit_scaled_image_d(90.0, 50.0, 60.5, 40.25, img)
+    sw.blit_scaled_image_i(5, 80, 50, 30, 0, [0, 0, 10, 10]); ctx.blit_scaled_image_i(5, 80, 50, 30, img, [0, 0, 10, 10])
+    m = [0.9, 0.4, -0.4, 0.9, 30.0, -10.0]
+    sw.transform(m); ctx.set_transform(m)
+    sw.blit_image_i(40, 40, 0); ctx.blit_image_i(40, 40, img)
+    ctx.end()
+    stream = sw.to_bytes()
+    assert not _diff(out, bg.render_stream(runtimes(), stream))
+    assert not _diff(out, oracle_lib.render(stream))
+    ctx2 = bg.Context(runtimes(), np.zeros((8, 8), dtype=np.uint32))
+    try:
+        with pytest.raises(bg.BLGpuError):
+            ctx2.blit_image_i(0, 0, img, [30, 0, 10, 5])        # area outside the image
+    finally:
+        ctx2.end()
