@@ -28,6 +28,7 @@ ERROR_INVALID_GEOMETRY = 0x00010034
 ERROR_DEVICE = 0x00011000
 
 FORMAT_PRGB32 = 1
+FORMAT_A8 = 3
 IMAGE_DEVICE_MEMORY = 1
 FLUSH_SYNC = 0x80000000
 FLUSH_ASYNC = 0x1            # start rendering what is recorded and return (see include/blgpu.h)
@@ -152,6 +153,8 @@ _SIGNATURES = {
     "blgpu_context_blit_scaled_image_i": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                           ctypes.POINTER(Image), _P],
     "blgpu_context_blit_scaled_image_d": [_P, _D, _D, _D, _D, ctypes.POINTER(Image), _P],
+    "blgpu_context_fill_mask_i": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(Image), _P],
+    "blgpu_context_fill_mask_d": [_P, _D, _D, ctypes.POINTER(Image), _P],
     "blgpu_stroke_outline_d": [_P, _P, ctypes.c_size_t, ctypes.POINTER(StrokeOptions), _P, _P, ctypes.c_size_t,
                                ctypes.POINTER(ctypes.c_size_t)],
     "blgpu_context_submit_stream": [_P, ctypes.c_char_p, ctypes.c_size_t],
@@ -411,6 +414,19 @@ class Context:
 
     def blit_scaled_image_d(self, x, y, w, h, image, area=None):
         self._blit("blgpu_context_blit_scaled_image_d", (x, y, w, h), image, area)
+
+    # -- masked fills (A8 masks: (h, w) uint8 arrays) ---------------------------------------------------
+    def _fill_mask(self, name, x, y, mask, area):
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        if m.ndim != 2:
+            raise ValueError("mask must be a (h, w) uint8 array")
+        img = Image(m.ctypes.data, m.shape[1], m.shape[1], m.shape[0], FORMAT_A8, 0)
+        self._keep.append((img, m))
+        ar = (ctypes.c_int32 * 4)(*area) if area is not None else None
+        self._call(name, x, y, ctypes.byref(img), ctypes.cast(ar, _P) if ar is not None else None)
+
+    def fill_mask_i(self, x, y, mask, area=None): self._fill_mask("blgpu_context_fill_mask_i", x, y, mask, area)
+    def fill_mask_d(self, x, y, mask, area=None): self._fill_mask("blgpu_context_fill_mask_d", x, y, mask, area)
 
     def stroke_box_d(self, x0, y0, x1, y1): self._call("blgpu_context_stroke_box_d", x0, y0, x1, y1)
     def stroke_rect_d(self, x, y, w, h): self._call("blgpu_context_stroke_rect_d", x, y, w, h)

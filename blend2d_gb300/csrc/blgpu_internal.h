@@ -31,7 +31,10 @@ constexpr int kStripShift = 2;
 enum FillKind : uint32_t {
   kFillAnalytic = 0,   // edges -> analytic coverage (FillAnalytic_Base)
   kFillBoxA = 1,       // pixel-aligned box (FillBoxA_Base)
-  kFillBoxU = 2        // 24.8 box with fractional borders (FillData::init_box_u_8bpc_24x8)
+  kFillBoxU = 2,       // 24.8 box with fractional borders (FillData::init_box_u_8bpc_24x8)
+  kFillMaskA = 3       // pixel-aligned box with an A8 mask (fill_box_masked_a): geom_first / xform =
+                       // low / high 32 bits of the mask's byte offset in the image pool at the box's
+                       // top-left pixel, geom_count = the mask's row pitch in bytes
 };
 
 enum GeomKind : uint32_t { kGeomPolygon = 0, kGeomPath = 1 };

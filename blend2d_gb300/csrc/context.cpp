@@ -874,6 +874,69 @@ struct BLGpuContext {
     return BLGPU_SUCCESS;
   }
 
+  // --- masked fills (rastercontext.cpp:3679-3790) -------------------------------------------
+  // The fill style composited through an A8 mask over a pixel-aligned box (fill_box_masked_a):
+  // per pixel the mask byte, times the fill alpha below 255. As in the reference, only a pixel
+  // aligned mask is supported; any other placement returns BLGPU_ERROR_NOT_IMPLEMENTED.
+  static bool valid_mask(const BLGpuImage* im) {
+    return im && im->format == BLGPU_FORMAT_A8 && im->width >= 0 && im->height >= 0 &&
+           (im->width == 0 || im->pixel_data) && im->stride >= intptr_t(im->width);
+  }
+
+  void record_mask(const Fill& f, int x0, int y0, int x1, int y1, const BLGpuImage& mask, int mx, int my) {
+    const uint64_t words = frame->add_image(mask);
+    const uint64_t off = words * 4u + uint64_t(uint32_t(my)) * uint32_t(mask.width) + uint32_t(mx);
+    DevCmd& c = push_cmd(kFillMaskA, f.style, f.src_copy, f.alpha);
+    c.box[0] = x0; c.box[1] = y0; c.box[2] = x1; c.box[3] = y1;
+    c.fetch_y0 = y0;
+    c.geom_first = uint32_t(off);
+    c.xform = uint32_t(off >> 32);
+    c.geom_count = uint32_t(mask.width);
+  }
+
+  BLGpuResult fill_mask_d(double x, double y, const BLGpuImage* mask, const int32_t* area) {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    if (!valid_mask(mask)) return BLGPU_ERROR_INVALID_VALUE;
+    int src[4];
+    if (!image_area(*mask, area, src)) return BLGPU_ERROR_INVALID_VALUE;
+    Fill f;
+    if (!resolve_fill(f)) return BLGPU_SUCCESS;
+    if (s.final_type > kTTTranslate) return BLGPU_ERROR_NOT_IMPLEMENTED;
+    // fill_unclipped_mask_d (rastercontext.cpp:3594-3676)
+    const Mat& t = s.final_fixed;
+    double sx = x * t.m00 + t.m20, sy = y * t.m11 + t.m21;
+    double bx0 = sx < 0.0 ? 0.0 : sx, by0 = sy < 0.0 ? 0.0 : sy;
+    double ex = sx + double(src[2]) * t.m00, ey = sy + double(src[3]) * t.m11;
+    double cx1 = double(w) * 256.0, cy1 = double(h) * 256.0;
+    double bx1 = cx1 < ex ? cx1 : ex, by1 = cy1 < ey ? cy1 : ey;
+    if (!((bx0 < bx1) & (by0 < by1))) return BLGPU_SUCCESS;
+    int64_t fx = floor_to_int64(sx), fy = floor_to_int64(sy);
+    int ux0 = trunc_to_int(bx0), uy0 = trunc_to_int(by0), ux1 = trunc_to_int(bx1), uy1 = trunc_to_int(by1);
+    if ((fx | fy) & 0xFF) return BLGPU_ERROR_NOT_IMPLEMENTED;
+    int x0 = ux0 >> 8, y0 = uy0 >> 8, x1 = (ux1 + 0xFF) >> 8, y1 = (uy1 + 0xFF) >> 8;
+    int tx = int(fx >> 8), ty = int(fy >> 8);
+    if (((ux0 | uy0 | ux1 | uy1) & 0xFF) != 0) return BLGPU_ERROR_NOT_IMPLEMENTED;
+    record_mask(f, x0, y0, x1, y1, *mask, src[0] + x0 - tx, src[1] + y0 - ty);
+    return BLGPU_SUCCESS;
+  }
+
+  BLGpuResult fill_mask_i(int32_t x, int32_t y, const BLGpuImage* mask, const int32_t* area) {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    if (!valid_mask(mask)) return BLGPU_ERROR_INVALID_VALUE;
+    if (!s.integral_translation) return fill_mask_d(double(x), double(y), mask, area);
+    int src[4];
+    if (!image_area(*mask, area, src)) return BLGPU_ERROR_INVALID_VALUE;
+    int64_t dx = int64_t(x) + s.tx_i, dy = int64_t(y) + s.ty_i;
+    int64_t x0 = dx, y0 = dy, x1 = x0 + src[2], y1 = y0 + src[3];
+    x0 = x0 < 0 ? 0 : x0; y0 = y0 < 0 ? 0 : y0;
+    x1 = x1 > w ? w : x1; y1 = y1 > h ? h : y1;
+    if ((x0 >= x1) | (y0 >= y1)) return BLGPU_SUCCESS;
+    Fill f;
+    if (!resolve_fill(f)) return BLGPU_SUCCESS;
+    record_mask(f, int(x0), int(y0), int(x1), int(y1), *mask, src[0] + int(x0 - dx), src[1] + int(y0 - dy));
+    return BLGPU_SUCCESS;
+  }
+
   BLGpuResult save() { stack.push_back(s); return BLGPU_SUCCESS; }
   BLGpuResult restore() {
     if (stack.empty()) return BLGPU_ERROR_NO_STATES_TO_RESTORE;
@@ -1059,6 +1122,28 @@ BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
         else if (op == BLGPU_OP_BLIT_IMAGE_D) r = blit_image_d(b.rect[0], b.rect[1], im, ar);
         else r = blit_scaled_image(b.rect[0], b.rect[1], b.rect[2], b.rect[3], im, ar, op == BLGPU_OP_BLIT_SCALED_IMAGE_I);
         if (r == BLGPU_ERROR_INVALID_VALUE) r = BLGPU_SUCCESS;   // an area outside the image draws nothing
+        break;
+      }
+      case BLGPU_OP_FILL_MASK_I: case BLGPU_OP_FILL_MASK_D: {
+        BLGpuStreamMask m;
+        if (!need(sizeof(m))) return BLGPU_ERROR_INVALID_VALUE;
+        memcpy(&m, p, sizeof(m));
+        if (m.width > 65535u || m.height > 65535u) return BLGPU_ERROR_INVALID_VALUE;
+        if (!need(sizeof(m) + size_t(m.width) * m.height)) return BLGPU_ERROR_INVALID_VALUE;
+        // copied out of the stream like its pattern images: read when the frame runs
+        const size_t nb = size_t(m.width) * m.height;
+        stream_images->emplace_back((nb + 3u) / 4u + 1u);
+        memcpy(stream_images->back().data(), p + sizeof(m), nb);
+        BLGpuImage im{};
+        im.pixel_data = stream_images->back().data();
+        im.stride = intptr_t(m.width);
+        im.width = int32_t(m.width);
+        im.height = int32_t(m.height);
+        im.format = BLGPU_FORMAT_A8;
+        const int32_t* ar = m.has_area ? m.area : nullptr;
+        if (op == BLGPU_OP_FILL_MASK_I) r = fill_mask_i(int32_t(m.origin[0]), int32_t(m.origin[1]), &im, ar);
+        else r = fill_mask_d(m.origin[0], m.origin[1], &im, ar);
+        if (r == BLGPU_ERROR_INVALID_VALUE || r == BLGPU_ERROR_NOT_IMPLEMENTED) r = BLGPU_SUCCESS;
         break;
       }
       case BLGPU_OP_SAVE: save(); break;
@@ -1276,6 +1361,12 @@ BLGPU_API BLGpuResult blgpu_context_blit_scaled_image_i(BLGpuContext* ctx, int32
 BLGPU_API BLGpuResult blgpu_context_blit_scaled_image_d(BLGpuContext* ctx, double x, double y, double w, double h,
                                                         const BLGpuImage* image, const int32_t* area) {
   CTX_CALL(blit_scaled_image(x, y, w, h, image, area, false));
+}
+BLGPU_API BLGpuResult blgpu_context_fill_mask_i(BLGpuContext* ctx, int32_t x, int32_t y, const BLGpuImage* mask, const int32_t* area) {
+  CTX_CALL(fill_mask_i(x, y, mask, area));
+}
+BLGPU_API BLGpuResult blgpu_context_fill_mask_d(BLGpuContext* ctx, double x, double y, const BLGpuImage* mask, const int32_t* area) {
+  CTX_CALL(fill_mask_d(x, y, mask, area));
 }
 BLGPU_API BLGpuResult blgpu_context_submit_stream(BLGpuContext* ctx, const void* stream, size_t size) {
   CTX_CALL(submit_stream(static_cast<const uint8_t*>(stream), size));

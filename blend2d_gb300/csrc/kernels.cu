@@ -719,7 +719,7 @@ __global__ void cmd_tiles_kernel(FrameView f, uint32_t* cmdrow_counts_per_cmd, u
       f.cmds_rw[c].box[2] = x1; f.cmds_rw[c].box[3] = y1;
     }
   }
-  else if (cmd.kind == kFillBoxA) {
+  else if (cmd.kind == kFillBoxA || cmd.kind == kFillMaskA) {
     x0 = cmd.box[0]; y0 = cmd.box[1]; x1 = cmd.box[2] - 1; y1 = cmd.box[3] - 1;
   }
   else {
@@ -1029,6 +1029,22 @@ __device__ __forceinline__ void strip_masks(const FrameView& f, uint32_t ckind, 
       bool in_y = y >= cmd.box[1] && y < cmd.box[3];
 #pragma unroll
       for (int k = 0; k < 4; k++) m[k] = (in_y && xp + k >= cmd.box[0] && xp + k < cmd.box[2]) ? alpha : 0u;
+    }
+    else if (ckind == kFillMaskA) {
+      // FillMask_Base's vmask spans (fillgeneric_p.h:67-162, compopgeneric_p.h:165-183): the mask
+      // byte, times the fill alpha below 255 (udiv255)
+      const bool in_y = y >= cmd.box[1] && y < cmd.box[3];
+      const uint8_t* row = reinterpret_cast<const uint8_t*>(f.images) +
+                           ((uint64_t(cmd.xform) << 32) | cmd.geom_first) + int64_t(y - cmd.box[1]) * cmd.geom_count;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        uint32_t v = 0u;
+        if (in_y && xp + k >= cmd.box[0] && xp + k < cmd.box[2]) {
+          v = __ldg(row + (xp + k - cmd.box[0]));
+          if (alpha < 255u) v = ((v * alpha + 0x80u) * 0x101u) >> 16;
+        }
+        m[k] = v;
+      }
     }
     else {
 #pragma unroll

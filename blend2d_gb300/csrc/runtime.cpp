@@ -83,17 +83,21 @@ uint32_t Frame::add_canvas(const BLGpuImage& image, bool upload) {
 }
 
 uint64_t Frame::add_image(const BLGpuImage& image) {
+  const int32_t bpp = image.format == BLGPU_FORMAT_A8 ? 1 : 4;
   for (const FrameImage& im : images)
-    if (im.pixels == image.pixel_data && im.w == image.width && im.h == image.height && im.stride == image.stride)
+    if (im.pixels == image.pixel_data && im.w == image.width && im.h == image.height && im.stride == image.stride &&
+        im.bpp == bpp)
       return im.pool_offset;
   FrameImage im;
   im.pixels = image.pixel_data;
   im.stride = image.stride;
   im.w = image.width;
   im.h = image.height;
+  im.bpp = bpp;
   im.device = (image.flags & BLGPU_IMAGE_DEVICE_MEMORY) != 0;
   im.pool_offset = image_words;
-  image_words += align_up(uint64_t(uint32_t(image.width)) * uint32_t(image.height), 4);
+  const uint64_t bytes = uint64_t(uint32_t(image.width)) * uint32_t(image.height) * uint32_t(bpp);
+  image_words += align_up((bytes + 3u) / 4u, 4);
   images.push_back(im);
   return im.pool_offset;
 }
@@ -353,7 +357,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   needs_pack(fr.lut_jobs.ptr_pinned, sizeof(DevLutJob) * fr.lut_jobs.size());
   needs_pack(fr.stops.ptr_pinned, sizeof(DevStop) * fr.stops.size());
   for (const FrameImage& im : fr.images)
-    if (!im.device) pack_bytes += align_up(size_t(im.w) * size_t(im.h) * 4u, 256);
+    if (!im.device) pack_bytes += align_up(size_t(im.w) * size_t(im.h) * size_t(im.bpp), 256);
   // the previous frame's copies out of the staging buffer must have completed
   BLGPU_CHECK(cudaStreamSynchronize(stream));
   if (pack_bytes > host_staging_size) {
@@ -393,7 +397,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   BLGPU_CHECK(put(v.stops, fr.stops.data(), sizeof(DevStop) * fr.stops.size(), fr.stops.ptr_pinned));
   for (const FrameImage& im : fr.images) {
     if (im.device) continue;
-    const size_t row = size_t(im.w) * 4u, bytes = row * size_t(im.h);
+    const size_t row = size_t(im.w) * size_t(im.bpp), bytes = row * size_t(im.h);
     char* dst = hs + hs_off;
     for (int y = 0; y < im.h; y++)
       memcpy(dst + size_t(y) * row, static_cast<const char*>(im.pixels) + intptr_t(y) * im.stride, row);
@@ -403,8 +407,8 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   }
   for (const FrameImage& im : fr.images) {
     if (!im.device) continue;
-    BLGPU_CHECK(cudaMemcpy2DAsync(const_cast<uint32_t*>(v.images) + im.pool_offset, size_t(im.w) * 4u, im.pixels,
-                                  size_t(im.stride), size_t(im.w) * 4u, size_t(im.h), cudaMemcpyDeviceToDevice, stream));
+    BLGPU_CHECK(cudaMemcpy2DAsync(const_cast<uint32_t*>(v.images) + im.pool_offset, size_t(im.w) * size_t(im.bpp), im.pixels,
+                                  size_t(im.stride), size_t(im.w) * size_t(im.bpp), size_t(im.h), cudaMemcpyDeviceToDevice, stream));
   }
   // Canvas content (the pipeline composites onto it).
   for (uint32_t i = 0; i < ncv; i++) {
@@ -707,8 +711,8 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
   BLGPU_CHECK(put(v.lut_jobs, fr.lut_jobs.data(), sizeof(DevLutJob) * fr.lut_jobs.size()));
   BLGPU_CHECK(put(v.stops, fr.stops.data(), sizeof(DevStop) * fr.stops.size()));
   for (const FrameImage& fi : fr.images) {
-    BLGPU_CHECK(cudaMemcpy2DAsync(const_cast<uint32_t*>(v.images) + fi.pool_offset, size_t(fi.w) * 4u, fi.pixels,
-                                  size_t(fi.stride), size_t(fi.w) * 4u, size_t(fi.h),
+    BLGPU_CHECK(cudaMemcpy2DAsync(const_cast<uint32_t*>(v.images) + fi.pool_offset, size_t(fi.w) * size_t(fi.bpp), fi.pixels,
+                                  size_t(fi.stride), size_t(fi.w) * size_t(fi.bpp), size_t(fi.h),
                                   fi.device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
   }
 

@@ -21,8 +21,9 @@ struct FrameImage {
   const void* pixels;
   intptr_t stride;          // bytes
   int32_t w, h;
+  int32_t bpp;              // bytes per pixel: 4 (PRGB32) or 1 (A8 masks, rows packed tightly)
   bool device;
-  uint64_t pool_offset;     // first pixel in the frame's image pool
+  uint64_t pool_offset;     // first pixel in the frame's image pool (32-bit words)
 };
 
 // A canvas's render target.

@@ -66,6 +66,8 @@ OP_BLIT_IMAGE_I = 35
 OP_BLIT_IMAGE_D = 36
 OP_BLIT_SCALED_IMAGE_I = 37
 OP_BLIT_SCALED_IMAGE_D = 38
+OP_FILL_MASK_I = 39
+OP_FILL_MASK_D = 40
 
 SRC_OVER, SRC_COPY = 0, 1
 NON_ZERO, EVEN_ODD = 0, 1
@@ -262,6 +264,21 @@ class StreamWriter:
 
     def blit_scaled_image_d(self, x, y, w, h, image_index, area=None):
         self._blit(OP_BLIT_SCALED_IMAGE_D, [x, y, w, h], image_index, area)
+
+    # -- masked fills (A8 masks travel in the record) -----------------------------------------------
+    def _mask(self, op, x, y, mask: np.ndarray, area):
+        mask = np.ascontiguousarray(mask, dtype=np.uint8)
+        h, w = mask.shape
+        ar = list(area) if area is not None else [0, 0, 0, 0]
+        self._rec(op, struct.pack("<2dIIII4i", float(x), float(y), w, h, 1 if area is not None else 0, 0, *ar)
+                  + mask.tobytes())
+        self.fill_count += 1
+
+    def fill_mask_i(self, x, y, mask, area=None):
+        self._mask(OP_FILL_MASK_I, int(x), int(y), mask, area)
+
+    def fill_mask_d(self, x, y, mask, area=None):
+        self._mask(OP_FILL_MASK_D, x, y, mask, area)
 
     def save(self):
         self._rec(OP_SAVE)
@@ -792,6 +809,60 @@ def blits(seed: int = 40, width: int = 320, height: int = 240, count: int = 150)
             sw.blit_scaled_image_d(x, y, float(rng.uniform(1, 200)), float(rng.uniform(1, 150)), idx, area)
         else:
             sw.blit_scaled_image_i(int(x), int(y), int(rng.integers(1, 200)), int(rng.integers(1, 150)), idx, area)
+    return sw
+
+
+def masks(seed: int = 50, width: int = 300, height: int = 220, count: int = 120) -> StreamWriter:
+    """Masked fills: A8 masks (noise, gradients, binary), integer and pixel-aligned double origins,
+    mask areas, clipping, translations (fractional ones and rotations: not supported by the
+    reference's masked fill, which draws nothing there), solid / gradient / pattern fill styles,
+    fill and global alpha, SrcOver/SrcCopy."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sw = StreamWriter(width, height)
+    sw.solid(0xFF202020)
+    sw.fill_all()
+    sw.add_image(premultiplied_noise(rng, 40, 30))
+    for i in range(count):
+        mw, mh = int(rng.integers(1, 90)), int(rng.integers(1, 70))
+        kind = int(rng.integers(0, 3))
+        if kind == 0:
+            mask = rng.integers(0, 256, (mh, mw), dtype=np.uint8)
+        elif kind == 1:
+            mask = (np.add.outer(np.arange(mh) * 3, np.arange(mw) * 2) % 256).astype(np.uint8)
+        else:
+            mask = (rng.random((mh, mw)) < 0.5).astype(np.uint8) * 255
+        area = None
+        if rng.random() < 0.3:
+            ax, ay = int(rng.integers(0, mw)), int(rng.integers(0, mh))
+            area = [ax, ay, int(rng.integers(1, mw - ax + 1)), int(rng.integers(1, mh - ay + 1))]
+        r = float(rng.random())
+        if r < 0.5:
+            sw.solid(int(rng.integers(0, 2**32, dtype=np.uint64)))
+        elif r < 0.8:
+            _gradient_style(rng, sw, 0.0, 0.0, float(max(width, height)))
+        else:
+            sw.pattern(0, int(rng.integers(0, 3)), transform=[1.0, 0.0, 0.0, 1.0, float(rng.integers(0, 50)), 3.0])
+        sw.comp_op(SRC_COPY if rng.random() < 0.2 else SRC_OVER)
+        if rng.random() < 0.2:
+            sw.fill_alpha(float(rng.uniform(0.1, 1.0)))
+        elif rng.random() < 0.2:
+            sw.fill_alpha(1.0)
+        if rng.random() < 0.1:
+            sw.global_alpha(float(rng.uniform(0.3, 1.0)))
+        t = float(rng.random())
+        if t < 0.15:
+            sw.transform([1.0, 0.0, 0.0, 1.0, float(rng.integers(-20, 20)), float(rng.integers(-20, 20))])
+        elif t < 0.2:
+            sw.transform([1.0, 0.0, 0.0, 1.0, float(rng.uniform(-20, 20)), 2.5])
+        elif t < 0.25:
+            sw.transform([0.9, 0.3, -0.3, 0.9, 10.0, 5.0])
+        elif t < 0.45:
+            sw.reset_transform()
+        x, y = int(rng.integers(-40, width)), int(rng.integers(-40, height))
+        if rng.random() < 0.5:
+            sw.fill_mask_i(x, y, mask, area)
+        else:
+            sw.fill_mask_d(float(x) + (0.5 if rng.random() < 0.15 else 0.0), float(y), mask, area)
     return sw
 
 

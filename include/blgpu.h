@@ -37,6 +37,7 @@ enum {
 /* Image formats (BLFormat) and image-placement flags. */
 enum {
   BLGPU_FORMAT_PRGB32 = 1,                   /* BL_FORMAT_PRGB32 */
+  BLGPU_FORMAT_A8 = 3,                       /* BL_FORMAT_A8 (masks for fill_mask) */
   BLGPU_IMAGE_DEVICE_MEMORY = 0x1u           /* pixel_data is a CUDA device pointer */
 };
 
@@ -207,6 +208,13 @@ BLGpuResult blgpu_context_blit_scaled_image_i(BLGpuContext* ctx, int32_t x, int3
                                               const BLGpuImage* image, const int32_t* area);                                  /* bl_context_blit_scaled_image_i */
 BLGpuResult blgpu_context_blit_scaled_image_d(BLGpuContext* ctx, double x, double y, double w, double h,
                                               const BLGpuImage* image, const int32_t* area);                                  /* bl_context_blit_scaled_image_d */
+
+/* Masked fills (rastercontext.cpp:3679-3790): the fill style composited through an A8 mask
+ * (BLGPU_FORMAT_A8; `area` = {x, y, w, h} of it or NULL) at the origin, per pixel mask x fill alpha.
+ * Like the reference, only a pixel-aligned placement under a translation is supported; any other
+ * returns BLGPU_ERROR_NOT_IMPLEMENTED. */
+BLGpuResult blgpu_context_fill_mask_i(BLGpuContext* ctx, int32_t x, int32_t y, const BLGpuImage* mask, const int32_t* area); /* bl_context_fill_mask_i */
+BLGpuResult blgpu_context_fill_mask_d(BLGpuContext* ctx, double x, double y, const BLGpuImage* mask, const int32_t* area);   /* bl_context_fill_mask_d */
 
 /* BLStrokeOptions without the dash array (core/path.h:330-352). */
 typedef struct BLGpuStrokeOptions {

@@ -84,6 +84,9 @@ enum {
   BLGPU_OP_BLIT_IMAGE_D = 36,      /* BLGpuStreamBlit (x, y)                       bl_context_blit_image_d */
   BLGPU_OP_BLIT_SCALED_IMAGE_I = 37, /* BLGpuStreamBlit (x, y, w, h as integers)   bl_context_blit_scaled_image_i */
   BLGPU_OP_BLIT_SCALED_IMAGE_D = 38, /* BLGpuStreamBlit (x, y, w, h)               bl_context_blit_scaled_image_d */
+  /* masked fills (rastercontext.cpp:3679-3790): the A8 mask travels in the record */
+  BLGPU_OP_FILL_MASK_I = 39,       /* BLGpuStreamMask (x, y integral) + u8 mask[w*h] (pad 8)  bl_context_fill_mask_i */
+  BLGPU_OP_FILL_MASK_D = 40,       /* BLGpuStreamMask + u8 mask[w*h] (pad 8)       bl_context_fill_mask_d */
   BLGPU_OP_COUNT
 };
 
@@ -135,5 +138,15 @@ typedef struct BLGpuStreamBlit {
   uint32_t has_area;
   int32_t area[4];       /* x, y, w, h */
 } BLGpuStreamBlit;
+
+/* Payload of the masked-fill records, followed by the A8 mask's rows (w bytes each). */
+typedef struct BLGpuStreamMask {
+  double origin[2];
+  uint32_t width;
+  uint32_t height;
+  uint32_t has_area;
+  uint32_t reserved;
+  int32_t area[4];       /* x, y, w, h of the mask */
+} BLGpuStreamMask;
 
 #endif /* BLGPU_STREAM_H_INCLUDED */

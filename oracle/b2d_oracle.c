@@ -778,6 +778,53 @@ static void blit_op(OCtx* c, uint32_t op, const uint8_t* p) {
   free(st);
 }
 
+/* --- masked fills (rastercontext.cpp:3679-3790, fill_unclipped_mask_d :3594-3676) ---------------
+ * Only a pixel-aligned mask under a translation renders (the reference returns
+ * BL_ERROR_NOT_IMPLEMENTED for the rest). */
+static void mask_op(OCtx* c, uint32_t op, const uint8_t* p) {
+  OState* s = &c->s;
+  BLGpuStreamMask m;
+  memcpy(&m, p, sizeof(m));
+  const uint8_t* bytes = p + sizeof(m);
+  BLGpuStreamBlit area_only;
+  memset(&area_only, 0, sizeof(area_only));
+  area_only.has_area = m.has_area;
+  memcpy(area_only.area, m.area, sizeof(m.area));
+  int src[4];
+  if (!o_image_area((int)m.width, (int)m.height, &area_only, src)) return;
+  int cop; uint32_t alpha;
+  int x0, y0, x1, y1;
+  if (op == BLGPU_OP_FILL_MASK_I && s->integral_translation) {
+    int64_t dx = (int64_t)(int32_t)m.origin[0] + s->tx_i, dy = (int64_t)(int32_t)m.origin[1] + s->ty_i;
+    int64_t bx0 = dx, by0 = dy, bx1 = bx0 + src[2], by1 = by0 + src[3];
+    bx0 = bx0 < 0 ? 0 : bx0; by0 = by0 < 0 ? 0 : by0;
+    bx1 = bx1 > c->w ? c->w : bx1; by1 = by1 > c->h ? c->h : by1;
+    if ((bx0 >= bx1) | (by0 >= by1)) return;
+    if (!resolve_fill(c, &cop, &alpha)) return;
+    src[0] += (int)(bx0 - dx); src[1] += (int)(by0 - dy);
+    x0 = (int)bx0; y0 = (int)by0; x1 = (int)bx1; y1 = (int)by1;
+  }
+  else {
+    if (!resolve_fill(c, &cop, &alpha)) return;
+    if (s->final_type > O_TT_TRANSLATE) return;
+    const OMat* t = &s->final_fixed;
+    double sx = m.origin[0] * t->m00 + t->m20, sy = m.origin[1] * t->m11 + t->m21;
+    double bx0 = o_max(sx, 0.0), by0 = o_max(sy, 0.0);
+    double bx1 = o_min(sx + (double)src[2] * t->m00, (double)c->w * 256.0);
+    double by1 = o_min(sy + (double)src[3] * t->m11, (double)c->h * 256.0);
+    if (!((bx0 < bx1) & (by0 < by1))) return;
+    int64_t fx = o_floor_to_int64(sx), fy = o_floor_to_int64(sy);
+    int ux0 = o_trunc_to_int(bx0), uy0 = o_trunc_to_int(by0), ux1 = o_trunc_to_int(bx1), uy1 = o_trunc_to_int(by1);
+    if ((fx | fy) & 0xFF) return;
+    x0 = ux0 >> 8; y0 = uy0 >> 8; x1 = (ux1 + 0xFF) >> 8; y1 = (uy1 + 0xFF) >> 8;
+    src[0] += x0 - (int)(fx >> 8); src[1] += y0 - (int)(fy >> 8);
+    if (((ux0 | uy0 | ux1 | uy1) & 0xFF) != 0) return;
+  }
+  if (c->stats) c->stats->fill_calls++;
+  c->fc.style = &s->style; c->fc.comp_op = cop; c->fc.alpha = alpha;
+  o_fill_mask_a(&c->fc, x0, y0, x1, y1, bytes + (size_t)src[1] * m.width + (size_t)src[0], (intptr_t)m.width);
+}
+
 static int replay(OCtx* c, const uint8_t* base, size_t size, size_t off) {
   while (off + 8 <= size) {
     uint32_t op, len;
@@ -861,6 +908,9 @@ static int replay(OCtx* c, const uint8_t* base, size_t size, size_t off) {
       case BLGPU_OP_BLIT_IMAGE_I: case BLGPU_OP_BLIT_IMAGE_D:
       case BLGPU_OP_BLIT_SCALED_IMAGE_I: case BLGPU_OP_BLIT_SCALED_IMAGE_D:
         blit_op(c, op, p);
+        break;
+      case BLGPU_OP_FILL_MASK_I: case BLGPU_OP_FILL_MASK_D:
+        mask_op(c, op, p);
         break;
 
       case BLGPU_OP_CLEAR_ALL: {

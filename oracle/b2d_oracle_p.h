@@ -178,6 +178,7 @@ typedef struct OFillCtx {
 
 void o_fill_box_a(OFillCtx* fc, int x0, int y0, int x1, int y1);
 void o_fill_box_u(OFillCtx* fc, int x0, int y0, int x1, int y1);
+void o_fill_mask_a(OFillCtx* fc, int x0, int y0, int x1, int y1, const uint8_t* mask, intptr_t mask_stride);
 void o_fill_analytic_band(OFillCtx* fc, int box_x1, int y0, int y1, uint32_t fill_rule,
                           uint64_t* bit_top, uint32_t* cell_top);
 

@@ -533,6 +533,28 @@ void o_fill_box_a(OFillCtx* fc, int x0, int y0, int x1, int y1) {   /* FillBoxA_
   }
 }
 
+/* Masked box fill: fill_box_masked_a (rendercommandprocsync_p.h:65-85), one vmask command per
+ * scanline repeated down the box, run by FillMask_Base (fillgeneric_p.h:67-162): the mask byte, or
+ * udiv255(mask * alpha) below full alpha (compopgeneric_p.h:165-183). */
+void o_fill_mask_a(OFillCtx* fc, int x0, int y0, int x1, int y1, const uint8_t* mask, intptr_t mask_stride) {
+  uint32_t alpha = fc->alpha;
+  OFetch f;
+  memset(&f, 0, sizeof(f));
+  f.s = fc->style;
+  fetch_span_init_y(&f, (uint32_t)y0);
+  for (int y = y0; y < y1; y++) {
+    uint32_t* drow = fc->dst + (intptr_t)y * fc->stride;
+    const uint8_t* m = mask + (intptr_t)(y - y0) * mask_stride;
+    fetch_span_start_x(&f, (uint32_t)x0);
+    for (int x = x0; x < x1; x++) {
+      uint32_t v = m[x - x0];
+      if (alpha < 255u) v = ((v * alpha + 0x80u) * 0x101u) >> 16;   /* Scalar::udiv255 */
+      comp_masked(fc, &f, drow + x, v);
+    }
+    fetch_advance_y(&f);
+  }
+}
+
 /* Box-unaligned fill: FillData::init_box_u_8bpc_24x8 mask commands (pipedefs_p.h:644-815)
  * executed by FillMask_Base (fillgeneric_p.h:67-162). Each scanline is a list of
  * {x0, x1, cmask | vmask pointer} spans. */

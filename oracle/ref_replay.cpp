@@ -225,6 +225,22 @@ static void replay(const Stream& s, BLImage& img, uint32_t threads) {
         }
         break;
       }
+      case BLGPU_OP_FILL_MASK_I: case BLGPU_OP_FILL_MASK_D: {
+        BLGpuStreamMask m = rd<BLGpuStreamMask>(p);
+        BLImage mask;
+        mask.create_from_data(int(m.width), int(m.height), BL_FORMAT_A8, const_cast<uint8_t*>(p + sizeof(m)), intptr_t(m.width));
+        BLRectI area(m.area[0], m.area[1], m.area[2], m.area[3]);
+        const BLRectI* ap = m.has_area ? &area : nullptr;
+        if (op == BLGPU_OP_FILL_MASK_I) {
+          BLPointI o(int(m.origin[0]), int(m.origin[1]));
+          bl_context_fill_mask_i(&ctx, &o, &mask, ap);
+        }
+        else {
+          BLPoint o(m.origin[0], m.origin[1]);
+          bl_context_fill_mask_d(&ctx, &o, &mask, ap);
+        }
+        break;
+      }
       case BLGPU_OP_SAVE: ctx.save(); break;
       case BLGPU_OP_RESTORE: ctx.restore(); break;
       default:

@@ -525,3 +525,38 @@ def test_blit_context_calls_match_stream(runtimes):
             ctx2.blit_image_i(0, 0, img, [30, 0, 10, 5])        # area outside the image
     finally:
         ctx2.end()
+
+
+# --- masked fills -------------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("seed", range(1400, 1405))
+def test_masked_fills_vs_oracle(runtimes, seed):
+    """A8-masked fills: integer / aligned double origins, areas, clipping, solid / gradient / pattern
+    styles, fill and global alpha (unsupported placements draw nothing, as in the reference)."""
+    sw = scenes.masks(seed=seed, count=120, width=(300, 61, 500)[seed % 3], height=(220, 203, 90)[seed % 3])
+    stream = sw.to_bytes()
+    got = bg.render_stream(runtimes(), stream)
+    want = oracle_lib.render(stream)
+    assert not _diff(got, want), _diff(got, want)
+
+
+def test_fill_mask_context_calls(runtimes):
+    rng = np.random.default_rng(11)
+    w, h = 120, 90
+    mask = rng.integers(0, 256, (40, 50), dtype=np.uint8)
+    sw = scenes.StreamWriter(w, h)
+    out = np.zeros((h, w), dtype=np.uint32)
+    ctx = bg.Context(runtimes(), out)
+    sw.solid(0xFF000000); sw.fill_all()
+    ctx.set_fill_style_rgba32(0xFF000000); ctx.fill_all()
+    sw.solid(0xFF40C0FF); ctx.set_fill_style_rgba32(0xFF40C0FF)
+    sw.fill_mask_i(10, 5, mask); ctx.fill_mask_i(10, 5, mask)
+    sw.fill_alpha(0.5); ctx.set_fill_alpha(0.5)
+    sw.fill_mask_d(80.0, 60.0, mask, [5, 5, 30, 20]); ctx.fill_mask_d(80.0, 60.0, mask, [5, 5, 30, 20])
+    with pytest.raises(bg.BLGpuError) as e:
+        ctx.fill_mask_d(3.5, 4.0, mask)                      # not pixel aligned
+    assert e.value.code == bg.ERROR_NOT_IMPLEMENTED
+    ctx.end()
+    stream = sw.to_bytes()
+    assert not _diff(out, bg.render_stream(runtimes(), stream))
+    assert not _diff(out, oracle_lib.render(stream))
