@@ -155,6 +155,8 @@ _SIGNATURES = {
     "blgpu_context_blit_scaled_image_d": [_P, _D, _D, _D, _D, ctypes.POINTER(Image), _P],
     "blgpu_context_fill_mask_i": [_P, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(Image), _P],
     "blgpu_context_fill_mask_d": [_P, _D, _D, ctypes.POINTER(Image), _P],
+    "blgpu_context_fill_geometry": [_P, _U32, ctypes.POINTER(ctypes.c_double)],
+    "blgpu_context_stroke_geometry": [_P, _U32, ctypes.POINTER(ctypes.c_double)],
     "blgpu_stroke_outline_d": [_P, _P, ctypes.c_size_t, ctypes.POINTER(StrokeOptions), _P, _P, ctypes.c_size_t,
                                ctypes.POINTER(ctypes.c_size_t)],
     "blgpu_context_submit_stream": [_P, ctypes.c_char_p, ctypes.c_size_t],
@@ -427,6 +429,15 @@ class Context:
 
     def fill_mask_i(self, x, y, mask, area=None): self._fill_mask("blgpu_context_fill_mask_i", x, y, mask, area)
     def fill_mask_d(self, x, y, mask, area=None): self._fill_mask("blgpu_context_fill_mask_d", x, y, mask, area)
+
+    # -- shapes: BL_GEOMETRY_TYPE_CIRCLE (5), ELLIPSE (6), ROUND_RECT (7), TRIANGLE (12) -------------------
+    def fill_geometry(self, gtype: int, values):
+        v = (ctypes.c_double * 6)(*([float(x) for x in values] + [0.0] * (6 - len(values))))
+        self._call("blgpu_context_fill_geometry", gtype, v)
+
+    def stroke_geometry(self, gtype: int, values):
+        v = (ctypes.c_double * 6)(*([float(x) for x in values] + [0.0] * (6 - len(values))))
+        self._call("blgpu_context_stroke_geometry", gtype, v)
 
     def stroke_box_d(self, x0, y0, x1, y1): self._call("blgpu_context_stroke_box_d", x0, y0, x1, y1)
     def stroke_rect_d(self, x, y, w, h): self._call("blgpu_context_stroke_rect_d", x, y, w, h)

@@ -937,6 +937,25 @@ struct BLGpuContext {
     return BLGPU_SUCCESS;
   }
 
+  // --- shapes (fill_unclipped_geometry, rastercontext.cpp:2926-2980): the shape's path, filled
+  // with the fill rule or stroked -------------------------------------------------------------
+  std::vector<uint8_t> shape_cmds;
+  std::vector<double> shape_xy;
+
+  BLGpuResult fill_geometry(uint32_t type, const double* v) {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    if (!v) return BLGPU_ERROR_INVALID_VALUE;
+    if (!shape_path(type, v, shape_cmds, shape_xy)) return BLGPU_ERROR_NOT_IMPLEMENTED;
+    return fill_path(shape_cmds.data(), shape_xy.data(), shape_cmds.size());
+  }
+
+  BLGpuResult stroke_geometry(uint32_t type, const double* v) {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    if (!v) return BLGPU_ERROR_INVALID_VALUE;
+    if (!shape_path(type, v, shape_cmds, shape_xy)) return BLGPU_ERROR_NOT_IMPLEMENTED;
+    return stroke_path(shape_cmds.data(), shape_xy.data(), shape_cmds.size());
+  }
+
   BLGpuResult save() { stack.push_back(s); return BLGPU_SUCCESS; }
   BLGpuResult restore() {
     if (stack.empty()) return BLGPU_ERROR_NO_STATES_TO_RESTORE;
@@ -1144,6 +1163,14 @@ BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
         if (op == BLGPU_OP_FILL_MASK_I) r = fill_mask_i(int32_t(m.origin[0]), int32_t(m.origin[1]), &im, ar);
         else r = fill_mask_d(m.origin[0], m.origin[1], &im, ar);
         if (r == BLGPU_ERROR_INVALID_VALUE || r == BLGPU_ERROR_NOT_IMPLEMENTED) r = BLGPU_SUCCESS;
+        break;
+      }
+      case BLGPU_OP_FILL_GEOMETRY: case BLGPU_OP_STROKE_GEOMETRY: {
+        if (!need(56)) return BLGPU_ERROR_INVALID_VALUE;
+        uint32_t type; memcpy(&type, p, 4);
+        double v[6]; memcpy(v, p + 8, 48);
+        r = op == BLGPU_OP_FILL_GEOMETRY ? fill_geometry(type, v) : stroke_geometry(type, v);
+        if (r == BLGPU_ERROR_NOT_IMPLEMENTED || r == BLGPU_ERROR_INVALID_GEOMETRY) r = BLGPU_SUCCESS;
         break;
       }
       case BLGPU_OP_SAVE: save(); break;
@@ -1368,6 +1395,8 @@ BLGPU_API BLGpuResult blgpu_context_fill_mask_i(BLGpuContext* ctx, int32_t x, in
 BLGPU_API BLGpuResult blgpu_context_fill_mask_d(BLGpuContext* ctx, double x, double y, const BLGpuImage* mask, const int32_t* area) {
   CTX_CALL(fill_mask_d(x, y, mask, area));
 }
+BLGPU_API BLGpuResult blgpu_context_fill_geometry(BLGpuContext* ctx, uint32_t type, const double* values) { CTX_CALL(fill_geometry(type, values)); }
+BLGPU_API BLGpuResult blgpu_context_stroke_geometry(BLGpuContext* ctx, uint32_t type, const double* values) { CTX_CALL(stroke_geometry(type, values)); }
 BLGPU_API BLGpuResult blgpu_context_submit_stream(BLGpuContext* ctx, const void* stream, size_t size) {
   CTX_CALL(submit_stream(static_cast<const uint8_t*>(stream), size));
 }

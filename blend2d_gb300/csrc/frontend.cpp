@@ -322,6 +322,62 @@ void style_gradient(HostStyle& s, const GradientDesc& g, const Mat& final_transf
   s.stops = std::move(stops);
 }
 
+// --- shapes -------------------------------------------------------------------------------------
+
+// BLPath::add_geometry (path.cpp:1408-1600, direction CW) for circles, ellipses, round rectangles
+// and triangles: the path the reference fills or strokes for fill_geometry / stroke_geometry.
+bool shape_path(uint32_t type, const double* v, std::vector<uint8_t>& cmd, std::vector<double>& xy) {
+  constexpr double kKappa = 0.55228474983;   // mathconst_p.h:52
+  cmd.clear();
+  xy.clear();
+  auto put = [&](uint8_t c, double x, double y) { cmd.push_back(c); xy.push_back(x); xy.push_back(y); };
+  auto cubic = [&](double x1, double y1, double x2, double y2, double x3, double y3) {
+    put(4, x1, y1); put(4, x2, y2); put(1, x3, y3);
+  };
+  auto box = [&](double x0, double y0, double x1, double y1) {   // PathAppender::add_box
+    put(0, x0, y0); put(1, x1, y0); put(1, x1, y1); put(1, x0, y1); put(5, NAN, NAN);
+  };
+  switch (type) {
+    case kGeometryCircle: case kGeometryEllipse: {
+      double x0 = v[0], y0 = v[1], rx = v[2];
+      double ry = type == kGeometryCircle ? fabs(rx) : v[3];
+      double kx = rx * kKappa, ky = ry * kKappa;
+      put(0, x0 + rx, y0);
+      cubic(x0 + rx, y0 + ky, x0 + kx, y0 + ry, x0, y0 + ry);
+      cubic(x0 - kx, y0 + ry, x0 - rx, y0 + ky, x0 - rx, y0);
+      cubic(x0 - rx, y0 - ky, x0 - kx, y0 - ry, x0, y0 - ry);
+      cubic(x0 + kx, y0 - ry, x0 + rx, y0 - ky, x0 + rx, y0);
+      put(5, NAN, NAN);
+      return true;
+    }
+    case kGeometryRoundRect: {
+      double x0 = v[0], y0 = v[1], x1 = v[0] + v[2], y1 = v[1] + v[3];
+      double w_half = v[2] * 0.5, h_half = v[3] * 0.5;
+      double arx = fabs(v[4]), ary = fabs(v[5]);
+      double rx = w_half < arx ? w_half : arx;
+      double ry = h_half < ary ? h_half : ary;
+      if (!(rx > 1e-14 && ry > 1e-14)) { box(x0, y0, x1, y1); return true; }   // degenerate radii
+      double kx = rx * (1.0 - kKappa), ky = ry * (1.0 - kKappa);
+      put(0, x0 + rx, y0);
+      put(1, x1 - rx, y0);
+      cubic(x1 - kx, y0, x1, y0 + ky, x1, y0 + ry);
+      put(1, x1, y1 - ry);
+      cubic(x1, y1 - ky, x1 - kx, y1, x1 - rx, y1);
+      put(1, x0 + rx, y1);
+      cubic(x0 + kx, y1, x0, y1 - ky, x0, y1 - ry);
+      put(1, x0, y0 + ry);
+      cubic(x0, y0 + ky, x0 + kx, y0, x0 + rx, y0);
+      put(5, NAN, NAN);
+      return true;
+    }
+    case kGeometryTriangle:
+      put(0, v[0], v[1]); put(1, v[2], v[3]); put(1, v[4], v[5]); put(5, NAN, NAN);
+      return true;
+    default:
+      return false;
+  }
+}
+
 // --- patterns ---------------------------------------------------------------------------------
 
 // init_pattern_tx_ty (blend2d/pipeline/pipedefs.cpp:49-110).

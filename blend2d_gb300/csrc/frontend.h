@@ -53,6 +53,12 @@ struct PatternDesc {
   const double* transform;
 };
 
+// BLGeometryType values of the shapes shape_path builds.
+constexpr uint32_t kGeometryCircle = 5, kGeometryEllipse = 6, kGeometryRoundRect = 7, kGeometryTriangle = 12;
+// The path BLPath::add_geometry makes of a circle {cx, cy, r}, ellipse {cx, cy, rx, ry}, round
+// rectangle {x, y, w, h, rx, ry} or triangle {x0, y0, x1, y1, x2, y2}; false for other types.
+bool shape_path(uint32_t type, const double* v, std::vector<uint8_t>& cmd, std::vector<double>& xy);
+
 void style_solid(HostStyle& s, uint32_t argb32);
 void style_gradient(HostStyle& s, const GradientDesc& g, const Mat& final_transform, uint32_t quality = 0);
 void style_pattern(HostStyle& s, const PatternDesc& p, uint32_t pattern_quality, const Mat& final_transform);

@@ -68,6 +68,9 @@ OP_BLIT_SCALED_IMAGE_I = 37
 OP_BLIT_SCALED_IMAGE_D = 38
 OP_FILL_MASK_I = 39
 OP_FILL_MASK_D = 40
+OP_FILL_GEOMETRY = 41
+OP_STROKE_GEOMETRY = 42
+GEOMETRY_CIRCLE, GEOMETRY_ELLIPSE, GEOMETRY_ROUND_RECT, GEOMETRY_TRIANGLE = 5, 6, 7, 12   # BLGeometryType
 
 SRC_OVER, SRC_COPY = 0, 1
 NON_ZERO, EVEN_ODD = 0, 1
@@ -279,6 +282,17 @@ class StreamWriter:
 
     def fill_mask_d(self, x, y, mask, area=None):
         self._mask(OP_FILL_MASK_D, x, y, mask, area)
+
+    # -- shapes (circle, ellipse, round rect, triangle through their paths) -------------------------
+    def fill_geometry(self, gtype: int, values):
+        v = [float(x) for x in values] + [0.0] * (6 - len(values))
+        self._rec(OP_FILL_GEOMETRY, struct.pack("<II6d", gtype, 0, *v))
+        self.fill_count += 1
+
+    def stroke_geometry(self, gtype: int, values):
+        v = [float(x) for x in values] + [0.0] * (6 - len(values))
+        self._rec(OP_STROKE_GEOMETRY, struct.pack("<II6d", gtype, 0, *v))
+        self.fill_count += 1
 
     def save(self):
         self._rec(OP_SAVE)
@@ -863,6 +877,49 @@ def masks(seed: int = 50, width: int = 300, height: int = 220, count: int = 120)
             sw.fill_mask_i(x, y, mask, area)
         else:
             sw.fill_mask_d(float(x) + (0.5 if rng.random() < 0.15 else 0.0), float(y), mask, area)
+    return sw
+
+
+def shapes(seed: int = 60, width: int = 320, height: int = 240, count: int = 200) -> StreamWriter:
+    """Circles (negative radii too), ellipses, round rectangles (radii clamped, degenerate ones as
+    boxes) and triangles, filled with both fill rules and stroked with every join and cap, under
+    identity, scale and rotation transforms."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sw = StreamWriter(width, height)
+    sw.solid(0xFF000000)
+    sw.fill_all()
+    for i in range(count):
+        cx, cy = float(rng.uniform(-20, width + 20)), float(rng.uniform(-20, height + 20))
+        size = float(_log_uniform(rng, 2.0, 120.0))
+        t = int(rng.integers(0, 4))
+        if t == 0:
+            gt, v = GEOMETRY_CIRCLE, [cx, cy, size * (1 if rng.random() < 0.9 else -1)]
+        elif t == 1:
+            gt, v = GEOMETRY_ELLIPSE, [cx, cy, size, float(rng.uniform(1.0, 80.0))]
+        elif t == 2:
+            w, h = size * 2, float(rng.uniform(2.0, 150.0))
+            r = [float(rng.uniform(0.0, 40.0)), float(rng.uniform(-40.0, 40.0))]
+            if rng.random() < 0.1:
+                r = [0.0, 5.0]                                   # degenerate: a box
+            gt, v = GEOMETRY_ROUND_RECT, [cx - w / 2, cy - h / 2, w, h] + r
+        else:
+            gt, v = GEOMETRY_TRIANGLE, list((rng.uniform(-size, size, 6) + np.array([cx, cy] * 3)).astype(float))
+        if rng.random() < 0.25:
+            a = float(rng.uniform(-0.8, 0.8))
+            sn, c = _sincos(a)
+            sw.transform([c, sn, -sn, c * 0.7, 10.0, -5.0])
+        elif rng.random() < 0.3:
+            sw.reset_transform()
+        if rng.random() < 0.5:
+            sw.fill_rule(int(rng.integers(0, 2)))
+            sw.solid(int(rng.integers(0, 2**32, dtype=np.uint64)))
+            sw.fill_geometry(gt, v)
+        else:
+            sw.stroke_width(float(_log_uniform(rng, 0.5, 20.0)))
+            sw.stroke_join(int(rng.integers(0, 5)))
+            sw.stroke_caps(int(rng.integers(0, 6)), int(rng.integers(0, 6)))
+            sw.stroke_solid(int(rng.integers(0, 2**32, dtype=np.uint64)))
+            sw.stroke_geometry(gt, v)
     return sw
 
 

@@ -87,6 +87,9 @@ enum {
   /* masked fills (rastercontext.cpp:3679-3790): the A8 mask travels in the record */
   BLGPU_OP_FILL_MASK_I = 39,       /* BLGpuStreamMask (x, y integral) + u8 mask[w*h] (pad 8)  bl_context_fill_mask_i */
   BLGPU_OP_FILL_MASK_D = 40,       /* BLGpuStreamMask + u8 mask[w*h] (pad 8)       bl_context_fill_mask_d */
+  /* shapes through their paths (BLPath::add_geometry): circle, ellipse, round rect, triangle */
+  BLGPU_OP_FILL_GEOMETRY = 41,     /* u32 BLGeometryType, u32 pad, f64 values[6]   bl_context_fill_geometry */
+  BLGPU_OP_STROKE_GEOMETRY = 42,   /* u32 BLGeometryType, u32 pad, f64 values[6]   bl_context_stroke_geometry */
   BLGPU_OP_COUNT
 };
 

@@ -825,6 +825,73 @@ static void mask_op(OCtx* c, uint32_t op, const uint8_t* p) {
   o_fill_mask_a(&c->fc, x0, y0, x1, y1, bytes + (size_t)src[1] * m.width + (size_t)src[0], (intptr_t)m.width);
 }
 
+/* fill_path_d: u32 n, u32 pad, u8 cmd[n] (padded to 8), f64 xy[2n] */
+static void fill_path_op(OCtx* c, const uint8_t* p) {
+  OState* s = &c->s;
+  int cop; uint32_t alpha;
+  uint32_t n; memcpy(&n, p, 4);
+  if (c->stats) c->stats->input_vertices += n;
+  if (!resolve_fill(c, &cop, &alpha)) return;
+  if (n == 0) return;
+  c->fc.style = &s->style; c->fc.comp_op = cop; c->fc.alpha = alpha;
+  const uint8_t* cmd = p + 8;
+  double* xy = (double*)malloc(sizeof(double) * 2 * n);
+  memcpy(xy, cmd + ((n + 7u) & ~7u), sizeof(double) * 2 * n);
+  o_storage_clear(&c->storage);
+  o_eb_begin(&c->eb);
+  if (o_eb_add_path(&c->eb, cmd, xy, n, &s->final_fixed, s->final_fixed_type) == 0) {
+    o_eb_done(&c->eb);
+    fill_edges(c, (uint32_t)s->fill_rule);
+  }
+  free(xy);
+}
+
+/* --- shapes: BLPath::add_geometry (path.cpp:1408-1600, direction CW) ----------------------------
+ * Returns the vertex count written to cmd/xy (at most 18), 0 for other types. */
+static size_t o_shape_path(uint32_t type, const double* v, uint8_t* cmd, double* xy) {
+  const double kappa = 0.55228474983;
+  size_t n = 0;
+#define PUT(c, x, y) do { cmd[n] = (uint8_t)(c); xy[2 * n] = (x); xy[2 * n + 1] = (y); n++; } while (0)
+#define CUBIC(a, b, c, d, e, f) do { PUT(4, a, b); PUT(4, c, d); PUT(1, e, f); } while (0)
+  if (type == 5 || type == 6) {
+    double x0 = v[0], y0 = v[1], rx = v[2];
+    double ry = type == 5 ? fabs(rx) : v[3];
+    double kx = rx * kappa, ky = ry * kappa;
+    PUT(0, x0 + rx, y0);
+    CUBIC(x0 + rx, y0 + ky, x0 + kx, y0 + ry, x0, y0 + ry);
+    CUBIC(x0 - kx, y0 + ry, x0 - rx, y0 + ky, x0 - rx, y0);
+    CUBIC(x0 - rx, y0 - ky, x0 - kx, y0 - ry, x0, y0 - ry);
+    CUBIC(x0 + kx, y0 - ry, x0 + rx, y0 - ky, x0 + rx, y0);
+    PUT(5, NAN, NAN);
+  }
+  else if (type == 7) {
+    double x0 = v[0], y0 = v[1], x1 = v[0] + v[2], y1 = v[1] + v[3];
+    double rx = o_min(fabs(v[4]), v[2] * 0.5), ry = o_min(fabs(v[5]), v[3] * 0.5);
+    if (!(rx > 1e-14 && ry > 1e-14)) {
+      PUT(0, x0, y0); PUT(1, x1, y0); PUT(1, x1, y1); PUT(1, x0, y1); PUT(5, NAN, NAN);
+    }
+    else {
+      double kx = rx * (1.0 - kappa), ky = ry * (1.0 - kappa);
+      PUT(0, x0 + rx, y0);
+      PUT(1, x1 - rx, y0);
+      CUBIC(x1 - kx, y0, x1, y0 + ky, x1, y0 + ry);
+      PUT(1, x1, y1 - ry);
+      CUBIC(x1, y1 - ky, x1 - kx, y1, x1 - rx, y1);
+      PUT(1, x0 + rx, y1);
+      CUBIC(x0 + kx, y1, x0, y1 - ky, x0, y1 - ry);
+      PUT(1, x0, y0 + ry);
+      CUBIC(x0, y0 + ky, x0 + kx, y0, x0 + rx, y0);
+      PUT(5, NAN, NAN);
+    }
+  }
+  else if (type == 12) {
+    PUT(0, v[0], v[1]); PUT(1, v[2], v[3]); PUT(1, v[4], v[5]); PUT(5, NAN, NAN);
+  }
+#undef CUBIC
+#undef PUT
+  return n;
+}
+
 static int replay(OCtx* c, const uint8_t* base, size_t size, size_t off) {
   while (off + 8 <= size) {
     uint32_t op, len;
@@ -912,6 +979,23 @@ static int replay(OCtx* c, const uint8_t* base, size_t size, size_t off) {
       case BLGPU_OP_FILL_MASK_I: case BLGPU_OP_FILL_MASK_D:
         mask_op(c, op, p);
         break;
+      case BLGPU_OP_FILL_GEOMETRY: case BLGPU_OP_STROKE_GEOMETRY: {
+        uint32_t type; memcpy(&type, p, 4);
+        double v[6]; memcpy(v, p + 8, sizeof(v));
+        uint8_t sc[24]; double sxy[48];
+        size_t sn = o_shape_path(type, v, sc, sxy);
+        if (!sn) break;
+        /* the same record layout as FILL_PATH_D / STROKE_PATH_D */
+        uint8_t rec[8 + 24 + 48 * 8];
+        uint32_t n32 = (uint32_t)sn;
+        memset(rec, 0, sizeof(rec));
+        memcpy(rec, &n32, 4);
+        memcpy(rec + 8, sc, sn);
+        memcpy(rec + 8 + ((sn + 7u) & ~7u), sxy, sizeof(double) * 2 * sn);
+        if (op == BLGPU_OP_FILL_GEOMETRY) fill_path_op(c, rec);
+        else stroke_op(c, BLGPU_OP_STROKE_PATH_D, rec);
+        break;
+      }
 
       case BLGPU_OP_CLEAR_ALL: {
         OStyle clear_style;
@@ -973,24 +1057,9 @@ static int replay(OCtx* c, const uint8_t* base, size_t size, size_t off) {
         free(xy);
         break;
       }
-      case BLGPU_OP_FILL_PATH_D: {
-        uint32_t n; memcpy(&n, p, 4);
-        if (c->stats) c->stats->input_vertices += n;
-        if (!resolve_fill(c, &cop, &alpha)) break;
-        if (n == 0) break;
-        c->fc.style = &s->style; c->fc.comp_op = cop; c->fc.alpha = alpha;
-        const uint8_t* cmd = p + 8;
-        double* xy = (double*)malloc(sizeof(double) * 2 * n);
-        memcpy(xy, cmd + ((n + 7u) & ~7u), sizeof(double) * 2 * n);
-        o_storage_clear(&c->storage);
-        o_eb_begin(&c->eb);
-        if (o_eb_add_path(&c->eb, cmd, xy, n, &s->final_fixed, s->final_fixed_type) == 0) {
-          o_eb_done(&c->eb);
-          fill_edges(c, (uint32_t)s->fill_rule);
-        }
-        free(xy);
+      case BLGPU_OP_FILL_PATH_D:
+        fill_path_op(c, p);
         break;
-      }
       case BLGPU_OP_SAVE:
         if (c->nstack == c->cap_stack) {
           c->cap_stack = c->cap_stack ? c->cap_stack * 2 : 8;

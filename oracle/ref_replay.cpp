@@ -241,6 +241,20 @@ static void replay(const Stream& s, BLImage& img, uint32_t threads) {
         }
         break;
       }
+      case BLGPU_OP_FILL_GEOMETRY: case BLGPU_OP_STROKE_GEOMETRY: {
+        uint32_t type = rd<uint32_t>(p);
+        double v[6];
+        memcpy(v, p + 8, sizeof(v));
+        BLCircle ci(v[0], v[1], v[2]);
+        BLEllipse el(v[0], v[1], v[2], v[3]);
+        BLRoundRect rr(v[0], v[1], v[2], v[3], v[4], v[5]);
+        BLTriangle tr(v[0], v[1], v[2], v[3], v[4], v[5]);
+        const void* data = type == BL_GEOMETRY_TYPE_CIRCLE ? (const void*)&ci : type == BL_GEOMETRY_TYPE_ELLIPSE ? (const void*)&el
+                         : type == BL_GEOMETRY_TYPE_ROUND_RECT ? (const void*)&rr : (const void*)&tr;
+        if (op == BLGPU_OP_FILL_GEOMETRY) bl_context_fill_geometry(&ctx, BLGeometryType(type), data);
+        else bl_context_stroke_geometry(&ctx, BLGeometryType(type), data);
+        break;
+      }
       case BLGPU_OP_SAVE: ctx.save(); break;
       case BLGPU_OP_RESTORE: ctx.restore(); break;
       default:

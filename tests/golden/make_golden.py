@@ -6,7 +6,7 @@ reference with oracle/ref.mk (no CMake) into oracle/_ref/ and records:
   * scenes  - sha256 of the PRGB32 pixels the reference renders for seeded command streams
               (blend2d_gb300.scenes; the mix_dither / curves_dither scenes use gradient quality
               DITHER, whose 64-bit LUT has a single builder; strokes_* / stroked_paths_* stroke
-              paths, polylines, polygons, boxes, rects and lines; blits_* image blits; masks_* masked fills), for the stock no-JIT x86-64 build ("default", SSE2 LUT
+              paths, polylines, polygons, boxes, rects and lines; blits_* image blits; masks_* masked fills; shapes_* circles, ellipses, round rects and triangles), for the stock no-JIT x86-64 build ("default", SSE2 LUT
               builder) and, for a subset, the portable-LUT build ("scalar");
   * luts    - sha256 of the gradient LUTs produced by the reference's three builders
               (interpolate_prgb32 / _sse2 / _avx2) for random stop arrays;
@@ -70,6 +70,8 @@ def scene_catalog(full: bool):
     cat.append(("blits_tall", "scenes.blits(seed=44, width=97, height=301)", ("default",)))
     for s in range(3):
         cat.append((f"masks_{s}", f"scenes.masks(seed={50 + s}, count=150)", ("default",)))
+    for s in range(3):
+        cat.append((f"shapes_{s}", f"scenes.shapes(seed={60 + s}, count=200)", ("default",)))
     for i in range(6):
         cat.append((f"batch_{i}", f"scenes.batch_canvases(seed=4, count=6, max_side=640, max_paths=400)[{i}]", ("default",)))
     if full:

@@ -560,3 +560,38 @@ def test_fill_mask_context_calls(runtimes):
     stream = sw.to_bytes()
     assert not _diff(out, bg.render_stream(runtimes(), stream))
     assert not _diff(out, oracle_lib.render(stream))
+
+
+# --- shapes ------------------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("seed", range(1500, 1504))
+def test_shapes_vs_oracle(runtimes, seed):
+    """Circles, ellipses, round rects and triangles, filled (both rules) and stroked."""
+    sw = scenes.shapes(seed=seed, count=150, width=(320, 61, 500)[seed % 3], height=(240, 203, 90)[seed % 3])
+    stream = sw.to_bytes()
+    got = bg.render_stream(runtimes(), stream)
+    want = oracle_lib.render(stream)
+    assert not _diff(got, want), _diff(got, want)
+
+
+def test_shape_context_calls_match_stream(runtimes):
+    w, h = 140, 100
+    sw = scenes.StreamWriter(w, h)
+    out = np.zeros((h, w), dtype=np.uint32)
+    ctx = bg.Context(runtimes(), out)
+    sw.solid(0xFF000000); sw.fill_all()
+    ctx.set_fill_style_rgba32(0xFF000000); ctx.fill_all()
+    sw.solid(0xFFFF8040); ctx.set_fill_style_rgba32(0xFFFF8040)
+    for gt, v in [(scenes.GEOMETRY_CIRCLE, [40, 40, 25]), (scenes.GEOMETRY_ELLIPSE, [100, 30, 30, 12]),
+                  (scenes.GEOMETRY_ROUND_RECT, [60, 55, 70, 40, 12, 8]), (scenes.GEOMETRY_TRIANGLE, [5, 95, 40, 60, 70, 98])]:
+        sw.fill_geometry(gt, v); ctx.fill_geometry(gt, v)
+    sw.stroke_solid(0xFF20FFA0); ctx.set_stroke_style_rgba32(0xFF20FFA0)
+    sw.stroke_width(3.0); ctx.set_stroke_width(3.0)
+    sw.stroke_geometry(scenes.GEOMETRY_CIRCLE, [40, 40, 30]); ctx.stroke_geometry(scenes.GEOMETRY_CIRCLE, [40, 40, 30])
+    with pytest.raises(bg.BLGpuError) as e:
+        ctx.fill_geometry(8, [10, 10, 5, 5, 0, 1])               # BL_GEOMETRY_TYPE_ARC
+    assert e.value.code == bg.ERROR_NOT_IMPLEMENTED
+    ctx.end()
+    stream = sw.to_bytes()
+    assert not _diff(out, bg.render_stream(runtimes(), stream))
+    assert not _diff(out, oracle_lib.render(stream))
