@@ -373,6 +373,56 @@ bool shape_path(uint32_t type, const double* v, std::vector<uint8_t>& cmd, std::
     case kGeometryTriangle:
       put(0, v[0], v[1]); put(1, v[2], v[3]); put(1, v[4], v[5]); put(5, NAN, NAN);
       return true;
+    case kGeometryArc: case kGeometryChord: case kGeometryPie: {
+      // {cx, cy, rx, ry, start, sweep}: arc_to_cubic_spline (path.cpp:503-570), quarter arcs as
+      // cubics and the rest as a conic turned into a cubic (PathAppender::conic_to, path_p.h:319)
+      const double cx = v[0], cy = v[1], rx = v[2], ry = v[3];
+      double sweep = v[5];
+      if (type == kGeometryPie) put(0, cx, cy);
+      double ss = sin(v[4]), sc = cos(v[4]);
+      // make_sin_cos, post_scale(r), post_translate(c)
+      double m00 = sc * rx, m01 = ss * ry, m10 = -ss * rx, m11 = sc * ry, m20 = 0.0 * rx + cx, m21 = 0.0 * ry + cy;
+      if (sweep < 0) { m10 *= -1.0; m11 *= -1.0; sweep = -sweep; }      // scale(1, -1)
+      auto map = [&](double x, double y, double& ox, double& oy) { ox = x * m00 + y * m10 + m20; oy = x * m01 + y * m11 + m21; };
+      double v1x = 1.0, v1y = 0.0, vcx = 1.0, vcy = 1.0, v2x, v2y;
+      constexpr double kPi2 = 6.28318530717958647692;
+      if (sweep >= kPi2 - 1e-14) { sweep = kPi2; v2x = v1x; v2y = v1y; }
+      else {
+        if (std::isnan(sweep)) { if (type != kGeometryArc) put(5, NAN, NAN); return true; }
+        v2x = cos(sweep); v2y = sin(sweep);
+      }
+      double p0x, p0y;
+      map(v1x, v1y, p0x, p0y);
+      put(type == kGeometryPie ? 1 : 0, p0x, p0y);
+      static const double steps[4] = {1.57079632679489661923, 3.14159265358979323846, 4.71238898038468985769,
+                                      6.28318530717958647692};
+      size_t i = 0;
+      bool full = false;
+      while (sweep > steps[i]) {
+        double t = v1x; v1x = -v1y; v1y = t;                                 // Geometry::normal
+        double p1x, p1y, p2x, p2y;
+        map(vcx, vcy, p1x, p1y);
+        map(v1x, v1y, p2x, p2y);
+        cubic(p0x + (p1x - p0x) * kKappa, p0y + (p1y - p0y) * kKappa, p2x + (p1x - p2x) * kKappa,
+              p2y + (p1y - p2y) * kKappa, p2x, p2y);
+        if (++i == 4) { full = true; break; }
+        t = vcx; vcx = -vcy; vcy = t;
+        p0x = p2x; p0y = p2y;
+      }
+      if (!full) {
+        double sx = v1x + v2x, sy = v1y + v2y;
+        double dd = sx * sx + sy * sy;
+        vcx = 2.0 * sx / dd; vcy = 2.0 * sy / dd;
+        double w = sqrt(0.5 * (v1x * v2x + v1y * v2y) + 0.5);
+        double k = 4.0 * w / (3.0 * (1.0 + w));
+        double p1x, p1y, p2x, p2y;
+        map(vcx, vcy, p1x, p1y);
+        map(v2x, v2y, p2x, p2y);
+        cubic(p0x + (p1x - p0x) * k, p0y + (p1y - p0y) * k, p2x + (p1x - p2x) * k, p2y + (p1y - p2y) * k, p2x, p2y);
+      }
+      if (type != kGeometryArc) put(5, NAN, NAN);
+      return true;
+    }
     default:
       return false;
   }

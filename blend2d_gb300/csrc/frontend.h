@@ -54,9 +54,11 @@ struct PatternDesc {
 };
 
 // BLGeometryType values of the shapes shape_path builds.
-constexpr uint32_t kGeometryCircle = 5, kGeometryEllipse = 6, kGeometryRoundRect = 7, kGeometryTriangle = 12;
+constexpr uint32_t kGeometryCircle = 5, kGeometryEllipse = 6, kGeometryRoundRect = 7, kGeometryArc = 8,
+                   kGeometryChord = 9, kGeometryPie = 10, kGeometryTriangle = 12;
 // The path BLPath::add_geometry makes of a circle {cx, cy, r}, ellipse {cx, cy, rx, ry}, round
-// rectangle {x, y, w, h, rx, ry} or triangle {x0, y0, x1, y1, x2, y2}; false for other types.
+// rectangle {x, y, w, h, rx, ry}, triangle {x0, y0, x1, y1, x2, y2} or arc / chord / pie
+// {cx, cy, rx, ry, start, sweep}; false for other types.
 bool shape_path(uint32_t type, const double* v, std::vector<uint8_t>& cmd, std::vector<double>& xy);
 
 void style_solid(HostStyle& s, uint32_t argb32);

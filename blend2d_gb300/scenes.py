@@ -71,6 +71,7 @@ OP_FILL_MASK_D = 40
 OP_FILL_GEOMETRY = 41
 OP_STROKE_GEOMETRY = 42
 GEOMETRY_CIRCLE, GEOMETRY_ELLIPSE, GEOMETRY_ROUND_RECT, GEOMETRY_TRIANGLE = 5, 6, 7, 12   # BLGeometryType
+GEOMETRY_ARC, GEOMETRY_CHORD, GEOMETRY_PIE = 8, 9, 10
 
 SRC_OVER, SRC_COPY = 0, 1
 NON_ZERO, EVEN_ODD = 0, 1
@@ -882,8 +883,9 @@ def masks(seed: int = 50, width: int = 300, height: int = 220, count: int = 120)
 
 def shapes(seed: int = 60, width: int = 320, height: int = 240, count: int = 200) -> StreamWriter:
     """Circles (negative radii too), ellipses, round rectangles (radii clamped, degenerate ones as
-    boxes) and triangles, filled with both fill rules and stroked with every join and cap, under
-    identity, scale and rotation transforms."""
+    boxes), triangles and arcs / chords / pies (sweeps of either sign, full turns), filled with
+    both fill rules and stroked with every join and cap, under identity, scale and rotation
+    transforms."""
     rng = np.random.Generator(np.random.PCG64(seed))
     sw = StreamWriter(width, height)
     sw.solid(0xFF000000)
@@ -891,8 +893,12 @@ def shapes(seed: int = 60, width: int = 320, height: int = 240, count: int = 200
     for i in range(count):
         cx, cy = float(rng.uniform(-20, width + 20)), float(rng.uniform(-20, height + 20))
         size = float(_log_uniform(rng, 2.0, 120.0))
-        t = int(rng.integers(0, 4))
-        if t == 0:
+        t = int(rng.integers(0, 5))
+        if t == 4:
+            sweep = float(rng.uniform(-7.0, 7.0))
+            gt = (GEOMETRY_ARC, GEOMETRY_CHORD, GEOMETRY_PIE)[int(rng.integers(0, 3))]
+            v = [cx, cy, size, float(rng.uniform(2.0, 90.0)), float(rng.uniform(-4.0, 4.0)), sweep]
+        elif t == 0:
             gt, v = GEOMETRY_CIRCLE, [cx, cy, size * (1 if rng.random() < 0.9 else -1)]
         elif t == 1:
             gt, v = GEOMETRY_ELLIPSE, [cx, cy, size, float(rng.uniform(1.0, 80.0))]

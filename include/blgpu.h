@@ -219,8 +219,9 @@ BLGpuResult blgpu_context_fill_mask_d(BLGpuContext* ctx, double x, double y, con
 /* Shapes (fill_geometry / stroke_geometry, rastercontext.cpp:2926-2980 and :3208-3234): the path
  * BLPath::add_geometry builds (path.cpp:1408-1600) filled with the fill rule or stroked. `type` is a
  * BLGeometryType: BL_GEOMETRY_TYPE_CIRCLE (5) {cx, cy, r}, ELLIPSE (6) {cx, cy, rx, ry}, ROUND_RECT
- * (7) {x, y, w, h, rx, ry}, TRIANGLE (12) {x0, y0, x1, y1, x2, y2}; boxes, rects, lines, polylines,
- * polygons and paths have their own entry points; other types return BLGPU_ERROR_NOT_IMPLEMENTED. */
+ * (7) {x, y, w, h, rx, ry}, ARC (8) / CHORD (9) / PIE (10) {cx, cy, rx, ry, start, sweep}, TRIANGLE
+ * (12) {x0, y0, x1, y1, x2, y2}; boxes, rects, lines, polylines, polygons and paths have their own
+ * entry points; other types return BLGPU_ERROR_NOT_IMPLEMENTED. */
 BLGpuResult blgpu_context_fill_geometry(BLGpuContext* ctx, uint32_t type, const double* values);   /* bl_context_fill_geometry */
 BLGpuResult blgpu_context_stroke_geometry(BLGpuContext* ctx, uint32_t type, const double* values); /* bl_context_stroke_geometry */
 

@@ -887,6 +887,48 @@ static size_t o_shape_path(uint32_t type, const double* v, uint8_t* cmd, double*
   else if (type == 12) {
     PUT(0, v[0], v[1]); PUT(1, v[2], v[3]); PUT(1, v[4], v[5]); PUT(5, NAN, NAN);
   }
+  else if (type == 8 || type == 9 || type == 10) {
+    /* arc_to_cubic_spline (path.cpp:496-570) with PathAppender::conic_to's cubic (path_p.h:319-334) */
+    static const double steps[4] = { 1.57079632679489661923, 3.14159265358979323846, 4.71238898038468985769,
+                                     6.28318530717958647692 };
+    double cx = v[0], cy = v[1], rx = v[2], ry = v[3], sweep = v[5];
+    if (type == 10) PUT(0, cx, cy);
+    double ss = sin(v[4]), sc = cos(v[4]);
+    OMat t = { sc, ss, -ss, sc, 0.0, 0.0 };                  /* make_sin_cos */
+    t.m00 *= rx; t.m01 *= ry; t.m10 *= rx; t.m11 *= ry; t.m20 *= rx; t.m21 *= ry;   /* post_scale */
+    t.m20 += cx; t.m21 += cy;                               /* post_translate */
+    if (sweep < 0) { t.m00 *= 1.0; t.m01 *= 1.0; t.m10 *= -1.0; t.m11 *= -1.0; sweep = -sweep; }
+    OPt v1 = { 1.0, 0.0 }, vc = { 1.0, 1.0 }, v2;
+    int ok = 1;
+    if (sweep >= 6.28318530717958647692 - 1e-14) { sweep = 6.28318530717958647692; v2 = v1; }
+    else if (isnan(sweep)) ok = 0;
+    else { v2.x = cos(sweep); v2.y = sin(sweep); }
+    if (ok) {
+      OPt p0 = o_mat_map(&t, v1.x, v1.y);
+      PUT(type == 10 ? 1 : 0, p0.x, p0.y);
+      int i = 0, full = 0;
+      while (sweep > steps[i]) {
+        double tmp = v1.x; v1.x = -v1.y; v1.y = tmp;
+        OPt p1 = o_mat_map(&t, vc.x, vc.y), p2 = o_mat_map(&t, v1.x, v1.y);
+        CUBIC(p0.x + (p1.x - p0.x) * kappa, p0.y + (p1.y - p0.y) * kappa,
+              p2.x + (p1.x - p2.x) * kappa, p2.y + (p1.y - p2.y) * kappa, p2.x, p2.y);
+        if (++i == 4) { full = 1; break; }
+        tmp = vc.x; vc.x = -vc.y; vc.y = tmp;
+        p0 = p2;
+      }
+      if (!full) {
+        OPt s2 = { v1.x + v2.x, v1.y + v2.y };
+        double dd = s2.x * s2.x + s2.y * s2.y;
+        vc.x = 2.0 * s2.x / dd; vc.y = 2.0 * s2.y / dd;
+        double w = sqrt(0.5 * (v1.x * v2.x + v1.y * v2.y) + 0.5);
+        double k = 4.0 * w / (3.0 * (1.0 + w));
+        OPt p1 = o_mat_map(&t, vc.x, vc.y), p2 = o_mat_map(&t, v2.x, v2.y);
+        CUBIC(p0.x + (p1.x - p0.x) * k, p0.y + (p1.y - p0.y) * k, p2.x + (p1.x - p2.x) * k, p2.y + (p1.y - p2.y) * k,
+              p2.x, p2.y);
+      }
+    }
+    if (type != 8) PUT(5, NAN, NAN);
+  }
 #undef CUBIC
 #undef PUT
   return n;

@@ -249,8 +249,10 @@ static void replay(const Stream& s, BLImage& img, uint32_t threads) {
         BLEllipse el(v[0], v[1], v[2], v[3]);
         BLRoundRect rr(v[0], v[1], v[2], v[3], v[4], v[5]);
         BLTriangle tr(v[0], v[1], v[2], v[3], v[4], v[5]);
+        BLArc ar(v[0], v[1], v[2], v[3], v[4], v[5]);
         const void* data = type == BL_GEOMETRY_TYPE_CIRCLE ? (const void*)&ci : type == BL_GEOMETRY_TYPE_ELLIPSE ? (const void*)&el
-                         : type == BL_GEOMETRY_TYPE_ROUND_RECT ? (const void*)&rr : (const void*)&tr;
+                         : type == BL_GEOMETRY_TYPE_ROUND_RECT ? (const void*)&rr : type == BL_GEOMETRY_TYPE_TRIANGLE ? (const void*)&tr
+                         : (const void*)&ar;
         if (op == BLGPU_OP_FILL_GEOMETRY) bl_context_fill_geometry(&ctx, BLGeometryType(type), data);
         else bl_context_stroke_geometry(&ctx, BLGeometryType(type), data);
         break;

@@ -588,8 +588,10 @@ def test_shape_context_calls_match_stream(runtimes):
     sw.stroke_solid(0xFF20FFA0); ctx.set_stroke_style_rgba32(0xFF20FFA0)
     sw.stroke_width(3.0); ctx.set_stroke_width(3.0)
     sw.stroke_geometry(scenes.GEOMETRY_CIRCLE, [40, 40, 30]); ctx.stroke_geometry(scenes.GEOMETRY_CIRCLE, [40, 40, 30])
+    sw.fill_geometry(scenes.GEOMETRY_PIE, [100, 70, 25, 20, 0.5, 4.0]); ctx.fill_geometry(scenes.GEOMETRY_PIE, [100, 70, 25, 20, 0.5, 4.0])
+    sw.stroke_geometry(scenes.GEOMETRY_ARC, [70, 50, 40, 30, -1.0, -2.5]); ctx.stroke_geometry(scenes.GEOMETRY_ARC, [70, 50, 40, 30, -1.0, -2.5])
     with pytest.raises(bg.BLGpuError) as e:
-        ctx.fill_geometry(8, [10, 10, 5, 5, 0, 1])               # BL_GEOMETRY_TYPE_ARC
+        ctx.fill_geometry(21, [0, 0, 0, 0, 0, 0])               # BL_GEOMETRY_TYPE_PATH: its own entry point
     assert e.value.code == bg.ERROR_NOT_IMPLEMENTED
     ctx.end()
     stream = sw.to_bytes()
