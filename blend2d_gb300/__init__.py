@@ -10,6 +10,7 @@ import ctypes
 import os
 import struct
 import threading
+import weakref
 
 import numpy as np
 
@@ -228,9 +229,14 @@ class Runtime:
         h = _P()
         _check(self._lib.blgpu_runtime_create(ctypes.byref(h), ctypes.byref(info)), "blgpu_runtime_create")
         self.handle = h
+        self._contexts = weakref.WeakSet()
 
     def close(self):
+        """Destroys the runtime, after every context still open on it: a context must not outlive
+        its runtime (its destruction waits on the runtime's frames)."""
         if self.handle:
+            for ctx in list(self._contexts):
+                ctx.close()
             self._lib.blgpu_runtime_destroy(self.handle)
             self.handle = None
 
@@ -300,6 +306,7 @@ class Context:
         h = _P()
         _check(self._lib.blgpu_context_create(ctypes.byref(h), runtime.handle), "blgpu_context_create")
         self.handle = h
+        runtime._contexts.add(self)
         self._keep = []
         self._inflight = []
         if target is not None:

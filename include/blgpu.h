@@ -132,6 +132,8 @@ typedef struct BLGpuLaunchConfig {
 
 /* --- runtime (device, stream, memory) --------------------------------------------------- */
 BLGpuResult blgpu_runtime_create(BLGpuRuntime** out, const BLGpuRuntimeCreateInfo* info);
+/* Destroy every context created on the runtime first: a context's destruction waits on the
+ * runtime's in-flight frames. */
 BLGpuResult blgpu_runtime_destroy(BLGpuRuntime* rt);
 BLGpuResult blgpu_runtime_get_stats(const BLGpuRuntime* rt, BLGpuStats* out);
 /* Re-runs the device pipeline of the last flushed frame on its device-resident inputs (no

@@ -94,3 +94,33 @@ def test_errors_reach_every_request_of_the_batch():
         for f in rest:
             with pytest.raises(RuntimeError):
                 f.result(timeout=5)
+
+
+def test_runtime_close_closes_its_contexts_first():
+    """A context kept alive past its runtime (a reference cycle, an exception traceback) must not be
+    destroyed after the runtime: Runtime.close() closes the contexts still open on it."""
+    import blend2d_gb300 as bg
+
+    class FakeLib:
+        def __init__(self):
+            self.calls = []
+
+        def blgpu_context_destroy(self, h):
+            self.calls.append(("ctx", h))
+
+        def blgpu_runtime_destroy(self, h):
+            self.calls.append(("rt", h))
+
+    rt = bg.Runtime.__new__(bg.Runtime)
+    rt._lib = FakeLib()
+    rt.handle = 1
+    import weakref
+    rt._contexts = weakref.WeakSet()
+    ctx = bg.Context.__new__(bg.Context)
+    ctx._lib = rt._lib
+    ctx.handle = 2
+    ctx.rt = rt
+    rt._contexts.add(ctx)
+    rt.close()
+    assert rt._lib.calls == [("ctx", 2), ("rt", 1)]
+    assert ctx.handle is None and rt.handle is None
