@@ -6,6 +6,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <cmath>
+
 #include <algorithm>
 
 namespace blgpu {
