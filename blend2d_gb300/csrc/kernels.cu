@@ -1132,7 +1132,10 @@ __global__ void __launch_bounds__(kFineThreads) cull_kernel(FrameView f) {
   }
 }
 
-__global__ void __launch_bounds__(kFineThreads, 4) fine_kernel(FrameView f) {
+// 5 resident blocks per SM (48 registers, a few spilled): the composite waits on dependent loads,
+// and the extra warps hide more of them than the spills cost (curves frame 2.98 -> 2.95 ms; 6
+// blocks, 40 registers, measured the same as 5).
+__global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
   const int lane = threadIdx.x & 31;
   const int prow = lane >> 3;            // row within the strip
   const int pcol = (lane & 7) * 4;       // first of this lane's 4 columns
