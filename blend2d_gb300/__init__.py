@@ -83,7 +83,7 @@ class LaunchConfig(ctypes.Structure):
     _fields_ = [("cover_slots", ctypes.c_int32), ("cover_blocks_per_sm", ctypes.c_int32),
                 ("fine_blocks_per_sm", ctypes.c_int32), ("edge_block", ctypes.c_int32),
                 ("cubic_blocks_per_sm", ctypes.c_int32), ("no_occlusion_cull", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 2)]
+                ("max_segments", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -270,6 +270,13 @@ class Runtime:
 
     def set_launch_config(self, config: LaunchConfig):
         _check(self._lib.blgpu_runtime_set_launch_config(self.handle, ctypes.byref(config)), "set_launch_config")
+
+    def set_segment_limit(self, max_segments: int):
+        """Caps the segment array at `max_segments` (0: grow as needed); a frame that emits more
+        fails with ERROR_DATA_TOO_LARGE."""
+        c = self.launch_config()
+        c.max_segments = int(max_segments)
+        self.set_launch_config(c)
 
     def autotune(self, trials: int = 3) -> tuple[LaunchConfig, float]:
         """Tunes the launch shapes on the last flushed frame; returns (best config, its ms)."""

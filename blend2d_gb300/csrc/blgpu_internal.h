@@ -39,6 +39,18 @@ enum FillKind : uint32_t {
 
 enum GeomKind : uint32_t { kGeomPolygon = 0, kGeomPath = 1 };
 
+// Bits of FrameView::error_flags[0]: a work array of the frame was too small for what the device
+// produced (the frame's pixels are then not valid and the host reports an error). The host sizes
+// every array from a bound, so none of them is expected; a replay whose data changed could meet
+// one.
+enum ErrorFlag : uint32_t {
+  kErrItems = 1u,        // lines / curves of the analytic commands (bound: one per vertex)
+  kErrPieces = 2u,       // monotonic curve pieces (bound: 3 per curve vertex)
+  kErrSeglist = 4u,      // coverage work items (sized by the binning count pass)
+  kErrMasks = 8u,        // slot masks (sized by the binning count pass)
+  kErrSegments = 16u     // segments (the segment array is grown and the frame re-run)
+};
+
 enum FetchKind : uint32_t {
   kFetchSolid = 0,
   kFetchLinearPad, kFetchLinearRoR,

@@ -1236,6 +1236,7 @@ static void to_abi(const LaunchConfig& c, BLGpuLaunchConfig* out) {
   out->edge_block = c.edge_block;
   out->cubic_blocks_per_sm = c.cubic_blocks_per_sm;
   out->no_occlusion_cull = c.no_occlusion_cull;
+  out->max_segments = c.max_segments;
 }
 
 BLGPU_API BLGpuResult blgpu_runtime_get_launch_config(const BLGpuRuntime* rt, BLGpuLaunchConfig* out) {
@@ -1250,7 +1251,7 @@ BLGPU_API BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BL
   if ((c->cover_slots != 0 && c->cover_slots != 16 && c->cover_slots != 32 && c->cover_slots != 64) ||
       (c->edge_block != 64 && c->edge_block != 128 && c->edge_block != 256) ||
       c->cover_blocks_per_sm < 0 || c->fine_blocks_per_sm < 0 || c->cubic_blocks_per_sm < 0 ||
-      (c->no_occlusion_cull != 0 && c->no_occlusion_cull != 1))
+      (c->no_occlusion_cull != 0 && c->no_occlusion_cull != 1) || c->max_segments < 0)
     return BLGPU_ERROR_INVALID_VALUE;
   LaunchConfig lc;
   lc.cover_slots = c->cover_slots;
@@ -1259,6 +1260,7 @@ BLGPU_API BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BL
   lc.edge_block = c->edge_block;
   lc.cubic_blocks_per_sm = c->cubic_blocks_per_sm;
   lc.no_occlusion_cull = c->no_occlusion_cull;
+  lc.max_segments = c->max_segments;
   std::lock_guard<std::mutex> e(rt->exec);
   rt->rt.cfg = lc;
   rt->rt.graph_valid = false;

@@ -399,6 +399,7 @@ __global__ void classify_kernel(FrameView f) {
     if (!finite) {
       uint32_t base = atomicAdd(f.work_counter + 1, 1u);
       if (base < f.item_capacity) f.items[base] = DevItem{c, kItemWhole, 0u, 0u};
+      else atomicOr(f.error_flags, kErrItems);
       return;
     }
   }
@@ -413,6 +414,10 @@ __global__ void classify_kernel(FrameView f) {
   uint32_t base = lines ? atomicAdd(f.work_counter + 1, lines) : 0u;
   uint32_t cbase = cubics ? atomicAdd(f.work_counter + 2, cubics) : 0u;
   uint32_t qbase = quads ? atomicAdd(f.work_counter + 21, quads) : 0u;
+  // cubics fill the curve list from the front and quadratics from the back: together, and each
+  // list on its own, they must fit (the bound is one item per vertex)
+  if (base + lines > f.item_capacity || cbase + cubics > f.item_capacity || qbase + quads > f.item_capacity)
+    atomicOr(f.error_flags, kErrItems);
   for_each_item(pc, n, [&](uint32_t kind, int a, int b) {
     const DevItem it{c, kind, uint32_t(a), uint32_t(b)};
     if (kind == kItemLine) {
@@ -517,7 +522,7 @@ __global__ void __launch_bounds__(128) curve_split_kernel(FrameView f) {
   base = __shfl_sync(0xFFFFFFFFu, base, 31) + incl - npieces;
   for (uint32_t k = 0; k < npieces; k++) {
     const uint32_t idx = base + k;
-    if (idx >= f.piece_capacity) break;
+    if (idx >= f.piece_capacity) { atomicOr(f.error_flags, kErrPieces); break; }
     DevPiece pc;
 #pragma unroll
     for (int i = 0; i <= DEG; i++) pc.p[i] = make_double2(spline[k * DEG + i].x, spline[k * DEG + i].y);
@@ -764,6 +769,8 @@ __global__ void cmd_tiles_kernel(FrameView f, uint32_t* cmdrow_counts_per_cmd, u
 // slots with segments are contiguous.
 __global__ void __launch_bounds__(256) seg_bin_kernel(FrameView f, int scatter) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  // the segments the edge builders emitted must all have found a place in the segment array
+  if (s == 0 && !scatter && f.totals[0] > f.seg_capacity) atomicOr(f.error_flags, kErrSegments);
   if (s >= f.num_segs) return;
   const uint32_t c = f.seg_meta[s] >> 1;
   const uint32_t ctx = f.cmd_tile_x[c];
@@ -789,7 +796,7 @@ __global__ void __launch_bounds__(256) seg_bin_kernel(FrameView f, int scatter) 
       }
       else {
         const uint32_t pos = f.slot_first[slot] + atomicSub(&f.cmdrow_counts[slot], 1u) - 1u;
-        if (pos >= f.num_seglist) { atomicOr(&f.error_flags[0], 4u); continue; }
+        if (pos >= f.num_seglist) { atomicOr(f.error_flags, kErrSeglist); continue; }
         f.entries[pos] = make_uint2(s, f.slot_mask[slot] - 1u);
       }
     }
@@ -917,6 +924,7 @@ __global__ void __launch_bounds__(4 * K) coverage_kernel(FrameView f) {
   __shared__ uint32_t kcount[5], kbase[5];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t num_masks = min(f.totals[5], f.mask_capacity);
+  if (blockIdx.x == 0 && tid == 0 && f.totals[5] > f.mask_capacity) atomicOr(f.error_flags, kErrMasks);
   const uint32_t groups = (num_masks + K - 1) / K;
 
   for (uint32_t grp = blockIdx.x; grp < groups; grp += gridDim.x) {

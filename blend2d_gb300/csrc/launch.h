@@ -17,6 +17,7 @@ struct LaunchConfig {
   int edge_block = 128;           // threads per block of the per-item edge builder (64/128/256)
   int cubic_blocks_per_sm = 3;    // lane-scheduled curve-piece flattener: blocks per SM (0 = as many as fit)
   int no_occlusion_cull = 0;      // 1: the composite starts every strip at its first command
+  int max_segments = 0;           // > 0: cap of the segment array (frames needing more fail)
 };
 
 int exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* tmp, cudaStream_t st);

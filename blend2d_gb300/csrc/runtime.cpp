@@ -425,7 +425,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   // Segment array: kept across frames, sized from the vertex count at first and from the actual
   // count whenever a frame overflows it (run() then repeats the counting half).
   size_t want_segs = std::max<size_t>(size_t(seg_capacity), vert_words * 2 + 65536);
-  want_segs = std::min<size_t>(want_segs, 0xFFFFFFF0u);
+  want_segs = std::min<size_t>(want_segs, cfg.max_segments > 0 ? size_t(cfg.max_segments) : size_t(0xFFFFFFF0u));
   if (want_segs > seg_capacity) {
     graph_valid = false;
     BLGpuResult rr = reserve_segments(uint32_t(want_segs));
@@ -433,7 +433,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   }
   v.segs = static_cast<DevSeg*>(seg_buf.ptr);
   v.seg_meta = reinterpret_cast<uint32_t*>(static_cast<char*>(seg_buf.ptr) + sizeof(DevSeg) * size_t(seg_capacity));
-  v.seg_capacity = seg_capacity;
+  v.seg_capacity = cfg.max_segments > 0 ? std::min<uint32_t>(seg_capacity, uint32_t(cfg.max_segments)) : seg_capacity;
   v.item_capacity = item_capacity;
   v.piece_capacity = piece_capacity;
   v.num_cmds = nc;
@@ -559,12 +559,13 @@ BLGpuResult Runtime::run(const Frame& fr) {
   d2h_bytes += 32;
   BLGPU_CHECK(cudaStreamSynchronize(stream));
   if (host_totals[0] > view.seg_capacity) {
+    if (cfg.max_segments > 0 && host_totals[0] > uint32_t(cfg.max_segments)) return BLGPU_ERROR_DATA_TOO_LARGE;
     // more segments than slots: grow and repeat the counting half (it is idempotent)
     r = reserve_segments(uint32_t(std::min<uint64_t>(uint64_t(host_totals[0]) * 5 / 4 + 1024, 0xFFFFFFF0u)));
     if (r) return r;
     view.segs = static_cast<DevSeg*>(seg_buf.ptr);
     view.seg_meta = reinterpret_cast<uint32_t*>(static_cast<char*>(seg_buf.ptr) + sizeof(DevSeg) * size_t(seg_capacity));
-    view.seg_capacity = seg_capacity;
+    view.seg_capacity = cfg.max_segments > 0 ? std::min<uint32_t>(seg_capacity, uint32_t(cfg.max_segments)) : seg_capacity;
     BLGPU_CHECK(cudaEventRecord(ev[0], stream));
     launches = enqueue_count_half(stream);
     BLGPU_CHECK(cudaGetLastError());
@@ -592,15 +593,17 @@ BLGpuResult Runtime::run(const Frame& fr) {
   launches += enqueue_render_half(stream, true);
   BLGPU_CHECK(cudaGetLastError());
   BLGPU_CHECK(cudaEventRecord(ev[3], stream));
-  BLGPU_CHECK(cudaMemcpyAsync(host_totals + 8, view.pixel_ops, 16, cudaMemcpyDeviceToHost, stream));
+  // error flags and pixel-op counters in one read-back
+  BLGPU_CHECK(cudaMemcpyAsync(host_totals + 20, view.error_flags, 32, cudaMemcpyDeviceToHost, stream));
   r = download();
   if (r) return r;
   BLGPU_CHECK(cudaStreamSynchronize(stream));
+  if (host_totals[20]) return BLGPU_ERROR_DATA_TOO_LARGE;   // a work array overflowed: pixels invalid
   has_frame = true;
   read_pixel_ops();
   stats.input_vertices = uint64_t((fr.verts.size() + fr.stroke_xy.size()) / 2);
   stats.h2d_bytes = h2d_bytes;
-  stats.d2h_bytes = d2h_bytes + 16;
+  stats.d2h_bytes = d2h_bytes + 32;
 
   float ms = 0.f, fine_ms = 0.f;
   cudaEventElapsedTime(&ms, ev[0], ev[3]);
@@ -748,8 +751,10 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     if (D.off > kNoAllocArenaBytes) { r = BLGPU_ERROR_DATA_TOO_LARGE; break; }
     launches += enqueue_render_half(stream, false);
     e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host_totals + 20, view.error_flags, 4, cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) { r = cuda_result(e); break; }
+    if (host_totals[20]) { r = BLGPU_ERROR_DATA_TOO_LARGE; break; }
     stats.fill_commands = nc;
     stats.segments = t.segs;
     stats.tiles = fr.tiles;
@@ -799,7 +804,7 @@ BLGpuResult Runtime::replay(bool use_graph) {
 
 void Runtime::read_pixel_ops() {
   uint64_t v[2];
-  memcpy(v, host_totals + 8, sizeof(v));
+  memcpy(v, host_totals + 24, sizeof(v));
   stats.pixel_ops = v[0];
   stats.pattern_ops = v[1];
 }
@@ -882,7 +887,8 @@ BLGpuResult Runtime::synchronize() {
   BLGPU_CHECK(cudaSetDevice(device));
   BLGPU_CHECK(cudaStreamSynchronize(stream));
   if (pending_timing) {
-    BLGPU_CHECK(cudaMemcpy(host_totals + 8, view.pixel_ops, 16, cudaMemcpyDeviceToHost));
+    BLGPU_CHECK(cudaMemcpy(host_totals + 20, view.error_flags, 32, cudaMemcpyDeviceToHost));
+    if (host_totals[20]) { pending_timing = 0; return BLGPU_ERROR_DATA_TOO_LARGE; }
     read_pixel_ops();
     float ms = 0.f, fine_ms = 0.f;
     cudaEventElapsedTime(&ms, ev[0], ev[3]);

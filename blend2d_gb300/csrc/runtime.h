@@ -159,7 +159,8 @@ struct Runtime {
   uint32_t seg_capacity = 0;
   void* host_staging = nullptr;
   size_t host_staging_size = 0;
-  uint32_t* host_totals = nullptr;   // pinned: [0..8) frame totals, [8..12) pixel ops
+  uint32_t* host_totals = nullptr;   // pinned: [0..8) frame totals, [16] stroke outline size,
+                                     // [20..24) error flags (ErrorFlag bits in [20]), [24..28) pixel ops
 
   cudaEvent_t ev[5] = {};
   // Gradient LUTs are built on a side stream, forked after the upload and joined before the

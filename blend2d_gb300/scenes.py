@@ -494,26 +494,146 @@ def patterns(seed: int = 3, width: int = 4096, height: int = 4096, count: int = 
     return sw
 
 
+def _ragged_rows(parts, n: int) -> np.ndarray:
+    """Row-wise concatenation of ragged parts: row i of the result is, for each (padded, lengths)
+    part in order, the first lengths[i] words of padded[i]; rows follow each other."""
+    lens = np.stack([l for _, l in parts], axis=1)
+    row_tot = lens.sum(axis=1)
+    row_start = np.cumsum(row_tot) - row_tot
+    out = np.empty(int(row_tot.sum()), dtype=np.uint64)
+    within = np.zeros(n, dtype=np.int64)
+    for arr, l in parts:
+        mask = np.arange(arr.shape[1])[None, :] < l[:, None]
+        vals = arr[mask]
+        first = np.cumsum(l) - l
+        dest = np.repeat(row_start + within, l) + (np.arange(vals.size) - np.repeat(first, l))
+        out[dest] = vals
+        within += l
+    return out
+
+
+def _rec_word(op: int, payload_bytes) -> np.ndarray:
+    """First word of a record: op code, payload size (little-endian <II)."""
+    return np.uint64(op) | (np.asarray(payload_bytes, dtype=np.uint64) << np.uint64(32))
+
+
+def _rgba64_words(c: np.ndarray) -> np.ndarray:
+    """Vectorized rgba64_from_rgba32 on uint64 arrays of ARGB32 values."""
+    out = np.zeros_like(c)
+    for sh in (0, 8, 16, 24):
+        out |= ((c >> np.uint64(sh)) & np.uint64(255)) * np.uint64(257) << np.uint64(2 * sh)
+    return out
+
+
 def _mixed_canvas(rng, w: int, h: int, n: int) -> StreamWriter:
-    """Opaque-black canvas with `n` paths of the polygon kind (10-vertex polygon, solid colour) or
-    the curve kind (closed cubic path, gradient), mixed comp-ops and fill rules."""
+    """Opaque-black canvas with `n` paths of the polygon kind (10-vertex polygon in the path's
+    box, solid colour) or the curve kind (closed path of 4-12 cubics with control points in the
+    box, linear/radial/conic gradient with 2-8 stops and pad/repeat/reflect extend), each with a
+    random comp-op (SrcOver/SrcCopy) and fill rule; box side log-uniform 8-256 px (at most the
+    canvas side), placed so that at least a quarter of the box lies on the canvas. The records are
+    laid out with whole-array operations (a canvas of 5,000 paths takes milliseconds)."""
+    u64 = np.uint64
+    side = np.minimum(_log_uniform(rng, 8.0, 256.0, n), float(max(w, h)))
+    x0 = rng.uniform(-side * 0.25, np.maximum(w - side * 0.75, 1.0))
+    y0 = rng.uniform(-side * 0.25, np.maximum(h - side * 0.75, 1.0))
+    comp = rng.integers(0, 2, n).astype(u64)
+    rule = rng.integers(0, 2, n).astype(u64)
+    curve = rng.integers(0, 2, n).astype(bool)
+    org = np.stack([x0, y0], axis=1)
+    # per-kind draws: solid colours and polygon vertices for the polygon rows, gradients and
+    # cubic control points for the curve rows
+    ip, ic = np.flatnonzero(~curve), np.flatnonzero(curve)
+    npoly, nc = ip.size, ic.size
+    color = np.zeros(n, dtype=u64)
+    color[ip] = rng.integers(0, 2**32, npoly, dtype=u64)
+    xy = np.zeros((n, 38, 2))
+    xy[ip, :10] = rng.uniform(0.0, 1.0, (npoly, 10, 2)) * side[ip, None, None] + org[ip, None, :]
+    gkind = np.zeros(n, dtype=np.int64)
+    nst = np.zeros(n, dtype=np.int64)
+    ext = np.zeros(n, dtype=u64)
+    gkind[ic] = rng.integers(0, 3, nc)
+    nst[ic] = rng.integers(2, 9, nc)
+    ext[ic] = rng.integers(0, 3, nc).astype(u64)
+    offs = np.full((n, 8), 2.0)
+    offs[ic] = rng.uniform(0.0, 1.0, (nc, 8))
+    offs = np.sort(np.where(np.arange(8)[None, :] < nst[:, None], offs, 2.0), axis=1)
+    scol = np.zeros((n, 8), dtype=u64)
+    scol[ic] = _rgba64_words(rng.integers(0, 2**32, (nc, 8), dtype=u64))
+    gp = np.zeros((n, 4))
+    gp[ic] = rng.uniform(0.0, 1.0, (nc, 4)) * side[ic, None] + np.stack([x0[ic], y0[ic], x0[ic], y0[ic]], axis=1)
+    angle = np.zeros(n)
+    angle[ic] = rng.uniform(0.0, 2 * math.pi, nc)
+    nseg = np.full(n, 4, dtype=np.int64)
+    nseg[ic] = rng.integers(4, 13, nc)
+    ctrl = rng.uniform(0.0, 1.0, (nc, 36, 2)) * side[ic, None, None] + org[ic, None, :]
+
+    # comp-op and fill-rule records (4 words)
+    pre = np.empty((n, 4), dtype=u64)
+    pre[:, 0] = _rec_word(OP_SET_COMP_OP, 8)
+    pre[:, 1] = comp
+    pre[:, 2] = _rec_word(OP_SET_FILL_RULE, 8)
+    pre[:, 3] = rule
+    # style: solid colour (2 words) or gradient (15 + 2 * stops words)
+    sty = np.zeros((n, 31), dtype=u64)
+    sty_len = np.where(curve, 15 + 2 * nst, 2)
+    sty[:, 0] = np.where(curve, _rec_word(OP_STYLE_GRADIENT, 112 + 16 * nst), _rec_word(OP_STYLE_RGBA32, 8))
+    sty[:, 1] = np.where(curve, gkind.astype(u64) | (ext << u64(32)), color)
+    sty[:, 2] = nst.astype(u64)                                   # stop count, no transform
+    vals = np.zeros((n, 6))
+    vals[:, 0:4] = gp                                             # linear: p0, p1; radial: c, f
+    vals[:, 4] = np.where(gkind == RADIAL, side * 0.5, 0.0)       # radial r0 (r1 = 0)
+    con = gkind == CONIC
+    vals[con, 2] = angle[con]                                     # conic: c, angle, repeat 1
+    vals[con, 3] = 1.0
+    sty[:, 3:9] = vals.view(u64)
+    sty[:, 9:15] = np.array([1.0, 0.0, 0.0, 1.0, 0.0, 0.0]).view(u64)[None, :]
+    sty[:, 15:31:2] = offs.view(u64)
+    sty[:, 16:31:2] = scol
+    # geometry: polygon (2 + 20 words) or path (2 + command words + 2 * vertices)
+    ncmd = 3 * nseg + 2
+    cw = (ncmd + 7) // 8
+    geo = np.empty((n, 2), dtype=u64)
+    geo[:, 0] = np.where(curve, _rec_word(OP_FILL_PATH_D, 8 + 8 * cw + 16 * ncmd), _rec_word(OP_FILL_POLYGON_D, 168))
+    geo[:, 1] = np.where(curve, ncmd, 10).astype(u64)
+    cmd_bytes = np.zeros((n, 40), dtype=np.uint8)
+    cmd_bytes[:, 0] = P_MOVE
+    cmd_bytes[:, 1:37] = P_CUBIC
+    rows = np.arange(n)
+    cmd_bytes[rows, 1 + 3 * nseg] = P_CLOSE
+    cmd_bytes[np.arange(40)[None, :] > (1 + 3 * nseg)[:, None]] = 0
+    cmd_words = cmd_bytes.view(u64)
+    start = ctrl[np.arange(nc), 3 * nseg[ic] - 1]
+    xy[ic, 0] = start
+    xy[ic, 1:37] = ctrl
+    xy[ic, 1 + 3 * nseg[ic]] = start
+    xy_words = xy.reshape(n, 76).view(u64)
+    body = _ragged_rows([(pre, np.full(n, 4)), (sty, sty_len), (geo, np.full(n, 2)),
+                         (cmd_words, np.where(curve, cw, 0)), (xy_words, np.where(curve, 2 * ncmd, 20))], n)
     sw = StreamWriter(w, h)
     sw.solid(0xFF000000)
     sw.fill_all()
-    for _ in range(n):
-        side = float(min(_log_uniform(rng, 8.0, 256.0), max(w, h)))
-        x0 = float(rng.uniform(-side * 0.25, max(w - side * 0.75, 1.0)))
-        y0 = float(rng.uniform(-side * 0.25, max(h - side * 0.75, 1.0)))
-        sw.comp_op(int(rng.integers(0, 2)))
-        sw.fill_rule(int(rng.integers(0, 2)))
-        if rng.integers(0, 2) == 0:
-            sw.solid(int(rng.integers(0, 2**32, dtype=np.uint64)))
-            sw.fill_polygon(rng.uniform(0, side, (10, 2)) + np.array([x0, y0]))
-        else:
-            _gradient_style(rng, sw, x0, y0, side)
-            cmds, xy = _cubic_path(rng, x0, y0, side, int(rng.integers(4, 13)))
-            sw.fill_path(cmds, xy)
+    sw.parts.append(body.astype("<u8").tobytes())
+    sw.fill_count += n
     return sw
+
+
+def batch_canvas_specs(seed: int = 4, count: int = 4096, min_side: int = 32, max_side: int = 2048,
+                       min_paths: int = 10, max_paths: int = 5000, scale: float = 1.0):
+    """(width, height, paths) of every canvas of the batched workload: width and height
+    log-uniform in [min_side, max_side], path count log-uniform in [min_paths, max_paths] (times
+    `scale`, at least 1)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    w = _log_uniform(rng, min_side, max_side, count).astype(np.int64)
+    h = _log_uniform(rng, min_side, max_side, count).astype(np.int64)
+    n = np.maximum(1, (_log_uniform(rng, min_paths, max_paths, count) * scale).astype(np.int64))
+    return [(int(a), int(b), int(c)) for a, b, c in zip(w, h, n)]
+
+
+def batch_canvas(index: int, seed: int = 4, count: int = 4096, **kw) -> StreamWriter:
+    """Canvas `index` of batch_canvases(seed, count, **kw), generated on its own: each canvas
+    draws from its own generator, seeded with (seed, index)."""
+    w, h, n = batch_canvas_specs(seed, count, **kw)[index]
+    return _mixed_canvas(np.random.Generator(np.random.PCG64([seed, index])), w, h, n)
 
 
 def batch_canvases(seed: int = 4, count: int = 4096, min_side: int = 32, max_side: int = 2048,
@@ -521,28 +641,34 @@ def batch_canvases(seed: int = 4, count: int = 4096, min_side: int = 32, max_sid
     """Independent canvases for the batched renderer: width and height log-uniform in
     [min_side, max_side], log-uniform path counts, each path of the polygon or cubic kind with a
     mixed style (solid or gradient) and comp-op. `scale` shrinks path counts for quick runs."""
+    specs = batch_canvas_specs(seed, count, min_side, max_side, min_paths, max_paths, scale)
+    return [_mixed_canvas(np.random.Generator(np.random.PCG64([seed, i])), w, h, n)
+            for i, (w, h, n) in enumerate(specs)]
+
+
+def serving_request_specs(seed: int = 5, count: int = 48, min_side: int = 64, max_side: int = 4096,
+                          min_paths: int = 1, max_paths: int = 20000, scale: float = 1.0):
+    """(side, paths) of every request of serving_requests(seed, count, ...)."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    out = []
-    for _ in range(count):
-        w = int(_log_uniform(rng, min_side, max_side))
-        h = int(_log_uniform(rng, min_side, max_side))
-        n = max(1, int(_log_uniform(rng, min_paths, max_paths) * scale))
-        out.append(_mixed_canvas(rng, w, h, n))
-    return out
+    sides = _log_uniform(rng, min_side, max_side, count).astype(np.int64)
+    n = np.maximum(1, (_log_uniform(rng, min_paths, max_paths, count) * scale).astype(np.int64))
+    return [(int(s), int(k)) for s, k in zip(sides, n)]
 
 
-def serving_requests(seed: int = 5, count: int = 32, min_side: int = 64, max_side: int = 4096,
+def serving_request(index: int, seed: int = 5, count: int = 48, **kw) -> StreamWriter:
+    """Request `index` of serving_requests(seed, count, **kw), generated on its own."""
+    s, k = serving_request_specs(seed, count, **kw)[index]
+    return _mixed_canvas(np.random.Generator(np.random.PCG64([seed, index])), s, s, k)
+
+
+def serving_requests(seed: int = 5, count: int = 48, min_side: int = 64, max_side: int = 4096,
                      min_paths: int = 1, max_paths: int = 20000, scale: float = 1.0):
     """Render requests for the serving loop: square canvases with side log-uniform in
     [min_side, max_side] and log-uniform path counts in [min_paths, max_paths] (times `scale`),
     paths of the polygon and curve kinds with mixed styles."""
-    rng = np.random.Generator(np.random.PCG64(seed))
-    out = []
-    for _ in range(count):
-        side = int(_log_uniform(rng, min_side, max_side))
-        n = max(1, int(_log_uniform(rng, min_paths, max_paths) * scale))
-        out.append(_mixed_canvas(rng, side, side, n))
-    return out
+    specs = serving_request_specs(seed, count, min_side, max_side, min_paths, max_paths, scale)
+    return [_mixed_canvas(np.random.Generator(np.random.PCG64([seed, i])), s, s, k)
+            for i, (s, k) in enumerate(specs)]
 
 
 # ------------------------------------------------------------------------------------------------

@@ -127,7 +127,10 @@ typedef struct BLGpuLaunchConfig {
   int32_t cubic_blocks_per_sm;  /* lane-scheduled curve-piece flattener grid */
   int32_t no_occlusion_cull;    /* 1: composite every command of every strip (pixel-op counts of the
                                    reference's work; same pixels) */
-  int32_t reserved[2];
+  int32_t max_segments;         /* 0: the segment array grows as frames need; N > 0: it never holds more
+                                   than N segments, and a frame that emits more fails with
+                                   BLGPU_ERROR_DATA_TOO_LARGE (a cap on the runtime's device memory) */
+  int32_t reserved[1];
 } BLGpuLaunchConfig;
 
 /* --- runtime (device, stream, memory) --------------------------------------------------- */

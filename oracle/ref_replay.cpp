@@ -5,9 +5,14 @@
 // Every record maps 1:1 onto the reference C++ API (blend2d/core/context.h:2155-2700).
 //
 //   b2d_replay_<variant> <stream.bin> <out.raw|-> [--threads N] [--frames K]
+//   b2d_replay_<variant> --batch <list.txt> [--threads N] [--repeat K] [--out-dir D]
 //
 // With --frames K the stream is rendered K+1 times (one warm-up) and the median wall time of
 // `begin -> all calls -> end()` is printed as JSON on stdout.
+// With --batch every stream named in list.txt (one path per line) is read and parsed first, then
+// all of them are rendered one after the other (one BLContext per canvas, `thread_count` N), K
+// times; the wall time of each pass is printed as JSON. --out-dir writes canvas i's pixels to
+// D/<i>.raw after the last pass.
 
 #include <blend2d/blend2d.h>
 #include <blgpu_stream.h>
@@ -267,7 +272,66 @@ static void replay(const Stream& s, BLImage& img, uint32_t threads) {
   ctx.end();
 }
 
+static int run_batch(int argc, char** argv) {
+  const char* list = argv[2];
+  uint32_t threads = 0;
+  int repeat = 1;
+  const char* out_dir = nullptr;
+  for (int i = 3; i + 1 < argc; i += 2) {
+    if (!strcmp(argv[i], "--threads")) threads = uint32_t(atoi(argv[i + 1]));
+    else if (!strcmp(argv[i], "--repeat")) repeat = atoi(argv[i + 1]);
+    else if (!strcmp(argv[i], "--out-dir")) out_dir = argv[i + 1];
+  }
+  std::vector<std::vector<uint8_t>> bufs;
+  {
+    FILE* f = fopen(list, "r");
+    if (!f) { fprintf(stderr, "cannot open %s\n", list); return 2; }
+    char line[4096];
+    while (fgets(line, sizeof(line), f)) {
+      size_t n = strlen(line);
+      while (n && (line[n - 1] == '\n' || line[n - 1] == '\r')) line[--n] = 0;
+      if (n) bufs.push_back(read_file(line));
+    }
+    fclose(f);
+  }
+  std::vector<Stream> streams(bufs.size());
+  std::vector<BLImage> imgs;
+  uint64_t pixels = 0;
+  for (size_t i = 0; i < bufs.size(); i++) {
+    streams[i].base = bufs[i].data();
+    streams[i].size = bufs[i].size();
+    parse_header(streams[i]);
+    imgs.emplace_back(int(streams[i].hdr.width), int(streams[i].hdr.height), BL_FORMAT_PRGB32);
+    pixels += uint64_t(streams[i].hdr.width) * streams[i].hdr.height;
+  }
+  std::vector<double> ms;
+  for (int k = 0; k < repeat; k++) {
+    auto t0 = std::chrono::steady_clock::now();
+    for (size_t i = 0; i < streams.size(); i++) replay(streams[i], imgs[i], threads);
+    auto t1 = std::chrono::steady_clock::now();
+    ms.push_back(std::chrono::duration<double, std::milli>(t1 - t0).count());
+  }
+  printf("{\"canvases\": %zu, \"pixels\": %llu, \"threads\": %u, \"times_ms\": [", streams.size(),
+         (unsigned long long)pixels, threads);
+  for (size_t k = 0; k < ms.size(); k++) printf("%s%.4f", k ? ", " : "", ms[k]);
+  printf("]}\n");
+  if (out_dir) {
+    for (size_t i = 0; i < imgs.size(); i++) {
+      BLImageData d;
+      imgs[i].get_data(&d);
+      std::string path = std::string(out_dir) + "/" + std::to_string(i) + ".raw";
+      FILE* f = fopen(path.c_str(), "wb");
+      if (!f) { fprintf(stderr, "cannot write %s\n", path.c_str()); return 2; }
+      for (int y = 0; y < d.size.h; y++)
+        fwrite(static_cast<const uint8_t*>(d.pixel_data) + intptr_t(y) * d.stride, 1, size_t(d.size.w) * 4u, f);
+      fclose(f);
+    }
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc >= 3 && !strcmp(argv[1], "--batch")) return run_batch(argc, argv);
   if (argc < 3) {
     fprintf(stderr, "usage: %s stream.bin out.raw|- [--threads N] [--frames K]\n", argv[0]);
     return 2;

@@ -75,9 +75,24 @@ def scene_catalog(full: bool):
     for i in range(6):
         cat.append((f"batch_{i}", f"scenes.batch_canvases(seed=4, count=6, max_side=640, max_paths=400)[{i}]", ("default",)))
     if full:
-        cat.append(("curves", "scenes.curves()", ("default",)))
+        # the benchmarked workloads at full size: the 20,000-path curves frame, the 50,000-quad
+        # pattern frame, a sample of the 4,096 batched canvases (the largest, the one with the
+        # most paths, the largest area x paths, eight seeded picks) and of the serving requests
+        cat.append(("curves", "scenes.curves()", ("default", "scalar")))
         cat.append(("patterns", "scenes.patterns()", ("default",)))
+        for i in BATCH_SAMPLE:
+            cat.append((f"batch4096_{i}", f"scenes.batch_canvas({i})", ("default", "scalar")))
+        for i in SERVE_SAMPLE:
+            cat.append((f"serve48_{i}", f"scenes.serving_request({i})", ("default",)))
     return cat
+
+
+# Canvases of scenes.batch_canvases() (4,096) and requests of scenes.serving_requests(count=48)
+# recorded at full size: the largest canvas (798), the most paths (2537), the largest area x
+# paths (248) and eight seeded picks; for serving, the largest side (9), the most paths (28) and
+# two more with over 10,000 paths on large canvases (1, 27).
+BATCH_SAMPLE = (248, 429, 701, 798, 1071, 1555, 2537, 3779, 3994, 4004, 4041)
+SERVE_SAMPLE = (1, 9, 27, 28)
 
 
 def build_reference(ref: str):

@@ -111,6 +111,55 @@ def test_batch_canvases_workload_matches_individual(runtimes):
             assert np.array_equal(single, oracle_lib.render(s)), f"canvas {i} vs oracle"
 
 
+def _oracle_many(streams, variant="default"):
+    """Oracle renders of many streams on the host's cores (the oracle's ctypes calls release the
+    GIL, so threads render in parallel)."""
+    from concurrent.futures import ThreadPoolExecutor
+    import os
+    with ThreadPoolExecutor(max_workers=max(1, os.cpu_count() or 1)) as ex:
+        return list(ex.map(lambda s: oracle_lib.render(s, variant), streams))
+
+
+# 64 canvases of the full batched workload (4,096 canvases of 32-2,048 px, 10-5,000 paths): the
+# canvases whose reference renders are recorded in the golden file (the largest canvas, the most
+# paths, the largest area x paths and eight seeded picks) and 53 more seeded picks.
+FULL_BATCH_SAMPLE = sorted(set(
+    [int(e["expr"].split("(")[1].rstrip(")")) for e in GOLDEN["scenes"] if e["name"].startswith("batch4096_")]
+    + np.random.default_rng(404).choice(4096, 53, replace=False).tolist()))
+
+
+def test_full_batch_sample_vs_oracle(runtimes):
+    """A 64-canvas sample of the full-size batched workload, rendered in one batched pipeline:
+    every canvas equals the oracle's render, and the ones the golden file holds equal the
+    reference's own renders."""
+    sws = [scenes.batch_canvas(i) for i in FULL_BATCH_SAMPLE]
+    streams = [sw.to_bytes() for sw in sws]
+    targets = [np.zeros((sw.height, sw.width), dtype=np.uint32) for sw in sws]
+    runtimes().render_batch(streams, targets)
+    golden = {e["expr"]: e["pixels_sha256"]["default"] for e in GOLDEN["scenes"] if e["name"].startswith("batch4096_")}
+    for i, t in zip(FULL_BATCH_SAMPLE, targets):
+        want = golden.get(f"scenes.batch_canvas({i})")
+        if want:
+            assert oracle_lib.sha256(t) == want, f"canvas {i}: differs from the reference render"
+    for i, t, want in zip(FULL_BATCH_SAMPLE, targets, _oracle_many(streams)):
+        assert not _diff(t, want), f"canvas {i}: {_diff(t, want)}"
+
+
+def test_capacity_overflow_is_an_error():
+    """A frame whose device work arrays overflow reports BL_ERROR_DATA_TOO_LARGE instead of
+    rendering with work dropped: the segment array is capped below what the frame emits (the
+    runtime's regrow is disabled for this runtime), and the frame must fail, not draw less."""
+    stream = scenes.curves(count=300, width=320, height=200).to_bytes()
+    with bg.Runtime(0) as rt:
+        rt.set_segment_limit(1000)
+        with pytest.raises(bg.BLGpuError) as ei:
+            bg.render_stream(rt, stream)
+        assert ei.value.code == bg.ERROR_DATA_TOO_LARGE
+        rt.set_segment_limit(0)
+        got = bg.render_stream(rt, stream)
+    assert not _diff(got, oracle_lib.render(stream))
+
+
 def test_context_calls_match_stream(runtimes):
     """The same scene through individual bl_context_* calls and through a submitted stream."""
     rng = np.random.default_rng(5)
