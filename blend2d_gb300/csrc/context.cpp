@@ -12,8 +12,10 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <deque>
 #include <condition_variable>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <new>
@@ -39,6 +41,7 @@ struct AsyncSlot {
 struct BLGpuRuntime {
   Runtime rt;
   Frame batch_frame;               // reused by blgpu_render_batch (its page-locked arrays persist)
+  std::vector<std::unique_ptr<Frame>> batch_parts;   // per recording thread of blgpu_render_batch
   std::mutex batch_lock;
   // One pipeline run at a time: the submission thread and every synchronous entry point that
   // touches `rt` hold it.
@@ -1404,32 +1407,74 @@ BLGPU_API BLGpuResult blgpu_context_submit_stream(BLGpuContext* ctx, const void*
 }
 
 // Batched rendering: every stream gets its own canvas in one shared frame, so one device
-// pipeline (one persistent fine launch) renders all of them.
+// pipeline (one persistent fine launch) renders all of them. Canvases are independent, so the
+// streams are recorded by several threads at once, each into a frame of its own over a contiguous
+// range of canvases (balanced by stream bytes), and the parts are then merged into the runtime's
+// batch frame in canvas order: the merged frame is the one sequential recording gives.
 BLGPU_API BLGpuResult blgpu_render_batch(BLGpuRuntime* rt, const void* const* streams, const size_t* sizes,
                                          const BLGpuImage* images, uint32_t count) {
   if (!rt || (count && (!streams || !sizes || !images))) return BLGPU_ERROR_INVALID_VALUE;
   if (!count) return BLGPU_SUCCESS;
-  std::lock_guard<std::mutex> guard(rt->batch_lock);
-  Frame& frame = rt->batch_frame;
-  frame.clear();
-  std::vector<BLGpuContext> ctxs(count);
   for (uint32_t i = 0; i < count; i++) {
-    BLGpuContext& c = ctxs[i];
     const BLGpuImage& im = images[i];
     if (im.format != BLGPU_FORMAT_PRGB32 || im.width <= 0 || im.height <= 0 || im.width > 65535 ||
         im.height > 65535 || !im.pixel_data || im.stride < intptr_t(im.width) * 4)
       return BLGPU_ERROR_INVALID_VALUE;
-    c.rt = rt;
-    c.frame = &frame;
-    c.target = im;
-    c.w = im.width;
-    c.h = im.height;
-    c.bound = true;
-    c.canvas = frame.add_canvas(im, true);
-    c.reset_state();
-    BLGpuResult r = c.submit_stream(static_cast<const uint8_t*>(streams[i]), sizes[i]);
+  }
+  std::lock_guard<std::mutex> guard(rt->batch_lock);
+  Frame& frame = rt->batch_frame;
+  std::vector<BLGpuContext> ctxs(count);
+  // recording threads: about one per 8 canvases, at most one per host core (and 32)
+  size_t total_bytes = 0;
+  for (uint32_t i = 0; i < count; i++) total_bytes += sizes[i];
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const unsigned nt = std::max(1u, std::min({hw, 32u, (count + 7u) / 8u}));
+  while (rt->batch_parts.size() < nt) rt->batch_parts.emplace_back(new Frame(false));
+  std::vector<uint32_t> first(nt + 1, count);
+  first[0] = 0;
+  {
+    size_t acc = 0;
+    unsigned t = 1;
+    for (uint32_t i = 0; i < count && t < nt; i++) {
+      acc += sizes[i];
+      if (acc * nt >= total_bytes * t) first[t++] = i + 1;
+    }
+  }
+  std::vector<BLGpuResult> errors(nt, BLGPU_SUCCESS);
+  auto record = [&](unsigned t) {
+    Frame& part = nt == 1 ? frame : *rt->batch_parts[t];
+    part.clear();
+    for (uint32_t i = first[t]; i < first[t + 1]; i++) {
+      BLGpuContext& c = ctxs[i];
+      const BLGpuImage& im = images[i];
+      c.rt = rt;
+      c.frame = &part;
+      c.target = im;
+      c.w = im.width;
+      c.h = im.height;
+      c.bound = true;
+      c.canvas = part.add_canvas(im, true);
+      c.reset_state();
+      BLGpuResult r = c.submit_stream(static_cast<const uint8_t*>(streams[i]), sizes[i]);
+      c.bound = false;
+      if (r) { errors[t] = r; return; }
+    }
+  };
+  if (nt == 1) {
+    record(0);
+  }
+  else {
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; t++) pool.emplace_back(record, t);
+    record(0);
+    for (auto& th : pool) th.join();
+  }
+  for (BLGpuResult r : errors)      // the first failing canvas's error, as sequential recording gives
     if (r) return r;
-    c.bound = false;
+  if (nt > 1) {
+    std::vector<Frame*> parts(nt);
+    for (unsigned t = 0; t < nt; t++) parts[t] = rt->batch_parts[t].get();
+    frame.merge(parts.data(), nt, nt);
   }
   if (frame.cmds.empty()) return BLGPU_SUCCESS;
   BLGpuContext::mark_uploads(frame);

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <thread>
 
 #include "launch.h"
 #include "noalloc.h"
@@ -100,6 +101,112 @@ uint64_t Frame::add_image(const BLGpuImage& image) {
   image_words += align_up((bytes + 3u) / 4u, 4);
   images.push_back(im);
   return im.pool_offset;
+}
+
+void Frame::merge(Frame* const* parts, size_t count, unsigned threads) {
+  // where each part's elements start in the merged frame
+  struct Base {
+    size_t cmd, style, xform, canvas, vert, stop, lut_job, image, fig, param, stroke_vert;
+    uint64_t image_words;
+    uint32_t lut_words, tiles, rows;
+  };
+  std::vector<Base> base(count + 1);
+  Base acc{};
+  for (size_t p = 0; p < count; p++) {
+    acc.lut_words = (acc.lut_words + 1u) & ~1u;   // 64-bit (dithered) LUT entries stay 8-byte aligned
+    base[p] = acc;
+    const Frame& f = *parts[p];
+    acc.cmd += f.cmds.size(); acc.style += f.styles.size(); acc.xform += f.xforms.size();
+    acc.canvas += f.canvases.size(); acc.vert += f.path_cmds.size(); acc.stop += f.stops.size();
+    acc.lut_job += f.lut_jobs.size(); acc.image += f.images.size(); acc.fig += f.stroke_figs.size();
+    acc.param += f.stroke_params.size(); acc.stroke_vert += f.stroke_cmds.size();
+    acc.image_words += f.image_words; acc.lut_words += f.lut_words; acc.tiles += f.tiles; acc.rows += f.rows;
+  }
+  clear();
+  cmds.resize_uninit(acc.cmd); styles.resize_uninit(acc.style); xforms.resize_uninit(acc.xform);
+  verts.resize_uninit(2 * acc.vert); path_cmds.resize_uninit(acc.vert); lut_jobs.resize_uninit(acc.lut_job);
+  stops.resize_uninit(acc.stop); stroke_figs.resize_uninit(acc.fig); stroke_params.resize_uninit(acc.param);
+  stroke_xy.resize_uninit(2 * acc.stroke_vert); stroke_cmds.resize_uninit(acc.stroke_vert);
+  canvases.resize(acc.canvas);
+  targets.resize(acc.canvas);
+  images.resize(acc.image);
+  image_words = acc.image_words; lut_words = acc.lut_words; tiles = acc.tiles; rows = acc.rows;
+
+  auto copy_part = [&](size_t p) {
+    const Frame& f = *parts[p];
+    const Base& o = base[p];
+    for (size_t i = 0; i < f.cmds.size(); i++) {
+      DevCmd c = f.cmds[i];
+      c.canvas += uint32_t(o.canvas);
+      c.style += uint32_t(o.style);
+      if (c.kind == kFillMaskA) {   // geom_first / xform: the mask's byte offset in the image pool
+        const uint64_t off = ((uint64_t(c.xform) << 32) | c.geom_first) + o.image_words * 4u;
+        c.geom_first = uint32_t(off);
+        c.xform = uint32_t(off >> 32);
+      }
+      else {
+        c.xform += uint32_t(o.xform);
+        if (c.kind == kFillAnalytic) c.geom_first += uint32_t(o.vert);
+      }
+      cmds[o.cmd + i] = c;
+    }
+    for (size_t i = 0; i < f.styles.size(); i++) {
+      DevStyle d = f.styles[i];
+      if (d.lut_size) d.lut_offset += o.lut_words;
+      if (d.fetch >= kFetchPatAlignedPad) d.src_offset += o.image_words;
+      styles[o.style + i] = d;
+    }
+    if (f.xforms.size()) memcpy(&xforms[o.xform], f.xforms.data(), sizeof(DevXform) * f.xforms.size());
+    for (size_t i = 0; i < f.canvases.size(); i++) {
+      DevCanvas cv = f.canvases[i];
+      cv.tile_base += o.tiles;
+      cv.row_base += o.rows;
+      cv.cmd_first += uint32_t(o.cmd);
+      canvases[o.canvas + i] = cv;
+      targets[o.canvas + i] = f.targets[i];
+    }
+    if (f.path_cmds.size()) {
+      memcpy(&verts[2 * o.vert], f.verts.data(), sizeof(double) * f.verts.size());
+      memcpy(&path_cmds[o.vert], f.path_cmds.data(), f.path_cmds.size());
+    }
+    for (size_t i = 0; i < f.lut_jobs.size(); i++) {
+      DevLutJob j = f.lut_jobs[i];
+      j.style += uint32_t(o.style);
+      j.stop_first += uint32_t(o.stop);
+      j.lut_offset += o.lut_words;
+      lut_jobs[o.lut_job + i] = j;
+    }
+    if (f.stops.size()) memcpy(&stops[o.stop], f.stops.data(), sizeof(DevStop) * f.stops.size());
+    for (size_t i = 0; i < f.images.size(); i++) {
+      FrameImage im = f.images[i];
+      im.pool_offset += o.image_words;
+      images[o.image + i] = im;
+    }
+    for (size_t i = 0; i < f.stroke_figs.size(); i++) {
+      DevStrokeFig g = f.stroke_figs[i];
+      g.first += uint32_t(o.stroke_vert);
+      g.end += uint32_t(o.stroke_vert);
+      g.cmd += uint32_t(o.cmd);
+      g.param += uint32_t(o.param);
+      stroke_figs[o.fig + i] = g;
+    }
+    if (f.stroke_params.size())
+      memcpy(&stroke_params[o.param], f.stroke_params.data(), sizeof(DevStrokeParams) * f.stroke_params.size());
+    if (f.stroke_cmds.size()) {
+      memcpy(&stroke_xy[2 * o.stroke_vert], f.stroke_xy.data(), sizeof(double) * f.stroke_xy.size());
+      memcpy(&stroke_cmds[o.stroke_vert], f.stroke_cmds.data(), f.stroke_cmds.size());
+    }
+  };
+  const size_t nt = std::max<size_t>(1, std::min<size_t>(threads, count));
+  if (nt == 1) {
+    for (size_t p = 0; p < count; p++) copy_part(p);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> pool;
+  for (size_t t = 0; t < nt; t++)
+    pool.emplace_back([&] { for (size_t p; (p = next.fetch_add(1)) < count;) copy_part(p); });
+  for (auto& th : pool) th.join();
 }
 
 // --- device memory ----------------------------------------------------------------------------

@@ -86,6 +86,11 @@ struct HostArray {
     memcpy(ptr + n, first, count * sizeof(T));
     n += count;
   }
+  // Sets the size to `count` elements; the new ones are left uninitialized (to be written).
+  void resize_uninit(size_t count) {
+    reserve(count);
+    n = count;
+  }
   void append_fill(size_t count, const T& v) {
     reserve(n + count);
     for (size_t i = 0; i < count; i++) ptr[n + i] = v;
@@ -127,6 +132,10 @@ struct Frame {
   uint32_t add_canvas(const BLGpuImage& image, bool upload);
   // Registers a pattern image (deduplicated by pixel pointer); returns the pool offset.
   uint64_t add_image(const BLGpuImage& image);
+  // Replaces this frame's content with the concatenation of `parts` (frames recorded on their
+  // own, e.g. by several threads), shifting every index a part holds by what the parts before it
+  // hold. The copies run on up to `threads` threads.
+  void merge(Frame* const* parts, size_t count, unsigned threads);
 };
 
 // Sizes produced by the counting half of the pipeline, cached for replay.

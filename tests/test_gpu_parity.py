@@ -111,6 +111,29 @@ def test_batch_canvases_workload_matches_individual(runtimes):
             assert np.array_equal(single, oracle_lib.render(s)), f"canvas {i} vs oracle"
 
 
+def test_batch_of_every_kind_equals_individual(runtimes):
+    """Batches are recorded by several threads and merged: canvases with every kind of recorded
+    data (dithered and plain gradients, patterns, strokes, A8 masks, blits, shapes) render in a
+    batch exactly as they render alone."""
+    streams = []
+    for k in range(5):
+        streams.append(scenes.random_mix(6000 + k, width=90 + 13 * k, height=70 + 7 * k, count=60, dither=k % 2 == 0).to_bytes())
+        streams.append(scenes.strokes(seed=6100 + k, width=120, height=90, count=40).to_bytes())
+        streams.append(scenes.masks(seed=6200 + k, width=110, height=80, count=30).to_bytes())
+        streams.append(scenes.blits(seed=6300 + k, width=100, height=100, count=30).to_bytes())
+        streams.append(scenes.shapes(seed=6400 + k, width=130, height=90, count=30).to_bytes())
+    rt = runtimes()
+    sizes = [oracle_lib.stream_size(s) for s in streams]
+    batched = [np.zeros((h, w), dtype=np.uint32) for w, h in sizes]
+    rt.render_batch(streams, batched)
+    for i, s in enumerate(streams):
+        single = bg.render_stream(rt, s)
+        assert not _diff(batched[i], single), f"canvas {i}: {_diff(batched[i], single)}"
+        if i % 5 == 0 or i < 5:
+            want = oracle_lib.render(s)
+            assert not _diff(single, want), f"canvas {i} vs oracle: {_diff(single, want)}"
+
+
 def _oracle_many(streams, variant="default"):
     """Oracle renders of many streams on the host's cores (the oracle's ctypes calls release the
     GIL, so threads render in parallel)."""
