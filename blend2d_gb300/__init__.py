@@ -133,6 +133,8 @@ _SIGNATURES = {
     "blgpu_context_fill_box_d": [_P, _D, _D, _D, _D],
     "blgpu_context_fill_polygon_d": [_P, _P, ctypes.c_size_t],
     "blgpu_context_fill_path_d": [_P, _P, _P, ctypes.c_size_t],
+    "blgpu_context_fill_path_at_d": [_P, ctypes.POINTER(ctypes.c_double), _P, _P, ctypes.c_size_t],
+    "blgpu_context_fill_path_fixed_d": [_P, _P, _P, ctypes.c_size_t],
     "blgpu_context_set_stroke_style_rgba32": [_P, _U32],
     "blgpu_context_set_stroke_style_gradient": [_P, ctypes.POINTER(Gradient)],
     "blgpu_context_set_stroke_style_pattern": [_P, ctypes.POINTER(Pattern)],
@@ -144,6 +146,7 @@ _SIGNATURES = {
     "blgpu_context_set_stroke_caps": [_P, _U32],
     "blgpu_context_set_stroke_transform_order": [_P, _U32],
     "blgpu_context_stroke_path_d": [_P, _P, _P, ctypes.c_size_t],
+    "blgpu_context_stroke_path_at_d": [_P, ctypes.POINTER(ctypes.c_double), _P, _P, ctypes.c_size_t],
     "blgpu_context_stroke_polyline_d": [_P, _P, ctypes.c_size_t],
     "blgpu_context_stroke_polygon_d": [_P, _P, ctypes.c_size_t],
     "blgpu_context_stroke_box_d": [_P, _D, _D, _D, _D],
@@ -400,12 +403,16 @@ class Context:
     def set_stroke_caps(self, cap: int): self._call("blgpu_context_set_stroke_caps", cap)
     def set_stroke_transform_order(self, order: int): self._call("blgpu_context_set_stroke_transform_order", order)
 
-    def stroke_path_d(self, cmds, xy):
+    def stroke_path_d(self, cmds, xy, origin=None):
         c = np.ascontiguousarray(cmds, dtype=np.uint8)
         a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
         if c.shape[0] != a.shape[0]:
             raise ValueError("one command per vertex")
-        self._call("blgpu_context_stroke_path_d", c.ctypes.data, a.ctypes.data, a.shape[0])
+        if origin is None:
+            self._call("blgpu_context_stroke_path_d", c.ctypes.data, a.ctypes.data, a.shape[0])
+        else:
+            self._call("blgpu_context_stroke_path_at_d", _mat(list(origin) + [0.0] * 4), c.ctypes.data,
+                       a.ctypes.data, a.shape[0])
 
     def stroke_polyline_d(self, xy):
         a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
@@ -467,12 +474,24 @@ class Context:
         a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
         self._call("blgpu_context_fill_polygon_d", a.ctypes.data, a.shape[0])
 
-    def fill_path_d(self, cmds, xy):
+    def fill_path_d(self, cmds, xy, origin=None):
         c = np.ascontiguousarray(cmds, dtype=np.uint8)
         a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
         if c.shape[0] != a.shape[0]:
             raise ValueError("one command per vertex")
-        self._call("blgpu_context_fill_path_d", c.ctypes.data, a.ctypes.data, a.shape[0])
+        if origin is None:
+            self._call("blgpu_context_fill_path_d", c.ctypes.data, a.ctypes.data, a.shape[0])
+        else:
+            self._call("blgpu_context_fill_path_at_d", _mat(list(origin) + [0.0] * 4), c.ctypes.data, a.ctypes.data,
+                       a.shape[0])
+
+    def fill_path_fixed_d(self, cmds, xy):
+        """Fills a path given in 24.8 pixel space (pixel coordinates x 256), non-zero."""
+        c = np.ascontiguousarray(cmds, dtype=np.uint8)
+        a = np.ascontiguousarray(xy, dtype=np.float64).reshape(-1, 2)
+        if c.shape[0] != a.shape[0]:
+            raise ValueError("one command per vertex")
+        self._call("blgpu_context_fill_path_fixed_d", c.ctypes.data, a.ctypes.data, a.shape[0])
 
     def submit_stream(self, stream: bytes):
         self._call("blgpu_context_submit_stream", stream, len(stream))

@@ -66,14 +66,29 @@ def _stale() -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def _object_stale(src: str) -> bool:
+    """A translation unit is recompiled when its object is older than it, than any header of the
+    package or of include/, or than this script."""
+    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    deps = [os.path.join(CSRC, src), os.path.abspath(__file__)]
+    deps += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    deps += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
 def build(jobs: int | None = None, force: bool = False) -> str:
-    """Compiles every translation unit and links libblgpu.so; returns its path."""
+    """Compiles the translation units that changed and links libblgpu.so; returns its path."""
     if not force and not _stale():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     sources = CUDA_SOURCES + HOST_SOURCES
-    with ThreadPoolExecutor(max_workers=jobs or len(sources)) as ex:
-        objs = list(ex.map(_compile, sources))
+    todo = [src for src in sources if force or _object_stale(src)]
+    with ThreadPoolExecutor(max_workers=jobs or max(1, len(todo))) as ex:
+        list(ex.map(_compile, todo))
+    objs = [os.path.join(BUILD, os.path.basename(src) + ".o") for src in sources]
     tmp = LIB + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs,
            "-Xlinker", "--no-undefined", "-lpthread", "-ldl", "-lrt"]

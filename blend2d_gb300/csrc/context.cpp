@@ -24,6 +24,7 @@
 #include "blgpu.h"
 #include "blgpu_stream.h"
 #include "frontend.h"
+#include "noalloc.h"
 #include "runtime.h"
 #include "stroke.h"
 
@@ -259,6 +260,34 @@ struct BLGpuContext {
     s.meta_xform_gen = frame->generation;
     s.meta_xform_index = uint32_t(frame->xforms.size() - 1);
     return s.meta_xform_index;
+  }
+
+  // A path drawn at an origin: the final (or, for strokes in transform order BEFORE, the meta)
+  // transform's linear part with the origin mapped by the final transform as its translation
+  // (fill_unclipped_path_with_origin, rastercontext.cpp:2813-2821; add_stroked_path_edges,
+  // rastercontextops_p.h:95-121). origin == nullptr: the registered transform as is.
+  uint32_t register_xform_at(const double* origin, bool meta) {
+    if (!origin) return meta ? register_meta_xform() : register_xform();
+    const Mat& t = s.final_fixed;
+    DevXform x{};
+    if (meta) { x.m[0] = 256.0; x.m[1] = 0.0; x.m[2] = 0.0; x.m[3] = 256.0; }
+    else { x.m[0] = t.m00; x.m[1] = t.m01; x.m[2] = t.m10; x.m[3] = t.m11; }
+    x.m[4] = origin[0] * t.m00 + origin[1] * t.m10 + t.m20;      // BLMatrix2D::map_point
+    x.m[5] = origin[0] * t.m01 + origin[1] * t.m11 + t.m21;
+    x.affine = (!meta && s.final_fixed_type > kTTScale) ? 1u : 0u;
+    frame->xforms.push_back(x);
+    return uint32_t(frame->xforms.size() - 1);
+  }
+
+  // Outlines already in the target's 24.8 space, as a font engine emits a glyph run under the
+  // final transform (add_filled_glyph_run_edges, rastercontextops_p.h:68-93: the edge builder
+  // takes them with the identity transform).
+  uint32_t register_fixed_identity_xform() {
+    DevXform x{};
+    x.m[0] = 1.0; x.m[3] = 1.0;
+    x.affine = 0u;
+    frame->xforms.push_back(x);
+    return uint32_t(frame->xforms.size() - 1);
   }
 
   DevCmd& push_cmd(uint32_t kind, uint32_t style, bool src_copy, uint32_t alpha) {
@@ -658,14 +687,27 @@ struct BLGpuContext {
     return BLGPU_SUCCESS;
   }
 
-  BLGpuResult fill_path(const uint8_t* cmds, const double* xy, size_t n) {
+  BLGpuResult fill_path(const uint8_t* cmds, const double* xy, size_t n, const double* origin = nullptr) {
     if (!bound) return BLGPU_ERROR_INVALID_STATE;
     if (n && (!xy || !cmds)) return BLGPU_ERROR_INVALID_VALUE;
     if (n > 0x3FFFFFFFu) return BLGPU_ERROR_INVALID_VALUE;
     Fill f;
     if (!resolve_fill(f)) return BLGPU_SUCCESS;
     if (n == 0) return BLGPU_SUCCESS;
-    fill_analytic(f, xy, cmds, n, s.fill_rule, register_xform());
+    fill_analytic(f, xy, cmds, n, s.fill_rule, register_xform_at(origin, false));
+    return BLGPU_SUCCESS;
+  }
+
+  // fill_unclipped_text<kSync> (rastercontext.cpp:3082-3110): glyph outlines in 24.8 space,
+  // filled non-zero with the fill style.
+  BLGpuResult fill_path_fixed(const uint8_t* cmds, const double* xy, size_t n) {
+    if (!bound) return BLGPU_ERROR_INVALID_STATE;
+    if (n && (!xy || !cmds)) return BLGPU_ERROR_INVALID_VALUE;
+    if (n > 0x3FFFFFFFu) return BLGPU_ERROR_INVALID_VALUE;
+    Fill f;
+    if (!resolve_fill(f)) return BLGPU_SUCCESS;
+    if (n == 0) return BLGPU_SUCCESS;
+    fill_analytic(f, xy, cmds, n, 0u, register_fixed_identity_xform());
     return BLGPU_SUCCESS;
   }
 
@@ -678,7 +720,7 @@ struct BLGpuContext {
   std::vector<uint8_t> stroke_in_cmds;
   std::vector<double> stroke_in_xy, stroke_poly_xy;
 
-  BLGpuResult stroke_path(const uint8_t* cmds, const double* xy, size_t n) {
+  BLGpuResult stroke_path(const uint8_t* cmds, const double* xy, size_t n, const double* origin = nullptr) {
     if (!bound) return BLGPU_ERROR_INVALID_STATE;
     if (n && (!xy || !cmds)) return BLGPU_ERROR_INVALID_VALUE;
     if (n > 0x3FFFFFFFu) return BLGPU_ERROR_INVALID_VALUE;
@@ -700,10 +742,10 @@ struct BLGpuContext {
         stroke_in_xy[2 * i + 1] = x * u.m01 + y * u.m11 + 0.0;
       }
       xy = stroke_in_xy.data();
-      xform = register_meta_xform();
+      xform = register_xform_at(origin, true);
     }
     else {
-      xform = register_xform();
+      xform = register_xform_at(origin, false);
     }
     DevCmd& c = push_cmd(kFillAnalytic, f.style, f.src_copy, f.alpha);   // non-zero
     c.geom = kGeomPath;
@@ -1336,6 +1378,11 @@ BLGPU_API BLGpuResult blgpu_context_fill_rect_d(BLGpuContext* ctx, double x, dou
 BLGPU_API BLGpuResult blgpu_context_fill_box_d(BLGpuContext* ctx, double x0, double y0, double x1, double y1) { CTX_CALL(fill_box(x0, y0, x1, y1)); }
 BLGPU_API BLGpuResult blgpu_context_fill_polygon_d(BLGpuContext* ctx, const double* xy, size_t n) { CTX_CALL(fill_polygon(xy, n)); }
 BLGPU_API BLGpuResult blgpu_context_fill_path_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n) { CTX_CALL(fill_path(cmds, xy, n)); }
+BLGPU_API BLGpuResult blgpu_context_fill_path_at_d(BLGpuContext* ctx, const double origin[2], const uint8_t* cmds, const double* xy, size_t n) {
+  if (!origin) return BLGPU_ERROR_INVALID_VALUE;
+  CTX_CALL(fill_path(cmds, xy, n, origin));
+}
+BLGPU_API BLGpuResult blgpu_context_fill_path_fixed_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n) { CTX_CALL(fill_path_fixed(cmds, xy, n)); }
 BLGPU_API BLGpuResult blgpu_context_set_stroke_style_rgba32(BLGpuContext* ctx, uint32_t c) { CTX_CALL(set_style_rgba32(c, 1)); }
 BLGPU_API BLGpuResult blgpu_context_set_stroke_style_gradient(BLGpuContext* ctx, const BLGpuGradient* g) { CTX_CALL(set_style_gradient(g, 1)); }
 BLGPU_API BLGpuResult blgpu_context_set_stroke_style_pattern(BLGpuContext* ctx, const BLGpuPattern* p) { CTX_CALL(set_style_pattern(p, 1)); }
@@ -1352,6 +1399,10 @@ BLGPU_API BLGpuResult blgpu_context_set_stroke_caps(BLGpuContext* ctx, uint32_t 
 }
 BLGPU_API BLGpuResult blgpu_context_set_stroke_transform_order(BLGpuContext* ctx, uint32_t order) { CTX_CALL(set_stroke_transform_order(order)); }
 BLGPU_API BLGpuResult blgpu_context_stroke_path_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n) { CTX_CALL(stroke_path(cmds, xy, n)); }
+BLGPU_API BLGpuResult blgpu_context_stroke_path_at_d(BLGpuContext* ctx, const double origin[2], const uint8_t* cmds, const double* xy, size_t n) {
+  if (!origin) return BLGPU_ERROR_INVALID_VALUE;
+  CTX_CALL(stroke_path(cmds, xy, n, origin));
+}
 BLGPU_API BLGpuResult blgpu_context_stroke_polyline_d(BLGpuContext* ctx, const double* xy, size_t n) { CTX_CALL(stroke_poly(xy, n, false)); }
 BLGPU_API BLGpuResult blgpu_context_stroke_polygon_d(BLGpuContext* ctx, const double* xy, size_t n) { CTX_CALL(stroke_poly(xy, n, true)); }
 BLGPU_API BLGpuResult blgpu_context_stroke_box_d(BLGpuContext* ctx, double x0, double y0, double x1, double y1) { CTX_CALL(stroke_box(x0, y0, x1, y1)); }
@@ -1486,14 +1537,14 @@ BLGPU_API BLGpuResult blgpu_render_batch(BLGpuRuntime* rt, const void* const* st
 // entirely inside the device's fixed scratch area (Runtime::run_noalloc).
 BLGPU_API BLGpuResult blgpu_render_stream_noalloc(BLGpuRuntime* rt, const void* stream, size_t size,
                                                   const BLGpuImage* device_image) {
-  static std::mutex lock;   // one scratch area per device: calls in this process take turns
   if (!rt || !stream || !device_image) return BLGPU_ERROR_INVALID_VALUE;
   const BLGpuImage& im = *device_image;
   if (!(im.flags & BLGPU_IMAGE_DEVICE_MEMORY) || im.format != BLGPU_FORMAT_PRGB32 || im.width <= 0 ||
       im.height <= 0 || im.width > 65535 || im.height > 65535 || !im.pixel_data ||
       im.stride < intptr_t(im.width) * 4 || (im.stride & 15) || (reinterpret_cast<uintptr_t>(im.pixel_data) & 15))
     return BLGPU_ERROR_INVALID_VALUE;
-  std::lock_guard<std::mutex> guard(lock);
+  // one scratch area per device: this process's calls on the device take turns
+  std::lock_guard<std::mutex> guard(noalloc_lock(rt->rt.device));
   Frame frame(false);              // plain heap memory: no page-locked allocation either
   BLGpuContext c;
   c.rt = rt;

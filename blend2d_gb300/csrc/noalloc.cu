@@ -28,4 +28,10 @@ cudaError_t noalloc_arena(int device, void** out) {
   return cudaSuccess;
 }
 
+std::mutex& noalloc_lock(int device) {
+  static std::mutex locks[kNoAllocMaxDevices];
+  static std::mutex fallback;
+  return device >= 0 && device < kNoAllocMaxDevices ? locks[device] : fallback;
+}
+
 }  // namespace blgpu

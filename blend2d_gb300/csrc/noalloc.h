@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 
+#include <mutex>
+
 namespace blgpu {
 
 // 32 MiB per device: enough for a frame of a few thousand fills on a canvas up to 2048 x 2048
@@ -13,7 +15,12 @@ constexpr size_t kNoAllocArenaBytes = size_t(32) << 20;
 constexpr int kNoAllocMaxDevices = 64;
 
 // Device address of the scratch area of `device`, which must be the current device. Looked up
-// with cudaGetSymbolAddress on the first call per device and cached.
+// with cudaGetSymbolAddress on the first call per device and cached for the life of the process
+// (a cudaDeviceReset after that first call is not supported: the cached address belongs to the
+// context the reset destroys).
 cudaError_t noalloc_arena(int device, void** out);
+
+// The lock that serializes calls of this process on `device`'s scratch area.
+std::mutex& noalloc_lock(int device);
 
 }  // namespace blgpu

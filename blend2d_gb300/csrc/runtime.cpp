@@ -862,10 +862,7 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) { r = cuda_result(e); break; }
     if (host_totals[20]) { r = BLGPU_ERROR_DATA_TOO_LARGE; break; }
-    stats.fill_commands = nc;
-    stats.segments = t.segs;
-    stats.tiles = fr.tiles;
-    stats.kernel_launches = uint64_t(launches);
+    (void)launches;               // the runtime's stats describe its own (kept) frame only
   } while (false);
   cudaStreamSynchronize(side);                 // a LUT build forked before an early exit
   restore();

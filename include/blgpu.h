@@ -178,7 +178,18 @@ BLGpuResult blgpu_context_fill_rect_i(BLGpuContext* ctx, int32_t x, int32_t y, i
 BLGpuResult blgpu_context_fill_rect_d(BLGpuContext* ctx, double x, double y, double w, double h);     /* bl_context_fill_rect_d */
 BLGpuResult blgpu_context_fill_box_d(BLGpuContext* ctx, double x0, double y0, double x1, double y1);  /* fill_geometry(BOXD) */
 BLGpuResult blgpu_context_fill_polygon_d(BLGpuContext* ctx, const double* xy, size_t n);              /* fill_geometry(POLYGOND) */
-BLGpuResult blgpu_context_fill_path_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n); /* bl_context_fill_path_d */
+BLGpuResult blgpu_context_fill_path_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n); /* bl_context_fill_path_d, origin (0, 0) */
+/* bl_context_fill_path_d with an origin (BLContextVirt::fill_path_d, context.h:477): the path is
+ * drawn with the final transform's linear part and the origin mapped by the final transform as the
+ * translation (rastercontext.cpp:2813-2821). */
+BLGpuResult blgpu_context_fill_path_at_d(BLGpuContext* ctx, const double origin[2], const uint8_t* cmds,
+                                         const double* xy, size_t n);
+/* Fills a path whose vertices are already in the target's 24.8 fixed-point pixel space (pixel
+ * coordinates x 256), with the fill style and non-zero rule: what a font engine produces for a
+ * glyph run under the context's final transform (bl_font_get_glyph_run_outlines with
+ * final_transform_fixed(origin), then the edge builder's identity transform -
+ * rastercontextops_p.h:68-93, rastercontext.cpp:3082-3110). Text fills go through it. */
+BLGpuResult blgpu_context_fill_path_fixed_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n);
 
 /* Stroking (rastercontext.cpp:2059-2165 options, :3794-3870 operations). The stroke has its own
  * style slot and alpha; the outline of the stroked geometry (pathstroke.cpp) is filled non-zero.
@@ -195,7 +206,11 @@ BLGpuResult blgpu_context_set_stroke_join(BLGpuContext* ctx, uint32_t join);    
 BLGpuResult blgpu_context_set_stroke_cap(BLGpuContext* ctx, uint32_t position, uint32_t cap); /* bl_context_set_stroke_cap */
 BLGpuResult blgpu_context_set_stroke_caps(BLGpuContext* ctx, uint32_t cap);         /* bl_context_set_stroke_caps */
 BLGpuResult blgpu_context_set_stroke_transform_order(BLGpuContext* ctx, uint32_t order); /* bl_context_set_stroke_transform_order */
-BLGpuResult blgpu_context_stroke_path_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n); /* bl_context_stroke_path_d */
+BLGpuResult blgpu_context_stroke_path_d(BLGpuContext* ctx, const uint8_t* cmds, const double* xy, size_t n); /* bl_context_stroke_path_d, origin (0, 0) */
+/* bl_context_stroke_path_d with an origin (BLContextVirt::stroke_path_d, context.h:565; origin
+ * handling in add_stroked_path_edges, rastercontextops_p.h:95-121). */
+BLGpuResult blgpu_context_stroke_path_at_d(BLGpuContext* ctx, const double origin[2], const uint8_t* cmds,
+                                           const double* xy, size_t n);
 BLGpuResult blgpu_context_stroke_polyline_d(BLGpuContext* ctx, const double* xy, size_t n);   /* stroke_geometry(POLYLINED) */
 BLGpuResult blgpu_context_stroke_polygon_d(BLGpuContext* ctx, const double* xy, size_t n);    /* stroke_geometry(POLYGOND) */
 BLGpuResult blgpu_context_stroke_box_d(BLGpuContext* ctx, double x0, double y0, double x1, double y1); /* stroke_geometry(BOXD) */
@@ -270,11 +285,15 @@ BLGpuResult blgpu_render_batch(BLGpuRuntime* rt, const void* const* streams, con
  *
  * Limit: the frame's data, LUTs, pattern images, segments and binning lists must fit in the 32 MiB
  * area (a few thousand fills on a canvas up to about 2048 x 2048); larger frames return
- * BLGPU_ERROR_DATA_TOO_LARGE and leave the image unchanged. Nothing in the area has to start at
- * zero: the call clears every counter and list it accumulates into before use. The area is shared
- * by every call on the device: calls that overlap in time (other threads or processes on the same
- * device) race on it; in one process the calls are serialized on a lock. Blocking: returns when
- * the image is written. For callers that must not allocate device memory while rendering, e.g. a
+ * BLGPU_ERROR_DATA_TOO_LARGE and leave the image unchanged. Frames with strokes return
+ * BLGPU_ERROR_NOT_IMPLEMENTED (their outline sizes come from a device pass whose buffers the area
+ * does not hold). Nothing in the area has to start at zero: the call clears every counter and
+ * list it accumulates into before use. The area exists once per device in each process (every
+ * process that loads the library holds its own 32 MiB copy on each device it uses); calls of one
+ * process on one device share it, and calls that overlapped on the GPU would race on it, so the
+ * library serializes them on a per-device lock. A cudaDeviceReset after the first call on a
+ * device is not supported (the address looked up then is cached). Blocking: returns when the
+ * image is written. For callers that must not allocate device memory while rendering, e.g. a
  * renderer running next to a job that owns the device's memory pool, or a process whose memory
  * budget is fixed up front. */
 BLGpuResult blgpu_render_stream_noalloc(BLGpuRuntime* rt, const void* stream, size_t size,

@@ -80,6 +80,18 @@ all: $(REPLAY) $(if $(filter default,$(VARIANT)),$(REFLUT) $(REFRAS))
 # The replay harness alone (what bench.py's reference arm and the GPU host's tests need).
 replay: $(REPLAY)
 
+# The BLContext binding (blend2d_gb300/blcontext) linked with this reference library and
+# libblgpu.so (built first by blend2d_gb300/build.py), with its check harness.
+BLGPU_LIB := $(HERE)../blend2d_gb300/_build
+BLCONTEXT := $(OUT)/b2d_blcontext_$(VARIANT)
+blcontext: $(BLCONTEXT)
+
+$(BLCONTEXT): $(HERE)../tests/native/blcontext_check.cpp $(HERE)../blend2d_gb300/blcontext/blgpu_blcontext.cpp \
+              $(HERE)../include/blgpu_blcontext.h $(HERE)../include/blgpu.h $(HERE)ref_stream.h $(LIB) $(BLGPU_LIB)/libblgpu.so
+	$(CXX) -std=c++17 -O2 -ffp-contract=off -DBL_STATIC -I$(REF) -I$(HERE)../include \
+	  $(HERE)../tests/native/blcontext_check.cpp $(HERE)../blend2d_gb300/blcontext/blgpu_blcontext.cpp $(LIB) \
+	  -L$(BLGPU_LIB) -lblgpu -Wl,-rpath,'$$ORIGIN/../../blend2d_gb300/_build' -lpthread -lrt -o $@
+
 $(OBJ)/%.o: $(REF)/%.cpp
 	@mkdir -p $(dir $@)
 	$(CXX) $(CXXFLAGS) $(if $(filter %pixelops/funcs.cpp,$<),$(FUNCS_DEFS),$(OPT_DEFS)) $(call isa_flags,$<) -c $< -o $@
@@ -88,7 +100,7 @@ $(LIB): $(OBJS)
 	rm -f $@
 	ar rcs $@ $(OBJS)
 
-$(REPLAY): $(HERE)ref_replay.cpp $(HERE)../include/blgpu_stream.h $(LIB)
+$(REPLAY): $(HERE)ref_replay.cpp $(HERE)ref_stream.h $(HERE)../include/blgpu_stream.h $(LIB)
 	$(CXX) -std=c++17 -O2 -ffp-contract=off -DBL_STATIC -I$(REF) -I$(HERE)../include $(HERE)ref_replay.cpp $(LIB) -lpthread -lrt -o $@
 
 $(REFLUT): $(HERE)ref_lut.cpp $(LIB)
@@ -97,4 +109,4 @@ $(REFLUT): $(HERE)ref_lut.cpp $(LIB)
 $(REFRAS): $(HERE)ref_raster.cpp $(LIB)
 	$(CXX) -std=c++17 -O2 -DBL_STATIC -DBL_BUILD_NO_JIT -I$(REF) $(HERE)ref_raster.cpp $(LIB) -lpthread -lrt -o $@
 
-.PHONY: all replay
+.PHONY: all replay blcontext

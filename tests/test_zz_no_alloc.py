@@ -57,3 +57,14 @@ def test_noalloc_rejects_host_images():
         with pytest.raises(bg.BLGpuError) as ei:
             rt.render_stream_noalloc(stream, host)
         assert ei.value.code == bg.ERROR_INVALID_VALUE
+
+
+def test_noalloc_reports_strokes_as_not_implemented():
+    """Stroke outlines are sized by a device pass whose buffers the fixed area does not hold."""
+    torch = pytest.importorskip("torch")
+    sw = scenes.strokes(seed=3, width=64, height=48, count=5)
+    out = torch.zeros((sw.height, sw.width), dtype=torch.int32, device="cuda")
+    with bg.Runtime(0) as rt:
+        with pytest.raises(bg.BLGpuError) as ei:
+            rt.render_stream_noalloc(sw.to_bytes(), out)
+        assert ei.value.code == bg.ERROR_NOT_IMPLEMENTED
