@@ -79,6 +79,11 @@ class StrokeOptions(ctypes.Structure):
                 ("start_cap", ctypes.c_uint32), ("end_cap", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
+class MemoryInfo(ctypes.Structure):
+    _fields_ = [("reserved_bytes", ctypes.c_uint64), ("last_frame_bytes", ctypes.c_uint64),
+                ("reserved", ctypes.c_uint64 * 6)]
+
+
 class LaunchConfig(ctypes.Structure):
     _fields_ = [("cover_slots", ctypes.c_int32), ("cover_blocks_per_sm", ctypes.c_int32),
                 ("fine_blocks_per_sm", ctypes.c_int32), ("edge_block", ctypes.c_int32),
@@ -105,6 +110,8 @@ _SIGNATURES = {
     "blgpu_runtime_destroy": [_P],
     "blgpu_runtime_get_stats": [_P, ctypes.POINTER(Stats)],
     "blgpu_runtime_replay": [_P, ctypes.c_int],
+    "blgpu_runtime_get_memory": [_P, ctypes.POINTER(MemoryInfo)],
+    "blgpu_runtime_release_memory": [_P],
     "blgpu_runtime_synchronize": [_P],
     "blgpu_runtime_get_launch_config": [_P, ctypes.POINTER(LaunchConfig)],
     "blgpu_runtime_set_launch_config": [_P, ctypes.POINTER(LaunchConfig)],
@@ -259,6 +266,16 @@ class Runtime:
         s = Stats()
         _check(self._lib.blgpu_runtime_get_stats(self.handle, ctypes.byref(s)), "blgpu_runtime_get_stats")
         return s
+
+    def memory(self) -> MemoryInfo:
+        """Device bytes the runtime's arenas hold, and what its last frame used."""
+        m = MemoryInfo()
+        _check(self._lib.blgpu_runtime_get_memory(self.handle, ctypes.byref(m)), "blgpu_runtime_get_memory")
+        return m
+
+    def release_memory(self):
+        """Frees the runtime's device arenas (the next frame allocates again)."""
+        _check(self._lib.blgpu_runtime_release_memory(self.handle), "blgpu_runtime_release_memory", self.handle)
 
     def replay(self, use_graph: bool = True):
         _check(self._lib.blgpu_runtime_replay(self.handle, int(use_graph)), "blgpu_runtime_replay")

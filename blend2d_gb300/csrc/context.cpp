@@ -1261,6 +1261,21 @@ BLGPU_API BLGpuResult blgpu_runtime_get_stats(const BLGpuRuntime* rt, BLGpuStats
   return BLGPU_SUCCESS;
 }
 
+BLGPU_API BLGpuResult blgpu_runtime_get_memory(const BLGpuRuntime* rt, BLGpuMemoryInfo* out) {
+  if (!rt || !out) return BLGPU_ERROR_INVALID_VALUE;
+  std::lock_guard<std::mutex> e(const_cast<BLGpuRuntime*>(rt)->exec);
+  *out = BLGpuMemoryInfo{};
+  out->reserved_bytes = rt->rt.reserved_bytes();
+  out->last_frame_bytes = rt->rt.last_frame_bytes;
+  return BLGPU_SUCCESS;
+}
+
+BLGPU_API BLGpuResult blgpu_runtime_release_memory(BLGpuRuntime* rt) {
+  if (!rt) return BLGPU_ERROR_INVALID_VALUE;
+  std::lock_guard<std::mutex> e(rt->exec);
+  return rt->rt.release_memory();
+}
+
 BLGPU_API BLGpuResult blgpu_runtime_replay(BLGpuRuntime* rt, int use_graph) {
   if (!rt) return BLGPU_ERROR_INVALID_VALUE;
   std::lock_guard<std::mutex> e(rt->exec);

@@ -336,6 +336,7 @@ BLGpuResult Runtime::prepare_strokes(const Frame& fr, FrameView& v, uint32_t& ou
   };
   Layout measure;
   plan(measure);
+  stroke_bytes = measure.off;
   if (measure.off > stroke_buf.size) {
     graph_valid = false;
     BLGPU_CHECK(cudaStreamSynchronize(stream));
@@ -374,6 +375,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   FrameView v{};
   uint32_t outline_verts = 0;
   strokes_counted = false;
+  stroke_bytes = 0;
   BLGpuResult sr = prepare_strokes(fr, v, outline_verts);
   if (sr) return sr;
   const size_t vert_words = fr.verts.size() + 2 * size_t(outline_verts);   // doubles
@@ -441,6 +443,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   Layout measure;
   plan(measure, v, nullptr);
   size_t total = measure.off;
+  in_bytes = total;
   if (total > in_buf.size) {
     graph_valid = false;
     BLGPU_CHECK(cudaStreamSynchronize(stream));
@@ -696,6 +699,7 @@ BLGpuResult Runtime::run(const Frame& fr) {
   Layout L;
   L.base = static_cast<char*>(dyn_buf.ptr);
   plan_dynamic(L, view, totals);
+  last_frame_bytes = in_bytes + stroke_bytes + measure.off + uint64_t(totals.segs) * (sizeof(DevSeg) + sizeof(uint32_t));
 
   launches += enqueue_render_half(stream, true);
   BLGPU_CHECK(cudaGetLastError());
@@ -985,6 +989,23 @@ BLGpuResult Runtime::autotune(int trials, LaunchConfig* best_out, double* best_m
   if (best_out) *best_out = best;
   if (best_ms_out) *best_ms_out = best_ms;
   return r;
+}
+
+BLGpuResult Runtime::release_memory() {
+  BLGPU_CHECK(cudaSetDevice(device));
+  BLGPU_CHECK(cudaStreamSynchronize(stream));
+  BLGPU_CHECK(cudaStreamSynchronize(side));
+  if (graph) cudaGraphExecDestroy(graph);
+  graph = nullptr;
+  graph_valid = false;
+  has_frame = false;
+  pending_timing = 0;
+  in_buf.release();
+  dyn_buf.release();
+  seg_buf.release();
+  stroke_buf.release();
+  seg_capacity = 0;
+  return BLGPU_SUCCESS;
 }
 
 BLGpuResult Runtime::synchronize() {

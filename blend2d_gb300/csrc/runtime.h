@@ -191,6 +191,9 @@ struct Runtime {
   bool has_frame = false;
   int pending_timing = 0;   // 1: graph replay timed, 2: eager replay timed (incl. fine kernel)
   uint64_t h2d_bytes = 0, d2h_bytes = 0;
+  uint64_t in_bytes = 0, stroke_bytes = 0;   // the last frame's planned input / stroke arena bytes
+  uint64_t last_frame_bytes = 0;             // ... and everything it used on the device
+  uint64_t reserved_bytes() const { return uint64_t(in_buf.size) + dyn_buf.size + seg_buf.size + stroke_buf.size; }
 
   BLGpuStats stats{};
   LaunchConfig cfg;
@@ -201,6 +204,8 @@ struct Runtime {
   BLGpuResult run(const Frame& fr);
   BLGpuResult replay(bool use_graph);
   BLGpuResult synchronize();
+  // Frees the device arenas (the kept frame is dropped).
+  BLGpuResult release_memory();
   // Picks the fastest launch shapes for the last frame (its pixels are left unchanged).
   BLGpuResult autotune(int trials, LaunchConfig* best, double* best_ms);
   // Renders a one-canvas frame into its device-memory image using only the fixed device scratch

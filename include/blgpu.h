@@ -139,6 +139,18 @@ BLGpuResult blgpu_runtime_create(BLGpuRuntime** out, const BLGpuRuntimeCreateInf
  * runtime's in-flight frames. */
 BLGpuResult blgpu_runtime_destroy(BLGpuRuntime* rt);
 BLGpuResult blgpu_runtime_get_stats(const BLGpuRuntime* rt, BLGpuStats* out);
+
+/* Device memory of a runtime (no counterpart in the reference, which renders in host memory). */
+typedef struct BLGpuMemoryInfo {
+  uint64_t reserved_bytes;   /* device memory the runtime's arenas hold now (kept across frames) */
+  uint64_t last_frame_bytes; /* device memory the last frame used: inputs, canvases, work arrays,
+                                segments and binning lists */
+  uint64_t reserved[6];
+} BLGpuMemoryInfo;
+BLGpuResult blgpu_runtime_get_memory(const BLGpuRuntime* rt, BLGpuMemoryInfo* out);
+/* Frees the runtime's device arenas (the next frame allocates what it needs again; the last frame
+ * can no longer be replayed). For servers that share a device-memory budget between runtimes. */
+BLGpuResult blgpu_runtime_release_memory(BLGpuRuntime* rt);
 /* Re-runs the device pipeline of the last flushed frame on its device-resident inputs (no
  * host<->device traffic); `use_graph` replays it as a captured CUDA graph. */
 BLGpuResult blgpu_runtime_replay(BLGpuRuntime* rt, int use_graph);

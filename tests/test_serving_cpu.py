@@ -124,3 +124,47 @@ def test_runtime_close_closes_its_contexts_first():
     rt.close()
     assert rt._lib.calls == [("ctx", 2), ("rt", 1)]
     assert ctx.handle is None and rt.handle is None
+
+
+class HoldingRuntime(FakeRuntime):
+    """A fake whose arenas keep what its largest batch needed, like a device runtime's."""
+
+    def __init__(self, per_request):
+        super().__init__(0.005)
+        self.per_request = per_request
+        self.held = 0
+        self.released = 0
+
+    def render_batch(self, streams, targets):
+        super().render_batch(streams, targets)
+        self.held = max(self.held, self.per_request * len(streams))
+
+    def memory(self):
+        class M:
+            pass
+        m = M()
+        m.reserved_bytes, m.last_frame_bytes = self.held, self.held
+        return m
+
+    def release_memory(self):
+        self.held = 0
+        self.released += 1
+
+
+def test_admission_charges_what_runtimes_hold_and_releases_idle_arenas():
+    """Workers keep their arenas between batches; the server charges what they hold, and when the
+    holdings leave no room for the next request, idle workers give their arenas back instead of
+    the queue stalling."""
+    streams = _streams(30)
+    per = max(footprint_bytes(s) for s in streams)
+    rts = []
+
+    def factory():
+        rts.append(HoldingRuntime(per))
+        return rts[-1]
+
+    with RenderServer(workers=3, max_batch=2, hbm_budget=4 * per, runtime_factory=factory) as srv:
+        outs = [f.result(timeout=20) for f in [srv.submit(s) for s in streams]]
+    assert len(outs) == 30 and srv.stats.completed == 30
+    assert srv.stats.max_inflight_bytes <= 4 * per
+    assert srv.stats.releases >= 1 and sum(r.released for r in rts) == srv.stats.releases
