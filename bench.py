@@ -69,6 +69,11 @@ L2_FLUSH_BYTES = 256 << 20
 DTYPE = "u8x4 (PRGB32); fp64 edges"
 
 
+def log(msg: str) -> None:
+    """Progress on stderr (the JSON line is the only stdout output)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -447,10 +452,12 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
     t_gen = time.perf_counter()
     streams = batch_streams(n)
     gen_s = time.perf_counter() - t_gen
+    log(f"batch: {n} canvases generated in {gen_s:.1f} s")
     shapes = [tuple(int(v) for v in np.frombuffer(s[8:16], dtype="<u4"))[::-1] for s in streams]   # (h, w)
     s = torch.cuda.Stream()
     rt = bg.Runtime(local, cuda_stream=s.cuda_stream)
     targets = [pinned_canvas(h, w) for h, w in shapes]
+    log("batch: pinned canvases allocated")
 
     # ---- e2e through the public API: host streams, pinned host canvases, one pipeline per step
     for _ in range(args.warmup):
@@ -462,6 +469,7 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
         rt.render_batch(streams, targets)
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e_clocks = clocks.stop()
+    log(f"batch: e2e {e2e_s * 1e3 / args.steps:.1f} ms/step")
     st = rt.stats()
     h2d, d2h = int(st.h2d_bytes), int(st.d2h_bytes)
     batch_dev_ms = float(st.last_gpu_ms)
@@ -471,6 +479,7 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
     dist.barrier()
     total_s = dist.max(sum(step_ms) / 1e3)
     st_culled = rt.stats()
+    log(f"batch: device {total_s * 1e3 / args.steps:.1f} ms/step")
     g_ms = graph_replay_ms(rt, s, 3)
     st_ref = reference_op_counts(rt, bg)
     roof = roofline(st_culled, st_ref, statistics.mean(fine_ms), statistics.mean(comp_ms), "batch")
@@ -487,6 +496,7 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
         dev_sum += rt.stats().last_gpu_ms
     single_s = time.perf_counter() - t0
     single_clocks = clocks.stop()
+    log(f"batch: per-canvas pass {single_s:.1f} s")
     mismatched = [i for i, (a, t) in enumerate(zip(batched, targets)) if not np.array_equal(a, t.numpy().view(np.uint32))]
 
     # ---- parity of a 64-canvas sample against the oracle (and the golden reference hashes)
@@ -504,6 +514,7 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
                 bad_px += d
                 bad.append(f"canvas {i}: oracle")
     rt.close()
+    log(f"batch: parity checked ({len(bad)} findings)")
 
     rec = {
         "metric": "Mpix/s", "value": round(world * args.steps * mpix / total_s, 3), "unit": "Mpix/s",
@@ -647,6 +658,7 @@ def frame_record(args, dist, local, workload: str, cpu: bool) -> dict:
         reps = max(1, min(64, int(args.cpu_seconds / max(one, 1e-3))))
         rec["cpu_baseline"] = cpu_baseline([stream] * reps, mpix * reps, f"{reps} full frames of the same workload")
     rec["parity"] = parity_text(bad_px, bad)
+    log(f"frame {workload}: done")
     return rec
 
 
@@ -666,6 +678,7 @@ def serving_record(args, local) -> dict:
     with RenderServer(workers=args.serve_workers, hbm_budget=150 << 30, device=local) as srv:
         for f in [srv.submit(r) for r in reqs[:2 * args.serve_workers]]:     # warm-up: device arenas grow
             f.result()
+        log("serving: warmed up")
         for rate in [float(x) for x in args.serve_rates.split(",")]:
             rng = random.Random(int(rate))
             srv.stats.latencies.clear()

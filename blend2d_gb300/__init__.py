@@ -88,7 +88,8 @@ class LaunchConfig(ctypes.Structure):
     _fields_ = [("cover_slots", ctypes.c_int32), ("cover_blocks_per_sm", ctypes.c_int32),
                 ("fine_blocks_per_sm", ctypes.c_int32), ("edge_block", ctypes.c_int32),
                 ("cubic_blocks_per_sm", ctypes.c_int32), ("no_occlusion_cull", ctypes.c_int32),
-                ("max_segments", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
+                ("max_segments", ctypes.c_int32), ("graph_frames", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -99,7 +100,8 @@ class Stats(ctypes.Structure):
                 ("tiles", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("last_gpu_ms", ctypes.c_double),
                 ("last_fine_ms", ctypes.c_double), ("pixel_ops", ctypes.c_uint64), ("pattern_ops", ctypes.c_uint64),
                 ("input_vertices", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
-                ("last_cuda_error", ctypes.c_int64), ("last_composite_ms", ctypes.c_double)]
+                ("last_cuda_error", ctypes.c_int64), ("last_composite_ms", ctypes.c_double),
+                ("graph_frames", ctypes.c_uint64)]
 
 
 _P = ctypes.c_void_p

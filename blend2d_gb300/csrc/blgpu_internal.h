@@ -48,8 +48,14 @@ enum ErrorFlag : uint32_t {
   kErrPieces = 2u,       // monotonic curve pieces (bound: 3 per curve vertex)
   kErrSeglist = 4u,      // coverage work items (sized by the binning count pass)
   kErrMasks = 8u,        // slot masks (sized by the binning count pass)
-  kErrSegments = 16u     // segments (the segment array is grown and the frame re-run)
+  kErrSegments = 16u,    // segments (the segment array is grown and the frame re-run)
+  kErrCapacity = 32u     // a work array sized by capacity (graph frames) is too small: the render
+                         // half was skipped
 };
+
+// FrameView::work_counter[kSkipWord] != 0: the binning and composite passes do nothing (their
+// inputs would not fit the arrays they write; set by frame_gate_kernel).
+constexpr int kSkipWord = 27;
 
 enum FetchKind : uint32_t {
   kFetchSolid = 0,
@@ -213,8 +219,19 @@ struct DevStrokeParams {
   uint32_t join, start_cap, end_cap, pad;
 };
 
-// Device-side view of a frame (pointers into one device arena).
+// The frame's sizes in device memory (FrameView::counts), uploaded with its data: kernels read
+// them there, so launches sized by capacities serve any frame that fits (a captured CUDA graph can
+// render new frames).
+enum CountIndex : uint32_t {
+  kCntCmds = 0, kCntCanvases = 1, kCntTiles = 2, kCntRows = 3, kCntLutJobs = 4, kCntStrokeFigs = 5,
+  kCntStrokeVertBase = 6, kCntWords = 8
+};
+
+// Device-side view of a frame (pointers into one device arena). The num_* fields are the
+// capacities the arrays are sized by (the frame's own sizes in an eager run): launches are sized by
+// them, and kernels take the actual sizes from `counts` and from the device totals.
 struct FrameView {
+  const uint32_t* counts;      // [kCntWords] CountIndex
   const DevCmd* cmds;
   DevCmd* cmds_rw;
   const DevStyle* styles;
@@ -297,6 +314,7 @@ struct FrameView {
   uint32_t num_seglist;
   uint32_t num_row_states;
   uint32_t num_row_runs;       // conic row runs (sum of rb_count)
+  uint32_t num_row_entries;    // row list entries (sum of row_counts)
 };
 
 }  // namespace blgpu

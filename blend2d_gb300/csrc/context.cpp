@@ -1258,6 +1258,7 @@ BLGPU_API BLGpuResult blgpu_runtime_get_stats(const BLGpuRuntime* rt, BLGpuStats
   std::lock_guard<std::mutex> e(const_cast<BLGpuRuntime*>(rt)->exec);
   *out = rt->rt.stats;
   out->last_cuda_error = last_cuda_error();
+  out->graph_frames = rt->rt.graph_frames_run;
   return BLGPU_SUCCESS;
 }
 
@@ -1297,6 +1298,7 @@ static void to_abi(const LaunchConfig& c, BLGpuLaunchConfig* out) {
   out->cubic_blocks_per_sm = c.cubic_blocks_per_sm;
   out->no_occlusion_cull = c.no_occlusion_cull;
   out->max_segments = c.max_segments;
+  out->graph_frames = c.graph_frames;
 }
 
 BLGPU_API BLGpuResult blgpu_runtime_get_launch_config(const BLGpuRuntime* rt, BLGpuLaunchConfig* out) {
@@ -1311,7 +1313,8 @@ BLGPU_API BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BL
   if ((c->cover_slots != 0 && c->cover_slots != 16 && c->cover_slots != 32 && c->cover_slots != 64) ||
       (c->edge_block != 64 && c->edge_block != 128 && c->edge_block != 256) ||
       c->cover_blocks_per_sm < 0 || c->fine_blocks_per_sm < 0 || c->cubic_blocks_per_sm < 0 ||
-      (c->no_occlusion_cull != 0 && c->no_occlusion_cull != 1) || c->max_segments < 0)
+      (c->no_occlusion_cull != 0 && c->no_occlusion_cull != 1) || c->max_segments < 0 ||
+      (c->graph_frames != 0 && c->graph_frames != 1))
     return BLGPU_ERROR_INVALID_VALUE;
   LaunchConfig lc;
   lc.cover_slots = c->cover_slots;
@@ -1321,6 +1324,7 @@ BLGPU_API BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BL
   lc.cubic_blocks_per_sm = c->cubic_blocks_per_sm;
   lc.no_occlusion_cull = c->no_occlusion_cull;
   lc.max_segments = c->max_segments;
+  lc.graph_frames = c->graph_frames;
   std::lock_guard<std::mutex> e(rt->exec);
   rt->rt.cfg = lc;
   rt->rt.graph_valid = false;

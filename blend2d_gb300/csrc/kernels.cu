@@ -240,7 +240,8 @@ __device__ void lut_build64(const DevLutJob& job, const DevStop* s, uint64_t* lu
 constexpr int kLutWarps = 8;
 
 __global__ void __launch_bounds__(32 * kLutWarps) lut_kernel(const DevLutJob* jobs, const DevStop* stops, uint32_t* luts,
-                                                             uint32_t num_jobs) {
+                                                             const uint32_t* counts) {
+  const uint32_t num_jobs = counts[kCntLutJobs];
   __shared__ LutSpan spans_all[kLutWarps][32];
   __shared__ LutSpan64 spans64_all[kLutWarps][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -377,7 +378,7 @@ __device__ void for_each_item(const uint8_t* cmd, int n, Fn&& fn) {
 
 __global__ void classify_kernel(FrameView f) {
   uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= f.num_cmds) return;
+  if (c >= f.counts[kCntCmds]) return;
   const DevCmd cmd = f.cmds[c];
   if (cmd.kind != kFillAnalytic) return;
   f.cmd_bbox[c] = make_int4(INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN);
@@ -703,10 +704,29 @@ __global__ void scan_add_kernel(uint32_t* out, const uint32_t* block_offsets, ui
 // K2 - binning
 // ---------------------------------------------------------------------------------------------
 
+// Between the halves: the sizes the counting half produced must fit the arrays the rendering half
+// writes (they always do in an eager run, whose arrays are sized from them; a graph frame's are
+// sized by capacities). Otherwise the rendering half is skipped and the host re-runs the frame.
+__global__ void frame_gate_kernel(FrameView f) {
+  const uint32_t* t = f.totals;
+  const bool over = t[0] > min(f.seg_capacity, f.num_segs) || t[1] > f.num_seglist || t[2] > f.num_cmdrows ||
+                    t[3] > f.num_row_entries || t[4] > f.num_row_states || t[6] > f.num_row_runs;
+  if (over) {
+    f.work_counter[kSkipWord] = 1u;
+    atomicOr(f.error_flags, kErrCapacity);
+  }
+}
+
+__device__ __forceinline__ bool frame_skipped(const FrameView& f) { return f.work_counter[kSkipWord] != 0u; }
+
 // Tile ranges of every command (empty commands get 0xFFFFFFFF) and its number of tile rows.
 __global__ void cmd_tiles_kernel(FrameView f, uint32_t* cmdrow_counts_per_cmd, uint32_t* row_counts) {
   uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= f.num_cmds) return;
+  if (c >= f.counts[kCntCmds]) {
+    // entries beyond the frame's commands (up to the capacity the scans run over) count nothing
+    if (c < f.num_cmds) { cmdrow_counts_per_cmd[c] = 0; f.rs_count[c] = 0; f.rb_count[c] = 0; }
+    return;
+  }
   const DevCmd cmd = f.cmds[c];
   const DevCanvas cv = f.canvases[cmd.canvas];
   int x0, y0, x1, y1;   // inclusive pixel range
@@ -768,10 +788,11 @@ __global__ void cmd_tiles_kernel(FrameView f, uint32_t* cmdrow_counts_per_cmd, u
 // (segment, mask index) work items, grouped by slot in slot order, so the items of consecutive
 // slots with segments are contiguous.
 __global__ void __launch_bounds__(256) seg_bin_kernel(FrameView f, int scatter) {
+  if (frame_skipped(f)) return;
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   // the segments the edge builders emitted must all have found a place in the segment array
   if (s == 0 && !scatter && f.totals[0] > f.seg_capacity) atomicOr(f.error_flags, kErrSegments);
-  if (s >= f.num_segs) return;
+  if (s >= min(f.totals[0], min(f.seg_capacity, f.num_segs))) return;
   const uint32_t c = f.seg_meta[s] >> 1;
   const uint32_t ctx = f.cmd_tile_x[c];
   if (ctx == 0xFFFFFFFFu) return;
@@ -813,15 +834,20 @@ __global__ void __launch_bounds__(256) seg_bin_kernel(FrameView f, int scatter) 
 }
 
 // Slots with segments get a compact mask index: flags for the scan ...
+// Slots of the frame: the binning count from the device totals, within the arrays' capacity.
+__device__ __forceinline__ uint32_t frame_slots(const FrameView& f) { return min(f.totals[2], f.num_cmdrows); }
+
 __global__ void slot_flags_kernel(FrameView f) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < f.num_cmdrows) f.cmdrow_offsets[i] = f.cmdrow_counts[i] ? 1u : 0u;
+  if (i < f.num_cmdrows) f.cmdrow_offsets[i] = (i < frame_slots(f) && f.cmdrow_counts[i]) ? 1u : 0u;
 }
 
 // ... and, after the scan, the maps between slots and mask indices.
 __global__ void slot_compact_kernel(FrameView f) {
+  if (frame_skipped(f)) return;
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= f.num_cmdrows) return;
+  const uint32_t n = frame_slots(f);
+  if (i >= n) return;
   if (f.cmdrow_counts[i]) {
     const uint32_t idx = f.cmdrow_offsets[i];
     f.slot_mask[i] = idx + 1u;
@@ -838,12 +864,14 @@ __global__ void slot_compact_kernel(FrameView f) {
   else {
     f.slot_mask[i] = 0u;
   }
-  if (i == f.num_cmdrows - 1) f.totals[5] = f.cmdrow_offsets[i] + (f.cmdrow_counts[i] ? 1u : 0u);
+  if (i == n - 1) f.totals[5] = f.cmdrow_offsets[i] + (f.cmdrow_counts[i] ? 1u : 0u);
 }
 
 // Prefix of the backdrop deltas over the tile columns of every (command, strip row, row).
 __global__ void backdrop_prefix_kernel(FrameView f) {
+  if (frame_skipped(f)) return;
   uint32_t c = blockIdx.x;
+  if (c >= f.counts[kCntCmds]) return;
   uint32_t ctx = f.cmd_tile_x[c];
   if (ctx == 0xFFFFFFFFu || f.cmds[c].kind != kFillAnalytic) return;
   const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
@@ -858,6 +886,11 @@ __global__ void backdrop_prefix_kernel(FrameView f) {
   }
 }
 
+int launch_frame_gate(const FrameView& f, cudaStream_t st) {
+  frame_gate_kernel<<<1, 1, 0, st>>>(f);
+  return 1;
+}
+
 int launch_backdrop_prefix(const FrameView& f, cudaStream_t st) {
   if (!f.num_cmds || !f.num_cmdrows) return 0;
   backdrop_prefix_kernel<<<f.num_cmds, 64, 0, st>>>(f);
@@ -868,6 +901,7 @@ int launch_backdrop_prefix(const FrameView& f, cudaStream_t st) {
 __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
   __shared__ uint32_t smem[32];
   uint32_t row = blockIdx.x;
+  if (row >= f.counts[kCntRows] || frame_skipped(f)) return;        // whole blocks leave together
   const DevCanvas cv = f.canvases[row_canvas[row]];
   uint32_t r = row - cv.row_base;
   uint32_t out = f.row_offsets[row];
@@ -923,6 +957,7 @@ __global__ void __launch_bounds__(4 * K) coverage_kernel(FrameView f) {
   __shared__ uint2 items[kCoverChunk];
   __shared__ uint32_t kcount[5], kbase[5];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (frame_skipped(f)) return;
   const uint32_t num_masks = min(f.totals[5], f.mask_capacity);
   if (blockIdx.x == 0 && tid == 0 && f.totals[5] > f.mask_capacity) atomicOr(f.error_flags, kErrMasks);
   const uint32_t groups = (num_masks + K - 1) / K;
@@ -1079,7 +1114,8 @@ __global__ void __launch_bounds__(kFineThreads) cull_kernel(FrameView f) {
   const int lane = threadIdx.x & 31;
   const int prow = lane >> 3;
   const int pcol = (lane & 7) * 4;
-  const uint32_t num_units = f.num_tiles * kStripsPerTile;
+  if (frame_skipped(f)) return;
+  const uint32_t num_units = f.counts[kCntTiles] * kStripsPerTile;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t unit = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); unit < num_units; unit += warps) {
     const uint32_t tile = f.tile_order[unit / kStripsPerTile];
@@ -1148,7 +1184,8 @@ __global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
   const int prow = lane >> 3;            // row within the strip
   const int pcol = (lane & 7) * 4;       // first of this lane's 4 columns
   uint32_t ops = 0, pat_ops = 0;         // composited pixels of this lane (all strips)
-  const uint32_t num_units = f.num_tiles * kStripsPerTile;
+  if (frame_skipped(f)) return;
+  const uint32_t num_units = f.counts[kCntTiles] * kStripsPerTile;
 
   for (;;) {
     uint32_t unit = 0;
@@ -1320,10 +1357,12 @@ __global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
 }
 
 // Gradient row states: one thread per (command, row) of every radial/conic command's bbox.
-__global__ void row_state_kernel(FrameView f, uint32_t total) {
+__global__ void row_state_kernel(FrameView f) {
+  if (frame_skipped(f)) return;
+  const uint32_t total = min(f.totals[4], f.num_row_states);
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= total) return;
-  uint32_t lo = 0, hi = f.num_cmds - 1;       // last command whose first row state is <= t
+  uint32_t lo = 0, hi = f.counts[kCntCmds] - 1;       // last command whose first row state is <= t
   while (lo < hi) { uint32_t mid = (lo + hi + 1) >> 1; if (f.rs_base[mid] <= t) lo = mid; else hi = mid - 1; }
   const uint32_t c = lo;
   const DevCmd& cmd = f.cmds[c];
@@ -1340,10 +1379,12 @@ __global__ void row_state_kernel(FrameView f, uint32_t total) {
 // Conic row values, one thread per run of rows sharing a fetcher start: the reference steps the
 // fetcher's FP64 position row by row from there, so a run is one sequential chain (a thread per
 // row would repeat the chain's prefix in every row; the FP64 pipe is the scarce one).
-__global__ void conic_rows_kernel(FrameView f, uint32_t total) {
+__global__ void conic_rows_kernel(FrameView f) {
+  if (frame_skipped(f)) return;
+  const uint32_t total = min(f.totals[6], f.num_row_runs);
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= total) return;
-  uint32_t lo = 0, hi = f.num_cmds - 1;       // last command whose first run is <= t
+  uint32_t lo = 0, hi = f.counts[kCntCmds] - 1;       // last command whose first run is <= t
   while (lo < hi) { uint32_t mid = (lo + hi + 1) >> 1; if (f.rb_base[mid] <= t) lo = mid; else hi = mid - 1; }
   const uint32_t c = lo;
   const DevCmd& cmd = f.cmds[c];
@@ -1372,15 +1413,16 @@ __global__ void conic_rows_kernel(FrameView f, uint32_t total) {
 // Tile/row bookkeeping: canvas of every global tile and tile row, identity processing order.
 __global__ void tile_setup_kernel(FrameView f, uint32_t* row_canvas) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t num_canvases = f.counts[kCntCanvases];
   // binary search the canvas owning tile i / row i
-  if (i < f.num_tiles) {
-    uint32_t lo = 0, hi = f.num_canvases - 1;
+  if (i < f.counts[kCntTiles]) {
+    uint32_t lo = 0, hi = num_canvases - 1;
     while (lo < hi) { uint32_t mid = (lo + hi + 1) >> 1; if (f.canvases[mid].tile_base <= i) lo = mid; else hi = mid - 1; }
     f.tile_canvas[i] = lo;
     f.tile_order[i] = i;
   }
-  if (i < f.num_rows) {
-    uint32_t lo = 0, hi = f.num_canvases - 1;
+  if (i < f.counts[kCntRows]) {
+    uint32_t lo = 0, hi = num_canvases - 1;
     while (lo < hi) { uint32_t mid = (lo + hi + 1) >> 1; if (f.canvases[mid].row_base <= i) lo = mid; else hi = mid - 1; }
     row_canvas[i] = lo;
   }
@@ -1448,7 +1490,7 @@ int launch_total(const uint32_t* counts, const uint32_t* offsets, uint32_t n, ui
 
 int launch_lut(const FrameView& f, cudaStream_t st) {
   if (!f.num_lut_jobs) return 0;
-  lut_kernel<<<cdiv(f.num_lut_jobs, kLutWarps), 32 * kLutWarps, 0, st>>>(f.lut_jobs, f.stops, f.luts, f.num_lut_jobs);
+  lut_kernel<<<cdiv(f.num_lut_jobs, kLutWarps), 32 * kLutWarps, 0, st>>>(f.lut_jobs, f.stops, f.luts, f.counts);
   return 1;
 }
 
@@ -1538,9 +1580,9 @@ int launch_coverage(const FrameView& f, const LaunchConfig& cfg, uint32_t* scan_
 
 int launch_row_states(const FrameView& f, cudaStream_t st) {
   if (!f.num_row_states) return 0;
-  row_state_kernel<<<cdiv(f.num_row_states, 128), 128, 0, st>>>(f, f.num_row_states);
+  row_state_kernel<<<cdiv(f.num_row_states, 128), 128, 0, st>>>(f);
   if (!f.num_row_runs) return 1;
-  conic_rows_kernel<<<cdiv(f.num_row_runs, 64), 64, 0, st>>>(f, f.num_row_runs);
+  conic_rows_kernel<<<cdiv(f.num_row_runs, 64), 64, 0, st>>>(f);
   return 2;
 }
 

@@ -18,6 +18,7 @@ struct LaunchConfig {
   int cubic_blocks_per_sm = 3;    // lane-scheduled curve-piece flattener: blocks per SM (0 = as many as fit)
   int no_occlusion_cull = 0;      // 1: the composite starts every strip at its first command
   int max_segments = 0;           // > 0: cap of the segment array (frames needing more fail)
+  int graph_frames = 0;           // 1: frames run as a captured graph over capacity-sized arrays
 };
 
 int exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* tmp, cudaStream_t st);
@@ -33,6 +34,7 @@ int launch_rows_and_tiles(const FrameView& f, uint32_t* row_canvas, cudaStream_t
 int launch_fine(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st);
 int launch_row_states(const FrameView& f, cudaStream_t st);
 int launch_backdrop_prefix(const FrameView& f, cudaStream_t st);
+int launch_frame_gate(const FrameView& f, cudaStream_t st);
 int launch_coverage(const FrameView& f, const LaunchConfig& cfg, uint32_t* scan_tmp, cudaStream_t st);
 int fine_grid_size(int blocks_per_sm);
 // Stroking: per-figure outline sizes and their exclusive scan (stroke_offsets), then the outlines.

@@ -270,6 +270,8 @@ BLGpuResult Runtime::init(const BLGpuRuntimeCreateInfo* info) {
   BLGPU_CHECK(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
   BLGPU_CHECK(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
   BLGPU_CHECK(cudaMallocHost(reinterpret_cast<void**>(&host_totals), 128));
+  BLGPU_CHECK(cudaMallocHost(reinterpret_cast<void**>(&host_counts), sizeof(uint32_t) * kCntWords));
+  BLGPU_CHECK(cudaMalloc(reinterpret_cast<void**>(&counts_dev), sizeof(uint32_t) * kCntWords));
   return BLGPU_SUCCESS;
 }
 
@@ -288,11 +290,14 @@ void Runtime::destroy() {
   seg_buf.release();
   if (host_staging) cudaFreeHost(host_staging);
   if (host_totals) cudaFreeHost(host_totals);
+  if (host_counts) cudaFreeHost(host_counts);
+  if (counts_dev) cudaFree(counts_dev);
+  host_totals = host_counts = counts_dev = nullptr;
   if (own_stream && stream) cudaStreamDestroy(stream);
   stream = nullptr;
 }
 
-static bool device_target_direct(const BLGpuImage& im) {
+bool device_target_direct(const BLGpuImage& im) {
   return (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) && (reinterpret_cast<uintptr_t>(im.pixel_data) & 15u) == 0 &&
          (im.stride & 15) == 0 && im.stride >= intptr_t(im.width) * 4;
 }
@@ -366,47 +371,88 @@ BLGpuResult Runtime::prepare_strokes(const Frame& fr, FrameView& v, uint32_t& ou
   return BLGPU_SUCCESS;
 }
 
-BLGpuResult Runtime::upload(const Frame& fr) {
-  const uint32_t nc = uint32_t(fr.cmds.size());
+cudaError_t Runtime::put_counts(const Frame& fr, uint32_t* dev) {
+  uint32_t* c = host_counts;
+  memset(c, 0, sizeof(uint32_t) * kCntWords);
+  c[kCntCmds] = uint32_t(fr.cmds.size());
+  c[kCntCanvases] = uint32_t(fr.canvases.size());
+  c[kCntTiles] = fr.tiles;
+  c[kCntRows] = fr.rows;
+  c[kCntLutJobs] = uint32_t(fr.lut_jobs.size());
+  c[kCntStrokeFigs] = uint32_t(fr.stroke_figs.size());
+  c[kCntStrokeVertBase] = uint32_t(fr.verts.size() / 2);
+  h2d_bytes += sizeof(uint32_t) * kCntWords;
+  return cudaMemcpyAsync(dev, c, sizeof(uint32_t) * kCntWords, cudaMemcpyHostToDevice, stream);
+}
+
+FrameSizes sizes_of(const Frame& fr, uint32_t outline_verts) {
+  FrameSizes z;
+  z.cmds = uint32_t(fr.cmds.size());
+  z.styles = uint32_t(fr.styles.size());
+  z.xforms = uint32_t(fr.xforms.size());
+  z.canvases = uint32_t(fr.canvases.size());
+  z.lut_jobs = uint32_t(fr.lut_jobs.size());
+  z.stops = uint32_t(fr.stops.size());
+  z.tiles = fr.tiles;
+  z.rows = fr.rows;
+  z.vert_words = fr.verts.size() + 2 * uint64_t(outline_verts);
+  z.cmd_bytes = fr.path_cmds.size() + uint64_t(outline_verts);
+  z.image_words = fr.image_words;
+  z.lut_words = fr.lut_words;
+  for (const FrameTarget& t : fr.targets)
+    if (!device_target_direct(t.image))
+      z.canvas_words += align_up(uint64_t(align_up(uint32_t(t.image.width), 4)) * uint32_t(t.image.height), 64);
+  return z;
+}
+
+BLGpuResult Runtime::upload(const Frame& fr, const FrameSizes* caps) {
   const uint32_t ncv = uint32_t(fr.canvases.size());
   h2d_bytes = 0;
   d2h_bytes = 0;
 
   FrameView v{};
+  v.counts = counts_dev;
+  // the previous frame (and its read of host_counts) has completed: run() returns when it has
+  BLGPU_CHECK(put_counts(fr, counts_dev));
   uint32_t outline_verts = 0;
   strokes_counted = false;
   stroke_bytes = 0;
   BLGpuResult sr = prepare_strokes(fr, v, outline_verts);
   if (sr) return sr;
-  const size_t vert_words = fr.verts.size() + 2 * size_t(outline_verts);   // doubles
-  const size_t cmd_bytes = fr.path_cmds.size() + size_t(outline_verts);
+  const FrameSizes z = caps ? *caps : sizes_of(fr, outline_verts);
+  const uint32_t nc = z.cmds;
+  const uint64_t vert_words = z.vert_words;   // doubles
 
   // Items: at most one per vertex (a line or curve consumes at least one; a closing line takes
   // the place of the figure's move-to).
-  const uint32_t item_capacity = uint32_t(std::min<size_t>(vert_words + 1, 0xFFFFFFF0u));
+  const uint32_t item_capacity = uint32_t(std::min<uint64_t>(vert_words + 1, 0xFFFFFFF0u));
   // a cubic (3 vertices) splits into at most 8 monotonic pieces, a quadratic (2) into at most 3
-  const uint32_t piece_capacity = uint32_t(std::min<size_t>(vert_words / 2 * 3 + 64, 0xFFFFFFF0u));
+  const uint32_t piece_capacity = uint32_t(std::min<uint64_t>(vert_words / 2 * 3 + 64, 0xFFFFFFF0u));
 
   // Plan: [staged inputs][luts][canvases][work arrays]
   auto plan = [&](Layout& L, FrameView& v, std::vector<uint32_t*>* cpix) -> size_t {
     v.cmds_rw = L.take<DevCmd>(nc);
     v.cmds = v.cmds_rw;
-    v.styles = L.take<DevStyle>(fr.styles.size());
-    v.xforms = L.take<DevXform>(fr.xforms.size());
-    v.canvases = L.take<DevCanvas>(ncv);
+    v.styles = L.take<DevStyle>(z.styles);
+    v.xforms = L.take<DevXform>(z.xforms);
+    v.canvases = L.take<DevCanvas>(z.canvases);
     v.verts = L.take<double>(vert_words);
-    v.path_cmds = L.take<uint8_t>(cmd_bytes);
-    v.lut_jobs = L.take<DevLutJob>(fr.lut_jobs.size());
-    v.stops = L.take<DevStop>(fr.stops.size());
-    v.images = L.take<uint32_t>(fr.image_words);
+    v.path_cmds = L.take<uint8_t>(z.cmd_bytes);
+    v.lut_jobs = L.take<DevLutJob>(z.lut_jobs);
+    v.stops = L.take<DevStop>(z.stops);
+    v.images = L.take<uint32_t>(z.image_words);
     size_t staged_end = align_up(L.off, 256);
-    v.luts = L.take<uint32_t>(fr.lut_words);
-    for (uint32_t i = 0; i < ncv; i++) {
-      const BLGpuImage& im = fr.targets[i].image;
-      uint32_t* p;
-      if (device_target_direct(im)) p = static_cast<uint32_t*>(im.pixel_data);
-      else p = L.take<uint32_t>(size_t(align_up(uint32_t(im.width), 4)) * uint32_t(im.height));
-      if (cpix) (*cpix)[i] = p;
+    v.luts = L.take<uint32_t>(z.lut_words);
+    // canvas pixels (host-memory targets): one pool, every canvas at a 256-byte boundary
+    uint32_t* pool = L.take<uint32_t>(z.canvas_words);
+    if (cpix) {
+      size_t off = 0;
+      for (uint32_t i = 0; i < ncv; i++) {
+        const BLGpuImage& im = fr.targets[i].image;
+        if (device_target_direct(im)) { (*cpix)[i] = static_cast<uint32_t*>(im.pixel_data); continue; }
+        (*cpix)[i] = pool ? pool + off : nullptr;
+        off += align_up(size_t(align_up(uint32_t(im.width), 4)) * uint32_t(im.height), 64);
+      }
     }
     v.items = L.take<DevItem>(item_capacity);
     v.curve_items = L.take<DevItem>(item_capacity);
@@ -418,13 +464,13 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     v.cmd_yr = L.take<uint32_t>(nc);
     cmdrow_per_cmd = L.take<uint32_t>(nc + 1);
     v.cmdrow_base = L.take<uint32_t>(nc + 1);
-    v.row_counts = L.take<uint32_t>(fr.rows + 1);
-    v.row_offsets = L.take<uint32_t>(fr.rows + 1);
-    v.row_copies = L.take<uint32_t>(fr.rows + 1);
-    v.strip_start = L.take<uint32_t>((size_t(fr.tiles) + 1) * (kTileH / kStripRows));
-    row_canvas = L.take<uint32_t>(fr.rows + 1);
-    v.tile_order = L.take<uint32_t>(fr.tiles + 1);
-    v.tile_canvas = L.take<uint32_t>(fr.tiles + 1);
+    v.row_counts = L.take<uint32_t>(z.rows + 1);
+    v.row_offsets = L.take<uint32_t>(z.rows + 1);
+    v.row_copies = L.take<uint32_t>(z.rows + 1);
+    v.strip_start = L.take<uint32_t>((size_t(z.tiles) + 1) * (kTileH / kStripRows));
+    row_canvas = L.take<uint32_t>(z.rows + 1);
+    v.tile_order = L.take<uint32_t>(z.tiles + 1);
+    v.tile_canvas = L.take<uint32_t>(z.tiles + 1);
     // [0] work queue, [1] line items, [2] cubic curves, [3] their queue, [4..12) totals,
     // [12..16) error flags, [16..20) pixel ops (2 x u64), [21] quadratic / conic curves, [22] their
     // queue
@@ -436,7 +482,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     v.rs_base = L.take<uint32_t>(nc + 1);
     v.rb_count = L.take<uint32_t>(nc + 1);
     v.rb_base = L.take<uint32_t>(nc + 1);
-    scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, fr.rows + 1)));
+    scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, z.rows + 1)));
     return staged_end;
   };
 
@@ -459,7 +505,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   // to pageable memory) is packed into the page-locked staging buffer first.
   size_t pack_bytes = align_up(sizeof(DevCanvas) * ncv, 256);
   auto needs_pack = [&](bool pinned_array, size_t bytes) { if (!pinned_array) pack_bytes += align_up(bytes, 256); };
-  needs_pack(fr.cmds.ptr_pinned, sizeof(DevCmd) * nc);
+  needs_pack(fr.cmds.ptr_pinned, sizeof(DevCmd) * fr.cmds.size());
   needs_pack(fr.styles.ptr_pinned, sizeof(DevStyle) * fr.styles.size());
   needs_pack(fr.xforms.ptr_pinned, sizeof(DevXform) * fr.xforms.size());
   needs_pack(fr.verts.ptr_pinned, sizeof(double) * fr.verts.size());
@@ -489,7 +535,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
     }
     return cudaMemcpyAsync(const_cast<void*>(dev_ptr), src, bytes, cudaMemcpyHostToDevice, stream);
   };
-  BLGPU_CHECK(put(v.cmds, fr.cmds.data(), sizeof(DevCmd) * nc, fr.cmds.ptr_pinned));
+  BLGPU_CHECK(put(v.cmds, fr.cmds.data(), sizeof(DevCmd) * fr.cmds.size(), fr.cmds.ptr_pinned));
   BLGPU_CHECK(put(v.styles, fr.styles.data(), sizeof(DevStyle) * fr.styles.size(), fr.styles.ptr_pinned));
   BLGPU_CHECK(put(v.xforms, fr.xforms.data(), sizeof(DevXform) * fr.xforms.size(), fr.xforms.ptr_pinned));
   std::vector<DevCanvas> cvs = fr.canvases;
@@ -534,7 +580,7 @@ BLGpuResult Runtime::upload(const Frame& fr) {
 
   // Segment array: kept across frames, sized from the vertex count at first and from the actual
   // count whenever a frame overflows it (run() then repeats the counting half).
-  size_t want_segs = std::max<size_t>(size_t(seg_capacity), vert_words * 2 + 65536);
+  size_t want_segs = std::max<size_t>(size_t(seg_capacity), caps ? size_t(caps->dyn.segs) : size_t(vert_words * 2 + 65536));
   want_segs = std::min<size_t>(want_segs, cfg.max_segments > 0 ? size_t(cfg.max_segments) : size_t(0xFFFFFFF0u));
   if (want_segs > seg_capacity) {
     graph_valid = false;
@@ -547,10 +593,10 @@ BLGpuResult Runtime::upload(const Frame& fr) {
   v.item_capacity = item_capacity;
   v.piece_capacity = piece_capacity;
   v.num_cmds = nc;
-  v.num_canvases = ncv;
-  v.num_tiles = fr.tiles;
-  v.num_rows = fr.rows;
-  v.num_lut_jobs = uint32_t(fr.lut_jobs.size());
+  v.num_canvases = z.canvases;
+  v.num_tiles = z.tiles;
+  v.num_rows = z.rows;
+  v.num_lut_jobs = z.lut_jobs;
   v.pixels = nullptr;
   view = v;
   targets = fr.targets;
@@ -598,7 +644,7 @@ int Runtime::enqueue_count_half(cudaStream_t st) {
 // coverage pass, the composite pass.
 int Runtime::enqueue_render_half(cudaStream_t st, bool timed) {
   const FrameView& f = view;
-  int k = 0;
+  int k = launch_frame_gate(f, st);
   cudaMemsetAsync(f.cmdrow_counts, 0, sizeof(uint32_t) * (f.num_cmdrows + 1), st);
   cudaMemsetAsync(f.backdrop, 0, sizeof(uint32_t) * kStripRows * (size_t(f.num_cmdrows) + 1), st);
   k += launch_seg_bin(f, 0, st);
@@ -637,6 +683,7 @@ static void plan_dynamic(Layout& L, FrameView& v, const FrameTotals& t) {
   v.num_seglist = t.seglist;
   v.num_row_states = t.row_states;
   v.num_row_runs = t.row_runs;
+  v.num_row_entries = t.row_entries;
 }
 
 BLGpuResult Runtime::download() {
@@ -653,6 +700,132 @@ BLGpuResult Runtime::download() {
 }
 
 BLGpuResult Runtime::run(const Frame& fr) {
+  if (cfg.graph_frames && fr.stroke_figs.empty()) {
+    // a graph frame that does not fit is re-run eagerly, so its device targets must be redrawable:
+    // either copied (host targets, unaligned device rows) or overwritten by the frame's first fill
+    bool redrawable = true;
+    for (const FrameTarget& t : fr.targets) redrawable &= !device_target_direct(t.image) || !t.upload;
+    if (redrawable) return run_graph(fr);
+  }
+  return run_eager(fr);
+}
+
+static uint32_t grow_u32(uint64_t v) { return uint32_t(std::min<uint64_t>(v + v / 4 + 64, 0xFFFFFFF0u)); }
+static uint64_t grow_u64(uint64_t v) { return v + v / 4 + 256; }
+
+static void raise_caps(FrameSizes& c, const FrameSizes& need) {
+  auto up32 = [](uint32_t& cap, uint32_t want) { if (want > cap) cap = grow_u32(want); };
+  auto up64 = [](uint64_t& cap, uint64_t want) { if (want > cap) cap = grow_u64(want); };
+  up32(c.cmds, need.cmds); up32(c.styles, need.styles); up32(c.xforms, need.xforms);
+  up32(c.canvases, need.canvases); up32(c.lut_jobs, need.lut_jobs); up32(c.stops, need.stops);
+  up32(c.tiles, need.tiles); up32(c.rows, need.rows);
+  up64(c.vert_words, need.vert_words); up64(c.cmd_bytes, need.cmd_bytes); up64(c.image_words, need.image_words);
+  up64(c.lut_words, need.lut_words); up64(c.canvas_words, need.canvas_words);
+}
+
+static void raise_dyn(FrameTotals& c, const FrameTotals& t) {
+  auto up = [](uint32_t& cap, uint32_t want) { if (want > cap) cap = grow_u32(want); };
+  up(c.segs, t.segs); up(c.seglist, t.seglist); up(c.cmdrows, t.cmdrows);
+  up(c.row_entries, t.row_entries); up(c.row_states, t.row_states); up(c.row_runs, t.row_runs);
+}
+
+// A frame as one launch of the captured graph. Every array is laid out by the capacities in
+// `caps` (the first frame runs eagerly to learn the sizes the device computes), so the layout and
+// with it the graph stay the same for every frame that fits: the frame's data is copied in place,
+// the graph replayed, and the host reads back only the totals and flags after it. A frame whose
+// inputs exceed the capacities grows them (the graph is captured again); one whose device-computed
+// sizes exceed them skips its rendering half on the device (frame_gate_kernel) and runs again
+// eagerly after the capacities grow.
+BLGpuResult Runtime::run_graph(const Frame& fr) {
+  BLGPU_CHECK(cudaSetDevice(device));
+  for (const FrameTarget& t : fr.targets)
+    if (t.image.width < 0 || t.image.height < 0) return BLGPU_ERROR_INVALID_VALUE;
+  const FrameSizes need = sizes_of(fr, 0);
+  if (!caps_ready) {
+    BLGpuResult r = run_eager(fr);
+    if (r) return r;
+    caps = FrameSizes{};
+    raise_caps(caps, need);
+    raise_dyn(caps.dyn, totals);
+    caps_ready = true;
+    graph_valid = false;
+    return BLGPU_SUCCESS;
+  }
+  if (!need.fits_in(caps)) {
+    raise_caps(caps, need);
+    graph_valid = false;
+  }
+  has_frame = false;
+  pending_timing = 0;
+  const void* in_ptr = in_buf.ptr;
+  BLGpuResult r = upload(fr, &caps);
+  if (r) return r;
+  if (in_buf.ptr != in_ptr) graph_valid = false;
+  Layout measure;
+  FrameView probe = view;
+  plan_dynamic(measure, probe, caps.dyn);
+  if (measure.off > dyn_buf.size) {
+    BLGPU_CHECK(cudaStreamSynchronize(stream));
+    BLGPU_CHECK(dyn_buf.reserve(measure.off));
+    graph_valid = false;
+  }
+  Layout L;
+  L.base = static_cast<char*>(dyn_buf.ptr);
+  plan_dynamic(L, view, caps.dyn);
+  totals = caps.dyn;
+  if (!graph_valid) {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    cudaGraph_t g = nullptr;
+    BLGPU_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    int launches = enqueue_count_half(stream);
+    launches += enqueue_render_half(stream, false);
+    cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (e != cudaSuccess) return cuda_result(e);
+    e = cudaGraphInstantiate(&graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { graph = nullptr; return cuda_result(e); }
+    graph_valid = true;
+    stats.kernel_launches = uint64_t(launches);
+  }
+  BLGPU_CHECK(cudaEventRecord(ev[0], stream));
+  BLGPU_CHECK(cudaGraphLaunch(graph, stream));
+  BLGPU_CHECK(cudaEventRecord(ev[3], stream));
+  BLGPU_CHECK(cudaMemcpyAsync(host_totals, view.totals, 32, cudaMemcpyDeviceToHost, stream));
+  BLGPU_CHECK(cudaMemcpyAsync(host_totals + 20, view.error_flags, 32, cudaMemcpyDeviceToHost, stream));
+  d2h_bytes += 64;
+  BLGPU_CHECK(cudaStreamSynchronize(stream));
+  FrameTotals t;
+  t.segs = host_totals[0]; t.seglist = host_totals[1]; t.cmdrows = host_totals[2];
+  t.row_entries = host_totals[3]; t.row_states = host_totals[4]; t.row_runs = host_totals[6];
+  if (host_totals[20]) {
+    // the device-computed sizes did not fit: grow to them and render this frame eagerly
+    raise_dyn(caps.dyn, t);
+    graph_valid = false;
+    return run_eager(fr);
+  }
+  r = download();
+  if (r) return r;
+  BLGPU_CHECK(cudaStreamSynchronize(stream));
+  has_frame = true;
+  graph_frames_run++;
+  read_pixel_ops();
+  totals = t;   // the frame's own sizes (the arrays keep their capacities)
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ev[0], ev[3]);
+  stats.last_gpu_ms = ms;
+  stats.frames++;
+  stats.fill_commands = fr.cmds.size();
+  stats.segments = t.segs;
+  stats.tiles = fr.tiles;
+  stats.input_vertices = uint64_t(fr.verts.size() / 2);
+  stats.h2d_bytes = h2d_bytes;
+  stats.d2h_bytes = d2h_bytes;
+  last_frame_bytes = in_bytes + measure.off + uint64_t(caps.dyn.segs) * (sizeof(DevSeg) + sizeof(uint32_t));
+  return BLGPU_SUCCESS;
+}
+
+BLGpuResult Runtime::run_eager(const Frame& fr) {
   BLGPU_CHECK(cudaSetDevice(device));
   for (const FrameTarget& t : fr.targets)
     if (t.image.width < 0 || t.image.height < 0) return BLGPU_ERROR_INVALID_VALUE;
@@ -788,6 +961,7 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     v.rb_count = L.take<uint32_t>(nc + 1);
     v.rb_base = L.take<uint32_t>(nc + 1);
     a_scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, fr.rows + 1)));
+    v.counts = L.take<uint32_t>(kCntWords);
   };
   Layout L;
   L.base = static_cast<char*>(arena);
@@ -816,6 +990,14 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
   const BLGpuImage& im = fr.targets[0].image;
   cv.pixels = static_cast<uint32_t*>(im.pixel_data);
   cv.stride = int32_t(im.stride / 4);
+  uint32_t counts[kCntWords] = {};
+  counts[kCntCmds] = nc;
+  counts[kCntCanvases] = 1;
+  counts[kCntTiles] = fr.tiles;
+  counts[kCntRows] = fr.rows;
+  counts[kCntLutJobs] = uint32_t(fr.lut_jobs.size());
+  counts[kCntStrokeVertBase] = uint32_t(fr.verts.size() / 2);
+  BLGPU_CHECK(put(v.counts, counts, sizeof(counts)));     // pageable: staged before the call returns
   BLGPU_CHECK(put(v.cmds, fr.cmds.data(), sizeof(DevCmd) * nc));
   BLGPU_CHECK(put(v.styles, fr.styles.data(), sizeof(DevStyle) * fr.styles.size()));
   BLGPU_CHECK(put(v.xforms, fr.xforms.data(), sizeof(DevXform) * fr.xforms.size()));

@@ -143,6 +143,21 @@ struct FrameTotals {
   uint32_t segs = 0, seglist = 0, cmdrows = 0, row_entries = 0, row_states = 0, row_runs = 0;
 };
 
+// What a frame's device arrays hold: a frame's own sizes (eager runs) or the capacities of a
+// layout that any frame up to them fits (graph frames). The work arrays sized on the device
+// (segments, slots, coverage items, row lists, gradient rows) have their own capacities.
+struct FrameSizes {
+  uint32_t cmds = 0, styles = 0, xforms = 0, canvases = 0, lut_jobs = 0, stops = 0, tiles = 0, rows = 0;
+  uint64_t vert_words = 0, cmd_bytes = 0, image_words = 0, lut_words = 0, canvas_words = 0;
+  FrameTotals dyn;
+  bool fits_in(const FrameSizes& c) const {
+    return cmds <= c.cmds && styles <= c.styles && xforms <= c.xforms && canvases <= c.canvases &&
+           lut_jobs <= c.lut_jobs && stops <= c.stops && tiles <= c.tiles && rows <= c.rows &&
+           vert_words <= c.vert_words && cmd_bytes <= c.cmd_bytes && image_words <= c.image_words &&
+           lut_words <= c.lut_words && canvas_words <= c.canvas_words;
+  }
+};
+
 constexpr int kCounterWords = 48;
 
 struct DeviceBuffer {
@@ -168,6 +183,8 @@ struct Runtime {
   uint32_t seg_capacity = 0;
   void* host_staging = nullptr;
   size_t host_staging_size = 0;
+  uint32_t* counts_dev = nullptr;    // the frame's sizes (CountIndex), read by the kernels
+  uint32_t* host_counts = nullptr;   // pinned staging of counts_dev
   uint32_t* host_totals = nullptr;   // pinned: [0..8) frame totals, [16] stroke outline size,
                                      // [20..24) error flags (ErrorFlag bits in [20]), [24..28) pixel ops
 
@@ -201,7 +218,14 @@ struct Runtime {
   BLGpuResult init(const BLGpuRuntimeCreateInfo* info);
   void destroy();
   // Uploads `fr`, runs the pipeline, downloads the canvases that live in host memory. Blocking.
+  // With cfg.graph_frames the frame runs as a captured graph over capacity-sized arrays when it
+  // can (run_graph); otherwise eagerly, every array sized from the frame (run_eager).
   BLGpuResult run(const Frame& fr);
+  BLGpuResult run_eager(const Frame& fr);
+  BLGpuResult run_graph(const Frame& fr);
+  FrameSizes caps{};             // graph frames: capacities of the layout the graph was captured on
+  bool caps_ready = false;
+  uint64_t graph_frames_run = 0; // frames that ran as a replay of the captured graph
   BLGpuResult replay(bool use_graph);
   BLGpuResult synchronize();
   // Frees the device arenas (the kept frame is dropped).
@@ -216,13 +240,18 @@ struct Runtime {
   int enqueue_count_half(cudaStream_t st);
   int enqueue_render_half(cudaStream_t st, bool timed);
   BLGpuResult prepare_strokes(const Frame& fr, FrameView& v, uint32_t& outline_verts);
-  BLGpuResult upload(const Frame& fr);
+  // Fills host_counts with the frame's sizes and copies them to `dev` on the stream.
+  cudaError_t put_counts(const Frame& fr, uint32_t* dev);
+  // Uploads `fr` into a layout sized by the frame itself, or by `caps` (graph frames).
+  BLGpuResult upload(const Frame& fr, const FrameSizes* caps = nullptr);
   BLGpuResult download();
   BLGpuResult reserve_segments(uint32_t count);
   void read_pixel_ops();
 };
 
 BLGpuResult cuda_result(cudaError_t e);
+bool device_target_direct(const BLGpuImage& im);
+FrameSizes sizes_of(const Frame& fr, uint32_t outline_verts);
 int last_cuda_error();
 
 }  // namespace blgpu

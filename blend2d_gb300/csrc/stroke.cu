@@ -15,7 +15,10 @@ constexpr int kStrokeThreads = 64;
 
 __global__ void __launch_bounds__(kStrokeThreads) stroke_count_kernel(FrameView f) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= f.num_stroke_figs) return;
+  if (t >= f.counts[kCntStrokeFigs]) {
+    if (t < f.num_stroke_figs) f.stroke_totals[t] = 0;   // beyond the frame's figures: nothing to scan
+    return;
+  }
   const uint32_t i = f.stroke_order[t];
   const DevStrokeFig fg = f.stroke_figs[i];
   const DevStrokeParams dp = f.stroke_params[fg.param];
@@ -29,11 +32,11 @@ __global__ void __launch_bounds__(kStrokeThreads) stroke_count_kernel(FrameView 
 
 __global__ void __launch_bounds__(kStrokeThreads) stroke_emit_kernel(FrameView f) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= f.num_stroke_figs) return;
+  if (t >= f.counts[kCntStrokeFigs]) return;
   const uint32_t i = f.stroke_order[t];
   const DevStrokeFig fg = f.stroke_figs[i];
   const uint32_t off = f.stroke_offsets[i];
-  const uint32_t vb = f.stroke_vert_base + off;
+  const uint32_t vb = f.counts[kCntStrokeVertBase] + off;
   if (fg.cmd_figs) {
     DevCmd& c = f.cmds_rw[fg.cmd];
     c.geom_first = vb;

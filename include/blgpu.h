@@ -114,6 +114,7 @@ typedef struct BLGpuStats {
   uint64_t d2h_bytes;      /* device->host bytes of the last flush (canvas downloads + sizes) */
   int64_t last_cuda_error; /* cudaError_t behind the last BLGPU_ERROR_DEVICE (0 if none) */
   double last_composite_ms;/* ... of which the composite kernel */
+  uint64_t graph_frames;   /* frames that ran as a replay of the captured graph (graph_frames launch config) */
 } BLGpuStats;
 
 /* Launch shapes of the device pipeline (0 in a *_blocks_per_sm field = as many as fit). Tile and
@@ -130,7 +131,13 @@ typedef struct BLGpuLaunchConfig {
   int32_t max_segments;         /* 0: the segment array grows as frames need; N > 0: it never holds more
                                    than N segments, and a frame that emits more fails with
                                    BLGPU_ERROR_DATA_TOO_LARGE (a cap on the runtime's device memory) */
-  int32_t reserved[1];
+  int32_t graph_frames;         /* 1: frames run as one captured CUDA graph over arrays sized by
+                                   capacities (grown as frames need, with headroom): a new frame that
+                                   fits is uploaded in place and the graph replayed, with no host
+                                   round trip inside the frame; a frame that does not fit grows the
+                                   capacities and runs eagerly. Frames with strokes, or whose device
+                                   targets are drawn in place onto existing content, run eagerly. */
+  int32_t reserved[2];
 } BLGpuLaunchConfig;
 
 /* --- runtime (device, stream, memory) --------------------------------------------------- */

@@ -53,14 +53,20 @@ def test_python_bindings_cover_the_abi(lib_path):
         assert getattr(lib, name).restype is ctypes.c_uint32
 
 
-def test_struct_layouts_match_header():
-    # sizes of the ABI structs as a C compiler lays them out on LP64
-    assert ctypes.sizeof(bg.RuntimeCreateInfo) == 32
-    assert ctypes.sizeof(bg.Image) == 32
-    assert ctypes.sizeof(bg.GradientStop) == 16
-    assert ctypes.sizeof(bg.Gradient) == 8 + 48 + 8 + 8 + 8
-    assert ctypes.sizeof(bg.Pattern) == 8 + 16 + 8 + 8
-    assert ctypes.sizeof(bg.Stats) == 112
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors have the sizes a C compiler gives the header's structs."""
+    structs = {"BLGpuRuntimeCreateInfo": bg.RuntimeCreateInfo, "BLGpuImage": bg.Image,
+               "BLGpuGradientStop": bg.GradientStop, "BLGpuGradient": bg.Gradient, "BLGpuPattern": bg.Pattern,
+               "BLGpuStats": bg.Stats, "BLGpuLaunchConfig": bg.LaunchConfig, "BLGpuMemoryInfo": bg.MemoryInfo,
+               "BLGpuStrokeOptions": bg.StrokeOptions}
+    src = tmp_path / "sizes.c"
+    src.write_text('#include <stdio.h>\n#include "blgpu.h"\nint main(void) {\n' +
+                   "".join(f'  printf("%zu\\n", sizeof({name}));\n' for name in structs) + "  return 0;\n}\n")
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    sizes = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    for (name, cls), size in zip(structs.items(), sizes):
+        assert ctypes.sizeof(cls) == size, name
 
 
 def test_missing_library_fails_loudly(tmp_path):

@@ -669,3 +669,32 @@ def test_shape_context_calls_match_stream(runtimes):
     stream = sw.to_bytes()
     assert not _diff(out, bg.render_stream(runtimes(), stream))
     assert not _diff(out, oracle_lib.render(stream))
+
+
+def test_graph_frames_replay_new_frames_bit_exact():
+    """With graph frames on, a frame that fits the captured layout is uploaded in place and the
+    captured graph replayed (no host round trip inside the frame): different frames in a row,
+    single canvases and batches, each bit-exact to the oracle; a frame larger than the layout
+    grows it and still renders exactly."""
+    with bg.Runtime(0) as rt:
+        cfg = rt.launch_config()
+        cfg.graph_frames = 1
+        rt.set_launch_config(cfg)
+        frames = [scenes.random_mix(7000 + i, width=200, height=150, count=120 - 7 * i).to_bytes() for i in range(6)]
+        frames.append(scenes.random_mix(7100, width=320, height=240, count=400).to_bytes())   # larger: grows
+        frames += [scenes.random_mix(7200 + i, width=180, height=140, count=60).to_bytes() for i in range(3)]
+        for i, s in enumerate(frames):
+            got = bg.render_stream(rt, s)
+            want = oracle_lib.render(s)
+            assert not _diff(got, want), f"frame {i}: {_diff(got, want)}"
+        assert rt.stats().graph_frames >= 5       # the frames that fit replayed the graph
+        # batches of different canvases through the same graph
+        before = rt.stats().graph_frames
+        for k in range(3):
+            sws = scenes.batch_canvases(seed=500 + k, count=12, max_side=300, max_paths=150)
+            streams = [sw.to_bytes() for sw in sws]
+            targets = [np.zeros((sw.height, sw.width), dtype=np.uint32) for sw in sws]
+            rt.render_batch(streams, targets)
+            for i, (s, t) in enumerate(zip(streams, targets)):
+                assert not _diff(t, oracle_lib.render(s)), f"batch {k} canvas {i}"
+        assert rt.stats().graph_frames > before
