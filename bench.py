@@ -459,9 +459,19 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
     targets = [pinned_canvas(h, w) for h, w in shapes]
     log("batch: pinned canvases allocated")
 
-    # ---- e2e through the public API: host streams, pinned host canvases, one pipeline per step
+    # ---- e2e through the public API: host streams, pinned host canvases, one pipeline per step.
+    # One eager step first (every array sized from the frame, a host read-back between the
+    # halves), for reference; then graph frames: the steps upload their data in place and replay
+    # one captured graph (the first warm-up step learns the capacities).
+    rt.render_batch(streams, targets)
+    t0 = time.perf_counter()
+    rt.render_batch(streams, targets)
+    eager_step_s = time.perf_counter() - t0
+    cfg0 = rt.launch_config()
+    rt.set_launch_config(bg.LaunchConfig(**{**cfg0.as_dict(), "graph_frames": 1}))
     for _ in range(args.warmup):
         rt.render_batch(streams, targets)
+    g0 = int(rt.stats().graph_frames)
     dist.barrier()
     clocks = ClockSampler(local).start()
     t0 = time.perf_counter()
@@ -469,10 +479,13 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
         rt.render_batch(streams, targets)
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e_clocks = clocks.stop()
-    log(f"batch: e2e {e2e_s * 1e3 / args.steps:.1f} ms/step")
+    graph_steps = int(rt.stats().graph_frames) - g0
+    log(f"batch: e2e {e2e_s * 1e3 / args.steps:.1f} ms/step ({graph_steps} graph frames), eager step {eager_step_s * 1e3:.1f} ms")
     st = rt.stats()
     h2d, d2h = int(st.h2d_bytes), int(st.d2h_bytes)
     batch_dev_ms = float(st.last_gpu_ms)
+    rt.set_launch_config(cfg0)
+    rt.render_batch(streams, targets)       # the eager frame the replays below time
 
     # ---- device-resident: the batch's device pipeline replayed on its inputs in HBM
     step_ms, fine_ms, comp_ms, launches, dev_clocks = time_replays(rt, s, args.steps, args.warmup)
@@ -522,7 +535,8 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
         "ms_per_step": round(total_s * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": DTYPE, "data": "synthetic", "config": cfg,
         "e2e": {"value": round(world * args.steps * mpix / e2e_s, 3), "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_s * 1e3 / args.steps, 3), "clocks": e2e_clocks},
+                "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_s * 1e3 / args.steps, 3), "clocks": e2e_clocks,
+                "graph_frames": graph_steps, "eager_ms_per_step": round(eager_step_s * 1e3, 3)},
         "gpu_launches": launches,
         "clocks": dev_clocks,
         "roofline": roof,

@@ -27,6 +27,7 @@ constexpr int kTileShift = 5;
 constexpr int kFineThreads = 256;   // 8 warps per block
 constexpr int kStripRows = 4;       // a strip (one warp: 32 lanes x 4 pixels) is 4 rows of a tile
 constexpr int kStripShift = 2;
+constexpr int kMaxListLog2 = kTileShift - kStripShift;   // list rows down to one strip (4 rows)
 
 enum FillKind : uint32_t {
   kFillAnalytic = 0,   // edges -> analytic coverage (FillAnalytic_Base)
@@ -137,7 +138,7 @@ struct alignas(16) DevCanvas {
   int32_t band_height;     // reference band height (conic fetch start rows)
   int32_t tiles_x, tiles_y;
   uint32_t tile_base;      // first global tile index
-  uint32_t row_base;       // first global tile-row index
+  uint32_t row_base;       // first global tile-row index (command-list rows: row_base << list_log2)
   uint32_t cmd_first, cmd_count;
   uint32_t pad[2];
 };
@@ -315,6 +316,10 @@ struct FrameView {
   uint32_t num_row_states;
   uint32_t num_row_runs;       // conic row runs (sum of rb_count)
   uint32_t num_row_entries;    // row list entries (sum of row_counts)
+  // Command lists are kept per list row of 1 << list_shift pixel rows (4 to 32; tunable): a canvas
+  // of tiles_y tile rows has tiles_y << list_log2 list rows (list_log2 = 5 - list_shift), from
+  // list row row_base << list_log2 on; rows past the canvas's bottom stay empty.
+  uint32_t list_shift;
 };
 
 }  // namespace blgpu

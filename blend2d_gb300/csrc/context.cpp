@@ -1299,6 +1299,7 @@ static void to_abi(const LaunchConfig& c, BLGpuLaunchConfig* out) {
   out->no_occlusion_cull = c.no_occlusion_cull;
   out->max_segments = c.max_segments;
   out->graph_frames = c.graph_frames;
+  out->list_rows = c.list_rows;
 }
 
 BLGPU_API BLGpuResult blgpu_runtime_get_launch_config(const BLGpuRuntime* rt, BLGpuLaunchConfig* out) {
@@ -1314,7 +1315,8 @@ BLGPU_API BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BL
       (c->edge_block != 64 && c->edge_block != 128 && c->edge_block != 256) ||
       c->cover_blocks_per_sm < 0 || c->fine_blocks_per_sm < 0 || c->cubic_blocks_per_sm < 0 ||
       (c->no_occlusion_cull != 0 && c->no_occlusion_cull != 1) || c->max_segments < 0 ||
-      (c->graph_frames != 0 && c->graph_frames != 1))
+      (c->graph_frames != 0 && c->graph_frames != 1) ||
+      (c->list_rows != 0 && c->list_rows != 4 && c->list_rows != 8 && c->list_rows != 16 && c->list_rows != 32))
     return BLGPU_ERROR_INVALID_VALUE;
   LaunchConfig lc;
   lc.cover_slots = c->cover_slots;
@@ -1325,6 +1327,7 @@ BLGPU_API BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BL
   lc.no_occlusion_cull = c->no_occlusion_cull;
   lc.max_segments = c->max_segments;
   lc.graph_frames = c->graph_frames;
+  lc.list_rows = c->list_rows ? c->list_rows : 32;
   std::lock_guard<std::mutex> e(rt->exec);
   rt->rt.cfg = lc;
   rt->rt.graph_valid = false;

@@ -771,14 +771,16 @@ __global__ void cmd_tiles_kernel(FrameView f, uint32_t* cmdrow_counts_per_cmd, u
   f.cmd_xr[c] = uint32_t(x0) | (uint32_t(x1) << 16);
   f.cmd_yr[c] = uint32_t(y0) | (uint32_t(y1) << 16);
   uint32_t tx0 = uint32_t(x0) >> kTileShift, tx1 = uint32_t(x1) >> kTileShift;
-  uint32_t ty0 = uint32_t(y0) >> kTileShift, ty1 = uint32_t(y1) >> kTileShift;
+  // the command's list rows (1 << list_shift pixel rows each)
+  uint32_t ty0 = uint32_t(y0) >> f.list_shift, ty1 = uint32_t(y1) >> f.list_shift;
   f.cmd_tile_x[c] = tx0 | (tx1 << 16);
   f.cmd_tile_y[c] = ty0 | (ty1 << 16);
   // segment lists are kept per (command, strip row, tile column)
   cmdrow_counts_per_cmd[c] = cmd.kind == kFillAnalytic
       ? ((uint32_t(y1) >> kStripShift) - (uint32_t(y0) >> kStripShift) + 1u) * (tx1 - tx0 + 1u) : 0u;
 
-  for (uint32_t r = ty0; r <= ty1; r++) atomicAdd(&row_counts[cv.row_base + r], 1u);
+  const uint32_t row_base = cv.row_base << (kTileShift - f.list_shift);
+  for (uint32_t r = ty0; r <= ty1; r++) atomicAdd(&row_counts[row_base + r], 1u);
 }
 
 // Segments per (command, strip row, tile column) slot: a segment belongs to every slot its cells
@@ -901,9 +903,10 @@ int launch_backdrop_prefix(const FrameView& f, cudaStream_t st) {
 __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
   __shared__ uint32_t smem[32];
   uint32_t row = blockIdx.x;
-  if (row >= f.counts[kCntRows] || frame_skipped(f)) return;        // whole blocks leave together
+  const uint32_t log2 = kTileShift - f.list_shift;
+  if (row >= (f.counts[kCntRows] << log2) || frame_skipped(f)) return;        // whole blocks leave together
   const DevCanvas cv = f.canvases[row_canvas[row]];
-  uint32_t r = row - cv.row_base;
+  uint32_t r = row - (cv.row_base << log2);
   uint32_t out = f.row_offsets[row];
   uint32_t copies = 0;
   for (uint32_t base = 0; base < cv.cmd_count; base += blockDim.x) {
@@ -1125,7 +1128,7 @@ __global__ void __launch_bounds__(kFineThreads) cull_kernel(FrameView f) {
     const int tx = int(local % uint32_t(cv.tiles_x)), ty = int(local / uint32_t(cv.tiles_x));
     const int x_base = tx * kTileW;
     const int row0 = ty * kTileH + strip * kStripRows;
-    const uint32_t row_id = cv.row_base + uint32_t(ty);
+    const uint32_t row_id = (cv.row_base << (kTileShift - f.list_shift)) + (uint32_t(row0) >> f.list_shift);
     if (row0 >= cv.h || f.row_copies[row_id] < 2) {
       if (lane == 0) f.strip_start[unit] = 0;
       continue;
@@ -1217,7 +1220,7 @@ __global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
       for (int k = 0; k < 4; k++) pix[k] = (row_ok && xp + k < cv.w) ? dst[k] : 0u;
     }
 
-    uint32_t row_id = cv.row_base + uint32_t(ty);
+    const uint32_t row_id = (cv.row_base << (kTileShift - f.list_shift)) + (uint32_t(row0) >> f.list_shift);
     uint32_t list_first = f.row_offsets[row_id];
     uint32_t list_count = f.row_counts[row_id];
     const uint32_t strip_y = uint32_t(row0) | (uint32_t(row1) << 16);
@@ -1421,9 +1424,10 @@ __global__ void tile_setup_kernel(FrameView f, uint32_t* row_canvas) {
     f.tile_canvas[i] = lo;
     f.tile_order[i] = i;
   }
-  if (i < f.counts[kCntRows]) {
+  const uint32_t log2 = kTileShift - f.list_shift;
+  if (i < (f.counts[kCntRows] << log2)) {
     uint32_t lo = 0, hi = num_canvases - 1;
-    while (lo < hi) { uint32_t mid = (lo + hi + 1) >> 1; if (f.canvases[mid].row_base <= i) lo = mid; else hi = mid - 1; }
+    while (lo < hi) { uint32_t mid = (lo + hi + 1) >> 1; if ((f.canvases[mid].row_base << log2) <= i) lo = mid; else hi = mid - 1; }
     row_canvas[i] = lo;
   }
 }
@@ -1545,9 +1549,10 @@ int launch_seg_bin(const FrameView& f, int scatter, cudaStream_t st) {
 
 int launch_rows_and_tiles(const FrameView& f, uint32_t* row_canvas, cudaStream_t st) {
   int k = 0;
-  uint32_t n = f.num_tiles > f.num_rows ? f.num_tiles : f.num_rows;
+  const uint32_t list_rows = f.num_rows << (kTileShift - f.list_shift);
+  uint32_t n = f.num_tiles > list_rows ? f.num_tiles : list_rows;
   if (n) { tile_setup_kernel<<<cdiv(n, 256), 256, 0, st>>>(f, row_canvas); k++; }
-  if (f.num_rows) { row_fill_kernel<<<f.num_rows, 512, 0, st>>>(f, row_canvas); k++; }
+  if (list_rows) { row_fill_kernel<<<list_rows, 512, 0, st>>>(f, row_canvas); k++; }
   return k;
 }
 

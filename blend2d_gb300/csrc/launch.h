@@ -19,7 +19,13 @@ struct LaunchConfig {
   int no_occlusion_cull = 0;      // 1: the composite starts every strip at its first command
   int max_segments = 0;           // > 0: cap of the segment array (frames needing more fail)
   int graph_frames = 0;           // 1: frames run as a captured graph over capacity-sized arrays
+  int list_rows = 32;             // pixel rows per command list (4, 8, 16 or 32)
 };
+
+// log2 of the list-row height a launch config selects.
+inline uint32_t list_shift_of(const LaunchConfig& c) {
+  return c.list_rows == 4 ? 2u : c.list_rows == 8 ? 3u : c.list_rows == 16 ? 4u : 5u;
+}
 
 int exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* tmp, cudaStream_t st);
 uint32_t scan_temp_words(uint32_t n);

@@ -464,11 +464,13 @@ BLGpuResult Runtime::upload(const Frame& fr, const FrameSizes* caps) {
     v.cmd_yr = L.take<uint32_t>(nc);
     cmdrow_per_cmd = L.take<uint32_t>(nc + 1);
     v.cmdrow_base = L.take<uint32_t>(nc + 1);
-    v.row_counts = L.take<uint32_t>(z.rows + 1);
-    v.row_offsets = L.take<uint32_t>(z.rows + 1);
-    v.row_copies = L.take<uint32_t>(z.rows + 1);
+    // command-list rows: room for the smallest list-row height
+    const size_t list_rows = (size_t(z.rows) << kMaxListLog2) + 1;
+    v.row_counts = L.take<uint32_t>(list_rows);
+    v.row_offsets = L.take<uint32_t>(list_rows);
+    v.row_copies = L.take<uint32_t>(list_rows);
     v.strip_start = L.take<uint32_t>((size_t(z.tiles) + 1) * (kTileH / kStripRows));
-    row_canvas = L.take<uint32_t>(z.rows + 1);
+    row_canvas = L.take<uint32_t>(list_rows);
     v.tile_order = L.take<uint32_t>(z.tiles + 1);
     v.tile_canvas = L.take<uint32_t>(z.tiles + 1);
     // [0] work queue, [1] line items, [2] cubic curves, [3] their queue, [4..12) totals,
@@ -482,7 +484,7 @@ BLGpuResult Runtime::upload(const Frame& fr, const FrameSizes* caps) {
     v.rs_base = L.take<uint32_t>(nc + 1);
     v.rb_count = L.take<uint32_t>(nc + 1);
     v.rb_base = L.take<uint32_t>(nc + 1);
-    scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, z.rows + 1)));
+    scan_tmp = L.take<uint32_t>(scan_temp_words(std::max<uint32_t>(nc + 1, (z.rows << kMaxListLog2) + 1)));
     return staged_end;
   };
 
@@ -612,10 +614,12 @@ BLGpuResult Runtime::reserve_segments(uint32_t count) {
 
 // Counting half: LUTs, edge building (segments appended), tile ranges, row-list sizes, totals.
 int Runtime::enqueue_count_half(cudaStream_t st) {
+  view.list_shift = list_shift_of(cfg);
   const FrameView& f = view;
+  const uint32_t list_rows = f.num_rows << (kTileShift - f.list_shift);
   int k = 0;
   cudaMemsetAsync(f.work_counter, 0, sizeof(uint32_t) * kCounterWords, st);
-  cudaMemsetAsync(f.row_counts, 0, sizeof(uint32_t) * (f.num_rows + 1), st);
+  cudaMemsetAsync(f.row_counts, 0, sizeof(uint32_t) * (list_rows + 1), st);
   if (f.num_lut_jobs) {
     cudaEventRecord(fork_ev, st);
     cudaStreamWaitEvent(side, fork_ev, 0);
@@ -631,8 +635,8 @@ int Runtime::enqueue_count_half(cudaStream_t st) {
   k += launch_cmd_tiles(f, cmdrow_per_cmd, st);
   k += exclusive_scan(cmdrow_per_cmd, f.cmdrow_base, f.num_cmds, scan_tmp, st);
   k += launch_total(cmdrow_per_cmd, f.cmdrow_base, f.num_cmds, f.totals + 2, st);
-  k += exclusive_scan(f.row_counts, f.row_offsets, f.num_rows, scan_tmp, st);
-  k += launch_total(f.row_counts, f.row_offsets, f.num_rows, f.totals + 3, st);
+  k += exclusive_scan(f.row_counts, f.row_offsets, list_rows, scan_tmp, st);
+  k += launch_total(f.row_counts, f.row_offsets, list_rows, f.totals + 3, st);
   k += exclusive_scan(f.rs_count, f.rs_base, f.num_cmds, scan_tmp, st);
   k += launch_total(f.rs_count, f.rs_base, f.num_cmds, f.totals + 4, st);
   k += exclusive_scan(f.rb_count, f.rb_base, f.num_cmds, scan_tmp, st);
@@ -773,6 +777,8 @@ BLGpuResult Runtime::run_graph(const Frame& fr) {
   L.base = static_cast<char*>(dyn_buf.ptr);
   plan_dynamic(L, view, caps.dyn);
   totals = caps.dyn;
+  view_by_caps = true;
+  planned_list_shift = list_shift_of(cfg);
   if (!graph_valid) {
     if (graph) cudaGraphExecDestroy(graph);
     graph = nullptr;
@@ -872,6 +878,8 @@ BLGpuResult Runtime::run_eager(const Frame& fr) {
   Layout L;
   L.base = static_cast<char*>(dyn_buf.ptr);
   plan_dynamic(L, view, totals);
+  view_by_caps = false;
+  planned_list_shift = list_shift_of(cfg);
   last_frame_bytes = in_bytes + stroke_bytes + measure.off + uint64_t(totals.segs) * (sizeof(DevSeg) + sizeof(uint32_t));
 
   launches += enqueue_render_half(stream, true);
@@ -945,11 +953,12 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     v.cmd_yr = L.take<uint32_t>(nc);
     a_cmdrow_per_cmd = L.take<uint32_t>(nc + 1);
     v.cmdrow_base = L.take<uint32_t>(nc + 1);
-    v.row_counts = L.take<uint32_t>(fr.rows + 1);
-    v.row_offsets = L.take<uint32_t>(fr.rows + 1);
-    v.row_copies = L.take<uint32_t>(fr.rows + 1);
+    const size_t list_rows = (size_t(fr.rows) << kMaxListLog2) + 1;
+    v.row_counts = L.take<uint32_t>(list_rows);
+    v.row_offsets = L.take<uint32_t>(list_rows);
+    v.row_copies = L.take<uint32_t>(list_rows);
     v.strip_start = L.take<uint32_t>((size_t(fr.tiles) + 1) * (kTileH / kStripRows));
-    a_row_canvas = L.take<uint32_t>(fr.rows + 1);
+    a_row_canvas = L.take<uint32_t>(list_rows);
     v.tile_order = L.take<uint32_t>(fr.tiles + 1);
     v.tile_canvas = L.take<uint32_t>(fr.tiles + 1);
     v.work_counter = L.take<uint32_t>(kCounterWords);
@@ -960,7 +969,7 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     v.rs_base = L.take<uint32_t>(nc + 1);
     v.rb_count = L.take<uint32_t>(nc + 1);
     v.rb_base = L.take<uint32_t>(nc + 1);
-    a_scan_tmp = L.take<uint32_t>(scan_temp_words(std::max(nc + 1, fr.rows + 1)));
+    a_scan_tmp = L.take<uint32_t>(scan_temp_words(std::max<uint32_t>(nc + 1, (fr.rows << kMaxListLog2) + 1)));
     v.counts = L.take<uint32_t>(kCntWords);
   };
   Layout L;
@@ -1057,9 +1066,38 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
 
 // Re-runs the last frame's device pipeline on its device-resident inputs and canvases (the
 // canvases keep what the previous run left in them). Asynchronous with respect to the host.
+BLGpuResult Runtime::resize_dynamic() {
+  BLGPU_CHECK(cudaSetDevice(device));
+  enqueue_count_half(stream);
+  BLGPU_CHECK(cudaGetLastError());
+  BLGPU_CHECK(cudaMemcpyAsync(host_totals, view.totals, 32, cudaMemcpyDeviceToHost, stream));
+  BLGPU_CHECK(cudaStreamSynchronize(stream));
+  BLGPU_CHECK(cudaStreamSynchronize(side));
+  FrameTotals t;
+  t.segs = host_totals[0]; t.seglist = host_totals[1]; t.cmdrows = host_totals[2];
+  t.row_entries = host_totals[3]; t.row_states = host_totals[4]; t.row_runs = host_totals[6];
+  FrameTotals plan_t = t;
+  if (view_by_caps) { raise_dyn(caps.dyn, t); plan_t = caps.dyn; }
+  Layout measure;
+  FrameView probe = view;
+  plan_dynamic(measure, probe, plan_t);
+  if (measure.off > dyn_buf.size) BLGPU_CHECK(dyn_buf.reserve(measure.off));
+  Layout L;
+  L.base = static_cast<char*>(dyn_buf.ptr);
+  plan_dynamic(L, view, plan_t);
+  totals = t;
+  planned_list_shift = list_shift_of(cfg);
+  graph_valid = false;
+  return BLGPU_SUCCESS;
+}
+
 BLGpuResult Runtime::replay(bool use_graph) {
   if (!has_frame) return BLGPU_ERROR_INVALID_STATE;
   BLGPU_CHECK(cudaSetDevice(device));
+  if (planned_list_shift != list_shift_of(cfg)) {
+    BLGpuResult r = resize_dynamic();
+    if (r) return r;
+  }
   if (!use_graph) {
     BLGPU_CHECK(cudaEventRecord(ev[0], stream));
     int launches = enqueue_count_half(stream);
@@ -1147,13 +1185,18 @@ BLGpuResult Runtime::autotune(int trials, LaunchConfig* best_out, double* best_m
   const int cover_slots[] = {0, 16, 32, 64};
   const int blocks[] = {0, 1, 2, 3};
   const int edge_blocks[] = {64, 128, 256};
-  for (int field = 0; field < 5 && !r; field++) {
-    const int* vals = field == 0 ? cover_slots : (field == 3 ? edge_blocks : blocks);
-    const int nvals = field == 0 ? 4 : (field == 3 ? 3 : 4);
+  const int list_rows[] = {32, 16, 8, 4};
+  // fields: list-row height (binning geometry of the composite), coverage slots per block (the
+  // band of slots a block rasterizes), coverage / composite / curve grids, edges per block
+  const int order[] = {5, 0, 1, 2, 3, 4};
+  for (int fi = 0; fi < 6 && !r; fi++) {
+    const int field = order[fi];
+    const int* vals = field == 0 ? cover_slots : field == 3 ? edge_blocks : field == 5 ? list_rows : blocks;
+    const int nvals = field == 3 ? 3 : 4;
     for (int k = 0; k < nvals && !r; k++) {
       LaunchConfig c = best;
       int* slot = field == 0 ? &c.cover_slots : field == 1 ? &c.cover_blocks_per_sm : field == 2 ? &c.fine_blocks_per_sm
-                : field == 3 ? &c.edge_block : &c.cubic_blocks_per_sm;
+                : field == 3 ? &c.edge_block : field == 4 ? &c.cubic_blocks_per_sm : &c.list_rows;
       if (*slot == vals[k]) continue;
       *slot = vals[k];
       double ms = 0.0;

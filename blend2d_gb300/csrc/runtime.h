@@ -224,6 +224,11 @@ struct Runtime {
   BLGpuResult run_eager(const Frame& fr);
   BLGpuResult run_graph(const Frame& fr);
   FrameSizes caps{};             // graph frames: capacities of the layout the graph was captured on
+  bool view_by_caps = false;     // the kept frame is laid out by `caps`
+  uint32_t planned_list_shift = 5;   // list-row height the kept frame's dynamic arrays were sized for
+  // Sizes the dynamic arrays of the kept frame again after a launch-config change that alters
+  // what the device computes (the list-row height): one counting half and a read-back.
+  BLGpuResult resize_dynamic();
   bool caps_ready = false;
   uint64_t graph_frames_run = 0; // frames that ran as a replay of the captured graph
   BLGpuResult replay(bool use_graph);

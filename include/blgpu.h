@@ -137,7 +137,10 @@ typedef struct BLGpuLaunchConfig {
                                    round trip inside the frame; a frame that does not fit grows the
                                    capacities and runs eagerly. Frames with strokes, or whose device
                                    targets are drawn in place onto existing content, run eagerly. */
-  int32_t reserved[2];
+  int32_t list_rows;            /* pixel rows per command list of the composite (4, 8, 16 or 32; 0 =
+                                   32): shorter lists hold fewer commands a strip must test, at the
+                                   cost of more list entries */
+  int32_t reserved[1];
 } BLGpuLaunchConfig;
 
 /* --- runtime (device, stream, memory) --------------------------------------------------- */

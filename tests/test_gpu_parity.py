@@ -359,6 +359,37 @@ def test_autotune_keeps_pixels_and_every_config_renders_the_same():
             rt.set_launch_config(bg.LaunchConfig(cover_slots=24, edge_block=128))
 
 
+def test_list_row_heights_render_the_same():
+    """The composite's command lists per 4, 8, 16 or 32 pixel rows (a tuning choice): every height
+    gives the oracle's pixels, for a frame run with it and for the kept frame replayed after the
+    height changed (its binning arrays are sized again)."""
+    torch = pytest.importorskip("torch")
+    w, h = 333, 211
+    stream = scenes.random_mix(778, width=w, height=h, count=300).to_bytes()
+    want = oracle_lib.render(stream)
+    batch = [scenes.random_mix(779 + i, width=90 + 40 * i, height=61 + 30 * i, count=80).to_bytes() for i in range(4)]
+    with bg.Runtime(0) as rt:
+        for rows in (4, 8, 16, 32):
+            rt.set_launch_config(bg.LaunchConfig(edge_block=128, list_rows=rows))
+            got = bg.render_stream(rt, stream)
+            assert not _diff(got, want), rows
+            targets = [np.zeros(oracle_lib.stream_size(s)[::-1], dtype=np.uint32) for s in batch]
+            rt.render_batch(batch, targets)
+            for s, t in zip(batch, targets):
+                assert not _diff(t, oracle_lib.render(s)), rows
+        dev = torch.zeros((h, w), dtype=torch.int32, device="cuda")
+        rt.set_launch_config(bg.LaunchConfig(edge_block=128, list_rows=32))
+        bg.render_stream(rt, stream, dev)
+        for rows in (8, 4, 16):
+            rt.set_launch_config(bg.LaunchConfig(edge_block=128, list_rows=rows))
+            dev.zero_()
+            torch.cuda.synchronize()
+            rt.replay(False)                   # the canvas is a device image: the replay redraws it
+            rt.synchronize()
+            torch.cuda.synchronize()
+            assert not _diff(dev.cpu().numpy().view(np.uint32), want), rows
+
+
 @pytest.mark.parametrize("variant,dither", [("default", False), ("avx2", False), ("scalar", False),
                                             ("default", True)])
 def test_gradients_with_many_stops(runtimes, variant, dither):
@@ -688,9 +719,10 @@ def test_graph_frames_replay_new_frames_bit_exact():
             want = oracle_lib.render(s)
             assert not _diff(got, want), f"frame {i}: {_diff(got, want)}"
         assert rt.stats().graph_frames >= 5       # the frames that fit replayed the graph
-        # batches of different canvases through the same graph
+        # batches of different canvases through the same graph (the first one twice: once to
+        # grow the layout to batch size, once through the graph for certain)
         before = rt.stats().graph_frames
-        for k in range(3):
+        for k in (0, 0, 1, 2):
             sws = scenes.batch_canvases(seed=500 + k, count=12, max_side=300, max_paths=150)
             streams = [sw.to_bytes() for sw in sws]
             targets = [np.zeros((sw.height, sw.width), dtype=np.uint32) for sw in sws]
