@@ -80,8 +80,9 @@ def parse_args(argv=None):
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="headline", choices=["headline", "batch", "frame", "serving"],
-                    help="headline: batch line with frame and serving records; batch / frame / serving alone")
+    ap.add_argument("--mode", default="headline", choices=["headline", "batch", "frame", "serving", "profile"],
+                    help="headline: batch line with frame and serving records; batch / frame / serving alone; "
+                         "profile: the first --batch-count canvases rendered twice and replayed once, for profilers")
     ap.add_argument("--workload", default="curves", choices=sorted(FRAMES), help="frame workload (--mode frame)")
     ap.add_argument("--batch-count", type=int, default=4096, help="canvases of the batched workload")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="bounded CPU-baseline sample of the frame (seconds)")
@@ -461,29 +462,59 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
 
     # ---- e2e through the public API: host streams, pinned host canvases, one pipeline per step.
     # One eager step first (every array sized from the frame, a host read-back between the
-    # halves), for reference; then graph frames: the steps upload their data in place and replay
-    # one captured graph (the first warm-up step learns the capacities).
+    # halves), for reference. Then two runtimes (each its own stream, arenas and pinned canvases)
+    # take the steps in turn from two host threads with graph frames (a step's data is uploaded in
+    # place and one captured graph replayed), so a step's host recording overlaps the device work
+    # of the step before; every step's upload, render and read-back is inside the timed region.
+    import threading
     rt.render_batch(streams, targets)
+    # launch shapes and the command-list row height chosen by the autotuner on this batch
+    tuned, tuned_ms = rt.autotune(trials=1)
+    log(f"batch: autotuned {tuned.as_dict()} ({tuned_ms:.1f} ms)")
     t0 = time.perf_counter()
     rt.render_batch(streams, targets)
     eager_step_s = time.perf_counter() - t0
     cfg0 = rt.launch_config()
-    rt.set_launch_config(bg.LaunchConfig(**{**cfg0.as_dict(), "graph_frames": 1}))
-    for _ in range(args.warmup):
-        rt.render_batch(streams, targets)
-    g0 = int(rt.stats().graph_frames)
+    graph_cfg = bg.LaunchConfig(**{**cfg0.as_dict(), "graph_frames": 1})
+    rt2 = bg.Runtime(local)
+    rts = [rt, rt2]
+    tgts = [targets, [pinned_canvas(h, w) for h, w in shapes]]
+    for r_ in rts:
+        r_.set_launch_config(graph_cfg)
+
+    def e2e_steps(count):
+        errors = []
+
+        def worker(k):
+            try:
+                for _ in range(k, count, 2):
+                    rts[k].render_batch(streams, tgts[k])
+            except Exception as e:      # re-raised on the main thread
+                errors.append(e)
+        ths = [threading.Thread(target=worker, args=(k,)) for k in range(2)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        if errors:
+            raise errors[0]
+
+    e2e_steps(max(args.warmup, 4))
+    g0 = sum(int(r_.stats().graph_frames) for r_ in rts)
     dist.barrier()
     clocks = ClockSampler(local).start()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        rt.render_batch(streams, targets)
+    e2e_steps(args.steps)
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e_clocks = clocks.stop()
-    graph_steps = int(rt.stats().graph_frames) - g0
+    graph_steps = sum(int(r_.stats().graph_frames) for r_ in rts) - g0
     log(f"batch: e2e {e2e_s * 1e3 / args.steps:.1f} ms/step ({graph_steps} graph frames), eager step {eager_step_s * 1e3:.1f} ms")
     st = rt.stats()
     h2d, d2h = int(st.h2d_bytes), int(st.d2h_bytes)
     batch_dev_ms = float(st.last_gpu_ms)
+    mismatched2 = [i for i, (a, b) in enumerate(zip(tgts[0], tgts[1])) if not np.array_equal(a.numpy(), b.numpy())]
+    rt2.close()
+    del tgts[1][:]
     rt.set_launch_config(cfg0)
     rt.render_batch(streams, targets)       # the eager frame the replays below time
 
@@ -511,6 +542,7 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
     single_clocks = clocks.stop()
     log(f"batch: per-canvas pass {single_s:.1f} s")
     mismatched = [i for i, (a, t) in enumerate(zip(batched, targets)) if not np.array_equal(a, t.numpy().view(np.uint32))]
+    mismatched += [i for i in mismatched2 if i not in mismatched]
 
     # ---- parity of a 64-canvas sample against the oracle (and the golden reference hashes)
     sample = batch_sample(n)
@@ -536,7 +568,8 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
         "vs_baseline": None, "dtype": DTYPE, "data": "synthetic", "config": cfg,
         "e2e": {"value": round(world * args.steps * mpix / e2e_s, 3), "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_s * 1e3 / args.steps, 3), "clocks": e2e_clocks,
-                "graph_frames": graph_steps, "eager_ms_per_step": round(eager_step_s * 1e3, 3)},
+                "graph_frames": graph_steps, "eager_ms_per_step": round(eager_step_s * 1e3, 3),
+                "pipelining": "two runtimes take the steps in turn from two host threads"},
         "gpu_launches": launches,
         "clocks": dev_clocks,
         "roofline": roof,
@@ -556,6 +589,7 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
             "speedup_device": round(dev_sum / (total_s * 1e3 / args.steps), 2),
             "speedup_device_graph": round(dev_sum / g_ms, 2),
             "stream_generation_s": round(gen_s, 2),
+            "autotuned_config": {k: v for k, v in tuned.as_dict().items() if k not in ("graph_frames", "max_segments")},
         },
     }
     if cpu:
@@ -731,6 +765,35 @@ def serving_record(args, local) -> dict:
             "clocks": clock_info, "parity": "bit-exact" if not bad else "; ".join(bad[:6])}
 
 
+def run_profile(args) -> int:
+    """A short, single-process run for profilers: the first --batch-count canvases of the batched
+    workload (generated in this process) rendered twice through blgpu_render_batch, then the
+    batch's device pipeline replayed once; prints the device times."""
+    import numpy as np
+
+    import blend2d_gb300 as bg
+    from blend2d_gb300 import scenes
+
+    n = args.batch_count
+    streams = [scenes.batch_canvas(i, seed=BATCH_SEED, count=4096).to_bytes() for i in range(n)]
+    shapes = [tuple(int(v) for v in np.frombuffer(s[8:16], dtype="<u4"))[::-1] for s in streams]
+    targets = [np.zeros(sh, dtype=np.uint32) for sh in shapes]
+    out = {"canvases": n}
+    with bg.Runtime(0) as rt:
+        for k in range(2):
+            rt.render_batch(streams, targets)
+        st = rt.stats()
+        out.update(device_ms=round(st.last_gpu_ms, 3), launches=int(st.kernel_launches), segments=int(st.segments),
+                   pixel_ops=int(st.pixel_ops))
+        rt.replay(False)
+        rt.synchronize()
+        st = rt.stats()
+        out.update(replay_ms=round(st.last_gpu_ms, 3), fine_ms=round(st.last_fine_ms, 3),
+                   composite_ms=round(st.last_composite_ms, 3))
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_ours(args) -> int:
     import torch
 
@@ -809,6 +872,8 @@ def main(argv=None) -> int:
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "profile":
+        return run_profile(args)
     return run_ours(args)
 
 
