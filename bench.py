@@ -508,6 +508,10 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e_clocks = clocks.stop()
     graph_steps = sum(int(r_.stats().graph_frames) for r_ in rts) - g0
+    stb = rt.stats()
+    host_split = {"record_ms": round(stb.last_record_ms, 2), "merge_ms": round(stb.last_merge_ms, 2),
+                  "upload_ms": round(stb.last_upload_ms, 2), "run_ms": round(stb.last_run_ms, 2)}
+    log(f"batch: last step host split {host_split}")
     log(f"batch: e2e {e2e_s * 1e3 / args.steps:.1f} ms/step ({graph_steps} graph frames), eager step {eager_step_s * 1e3:.1f} ms")
     st = rt.stats()
     h2d, d2h = int(st.h2d_bytes), int(st.d2h_bytes)
@@ -569,7 +573,8 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
         "e2e": {"value": round(world * args.steps * mpix / e2e_s, 3), "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_s * 1e3 / args.steps, 3), "clocks": e2e_clocks,
                 "graph_frames": graph_steps, "eager_ms_per_step": round(eager_step_s * 1e3, 3),
-                "pipelining": "two runtimes take the steps in turn from two host threads"},
+                "pipelining": "two runtimes take the steps in turn from two host threads",
+                "host_split_of_a_step": host_split},
         "gpu_launches": launches,
         "clocks": dev_clocks,
         "roofline": roof,
@@ -781,10 +786,14 @@ def run_profile(args) -> int:
     out = {"canvases": n}
     with bg.Runtime(0) as rt:
         for k in range(2):
+            t0 = time.perf_counter()
             rt.render_batch(streams, targets)
+            wall = time.perf_counter() - t0
         st = rt.stats()
         out.update(device_ms=round(st.last_gpu_ms, 3), launches=int(st.kernel_launches), segments=int(st.segments),
-                   pixel_ops=int(st.pixel_ops))
+                   pixel_ops=int(st.pixel_ops), host_call_ms=round(wall * 1e3, 3), record_ms=round(st.last_record_ms, 3),
+                   merge_ms=round(st.last_merge_ms, 3), upload_ms=round(st.last_upload_ms, 3),
+                   run_ms=round(st.last_run_ms, 3))
         rt.replay(False)
         rt.synchronize()
         st = rt.stats()

@@ -101,7 +101,9 @@ class Stats(ctypes.Structure):
                 ("last_fine_ms", ctypes.c_double), ("pixel_ops", ctypes.c_uint64), ("pattern_ops", ctypes.c_uint64),
                 ("input_vertices", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
                 ("last_cuda_error", ctypes.c_int64), ("last_composite_ms", ctypes.c_double),
-                ("graph_frames", ctypes.c_uint64)]
+                ("graph_frames", ctypes.c_uint64), ("last_record_ms", ctypes.c_double),
+                ("last_merge_ms", ctypes.c_double), ("last_upload_ms", ctypes.c_double),
+                ("last_run_ms", ctypes.c_double)]
 
 
 _P = ctypes.c_void_p

@@ -13,6 +13,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <deque>
 #include <condition_variable>
 #include <memory>
@@ -1514,6 +1515,7 @@ BLGPU_API BLGpuResult blgpu_render_batch(BLGpuRuntime* rt, const void* const* st
     }
   }
   std::vector<BLGpuResult> errors(nt, BLGPU_SUCCESS);
+  const auto t_record = std::chrono::steady_clock::now();
   auto record = [&](unsigned t) {
     Frame& part = nt == 1 ? frame : *rt->batch_parts[t];
     part.clear();
@@ -1544,10 +1546,17 @@ BLGPU_API BLGpuResult blgpu_render_batch(BLGpuRuntime* rt, const void* const* st
   }
   for (BLGpuResult r : errors)      // the first failing canvas's error, as sequential recording gives
     if (r) return r;
+  const auto t_merge = std::chrono::steady_clock::now();
   if (nt > 1) {
     std::vector<Frame*> parts(nt);
     for (unsigned t = 0; t < nt; t++) parts[t] = rt->batch_parts[t].get();
     frame.merge(parts.data(), nt, nt);
+  }
+  const auto t_end = std::chrono::steady_clock::now();
+  {
+    std::lock_guard<std::mutex> e(rt->exec);
+    rt->rt.stats.last_record_ms = std::chrono::duration<double, std::milli>(t_merge - t_record).count();
+    rt->rt.stats.last_merge_ms = std::chrono::duration<double, std::milli>(t_end - t_merge).count();
   }
   if (frame.cmds.empty()) return BLGPU_SUCCESS;
   BLGpuContext::mark_uploads(frame);

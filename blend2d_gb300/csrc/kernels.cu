@@ -452,10 +452,15 @@ __device__ __forceinline__ void finish_curve(FrameView& f, eb::Builder& b, uint3
   }
 }
 
-// The lanes' subdivision stacks live in local memory with the top entry in registers
-// (eb::CachedStack): the piece kernel is bound by the FP64 pipe and the latency of its stack, and
-// needs every resident warp, so the stacks stay out of shared memory.
+// The lanes' subdivision stacks keep their top entry in registers and the next kPieceStackShared
+// entries in shared memory (eb::SharedStack), deeper ones in local memory: the piece kernel waits
+// on its stack otherwise (long-scoreboard stalls on local memory).
 constexpr int kCurveThreads = 128;
+constexpr int kPieceStackShared = 8;
+template<int DEG>
+using PieceStack = eb::SharedStack<DEG, kPieceStackShared>;
+template<int DEG>
+constexpr size_t piece_stack_bytes() { return size_t(PieceStack<DEG>::kSharedDoubles) * kCurveThreads * sizeof(double); }
 constexpr int kPieceRefillLanes = 16;
 
 // Curves in two kernels. curve_split_kernel<DEG>: one thread per curve of the curve list does
@@ -541,8 +546,10 @@ __global__ void __launch_bounds__(kCurveThreads) edge_pieces_kernel(FrameView f)
   const uint32_t n_cubic = min(f.work_counter[23], f.piece_capacity);
   const uint32_t n_items = DEG == 3 ? n_cubic : min(f.work_counter[25], f.piece_capacity - n_cubic);
   uint32_t* queue = f.work_counter + (DEG == 3 ? 24 : 26);
+  extern __shared__ double piece_stacks[];
   eb::Builder b;
-  eb::LaneCurve<DEG, eb::CachedStack<DEG>> lc;
+  eb::LaneCurve<DEG, PieceStack<DEG>> lc;
+  lc.mc.stack.init(piece_stacks + threadIdx.x, kCurveThreads);
   bool busy = false, exhausted = false;
   uint32_t cur = 0, rows = 0;
 
@@ -1510,16 +1517,16 @@ static int device_sms() {
   return v;
 }
 template<typename K>
-static int max_blocks_per_sm(K kernel, int threads) {
+static int max_blocks_per_sm(K kernel, int threads, size_t dyn_smem = 0) {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, dyn_smem);
   return n > 0 ? n : 1;
 }
 
 int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   if (!f.num_cmds) return 0;
   const int sms = device_sms();
-  static const int max_per_sm = max_blocks_per_sm(edge_pieces_kernel<3>, kCurveThreads);
+  static const int max_per_sm = max_blocks_per_sm(edge_pieces_kernel<3>, kCurveThreads, piece_stack_bytes<3>());
   const int per_sm = cfg.cubic_blocks_per_sm > 0 && cfg.cubic_blocks_per_sm < max_per_sm ? cfg.cubic_blocks_per_sm : max_per_sm;
   const uint32_t eb = cfg.edge_block == 64 || cfg.edge_block == 256 ? uint32_t(cfg.edge_block) : 128u;
   classify_kernel<<<cdiv(f.num_cmds, 128), 128, 0, st>>>(f);
@@ -1530,8 +1537,8 @@ int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   curve_split_kernel<2><<<split_grid, 128, 0, st>>>(f);
   const uint32_t pgrid = cdiv(f.piece_capacity ? f.piece_capacity : 1, kCurveThreads);
   const uint32_t pieces_grid = pgrid < cubic_grid ? pgrid : cubic_grid;
-  edge_pieces_kernel<3><<<pieces_grid, kCurveThreads, 0, st>>>(f);
-  edge_pieces_kernel<2><<<pieces_grid, kCurveThreads, 0, st>>>(f);
+  edge_pieces_kernel<3><<<pieces_grid, kCurveThreads, piece_stack_bytes<3>(), st>>>(f);
+  edge_pieces_kernel<2><<<pieces_grid, kCurveThreads, piece_stack_bytes<2>(), st>>>(f);
   return 6;
 }
 

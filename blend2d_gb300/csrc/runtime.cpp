@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <thread>
 
 #include "launch.h"
@@ -405,7 +406,7 @@ FrameSizes sizes_of(const Frame& fr, uint32_t outline_verts) {
   return z;
 }
 
-BLGpuResult Runtime::upload(const Frame& fr, const FrameSizes* caps) {
+BLGpuResult Runtime::upload_frame(const Frame& fr, const FrameSizes* caps) {
   const uint32_t ncv = uint32_t(fr.canvases.size());
   h2d_bytes = 0;
   d2h_bytes = 0;
@@ -703,7 +704,25 @@ BLGpuResult Runtime::download() {
   return BLGPU_SUCCESS;
 }
 
+static double ms_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
 BLGpuResult Runtime::run(const Frame& fr) {
+  const auto t0 = std::chrono::steady_clock::now();
+  BLGpuResult r = run_frame(fr);
+  stats.last_run_ms = ms_since(t0);
+  return r;
+}
+
+BLGpuResult Runtime::upload(const Frame& fr, const FrameSizes* caps) {
+  const auto t0 = std::chrono::steady_clock::now();
+  BLGpuResult r = upload_frame(fr, caps);
+  stats.last_upload_ms = ms_since(t0);
+  return r;
+}
+
+BLGpuResult Runtime::run_frame(const Frame& fr) {
   if (cfg.graph_frames && fr.stroke_figs.empty()) {
     // a graph frame that does not fit is re-run eagerly, so its device targets must be redrawable:
     // either copied (host targets, unaligned device rows) or overwritten by the frame's first fill

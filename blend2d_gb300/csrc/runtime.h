@@ -221,6 +221,7 @@ struct Runtime {
   // With cfg.graph_frames the frame runs as a captured graph over capacity-sized arrays when it
   // can (run_graph); otherwise eagerly, every array sized from the frame (run_eager).
   BLGpuResult run(const Frame& fr);
+  BLGpuResult run_frame(const Frame& fr);
   BLGpuResult run_eager(const Frame& fr);
   BLGpuResult run_graph(const Frame& fr);
   FrameSizes caps{};             // graph frames: capacities of the layout the graph was captured on
@@ -249,6 +250,7 @@ struct Runtime {
   cudaError_t put_counts(const Frame& fr, uint32_t* dev);
   // Uploads `fr` into a layout sized by the frame itself, or by `caps` (graph frames).
   BLGpuResult upload(const Frame& fr, const FrameSizes* caps = nullptr);
+  BLGpuResult upload_frame(const Frame& fr, const FrameSizes* caps);
   BLGpuResult download();
   BLGpuResult reserve_segments(uint32_t count);
   void read_pixel_ops();

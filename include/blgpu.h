@@ -115,6 +115,10 @@ typedef struct BLGpuStats {
   int64_t last_cuda_error; /* cudaError_t behind the last BLGPU_ERROR_DEVICE (0 if none) */
   double last_composite_ms;/* ... of which the composite kernel */
   uint64_t graph_frames;   /* frames that ran as a replay of the captured graph (graph_frames launch config) */
+  double last_record_ms;   /* host time of the last blgpu_render_batch's recording (all threads) */
+  double last_merge_ms;    /* ... of merging its threads' frame parts */
+  double last_upload_ms;   /* host time of the last frame's upload call (staging, copies enqueued) */
+  double last_run_ms;      /* host time of the last frame's run: upload, pipeline, read-back */
 } BLGpuStats;
 
 /* Launch shapes of the device pipeline (0 in a *_blocks_per_sm field = as many as fit). Tile and
