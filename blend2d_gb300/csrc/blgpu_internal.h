@@ -164,6 +164,15 @@ struct DevSeg {            // one non-horizontal 24.8 segment, y0 < y1
 
 enum ItemKind : uint32_t { kItemLine = 0, kItemQuad = 1, kItemCubic = 2, kItemConic = 3, kItemWhole = 4 };
 
+// A canvas copied between the runtime's canvas pool and a page-locked host image by a kernel (the
+// device reaches page-locked memory directly): rows of w pixels, strides in pixels.
+struct DevXfer {
+  uint32_t* dev;
+  uint32_t* host;              // the host image's device-accessible address
+  int32_t w, h;
+  int32_t dev_stride, host_stride;
+};
+
 // One line, curve or closing line of an analytic command, built independently of the command's
 // other items. Vertex indices are relative to geom_first.
 struct DevItem {
@@ -275,7 +284,10 @@ struct FrameView {
                                //   from segments entirely left of it (cover << 9 per row)
   uint32_t* row_counts;        // [num_rows + 1]
   uint32_t* row_offsets;
-  uint32_t* row_cmds;          // command indices grouped by tile row, painter's order
+  uint4* row_recs;             // command lists per list row, painter's order: two records per entry,
+                               //   {command, pixel columns x0 | x1 << 16, rows y0 | y1 << 16, meta}
+                               //   {first slot, tile column tx0 | columns << 16, style, first row state}
+                               //   with meta = kind | flags << 2 | alpha << 4
   uint32_t* row_copies;        // [num_rows] SrcCopy commands in each tile row's list
   uint32_t* strip_start;       // [num_tiles * strips per tile] first list entry the composite needs (occlusion)
   uint32_t* tile_order;        // tile processing order for the persistent fine kernel

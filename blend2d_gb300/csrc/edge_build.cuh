@@ -596,46 +596,6 @@ struct CachedStack {
   }
 };
 
-// The same with the entries under the top held in shared memory down to LS levels (one column of
-// doubles per thread, so a warp's accesses are conflict-free whatever level each lane is at) and in
-// local memory below that (subdivisions of the canvases' curves rarely go that deep).
-template<int DEG, int LS>
-struct SharedStack {
-  Pt top[DEG];
-  double* col;                 // this thread's column: element i at col[i * stride]
-  int stride;
-  Pt deep[kStackLevels - LS][DEG];
-  static constexpr int kSharedDoubles = LS * DEG * 2;   // per thread
-  __device__ __forceinline__ void init(double* column, int col_stride) { col = column; stride = col_stride; }
-  __device__ __forceinline__ void put(int e, int k, Pt v) {
-    if (e < LS) {
-      col[((e * DEG + k) * 2) * stride] = v.x;
-      col[((e * DEG + k) * 2 + 1) * stride] = v.y;
-    }
-    else {
-      deep[e - LS][k] = v;
-    }
-  }
-  __device__ __forceinline__ Pt get(int e, int k) const {
-    if (e < LS) return Pt{col[((e * DEG + k) * 2) * stride], col[((e * DEG + k) * 2 + 1) * stride]};
-    return deep[e - LS][k];
-  }
-  __device__ __forceinline__ void push(int lvl, const Pt* v) {
-#pragma unroll
-    for (int k = 0; k < DEG; k++) {
-      if (lvl > 0) put(lvl - 1, k, top[k]);
-      top[k] = v[k];
-    }
-  }
-  __device__ __forceinline__ void pop(int lvl, Pt* v) {
-#pragma unroll
-    for (int k = 0; k < DEG; k++) {
-      v[k] = top[k];
-      if (lvl > 0) top[k] = get(lvl - 1, k);
-    }
-  }
-};
-
 // Monotonic curve with an explicit subdivision stack (FlattenMonoQuad / FlattenMonoCubic).
 template<int DEG, class S = LocalStack<DEG>>
 struct Mono {

@@ -452,15 +452,11 @@ __device__ __forceinline__ void finish_curve(FrameView& f, eb::Builder& b, uint3
   }
 }
 
-// The lanes' subdivision stacks keep their top entry in registers and the next kPieceStackShared
-// entries in shared memory (eb::SharedStack), deeper ones in local memory: the piece kernel waits
-// on its stack otherwise (long-scoreboard stalls on local memory).
+// The lanes' subdivision stacks live in local memory with the top entry in registers
+// (eb::CachedStack). Holding the next eight entries in shared memory instead measured slower on
+// the batched workload (piece kernel 10.8 -> 14.2 ms): the shared-memory carve-out shrinks the L1
+// that the stacks' and the segment sinks' local memory hits in.
 constexpr int kCurveThreads = 128;
-constexpr int kPieceStackShared = 8;
-template<int DEG>
-using PieceStack = eb::SharedStack<DEG, kPieceStackShared>;
-template<int DEG>
-constexpr size_t piece_stack_bytes() { return size_t(PieceStack<DEG>::kSharedDoubles) * kCurveThreads * sizeof(double); }
 constexpr int kPieceRefillLanes = 16;
 
 // Curves in two kernels. curve_split_kernel<DEG>: one thread per curve of the curve list does
@@ -546,10 +542,8 @@ __global__ void __launch_bounds__(kCurveThreads) edge_pieces_kernel(FrameView f)
   const uint32_t n_cubic = min(f.work_counter[23], f.piece_capacity);
   const uint32_t n_items = DEG == 3 ? n_cubic : min(f.work_counter[25], f.piece_capacity - n_cubic);
   uint32_t* queue = f.work_counter + (DEG == 3 ? 24 : 26);
-  extern __shared__ double piece_stacks[];
   eb::Builder b;
-  eb::LaneCurve<DEG, PieceStack<DEG>> lc;
-  lc.mc.stack.init(piece_stacks + threadIdx.x, kCurveThreads);
+  eb::LaneCurve<DEG, eb::CachedStack<DEG>> lc;
   bool busy = false, exhausted = false;
   uint32_t cur = 0, rows = 0;
 
@@ -895,6 +889,27 @@ __global__ void backdrop_prefix_kernel(FrameView f) {
   }
 }
 
+// Canvas transfers with page-locked host images: one block column per canvas, one warp per row,
+// 4-byte words across the lanes. One launch moves every canvas of a frame, with any strides on
+// either side (a DMA copy per canvas pays a per-row cost on the many short rows of small canvases).
+__global__ void __launch_bounds__(256) canvas_copy_kernel(const DevXfer* xfers, uint32_t n, int to_host) {
+  const uint32_t i = blockIdx.x;
+  if (i >= n) return;
+  const DevXfer t = xfers[i];
+  const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+  for (int y = int(blockIdx.y) * warps + (threadIdx.x >> 5); y < t.h; y += int(gridDim.y) * warps) {
+    const uint32_t* src = to_host ? t.dev + int64_t(y) * t.dev_stride : t.host + int64_t(y) * t.host_stride;
+    uint32_t* dst = to_host ? t.host + int64_t(y) * t.host_stride : t.dev + int64_t(y) * t.dev_stride;
+    for (int x = lane; x < t.w; x += 32) dst[x] = src[x];
+  }
+}
+
+int launch_canvas_copy(const DevXfer* xfers, uint32_t n, int to_host, cudaStream_t st) {
+  if (!n) return 0;
+  canvas_copy_kernel<<<dim3(n, 16), 256, 0, st>>>(xfers, n, to_host);
+  return 1;
+}
+
 int launch_frame_gate(const FrameView& f, cudaStream_t st) {
   frame_gate_kernel<<<1, 1, 0, st>>>(f);
   return 1;
@@ -926,7 +941,17 @@ __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
     }
     uint32_t total;
     uint32_t pos = block_exclusive_scan(flag, smem, total);
-    if (flag) f.row_cmds[out + pos] = c;
+    if (flag) {
+      // everything the composite needs of the command to test it against a strip and find its
+      // slot, gathered once here for every strip of the list row
+      const DevCmd& cmd = f.cmds[c];
+      const uint32_t ctx = f.cmd_tile_x[c];
+      const uint32_t meta = cmd.kind | (cmd.flags << 2) | (cmd.alpha << 4);
+      uint4* rec = f.row_recs + 2u * (out + pos);
+      rec[0] = make_uint4(c, f.cmd_xr[c], f.cmd_yr[c], meta);
+      rec[1] = make_uint4(f.cmdrow_base[c], (ctx & 0xFFFFu) | (((ctx >> 16) - (ctx & 0xFFFFu) + 1u) << 16), cmd.style,
+                          f.rs_base[c]);
+    }
     out += total;
   }
   uint32_t total_copies;
@@ -1106,12 +1131,12 @@ __device__ __forceinline__ void strip_masks(const FrameView& f, uint32_t ckind, 
   }
 }
 
-// Slot of analytic command c in strip row `strip_row`, tile column tx, and its mask index + 1
-// (0: no segment reaches it).
-__device__ __forceinline__ uint32_t strip_slot(const FrameView& f, uint32_t c, uint32_t strip_row, int tx, uint32_t& nseg) {
-  const uint32_t ctx = f.cmd_tile_x[c];
-  const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
-  const uint32_t slot = f.cmdrow_base[c] + (strip_row - ((f.cmd_yr[c] & 0xFFFFu) >> kStripShift)) * ntx + (uint32_t(tx) - (ctx & 0xFFFFu));
+// Slot of an analytic command in strip row `strip_row`, tile column tx, from its list records
+// (first slot, tx0 | columns << 16, rows y0 | y1 << 16), and its mask index + 1 (0: no segment
+// reaches it).
+__device__ __forceinline__ uint32_t strip_slot(const FrameView& f, uint32_t slot0, uint32_t tcols, uint32_t yr,
+                                               uint32_t strip_row, int tx, uint32_t& nseg) {
+  const uint32_t slot = slot0 + (strip_row - ((yr & 0xFFFFu) >> kStripShift)) * (tcols >> 16) + (uint32_t(tx) - (tcols & 0xFFFFu));
   nseg = f.slot_mask[slot];
   return slot;
 }
@@ -1150,26 +1175,30 @@ __global__ void __launch_bounds__(kFineThreads) cull_kernel(FrameView f) {
     const uint32_t strip_x = uint32_t(x_base) | (uint32_t(min(x_base + kTileW, cv.w) - 1) << 16);
     uint32_t start = 0;
     for (int cb = int((list_count - 1u) & ~31u); cb >= 0; cb -= 32) {
-      uint32_t c = 0;
+      uint4 ra = make_uint4(0u, 0u, 0u, 0u), rb = ra;
       bool cand = false;
       if (uint32_t(cb + lane) < list_count) {
-        c = f.row_cmds[list_first + uint32_t(cb + lane)];
-        const uint32_t bx = f.cmd_xr[c], by = f.cmd_yr[c];
+        const uint4* rec = f.row_recs + 2u * (list_first + uint32_t(cb + lane));
+        ra = rec[0];
+        rb = rec[1];
+        const uint32_t bx = ra.y, by = ra.z;
         cand = (bx & 0xFFFFu) <= (strip_x & 0xFFFFu) && (bx >> 16) >= (strip_x >> 16) &&
                (by & 0xFFFFu) <= (strip_y & 0xFFFFu) && (by >> 16) >= (strip_y >> 16) &&
-               (f.cmds[c].flags & 1u) && f.cmds[c].alpha == 255u;
+               ((ra.w >> 2) & 1u) && (ra.w >> 4) == 255u;
       }
       uint32_t todo = __ballot_sync(0xFFFFFFFFu, cand);
       bool found = false;
       while (todo) {
         const int bit = 31 - __clz(todo);
         todo &= ~(1u << bit);
-        const uint32_t ci = __shfl_sync(0xFFFFFFFFu, c, bit);
-        const uint32_t ckind = f.cmds[ci].kind;
-        const uint32_t cmeta = (f.cmds[ci].flags << 16) | f.cmds[ci].alpha;
+        const uint32_t ci = __shfl_sync(0xFFFFFFFFu, ra.x, bit);
+        const uint32_t rmeta = __shfl_sync(0xFFFFFFFFu, ra.w, bit);
+        const uint32_t ckind = rmeta & 3u;
+        const uint32_t cmeta = (((rmeta >> 2) & 3u) << 16) | (rmeta >> 4);
         uint32_t cnseg = 0, mw = 0;
         if (ckind == kFillAnalytic) {
-          const uint32_t slot = strip_slot(f, ci, strip_row, tx, cnseg);
+          const uint32_t slot = strip_slot(f, __shfl_sync(0xFFFFFFFFu, rb.x, bit), __shfl_sync(0xFFFFFFFFu, rb.y, bit),
+                                           __shfl_sync(0xFFFFFFFFu, ra.z, bit), strip_row, tx, cnseg);
           mw = cnseg ? reinterpret_cast<const uint32_t*>(f.masks + size_t(cnseg - 1u) * kSlotPixels)[lane]
                      : f.backdrop[size_t(slot) * kStripRows + prow];
         }
@@ -1236,25 +1265,27 @@ __global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
     const uint32_t start = f.strip_start[unit];      // cull_kernel
 
     for (uint32_t base = start & ~31u; base < list_count; base += 32) {
-      // commands of this chunk whose pixel bbox overlaps the strip, in painter's order
-      uint32_t c = 0;
+      // commands of this chunk whose pixel bbox overlaps the strip, in painter's order: one pair
+      // of list records per lane holds everything the tests and the slot lookup need
+      uint4 ra = make_uint4(0u, 0u, 0u, 0u), rb = ra;
       bool hit = false;
       if (base + lane < list_count && base + lane >= start) {
-        c = f.row_cmds[list_first + base + lane];
-        uint32_t bx = f.cmd_xr[c], by = f.cmd_yr[c];
+        const uint4* rec = f.row_recs + 2u * (list_first + base + lane);
+        ra = rec[0];
+        rb = rec[1];
+        const uint32_t bx = ra.y, by = ra.z;
         hit = (bx & 0xFFFFu) <= (strip_x >> 16) && (bx >> 16) >= (strip_x & 0xFFFFu) &&
               (by & 0xFFFFu) <= (strip_y >> 16) && (by >> 16) >= (strip_y & 0xFFFFu);
       }
       const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, hit);
       if (!ballot) continue;
-      // Each hit lane fetches its command's metadata in parallel (one command per lane), so the
+      // Each hit lane looks up its command's slot in parallel (one command per lane), so the
       // painter's-order loop below only waits on the mask words.
       uint32_t kind = 0, slot = 0xFFFFFFFFu, nseg = 0, meta = 0;   // meta: flags << 16 | alpha
       if (hit) {
-        const DevCmd& hc = f.cmds[c];
-        kind = hc.kind;
-        meta = (hc.flags << 16) | hc.alpha;
-        if (kind == kFillAnalytic) slot = strip_slot(f, c, strip_row, tx, nseg);
+        kind = ra.w & 3u;
+        meta = (((ra.w >> 2) & 3u) << 16) | (ra.w >> 4);
+        if (kind == kFillAnalytic) slot = strip_slot(f, rb.x, rb.y, ra.z, strip_row, tx, nseg);
       }
       uint32_t todo = ballot;
       // the first command's mask word, then each next one's while the current one composites
@@ -1268,10 +1299,13 @@ __global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
       }
       while (todo) {
         todo &= todo - 1;
-        const uint32_t ci = __shfl_sync(0xFFFFFFFFu, c, bit);
+        const uint32_t ci = __shfl_sync(0xFFFFFFFFu, ra.x, bit);
         const uint32_t ckind = __shfl_sync(0xFFFFFFFFu, kind, bit);
         const uint32_t cmeta = __shfl_sync(0xFFFFFFFFu, meta, bit);
         const uint32_t cnseg = __shfl_sync(0xFFFFFFFFu, nseg, bit);
+        const uint32_t cstyle = __shfl_sync(0xFFFFFFFFu, rb.z, bit);
+        const uint32_t crs = __shfl_sync(0xFFFFFFFFu, rb.w, bit);
+        const uint32_t cy0 = __shfl_sync(0xFFFFFFFFu, ra.z, bit) & 0xFFFFu;
         const uint32_t mw = next_mw;
         if (todo) {
           const int nb = __ffs(todo) - 1;
@@ -1286,11 +1320,11 @@ __global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
 
         if (row_ok && (m[0] | m[1] | m[2] | m[3])) {
           const DevCmd& cmd = f.cmds[ci];
-          const DevStyle& st = f.styles[cmd.style];
+          const DevStyle& st = f.styles[cstyle];
           const bool src_copy = (cmeta >> 16) & 1u;
           px::RowState rs;
           if (px::has_row_table(st.fetch)) {
-            const float4 t4 = f.row_states[f.rs_base[ci] + uint32_t(y - int(f.cmd_yr[ci] & 0xFFFFu))];
+            const float4 t4 = f.row_states[crs + uint32_t(y - int(cy0))];
             rs.f0 = t4.x; rs.f1 = t4.y; rs.f2 = t4.z;
           }
           else {
@@ -1526,7 +1560,7 @@ static int max_blocks_per_sm(K kernel, int threads, size_t dyn_smem = 0) {
 int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   if (!f.num_cmds) return 0;
   const int sms = device_sms();
-  static const int max_per_sm = max_blocks_per_sm(edge_pieces_kernel<3>, kCurveThreads, piece_stack_bytes<3>());
+  static const int max_per_sm = max_blocks_per_sm(edge_pieces_kernel<3>, kCurveThreads);
   const int per_sm = cfg.cubic_blocks_per_sm > 0 && cfg.cubic_blocks_per_sm < max_per_sm ? cfg.cubic_blocks_per_sm : max_per_sm;
   const uint32_t eb = cfg.edge_block == 64 || cfg.edge_block == 256 ? uint32_t(cfg.edge_block) : 128u;
   classify_kernel<<<cdiv(f.num_cmds, 128), 128, 0, st>>>(f);
@@ -1537,8 +1571,8 @@ int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   curve_split_kernel<2><<<split_grid, 128, 0, st>>>(f);
   const uint32_t pgrid = cdiv(f.piece_capacity ? f.piece_capacity : 1, kCurveThreads);
   const uint32_t pieces_grid = pgrid < cubic_grid ? pgrid : cubic_grid;
-  edge_pieces_kernel<3><<<pieces_grid, kCurveThreads, piece_stack_bytes<3>(), st>>>(f);
-  edge_pieces_kernel<2><<<pieces_grid, kCurveThreads, piece_stack_bytes<2>(), st>>>(f);
+  edge_pieces_kernel<3><<<pieces_grid, kCurveThreads, 0, st>>>(f);
+  edge_pieces_kernel<2><<<pieces_grid, kCurveThreads, 0, st>>>(f);
   return 6;
 }
 

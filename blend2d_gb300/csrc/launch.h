@@ -41,6 +41,8 @@ int launch_fine(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st);
 int launch_row_states(const FrameView& f, cudaStream_t st);
 int launch_backdrop_prefix(const FrameView& f, cudaStream_t st);
 int launch_frame_gate(const FrameView& f, cudaStream_t st);
+// Copies the `n` canvases of `xfers` (device memory) to their host images (to_host) or back.
+int launch_canvas_copy(const DevXfer* xfers, uint32_t n, int to_host, cudaStream_t st);
 int launch_coverage(const FrameView& f, const LaunchConfig& cfg, uint32_t* scan_tmp, cudaStream_t st);
 int fine_grid_size(int blocks_per_sm);
 // Stroking: per-figure outline sizes and their exclusive scan (stroke_offsets), then the outlines.

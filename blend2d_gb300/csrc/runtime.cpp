@@ -289,6 +289,9 @@ void Runtime::destroy() {
   in_buf.release();
   dyn_buf.release();
   seg_buf.release();
+  stroke_buf.release();
+  xfer_buf.release();
+  xfers.release();
   if (host_staging) cudaFreeHost(host_staging);
   if (host_totals) cudaFreeHost(host_totals);
   if (host_counts) cudaFreeHost(host_counts);
@@ -570,16 +573,8 @@ BLGpuResult Runtime::upload_frame(const Frame& fr, const FrameSizes* caps) {
                                   size_t(im.stride), size_t(im.w) * size_t(im.bpp), size_t(im.h), cudaMemcpyDeviceToDevice, stream));
   }
   // Canvas content (the pipeline composites onto it).
-  for (uint32_t i = 0; i < ncv; i++) {
-    const FrameTarget& t = fr.targets[i];
-    const BLGpuImage& im = t.image;
-    if (!t.upload || device_target_direct(im) || im.width == 0 || im.height == 0) continue;
-    bool dev = (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) != 0;
-    if (!dev) h2d_bytes += uint64_t(uint32_t(im.width)) * uint32_t(im.height) * 4u;
-    BLGPU_CHECK(cudaMemcpy2DAsync(canvas_dev[i], size_t(canvas_stride[i]) * 4u, im.pixel_data, size_t(im.stride),
-                                  size_t(im.width) * 4u, size_t(im.height),
-                                  dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
-  }
+  BLGpuResult cr = stage_canvases(fr);
+  if (cr) return cr;
 
   // Segment array: kept across frames, sized from the vertex count at first and from the actual
   // count whenever a frame overflows it (run() then repeats the counting half).
@@ -680,7 +675,7 @@ static void plan_dynamic(Layout& L, FrameView& v, const FrameTotals& t) {
   v.mask_slot = L.take<uint32_t>(size_t(slots) + 1);
   v.mask_info = L.take<uint4>(size_t(slots) + 1);
   v.masks = L.take<uint8_t>((size_t(slots) + 1) * kStripRows * kTileW);
-  v.row_cmds = L.take<uint32_t>(t.row_entries + 1);
+  v.row_recs = L.take<uint4>(2 * (size_t(t.row_entries) + 1));
   v.row_states = L.take<float4>(t.row_states + 1);
   v.mask_capacity = slots + 1;
   v.num_segs = t.segs;
@@ -691,10 +686,74 @@ static void plan_dynamic(Layout& L, FrameView& v, const FrameTotals& t) {
   v.num_row_entries = t.row_entries;
 }
 
+BLGpuResult Runtime::stage_canvases(const Frame& fr) {
+  const uint32_t ncv = uint32_t(fr.canvases.size());
+  xfers.clear();
+  canvas_xfer.assign(ncv, -1);
+  for (uint32_t i = 0; i < ncv; i++) {
+    const BLGpuImage& im = fr.targets[i].image;
+    if (device_target_direct(im) || im.width == 0 || im.height == 0 || (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) ||
+        (im.stride & 3) != 0)
+      continue;
+    // page-locked host memory is reachable from the device at the address the driver reports
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, im.pixel_data) != cudaSuccess) { cudaGetLastError(); continue; }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) continue;
+    canvas_xfer[i] = int32_t(xfers.size());
+    xfers.push_back(DevXfer{canvas_dev[i], static_cast<uint32_t*>(a.devicePointer), im.width, im.height,
+                            canvas_stride[i], int32_t(im.stride / 4)});
+  }
+  if (!xfers.empty()) {
+    BLGPU_CHECK(xfer_buf.reserve(sizeof(DevXfer) * xfers.size()));
+    BLGPU_CHECK(cudaMemcpyAsync(xfer_buf.ptr, xfers.data(), sizeof(DevXfer) * xfers.size(), cudaMemcpyHostToDevice, stream));
+  }
+  // canvases the frame composites onto: their content goes up first
+  std::vector<DevXfer> up;
+  for (uint32_t i = 0; i < ncv; i++) {
+    const FrameTarget& t = fr.targets[i];
+    const BLGpuImage& im = t.image;
+    if (!t.upload || device_target_direct(im) || im.width == 0 || im.height == 0) continue;
+    const bool dev = (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) != 0;
+    if (!dev) h2d_bytes += uint64_t(uint32_t(im.width)) * uint32_t(im.height) * 4u;
+    if (canvas_xfer[i] >= 0) continue;
+    BLGPU_CHECK(cudaMemcpy2DAsync(canvas_dev[i], size_t(canvas_stride[i]) * 4u, im.pixel_data, size_t(im.stride),
+                                  size_t(im.width) * 4u, size_t(im.height),
+                                  dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
+  }
+  // the kernel copy of the page-locked ones, when any of them is uploaded: copy all of them up
+  // unless none needs it (those that do not are overwritten by their first fill anyway)
+  bool any_up = false;
+  for (uint32_t i = 0; i < ncv; i++) any_up |= canvas_xfer[i] >= 0 && fr.targets[i].upload;
+  if (any_up) {
+    up.reserve(xfers.size());
+    for (uint32_t i = 0; i < ncv; i++)
+      if (canvas_xfer[i] >= 0 && fr.targets[i].upload) up.push_back(xfers[size_t(canvas_xfer[i])]);
+    // a separate table after the download table (the stream orders the copy before the kernel)
+    const size_t off = align_up(sizeof(DevXfer) * xfers.size(), 256);
+    BLGPU_CHECK(xfer_buf.reserve(off + sizeof(DevXfer) * up.size()));
+    DevXfer* dev_up = reinterpret_cast<DevXfer*>(static_cast<char*>(xfer_buf.ptr) + off);
+    if (!xfers.empty())   // the reserve above may have moved the table
+      BLGPU_CHECK(cudaMemcpyAsync(xfer_buf.ptr, xfers.data(), sizeof(DevXfer) * xfers.size(), cudaMemcpyHostToDevice, stream));
+    BLGPU_CHECK(cudaMemcpyAsync(dev_up, up.data(), sizeof(DevXfer) * up.size(), cudaMemcpyHostToDevice, stream));
+    launch_canvas_copy(dev_up, uint32_t(up.size()), 0, stream);
+    BLGPU_CHECK(cudaGetLastError());
+    BLGPU_CHECK(cudaStreamSynchronize(stream));      // `up` is pageable: its copy must be done
+  }
+  return BLGPU_SUCCESS;
+}
+
 BLGpuResult Runtime::download() {
+  if (!xfers.empty()) {
+    launch_canvas_copy(static_cast<const DevXfer*>(xfer_buf.ptr), uint32_t(xfers.size()), 1, stream);
+    BLGPU_CHECK(cudaGetLastError());
+  }
   for (size_t i = 0; i < targets.size(); i++) {
     const BLGpuImage& im = targets[i].image;
     if (device_target_direct(im) || im.width == 0 || im.height == 0) continue;
+    if (i < canvas_xfer.size() && canvas_xfer[i] >= 0) {
+      d2h_bytes += uint64_t(uint32_t(im.width)) * uint32_t(im.height) * 4u;
+      continue;
+    }
     bool dev = (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) != 0;
     if (!dev) d2h_bytes += uint64_t(uint32_t(im.width)) * uint32_t(im.height) * 4u;
     BLGPU_CHECK(cudaMemcpy2DAsync(im.pixel_data, size_t(im.stride), canvas_dev[i], size_t(canvas_stride[i]) * 4u,

@@ -202,6 +202,11 @@ struct Runtime {
   std::vector<FrameTarget> targets;
   std::vector<uint32_t*> canvas_dev;   // device pixels per canvas
   std::vector<int32_t> canvas_stride;  // device stride in pixels
+  // canvases copied by canvas_copy_kernel (page-locked host images): the table (device), its
+  // staging copy, and each canvas's index in it (-1: copied with cudaMemcpy2DAsync)
+  DeviceBuffer xfer_buf;
+  HostArray<DevXfer> xfers;
+  std::vector<int32_t> canvas_xfer;
   uint32_t* cmdrow_per_cmd = nullptr;
   uint32_t* row_canvas = nullptr;
   uint32_t* scan_tmp = nullptr;
@@ -252,6 +257,9 @@ struct Runtime {
   BLGpuResult upload(const Frame& fr, const FrameSizes* caps = nullptr);
   BLGpuResult upload_frame(const Frame& fr, const FrameSizes* caps);
   BLGpuResult download();
+  // Builds the kernel-copy table of the frame's host canvases and uploads the canvases whose
+  // content the frame composites onto.
+  BLGpuResult stage_canvases(const Frame& fr);
   BLGpuResult reserve_segments(uint32_t count);
   void read_pixel_ops();
 };

@@ -730,3 +730,35 @@ def test_graph_frames_replay_new_frames_bit_exact():
             for i, (s, t) in enumerate(zip(streams, targets)):
                 assert not _diff(t, oracle_lib.render(s)), f"batch {k} canvas {i}"
         assert rt.stats().graph_frames > before
+
+
+def test_page_locked_host_images_match_pageable_ones():
+    """Page-locked host images are copied to and from the device by a kernel (the device reaches
+    them directly), pageable ones by DMA: the same scenes give the same pixels either way, for
+    canvases of every width modulo 4, batched and alone, onto existing content and onto a clear."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(91)
+    streams, init = [], []
+    for i, (w, h) in enumerate([(61, 37), (64, 40), (97, 3), (130, 77), (1, 1), (255, 129)]):
+        sw = scenes.StreamWriter(w, h)
+        for k in range(12):                       # SrcOver fills onto whatever the canvas holds
+            sw.solid(int(rng.integers(0, 2**32)))
+            sw.fill_rect_d(rng.uniform(-5, w), rng.uniform(-5, h), rng.uniform(1, w), rng.uniform(1, h))
+        streams.append(sw.to_bytes())
+        init.append(rng.integers(0, 2**32, (h, w), dtype=np.uint64).astype(np.uint32))
+    streams.append(scenes.random_mix(92, width=203, height=101, count=150).to_bytes())
+    init.append(np.zeros((101, 203), dtype=np.uint32))
+    with bg.Runtime(0) as rt:
+        pageable = [a.copy() for a in init]
+        rt.render_batch(streams, pageable)
+        pinned = [torch.from_numpy(a.view(np.int32).copy()).pin_memory() for a in init]
+        rt.render_batch(streams, pinned)
+        for i, (p, q) in enumerate(zip(pageable, pinned)):
+            assert not _diff(q.numpy().view(np.uint32), p), f"batched canvas {i}"
+        for i, s in enumerate(streams):
+            p = init[i].copy()
+            bg.render_stream(rt, s, p)
+            q = torch.from_numpy(init[i].view(np.int32).copy()).pin_memory()
+            bg.render_stream(rt, s, q)
+            assert not _diff(q.numpy().view(np.uint32), p), f"canvas {i}"
+            assert not _diff(p, pageable[i]), f"canvas {i} alone vs batched"
