@@ -74,6 +74,7 @@ GEOMETRY_CIRCLE, GEOMETRY_ELLIPSE, GEOMETRY_ROUND_RECT, GEOMETRY_TRIANGLE = 5, 6
 GEOMETRY_ARC, GEOMETRY_CHORD, GEOMETRY_PIE = 8, 9, 10
 
 SRC_OVER, SRC_COPY = 0, 1
+FORMAT_PRGB32, FORMAT_XRGB32, FORMAT_A8 = 1, 2, 3                                              # BLFormat
 NON_ZERO, EVEN_ODD = 0, 1
 LINEAR, RADIAL, CONIC = 0, 1, 2
 PAD, REPEAT, REFLECT = 0, 1, 2
@@ -95,17 +96,23 @@ def rgba64_from_rgba32(c: int) -> int:
 class StreamWriter:
     """Builds one command stream (one canvas, one frame)."""
 
-    def __init__(self, width: int, height: int):
+    def __init__(self, width: int, height: int, format: int = FORMAT_PRGB32):
         self.width = int(width)
         self.height = int(height)
+        self.format = int(format)             # the target's BLFormat
         self.images: list[np.ndarray] = []
+        self.image_formats: list[int] = []
         self.parts: list[bytes] = []
         self.fill_count = 0
 
     # -- images ---------------------------------------------------------------------------------
-    def add_image(self, pixels: np.ndarray) -> int:
-        assert pixels.dtype == np.uint32 and pixels.ndim == 2
+    def add_image(self, pixels: np.ndarray, format: int = FORMAT_PRGB32) -> int:
+        """A pattern / blit source: 32-bit pixels, PRGB32 or XRGB32 (whose alpha bytes the
+        fetchers read as 0xFF)."""
+        assert pixels.dtype == np.uint32 and pixels.ndim == 2 and pixels.shape[0] <= 65535
+        assert format in (FORMAT_PRGB32, FORMAT_XRGB32)
         self.images.append(np.ascontiguousarray(pixels))
+        self.image_formats.append(int(format))
         return len(self.images) - 1
 
     # -- records --------------------------------------------------------------------------------
@@ -303,11 +310,12 @@ class StreamWriter:
 
     # -- output ---------------------------------------------------------------------------------
     def to_bytes(self) -> bytes:
-        out = [struct.pack("<6I", MAGIC, VERSION, self.width, self.height, len(self.images), 0)]
-        for img in self.images:
+        fmt = 0 if self.format == FORMAT_PRGB32 else self.format     # PRGB32 streams keep their old bytes
+        out = [struct.pack("<6I", MAGIC, VERSION, self.width, self.height, len(self.images), fmt)]
+        for img, ifmt in zip(self.images, self.image_formats):
             h, w = img.shape
             raw = img.astype("<u4").tobytes()
-            out.append(struct.pack("<II", w, h) + raw + b"\0" * ((-len(raw)) % 8))
+            out.append(struct.pack("<IHH", w, h, 0 if ifmt == FORMAT_PRGB32 else ifmt) + raw + b"\0" * ((-len(raw)) % 8))
         out.extend(self.parts)
         out.append(struct.pack("<II", OP_END, 0))
         return b"".join(out)
@@ -678,14 +686,18 @@ def serving_requests(seed: int = 5, count: int = 48, min_side: int = 64, max_sid
 def random_mix(seed: int, width: int = 257, height: int = 257, count: int = 200,
                styles=("solid", "linear", "radial", "conic", "pattern_nn", "pattern_bi"),
                commands=("rect_i", "rect_d", "box_d", "polygon", "path_quad", "path_cubic"),
-               transforms: bool = True, alphas: bool = True, dither: bool = False) -> StreamWriter:
+               transforms: bool = True, alphas: bool = True, dither: bool = False,
+               format: int = FORMAT_PRGB32, xrgb_images: bool = False) -> StreamWriter:
     """Mixed commands/styles/comp-ops over a canvas slightly larger than the shapes' range
     (coordinates span -30 .. size+30 like the reference tester, so clipping is exercised).
-    `dither`: each gradient is set with gradient quality DITHER (2 in 3) or NEAREST."""
+    `dither`: each gradient is set with gradient quality DITHER (2 in 3) or NEAREST.
+    `format`: the target's pixel format; `xrgb_images`: the first and third pattern images are
+    XRGB32 (the random draws are the same either way)."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    sw = StreamWriter(width, height)
-    for _ in range(3):
-        sw.add_image(premultiplied_noise(rng, int(rng.integers(5, 80)), int(rng.integers(5, 80))))
+    sw = StreamWriter(width, height, format)
+    for k in range(3):
+        sw.add_image(premultiplied_noise(rng, int(rng.integers(5, 80)), int(rng.integers(5, 80))),
+                     FORMAT_XRGB32 if xrgb_images and k != 1 else FORMAT_PRGB32)
     sw.clear_all()
     lo_x, hi_x, lo_y, hi_y = -30.0, width + 30.0, -30.0, height + 30.0
 
@@ -899,16 +911,19 @@ def strokes(seed: int = 9, width: int = 640, height: int = 480, count: int = 400
     return sw
 
 
-def blits(seed: int = 40, width: int = 320, height: int = 240, count: int = 150) -> StreamWriter:
+def blits(seed: int = 40, width: int = 320, height: int = 240, count: int = 150,
+          format: int = FORMAT_PRGB32, xrgb_images: bool = False) -> StreamWriter:
     """Image blits: integer and fractional origins, scaled rectangles, image areas (some outside the
     image, which the reference rejects), partly clipped, with translations, rotations and scales,
-    nearest and bilinear quality, SrcOver/SrcCopy and global alpha."""
+    nearest and bilinear quality, SrcOver/SrcCopy and global alpha. `format` and `xrgb_images`
+    as in random_mix."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    sw = StreamWriter(width, height)
+    sw = StreamWriter(width, height, format)
     sw.solid(0xFF303030)
     sw.fill_all()
-    for _ in range(3):
-        sw.add_image(premultiplied_noise(rng, int(rng.integers(1, 90)), int(rng.integers(1, 70))))
+    for k in range(3):
+        sw.add_image(premultiplied_noise(rng, int(rng.integers(1, 90)), int(rng.integers(1, 70))),
+                     FORMAT_XRGB32 if xrgb_images and k != 1 else FORMAT_PRGB32)
     sizes = [im.shape for im in sw.images]
     for i in range(count):
         idx = int(rng.integers(0, len(sizes)))

@@ -93,20 +93,30 @@ enum {
   BLGPU_OP_COUNT
 };
 
+/* Pixel formats of the target and of the images (BLFormat values, image.h:21-31). 0 reads as
+ * PRGB32. */
+enum {
+  BLGPU_STREAM_FORMAT_PRGB32 = 1,      /* BL_FORMAT_PRGB32 */
+  BLGPU_STREAM_FORMAT_XRGB32 = 2,      /* BL_FORMAT_XRGB32 */
+  BLGPU_STREAM_FORMAT_A8 = 3           /* BL_FORMAT_A8 (targets only) */
+};
+
 typedef struct BLGpuStreamHeader {
   uint32_t magic;        /* BLGPU_STREAM_MAGIC */
   uint32_t version;      /* BLGPU_STREAM_VERSION */
-  uint32_t width;        /* canvas width in pixels (PRGB32) */
+  uint32_t width;        /* canvas width in pixels */
   uint32_t height;       /* canvas height in pixels */
   uint32_t image_count;  /* number of pattern images that follow the header */
-  uint32_t reserved;
+  uint32_t format;       /* the target's BLGPU_STREAM_FORMAT_* (0: PRGB32) */
 } BLGpuStreamHeader;
 
-/* Each image: BLGpuStreamImage followed by w*h PRGB32 pixels (uint32, tightly packed rows),
- * padded to 8 bytes. */
+/* Each image: BLGpuStreamImage followed by w*h 32-bit pixels (tightly packed rows), padded to
+ * 8 bytes. An XRGB32 image's pixels are read with the alpha byte forced to 0xFF, as the
+ * reference's fetchers read them (PixelIO<..., XRGB32>, pipeline/reference/pixelgeneric_p.h). */
 typedef struct BLGpuStreamImage {
   uint32_t width;
-  uint32_t height;
+  uint16_t height;       /* images are at most 65,535 px high (BL_RUNTIME_MAX_IMAGE_SIZE) */
+  uint16_t format;       /* BLGPU_STREAM_FORMAT_PRGB32 or _XRGB32 (0: PRGB32) */
 } BLGpuStreamImage;
 
 typedef struct BLGpuStreamGradient {

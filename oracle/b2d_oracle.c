@@ -348,6 +348,8 @@ typedef struct {
   OEdgeBuilder eb;
   OFillCtx fc;
   const uint32_t** images; const int* iw; const int* ih;
+  const int* ifmt;                    /* O_FMT_PRGB32 / O_FMT_XRGB32 of each image */
+  int dst_format;                     /* BLGPU_STREAM_FORMAT_* of the target */
   B2DOracleStats* stats;
 } OCtx;
 
@@ -436,7 +438,8 @@ static void set_style_gradient(OCtx* c, int slot, const uint8_t* p) {
       st->solid = o_premultiply(c32);
       goto done;
     }
-    if (c->s.gradient_quality >= 2u) {
+    /* gradients are not dithered into A8 targets (rastercontext.cpp:456-458) */
+    if (c->s.gradient_quality >= 2u && c->dst_format != BLGPU_STREAM_FORMAT_A8) {
       /* BL_GRADIENT_QUALITY_DITHER: lut_size(true) (gradient_p.h:113-120), ensure_lut64 */
       lut_size = lut_size * 2u < 1024u ? lut_size * 2u : 1024u;
       st->dither = 1;
@@ -461,7 +464,7 @@ static void set_style_pattern(OCtx* c, int slot, const uint8_t* p) {
   int iw = c->iw[pt.image_index], ih = c->ih[pt.image_index];
   int ax = 0, ay = 0, aw = iw, ah = ih;
   if (pt.area[2] > 0) { ax = pt.area[0]; ay = pt.area[1]; aw = pt.area[2]; ah = pt.area[3]; }
-  st->format = O_FMT_PRGB32;
+  st->format = c->ifmt[pt.image_index];   /* fetch_data->extra.format = the image's (rastercontext.cpp:415) */
   if (!aw || !ah) { st->nop = 1; return; }
   st->src = c->images[pt.image_index] + (intptr_t)ay * iw + ax;
   st->src_w = aw; st->src_h = ah; st->src_stride = iw;
@@ -474,17 +477,38 @@ static void set_style_pattern(OCtx* c, int slot, const uint8_t* p) {
   if (!o_init_pattern_affine(st, pt.extend_mode, c->s.pattern_quality, &tf)) st->nop = 1;
 }
 
-/* Resolve the fill: returns 0 for NOP, else sets comp-op (0/1) and alpha. */
+static int is_pattern_fetch(int fetch_type) { return fetch_type >= O_FT_PAT_ALIGNED_PAD; }
+
+/* SrcOver / SrcCopy simplified by the destination and source formats (CompOpSimplifyInfoImpl::
+ * src_over / src_copy, compopsimplifyimpl_p.h:86-162). Returns -1 for DstCopy (nothing drawn),
+ * else the operator (0 SrcOver, 1 SrcCopy); *src_or is 0xFF000000 when the simplified source
+ * format is XRGB32 and the fetcher reads an image (solid and gradient fetchers do not look at the
+ * source format: fixedpiperuntime.cpp:250-270).
+ *   SrcOver: ZERO32 -> DstCopy; FRGB32 -> SrcCopy; XRGB32 -> SrcCopy of XRGB32; PRGB32 -> SrcOver.
+ *   SrcCopy: XRGB32 -> SrcCopy of XRGB32; PRGB32 into an XRGB32 target -> SrcCopy of XRGB32.
+ * An A8 target's simplifications (opaque alpha, transparent) give the alpha byte these do. */
+static int o_simplify(int dst_format, int op, int src_format, int fetch_type, uint32_t* src_or) {
+  int xrgb_src = src_format == O_FMT_XRGB32;
+  if (op == 0) {
+    if (src_format == O_FMT_ZERO32) return -1;
+    if (src_format == O_FMT_FRGB32 || xrgb_src) op = 1;
+  }
+  else if (src_format == O_FMT_PRGB32 && dst_format == BLGPU_STREAM_FORMAT_XRGB32) {
+    xrgb_src = 1;
+  }
+  *src_or = (xrgb_src && is_pattern_fetch(fetch_type)) ? 0xFF000000u : 0u;
+  return op;
+}
+
+/* Resolve the fill: returns 0 for NOP, else sets comp-op (0/1), alpha and the fill context's
+ * src_or (consumed by the fill that follows). */
 static int resolve_slot(OCtx* c, int slot, int* comp_op, uint32_t* alpha) {
   OState* s = &c->s;
   const OStyle* st = slot_style(c, slot);
   uint32_t a = slot ? s->stroke_alpha_i : s->fill_alpha_i;
   if (s->global_alpha_i == 0 || a == 0 || st->nop) return 0;
-  int op = s->comp_op;
-  if (op == 0) {   /* SrcOver simplification for a PRGB32 destination */
-    if (st->format == O_FMT_ZERO32) return 0;             /* DstCopy */
-    if (st->format == O_FMT_FRGB32) op = 1;               /* SrcCopy */
-  }
+  int op = o_simplify(c->dst_format, s->comp_op, st->format, st->fetch_type, &c->fc.src_or);
+  if (op < 0) return 0;
   *comp_op = op;
   *alpha = a;
   return 1;
@@ -692,7 +716,7 @@ static int o_image_area(int iw, int ih, const BLGpuStreamBlit* b, int out[4]) {
 
 static int o_blit_source(OCtx* c, OStyle* st, uint32_t image_index, const int a[4]) {
   memset(st, 0, sizeof(*st));
-  st->format = O_FMT_PRGB32;
+  st->format = c->ifmt[image_index];
   if (a[2] <= 0 || a[3] <= 0) { st->nop = 1; return 0; }
   int iw = c->iw[image_index];
   st->src = c->images[image_index] + (intptr_t)a[1] * iw + a[0];
@@ -714,7 +738,10 @@ static void blit_op(OCtx* c, uint32_t op, const uint8_t* p) {
   if (op == BLGPU_OP_BLIT_IMAGE_I && !s->integral_translation) op = BLGPU_OP_BLIT_IMAGE_D;
   if (!o_image_area(iw, ih, &b, src)) return;
   OStyle* st = (OStyle*)malloc(sizeof(OStyle));
-  c->fc.style = st; c->fc.comp_op = s->comp_op; c->fc.alpha = s->global_alpha_i;
+  /* resolve_blit_op (rastercontext.cpp:1331-1342): the comp-op simplified for the image format */
+  int bop = o_simplify(c->dst_format, s->comp_op, c->ifmt[b.image_index], O_FT_PAT_ALIGNED_PAD, &c->fc.src_or);
+  if (bop < 0) { free(st); return; }
+  c->fc.style = st; c->fc.comp_op = bop; c->fc.alpha = s->global_alpha_i;
   if (op == BLGPU_OP_BLIT_IMAGE_I) {
     /* translate_and_clip_rect_to_blit_i (rastercontext.cpp:922-990) */
     int64_t dx = (int64_t)(int32_t)b.rect[0] + s->tx_i, dy = (int64_t)(int32_t)b.rect[1] + s->ty_i;
@@ -1043,8 +1070,11 @@ static int replay(OCtx* c, const uint8_t* base, size_t size, size_t off) {
         OStyle clear_style;
         memset(&clear_style, 0, sizeof(clear_style));
         clear_style.fetch_type = O_FT_SOLID;
+        /* resolve_clear_op (rastercontext.cpp:1230-1242): SrcCopy of the override table's first
+         * entry, 0x00000000, whatever the target format */
         c->fc.style = &clear_style;
         c->fc.comp_op = 1;
+        c->fc.src_or = 0;
         c->fc.alpha = 255;
         fill_box_a(c, 0, 0, c->w, c->h);
         break;
@@ -1131,6 +1161,7 @@ static int default_band_height(int w) {   /* calculate_band_height, thread_count
 }
 
 int b2d_oracle_render(const uint8_t* stream, size_t size, uint32_t* out, const B2DOracleOptions* opt, B2DOracleStats* stats) {
+  void* out_a8 = out;
   if (size < sizeof(BLGpuStreamHeader)) return -1;
   BLGpuStreamHeader hdr;
   memcpy(&hdr, stream, sizeof(hdr));
@@ -1140,6 +1171,17 @@ int b2d_oracle_render(const uint8_t* stream, size_t size, uint32_t* out, const B
   memset(&c, 0, sizeof(c));
   c.w = (int)hdr.width;
   c.h = (int)hdr.height;
+  c.dst_format = hdr.format ? (int)hdr.format : BLGPU_STREAM_FORMAT_PRGB32;
+  if (c.dst_format < BLGPU_STREAM_FORMAT_PRGB32 || c.dst_format > BLGPU_STREAM_FORMAT_A8) return -1;
+  /* An A8 target renders into a 32-bit canvas whose alpha bytes are the A8 pixels: the
+   * reference's P8_Alpha operators (compopgeneric_p.h, fetchgeneric_p.h with PixelIO<P8_Alpha, ...>)
+   * are its P32 operators' alpha lane, and no P32 lane reads another lane. */
+  uint32_t* canvas = out;
+  if (c.dst_format == BLGPU_STREAM_FORMAT_A8) {
+    canvas = (uint32_t*)calloc((size_t)c.w * (size_t)c.h + 1u, 4u);
+    if (!canvas) return -2;
+  }
+  out = canvas;
   c.pixels = out;
   c.lut_variant = opt ? opt->lut_variant : B2D_ORACLE_LUT_SSE2;
   c.stats = stats;
@@ -1150,6 +1192,7 @@ int b2d_oracle_render(const uint8_t* stream, size_t size, uint32_t* out, const B
   const uint32_t** images = (const uint32_t**)calloc(hdr.image_count + 1, sizeof(void*));
   int* iw = (int*)calloc(hdr.image_count + 1, sizeof(int));
   int* ih = (int*)calloc(hdr.image_count + 1, sizeof(int));
+  int* ifmt = (int*)calloc(hdr.image_count + 1, sizeof(int));
   uint32_t** owned = (uint32_t**)calloc(hdr.image_count + 1, sizeof(void*));
   for (uint32_t i = 0; i < hdr.image_count; i++) {
     BLGpuStreamImage im;
@@ -1160,9 +1203,10 @@ int b2d_oracle_render(const uint8_t* stream, size_t size, uint32_t* out, const B
     memcpy(owned[i], stream + off, n * 4u);
     images[i] = owned[i];
     iw[i] = (int)im.width; ih[i] = (int)im.height;
+    ifmt[i] = im.format == BLGPU_STREAM_FORMAT_XRGB32 ? O_FMT_XRGB32 : O_FMT_PRGB32;
     off += (n * 4u + 7u) & ~(size_t)7;
   }
-  c.images = images; c.iw = iw; c.ih = ih;
+  c.images = images; c.iw = iw; c.ih = ih; c.ifmt = ifmt;
 
   /* default state (rastercontext.cpp:4380-4415) */
   c.s.comp_op = 0; c.s.fill_rule = 0;
@@ -1196,6 +1240,11 @@ int b2d_oracle_render(const uint8_t* stream, size_t size, uint32_t* out, const B
   o_storage_free(&c.storage);
   free(c.stack);
   for (uint32_t i = 0; i < hdr.image_count; i++) free(owned[i]);
-  free(owned); free(images); free(iw); free(ih);
+  free(owned); free(images); free(iw); free(ih); free(ifmt);
+  if (c.dst_format == BLGPU_STREAM_FORMAT_A8) {
+    uint8_t* bytes = (uint8_t*)out_a8;
+    for (size_t i = 0, n = (size_t)c.w * (size_t)c.h; i < n; i++) bytes[i] = (uint8_t)(canvas[i] >> 24);
+    free(canvas);
+  }
   return rc;
 }

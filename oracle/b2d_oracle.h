@@ -39,8 +39,9 @@ typedef struct B2DOracleStats {
   uint64_t input_vertices;   /* vertices read from polygon/path records */
 } B2DOracleStats;
 
-/* Renders `stream` into `out_pixels` (width*height PRGB32, tightly packed). The canvas starts
- * zeroed. Returns 0 on success, a negative value for a malformed stream. */
+/* Renders `stream` into `out_pixels`: width*height 32-bit pixels (PRGB32 or XRGB32 targets) or
+ * width*height bytes (A8 targets), tightly packed. The canvas starts zeroed. Returns 0 on
+ * success, a negative value for a malformed stream. */
 int b2d_oracle_render(const uint8_t* stream, size_t size, uint32_t* out_pixels,
                       const B2DOracleOptions* options, B2DOracleStats* stats);
 

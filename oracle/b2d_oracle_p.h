@@ -136,7 +136,7 @@ enum {
   O_FT_PAT_AFFINE_NN, O_FT_PAT_AFFINE_BI
 };
 
-enum { O_FMT_PRGB32 = 0, O_FMT_FRGB32 = 1, O_FMT_ZERO32 = 2 };
+enum { O_FMT_PRGB32 = 0, O_FMT_FRGB32 = 1, O_FMT_ZERO32 = 2, O_FMT_XRGB32 = 3 };
 
 typedef struct OStyle {
   int nop;                     /* style resolves to nothing (NoFillStyle) */
@@ -170,6 +170,7 @@ typedef struct OFillCtx {
   uint32_t* dst; int width, height; intptr_t stride;  /* stride in pixels */
   int comp_op;            /* after simplification: 0 SrcOver, 1 SrcCopy */
   uint32_t alpha;         /* 0..255 */
+  uint32_t src_or;        /* 0xFF000000 when the pattern fetcher reads its source as XRGB32 */
   const OStyle* style;
   /* scratch for analytic fills */
   uint32_t* cells; uint64_t* bits; size_t cell_stride, bit_stride; /* in elements */

@@ -498,13 +498,16 @@ static void fetch_rect_start_x(OFetch* f, uint32_t x) {
  * Compositing helpers
  * ============================================================================================ */
 
+/* src_or: PixelIO<P32_A8R8G8B8, XRGB32>::fetch (pixelgeneric_p.h:650-661) sets the alpha byte of
+ * every texel it reads; the bilinear weights are per channel, so setting it after the
+ * interpolation gives the same pixel. */
 static inline void comp_masked(OFillCtx* fc, OFetch* f, uint32_t* d, uint32_t m) {
-  uint32_t s = fetch_pixel(f);
+  uint32_t s = fetch_pixel(f) | fc->src_or;
   *d = fc->comp_op ? op_src_copy_m(*d, s, m) : op_src_over_m(*d, s, m);
   if (m && fc->stats) fc->stats->composited_pixels++;
 }
 static inline void comp_opaque(OFillCtx* fc, OFetch* f, uint32_t* d) {
-  uint32_t s = fetch_pixel(f);
+  uint32_t s = fetch_pixel(f) | fc->src_or;
   *d = fc->comp_op ? s : op_src_over(*d, s);
   if (fc->stats) fc->stats->composited_pixels++;
 }

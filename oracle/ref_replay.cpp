@@ -1,5 +1,5 @@
 // ref_replay.cpp - replays a blgpu command stream (include/blgpu_stream.h) into the reference
-// Blend2D BLContext and writes the resulting PRGB32 pixels.
+// Blend2D BLContext and writes the resulting pixels (4 bytes per pixel, 1 for an A8 target).
 //
 // Test infrastructure: built by oracle/ref.mk against the reference sources (never shipped).
 // Every record maps 1:1 onto the reference C++ API (blend2d/core/context.h:2155-2700).
@@ -28,7 +28,7 @@ static void replay(const Stream& s, BLImage& img, uint32_t threads) {
   BLImageData d;
   img.make_mutable(&d);
   for (int y = 0; y < d.size.h; y++)
-    memset(static_cast<uint8_t*>(d.pixel_data) + intptr_t(y) * d.stride, 0, size_t(d.size.w) * 4u);
+    memset(static_cast<uint8_t*>(d.pixel_data) + intptr_t(y) * d.stride, 0, size_t(d.size.w) * target_bpp(s));
 
   BLContextCreateInfo cci {};
   cci.thread_count = threads;
@@ -66,7 +66,7 @@ static int run_batch(int argc, char** argv) {
     streams[i].base = bufs[i].data();
     streams[i].size = bufs[i].size();
     parse_header(streams[i]);
-    imgs.emplace_back(int(streams[i].hdr.width), int(streams[i].hdr.height), BL_FORMAT_PRGB32);
+    imgs.emplace_back(int(streams[i].hdr.width), int(streams[i].hdr.height), target_format(streams[i]));
     pixels += uint64_t(streams[i].hdr.width) * streams[i].hdr.height;
   }
   std::vector<double> ms;
@@ -88,7 +88,7 @@ static int run_batch(int argc, char** argv) {
       FILE* f = fopen(path.c_str(), "wb");
       if (!f) { fprintf(stderr, "cannot write %s\n", path.c_str()); return 2; }
       for (int y = 0; y < d.size.h; y++)
-        fwrite(static_cast<const uint8_t*>(d.pixel_data) + intptr_t(y) * d.stride, 1, size_t(d.size.w) * 4u, f);
+        fwrite(static_cast<const uint8_t*>(d.pixel_data) + intptr_t(y) * d.stride, 1, size_t(d.size.w) * target_bpp(streams[i]), f);
       fclose(f);
     }
   }
@@ -114,7 +114,7 @@ int main(int argc, char** argv) {
   s.size = buf.size();
   parse_header(s);
 
-  BLImage img(int(s.hdr.width), int(s.hdr.height), BL_FORMAT_PRGB32);
+  BLImage img(int(s.hdr.width), int(s.hdr.height), target_format(s));
   replay(s, img, threads);
 
   if (frames > 0) {
@@ -134,7 +134,7 @@ int main(int argc, char** argv) {
     img.get_data(&d);
     FILE* f = fopen(argv[2], "wb");
     for (int y = 0; y < d.size.h; y++)
-      fwrite(static_cast<const uint8_t*>(d.pixel_data) + intptr_t(y) * d.stride, 1, size_t(d.size.w) * 4u, f);
+      fwrite(static_cast<const uint8_t*>(d.pixel_data) + intptr_t(y) * d.stride, 1, size_t(d.size.w) * target_bpp(s), f);
     fclose(f);
   }
   return 0;

@@ -46,7 +46,7 @@ static void parse_header(Stream& s) {
     BLGpuStreamImage ih;
     memcpy(&ih, s.base + off, sizeof(ih));
     off += sizeof(ih);
-    BLImage img(int(ih.width), int(ih.height), BL_FORMAT_PRGB32);
+    BLImage img(int(ih.width), int(ih.height), ih.format == BLGPU_STREAM_FORMAT_XRGB32 ? BL_FORMAT_XRGB32 : BL_FORMAT_PRGB32);
     BLImageData d;
     img.make_mutable(&d);
     for (uint32_t y = 0; y < ih.height; y++)
@@ -56,6 +56,12 @@ static void parse_header(Stream& s) {
   }
   s.records_offset = off;
 }
+
+// The target's BLFormat (the header's 0 reads as PRGB32) and its bytes per pixel.
+static BLFormat target_format(const Stream& s) {
+  return s.hdr.format ? BLFormat(s.hdr.format) : BL_FORMAT_PRGB32;
+}
+static size_t target_bpp(const Stream& s) { return target_format(s) == BL_FORMAT_A8 ? 1u : 4u; }
 
 template<typename T>
 static T rd(const uint8_t* p) { T v; memcpy(&v, p, sizeof(T)); return v; }

@@ -3,7 +3,8 @@
 Run in a checkout that has the reference sources (default /root/reference); it builds the
 reference with oracle/ref.mk (no CMake) into oracle/_ref/ and records:
 
-  * scenes  - sha256 of the PRGB32 pixels the reference renders for seeded command streams
+  * scenes  - sha256 of the pixels the reference renders for seeded command streams (4 bytes
+              per pixel; 1 for the A8 targets of the mix_a8 scenes)
               (blend2d_gb300.scenes; the mix_dither / curves_dither scenes use gradient quality
               DITHER, whose 64-bit LUT has a single builder; strokes_* / stroked_paths_* stroke
               paths, polylines, polygons, boxes, rects and lines; blits_* image blits; masks_* masked fills; shapes_* circles, ellipses, round rects and triangles), for the stock no-JIT x86-64 build ("default", SSE2 LUT
@@ -74,6 +75,17 @@ def scene_catalog(full: bool):
         cat.append((f"shapes_{s}", f"scenes.shapes(seed={60 + s}, count=200)", ("default",)))
     for i in range(6):
         cat.append((f"batch_{i}", f"scenes.batch_canvases(seed=4, count=6, max_side=640, max_paths=400)[{i}]", ("default",)))
+    # XRGB32 and A8 targets, XRGB32 pattern and blit sources
+    for s in range(4):
+        cat.append((f"mix_xrgb_{s}", f"scenes.random_mix({400 + s}, format=scenes.FORMAT_XRGB32, xrgb_images={s % 2 == 1})",
+                    ("default",) if s else ("default", "scalar")))
+        cat.append((f"mix_a8_{s}", f"scenes.random_mix({410 + s}, format=scenes.FORMAT_A8, xrgb_images={s % 2 == 1})",
+                    ("default",) if s else ("default", "scalar")))
+        cat.append((f"mix_xrgb_images_{s}", f"scenes.random_mix({420 + s}, xrgb_images=True)", ("default",)))
+    cat.append(("mix_a8_dither", "scenes.random_mix(430, format=scenes.FORMAT_A8, dither=True)", ("default",)))
+    cat.append(("mix_xrgb_dither", "scenes.random_mix(431, format=scenes.FORMAT_XRGB32, dither=True)", ("default",)))
+    for f, tag in (("scenes.FORMAT_PRGB32", "prgb"), ("scenes.FORMAT_XRGB32", "xrgb"), ("scenes.FORMAT_A8", "a8")):
+        cat.append((f"blits_xrgb_images_{tag}", f"scenes.blits(seed=45, format={f}, xrgb_images=True)", ("default",)))
     if full:
         # the benchmarked workloads at full size: the 20,000-path curves frame, the 50,000-quad
         # pattern frame, a sample of the 4,096 batched canvases (the largest, the one with the
@@ -187,15 +199,27 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--full", action="store_true", help="also render the full-size curve and pattern workloads")
+    ap.add_argument("--update", action="store_true",
+                    help="keep the entries of the existing golden.json whose stream bytes are unchanged; render the rest")
     args = ap.parse_args()
     build_reference(args.ref)
 
+    kept = {}
+    if args.update:
+        with open(os.path.join(HERE, "golden.json")) as f:
+            old = json.load(f)
+        kept = {e["name"]: e for e in old["scenes"]}
     golden = {"note": "generated by tests/golden/make_golden.py from the reference library", "scenes": [], "luts": [], "lines": []}
     for name, expr, variants in scene_catalog(args.full):
         sw = eval(expr, {"scenes": scenes})
         stream = sw.to_bytes()
-        entry = {"name": name, "expr": expr, "width": sw.width, "height": sw.height,
-                 "stream_sha256": hashlib.sha256(stream).hexdigest(), "pixels_sha256": {}}
+        digest = hashlib.sha256(stream).hexdigest()
+        prev = kept.get(name)
+        if prev and prev["expr"] == expr and prev["stream_sha256"] == digest and set(prev["pixels_sha256"]) == set(variants):
+            golden["scenes"].append(prev)
+            continue
+        entry = {"name": name, "expr": expr, "width": sw.width, "height": sw.height, "format": sw.format,
+                 "stream_sha256": digest, "pixels_sha256": {}}
         for v in variants:
             entry["pixels_sha256"][v] = render_ref(stream, v)
         golden["scenes"].append(entry)

@@ -55,15 +55,24 @@ def lib():
         return _lib
 
 
+FORMAT_PRGB32, FORMAT_XRGB32, FORMAT_A8 = 1, 2, 3
+
+
 def stream_size(stream: bytes):
     w, h = struct.unpack_from("<II", stream, 8)
     return w, h
 
 
+def stream_format(stream: bytes) -> int:
+    """The target format of a stream (BLGPU_STREAM_FORMAT_*; 0 in the header reads as PRGB32)."""
+    return struct.unpack_from("<I", stream, 20)[0] or FORMAT_PRGB32
+
+
 def render(stream: bytes, lut: str = "default", band_height: int = 0, stats: bool = False):
-    """Renders a command stream on the CPU oracle; returns (h, w) uint32 pixels [and stats]."""
+    """Renders a command stream on the CPU oracle; returns (h, w) pixels, uint32 (uint8 for an A8
+    target) [and stats]."""
     w, h = stream_size(stream)
-    out = np.zeros((h, w), dtype=np.uint32)
+    out = np.zeros((h, w), dtype=np.uint8 if stream_format(stream) == FORMAT_A8 else np.uint32)
     opt = OracleOptions(LUT_VARIANTS[lut], band_height)
     st = OracleStats()
     rc = lib().b2d_oracle_render(stream, len(stream), out.ctypes.data, ctypes.byref(opt), ctypes.byref(st))
