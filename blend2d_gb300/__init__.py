@@ -29,6 +29,7 @@ ERROR_INVALID_GEOMETRY = 0x00010034
 ERROR_DEVICE = 0x00011000
 
 FORMAT_PRGB32 = 1
+FORMAT_XRGB32 = 2
 FORMAT_A8 = 3
 IMAGE_DEVICE_MEMORY = 1
 FLUSH_SYNC = 0x80000000
@@ -217,21 +218,27 @@ def _mat(m):
     return arr
 
 
-def make_image(target) -> tuple[Image, object]:
-    """BLGpuImage for a (h, w) uint32 numpy array (host) or torch tensor (host or CUDA)."""
+def make_image(target, format: int | None = None) -> tuple[Image, object]:
+    """BLGpuImage for a (h, w) numpy array (host) or torch tensor (host or CUDA): 32-bit pixels
+    are PRGB32 unless `format` is FORMAT_XRGB32; 8-bit pixels are A8."""
     if isinstance(target, np.ndarray):
-        if target.dtype != np.uint32 or target.ndim != 2 or not target.flags["C_CONTIGUOUS"]:
-            raise ValueError("target must be a C-contiguous (h, w) uint32 array")
+        if target.dtype not in (np.uint32, np.uint8) or target.ndim != 2 or not target.flags["C_CONTIGUOUS"]:
+            raise ValueError("target must be a C-contiguous (h, w) uint32 or uint8 array")
         h, w = target.shape
-        return Image(target.ctypes.data, w * 4, w, h, FORMAT_PRGB32, 0), target
-    import torch  # device images come from torch tensors
-    if not isinstance(target, torch.Tensor) or target.dim() != 2 or target.element_size() != 4:
-        raise ValueError("target must be a 2-D 32-bit tensor")
-    if not target.is_contiguous():
-        raise ValueError("target tensor must be contiguous")
-    h, w = target.shape
-    flags = IMAGE_DEVICE_MEMORY if target.is_cuda else 0
-    return Image(target.data_ptr(), w * 4, w, h, FORMAT_PRGB32, flags), target
+        bpp, flags, ptr = target.itemsize, 0, target.ctypes.data
+    else:
+        import torch  # device images come from torch tensors
+        if not isinstance(target, torch.Tensor) or target.dim() != 2 or target.element_size() not in (1, 4):
+            raise ValueError("target must be a 2-D 8-bit or 32-bit tensor")
+        if not target.is_contiguous():
+            raise ValueError("target tensor must be contiguous")
+        h, w = target.shape
+        bpp, flags, ptr = target.element_size(), IMAGE_DEVICE_MEMORY if target.is_cuda else 0, target.data_ptr()
+    if bpp == 1:
+        fmt = FORMAT_A8
+    else:
+        fmt = FORMAT_PRGB32 if format in (None, 0, FORMAT_A8) else int(format)
+    return Image(ptr, w * bpp, w, h, fmt, flags), target
 
 
 class Runtime:
@@ -311,7 +318,7 @@ class Runtime:
 
     def render_stream_noalloc(self, stream: bytes, device_target) -> None:
         """Renders `stream` into a CUDA tensor without any allocating call (fixed scratch area)."""
-        img, _keep = make_image(device_target)
+        img, _keep = make_image(device_target, stream_format(stream))
         _check(self._lib.blgpu_render_stream_noalloc(self.handle, stream, len(stream), ctypes.byref(img)),
                "blgpu_render_stream_noalloc", self.handle)
 
@@ -321,7 +328,7 @@ class Runtime:
         imgs = (Image * n)()
         keep = []
         for i, t in enumerate(targets):
-            imgs[i], k = make_image(t)
+            imgs[i], k = make_image(t, stream_format(streams[i]))
             keep.append(k)
         ptrs = (ctypes.c_char_p * n)(*streams)
         sizes = (ctypes.c_size_t * n)(*[len(s) for s in streams])
@@ -329,9 +336,9 @@ class Runtime:
 
 
 class Context:
-    """Rendering context bound to one PRGB32 image (BLContext, synchronous mode)."""
+    """Rendering context bound to one PRGB32, XRGB32 or A8 image (BLContext)."""
 
-    def __init__(self, runtime: Runtime, target=None):
+    def __init__(self, runtime: Runtime, target=None, format: int | None = None):
         self.rt = runtime
         self._lib = runtime._lib
         h = _P()
@@ -341,13 +348,14 @@ class Context:
         self._keep = []
         self._inflight = []
         if target is not None:
-            self.begin(target)
+            self.begin(target, format)
 
     def _call(self, name, *args):
         _check(getattr(self._lib, name)(self.handle, *args), name, self.rt.handle)
 
-    def begin(self, target):
-        img, keep = make_image(target)
+    def begin(self, target, format: int | None = None):
+        """Binds the image: 32-bit pixels are PRGB32 unless `format` is FORMAT_XRGB32, 8-bit ones A8."""
+        img, keep = make_image(target, format)
         self._img = img
         self._keep = [keep]
         self._inflight = []
@@ -399,8 +407,9 @@ class Context:
                      ctypes.cast(m, ctypes.POINTER(ctypes.c_double)) if m is not None else None)
         self._call(f"blgpu_context_set_{_slot}_style_gradient", ctypes.byref(g))
 
-    def set_fill_style_pattern(self, image, area=(0, 0, 0, 0), extend_mode=EXTEND_REPEAT, transform=None, _slot="fill"):
-        img, keep = make_image(image)
+    def set_fill_style_pattern(self, image, area=(0, 0, 0, 0), extend_mode=EXTEND_REPEAT, transform=None, _slot="fill",
+                               format: int | None = None):
+        img, keep = make_image(image, format)
         self._keep.append((img, keep))
         m = _mat(transform)
         p = Pattern(ctypes.pointer(img), (ctypes.c_int32 * 4)(*area), extend_mode,
@@ -444,20 +453,24 @@ class Context:
         self._call("blgpu_context_stroke_polygon_d", a.ctypes.data, a.shape[0])
 
     # -- image blits -----------------------------------------------------------------------------------
-    def _blit(self, name, args, image, area):
-        img, keep = make_image(image)
+    def _blit(self, name, args, image, area, format=None):
+        img, keep = make_image(image, format)
         self._keep.append((img, keep))
         ar = (ctypes.c_int32 * 4)(*area) if area is not None else None
         self._call(name, *args, ctypes.byref(img), ctypes.cast(ar, _P) if ar is not None else None)
 
-    def blit_image_i(self, x, y, image, area=None): self._blit("blgpu_context_blit_image_i", (x, y), image, area)
-    def blit_image_d(self, x, y, image, area=None): self._blit("blgpu_context_blit_image_d", (x, y), image, area)
+    # `format`: FORMAT_XRGB32 for a 32-bit image whose alpha bytes are to be read as 0xFF
+    def blit_image_i(self, x, y, image, area=None, format=None):
+        self._blit("blgpu_context_blit_image_i", (x, y), image, area, format)
 
-    def blit_scaled_image_i(self, x, y, w, h, image, area=None):
-        self._blit("blgpu_context_blit_scaled_image_i", (x, y, w, h), image, area)
+    def blit_image_d(self, x, y, image, area=None, format=None):
+        self._blit("blgpu_context_blit_image_d", (x, y), image, area, format)
 
-    def blit_scaled_image_d(self, x, y, w, h, image, area=None):
-        self._blit("blgpu_context_blit_scaled_image_d", (x, y, w, h), image, area)
+    def blit_scaled_image_i(self, x, y, w, h, image, area=None, format=None):
+        self._blit("blgpu_context_blit_scaled_image_i", (x, y, w, h), image, area, format)
+
+    def blit_scaled_image_d(self, x, y, w, h, image, area=None, format=None):
+        self._blit("blgpu_context_blit_scaled_image_d", (x, y, w, h), image, area, format)
 
     # -- masked fills (A8 masks: (h, w) uint8 arrays) ---------------------------------------------------
     def _fill_mask(self, name, x, y, mask, area):
@@ -543,12 +556,19 @@ def stream_size(stream: bytes) -> tuple[int, int]:
     return w, h
 
 
+def stream_format(stream: bytes) -> int:
+    """The target format a stream was recorded for (its header's 0 reads as PRGB32)."""
+    return struct.unpack_from("<I", stream, 20)[0] or FORMAT_PRGB32
+
+
 def render_stream(runtime: Runtime, stream: bytes, target=None):
-    """Renders a command stream into `target` (default: a new zeroed host image); returns it."""
+    """Renders a command stream into `target` (default: a new zeroed host image, uint8 for an A8
+    stream); returns it."""
+    fmt = stream_format(stream)
     if target is None:
         w, h = stream_size(stream)
-        target = np.zeros((h, w), dtype=np.uint32)
-    ctx = Context(runtime, target)
+        target = np.zeros((h, w), dtype=np.uint8 if fmt == FORMAT_A8 else np.uint32)
+    ctx = Context(runtime, target, fmt)
     try:
         ctx.submit_stream(stream)
         ctx.end()

@@ -90,13 +90,16 @@ BLResult BL_CDECL set_property_impl(BLObjectImpl*, const char*, size_t, const BL
 
 // --- conversions -----------------------------------------------------------------------------
 
+// The device view of an image whose BLFormat is `format`, or (`format` 0) PRGB32 or XRGB32, the
+// formats a pattern or blit source may have (BLGPU_FORMAT_* values are BLFormat's).
 bool gpu_image_of(const BLImageCore* img, uint32_t format, BLGpuImage& out, BLImageData& d) {
-  if (bl_image_get_data(img, &d) != BL_SUCCESS || d.format != format) return false;
+  if (bl_image_get_data(img, &d) != BL_SUCCESS) return false;
+  if (format ? d.format != format : (d.format != BL_FORMAT_PRGB32 && d.format != BL_FORMAT_XRGB32)) return false;
   out.pixel_data = d.pixel_data;
   out.stride = d.stride;
   out.width = d.size.w;
   out.height = d.size.h;
-  out.format = format == BL_FORMAT_A8 ? BLGPU_FORMAT_A8 : BLGPU_FORMAT_PRGB32;
+  out.format = d.format;
   out.flags = 0;
   return true;
 }
@@ -123,7 +126,7 @@ BLResult set_style_object(GpuImpl* self, uint32_t slot, const BLObjectCore* styl
     BL_PROPAGATE(bl_pattern_get_image(&p, &img));
     BLGpuImage gi{};
     BLImageData d;
-    if (!gpu_image_of(&img, BL_FORMAT_PRGB32, gi, d)) return kNotImplemented;
+    if (!gpu_image_of(&img, 0, gi, d)) return kNotImplemented;
     BLRectI area;
     BL_PROPAGATE(bl_pattern_get_area(&p, &area));
     BLMatrix2D t;
@@ -279,7 +282,7 @@ BLResult fill_mask_(GpuImpl* self, double x, double y, bool integral, const BLIm
 BLResult blit_(GpuImpl* self, int kind, const double* r, const BLImageCore* img, const BLRectI* area) {
   BLGpuImage gi{};
   BLImageData d;
-  if (!gpu_image_of(img, BL_FORMAT_PRGB32, gi, d)) return kNotImplemented;
+  if (!gpu_image_of(img, 0, gi, d)) return kNotImplemented;
   const int32_t a[4] = {area ? area->x : 0, area ? area->y : 0, area ? area->w : 0, area ? area->h : 0};
   const int32_t* ap = area ? a : nullptr;
   switch (kind) {
@@ -670,7 +673,7 @@ extern "C" BLResult blgpu_blcontext_begin(BLContextCore* self, BLImageCore* imag
   BLImageData d;
   BL_PROPAGATE(bl_image_make_mutable(image, &d));
   if (d.size.w <= 0 || d.size.h <= 0) return BL_ERROR_INVALID_VALUE;
-  if (d.format != BL_FORMAT_PRGB32) return kNotImplemented;
+  if (d.format != BL_FORMAT_PRGB32 && d.format != BL_FORMAT_XRGB32 && d.format != BL_FORMAT_A8) return kNotImplemented;
 
   BLResult err = BL_SUCCESS;
   BLGpuRuntime* rt = info && info->runtime ? info->runtime
@@ -689,7 +692,7 @@ extern "C" BLResult blgpu_blcontext_begin(BLContextCore* self, BLImageCore* imag
   bl_var_assign_rgba32(&impl->cur.style[1], 0xFF000000u);
   impl->image.assign(static_cast<const BLImage&>(*image));
 
-  BLGpuImage gi{d.pixel_data, d.stride, d.size.w, d.size.h, BLGPU_FORMAT_PRGB32, 0};
+  BLGpuImage gi{d.pixel_data, d.stride, d.size.w, d.size.h, d.format, 0};
   BLResult r = blgpu_context_create(&impl->gpu, rt);
   if (r == BL_SUCCESS) r = blgpu_context_begin(impl->gpu, &gi);
   if (r != BL_SUCCESS) {

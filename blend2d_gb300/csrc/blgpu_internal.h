@@ -99,7 +99,8 @@ struct alignas(16) DevStyle {
   uint32_t pat_wa, pat_wb, pat_wc, pat_wd;
   uint32_t ext_y;          // vertical extend: 0 pad, 1 repeat, 2 reflect
   uint32_t dither;         // gradient quality DITHER: 64-bit LUT (2 words per entry) + ordered dither
-  uint32_t pad2[2];
+  uint32_t src_or;         // OR-ed into every pattern fetch: 0xFF000000 when the source is read as XRGB32
+  uint32_t pad2;
   // pattern affine (32.32 fixed point)
   uint64_t af_xx, af_xy, af_yx, af_yy, af_tx, af_ty;
   int32_t af_ox, af_oy, af_rx, af_ry;
@@ -140,7 +141,8 @@ struct alignas(16) DevCanvas {
   uint32_t tile_base;      // first global tile index
   uint32_t row_base;       // first global tile-row index (command-list rows: row_base << list_log2)
   uint32_t cmd_first, cmd_count;
-  uint32_t pad[2];
+  uint32_t a8;             // 1: one byte per pixel (A8 target); pixels/stride then count bytes
+  uint32_t pad;
 };
 
 struct alignas(16) DevLutJob {
@@ -165,12 +167,14 @@ struct DevSeg {            // one non-horizontal 24.8 segment, y0 < y1
 enum ItemKind : uint32_t { kItemLine = 0, kItemQuad = 1, kItemCubic = 2, kItemConic = 3, kItemWhole = 4 };
 
 // A canvas copied between the runtime's canvas pool and a page-locked host image by a kernel (the
-// device reaches page-locked memory directly): rows of w pixels, strides in pixels.
+// device reaches page-locked memory directly): rows of w pixels, strides in pixels (one byte each
+// for an A8 canvas).
 struct DevXfer {
   uint32_t* dev;
   uint32_t* host;              // the host image's device-accessible address
   int32_t w, h;
   int32_t dev_stride, host_stride;
+  int32_t a8, pad;
 };
 
 // One line, curve or closing line of an analytic command, built independently of the command's

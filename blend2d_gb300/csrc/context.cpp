@@ -119,7 +119,42 @@ struct CtxStyle {
   BLGpuImage image{};
   uint64_t frame_gen = 0;       // frame generation the style was registered in
   uint32_t frame_index = 0;
+  uint64_t frame_gen_x = 0;     // the same for its copy whose pattern fetches read XRGB32
+  uint32_t frame_index_x = 0;
 };
+
+// BLFormat values a render target may have, with their bytes per pixel.
+static bool target_format_ok(uint32_t f) {
+  return f == BLGPU_FORMAT_PRGB32 || f == BLGPU_FORMAT_XRGB32 || f == BLGPU_FORMAT_A8;
+}
+static intptr_t format_bpp(uint32_t f) { return f == BLGPU_FORMAT_A8 ? 1 : 4; }
+
+// A host or device render target: PRGB32, XRGB32 or A8, at most 65,535 px a side.
+static bool valid_target(const BLGpuImage& im) {
+  return target_format_ok(im.format) && im.width > 0 && im.height > 0 && im.width <= 65535 &&
+         im.height <= 65535 && im.pixel_data && im.stride >= intptr_t(im.width) * format_bpp(im.format);
+}
+
+// SrcOver / SrcCopy simplified by the destination and source formats (CompOpSimplifyInfoImpl::
+// src_over / src_copy, compopsimplifyimpl_p.h:86-162). False for DstCopy (nothing drawn); else
+// `src_copy` and `xrgb_read`: the simplified source format is XRGB32, so a pattern fetcher reads
+// every texel with its alpha byte set (PixelIO<..., XRGB32>, pipeline/reference/pixelgeneric_p.h).
+// Solid and gradient fetchers do not look at the source format (fixedpiperuntime.cpp:250-270).
+//   SrcOver: ZERO32 -> DstCopy; FRGB32 -> SrcCopy; XRGB32 -> SrcCopy of XRGB32; PRGB32 -> SrcOver.
+//   SrcCopy: XRGB32 -> SrcCopy of XRGB32; PRGB32 into an XRGB32 target -> SrcCopy of XRGB32.
+// An A8 target's simplifications (opaque alpha, transparent) give the alpha these do.
+static bool simplify_comp_op(uint32_t dst_format, uint32_t op, int src_format, bool& src_copy, bool& xrgb_read) {
+  xrgb_read = src_format == kFmtXRGB32;
+  if (op == kCompOpSrcOver) {
+    if (src_format == kFmtZERO32) return false;
+    if (src_format == kFmtFRGB32 || xrgb_read) op = kCompOpSrcCopy;
+  }
+  else if (src_format == kFmtPRGB32 && dst_format == BLGPU_FORMAT_XRGB32) {
+    xrgb_read = true;
+  }
+  src_copy = op == kCompOpSrcCopy;
+  return true;
+}
 
 struct State {
   uint32_t comp_op = kCompOpSrcOver;
@@ -200,9 +235,13 @@ struct BLGpuContext {
 
   // --- frame registration ---------------------------------------------------------------
 
-  uint32_t register_style(CtxStyle& cs) {
-    if (cs.frame_gen == frame->generation) return cs.frame_index;
+  // The style's index in the frame; `xrgb_read`: the copy whose pattern fetches set the alpha byte.
+  uint32_t register_style(CtxStyle& cs, bool xrgb_read = false) {
+    xrgb_read = xrgb_read && cs.hs.dev.fetch >= kFetchPatAlignedPad;
+    if (!xrgb_read && cs.frame_gen == frame->generation) return cs.frame_index;
+    if (xrgb_read && cs.frame_gen_x == frame->generation) return cs.frame_index_x;
     DevStyle d = cs.hs.dev;
+    d.src_or = xrgb_read ? 0xFF000000u : 0u;
     if (d.lut_size) {
       if (d.dither) frame->lut_words = (frame->lut_words + 1u) & ~1u;   // 8-byte aligned entries
       DevLutJob job{};
@@ -219,9 +258,15 @@ struct BLGpuContext {
     }
     if (cs.has_image) d.src_offset += frame->add_image(cs.image);
     frame->styles.push_back(d);
-    cs.frame_gen = frame->generation;
-    cs.frame_index = uint32_t(frame->styles.size() - 1);
-    return cs.frame_index;
+    if (xrgb_read) {
+      cs.frame_gen_x = frame->generation;
+      cs.frame_index_x = uint32_t(frame->styles.size() - 1);
+    }
+    else {
+      cs.frame_gen = frame->generation;
+      cs.frame_index = uint32_t(frame->styles.size() - 1);
+    }
+    return uint32_t(frame->styles.size() - 1);
   }
 
   uint32_t register_clear_style() {
@@ -313,14 +358,10 @@ struct BLGpuContext {
     CtxStyle& cs = slot_style(slot);
     uint32_t alpha = slot ? s.stroke_alpha_i : s.fill_alpha_i;
     if (s.global_alpha_i == 0 || alpha == 0 || cs.hs.nop) return false;
-    uint32_t op = s.comp_op;
-    if (op == kCompOpSrcOver) {
-      if (cs.hs.format == kFmtZERO32) return false;
-      if (cs.hs.format == kFmtFRGB32) op = kCompOpSrcCopy;
-    }
-    f.src_copy = op == kCompOpSrcCopy;
+    bool xrgb_read = false;
+    if (!simplify_comp_op(target.format, s.comp_op, cs.hs.format, f.src_copy, xrgb_read)) return false;
     f.alpha = alpha;
-    f.style = register_style(cs);
+    f.style = register_style(cs, xrgb_read);
     return true;
   }
 
@@ -403,10 +444,7 @@ struct BLGpuContext {
   // --- API ---------------------------------------------------------------------------------
 
   BLGpuResult begin(const BLGpuImage* image) {
-    if (!image || image->format != BLGPU_FORMAT_PRGB32 || image->width <= 0 || image->height <= 0 ||
-        image->width > 65535 || image->height > 65535 || !image->pixel_data ||
-        image->stride < intptr_t(image->width) * 4)
-      return BLGPU_ERROR_INVALID_VALUE;
+    if (!image || !valid_target(*image)) return BLGPU_ERROR_INVALID_VALUE;
     if (bound) { BLGpuResult r = end(); if (r) return r; }
     target = *image;
     w = image->width;
@@ -582,6 +620,8 @@ struct BLGpuContext {
     cs.image = BLGpuImage{};
     cs.frame_gen = 0;
     cs.frame_index = 0;
+    cs.frame_gen_x = 0;
+    cs.frame_index_x = 0;
   }
   CtxStyle& slot_style(uint32_t slot) { return slot ? s.stroke_style : s.style; }
 
@@ -603,15 +643,16 @@ struct BLGpuContext {
     d.transform = g->transform;
     CtxStyle& cs = slot_style(slot);
     reset_style_slot(cs);
-    style_gradient(cs.hs, d, s.final_t, s.gradient_quality);
+    // gradients are not dithered into A8 targets (rastercontext.cpp:456-458)
+    style_gradient(cs.hs, d, s.final_t, target.format == BLGPU_FORMAT_A8 ? 0u : s.gradient_quality);
     return BLGPU_SUCCESS;
   }
 
   BLGpuResult set_style_pattern(const BLGpuPattern* p, uint32_t slot = 0) {
     if (!p || !p->image) return BLGPU_ERROR_INVALID_VALUE;
     const BLGpuImage& im = *p->image;
-    if (im.format != BLGPU_FORMAT_PRGB32 || im.width < 0 || im.height < 0 || (im.width && !im.pixel_data) ||
-        im.stride < intptr_t(im.width) * 4)
+    if ((im.format != BLGPU_FORMAT_PRGB32 && im.format != BLGPU_FORMAT_XRGB32) || im.width < 0 || im.height < 0 ||
+        (im.width && !im.pixel_data) || im.stride < intptr_t(im.width) * 4)
       return BLGPU_ERROR_INVALID_VALUE;
     if (p->extend_mode > 8) return BLGPU_ERROR_INVALID_VALUE;
     if (p->extend_mode > 2) return BLGPU_ERROR_NOT_IMPLEMENTED;   // complex (per-axis) extend modes
@@ -629,6 +670,8 @@ struct BLGpuContext {
     CtxStyle& cs = slot_style(slot);
     reset_style_slot(cs);
     style_pattern(cs.hs, d, s.pattern_quality, s.final_t);
+    // fetch_data->extra.format is the image's (rastercontext.cpp:415)
+    if (im.format == BLGPU_FORMAT_XRGB32) cs.hs.format = kFmtXRGB32;
     if (!cs.hs.nop) {
       cs.has_image = true;
       cs.image = im;
@@ -802,7 +845,7 @@ struct BLGpuContext {
   CtxStyle blit_style;
 
   static bool valid_image(const BLGpuImage* im) {
-    return im && im->format == BLGPU_FORMAT_PRGB32 && im->width >= 0 && im->height >= 0 &&
+    return im && (im->format == BLGPU_FORMAT_PRGB32 || im->format == BLGPU_FORMAT_XRGB32) && im->width >= 0 && im->height >= 0 &&
            (im->width == 0 || im->pixel_data) && im->stride >= intptr_t(im->width) * 4;
   }
 
@@ -820,16 +863,19 @@ struct BLGpuContext {
     return true;
   }
 
-  // resolve_blit_op (rastercontext.cpp:1331-1342) for a PRGB32 image: the comp-op as set, the
-  // global alpha; false when the global alpha is zero.
+  // resolve_blit_op (rastercontext.cpp:1331-1342): the comp-op simplified for the image's format,
+  // the global alpha; false when the global alpha is zero.
   bool resolve_blit(Fill& f, const BLGpuImage& im) {
     if (s.global_alpha_i == 0 || blit_style.hs.nop) return false;
-    f.src_copy = s.comp_op == kCompOpSrcCopy;
+    bool xrgb_read = false;
+    simplify_comp_op(target.format, s.comp_op, im.format == BLGPU_FORMAT_XRGB32 ? kFmtXRGB32 : kFmtPRGB32,
+                     f.src_copy, xrgb_read);
     f.alpha = s.global_alpha_i;
     blit_style.has_image = true;
     blit_style.image = im;
     blit_style.frame_gen = 0;
-    f.style = register_style(blit_style);
+    blit_style.frame_gen_x = 0;
+    f.style = register_style(blit_style, xrgb_read);
     return true;
   }
 
@@ -1031,6 +1077,8 @@ BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
   memcpy(&hdr, base, sizeof(hdr));
   if (hdr.magic != BLGPU_STREAM_MAGIC || hdr.version != BLGPU_STREAM_VERSION) return BLGPU_ERROR_INVALID_VALUE;
   if (int(hdr.width) != w || int(hdr.height) != h) return BLGPU_ERROR_INVALID_VALUE;
+  // the stream was recorded for a target of this format (0 reads as PRGB32)
+  if ((hdr.format ? hdr.format : uint32_t(BLGPU_FORMAT_PRGB32)) != target.format) return BLGPU_ERROR_INVALID_VALUE;
   size_t off = sizeof(hdr);
   std::vector<BLGpuImage> images(hdr.image_count);
   for (uint32_t i = 0; i < hdr.image_count; i++) {
@@ -1042,8 +1090,10 @@ BLGpuResult BLGpuContext::submit_stream(const uint8_t* base, size_t size) {
     if (im.width > 65535 || im.height > 65535 || off + n * 4u > size) return BLGPU_ERROR_INVALID_VALUE;
     stream_images->emplace_back(n ? n : 1);
     memcpy(stream_images->back().data(), base + off, n * 4u);
+    if (im.format != 0 && im.format != BLGPU_FORMAT_PRGB32 && im.format != BLGPU_FORMAT_XRGB32)
+      return BLGPU_ERROR_INVALID_VALUE;
     images[i] = BLGpuImage{stream_images->back().data(), intptr_t(im.width) * 4, int32_t(im.width), int32_t(im.height),
-                           BLGPU_FORMAT_PRGB32, 0};
+                           im.format == BLGPU_FORMAT_XRGB32 ? uint32_t(BLGPU_FORMAT_XRGB32) : uint32_t(BLGPU_FORMAT_PRGB32), 0};
     off += (n * 4u + 7u) & ~size_t(7);
   }
   while (off + 8 <= size) {
@@ -1489,12 +1539,8 @@ BLGPU_API BLGpuResult blgpu_render_batch(BLGpuRuntime* rt, const void* const* st
                                          const BLGpuImage* images, uint32_t count) {
   if (!rt || (count && (!streams || !sizes || !images))) return BLGPU_ERROR_INVALID_VALUE;
   if (!count) return BLGPU_SUCCESS;
-  for (uint32_t i = 0; i < count; i++) {
-    const BLGpuImage& im = images[i];
-    if (im.format != BLGPU_FORMAT_PRGB32 || im.width <= 0 || im.height <= 0 || im.width > 65535 ||
-        im.height > 65535 || !im.pixel_data || im.stride < intptr_t(im.width) * 4)
-      return BLGPU_ERROR_INVALID_VALUE;
-  }
+  for (uint32_t i = 0; i < count; i++)
+    if (!valid_target(images[i])) return BLGPU_ERROR_INVALID_VALUE;
   std::lock_guard<std::mutex> guard(rt->batch_lock);
   Frame& frame = rt->batch_frame;
   std::vector<BLGpuContext> ctxs(count);
@@ -1570,9 +1616,8 @@ BLGPU_API BLGpuResult blgpu_render_stream_noalloc(BLGpuRuntime* rt, const void* 
                                                   const BLGpuImage* device_image) {
   if (!rt || !stream || !device_image) return BLGPU_ERROR_INVALID_VALUE;
   const BLGpuImage& im = *device_image;
-  if (!(im.flags & BLGPU_IMAGE_DEVICE_MEMORY) || im.format != BLGPU_FORMAT_PRGB32 || im.width <= 0 ||
-      im.height <= 0 || im.width > 65535 || im.height > 65535 || !im.pixel_data ||
-      im.stride < intptr_t(im.width) * 4 || (im.stride & 15) || (reinterpret_cast<uintptr_t>(im.pixel_data) & 15))
+  if (!(im.flags & BLGPU_IMAGE_DEVICE_MEMORY) || !valid_target(im) || (im.stride & 15) ||
+      (reinterpret_cast<uintptr_t>(im.pixel_data) & 15))
     return BLGPU_ERROR_INVALID_VALUE;
   // one scratch area per device: this process's calls on the device take turns
   std::lock_guard<std::mutex> guard(noalloc_lock(rt->rt.device));

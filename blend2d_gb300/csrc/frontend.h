@@ -17,7 +17,7 @@ namespace blgpu {
 struct Mat { double m00, m01, m10, m11, m20, m21; };
 
 enum TransformType : int { kTTIdentity = 0, kTTTranslate, kTTScale, kTTSwap, kTTAffine, kTTInvalid };
-enum SrcFormat : int { kFmtPRGB32 = 0, kFmtFRGB32 = 1, kFmtZERO32 = 2 };
+enum SrcFormat : int { kFmtPRGB32 = 0, kFmtFRGB32 = 1, kFmtZERO32 = 2, kFmtXRGB32 = 3 };
 
 int trunc_to_int(double x);
 int64_t floor_to_int64(double x);

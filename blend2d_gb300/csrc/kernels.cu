@@ -898,6 +898,13 @@ __global__ void __launch_bounds__(256) canvas_copy_kernel(const DevXfer* xfers, 
   const DevXfer t = xfers[i];
   const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
   for (int y = int(blockIdx.y) * warps + (threadIdx.x >> 5); y < t.h; y += int(gridDim.y) * warps) {
+    if (t.a8) {      // strides in bytes
+      const uint8_t* src = reinterpret_cast<const uint8_t*>(to_host ? t.dev : t.host) +
+                           int64_t(y) * (to_host ? t.dev_stride : t.host_stride);
+      uint8_t* dst = reinterpret_cast<uint8_t*>(to_host ? t.host : t.dev) + int64_t(y) * (to_host ? t.host_stride : t.dev_stride);
+      for (int x = lane; x < t.w; x += 32) dst[x] = src[x];
+      continue;
+    }
     const uint32_t* src = to_host ? t.dev + int64_t(y) * t.dev_stride : t.host + int64_t(y) * t.host_stride;
     uint32_t* dst = to_host ? t.host + int64_t(y) * t.host_stride : t.dev + int64_t(y) * t.dev_stride;
     for (int x = lane; x < t.w; x += 32) dst[x] = src[x];
@@ -1244,10 +1251,25 @@ __global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
     int y = row0 + prow, xp = x_base + pcol;
     bool row_ok = y < cv.h;
     uint32_t* dst = cv.pixels + int64_t(y) * cv.stride + xp;
+    // an A8 canvas: one byte per pixel, composited as the alpha byte of a 32-bit pixel (the
+    // reference's P8_Alpha operators are its P32 operators' alpha lane); rows start at 16-byte
+    // boundaries and xp is a multiple of 4, so 4 pixels are one aligned word
+    uint8_t* dst8 = reinterpret_cast<uint8_t*>(cv.pixels) + int64_t(y) * cv.stride + xp;
 
     uint32_t pix[4];
     bool full = row_ok && (xp + 3 < cv.w);
-    if (full) {
+    if (cv.a8) {
+      if (full) {
+        const uint32_t v = *reinterpret_cast<const uint32_t*>(dst8);
+#pragma unroll
+        for (int k = 0; k < 4; k++) pix[k] = ((v >> (8 * k)) & 0xFFu) << 24;
+      }
+      else {
+#pragma unroll
+        for (int k = 0; k < 4; k++) pix[k] = (row_ok && xp + k < cv.w) ? uint32_t(dst8[k]) << 24 : 0u;
+      }
+    }
+    else if (full) {
       uint4 v = *reinterpret_cast<const uint4*>(dst);
       pix[0] = v.x; pix[1] = v.y; pix[2] = v.z; pix[3] = v.w;
     }
@@ -1369,7 +1391,7 @@ __global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
 #pragma unroll 1
             for (int k = 0; k < 4; k++) {
               if (m[0] && xp + k < cv.w) {
-                uint32_t sv = px::fetch(st, rs, xp + k, f.luts, f.images);
+                uint32_t sv = px::fetch(st, rs, xp + k, f.luts, f.images) | st.src_or;
                 pix[0] = px::composite(pix[0], sv, m[0], src_copy);
                 n++;
               }
@@ -1383,7 +1405,17 @@ __global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
       }
     }
 
-    if (full) {
+    if (cv.a8) {
+      if (full) {
+        *reinterpret_cast<uint32_t*>(dst8) = (pix[0] >> 24) | ((pix[1] >> 24) << 8) | ((pix[2] >> 24) << 16) |
+                                             (pix[3] & 0xFF000000u);
+      }
+      else {
+#pragma unroll
+        for (int k = 0; k < 4; k++) if (row_ok && xp + k < cv.w) dst8[k] = uint8_t(pix[k] >> 24);
+      }
+    }
+    else if (full) {
       *reinterpret_cast<uint4*>(dst) = make_uint4(pix[0], pix[1], pix[2], pix[3]);
     }
     else {

@@ -39,6 +39,18 @@ int last_cuda_error() { return g_last_cuda_error.load(); }
 
 static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
 
+// Bytes per pixel of a canvas: an A8 target stays one byte per pixel on the device as well.
+static inline int32_t canvas_bpp(const BLGpuImage& im) { return im.format == BLGPU_FORMAT_A8 ? 1 : 4; }
+// Row pitch, in pixels, of a canvas kept in the runtime's canvas pool: rows start at 16 bytes.
+static inline int32_t pooled_stride(const BLGpuImage& im) {
+  return int32_t(align_up(size_t(uint32_t(im.width)), canvas_bpp(im) == 1 ? 16 : 4));
+}
+// 32-bit words of the canvas pool a canvas takes (every canvas starts at a 256-byte boundary).
+static inline uint64_t pooled_words(const BLGpuImage& im) {
+  const uint64_t bytes = uint64_t(pooled_stride(im)) * uint32_t(im.height) * uint32_t(canvas_bpp(im));
+  return align_up((bytes + 3) / 4, 64);
+}
+
 // --- Frame ------------------------------------------------------------------------------------
 
 // Generations are unique across all frames of the process: a context records into two frames in
@@ -77,6 +89,7 @@ uint32_t Frame::add_canvas(const BLGpuImage& image, bool upload) {
   cv.row_base = rows;
   cv.cmd_first = uint32_t(cmds.size());
   cv.cmd_count = 0;
+  cv.a8 = image.format == BLGPU_FORMAT_A8 ? 1u : 0u;
   tiles += uint32_t(cv.tiles_x) * uint32_t(cv.tiles_y);
   rows += uint32_t(cv.tiles_y);
   canvases.push_back(cv);
@@ -303,7 +316,7 @@ void Runtime::destroy() {
 
 bool device_target_direct(const BLGpuImage& im) {
   return (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) && (reinterpret_cast<uintptr_t>(im.pixel_data) & 15u) == 0 &&
-         (im.stride & 15) == 0 && im.stride >= intptr_t(im.width) * 4;
+         (im.stride & 15) == 0 && im.stride >= intptr_t(im.width) * canvas_bpp(im);
 }
 
 // Stroke sizing: the stroke inputs go to the device and the count pass runs once, so the frame's
@@ -405,7 +418,7 @@ FrameSizes sizes_of(const Frame& fr, uint32_t outline_verts) {
   z.lut_words = fr.lut_words;
   for (const FrameTarget& t : fr.targets)
     if (!device_target_direct(t.image))
-      z.canvas_words += align_up(uint64_t(align_up(uint32_t(t.image.width), 4)) * uint32_t(t.image.height), 64);
+      z.canvas_words += pooled_words(t.image);
   return z;
 }
 
@@ -455,7 +468,7 @@ BLGpuResult Runtime::upload_frame(const Frame& fr, const FrameSizes* caps) {
         const BLGpuImage& im = fr.targets[i].image;
         if (device_target_direct(im)) { (*cpix)[i] = static_cast<uint32_t*>(im.pixel_data); continue; }
         (*cpix)[i] = pool ? pool + off : nullptr;
-        off += align_up(size_t(align_up(uint32_t(im.width), 4)) * uint32_t(im.height), 64);
+        off += pooled_words(im);
       }
     }
     v.items = L.take<DevItem>(item_capacity);
@@ -549,7 +562,7 @@ BLGpuResult Runtime::upload_frame(const Frame& fr, const FrameSizes* caps) {
   for (uint32_t i = 0; i < ncv; i++) {
     const BLGpuImage& im = fr.targets[i].image;
     cvs[i].pixels = canvas_dev[i];
-    cvs[i].stride = device_target_direct(im) ? int32_t(im.stride / 4) : int32_t(align_up(uint32_t(im.width), 4));
+    cvs[i].stride = device_target_direct(im) ? int32_t(im.stride / canvas_bpp(im)) : pooled_stride(im);
     canvas_stride[i] = cvs[i].stride;
   }
   BLGPU_CHECK(put(v.canvases, cvs.data(), sizeof(DevCanvas) * ncv, false));
@@ -693,7 +706,7 @@ BLGpuResult Runtime::stage_canvases(const Frame& fr) {
   for (uint32_t i = 0; i < ncv; i++) {
     const BLGpuImage& im = fr.targets[i].image;
     if (device_target_direct(im) || im.width == 0 || im.height == 0 || (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) ||
-        (im.stride & 3) != 0)
+        (im.stride % canvas_bpp(im)) != 0)
       continue;
     // page-locked host memory is reachable from the device at the address the driver reports
     cudaPointerAttributes a{};
@@ -701,7 +714,7 @@ BLGpuResult Runtime::stage_canvases(const Frame& fr) {
     if (a.type != cudaMemoryTypeHost || !a.devicePointer) continue;
     canvas_xfer[i] = int32_t(xfers.size());
     xfers.push_back(DevXfer{canvas_dev[i], static_cast<uint32_t*>(a.devicePointer), im.width, im.height,
-                            canvas_stride[i], int32_t(im.stride / 4)});
+                            canvas_stride[i], int32_t(im.stride / canvas_bpp(im)), canvas_bpp(im) == 1 ? 1 : 0, 0});
   }
   if (!xfers.empty()) {
     BLGPU_CHECK(xfer_buf.reserve(sizeof(DevXfer) * xfers.size()));
@@ -714,10 +727,11 @@ BLGpuResult Runtime::stage_canvases(const Frame& fr) {
     const BLGpuImage& im = t.image;
     if (!t.upload || device_target_direct(im) || im.width == 0 || im.height == 0) continue;
     const bool dev = (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) != 0;
-    if (!dev) h2d_bytes += uint64_t(uint32_t(im.width)) * uint32_t(im.height) * 4u;
+    const size_t bpp = size_t(canvas_bpp(im));
+    if (!dev) h2d_bytes += uint64_t(uint32_t(im.width)) * uint32_t(im.height) * bpp;
     if (canvas_xfer[i] >= 0) continue;
-    BLGPU_CHECK(cudaMemcpy2DAsync(canvas_dev[i], size_t(canvas_stride[i]) * 4u, im.pixel_data, size_t(im.stride),
-                                  size_t(im.width) * 4u, size_t(im.height),
+    BLGPU_CHECK(cudaMemcpy2DAsync(canvas_dev[i], size_t(canvas_stride[i]) * bpp, im.pixel_data, size_t(im.stride),
+                                  size_t(im.width) * bpp, size_t(im.height),
                                   dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
   }
   // the kernel copy of the page-locked ones, when any of them is uploaded: copy all of them up
@@ -750,14 +764,15 @@ BLGpuResult Runtime::download() {
   for (size_t i = 0; i < targets.size(); i++) {
     const BLGpuImage& im = targets[i].image;
     if (device_target_direct(im) || im.width == 0 || im.height == 0) continue;
+    const size_t bpp = size_t(canvas_bpp(im));
     if (i < canvas_xfer.size() && canvas_xfer[i] >= 0) {
-      d2h_bytes += uint64_t(uint32_t(im.width)) * uint32_t(im.height) * 4u;
+      d2h_bytes += uint64_t(uint32_t(im.width)) * uint32_t(im.height) * bpp;
       continue;
     }
     bool dev = (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) != 0;
-    if (!dev) d2h_bytes += uint64_t(uint32_t(im.width)) * uint32_t(im.height) * 4u;
-    BLGPU_CHECK(cudaMemcpy2DAsync(im.pixel_data, size_t(im.stride), canvas_dev[i], size_t(canvas_stride[i]) * 4u,
-                                  size_t(im.width) * 4u, size_t(im.height),
+    if (!dev) d2h_bytes += uint64_t(uint32_t(im.width)) * uint32_t(im.height) * bpp;
+    BLGPU_CHECK(cudaMemcpy2DAsync(im.pixel_data, size_t(im.stride), canvas_dev[i], size_t(canvas_stride[i]) * bpp,
+                                  size_t(im.width) * bpp, size_t(im.height),
                                   dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream));
   }
   return BLGPU_SUCCESS;
@@ -1076,7 +1091,7 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
   DevCanvas cv = fr.canvases[0];
   const BLGpuImage& im = fr.targets[0].image;
   cv.pixels = static_cast<uint32_t*>(im.pixel_data);
-  cv.stride = int32_t(im.stride / 4);
+  cv.stride = int32_t(im.stride / canvas_bpp(im));
   uint32_t counts[kCntWords] = {};
   counts[kCntCmds] = nc;
   counts[kCntCanvases] = 1;
@@ -1226,13 +1241,13 @@ BLGpuResult Runtime::autotune(int trials, LaunchConfig* best_out, double* best_m
   // save every canvas
   size_t bytes = 0;
   for (size_t i = 0; i < targets.size(); i++)
-    bytes += size_t(targets[i].image.height) * size_t(canvas_stride[i]) * 4u;
+    bytes += size_t(targets[i].image.height) * size_t(canvas_stride[i]) * size_t(canvas_bpp(targets[i].image));
   void* save = nullptr;
   if (bytes) BLGPU_CHECK(cudaMalloc(&save, bytes));
   auto copy_canvases = [&](bool to_save) -> cudaError_t {
     size_t off = 0;
     for (size_t i = 0; i < targets.size(); i++) {
-      size_t pitch = size_t(canvas_stride[i]) * 4u, h = size_t(targets[i].image.height);
+      size_t pitch = size_t(canvas_stride[i]) * size_t(canvas_bpp(targets[i].image)), h = size_t(targets[i].image.height);
       char* a = static_cast<char*>(save) + off;
       cudaError_t e = to_save ? cudaMemcpyAsync(a, canvas_dev[i], pitch * h, cudaMemcpyDeviceToDevice, stream)
                               : cudaMemcpyAsync(canvas_dev[i], a, pitch * h, cudaMemcpyDeviceToDevice, stream);

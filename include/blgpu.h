@@ -37,7 +37,8 @@ enum {
 /* Image formats (BLFormat) and image-placement flags. */
 enum {
   BLGPU_FORMAT_PRGB32 = 1,                   /* BL_FORMAT_PRGB32 */
-  BLGPU_FORMAT_A8 = 3,                       /* BL_FORMAT_A8 (masks for fill_mask) */
+  BLGPU_FORMAT_XRGB32 = 2,                   /* BL_FORMAT_XRGB32 (targets; pattern and blit sources) */
+  BLGPU_FORMAT_A8 = 3,                       /* BL_FORMAT_A8 (targets; masks for fill_mask) */
   BLGPU_IMAGE_DEVICE_MEMORY = 0x1u           /* pixel_data is a CUDA device pointer */
 };
 
@@ -70,11 +71,16 @@ typedef struct BLGpuRuntimeCreateInfo {
   uint32_t reserved[4];
 } BLGpuRuntimeCreateInfo;
 
+/* An image (BLImageData). A render target is PRGB32, XRGB32 or A8. The reference renders into
+   an XRGB32 target with the PRGB32 pipelines, its comp-ops simplified for that format
+   (compopsimplifyimpl_p.h), and into an A8 target with the alpha byte of the same arithmetic,
+   without dithering. Pattern and blit sources are PRGB32 or XRGB32, whose texels are read with
+   the alpha byte set. fill_mask masks are A8. */
 typedef struct BLGpuImage {
-  void* pixel_data;        /* PRGB32 pixels (host memory unless BLGPU_IMAGE_DEVICE_MEMORY) */
+  void* pixel_data;        /* pixels (host memory unless BLGPU_IMAGE_DEVICE_MEMORY) */
   intptr_t stride;         /* bytes per row */
   int32_t width, height;
-  uint32_t format;         /* BLGPU_FORMAT_PRGB32 */
+  uint32_t format;         /* BLGPU_FORMAT_* */
   uint32_t flags;          /* BLGPU_IMAGE_* */
 } BLGpuImage;
 

@@ -38,7 +38,7 @@ typedef struct BLGpuContextCreateInfo {
 } BLGpuContextCreateInfo;
 
 /* Mirrors bl_context_begin (blend2d/core/context.cpp:316-328): replaces `self` with a GPU
- * rendering context bound to `image` (PRGB32). The impl is allocated like the raster context's
+ * rendering context bound to `image` (PRGB32, XRGB32 or A8). The impl is allocated like the raster context's
  * (bl_object_alloc_impl_aligned with a BL_OBJECT_TYPE_CONTEXT marker, rastercontext.cpp:4626-4627),
  * so BLContext's destructor, reset() and end() release it; its destruction renders what is still
  * recorded into the image. */

@@ -29,26 +29,30 @@ static bool same_pixels(const BLImage& a, const BLImage& b, size_t& differ) {
   a.get_data(&da);
   b.get_data(&db);
   differ = 0;
-  if (da.size != db.size) { differ = size_t(-1); return false; }
+  if (da.size != db.size || da.format != db.format) { differ = size_t(-1); return false; }
+  const size_t bpp = da.format == BL_FORMAT_A8 ? 1u : 4u;
   for (int y = 0; y < da.size.h; y++) {
-    const uint32_t* pa = reinterpret_cast<const uint32_t*>(static_cast<const uint8_t*>(da.pixel_data) + intptr_t(y) * da.stride);
-    const uint32_t* pb = reinterpret_cast<const uint32_t*>(static_cast<const uint8_t*>(db.pixel_data) + intptr_t(y) * db.stride);
-    for (int x = 0; x < da.size.w; x++) differ += pa[x] != pb[x];
+    const uint8_t* pa = static_cast<const uint8_t*>(da.pixel_data) + intptr_t(y) * da.stride;
+    const uint8_t* pb = static_cast<const uint8_t*>(db.pixel_data) + intptr_t(y) * db.stride;
+    for (int x = 0; x < da.size.w; x++) differ += memcmp(pa + size_t(x) * bpp, pb + size_t(x) * bpp, bpp) != 0;
   }
   return differ == 0;
 }
 
-static BLImage blank(int w, int h) {
-  BLImage img(w, h, BL_FORMAT_PRGB32);
+static BLImage blank(int w, int h, BLFormat format = BL_FORMAT_PRGB32) {
+  BLImage img(w, h, format);
   BLImageData d;
   img.make_mutable(&d);
-  for (int y = 0; y < h; y++) memset(static_cast<uint8_t*>(d.pixel_data) + intptr_t(y) * d.stride, 0, size_t(w) * 4u);
+  const size_t bpp = format == BL_FORMAT_A8 ? 1u : 4u;
+  for (int y = 0; y < h; y++) memset(static_cast<uint8_t*>(d.pixel_data) + intptr_t(y) * d.stride, 0, size_t(w) * bpp);
   return img;
 }
 
-// Draws `scene` into a reference context and into a GPU context; returns the differing pixels.
-static size_t compare(int w, int h, const std::function<void(BLContext&)>& scene, std::string& error) {
-  BLImage ref = blank(w, h), gpu = blank(w, h);
+// Draws `scene` into a reference context and into a GPU context, both bound to a zeroed image of
+// `format`; returns the differing pixels.
+static size_t compare(int w, int h, const std::function<void(BLContext&)>& scene, std::string& error,
+                      BLFormat format = BL_FORMAT_PRGB32) {
+  BLImage ref = blank(w, h, format), gpu = blank(w, h, format);
   {
     BLContextCreateInfo cci{};
     BLContext ctx(ref, cci);
@@ -133,7 +137,8 @@ static int check_streams(const char* list) {
     s.size = buf.size();
     parse_header(s);
     std::string err;
-    const size_t d = compare(int(s.hdr.width), int(s.hdr.height), [&](BLContext& ctx) { replay_records(s, ctx); }, err);
+    const size_t d = compare(int(s.hdr.width), int(s.hdr.height), [&](BLContext& ctx) { replay_records(s, ctx); }, err,
+                             target_format(s));
     n++;
     if (d) {
       failed++;

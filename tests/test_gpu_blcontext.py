@@ -16,7 +16,10 @@ pytestmark = [pytest.mark.gpu,
 
 STREAM_SCENES = ["polygons", "curves_2k", "patterns_1k", "edge_cases", "conics", "mix_0", "mix_1", "mix_2", "mix_5",
                  "mix_notf_0", "mix_wide", "mix_tall", "mix_dither_1", "strokes_0", "strokes_wide", "strokes_lines",
-                 "stroked_paths_2k", "blits_0", "blits_tall", "masks_0", "shapes_0", "shapes_1", "batch_0", "batch_3"]
+                 "stroked_paths_2k", "blits_0", "blits_tall", "masks_0", "shapes_0", "shapes_1", "batch_0", "batch_3",
+                 # XRGB32 and A8 targets, XRGB32 pattern and blit sources
+                 "mix_xrgb_0", "mix_xrgb_1", "mix_a8_0", "mix_a8_1", "mix_a8_dither", "mix_xrgb_images_0",
+                 "blits_xrgb_images_xrgb", "blits_xrgb_images_a8"]
 
 
 def test_recorded_scenes_through_blcontext():

@@ -762,3 +762,100 @@ def test_page_locked_host_images_match_pageable_ones():
             bg.render_stream(rt, s, q)
             assert not _diff(q.numpy().view(np.uint32), p), f"canvas {i}"
             assert not _diff(p, pageable[i]), f"canvas {i} alone vs batched"
+
+
+FORMAT_CASES = [(seed, w, h, fmt, xrgb) for seed, (w, h), fmt, xrgb in
+                zip(range(1200, 1224), [(257, 257), (61, 37), (1, 1), (333, 97), (129, 130), (5, 600)] * 4,
+                    [scenes.FORMAT_XRGB32, scenes.FORMAT_A8] * 12, [False, False, True, True] * 6)]
+
+
+@pytest.mark.parametrize("seed,w,h,fmt,xrgb", FORMAT_CASES)
+def test_target_formats_vs_oracle(runtimes, seed, w, h, fmt, xrgb):
+    """XRGB32 and A8 targets (and XRGB32 pattern sources): the comp-op simplified for the formats,
+    pattern texels read with their alpha set, A8 canvases one byte per pixel on the device."""
+    stream = scenes.random_mix(seed, width=w, height=h, count=150, format=fmt, xrgb_images=xrgb,
+                               dither=seed % 3 == 0).to_bytes()
+    got = bg.render_stream(runtimes(), stream)
+    want = oracle_lib.render(stream)
+    assert got.dtype == want.dtype
+    assert not _diff(got, want), _diff(got, want)
+
+
+@pytest.mark.parametrize("fmt", [scenes.FORMAT_PRGB32, scenes.FORMAT_XRGB32, scenes.FORMAT_A8])
+def test_blits_of_xrgb_images_vs_oracle(runtimes, fmt):
+    stream = scenes.blits(seed=46, format=fmt, xrgb_images=True).to_bytes()
+    got = bg.render_stream(runtimes(), stream)
+    want = oracle_lib.render(stream)
+    assert not _diff(got, want), _diff(got, want)
+
+
+def test_target_formats_on_device_pinned_and_batched(runtimes):
+    """A8 and XRGB32 canvases as CUDA tensors (aligned rows are rendered in place, others are
+    staged), page-locked and pageable host images, and one batch mixing the three formats onto
+    existing content."""
+    torch = pytest.importorskip("torch")
+    rt = runtimes()
+    rng = np.random.default_rng(1230)
+    streams, init = [], []
+    for i, (w, h) in enumerate([(256, 64), (131, 77), (16, 9), (97, 40), (1, 1), (203, 101)]):
+        fmt = (scenes.FORMAT_A8, scenes.FORMAT_XRGB32, scenes.FORMAT_PRGB32)[i % 3]
+        streams.append(scenes.random_mix(1240 + i, width=w, height=h, count=120, format=fmt,
+                                         xrgb_images=i % 2 == 0, alphas=True).to_bytes())
+        dt = np.uint8 if fmt == scenes.FORMAT_A8 else np.uint32
+        init.append(rng.integers(0, 256 if dt == np.uint8 else 2**32, (h, w), dtype=np.uint64).astype(dt))
+    want = []
+    for s, a in zip(streams, init):
+        # the oracle starts from zeros: compare runs onto zeroed canvases with it, and runs onto
+        # existing content with each other
+        want.append(oracle_lib.render(s))
+    for i, s in enumerate(streams):
+        h, w = init[i].shape
+        a8 = init[i].dtype == np.uint8
+        dev = torch.zeros((h, w), dtype=torch.uint8 if a8 else torch.int32, device="cuda")
+        bg.render_stream(rt, s, dev)
+        torch.cuda.synchronize()
+        got = dev.cpu().numpy()
+        got = got if a8 else got.view(np.uint32)
+        assert not _diff(got, want[i]), f"device canvas {i}: {_diff(got, want[i])}"
+        pinned = torch.zeros((h, w), dtype=torch.uint8 if a8 else torch.int32).pin_memory()
+        bg.render_stream(rt, s, pinned)
+        got = pinned.numpy() if a8 else pinned.numpy().view(np.uint32)
+        assert not _diff(got, want[i]), f"page-locked canvas {i}: {_diff(got, want[i])}"
+    batched = [a.copy() for a in init]
+    rt.render_batch(streams, batched)
+    for i, s in enumerate(streams):
+        alone = init[i].copy()
+        bg.render_stream(rt, s, alone)
+        assert not _diff(batched[i], alone), f"canvas {i} batched vs alone"
+
+
+def test_target_format_context_calls(runtimes):
+    """The context API on XRGB32 and A8 targets gives what the same calls recorded as a stream
+    give on the oracle; a stream recorded for another format is refused."""
+    rt = runtimes()
+    img = scenes.premultiplied_noise(np.random.default_rng(3), 23, 17)
+    for fmt in (scenes.FORMAT_XRGB32, scenes.FORMAT_A8):
+        sw = scenes.StreamWriter(90, 70, fmt)
+        x = sw.add_image(img, scenes.FORMAT_XRGB32)
+        p = sw.add_image(img)
+        target = np.zeros((70, 90), dtype=np.uint8 if fmt == scenes.FORMAT_A8 else np.uint32)
+        ctx = bg.Context(rt, target, fmt)
+        try:
+            for op in (scenes.SRC_OVER, scenes.SRC_COPY):
+                sw.comp_op(op); ctx.set_comp_op(op)
+                sw.solid(0x80FF2010); ctx.set_fill_style_rgba32(0x80FF2010)
+                sw.fill_rect_d(3.5, 4.25, 40, 20); ctx.fill_rect_d(3.5, 4.25, 40, 20)
+                sw.pattern(x, scenes.REPEAT, transform=[1, 0.2, -0.1, 1, 10, 5])
+                ctx.set_fill_style_pattern(img, extend_mode=bg.EXTEND_REPEAT, transform=[1, 0.2, -0.1, 1, 10, 5],
+                                           format=bg.FORMAT_XRGB32)
+                sw.fill_rect_d(20, 30, 50, 30); ctx.fill_rect_d(20, 30, 50, 30)
+                sw.blit_image_d(50.5, 2.25, p); ctx.blit_image_d(50.5, 2.25, img)
+                sw.blit_image_i(1, 50, x); ctx.blit_image_i(1, 50, img, format=bg.FORMAT_XRGB32)
+            ctx.end()
+        finally:
+            ctx.close()
+        want = oracle_lib.render(sw.to_bytes())
+        assert not _diff(target, want), f"format {fmt}: {_diff(target, want)}"
+    prgb_stream = scenes.random_mix(1250, width=40, height=30, count=10).to_bytes()
+    with pytest.raises(bg.BLGpuError):
+        bg.render_stream(rt, prgb_stream, np.zeros((30, 40), dtype=np.uint8))
