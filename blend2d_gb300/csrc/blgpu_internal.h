@@ -291,7 +291,8 @@ struct FrameView {
   uint4* row_recs;             // command lists per list row, painter's order: two records per entry,
                                //   {command, pixel columns x0 | x1 << 16, rows y0 | y1 << 16, meta}
                                //   {first slot, tile column tx0 | columns << 16, style, first row state}
-                               //   with meta = kind | flags << 2 | alpha << 4
+                               //   with meta = kind | flags << 2 | alpha << 4; for a solid style the
+                               //   style word has bit 31 set and the colour replaces the row state
   uint32_t* row_copies;        // [num_rows] SrcCopy commands in each tile row's list
   uint32_t* strip_start;       // [num_tiles * strips per tile] first list entry the composite needs (occlusion)
   uint32_t* tile_order;        // tile processing order for the persistent fine kernel

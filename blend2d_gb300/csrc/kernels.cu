@@ -928,6 +928,8 @@ int launch_backdrop_prefix(const FrameView& f, cudaStream_t st) {
   return 1;
 }
 
+constexpr uint32_t kRecSolid = 0x80000000u;   // command-list record: the style is solid, its colour in the record
+
 // Per tile row: commands overlapping the row in painter's order (one block per row).
 __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
   __shared__ uint32_t smem[32];
@@ -951,13 +953,16 @@ __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
     if (flag) {
       // everything the composite needs of the command to test it against a strip and find its
       // slot, gathered once here for every strip of the list row
+      // A solid style's colour takes the place of the row-state base it does not use, with bit 31
+      // of the style word saying so: the composite then loads neither the command nor the style.
       const DevCmd& cmd = f.cmds[c];
       const uint32_t ctx = f.cmd_tile_x[c];
       const uint32_t meta = cmd.kind | (cmd.flags << 2) | (cmd.alpha << 4);
+      const bool solid = f.styles[cmd.style].fetch == kFetchSolid;
       uint4* rec = f.row_recs + 2u * (out + pos);
       rec[0] = make_uint4(c, f.cmd_xr[c], f.cmd_yr[c], meta);
-      rec[1] = make_uint4(f.cmdrow_base[c], (ctx & 0xFFFFu) | (((ctx >> 16) - (ctx & 0xFFFFu) + 1u) << 16), cmd.style,
-                          f.rs_base[c]);
+      rec[1] = make_uint4(f.cmdrow_base[c], (ctx & 0xFFFFu) | (((ctx >> 16) - (ctx & 0xFFFFu) + 1u) << 16),
+                          cmd.style | (solid ? kRecSolid : 0u), solid ? f.styles[cmd.style].solid : f.rs_base[c]);
     }
     out += total;
   }
@@ -1340,7 +1345,17 @@ __global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
         uint32_t m[4];
         strip_masks(f, ckind, ci, cmeta, cnseg, mw, xp, y, m);
 
-        if (row_ok && (m[0] | m[1] | m[2] | m[3])) {
+        if (row_ok && (m[0] | m[1] | m[2] | m[3]) && (cstyle & kRecSolid)) {
+          const bool src_copy = (cmeta >> 16) & 1u;
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            if (m[k] && xp + k < cv.w) {
+              pix[k] = px::composite(pix[k], crs, m[k], src_copy);
+              ops++;
+            }
+          }
+        }
+        else if (row_ok && (m[0] | m[1] | m[2] | m[3])) {
           const DevCmd& cmd = f.cmds[ci];
           const DevStyle& st = f.styles[cstyle];
           const bool src_copy = (cmeta >> 16) & 1u;

@@ -312,7 +312,9 @@ class StreamWriter:
     def to_bytes(self) -> bytes:
         fmt = 0 if self.format == FORMAT_PRGB32 else self.format     # PRGB32 streams keep their old bytes
         out = [struct.pack("<6I", MAGIC, VERSION, self.width, self.height, len(self.images), fmt)]
-        for img, ifmt in zip(self.images, self.image_formats):
+        # images assigned to .images directly (without add_image) are PRGB32
+        formats = self.image_formats + [FORMAT_PRGB32] * (len(self.images) - len(self.image_formats))
+        for img, ifmt in zip(self.images, formats):
             h, w = img.shape
             raw = img.astype("<u4").tobytes()
             out.append(struct.pack("<IHH", w, h, 0 if ifmt == FORMAT_PRGB32 else ifmt) + raw + b"\0" * ((-len(raw)) % 8))
