@@ -243,31 +243,85 @@ BLResult geometry_(GpuImpl* self, bool stroke, BLGeometryType type, const void* 
 // outlines are decoded by the font engine under the final transform in 24.8 space with the origin
 // mapped by it (add_filled_glyph_run_edges, rastercontextops_p.h:68-93), and the outlines are
 // filled non-zero on the device.
-BLResult fill_text_(GpuImpl* self, const BLPoint* origin, const BLFontCore* font, BLContextRenderTextOp op, const void* data) {
+// The glyph run of a text call: shaped from UTF-8/16/32 or Latin-1 text, or given
+// (fill_unclipped_text / stroke_unclipped_text, rastercontext.cpp:3082-3110, 3263-3290).
+BLResult glyph_run_of(GpuImpl* self, const BLFontCore* font, BLContextRenderTextOp op, const void* data,
+                      const BLGlyphRun*& run) {
   const BLFont& f = static_cast<const BLFont&>(*font);
   if (!f.is_valid()) return BL_ERROR_FONT_NOT_INITIALIZED;
-  const BLGlyphRun* run = nullptr;
   if (uint32_t(op) <= uint32_t(BL_TEXT_ENCODING_MAX_VALUE)) {
     const BLDataView* view = static_cast<const BLDataView*>(data);
     BL_PROPAGATE(self->glyphs.set_text(view->data, view->size, BLTextEncoding(op)));
     BL_PROPAGATE(f.shape(self->glyphs));
     run = &self->glyphs.glyph_run();
+    return BL_SUCCESS;
   }
-  else if (op == BL_CONTEXT_RENDER_TEXT_OP_GLYPH_RUN) {
+  if (op == BL_CONTEXT_RENDER_TEXT_OP_GLYPH_RUN) {
     run = static_cast<const BLGlyphRun*>(data);
+    return BL_SUCCESS;
   }
-  else {
-    return BL_ERROR_INVALID_VALUE;
-  }
-  if (run->is_empty()) return BL_SUCCESS;
-  BLMatrix2D ft = self->cur.st.final_transform;   // final_transform_fixed: post-scaled by 256
+  return BL_ERROR_INVALID_VALUE;
+}
+
+// final_transform_fixed (the final transform post-scaled by 256) and the origin mapped by it.
+void fixed_origin(const GpuImpl* self, const BLPoint* origin, BLMatrix2D& ft, BLPoint& of) {
+  ft = self->cur.st.final_transform;
   ft.m00 *= 256.0; ft.m01 *= 256.0; ft.m10 *= 256.0; ft.m11 *= 256.0; ft.m20 *= 256.0; ft.m21 *= 256.0;
-  const BLPoint of(origin->x * ft.m00 + origin->y * ft.m10 + ft.m20, origin->x * ft.m01 + origin->y * ft.m11 + ft.m21);
+  of.reset(origin->x * ft.m00 + origin->y * ft.m10 + ft.m20, origin->x * ft.m01 + origin->y * ft.m11 + ft.m21);
+}
+
+BLResult fill_text_(GpuImpl* self, const BLPoint* origin, const BLFontCore* font, BLContextRenderTextOp op, const void* data) {
+  const BLGlyphRun* run = nullptr;
+  BL_PROPAGATE(glyph_run_of(self, font, op, data, run));
+  if (run->is_empty()) return BL_SUCCESS;
+  BLMatrix2D ft;
+  BLPoint of;
+  fixed_origin(self, origin, ft, of);
   const BLMatrix2D t(ft.m00, ft.m01, ft.m10, ft.m11, of.x, of.y);
   self->outline.clear();
   BL_PROPAGATE(bl_font_get_glyph_run_outlines(font, run, &t, &self->outline, nullptr, nullptr));
   const BLPath& p = self->outline;
   return blgpu_context_fill_path_fixed_d(self->gpu, p.command_data(), reinterpret_cast<const double*>(p.vertex_data()), p.size());
+}
+
+// Stroked text (add_stroked_glyph_run_edges, rastercontextops_p.h:145-187): the glyph outlines are
+// stroked figure by figure into one non-zero fill, which is what the device stroker does with the
+// run's outline path.
+//   AFTER: the outlines decoded with the identity, stroked in user space, the strokes mapped by
+//   final_transform_fixed(origin): a stroke of the path at `origin`.
+//   BEFORE: the outlines decoded under the user transform's linear part (the font engine composes
+//   it with its own matrices, so they are decoded that way here too), stroked in meta space and
+//   mapped by meta_transform_fixed(origin). The meta transform is the identity here, so that is
+//   an AFTER stroke under an identity user transform, at the origin whose fixed-point image is
+//   the real one (division and multiplication by 256 are exact).
+BLResult stroke_text_(GpuImpl* self, const BLPoint* origin, const BLFontCore* font, BLContextRenderTextOp op, const void* data) {
+  const BLGlyphRun* run = nullptr;
+  BL_PROPAGATE(glyph_run_of(self, font, op, data, run));
+  if (run->is_empty()) return BL_SUCCESS;
+  const BLContextState& st = self->cur.st;
+  self->outline.clear();
+  if (st.stroke_options.transform_order == BL_STROKE_TRANSFORM_ORDER_AFTER) {
+    const BLMatrix2D id = BLMatrix2D::make_identity();
+    BL_PROPAGATE(bl_font_get_glyph_run_outlines(font, run, &id, &self->outline, nullptr, nullptr));
+    const BLPath& p = self->outline;
+    const double o[2] = {origin->x, origin->y};
+    return blgpu_context_stroke_path_at_d(self->gpu, o, p.command_data(), reinterpret_cast<const double*>(p.vertex_data()), p.size());
+  }
+  const BLMatrix2D& u = st.user_transform;
+  const BLMatrix2D ut(u.m00, u.m01, u.m10, u.m11, 0.0, 0.0);
+  BL_PROPAGATE(bl_font_get_glyph_run_outlines(font, run, &ut, &self->outline, nullptr, nullptr));
+  BLMatrix2D ft;
+  BLPoint of;
+  fixed_origin(self, origin, ft, of);
+  const double o[2] = {of.x / 256.0, of.y / 256.0};
+  const BLPath& p = self->outline;
+  BL_PROPAGATE(blgpu_context_save(self->gpu));
+  BLResult r = blgpu_context_reset_transform(self->gpu);
+  if (r == BL_SUCCESS) r = blgpu_context_set_stroke_transform_order(self->gpu, BL_STROKE_TRANSFORM_ORDER_AFTER);
+  if (r == BL_SUCCESS)
+    r = blgpu_context_stroke_path_at_d(self->gpu, o, p.command_data(), reinterpret_cast<const double*>(p.vertex_data()), p.size());
+  const BLResult r2 = blgpu_context_restore(self->gpu);
+  return r != BL_SUCCESS ? r : r2;
 }
 
 BLResult fill_mask_(GpuImpl* self, double x, double y, bool integral, const BLImageCore* mask, const BLRectI* area) {
@@ -594,12 +648,24 @@ BLResult BL_CDECL v_stroke_geometry_ext(BLContextImpl* impl, BLGeometryType t, c
 }
 
 // Stroked text is not supported.
-BLResult BL_CDECL v_stroke_text_op_i(BLContextImpl*, const BLPointI*, const BLFontCore*, BLContextRenderTextOp, const void*) noexcept { return kNotImplemented; }
-BLResult BL_CDECL v_stroke_text_op_i_rgba32(BLContextImpl*, const BLPointI*, const BLFontCore*, BLContextRenderTextOp, const void*, uint32_t) noexcept { return kNotImplemented; }
-BLResult BL_CDECL v_stroke_text_op_i_ext(BLContextImpl*, const BLPointI*, const BLFontCore*, BLContextRenderTextOp, const void*, const BLObjectCore*) noexcept { return kNotImplemented; }
-BLResult BL_CDECL v_stroke_text_op_d(BLContextImpl*, const BLPoint*, const BLFontCore*, BLContextRenderTextOp, const void*) noexcept { return kNotImplemented; }
-BLResult BL_CDECL v_stroke_text_op_d_rgba32(BLContextImpl*, const BLPoint*, const BLFontCore*, BLContextRenderTextOp, const void*, uint32_t) noexcept { return kNotImplemented; }
-BLResult BL_CDECL v_stroke_text_op_d_ext(BLContextImpl*, const BLPoint*, const BLFontCore*, BLContextRenderTextOp, const void*, const BLObjectCore*) noexcept { return kNotImplemented; }
+BLResult BL_CDECL v_stroke_text_op_d(BLContextImpl* impl, const BLPoint* o, const BLFontCore* f, BLContextRenderTextOp op, const void* d) noexcept {
+  SELF; return stroke_text_(self, o, f, op, d);
+}
+BLResult BL_CDECL v_stroke_text_op_d_rgba32(BLContextImpl* impl, const BLPoint* o, const BLFontCore* f, BLContextRenderTextOp op, const void* d, uint32_t c) noexcept {
+  SELF; return with_style_rgba32(self, 1, c, [&] { return stroke_text_(self, o, f, op, d); });
+}
+BLResult BL_CDECL v_stroke_text_op_d_ext(BLContextImpl* impl, const BLPoint* o, const BLFontCore* f, BLContextRenderTextOp op, const void* d, const BLObjectCore* s) noexcept {
+  SELF; return with_style_object(self, 1, s, [&] { return stroke_text_(self, o, f, op, d); });
+}
+BLResult BL_CDECL v_stroke_text_op_i(BLContextImpl* impl, const BLPointI* o, const BLFontCore* f, BLContextRenderTextOp op, const void* d) noexcept {
+  const BLPoint od(*o); return v_stroke_text_op_d(impl, &od, f, op, d);
+}
+BLResult BL_CDECL v_stroke_text_op_i_rgba32(BLContextImpl* impl, const BLPointI* o, const BLFontCore* f, BLContextRenderTextOp op, const void* d, uint32_t c) noexcept {
+  const BLPoint od(*o); return v_stroke_text_op_d_rgba32(impl, &od, f, op, d, c);
+}
+BLResult BL_CDECL v_stroke_text_op_i_ext(BLContextImpl* impl, const BLPointI* o, const BLFontCore* f, BLContextRenderTextOp op, const void* d, const BLObjectCore* s) noexcept {
+  const BLPoint od(*o); return v_stroke_text_op_d_ext(impl, &od, f, op, d, s);
+}
 
 #undef SELF
 

@@ -90,10 +90,7 @@ static int check_virt() {
   BLContextImpl* impl = reinterpret_cast<BLContextImpl*>(storage);
   const BLRectI ri(0, 0, 1, 1);
   const BLRect rd(0, 0, 1, 1);
-  const BLPoint pd(0, 0);
-  const BLPointI pi(0, 0);
   const BLRgba rgba(1, 1, 1, 1);
-  BLFontCore* font = nullptr;
   int bad = 0;
   auto expect = [&](BLResult got, BLResult want, const char* what) {
     if (got != want) { fprintf(stderr, "%s: got 0x%x want 0x%x\n", what, got, want); bad++; }
@@ -108,9 +105,6 @@ static int check_virt() {
   expect(v->restore_clipping(impl), BL_ERROR_NOT_IMPLEMENTED, "restore_clipping");
   expect(v->clear_recti(impl, &ri), BL_ERROR_NOT_IMPLEMENTED, "clear_recti");
   expect(v->clear_rectd(impl, &rd), BL_ERROR_NOT_IMPLEMENTED, "clear_rectd");
-  expect(v->stroke_text_op_i(impl, &pi, font, BL_CONTEXT_RENDER_TEXT_OP_UTF8, nullptr), BL_ERROR_NOT_IMPLEMENTED, "stroke_text_op_i");
-  expect(v->stroke_text_op_d(impl, &pd, font, BL_CONTEXT_RENDER_TEXT_OP_UTF8, nullptr), BL_ERROR_NOT_IMPLEMENTED, "stroke_text_op_d");
-  expect(v->stroke_text_op_d_rgba32(impl, &pd, font, BL_CONTEXT_RENDER_TEXT_OP_UTF8, nullptr, 0), BL_ERROR_NOT_IMPLEMENTED, "stroke_text_op_d_rgba32");
   expect(v->set_flatten_tolerance(impl, 0.5), BL_ERROR_NOT_IMPLEMENTED, "set_flatten_tolerance(0.5)");
   expect(v->set_flatten_tolerance(impl, bl_default_approximation_options.flatten_tolerance), BL_SUCCESS, "set_flatten_tolerance(default)");
   expect(v->set_flatten_mode(impl, BL_FLATTEN_MODE_RECURSIVE), BL_ERROR_NOT_IMPLEMENTED, "set_flatten_mode(recursive)");
@@ -273,6 +267,28 @@ static int check_scenes(const char* font_path) {
         if (i % 4 == 2) ctx.set_fill_style(random_gradient(r, 0, 0, 200));
         else ctx.set_fill_style(BLRgba32(r.u32() | 0x80000000u));
         ctx.fill_utf8_text(BLPoint(r.uniform(-10, 300), r.uniform(10, 150)), font, lines[i % 4]);
+        ctx.restore();
+      }
+    }});
+    // stroked text: both transform orders, joins and widths, under rotations and scales
+    scenes.push_back({"stroked_text", 420, 200, [&face](BLContext& ctx) {
+      Rng r(16);
+      ctx.fill_all(BLRgba32(0xFF202020u));
+      const char* lines[] = {"Stroked GB300", "quick brown fox", "AVAWA 0123", "fi fl ffi"};
+      for (int i = 0; i < 12; i++) {
+        BLFont font;
+        font.create_from_face(face, float(r.uniform(12, 48)));
+        ctx.save();
+        if (i % 3 == 1) ctx.rotate(r.uniform(-0.4, 0.4), 200, 100);
+        if (i % 4 == 3) ctx.scale(r.uniform(0.6, 1.6), r.uniform(0.6, 1.6));
+        ctx.set_stroke_transform_order(i % 2 ? BL_STROKE_TRANSFORM_ORDER_BEFORE : BL_STROKE_TRANSFORM_ORDER_AFTER);
+        ctx.set_stroke_width(r.uniform(0.5, 4.0));
+        ctx.set_stroke_join(BLStrokeJoin(r.u32() % 5));
+        if (i % 4 == 2) ctx.set_stroke_style(random_gradient(r, 0, 0, 200));
+        else ctx.set_stroke_style(BLRgba32(r.u32() | 0x80000000u));
+        const BLPoint at(r.uniform(-10, 300), r.uniform(10, 190));
+        if (i % 5 == 4) ctx.stroke_utf8_text(at, font, lines[i % 4], SIZE_MAX, BLRgba32(0xFFFFC000u));
+        else ctx.stroke_utf8_text(at, font, lines[i % 4]);
         ctx.restore();
       }
     }});
