@@ -1362,8 +1362,7 @@ BLGPU_API BLGpuResult blgpu_runtime_get_launch_config(const BLGpuRuntime* rt, BL
 
 BLGPU_API BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BLGpuLaunchConfig* c) {
   if (!rt || !c) return BLGPU_ERROR_INVALID_VALUE;
-  if ((c->cover_slots != 0 && c->cover_slots != 4 && c->cover_slots != 8 && c->cover_slots != 16 &&
-       c->cover_slots != 32 && c->cover_slots != 64) ||
+  if ((c->cover_slots != 0 && c->cover_slots != 16 && c->cover_slots != 32 && c->cover_slots != 64) ||
       (c->edge_block != 64 && c->edge_block != 128 && c->edge_block != 256) ||
       c->cover_blocks_per_sm < 0 || c->fine_blocks_per_sm < 0 || c->cubic_blocks_per_sm < 0 ||
       (c->no_occlusion_cull != 0 && c->no_occlusion_cull != 1) || c->max_segments < 0 ||

@@ -1088,93 +1088,6 @@ __global__ void __launch_bounds__(4 * K) coverage_kernel(FrameView f) {
   }
 }
 
-// The same pass with warp-private groups: each warp takes S consecutive slots with segments, zeroes
-// their cells, rasterizes their items 32 at a time (sorted by DDA path within the warp) and sweeps
-// them into masks, with no block-wide barrier: a warp whose segments are long does not hold up the
-// others. W warps per block share nothing but the block.
-template<int S, int W>
-__global__ void __launch_bounds__(32 * W) coverage_warp_kernel(FrameView f) {
-  __shared__ __align__(16) uint32_t cells[W][S][kSlotPixels];
-  __shared__ uint32_t bd[W][S][kStripRows];
-  __shared__ int2 org[W][S];
-  __shared__ uint32_t meta[W][S];
-  __shared__ uint2 items[W][32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (frame_skipped(f)) return;
-  const uint32_t num_masks = min(f.totals[5], f.mask_capacity);
-  if (blockIdx.x == 0 && threadIdx.x == 0 && f.totals[5] > f.mask_capacity) atomicOr(f.error_flags, kErrMasks);
-  const uint32_t groups = (num_masks + S - 1) / S;
-  const int prow = lane >> 3;
-
-  for (uint32_t grp = blockIdx.x * W + uint32_t(w); grp < groups; grp += gridDim.x * W) {
-    const uint32_t m0 = grp * S;
-    const int nk = int(min(uint32_t(S), num_masks - m0));
-    if (lane < nk) {
-      const uint4 info = f.mask_info[m0 + uint32_t(lane)];
-      org[w][lane] = make_int2(int(info.x), int(info.y));
-      meta[w][lane] = info.z;
-      const uint4 b4 = *reinterpret_cast<const uint4*>(f.backdrop + size_t(info.w) * kStripRows);
-      bd[w][lane][0] = b4.x; bd[w][lane][1] = b4.y; bd[w][lane][2] = b4.z; bd[w][lane][3] = b4.w;
-    }
-#pragma unroll
-    for (int i = lane; i < S * kSlotPixels / 4; i += 32)
-      reinterpret_cast<uint4*>(&cells[w][0][0])[i] = make_uint4(0u, 0u, 0u, 0u);
-    const uint32_t e0 = f.slot_first[f.mask_slot[m0]];
-    const uint32_t e1 = f.slot_first[f.mask_slot[m0 + uint32_t(nk) - 1u] + 1u];
-    __syncwarp();
-
-    for (uint32_t chunk = e0; chunk < e1; chunk += 32) {
-      const int n = int(min(32u, e1 - chunk));
-      uint2 it = make_uint2(0u, 0u);
-      uint32_t kind = 5u;
-      if (lane < n) {
-        it = f.entries[chunk + uint32_t(lane)];
-        kind = dda_kind(f.segs[it.x]);
-      }
-      // the lane's place among the chunk's items ordered by DDA path (a stable counting sort by
-      // ballots), so lanes that follow the same path sit side by side
-      uint32_t pos = 0, base = 0;
-#pragma unroll
-      for (uint32_t k = 0; k < 5u; k++) {
-        const uint32_t b = __ballot_sync(0xFFFFFFFFu, kind == k);
-        if (kind == k) pos = base + uint32_t(__popc(b & ((1u << lane) - 1u)));
-        base += uint32_t(__popc(b));
-      }
-      if (lane < n) items[w][pos] = it;
-      __syncwarp();
-      if (lane < n) {
-        const uint2 e = items[w][lane];
-        const int j = int(e.y - m0);
-        ras::WindowSink sink{cells[w][j], bd[w][j], org[w][j].x};
-        ras::segment_to_window(f.segs[e.x], f.seg_meta[e.x] & 1u, org[w][j].y, kStripRows, INT32_MAX, sink);
-      }
-      __syncwarp();
-    }
-
-    // sweep: lane covers row lane / 8, columns (lane % 8) * 4 .. + 3 of each slot
-    for (int j = 0; j < nk; j++) {
-      const uint32_t flags = meta[w][j] >> 16, alpha = meta[w][j] & 0xFFFFu;
-      const uint4 cv4 = *reinterpret_cast<const uint4*>(&cells[w][j][lane * 4]);
-      const uint32_t s4 = cv4.x + cv4.y + cv4.z + cv4.w;
-      uint32_t inc = s4;
-#pragma unroll
-      for (int o = 1; o < 8; o <<= 1) {
-        uint32_t v = __shfl_up_sync(0xFFFFFFFFu, inc, o, 8);
-        if ((lane & 7) >= o) inc += v;
-      }
-      uint32_t cov = (256u << 9) + bd[w][j][prow] + inc - s4;
-      const uint32_t rule = (flags & 2u) ? 0x1FFu : 0xFFFFFFFFu;
-      uint32_t m;
-      cov += cv4.x; m = px::calc_mask(cov, rule, alpha);
-      cov += cv4.y; m |= px::calc_mask(cov, rule, alpha) << 8;
-      cov += cv4.z; m |= px::calc_mask(cov, rule, alpha) << 16;
-      cov += cv4.w; m |= px::calc_mask(cov, rule, alpha) << 24;
-      reinterpret_cast<uint32_t*>(f.masks + size_t(m0 + uint32_t(j)) * kSlotPixels)[lane] = m;
-    }
-    __syncwarp();
-  }
-}
-
 // ---------------------------------------------------------------------------------------------
 // K3b - composite, persistent. The work unit is a strip of kStripRows x kTileW pixels (one warp,
 // 4 pixels per lane held in registers from one 128-bit load to one 128-bit store). Warps pull
@@ -1752,9 +1665,7 @@ int launch_coverage(const FrameView& f, const LaunchConfig& cfg, uint32_t* scan_
   // by frame: scenes of long edges (many strip rows per segment) have few work items per slot,
   // where smaller groups keep more of them in flight per SM
   const int slots = cfg.cover_slots ? cfg.cover_slots : (f.num_seglist > 16u * f.num_segs ? 32 : 64);
-  if (slots == 4) coverage_warp_kernel<4, 8><<<sms * per_sm, 256, 0, st>>>(f);
-  else if (slots == 8) coverage_warp_kernel<8, 8><<<sms * per_sm, 256, 0, st>>>(f);
-  else if (slots == 16) coverage_kernel<16><<<sms * per_sm, 64, 0, st>>>(f);
+  if (slots == 16) coverage_kernel<16><<<sms * per_sm, 64, 0, st>>>(f);
   else if (slots == 64) coverage_kernel<64><<<sms * per_sm, 256, 0, st>>>(f);
   else coverage_kernel<32><<<sms * per_sm, 128, 0, st>>>(f);
   return k + 1;

@@ -11,8 +11,7 @@ namespace blgpu {
 
 // Launch shapes the autotuner chooses between (0 = the default for that field).
 struct LaunchConfig {
-  int cover_slots = 0;            // slots with segments per coverage group: 16, 32 or 64 per block, 4 or 8
-                                  // per warp (warp-private groups); 0 = by frame
+  int cover_slots = 0;            // slots with segments per coverage block (16, 32 or 64; 0 = by frame)
   int cover_blocks_per_sm = 0;    // coverage grid: blocks per SM (0 = as many as fit)
   int fine_blocks_per_sm = 0;     // composite grid: blocks per SM (0 = as many as fit)
   int edge_block = 128;           // threads per block of the per-item edge builder (64/128/256)

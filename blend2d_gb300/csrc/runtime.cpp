@@ -1275,7 +1275,7 @@ BLGpuResult Runtime::autotune(int trials, LaunchConfig* best_out, double* best_m
   LaunchConfig best = cfg;
   double best_ms = 0.0;
   if (!r) r = measure(best, best_ms);
-  const int cover_slots[] = {0, 4, 8, 16, 32, 64};
+  const int cover_slots[] = {0, 16, 32, 64};
   const int blocks[] = {0, 1, 2, 3};
   const int edge_blocks[] = {64, 128, 256};
   const int list_rows[] = {32, 16, 8, 4};
@@ -1285,7 +1285,7 @@ BLGpuResult Runtime::autotune(int trials, LaunchConfig* best_out, double* best_m
   for (int fi = 0; fi < 6 && !r; fi++) {
     const int field = order[fi];
     const int* vals = field == 0 ? cover_slots : field == 3 ? edge_blocks : field == 5 ? list_rows : blocks;
-    const int nvals = field == 0 ? 6 : field == 3 ? 3 : 4;
+    const int nvals = field == 3 ? 3 : 4;
     for (int k = 0; k < nvals && !r; k++) {
       LaunchConfig c = best;
       int* slot = field == 0 ? &c.cover_slots : field == 1 ? &c.cover_blocks_per_sm : field == 2 ? &c.fine_blocks_per_sm

@@ -131,8 +131,7 @@ typedef struct BLGpuStats {
  * band geometry are fixed by the pipeline (32-pixel tile columns matching a warp's lanes, the
  * reference's band heights), so the tunable parameters are how work is grouped and gridded. */
 typedef struct BLGpuLaunchConfig {
-  int32_t cover_slots;          /* slots (command x 4-row strip x 32-px tile column) per coverage group: 16, 32 or 64
-                                   per block, 4 or 8 per warp (warp-private groups, no block barrier); 0 = chosen per frame */
+  int32_t cover_slots;          /* slots (command x 4-row strip x 32-px tile column) per coverage block: 16, 32 or 64; 0 = chosen per frame */
   int32_t cover_blocks_per_sm;  /* coverage pass grid */
   int32_t fine_blocks_per_sm;   /* composite pass grid */
   int32_t edge_block;           /* threads per block of the per-item edge builder: 64, 128 or 256 */
