@@ -288,6 +288,8 @@ struct FrameView {
                                //   from segments entirely left of it (cover << 9 per row)
   uint32_t* row_counts;        // [num_rows + 1]
   uint32_t* row_offsets;
+  uint2* row_box;              // per list entry: its command's pixel columns x0 | x1 << 16 and rows
+                               //   y0 | y1 << 16, what a strip tests before it reads the records
   uint4* row_recs;             // command lists per list row, painter's order: two records per entry,
                                //   {command, pixel columns x0 | x1 << 16, rows y0 | y1 << 16, meta}
                                //   {first slot, tile column tx0 | columns << 16, style, first row state}

@@ -960,6 +960,7 @@ __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
       const uint32_t meta = cmd.kind | (cmd.flags << 2) | (cmd.alpha << 4);
       const bool solid = f.styles[cmd.style].fetch == kFetchSolid;
       uint4* rec = f.row_recs + 2u * (out + pos);
+      f.row_box[out + pos] = make_uint2(f.cmd_xr[c], f.cmd_yr[c]);
       rec[0] = make_uint4(c, f.cmd_xr[c], f.cmd_yr[c], meta);
       rec[1] = make_uint4(f.cmdrow_base[c], (ctx & 0xFFFFu) | (((ctx >> 16) - (ctx & 0xFFFFu) + 1u) << 16),
                           cmd.style | (solid ? kRecSolid : 0u), solid ? f.styles[cmd.style].solid : f.rs_base[c]);
@@ -1190,13 +1191,16 @@ __global__ void __launch_bounds__(kFineThreads) cull_kernel(FrameView f) {
       uint4 ra = make_uint4(0u, 0u, 0u, 0u), rb = ra;
       bool cand = false;
       if (uint32_t(cb + lane) < list_count) {
-        const uint4* rec = f.row_recs + 2u * (list_first + uint32_t(cb + lane));
-        ra = rec[0];
-        rb = rec[1];
-        const uint32_t bx = ra.y, by = ra.z;
-        cand = (bx & 0xFFFFu) <= (strip_x & 0xFFFFu) && (bx >> 16) >= (strip_x >> 16) &&
-               (by & 0xFFFFu) <= (strip_y & 0xFFFFu) && (by >> 16) >= (strip_y >> 16) &&
-               ((ra.w >> 2) & 1u) && (ra.w >> 4) == 255u;
+        // the box first; the records only for commands that cover the whole strip
+        const uint2 bb = f.row_box[list_first + uint32_t(cb + lane)];
+        cand = (bb.x & 0xFFFFu) <= (strip_x & 0xFFFFu) && (bb.x >> 16) >= (strip_x >> 16) &&
+               (bb.y & 0xFFFFu) <= (strip_y & 0xFFFFu) && (bb.y >> 16) >= (strip_y >> 16);
+        if (cand) {
+          const uint4* rec = f.row_recs + 2u * (list_first + uint32_t(cb + lane));
+          ra = rec[0];
+          rb = rec[1];
+          cand = ((ra.w >> 2) & 1u) && (ra.w >> 4) == 255u;
+        }
       }
       uint32_t todo = __ballot_sync(0xFFFFFFFFu, cand);
       bool found = false;
@@ -1297,12 +1301,15 @@ __global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
       uint4 ra = make_uint4(0u, 0u, 0u, 0u), rb = ra;
       bool hit = false;
       if (base + lane < list_count && base + lane >= start) {
-        const uint4* rec = f.row_recs + 2u * (list_first + base + lane);
-        ra = rec[0];
-        rb = rec[1];
-        const uint32_t bx = ra.y, by = ra.z;
-        hit = (bx & 0xFFFFu) <= (strip_x >> 16) && (bx >> 16) >= (strip_x & 0xFFFFu) &&
-              (by & 0xFFFFu) <= (strip_y >> 16) && (by >> 16) >= (strip_y & 0xFFFFu);
+        // 8 bytes per entry to find the commands over the strip; their records only for those
+        const uint2 bb = f.row_box[list_first + base + lane];
+        hit = (bb.x & 0xFFFFu) <= (strip_x >> 16) && (bb.x >> 16) >= (strip_x & 0xFFFFu) &&
+              (bb.y & 0xFFFFu) <= (strip_y >> 16) && (bb.y >> 16) >= (strip_y & 0xFFFFu);
+        if (hit) {
+          const uint4* rec = f.row_recs + 2u * (list_first + base + lane);
+          ra = rec[0];
+          rb = rec[1];
+        }
       }
       const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, hit);
       if (!ballot) continue;

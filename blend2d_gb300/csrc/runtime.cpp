@@ -688,6 +688,7 @@ static void plan_dynamic(Layout& L, FrameView& v, const FrameTotals& t) {
   v.mask_slot = L.take<uint32_t>(size_t(slots) + 1);
   v.mask_info = L.take<uint4>(size_t(slots) + 1);
   v.masks = L.take<uint8_t>((size_t(slots) + 1) * kStripRows * kTileW);
+  v.row_box = L.take<uint2>(size_t(t.row_entries) + 1);
   v.row_recs = L.take<uint4>(2 * (size_t(t.row_entries) + 1));
   v.row_states = L.take<float4>(t.row_states + 1);
   v.mask_capacity = slots + 1;
