@@ -90,7 +90,7 @@ class LaunchConfig(ctypes.Structure):
                 ("fine_blocks_per_sm", ctypes.c_int32), ("edge_block", ctypes.c_int32),
                 ("cubic_blocks_per_sm", ctypes.c_int32), ("no_occlusion_cull", ctypes.c_int32),
                 ("max_segments", ctypes.c_int32), ("graph_frames", ctypes.c_int32),
-                ("list_rows", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
+                ("list_rows", ctypes.c_int32), ("device_order", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}

@@ -1351,6 +1351,7 @@ static void to_abi(const LaunchConfig& c, BLGpuLaunchConfig* out) {
   out->max_segments = c.max_segments;
   out->graph_frames = c.graph_frames;
   out->list_rows = c.list_rows;
+  out->device_order = c.device_order;
 }
 
 BLGPU_API BLGpuResult blgpu_runtime_get_launch_config(const BLGpuRuntime* rt, BLGpuLaunchConfig* out) {
@@ -1367,7 +1368,8 @@ BLGPU_API BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BL
       c->cover_blocks_per_sm < 0 || c->fine_blocks_per_sm < 0 || c->cubic_blocks_per_sm < 0 ||
       (c->no_occlusion_cull != 0 && c->no_occlusion_cull != 1) || c->max_segments < 0 ||
       (c->graph_frames != 0 && c->graph_frames != 1) ||
-      (c->list_rows != 0 && c->list_rows != 4 && c->list_rows != 8 && c->list_rows != 16 && c->list_rows != 32))
+      (c->list_rows != 0 && c->list_rows != 4 && c->list_rows != 8 && c->list_rows != 16 && c->list_rows != 32) ||
+      (c->device_order != 0 && c->device_order != 1))
     return BLGPU_ERROR_INVALID_VALUE;
   LaunchConfig lc;
   lc.cover_slots = c->cover_slots;
@@ -1379,6 +1381,7 @@ BLGPU_API BLGpuResult blgpu_runtime_set_launch_config(BLGpuRuntime* rt, const BL
   lc.max_segments = c->max_segments;
   lc.graph_frames = c->graph_frames;
   lc.list_rows = c->list_rows ? c->list_rows : 32;
+  lc.device_order = c->device_order;
   std::lock_guard<std::mutex> e(rt->exec);
   rt->rt.cfg = lc;
   rt->rt.graph_valid = false;

@@ -20,6 +20,7 @@ struct LaunchConfig {
   int max_segments = 0;           // > 0: cap of the segment array (frames needing more fail)
   int graph_frames = 0;           // 1: frames run as a captured graph over capacity-sized arrays
   int list_rows = 32;             // pixel rows per command list (4, 8, 16 or 32)
+  int device_order = 0;           // 1: pipelines of runtimes that set it run one after another on the device
 };
 
 // log2 of the list-row height a launch config selects.

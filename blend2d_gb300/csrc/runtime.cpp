@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <mutex>
 #include <thread>
 
 #include "launch.h"
@@ -38,6 +39,20 @@ BLGpuResult cuda_result(cudaError_t e) {
 int last_cuda_error() { return g_last_cuda_error.load(); }
 
 static inline size_t align_up(size_t x, size_t a) { return (x + a - 1) & ~(a - 1); }
+
+// Device order (LaunchConfig::device_order): the graph-frame pipelines of the runtimes on a device
+// that set it are chained: each waits, on its stream, for the kernels of the one enqueued before it.
+// Copies stay outside the chain.
+namespace {
+struct DeviceOrder {
+  std::mutex m;
+  cudaEvent_t last = nullptr;         // recorded after the last ordered pipeline's kernels
+};
+DeviceOrder& device_order_of(int device) {
+  static DeviceOrder orders[64];
+  return orders[unsigned(device) % 64u];
+}
+}  // namespace
 
 // Bytes per pixel of a canvas: an A8 target stays one byte per pixel on the device as well.
 static inline int32_t canvas_bpp(const BLGpuImage& im) { return im.format == BLGPU_FORMAT_A8 ? 1 : 4; }
@@ -283,6 +298,7 @@ BLGpuResult Runtime::init(const BLGpuRuntimeCreateInfo* info) {
   BLGPU_CHECK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
   BLGPU_CHECK(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
   BLGPU_CHECK(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
+  BLGPU_CHECK(cudaEventCreateWithFlags(&order_ev, cudaEventDisableTiming));
   BLGPU_CHECK(cudaMallocHost(reinterpret_cast<void**>(&host_totals), 128));
   BLGPU_CHECK(cudaMallocHost(reinterpret_cast<void**>(&host_counts), sizeof(uint32_t) * kCntWords));
   BLGPU_CHECK(cudaMalloc(reinterpret_cast<void**>(&counts_dev), sizeof(uint32_t) * kCntWords));
@@ -299,6 +315,13 @@ void Runtime::destroy() {
   if (fork_ev) cudaEventDestroy(fork_ev);
   if (join_ev) cudaEventDestroy(join_ev);
   side = nullptr; fork_ev = join_ev = nullptr;
+  if (order_ev) {
+    DeviceOrder& d = device_order_of(device);
+    std::lock_guard<std::mutex> g(d.m);
+    if (d.last == order_ev) d.last = nullptr;
+    cudaEventDestroy(order_ev);
+    order_ev = nullptr;
+  }
   in_buf.release();
   dyn_buf.release();
   seg_buf.release();
@@ -888,12 +911,29 @@ BLGpuResult Runtime::run_graph(const Frame& fr) {
     graph_valid = true;
     stats.kernel_launches = uint64_t(launches);
   }
-  BLGPU_CHECK(cudaEventRecord(ev[0], stream));
-  BLGPU_CHECK(cudaGraphLaunch(graph, stream));
-  BLGPU_CHECK(cudaEventRecord(ev[3], stream));
+  {
+    std::unique_lock<std::mutex> order;
+    if (cfg.device_order) {
+      DeviceOrder& d = device_order_of(device);
+      order = std::unique_lock<std::mutex>(d.m);
+      if (d.last && d.last != order_ev) BLGPU_CHECK(cudaStreamWaitEvent(stream, d.last, 0));
+    }
+    BLGPU_CHECK(cudaEventRecord(ev[0], stream));
+    BLGPU_CHECK(cudaGraphLaunch(graph, stream));
+    BLGPU_CHECK(cudaEventRecord(ev[3], stream));
+    if (order) {
+      BLGPU_CHECK(cudaEventRecord(order_ev, stream));
+      device_order_of(device).last = order_ev;
+    }
+  }
   BLGPU_CHECK(cudaMemcpyAsync(host_totals, view.totals, 32, cudaMemcpyDeviceToHost, stream));
   BLGPU_CHECK(cudaMemcpyAsync(host_totals + 20, view.error_flags, 32, cudaMemcpyDeviceToHost, stream));
   d2h_bytes += 64;
+  // The canvases go back in the same round trip. When the frame turns out not to fit, its render
+  // half did not run: each canvas that was uploaded comes back unchanged, and the others are
+  // overwritten whole by their first command when the frame runs again below.
+  r = download();
+  if (r) return r;
   BLGPU_CHECK(cudaStreamSynchronize(stream));
   FrameTotals t;
   t.segs = host_totals[0]; t.seglist = host_totals[1]; t.cmdrows = host_totals[2];
@@ -904,9 +944,6 @@ BLGpuResult Runtime::run_graph(const Frame& fr) {
     graph_valid = false;
     return run_eager(fr);
   }
-  r = download();
-  if (r) return r;
-  BLGPU_CHECK(cudaStreamSynchronize(stream));
   has_frame = true;
   graph_frames_run++;
   read_pixel_ops();

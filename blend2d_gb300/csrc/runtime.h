@@ -193,6 +193,7 @@ struct Runtime {
   // composite pass, so they overlap the FP64-bound edge building.
   cudaStream_t side = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  cudaEvent_t order_ev = nullptr;      // end of this runtime's last ordered pipeline (LaunchConfig::device_order)
   cudaGraphExec_t graph = nullptr;
   bool graph_valid = false;
 

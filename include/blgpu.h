@@ -150,7 +150,12 @@ typedef struct BLGpuLaunchConfig {
   int32_t list_rows;            /* pixel rows per command list of the composite (4, 8, 16 or 32; 0 =
                                    32): shorter lists hold fewer commands a strip must test, at the
                                    cost of more list entries */
-  int32_t reserved[1];
+  int32_t device_order;         /* 1: this runtime's frame pipelines and those of the other runtimes on
+                                   the device that set it run their kernels one frame after another, in
+                                   the order their frames were submitted (their copies are not ordered,
+                                   so one frame's transfers overlap another's kernels). For runtimes
+                                   taking turns on large frames, whose kernels each fill the device and
+                                   only slow each other down when run at once. */
 } BLGpuLaunchConfig;
 
 /* --- runtime (device, stream, memory) --------------------------------------------------- */
