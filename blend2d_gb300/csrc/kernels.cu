@@ -907,7 +907,17 @@ __global__ void __launch_bounds__(256) canvas_copy_kernel(const DevXfer* xfers, 
     }
     const uint32_t* src = to_host ? t.dev + int64_t(y) * t.dev_stride : t.host + int64_t(y) * t.host_stride;
     uint32_t* dst = to_host ? t.host + int64_t(y) * t.host_stride : t.dev + int64_t(y) * t.dev_stride;
-    for (int x = lane; x < t.w; x += 32) dst[x] = src[x];
+    // 16-byte accesses when both rows start at 16-byte boundaries: a quarter of the instructions
+    // and of the link transactions, so the copy takes less from the kernels it runs beside
+    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0) {
+      const int w4 = t.w >> 2;
+      for (int x = lane; x < w4; x += 32)
+        reinterpret_cast<uint4*>(dst)[x] = reinterpret_cast<const uint4*>(src)[x];
+      for (int x = (w4 << 2) + lane; x < t.w; x += 32) dst[x] = src[x];
+    }
+    else {
+      for (int x = lane; x < t.w; x += 32) dst[x] = src[x];
+    }
   }
 }
 

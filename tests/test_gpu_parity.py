@@ -859,3 +859,41 @@ def test_target_format_context_calls(runtimes):
     prgb_stream = scenes.random_mix(1250, width=40, height=30, count=10).to_bytes()
     with pytest.raises(bg.BLGpuError):
         bg.render_stream(rt, prgb_stream, np.zeros((30, 40), dtype=np.uint8))
+
+
+def test_device_ordered_runtimes_take_turns():
+    """Two runtimes with graph frames and device_order, taking steps in turn from two threads (their
+    kernels chained on the device, their copies not): every step's canvases equal the oracle's."""
+    import threading
+    torch = pytest.importorskip("torch")
+    batches = [[scenes.random_mix(1400 + 10 * k + i, width=60 + 23 * i, height=40 + 17 * i, count=90).to_bytes()
+                for i in range(5)] for k in range(6)]
+    want = [[oracle_lib.render(s) for s in b] for b in batches]
+    cfg = bg.LaunchConfig(graph_frames=1, device_order=1, edge_block=128)
+    rts = [bg.Runtime(0), bg.Runtime(0)]
+    errors, got = [], {}
+    try:
+        for r in rts:
+            r.set_launch_config(cfg)
+            assert r.launch_config().device_order == 1
+
+        def worker(k):
+            try:
+                for step in range(k, len(batches), 2):
+                    tg = [torch.zeros(oracle_lib.stream_size(s)[::-1], dtype=torch.int32).pin_memory() for s in batches[step]]
+                    rts[k].render_batch(batches[step], tg)
+                    got[step] = [t.numpy().view(np.uint32).copy() for t in tg]
+            except Exception as e:          # re-raised below
+                errors.append(e)
+        ths = [threading.Thread(target=worker, args=(k,)) for k in range(2)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+    finally:
+        for r in rts:
+            r.close()
+    assert not errors, errors
+    for step in range(len(batches)):
+        for i, (g, w) in enumerate(zip(got[step], want[step])):
+            assert not _diff(g, w), f"step {step} canvas {i}: {_diff(g, w)}"
