@@ -626,7 +626,10 @@ def frame_record(args, dist, local, workload: str, cpu: bool) -> dict:
 
     # e2e: two recording threads, each with its own context and pinned canvas, take the steps in
     # turn and flush asynchronously, so a step is recorded while the one before renders; every
-    # step's upload, render and read-back is inside the timed region
+    # step's upload, render and read-back is inside the timed region. Graph frames: each step's
+    # frame is uploaded in place and runs as one captured graph, with no host round trip inside it.
+    cfg0 = rt.launch_config()
+    rt.set_launch_config(bg.LaunchConfig(**{**cfg0.as_dict(), "graph_frames": 1}))
     threads_n = 2
     hosts = [pinned_canvas(h, w) for _ in range(threads_n)]
     ctxs = [bg.Context(rt) for _ in range(threads_n)]
@@ -672,6 +675,11 @@ def frame_record(args, dist, local, workload: str, cpu: bool) -> dict:
     got = hosts[0].numpy().view(np.uint32).copy()
     for c in ctxs:
         c.close()
+    rt.set_launch_config(cfg0)
+    ctx = bg.Context(rt, hosts[0])       # the eager frame the replays below time
+    ctx.submit_stream(stream)
+    ctx.end()
+    ctx.close()
 
     step_ms, fine_ms, comp_ms, launches, clocks = time_replays(rt, s, args.steps, args.warmup, flush_buf)
     dist.barrier()
