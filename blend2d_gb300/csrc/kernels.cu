@@ -466,35 +466,10 @@ constexpr int kPieceRefillLanes = 16;
 // piece is cheap and the lanes' subdivision steps stay together. A piece is built by its own
 // builder: the border runs a curve accumulates are vertical lines at the clip box's x0/x1 whose
 // cells add up the same whether the runs of consecutive pieces are merged or not.
-constexpr int kPieceDepths = 8;
-constexpr uint32_t kPieceBinWord = 32;     // work_counter words of the depth bins (DEG 3; DEG 2 + 16)
-
-// Estimated subdivision depth of a monotonic piece, 0..kPieceDepths-1: the flattener splits while
-// a control point's squared distance from the chord is above the tolerance (Mono::is_flat), and a
-// split divides that distance by about 4, so the depth is about log16 of the ratio. Only the
-// order the pieces are flattened in depends on it.
-template<int DEG>
-__device__ __forceinline__ uint32_t piece_depth(const eb::Pt* p, double tol_sq) {
-  const float vx = float(p[DEG].x - p[0].x), vy = float(p[DEG].y - p[0].y);
-  float dev = 0.f;
-#pragma unroll
-  for (int i = 1; i < DEG; i++) {
-    const float c = vx * float(p[i].y - p[0].y) - vy * float(p[i].x - p[0].x);
-    dev = fmaxf(dev, c * c);
-  }
-  const float r = dev / (float(tol_sq) * (vx * vx + vy * vy) + 1e-30f);
-  if (!(r > 1.f)) return 0u;
-  if (!(r < 1e30f)) return uint32_t(kPieceDepths - 1);
-  return min(uint32_t(ilogbf(r) + 4) >> 2, uint32_t(kPieceDepths - 1));
-}
-
 template<int DEG>
 __global__ void __launch_bounds__(128) curve_split_kernel(FrameView f) {
-  __shared__ uint32_t depth_hist[kPieceDepths];
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
-  if (threadIdx.x < kPieceDepths) depth_hist[threadIdx.x] = 0u;
-  __syncthreads();
   const uint32_t n_cubic = min(f.work_counter[2], f.item_capacity);
   const uint32_t n_items = DEG == 3 ? n_cubic : min(f.work_counter[21], f.item_capacity - n_cubic);
   uint32_t rows = 0, npieces = 0, cmd_i = 0;
@@ -555,50 +530,10 @@ __global__ void __launch_bounds__(128) curve_split_kernel(FrameView f) {
     for (int i = 0; i <= DEG; i++) pc.p[i] = make_double2(spline[k * DEG + i].x, spline[k * DEG + i].y);
     pc.cmd = cmd_i;
     pc.any = any;
-    pc.pad[0] = piece_depth<DEG>(spline + k * DEG, 0.20 * 256.0 * (0.20 * 256.0));
-    pc.pad[1] = 0u;
-    atomicAdd(&depth_hist[pc.pad[0]], 1u);
     f.pieces[DEG == 3 ? idx : f.piece_capacity - 1u - idx] = pc;
   }
-  __syncthreads();
-  if (threadIdx.x < kPieceDepths && depth_hist[threadIdx.x])
-    atomicAdd(f.work_counter + kPieceBinWord + (DEG == 3 ? 0u : 16u) + threadIdx.x, depth_hist[threadIdx.x]);
   rows = __reduce_add_sync(0xFFFFFFFFu, rows);
   if (lane == 0 && rows) atomicAdd(f.totals + 1, rows);
-}
-
-// The pieces in flattening order: by estimated depth, deepest first, so a warp's lanes take pieces
-// of about the same length and finish them together (refills then serve many lanes at once). The
-// order within a depth follows the atomics; the pixels do not depend on the order.
-template<int DEG>
-__global__ void __launch_bounds__(256) piece_order_kernel(FrameView f) {
-  __shared__ uint32_t base[kPieceDepths];
-  const uint32_t* cnt = f.work_counter + kPieceBinWord + (DEG == 3 ? 0u : 16u);
-  uint32_t* cursor = f.work_counter + kPieceBinWord + (DEG == 3 ? 0u : 16u) + kPieceDepths;
-  if (threadIdx.x == 0) {
-    uint32_t acc = 0;
-    for (int d = kPieceDepths - 1; d >= 0; d--) { base[d] = acc; acc += cnt[d]; }
-  }
-  __syncthreads();
-  const uint32_t n_cubic = min(f.work_counter[23], f.piece_capacity);
-  const uint32_t n = DEG == 3 ? n_cubic : min(f.work_counter[25], f.piece_capacity - n_cubic);
-  const int lane = threadIdx.x & 31;
-  for (uint32_t t0 = blockIdx.x * blockDim.x; t0 < n; t0 += gridDim.x * blockDim.x) {   // uniform per block
-    const uint32_t t = t0 + threadIdx.x;
-    const bool on = t < n;
-    const uint32_t idx = DEG == 3 ? t : f.piece_capacity - 1u - t;
-    const uint32_t d = on ? min(f.pieces[idx].pad[0], uint32_t(kPieceDepths - 1)) : uint32_t(kPieceDepths);
-    // one atomic per depth present in the warp
-    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
-    const int leader = __ffs(peers) - 1;
-    uint32_t pos = 0;
-    if (on && lane == leader) pos = atomicAdd(cursor + d, uint32_t(__popc(peers)));
-    pos = __shfl_sync(0xFFFFFFFFu, pos, leader) + uint32_t(__popc(peers & ((1u << lane) - 1u)));
-    if (on) {
-      const uint32_t p = min(base[d] + pos, n - 1u);
-      f.piece_order[DEG == 3 ? p : f.piece_capacity - 1u - p] = idx;
-    }
-  }
 }
 
 template<int DEG>
@@ -627,7 +562,7 @@ __global__ void __launch_bounds__(kCurveThreads) edge_pieces_kernel(FrameView f)
           exhausted = true;
         }
         else {
-          const DevPiece pc = f.pieces[f.piece_order[DEG == 3 ? t : f.piece_capacity - 1u - t]];
+          const DevPiece pc = f.pieces[DEG == 3 ? t : f.piece_capacity - 1u - t];
           cur = pc.cmd;
           init_builder(b, f.canvases[f.cmds[cur].canvas]);
           b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, cur);
@@ -1701,13 +1636,11 @@ int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   const uint32_t split_grid = cdiv(f.item_capacity ? f.item_capacity : 1, 128);
   curve_split_kernel<3><<<split_grid, 128, 0, st>>>(f);
   curve_split_kernel<2><<<split_grid, 128, 0, st>>>(f);
-  piece_order_kernel<3><<<uint32_t(sms * 4), 256, 0, st>>>(f);
-  piece_order_kernel<2><<<uint32_t(sms * 4), 256, 0, st>>>(f);
   const uint32_t pgrid = cdiv(f.piece_capacity ? f.piece_capacity : 1, kCurveThreads);
   const uint32_t pieces_grid = pgrid < cubic_grid ? pgrid : cubic_grid;
   edge_pieces_kernel<3><<<pieces_grid, kCurveThreads, 0, st>>>(f);
   edge_pieces_kernel<2><<<pieces_grid, kCurveThreads, 0, st>>>(f);
-  return 8;
+  return 6;
 }
 
 int launch_cmd_tiles(const FrameView& f, uint32_t* cmdrow_counts_per_cmd, cudaStream_t st) {

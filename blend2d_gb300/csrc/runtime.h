@@ -158,7 +158,7 @@ struct FrameSizes {
   }
 };
 
-constexpr int kCounterWords = 64;
+constexpr int kCounterWords = 48;
 
 struct DeviceBuffer {
   void* ptr = nullptr;
