@@ -727,7 +727,10 @@ BLGpuResult Runtime::stage_canvases(const Frame& fr) {
   const uint32_t ncv = uint32_t(fr.canvases.size());
   xfers.clear();
   canvas_xfer.assign(ncv, -1);
-  for (uint32_t i = 0; i < ncv; i++) {
+  // Page-locked canvases move by a copy kernel, which beats one DMA copy per canvas when the frame
+  // has the device to itself. Under device order another runtime's kernels are running, and the
+  // copy engines then move them without taking any SM time from those kernels.
+  for (uint32_t i = 0; i < ncv && !cfg.device_order; i++) {
     const BLGpuImage& im = fr.targets[i].image;
     if (device_target_direct(im) || im.width == 0 || im.height == 0 || (im.flags & BLGPU_IMAGE_DEVICE_MEMORY) ||
         (im.stride % canvas_bpp(im)) != 0)

@@ -155,7 +155,9 @@ typedef struct BLGpuLaunchConfig {
                                    the order their frames were submitted (their copies are not ordered,
                                    so one frame's transfers overlap another's kernels). For runtimes
                                    taking turns on large frames, whose kernels each fill the device and
-                                   only slow each other down when run at once. */
+                                   only slow each other down when run at once. Such a runtime moves
+                                   page-locked canvases by DMA rather than by a copy kernel, so its
+                                   copies take no SM time from the other runtimes' kernels. */
 } BLGpuLaunchConfig;
 
 /* --- runtime (device, stream, memory) --------------------------------------------------- */
