@@ -66,6 +66,7 @@ BATCH_LABEL = "batch_{n}_canvases_32-2048px_10-5000_paths"
 SERVE_SEED = 5
 FALLBACK_HBM_GBS = 6800.0
 L2_FLUSH_BYTES = 256 << 20
+E2E_RUNTIMES = 3          # runtimes taking the batched e2e steps in turn (device-ordered)
 DTYPE = "u8x4 (PRGB32); fp64 edges"
 
 
@@ -462,12 +463,12 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
 
     # ---- e2e through the public API: host streams, pinned host canvases, one pipeline per step.
     # One eager step first (every array sized from the frame, a host read-back between the
-    # halves), for reference. Then two runtimes (each its own stream, arenas and pinned canvases)
-    # take the steps in turn from two host threads with graph frames (a step's data is uploaded in
-    # place and one captured graph replayed), so a step's host recording overlaps the device work
-    # of the step before. Their kernels run one frame after another (device_order): two frames'
-    # kernels at once only slow each other down, while one frame's copies overlap the other's
-    # kernels. Every step's upload, render and read-back is inside the timed region.
+    # halves), for reference. Then three runtimes (each its own stream, arenas and pinned canvases)
+    # take the steps in turn from three host threads with graph frames (a step's data is uploaded
+    # in place and one captured graph replayed), so a step's host recording and copies overlap the
+    # device work of the steps before. Their kernels run one frame after another (device_order):
+    # two frames' kernels at once only slow each other down. Every step's upload, render and
+    # read-back is inside the timed region.
     import threading
     rt.render_batch(streams, targets)
     # launch shapes and the command-list row height chosen by the autotuner on this batch
@@ -478,9 +479,8 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
     eager_step_s = time.perf_counter() - t0
     cfg0 = rt.launch_config()
     graph_cfg = bg.LaunchConfig(**{**cfg0.as_dict(), "graph_frames": 1, "device_order": 1})
-    rt2 = bg.Runtime(local)
-    rts = [rt, rt2]
-    tgts = [targets, [pinned_canvas(h, w) for h, w in shapes]]
+    rts = [rt] + [bg.Runtime(local) for _ in range(E2E_RUNTIMES - 1)]
+    tgts = [targets] + [[pinned_canvas(h, w) for h, w in shapes] for _ in range(E2E_RUNTIMES - 1)]
     for r_ in rts:
         r_.set_launch_config(graph_cfg)
 
@@ -489,11 +489,11 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
 
         def worker(k):
             try:
-                for _ in range(k, count, 2):
+                for _ in range(k, count, E2E_RUNTIMES):
                     rts[k].render_batch(streams, tgts[k])
             except Exception as e:      # re-raised on the main thread
                 errors.append(e)
-        ths = [threading.Thread(target=worker, args=(k,)) for k in range(2)]
+        ths = [threading.Thread(target=worker, args=(k,)) for k in range(E2E_RUNTIMES)]
         for t in ths:
             t.start()
         for t in ths:
@@ -518,9 +518,13 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
     st = rt.stats()
     h2d, d2h = int(st.h2d_bytes), int(st.d2h_bytes)
     batch_dev_ms = float(st.last_gpu_ms)
-    mismatched2 = [i for i, (a, b) in enumerate(zip(tgts[0], tgts[1])) if not np.array_equal(a.numpy(), b.numpy())]
-    rt2.close()
-    del tgts[1][:]
+    # every runtime's canvases equal the first one's
+    mismatched2 = sorted({i for t in tgts[1:] for i, (a, b) in enumerate(zip(tgts[0], t))
+                          if not np.array_equal(a.numpy(), b.numpy())})
+    for r_ in rts[1:]:
+        r_.close()
+    for t in tgts[1:]:
+        del t[:]
     rt.set_launch_config(cfg0)
     rt.render_batch(streams, targets)       # the eager frame the replays below time
 
@@ -575,7 +579,7 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
         "e2e": {"value": round(world * args.steps * mpix / e2e_s, 3), "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_s * 1e3 / args.steps, 3), "clocks": e2e_clocks,
                 "graph_frames": graph_steps, "eager_ms_per_step": round(eager_step_s * 1e3, 3),
-                "pipelining": "two runtimes take the steps in turn from two host threads; their kernels run one frame after another (device_order), their copies overlap",
+                "pipelining": f"{E2E_RUNTIMES} runtimes take the steps in turn from {E2E_RUNTIMES} host threads; their kernels run one frame after another (device_order), their copies (DMA) overlap",
                 "host_split_of_a_step": host_split},
         "gpu_launches": launches,
         "clocks": dev_clocks,
