@@ -663,7 +663,7 @@ def frame_record(args, dist, local, workload: str, cpu: bool) -> dict:
         if errors:
             raise errors[0]
 
-    e2e_run(args.warmup)
+    e2e_run(max(args.warmup, 8))        # every context's two recording buffers warmed up
     dist.barrier()
     t0 = time.perf_counter()
     e2e_run(args.steps)
