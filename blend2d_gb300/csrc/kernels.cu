@@ -1008,10 +1008,7 @@ template<int K>
 __global__ void __launch_bounds__(4 * K) coverage_kernel(FrameView f) {
   constexpr int kCoverThreads = 4 * K;
   constexpr int kCoverChunk = 4 * kCoverThreads;
-  // slots 4 words apart in the banks: lanes rasterizing the same cell of different slots collide
-  // less (a slot's 128 cells would otherwise put every slot's cell i in the same bank)
-  constexpr int kCellStride = kSlotPixels + 4;
-  __shared__ __align__(16) uint32_t cells[K][kCellStride];
+  __shared__ __align__(16) uint32_t cells[K][kSlotPixels];
   __shared__ uint32_t bd[K][kStripRows];
   __shared__ int2 org[K];                  // x of the slot's first column, its first row
   __shared__ uint32_t meta[K];             // command flags << 16 | alpha
@@ -1034,7 +1031,7 @@ __global__ void __launch_bounds__(4 * K) coverage_kernel(FrameView f) {
       const uint4 b4 = *reinterpret_cast<const uint4*>(f.backdrop + size_t(slot) * kStripRows);
       bd[tid][0] = b4.x; bd[tid][1] = b4.y; bd[tid][2] = b4.z; bd[tid][3] = b4.w;
     }
-    for (int i = tid; i < K * kCellStride / 4; i += kCoverThreads)
+    for (int i = tid; i < K * kSlotPixels / 4; i += kCoverThreads)
       reinterpret_cast<uint4*>(&cells[0][0])[i] = make_uint4(0u, 0u, 0u, 0u);
     const uint32_t e0 = f.slot_first[f.mask_slot[m0]];
     const uint32_t e1 = f.slot_first[f.mask_slot[m0 + uint32_t(nk) - 1u] + 1u];
