@@ -1362,16 +1362,7 @@ __global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
         uint32_t m[4];
         strip_masks(f, ckind, ci, cmeta, cnseg, mw, xp, y, m);
 
-        // a command that covers every pixel of the strip (a warp-wide test, so the warp takes one
-        // path) composites without scaling its source by the mask
-        const bool covered = __all_sync(0xFFFFFFFFu, full && (m[0] & m[1] & m[2] & m[3]) == 255u);
-        if (covered && (cstyle & kRecSolid)) {
-          const bool src_copy = (cmeta >> 16) & 1u;
-#pragma unroll
-          for (int k = 0; k < 4; k++) pix[k] = px::composite_full(pix[k], crs, src_copy);
-          ops += 4;
-        }
-        else if (row_ok && (m[0] | m[1] | m[2] | m[3]) && (cstyle & kRecSolid)) {
+        if (row_ok && (m[0] | m[1] | m[2] | m[3]) && (cstyle & kRecSolid)) {
           const bool src_copy = (cmeta >> 16) & 1u;
 #pragma unroll
           for (int k = 0; k < 4; k++) {
@@ -1419,18 +1410,11 @@ __global__ void __launch_bounds__(kFineThreads, 5) fine_kernel(FrameView f) {
 #pragma unroll
               for (int k = 0; k < 4; k++) sv[k] = px::dither_pixel(e[k], px::dither_threshold(xp + k, y));
             }
-            if (covered) {
 #pragma unroll
-              for (int k = 0; k < 4; k++) pix[k] = px::composite_full(pix[k], sv[k], src_copy);
-              n = 4;
-            }
-            else {
-#pragma unroll
-              for (int k = 0; k < 4; k++) {
-                if (m[k] && xp + k < cv.w) {
-                  pix[k] = px::composite(pix[k], sv[k], m[k], src_copy);
-                  n++;
-                }
+            for (int k = 0; k < 4; k++) {
+              if (m[k] && xp + k < cv.w) {
+                pix[k] = px::composite(pix[k], sv[k], m[k], src_copy);
+                n++;
               }
             }
           }

@@ -48,15 +48,6 @@ __device__ __forceinline__ uint32_t composite(uint32_t d, uint32_t s, uint32_t m
   return sm + (div255_2x16((d & kM) * ia) | (div255_2x16(((d >> 8) & kM) * ia) << 8));
 }
 
-// composite() with m = 255: div255(s * 255) is s for every channel value, so the source needs no
-// scaling (SrcOver is then the reference's unmasked op_prgb32_prgb32, SrcCopy the source).
-__device__ __forceinline__ uint32_t composite_full(uint32_t d, uint32_t s, bool src_copy) {
-  if (src_copy) return s;
-  const uint32_t kM = 0x00FF00FFu;
-  const uint32_t ia = (s >> 24) ^ 0xFFu;
-  return s + (div255_2x16((d & kM) * ia) | (div255_2x16(((d >> 8) & kM) * ia) << 8));
-}
-
 // x86 cvttss2si / cvtss2si semantics (INT_MIN for NaN and out-of-range values).
 __device__ __forceinline__ int trunc_f(float v) {
   if (!(v >= -2147483648.0f && v < 2147483648.0f)) return INT32_MIN;
