@@ -457,7 +457,10 @@ __device__ __forceinline__ void finish_curve(FrameView& f, eb::Builder& b, uint3
 // the batched workload (piece kernel 10.8 -> 14.2 ms): the shared-memory carve-out shrinks the L1
 // that the stacks' and the segment sinks' local memory hits in.
 constexpr int kCurveThreads = 128;
-constexpr int kPieceRefillLanes = 16;
+// Idle lanes a warp waits for before it takes new pieces: each refill's set-up costs the warp its
+// FP64 instructions whatever the number of lanes refilled. On the batched workload 24 and 28
+// measured 246-248 ms per step, 16 and 20 250 ms, 32 251 ms, 8 257 ms and 4 259 ms.
+constexpr int kPieceRefillLanes = 24;
 
 // Curves in two kernels. curve_split_kernel<DEG>: one thread per curve of the curve list does
 // curve_to's set-up (transform, clip flags, a curve entirely on one side of the clip box, the split
