@@ -999,17 +999,11 @@ constexpr int kStripsPerTile = kTileH / kStripRows;
 constexpr int kFineWarps = kFineThreads / 32;
 constexpr int kSlotPixels = kStripRows * kTileW;
 
-// DDA path a segment takes through the reference rasterizer (prepare's classification), times 4,
-// plus for the shallow paths (which step cell by cell) a bucket of the cells they cross: 0-3,
-// 4-15, 16-63, more. Lanes sorted by it follow the same path for about as long.
-constexpr uint32_t kDdaKeys = 20;
+// DDA path a segment takes through the reference rasterizer (prepare's classification).
 __device__ __forceinline__ uint32_t dda_kind(const DevSeg& g) {
   const int dx = g.x1 - g.x0, adx = dx < 0 ? -dx : dx, dy = g.y1 - g.y0;
   if ((g.x0 >> 8) == (g.x1 >> 8) && ((g.y0 >> 8) == ((g.y1 - 1) >> 8) || adx == 0)) return 0u;
-  if (dy >= adx) return dx < 0 ? 8u : 4u;
-  const uint32_t cells = uint32_t(adx >> 8) + 1u;
-  const uint32_t bucket = min((31u - uint32_t(__clz(cells))) >> 1, 3u);
-  return (dx < 0 ? 16u : 12u) + bucket;
+  return dy >= adx ? (dx < 0 ? 2u : 1u) : (dx < 0 ? 4u : 3u);
 }
 
 // K slots per group, 4 threads per slot; a round sorts and rasterizes up to 4 items per thread.
@@ -1022,7 +1016,7 @@ __global__ void __launch_bounds__(4 * K) coverage_kernel(FrameView f) {
   __shared__ int2 org[K];                  // x of the slot's first column, its first row
   __shared__ uint32_t meta[K];             // command flags << 16 | alpha
   __shared__ uint2 items[kCoverChunk];
-  __shared__ uint32_t kcount[kDdaKeys], kbase[kDdaKeys];
+  __shared__ uint32_t kcount[5], kbase[5];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (frame_skipped(f)) return;
   const uint32_t num_masks = min(f.totals[5], f.mask_capacity);
@@ -1048,7 +1042,7 @@ __global__ void __launch_bounds__(4 * K) coverage_kernel(FrameView f) {
 
     for (uint32_t chunk = e0; chunk < e1; chunk += kCoverChunk) {
       const int n = int(min(uint32_t(kCoverChunk), e1 - chunk));
-      if (tid < int(kDdaKeys)) kcount[tid] = 0;
+      if (tid < 5) kcount[tid] = 0;
       __syncthreads();
       // sort the chunk's items by DDA kind (counting sort through shared memory)
       uint2 it[kCoverChunk / kCoverThreads];
@@ -1065,7 +1059,7 @@ __global__ void __launch_bounds__(4 * K) coverage_kernel(FrameView f) {
       __syncthreads();
       if (tid == 0) {
         uint32_t acc = 0;
-        for (int k = 0; k < int(kDdaKeys); k++) { kbase[k] = acc; acc += kcount[k]; }
+        for (int k = 0; k < 5; k++) { kbase[k] = acc; acc += kcount[k]; }
       }
       __syncthreads();
 #pragma unroll
