@@ -262,6 +262,7 @@ struct FrameView {
   DevItem* items;              // lines and curves of every analytic command (any order)
   DevItem* curve_items;        // cubic curves from the front, quadratic / conic curves from the back
   DevPiece* pieces;            // their monotonic pieces, cubic from the front, quadratic from the back
+  uint32_t* piece_list;        // cubic piece indices: inside the clip box from the front, clipped from the back
   uint32_t piece_capacity;
   int4* cmd_bbox;              // [num_cmds] 24.8 bbox of the emitted segments: xmin, ymin, xmax, ymax
   DevSeg* segs;                // emitted segments (any order)
@@ -300,7 +301,8 @@ struct FrameView {
   uint32_t* tile_order;        // tile processing order for the persistent fine kernel
   uint32_t* tile_canvas;       // canvas index per global tile
   uint32_t* work_counter;      // [0] fine work queue, [1] items, [2] cubics, [3] their queue, [21] quads, [22] their queue,
-                               //   [23] cubic pieces, [24] their queue, [25] quadratic pieces, [26] their queue
+                               //   [23] cubic pieces, [24] their queue, [25] quadratic pieces, [26] their queue,
+                               //   [28] / [29] cubic pieces inside the clip box / clipped, [30] / [31] their queues
   uint32_t* totals;            // [8] segments, seglist bound, (cmd,strip) slots, row entries, gradient rows,
                                //   slots with segments, conic row runs
   uint32_t* rs_count;          // [num_cmds + 1] gradient row states per command (radial/conic styles)

@@ -1073,6 +1073,31 @@ struct LaneCurve {
     return next_piece(eb, false);
   }
 
+  // A monotonic piece of a curve inside the clip box (no clip flags): start_piece's first branch.
+  __device__ __forceinline__ void begin_safe_piece(Builder& eb, const Pt* pts) {
+    mc.tol_sq = eb.tol_sq;
+#pragma unroll
+    for (int i = 0; i <= DEG; i++) spline[i] = pts[i];
+    sign = spline[0].y > spline[DEG].y;
+    mc.begin(spline, sign);
+    if (mc.ltr()) mc.bound_ltr(); else mc.bound_rtl();
+    eb.desc_open(trunc_i(mc.first().x), trunc_i(mc.first().y), sign);
+    state = kLsSafe;
+  }
+  // One pass of the safe loop's body (step() and leaf() in state kLsSafe, whose split never
+  // discards): split and push while not flat and the stack has room, else emit and pop.
+  __device__ __forceinline__ void step_safe(Builder& eb) {
+    Step st;
+    if (!mc.is_flat(st) && mc.can_push()) {
+      mc.split(st);
+      mc.push(st);
+      return;
+    }
+    eb.add(trunc_i(mc.last().x), trunc_i(mc.last().y));
+    if (!mc.can_pop()) { state = kLsDone; return; }
+    mc.pop();
+  }
+
   // Starts the next piece with work (pieces that finish at their start are skipped). Returns
   // false when the curve is done.
   __device__ __forceinline__ bool next_piece(Builder& eb, bool advance) {

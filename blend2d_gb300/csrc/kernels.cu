@@ -457,6 +457,8 @@ __device__ __forceinline__ void finish_curve(FrameView& f, eb::Builder& b, uint3
 // the batched workload (piece kernel 10.8 -> 14.2 ms): the shared-memory carve-out shrinks the L1
 // that the stacks' and the segment sinks' local memory hits in.
 constexpr int kCurveThreads = 128;
+// work_counter words: cubic pieces inside the clip box, clipped cubic pieces, and their queues
+constexpr uint32_t kSafePieces = 28, kClipPieces = 29;
 // Idle lanes a warp waits for before it takes new pieces: each refill's set-up costs the warp its
 // FP64 instructions whatever the number of lanes refilled. On the batched workload 24 and 28
 // measured 246-248 ms per step, 16 and 20 250 ms, 32 251 ms, 8 257 ms and 4 259 ms.
@@ -535,16 +537,50 @@ __global__ void __launch_bounds__(128) curve_split_kernel(FrameView f) {
     pc.any = any;
     f.pieces[DEG == 3 ? idx : f.piece_capacity - 1u - idx] = pc;
   }
+  if (DEG == 3) {
+    // cubic pieces inside the clip box listed from the front of piece_list, the others from its
+    // back (one atomic per warp for each), in the pieces' order
+    const bool safe = any == 0u;
+    const uint32_t n_safe = safe ? npieces : 0u, n_clip = safe ? 0u : npieces;
+    uint32_t is = n_safe, ic = n_clip;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t vs = __shfl_up_sync(0xFFFFFFFFu, is, o), vc = __shfl_up_sync(0xFFFFFFFFu, ic, o);
+      if (lane >= o) { is += vs; ic += vc; }
+    }
+    const uint32_t ts = __shfl_sync(0xFFFFFFFFu, is, 31), tc = __shfl_sync(0xFFFFFFFFu, ic, 31);
+    uint32_t bs = 0, bc = 0;
+    if (lane == 31) {
+      if (ts) bs = atomicAdd(f.work_counter + kSafePieces, ts);
+      if (tc) bc = atomicAdd(f.work_counter + kClipPieces, tc);
+    }
+    bs = __shfl_sync(0xFFFFFFFFu, bs, 31) + is - n_safe;
+    bc = __shfl_sync(0xFFFFFFFFu, bc, 31) + ic - n_clip;
+    for (uint32_t k = 0; k < npieces; k++) {
+      const uint32_t idx = base + k;
+      if (idx >= f.piece_capacity) break;
+      if (safe) f.piece_list[bs + k] = idx;
+      else f.piece_list[f.piece_capacity - 1u - (bc + k)] = idx;
+    }
+  }
   rows = __reduce_add_sync(0xFFFFFFFFu, rows);
   if (lane == 0 && rows) atomicAdd(f.totals + 1, rows);
 }
 
-template<int DEG>
+// Cubic pieces in two kernels: those inside the clip box (most of them) run the safe loop alone,
+// a small kernel whose warps stay on the same few instructions; the clipped ones run the whole
+// clipping state machine. Quadratic and conic pieces all take the general kernel.
+enum PieceSet : int { kPiecesAll = 0, kPiecesSafe = 1, kPiecesClipped = 2 };
+
+template<int DEG, int SET>
 __global__ void __launch_bounds__(kCurveThreads) edge_pieces_kernel(FrameView f) {
   const int lane = threadIdx.x & 31;
   const uint32_t n_cubic = min(f.work_counter[23], f.piece_capacity);
-  const uint32_t n_items = DEG == 3 ? n_cubic : min(f.work_counter[25], f.piece_capacity - n_cubic);
-  uint32_t* queue = f.work_counter + (DEG == 3 ? 24 : 26);
+  const uint32_t n_items = SET == kPiecesSafe ? min(f.work_counter[kSafePieces], n_cubic)
+                         : SET == kPiecesClipped ? min(f.work_counter[kClipPieces], n_cubic)
+                         : DEG == 3 ? n_cubic : min(f.work_counter[25], f.piece_capacity - n_cubic);
+  uint32_t* queue = f.work_counter + (SET == kPiecesSafe ? kSafePieces + 2 : SET == kPiecesClipped ? kClipPieces + 2
+                                      : DEG == 3 ? 24 : 26);
   eb::Builder b;
   eb::LaneCurve<DEG, eb::CachedStack<DEG>> lc;
   bool busy = false, exhausted = false;
@@ -565,24 +601,47 @@ __global__ void __launch_bounds__(kCurveThreads) edge_pieces_kernel(FrameView f)
           exhausted = true;
         }
         else {
-          const DevPiece pc = f.pieces[DEG == 3 ? t : f.piece_capacity - 1u - t];
-          cur = pc.cmd;
-          init_builder(b, f.canvases[f.cmds[cur].canvas]);
-          b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, cur);
-          eb::Pt pts[DEG + 1];
+          const uint32_t pi = SET == kPiecesSafe ? f.piece_list[t]
+                            : SET == kPiecesClipped ? f.piece_list[f.piece_capacity - 1u - t]
+                            : DEG == 3 ? t : f.piece_capacity - 1u - t;
+          // a list entry is written only for a piece that fit in the piece array; with a frame
+          // that overflowed it (reported by curve_split), an entry may be stale: the lane then
+          // stays idle and takes another piece
+          if (SET == kPiecesAll || pi < n_cubic) {
+            const DevPiece pc = f.pieces[pi];
+            cur = pc.cmd;
+            init_builder(b, f.canvases[f.cmds[cur].canvas]);
+            b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, cur);
+            eb::Pt pts[DEG + 1];
 #pragma unroll
-          for (int i = 0; i <= DEG; i++) pts[i] = eb::Pt{pc.p[i].x, pc.p[i].y};
-          busy = lc.begin_piece(b, pts, pc.any);
-          if (!busy) finish_curve(f, b, cur, rows);
+            for (int i = 0; i <= DEG; i++) pts[i] = eb::Pt{pc.p[i].x, pc.p[i].y};
+            if (SET == kPiecesSafe) {
+              lc.begin_safe_piece(b, pts);
+              busy = true;
+            }
+            else {
+              busy = lc.begin_piece(b, pts, pc.any);
+              if (!busy) finish_curve(f, b, cur, rows);
+            }
+          }
         }
       }
     }
     if (__all_sync(0xFFFFFFFFu, !busy && exhausted)) break;   // the list is exhausted
     if (busy) {
-      lc.step(b);
-      if (lc.state == eb::kLsDone && !lc.next_piece(b, true)) {
-        finish_curve(f, b, cur, rows);
-        busy = false;
+      if (SET == kPiecesSafe) {
+        lc.step_safe(b);
+        if (lc.state == eb::kLsDone) {
+          finish_curve(f, b, cur, rows);
+          busy = false;
+        }
+      }
+      else {
+        lc.step(b);
+        if (lc.state == eb::kLsDone && !lc.next_piece(b, true)) {
+          finish_curve(f, b, cur, rows);
+          busy = false;
+        }
       }
     }
   }
@@ -1627,7 +1686,7 @@ static int max_blocks_per_sm(K kernel, int threads, size_t dyn_smem = 0) {
 int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   if (!f.num_cmds) return 0;
   const int sms = device_sms();
-  static const int max_per_sm = max_blocks_per_sm(edge_pieces_kernel<3>, kCurveThreads);
+  static const int max_per_sm = max_blocks_per_sm(edge_pieces_kernel<3, kPiecesClipped>, kCurveThreads);
   const int per_sm = cfg.cubic_blocks_per_sm > 0 && cfg.cubic_blocks_per_sm < max_per_sm ? cfg.cubic_blocks_per_sm : max_per_sm;
   const uint32_t eb = cfg.edge_block == 64 || cfg.edge_block == 256 ? uint32_t(cfg.edge_block) : 128u;
   classify_kernel<<<cdiv(f.num_cmds, 128), 128, 0, st>>>(f);
@@ -1638,9 +1697,10 @@ int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   curve_split_kernel<2><<<split_grid, 128, 0, st>>>(f);
   const uint32_t pgrid = cdiv(f.piece_capacity ? f.piece_capacity : 1, kCurveThreads);
   const uint32_t pieces_grid = pgrid < cubic_grid ? pgrid : cubic_grid;
-  edge_pieces_kernel<3><<<pieces_grid, kCurveThreads, 0, st>>>(f);
-  edge_pieces_kernel<2><<<pieces_grid, kCurveThreads, 0, st>>>(f);
-  return 6;
+  edge_pieces_kernel<3, kPiecesSafe><<<pieces_grid, kCurveThreads, 0, st>>>(f);
+  edge_pieces_kernel<3, kPiecesClipped><<<pieces_grid, kCurveThreads, 0, st>>>(f);
+  edge_pieces_kernel<2, kPiecesAll><<<pieces_grid, kCurveThreads, 0, st>>>(f);
+  return 7;
 }
 
 int launch_cmd_tiles(const FrameView& f, uint32_t* cmdrow_counts_per_cmd, cudaStream_t st) {

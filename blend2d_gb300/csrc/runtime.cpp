@@ -497,6 +497,7 @@ BLGpuResult Runtime::upload_frame(const Frame& fr, const FrameSizes* caps) {
     v.items = L.take<DevItem>(item_capacity);
     v.curve_items = L.take<DevItem>(item_capacity);
     v.pieces = L.take<DevPiece>(piece_capacity);
+    v.piece_list = L.take<uint32_t>(piece_capacity);
     v.cmd_bbox = L.take<int4>(nc);
     v.cmd_tile_x = L.take<uint32_t>(nc);
     v.cmd_tile_y = L.take<uint32_t>(nc);
@@ -1080,6 +1081,7 @@ BLGpuResult Runtime::run_noalloc(const Frame& fr) {
     v.items = L.take<DevItem>(item_capacity);
     v.curve_items = L.take<DevItem>(item_capacity);
     v.pieces = L.take<DevPiece>(piece_capacity);
+    v.piece_list = L.take<uint32_t>(piece_capacity);
     v.cmd_bbox = L.take<int4>(nc);
     v.cmd_tile_x = L.take<uint32_t>(nc);
     v.cmd_tile_y = L.take<uint32_t>(nc);

@@ -81,6 +81,49 @@ static bool same_segments(const double* xy, const uint8_t* cmd, int npts, bool c
   return true;
 }
 
+// The safe loop of the piece kernel for curves inside the clip box (eb::LaneCurve::begin_safe_piece /
+// step_safe, one builder per monotonic piece as the kernel has) against the loop flattener.
+// Returns 1 when the curve was inside the box and matched, 0 when it was not inside, -1 on a
+// mismatch.
+template<int DEG, class S>
+static int same_segments_safe(const double* xy, const uint8_t* cmd, int npts, double w, double h) {
+  Src src;
+  src.xy = xy; src.cmd = cmd; src.affine = false;
+  src.m00 = 256.0; src.m01 = 0.0; src.m10 = 0.0; src.m11 = 256.0; src.m20 = 0.0; src.m21 = 0.0;
+  static Out o1, o2;
+  Builder b1;
+  init_builder(b1, w, h, o1);
+  Pt p0 = src.tf(0);
+  uint32_t f0 = b1.fxy(p0);
+  const Pt q0 = p0;
+  src.i = 1; src.n = npts;
+  curve_to<DEG>(b1, src, p0, f0, false);
+  b1.done(); b1.sink.flush();
+
+  Builder b2;
+  init_builder(b2, w, h, o2);
+  LaneCurve<DEG, S> lc;
+  lc.spline[1] = src.tf(1);
+  if (DEG == 3) { lc.spline[2] = src.tf(2); lc.spline[3] = src.tf(3); }
+  else lc.spline[DEG] = src.tf(2);
+  if (!lc.prepare(b2, q0, b2.fxy(q0)) || lc.any) return 0;
+  for (int piece = 0; piece < lc.nout; piece += DEG) {
+    LaneCurve<DEG, S> one;
+    one.begin_safe_piece(b2, lc.spline + piece);
+    for (long guard = 0; one.state != kLsDone; guard++) {
+      if (guard > 10000000) return -1;
+      one.step_safe(b2);
+    }
+  }
+  b2.done(); b2.sink.flush();
+  if (o1.counter != o2.counter || o1.counter > (1u << 14)) return -1;
+  for (uint32_t i = 0; i < o1.counter; i++) {
+    const DevSeg &a = o1.segs[i], &c = o2.segs[i];
+    if (a.x0 != c.x0 || a.y0 != c.y0 || a.x1 != c.x1 || a.y1 != c.y1 || o1.meta[i] != o2.meta[i]) return -1;
+  }
+  return 1;
+}
+
 int main(int argc, char** argv) {
   std::mt19937_64 rng(argc > 1 ? strtoull(argv[1], nullptr, 10) : 1);
   const int n = argc > 2 ? atoi(argv[2]) : 100000;
@@ -140,6 +183,35 @@ int main(int argc, char** argv) {
     }
     if (!ok && ++fails <= 5) printf("mismatch: curve %d (kind %d)\n", it, it % 3);
   }
+  // curves inside the clip box (points anywhere on the canvas, borders included) through the safe
+  // loop, cubic and quadratic
+  long safe_tested = 0;
+  for (int it = 0; it < n; it++) {
+    const bool cached = (it & 4) != 0;
+    const double w = 16 + std::floor(u(rng) * 200), h = 16 + std::floor(u(rng) * 200);
+    auto inside = [&](double lim) {
+      const double r = u(rng);
+      if (r < 0.05) return 0.0;
+      if (r < 0.1) return lim;
+      if (r < 0.3) return std::floor(u(rng) * lim) + (u(rng) < 0.5 ? 0.5 : 0.0);
+      return lim * u(rng);
+    };
+    double xy[8];
+    for (int k = 0; k < 4; k++) { xy[2 * k] = inside(w); xy[2 * k + 1] = inside(h); }
+    if (u(rng) < 0.1) xy[2] = xy[0];
+    int r;
+    if (it & 1) {
+      const uint8_t c[4] = {0, 4, 4, 4};
+      r = cached ? same_segments_safe<3, CachedStack<3>>(xy, c, 4, w, h) : same_segments_safe<3, LocalStack<3>>(xy, c, 4, w, h);
+    }
+    else {
+      const uint8_t c[3] = {0, 2, 2};
+      r = cached ? same_segments_safe<2, CachedStack<2>>(xy, c, 3, w, h) : same_segments_safe<2, LocalStack<2>>(xy, c, 3, w, h);
+    }
+    if (r > 0) safe_tested++;
+    if (r < 0 && ++fails <= 10) printf("mismatch: safe curve %d\n", it);
+  }
+  printf("safe curves %ld\n", safe_tested);
   printf("curves %d mismatches %ld\n", n, fails);
   return fails ? 1 : 0;
 }
