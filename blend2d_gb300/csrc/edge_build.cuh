@@ -596,6 +596,8 @@ struct CachedStack {
   }
 };
 
+struct NoStack {};
+
 // Monotonic curve with an explicit subdivision stack (FlattenMonoQuad / FlattenMonoCubic).
 template<int DEG, class S = LocalStack<DEG>>
 struct Mono {
@@ -681,6 +683,57 @@ struct Mono {
     stack.pop(sp, p + 1);
   }
 };
+
+// The subdivision of a monotonic piece inside the clip box as a tree. The loop flattener
+// (flatten_safe) walks it depth first with a stack: a node that is not flat and finds the stack with
+// room is split, its right half pushed and its left half taken next; any other node is a leaf, whose
+// segment (first point to last point, truncated) is emitted, and the next node is popped. A leaf's
+// segment depends only on the leaf, and a node's fate only on its points and on its level (the
+// stack entries pending while it is processed: one more than its parent's for a left half, the
+// parent's for a right half). Taking the nodes in another order, or on other lanes, therefore gives
+// the same segments; only their order in the output differs, and nothing downstream depends on it.
+template<int DEG>
+struct TreeNode {
+  Pt p[DEG + 1];
+  int level;
+};
+
+// The tree's root: the piece oriented and bounded as start_piece does for a piece with no clip flags.
+template<int DEG>
+__device__ __forceinline__ TreeNode<DEG> tree_root(const Pt* pts, uint32_t& sign) {
+  Mono<DEG, NoStack> mc;
+  sign = pts[0].y > pts[DEG].y;
+  mc.begin(pts, sign);
+  if (mc.ltr()) mc.bound_ltr(); else mc.bound_rtl();
+  TreeNode<DEG> n;
+#pragma unroll
+  for (int i = 0; i <= DEG; i++) n.p[i] = mc.p[i];
+  n.level = 0;
+  return n;
+}
+
+// One node: true for a leaf, else its two halves (Mono::is_flat / split / push / pop).
+template<int DEG>
+__device__ __forceinline__ bool tree_step(const TreeNode<DEG>& n, double tol_sq, TreeNode<DEG>& left, TreeNode<DEG>& right) {
+  Mono<DEG, NoStack> mc;
+  mc.tol_sq = tol_sq;
+#pragma unroll
+  for (int i = 0; i <= DEG; i++) mc.p[i] = n.p[i];
+  Step st;
+  if (mc.is_flat(st) || n.level == kStackLevels) return true;
+  mc.split(st);
+  if (DEG == 2) {
+    left.p[0] = n.p[0]; left.p[1] = st.p01; left.p[2] = st.p012;
+    right.p[0] = st.p012; right.p[1] = st.p12; right.p[2] = n.p[2];
+  }
+  else {
+    left.p[0] = n.p[0]; left.p[1] = st.p01; left.p[2] = st.p012; left.p[DEG] = st.p0123;
+    right.p[0] = st.p0123; right.p[1] = st.p123; right.p[2] = st.p23; right.p[DEG] = n.p[DEG];
+  }
+  left.level = n.level + 1;
+  right.level = n.level;
+  return false;
+}
 
 __device__ __forceinline__ double dx_div_dy(Pt a, Pt b) { return (b.x - a.x) / (b.y - a.y); }
 __device__ __forceinline__ double dy_div_dx(Pt a, Pt b) { return (b.y - a.y) / (b.x - a.x); }
@@ -1071,31 +1124,6 @@ struct LaneCurve {
     any = any_flags;
     piece = 0;
     return next_piece(eb, false);
-  }
-
-  // A monotonic piece of a curve inside the clip box (no clip flags): start_piece's first branch.
-  __device__ __forceinline__ void begin_safe_piece(Builder& eb, const Pt* pts) {
-    mc.tol_sq = eb.tol_sq;
-#pragma unroll
-    for (int i = 0; i <= DEG; i++) spline[i] = pts[i];
-    sign = spline[0].y > spline[DEG].y;
-    mc.begin(spline, sign);
-    if (mc.ltr()) mc.bound_ltr(); else mc.bound_rtl();
-    eb.desc_open(trunc_i(mc.first().x), trunc_i(mc.first().y), sign);
-    state = kLsSafe;
-  }
-  // One pass of the safe loop's body (step() and leaf() in state kLsSafe, whose split never
-  // discards): split and push while not flat and the stack has room, else emit and pop.
-  __device__ __forceinline__ void step_safe(Builder& eb) {
-    Step st;
-    if (!mc.is_flat(st) && mc.can_push()) {
-      mc.split(st);
-      mc.push(st);
-      return;
-    }
-    eb.add(trunc_i(mc.last().x), trunc_i(mc.last().y));
-    if (!mc.can_pop()) { state = kLsDone; return; }
-    mc.pop();
   }
 
   // Starts the next piece with work (pieces that finish at their start are skipped). Returns

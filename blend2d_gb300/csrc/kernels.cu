@@ -567,20 +567,175 @@ __global__ void __launch_bounds__(128) curve_split_kernel(FrameView f) {
   if (lane == 0 && rows) atomicAdd(f.totals + 1, rows);
 }
 
-// Cubic pieces in two kernels: those inside the clip box (most of them) run the safe loop alone,
-// a small kernel whose warps stay on the same few instructions; the clipped ones run the whole
-// clipping state machine. Quadratic and conic pieces all take the general kernel.
-enum PieceSet : int { kPiecesAll = 0, kPiecesSafe = 1, kPiecesClipped = 2 };
+// The cubic pieces inside the clip box, flattened as subdivision trees (eb::TreeNode) whose nodes
+// the lanes of a warp share. A lane splits its node, goes on with the left half and keeps the
+// right half on its own stack, unless a lane of the warp is out of work: then the right half goes
+// to that lane through shared memory. So lanes do not sit idle while other lanes' trees still have
+// nodes, and the FP64 instructions (whose cost to the pipe does not depend on the active lanes)
+// serve more of them. The segments are those of the loop flattener, in another order; they are
+// appended for the warp with one atomic per step, and each lane accumulates the command bounds
+// finish_curve would for the run of segments it emits for one command.
+struct alignas(16) TreeXchg {
+  double x[4], y[4];
+  uint32_t cmd, level, sign, pad;
+};
+
+__global__ void __launch_bounds__(kCurveThreads) edge_tree_kernel(FrameView f) {
+  constexpr int kWarps = kCurveThreads / 32;
+  __shared__ TreeXchg xchg[kWarps][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t n_cubic = min(f.work_counter[23], f.piece_capacity);
+  const uint32_t n_items = min(f.work_counter[kSafePieces], n_cubic);
+  uint32_t* queue = f.work_counter + kSafePieces + 2;
+  const double tol = 0.20 * 256.0;
+  const double tol_sq = tol * tol;                    // init_builder's
+  eb::TreeNode<3> cur;
+  eb::TreeNode<3> stack[eb::kStackLevels];
+  int nst = 0;
+  uint32_t cmd = 0, sign = 0;
+  bool busy = false, exhausted = false;
+  // bounds of the segments emitted for command acc_cmd since the last flush
+  uint32_t acc_cmd = 0xFFFFFFFFu, acc_rows = 0, rows = 0;
+  int xmin = INT32_MAX, ymin = INT32_MAX, xmax = INT32_MIN, ymax = INT32_MIN;
+  auto flush_bounds = [&]() {
+    if (acc_cmd == 0xFFFFFFFFu) return;
+    int4* bb = f.cmd_bbox + acc_cmd;
+    atomicMin(&bb->x, xmin);
+    atomicMin(&bb->y, ymin);
+    atomicMax(&bb->z, xmax);
+    atomicMax(&bb->w, ymax);
+    atomicOr(&f.cmds_rw[acc_cmd].status, kCmdHasSegments);
+    rows += acc_rows;
+    acc_cmd = 0xFFFFFFFFu;
+    acc_rows = 0;
+    xmin = ymin = INT32_MAX;
+    xmax = ymax = INT32_MIN;
+  };
+
+  for (;;) {
+    // new pieces for the idle lanes, as edge_pieces_kernel takes them
+    const uint32_t want = __ballot_sync(0xFFFFFFFFu, !busy && !exhausted);
+    if (want && (__popc(want) >= kPieceRefillLanes || !__any_sync(0xFFFFFFFFu, busy))) {
+      const int leader = __ffs(want) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(queue, uint32_t(__popc(want)));
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (!busy && !exhausted) {
+        const uint32_t t = base + uint32_t(__popc(want & lt));
+        if (t >= n_items) {
+          exhausted = true;
+        }
+        else {
+          const uint32_t pi = f.piece_list[t];
+          // an entry of a piece that did not fit in the piece array (the frame fails) is skipped
+          if (pi < n_cubic) {
+            const DevPiece pc = f.pieces[pi];
+            eb::Pt pts[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) pts[i] = eb::Pt{pc.p[i].x, pc.p[i].y};
+            cur = eb::tree_root<3>(pts, sign);
+            cmd = pc.cmd;
+            nst = 0;
+            busy = true;
+          }
+        }
+      }
+    }
+    if (__all_sync(0xFFFFFFFFu, !busy && exhausted)) break;
+
+    eb::TreeNode<3> left, right;
+    const bool leaf = busy && eb::tree_step<3>(cur, tol_sq, left, right);
+    const bool split = busy && !leaf;
+
+    // a leaf's segment (Builder::add after desc_open, Sink::emit), one atomic for the warp
+    int x0 = 0, y0 = 0, x1 = 0, y1 = 0;
+    if (leaf) {
+      x0 = eb::trunc_i(cur.p[0].x); y0 = eb::trunc_i(cur.p[0].y);
+      x1 = eb::trunc_i(cur.p[3].x); y1 = eb::trunc_i(cur.p[3].y);
+    }
+    const bool emit = leaf && y0 != y1;
+    const uint32_t em = __ballot_sync(0xFFFFFFFFu, emit);
+    if (em) {
+      const int leader = __ffs(em) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(f.totals + 0, uint32_t(__popc(em)));
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (emit) {
+        const uint32_t idx = base + uint32_t(__popc(em & lt));
+        if (idx < f.seg_capacity) {
+          f.segs[idx] = DevSeg{x0, y0, x1, y1};
+          f.seg_meta[idx] = (cmd << 1) | sign;
+        }
+        if (cmd != acc_cmd) { flush_bounds(); acc_cmd = cmd; }
+        // Sink::emit's bounds and seglist-entry bound
+        const uint32_t strips = (uint32_t((y1 - 1) >> 8) >> kStripShift) - (uint32_t(y0 >> 8) >> kStripShift) + 1u;
+        const int lo = min(x0, x1) - 256, hi = max(x0, x1) + 256;
+        const uint32_t tiles = uint32_t((((hi >> 8) + 1) >> kTileShift) - ((lo >> 8) >> kTileShift) + 1);
+        acc_rows += tiles + 3u * strips;
+        ymin = min(ymin, y0);
+        ymax = max(ymax, y1);
+        xmin = min(xmin, min(x0, x1));
+        xmax = max(xmax, max(x0, x1));
+      }
+    }
+    if (leaf) {
+      if (nst) cur = stack[--nst];
+      else busy = false;
+    }
+
+    // the right halves of this step's splits go first to the lanes out of work
+    const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !busy);
+    const uint32_t donors = __ballot_sync(0xFFFFFFFFu, split);
+    const int k = min(__popc(idle), __popc(donors));
+    if (split) {
+      const int r = __popc(donors & lt);
+      if (r < k) {
+        TreeXchg& x = xchg[w][r];
+#pragma unroll
+        for (int i = 0; i < 4; i++) { x.x[i] = right.p[i].x; x.y[i] = right.p[i].y; }
+        x.cmd = cmd;
+        x.level = uint32_t(right.level);
+        x.sign = sign;
+      }
+      else {
+        stack[nst++] = right;
+      }
+      cur = left;
+    }
+    __syncwarp();
+    if (!busy) {
+      const int q = __popc(idle & lt);
+      if (q < k) {
+        const TreeXchg& x = xchg[w][q];
+#pragma unroll
+        for (int i = 0; i < 4; i++) cur.p[i] = eb::Pt{x.x[i], x.y[i]};
+        cur.level = int(x.level);
+        cmd = x.cmd;
+        sign = x.sign;
+        nst = 0;
+        busy = true;
+      }
+    }
+    __syncwarp();
+  }
+  flush_bounds();
+  rows = __reduce_add_sync(0xFFFFFFFFu, rows);
+  if (lane == 0 && rows) atomicAdd(f.totals + 1, rows);
+}
+
+// Cubic pieces in two kernels: those inside the clip box (most of them) are flattened by
+// edge_tree_kernel, whose lanes share the nodes of their subdivision trees; the clipped ones run the
+// clipping state machine here. Quadratic and conic pieces all take this kernel.
+enum PieceSet : int { kPiecesAll = 0, kPiecesClipped = 2 };
 
 template<int DEG, int SET>
 __global__ void __launch_bounds__(kCurveThreads) edge_pieces_kernel(FrameView f) {
   const int lane = threadIdx.x & 31;
   const uint32_t n_cubic = min(f.work_counter[23], f.piece_capacity);
-  const uint32_t n_items = SET == kPiecesSafe ? min(f.work_counter[kSafePieces], n_cubic)
-                         : SET == kPiecesClipped ? min(f.work_counter[kClipPieces], n_cubic)
+  const uint32_t n_items = SET == kPiecesClipped ? min(f.work_counter[kClipPieces], n_cubic)
                          : DEG == 3 ? n_cubic : min(f.work_counter[25], f.piece_capacity - n_cubic);
-  uint32_t* queue = f.work_counter + (SET == kPiecesSafe ? kSafePieces + 2 : SET == kPiecesClipped ? kClipPieces + 2
-                                      : DEG == 3 ? 24 : 26);
+  uint32_t* queue = f.work_counter + (SET == kPiecesClipped ? kClipPieces + 2 : DEG == 3 ? 24 : 26);
   eb::Builder b;
   eb::LaneCurve<DEG, eb::CachedStack<DEG>> lc;
   bool busy = false, exhausted = false;
@@ -601,8 +756,7 @@ __global__ void __launch_bounds__(kCurveThreads) edge_pieces_kernel(FrameView f)
           exhausted = true;
         }
         else {
-          const uint32_t pi = SET == kPiecesSafe ? f.piece_list[t]
-                            : SET == kPiecesClipped ? f.piece_list[f.piece_capacity - 1u - t]
+          const uint32_t pi = SET == kPiecesClipped ? f.piece_list[f.piece_capacity - 1u - t]
                             : DEG == 3 ? t : f.piece_capacity - 1u - t;
           // a list entry is written only for a piece that fit in the piece array; with a frame
           // that overflowed it (reported by curve_split), an entry may be stale: the lane then
@@ -615,33 +769,18 @@ __global__ void __launch_bounds__(kCurveThreads) edge_pieces_kernel(FrameView f)
             eb::Pt pts[DEG + 1];
 #pragma unroll
             for (int i = 0; i <= DEG; i++) pts[i] = eb::Pt{pc.p[i].x, pc.p[i].y};
-            if (SET == kPiecesSafe) {
-              lc.begin_safe_piece(b, pts);
-              busy = true;
-            }
-            else {
-              busy = lc.begin_piece(b, pts, pc.any);
-              if (!busy) finish_curve(f, b, cur, rows);
-            }
+            busy = lc.begin_piece(b, pts, pc.any);
+            if (!busy) finish_curve(f, b, cur, rows);
           }
         }
       }
     }
     if (__all_sync(0xFFFFFFFFu, !busy && exhausted)) break;   // the list is exhausted
     if (busy) {
-      if (SET == kPiecesSafe) {
-        lc.step_safe(b);
-        if (lc.state == eb::kLsDone) {
-          finish_curve(f, b, cur, rows);
-          busy = false;
-        }
-      }
-      else {
-        lc.step(b);
-        if (lc.state == eb::kLsDone && !lc.next_piece(b, true)) {
-          finish_curve(f, b, cur, rows);
-          busy = false;
-        }
+      lc.step(b);
+      if (lc.state == eb::kLsDone && !lc.next_piece(b, true)) {
+        finish_curve(f, b, cur, rows);
+        busy = false;
       }
     }
   }
@@ -1697,7 +1836,7 @@ int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   curve_split_kernel<2><<<split_grid, 128, 0, st>>>(f);
   const uint32_t pgrid = cdiv(f.piece_capacity ? f.piece_capacity : 1, kCurveThreads);
   const uint32_t pieces_grid = pgrid < cubic_grid ? pgrid : cubic_grid;
-  edge_pieces_kernel<3, kPiecesSafe><<<pieces_grid, kCurveThreads, 0, st>>>(f);
+  edge_tree_kernel<<<pieces_grid, kCurveThreads, 0, st>>>(f);
   edge_pieces_kernel<3, kPiecesClipped><<<pieces_grid, kCurveThreads, 0, st>>>(f);
   edge_pieces_kernel<2, kPiecesAll><<<pieces_grid, kCurveThreads, 0, st>>>(f);
   return 7;

@@ -9,6 +9,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <random>
+#include <tuple>
 #include <vector>
 
 #define __device__
@@ -81,16 +82,16 @@ static bool same_segments(const double* xy, const uint8_t* cmd, int npts, bool c
   return true;
 }
 
-// The safe loop of the piece kernel for curves inside the clip box (eb::LaneCurve::begin_safe_piece /
-// step_safe, one builder per monotonic piece as the kernel has) against the loop flattener.
-// Returns 1 when the curve was inside the box and matched, 0 when it was not inside, -1 on a
-// mismatch.
-template<int DEG, class S>
-static int same_segments_safe(const double* xy, const uint8_t* cmd, int npts, double w, double h) {
+// The subdivision trees of the tree kernel (edge_tree_kernel) for curves inside the clip box: every
+// monotonic piece's tree (eb::tree_root / tree_step) walked in a random order, as lanes sharing
+// nodes would, must give the loop flattener's segments, as a multiset. Returns 1 when the curve was
+// inside the box and matched, 0 when it was not inside, -1 on a mismatch.
+template<int DEG>
+static int same_segments_tree(const double* xy, const uint8_t* cmd, int npts, double w, double h, std::mt19937_64& rng) {
   Src src;
   src.xy = xy; src.cmd = cmd; src.affine = false;
   src.m00 = 256.0; src.m01 = 0.0; src.m10 = 0.0; src.m11 = 256.0; src.m20 = 0.0; src.m21 = 0.0;
-  static Out o1, o2;
+  static Out o1;
   Builder b1;
   init_builder(b1, w, h, o1);
   Pt p0 = src.tf(0);
@@ -101,26 +102,43 @@ static int same_segments_safe(const double* xy, const uint8_t* cmd, int npts, do
   b1.done(); b1.sink.flush();
 
   Builder b2;
+  static Out o2;
   init_builder(b2, w, h, o2);
-  LaneCurve<DEG, S> lc;
+  LaneCurve<DEG, LocalStack<DEG>> lc;
   lc.spline[1] = src.tf(1);
   if (DEG == 3) { lc.spline[2] = src.tf(2); lc.spline[3] = src.tf(3); }
   else lc.spline[DEG] = src.tf(2);
   if (!lc.prepare(b2, q0, b2.fxy(q0)) || lc.any) return 0;
+  struct Seg { int x0, y0, x1, y1; uint32_t meta; };
+  std::vector<Seg> want, got;
+  for (uint32_t i = 0; i < o1.counter; i++)
+    want.push_back(Seg{o1.segs[i].x0, o1.segs[i].y0, o1.segs[i].x1, o1.segs[i].y1, o1.meta[i]});
   for (int piece = 0; piece < lc.nout; piece += DEG) {
-    LaneCurve<DEG, S> one;
-    one.begin_safe_piece(b2, lc.spline + piece);
-    for (long guard = 0; one.state != kLsDone; guard++) {
+    uint32_t sign = 0;
+    std::vector<TreeNode<DEG>> pending{tree_root<DEG>(lc.spline + piece, sign)};
+    for (long guard = 0; !pending.empty(); guard++) {
       if (guard > 10000000) return -1;
-      one.step_safe(b2);
+      const size_t pick = size_t(rng() % pending.size());
+      const TreeNode<DEG> n = pending[pick];
+      pending[pick] = pending.back();
+      pending.pop_back();
+      TreeNode<DEG> l, r;
+      if (tree_step<DEG>(n, b2.tol_sq, l, r)) {
+        const int x0 = trunc_i(n.p[0].x), y0 = trunc_i(n.p[0].y), x1 = trunc_i(n.p[DEG].x), y1 = trunc_i(n.p[DEG].y);
+        if (y0 != y1) got.push_back(Seg{x0, y0, x1, y1, (7u << 1) | sign});
+      }
+      else {
+        pending.push_back(l);
+        pending.push_back(r);
+      }
     }
   }
-  b2.done(); b2.sink.flush();
-  if (o1.counter != o2.counter || o1.counter > (1u << 14)) return -1;
-  for (uint32_t i = 0; i < o1.counter; i++) {
-    const DevSeg &a = o1.segs[i], &c = o2.segs[i];
-    if (a.x0 != c.x0 || a.y0 != c.y0 || a.x1 != c.x1 || a.y1 != c.y1 || o1.meta[i] != o2.meta[i]) return -1;
-  }
+  auto key = [](const Seg& s) { return std::make_tuple(s.x0, s.y0, s.x1, s.y1, s.meta); };
+  std::sort(want.begin(), want.end(), [&](const Seg& a, const Seg& c) { return key(a) < key(c); });
+  std::sort(got.begin(), got.end(), [&](const Seg& a, const Seg& c) { return key(a) < key(c); });
+  if (want.size() != got.size()) return -1;
+  for (size_t i = 0; i < want.size(); i++)
+    if (key(want[i]) != key(got[i])) return -1;
   return 1;
 }
 
@@ -183,12 +201,12 @@ int main(int argc, char** argv) {
     }
     if (!ok && ++fails <= 5) printf("mismatch: curve %d (kind %d)\n", it, it % 3);
   }
-  // curves inside the clip box (points anywhere on the canvas, borders included) through the safe
-  // loop, cubic and quadratic
+  // curves inside the clip box (points anywhere on the canvas, borders included) as subdivision
+  // trees walked in a random order, cubic and quadratic
   long safe_tested = 0;
   for (int it = 0; it < n; it++) {
-    const bool cached = (it & 4) != 0;
-    const double w = 16 + std::floor(u(rng) * 200), h = 16 + std::floor(u(rng) * 200);
+    const double span = (it % 4 == 0) ? 4000.0 : 200.0;     // some large curves: deep trees
+    const double w = 16 + std::floor(u(rng) * span), h = 16 + std::floor(u(rng) * span);
     auto inside = [&](double lim) {
       const double r = u(rng);
       if (r < 0.05) return 0.0;
@@ -202,11 +220,11 @@ int main(int argc, char** argv) {
     int r;
     if (it & 1) {
       const uint8_t c[4] = {0, 4, 4, 4};
-      r = cached ? same_segments_safe<3, CachedStack<3>>(xy, c, 4, w, h) : same_segments_safe<3, LocalStack<3>>(xy, c, 4, w, h);
+      r = same_segments_tree<3>(xy, c, 4, w, h, rng);
     }
     else {
       const uint8_t c[3] = {0, 2, 2};
-      r = cached ? same_segments_safe<2, CachedStack<2>>(xy, c, 3, w, h) : same_segments_safe<2, LocalStack<2>>(xy, c, 3, w, h);
+      r = same_segments_tree<2>(xy, c, 3, w, h, rng);
     }
     if (r > 0) safe_tested++;
     if (r < 0 && ++fails <= 10) printf("mismatch: safe curve %d\n", it);
