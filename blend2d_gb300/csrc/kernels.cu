@@ -575,6 +575,12 @@ __global__ void __launch_bounds__(128) curve_split_kernel(FrameView f) {
 // serve more of them. The segments are those of the loop flattener, in another order; they are
 // appended for the warp with one atomic per step, and each lane accumulates the command bounds
 // finish_curve would for the run of segments it emits for one command.
+// Idle lanes a warp of the tree flattener waits for before it takes new pieces, and its blocks per
+// SM: refills of 16, 24 and 32 lanes and 3, 4 and 6 blocks measured within 1 % of each other on the
+// batched workload (215.6-218.6 ms per step); 16 was the best on the curves frame (2.60 ms).
+constexpr int kTreeRefillLanes = 16;
+constexpr int kTreeBlocksPerSM = 3;
+
 struct alignas(16) TreeXchg {
   double x[4], y[4];
   uint32_t cmd, level, sign, pad;
@@ -616,7 +622,7 @@ __global__ void __launch_bounds__(kCurveThreads) edge_tree_kernel(FrameView f) {
   for (;;) {
     // new pieces for the idle lanes, as edge_pieces_kernel takes them
     const uint32_t want = __ballot_sync(0xFFFFFFFFu, !busy && !exhausted);
-    if (want && (__popc(want) >= kPieceRefillLanes || !__any_sync(0xFFFFFFFFu, busy))) {
+    if (want && (__popc(want) >= kTreeRefillLanes || !__any_sync(0xFFFFFFFFu, busy))) {
       const int leader = __ffs(want) - 1;
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(queue, uint32_t(__popc(want)));
@@ -1836,7 +1842,8 @@ int launch_edges(const FrameView& f, const LaunchConfig& cfg, cudaStream_t st) {
   curve_split_kernel<2><<<split_grid, 128, 0, st>>>(f);
   const uint32_t pgrid = cdiv(f.piece_capacity ? f.piece_capacity : 1, kCurveThreads);
   const uint32_t pieces_grid = pgrid < cubic_grid ? pgrid : cubic_grid;
-  edge_tree_kernel<<<pieces_grid, kCurveThreads, 0, st>>>(f);
+  const uint32_t tree_grid = min(pgrid, uint32_t(sms * kTreeBlocksPerSM));
+  edge_tree_kernel<<<tree_grid, kCurveThreads, 0, st>>>(f);
   edge_pieces_kernel<3, kPiecesClipped><<<pieces_grid, kCurveThreads, 0, st>>>(f);
   edge_pieces_kernel<2, kPiecesAll><<<pieces_grid, kCurveThreads, 0, st>>>(f);
   return 7;
