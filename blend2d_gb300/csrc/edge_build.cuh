@@ -712,6 +712,24 @@ __device__ __forceinline__ TreeNode<DEG> tree_root(const Pt* pts, uint32_t& sign
   return n;
 }
 
+// Whether a monotonic piece is flattened exactly as by the safe loop, so that its tree can be
+// walked in any order. True for a piece of a curve with no clip flags (`any` 0). For a piece of a
+// clipped curve, oriented to increasing y (first point f, last point l), the clipping flattener
+// (flatten_unsafe) runs its "inside" loop (LTR_AddLine / RTL_AddLine) with no clip ever firing
+// when: its x extent exceeds the vertical-line limit (else it is emitted as one line); it starts
+// at or below the clip box's top (else the top loop); it ends above its bottom (y_end is then l.y,
+// and no leaf reaches cy1); and it stays between x0 and x1 (its subdivision points lie between f
+// and l once the control points are bounded): then that loop is the safe loop, with the same
+// desc_open, and finishes with nothing outside to accumulate.
+__device__ __forceinline__ bool piece_flattens_safe(const Pt* pts, int deg, uint32_t any, const Builder& eb) {
+  if (!any) return true;
+  const bool sign = pts[0].y > pts[deg].y;
+  const Pt f = sign ? pts[deg] : pts[0], l = sign ? pts[0] : pts[deg];
+  if (!(fabs(f.x - l.x) > 0.00390625)) return false;
+  if (!(f.y >= eb.cy0) || !(l.y < eb.cy1)) return false;
+  return f.x < l.x ? (f.x >= eb.cx0 && l.x <= eb.cx1) : (f.x <= eb.cx1 && l.x >= eb.cx0);
+}
+
 // One node: true for a leaf, else its two halves (Mono::is_flat / split / push / pop).
 template<int DEG>
 __device__ __forceinline__ bool tree_step(const TreeNode<DEG>& n, double tol_sq, TreeNode<DEG>& left, TreeNode<DEG>& right) {

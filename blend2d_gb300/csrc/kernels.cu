@@ -538,10 +538,16 @@ __global__ void __launch_bounds__(128) curve_split_kernel(FrameView f) {
     f.pieces[DEG == 3 ? idx : f.piece_capacity - 1u - idx] = pc;
   }
   if (DEG == 3) {
-    // cubic pieces inside the clip box listed from the front of piece_list, the others from its
+    // cubic pieces the safe loop flattens listed from the front of piece_list, the others from its
     // back (one atomic per warp for each), in the pieces' order
-    const bool safe = any == 0u;
-    const uint32_t n_safe = safe ? npieces : 0u, n_clip = safe ? 0u : npieces;
+    uint32_t safe_mask = 0;                    // bit k: piece k flattens as by the safe loop
+    if (npieces) {
+      eb::Builder cb;
+      init_builder(cb, f.canvases[f.cmds[cmd_i].canvas]);
+      for (uint32_t k = 0; k < npieces; k++)
+        if (eb::piece_flattens_safe(spline + k * DEG, DEG, any, cb)) safe_mask |= 1u << k;
+    }
+    const uint32_t n_safe = uint32_t(__popc(safe_mask)), n_clip = npieces - n_safe;
     uint32_t is = n_safe, ic = n_clip;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -556,11 +562,12 @@ __global__ void __launch_bounds__(128) curve_split_kernel(FrameView f) {
     }
     bs = __shfl_sync(0xFFFFFFFFu, bs, 31) + is - n_safe;
     bc = __shfl_sync(0xFFFFFFFFu, bc, 31) + ic - n_clip;
+    uint32_t ks = 0, kc = 0;
     for (uint32_t k = 0; k < npieces; k++) {
       const uint32_t idx = base + k;
       if (idx >= f.piece_capacity) break;
-      if (safe) f.piece_list[bs + k] = idx;
-      else f.piece_list[f.piece_capacity - 1u - (bc + k)] = idx;
+      if ((safe_mask >> k) & 1u) f.piece_list[bs + ks++] = idx;
+      else f.piece_list[f.piece_capacity - 1u - (bc + kc++)] = idx;
     }
   }
   rows = __reduce_add_sync(0xFFFFFFFFu, rows);

@@ -142,6 +142,68 @@ static int same_segments_tree(const double* xy, const uint8_t* cmd, int npts, do
   return 1;
 }
 
+// Pieces routed to the tree flattener (eb::piece_flattens_safe), including pieces of clipped
+// curves: each must give, as a multiset, the segments the lane flattener gives for it alone with a
+// builder of its own (as edge_pieces_kernel runs it). Returns the number of routed pieces of
+// clipped curves compared, or -1 on a mismatch.
+static int same_segments_routed(const double* xy, const uint8_t* cmd, double w, double h, std::mt19937_64& rng) {
+  Src src;
+  src.xy = xy; src.cmd = cmd; src.affine = false;
+  src.m00 = 256.0; src.m01 = 0.0; src.m10 = 0.0; src.m11 = 256.0; src.m20 = 0.0; src.m21 = 0.0;
+  static Out ob, oa;
+  Builder b;
+  init_builder(b, w, h, ob);
+  LaneCurve<3, CachedStack<3>> lc;
+  const Pt q0 = src.tf(0);
+  lc.spline[1] = src.tf(1); lc.spline[2] = src.tf(2); lc.spline[3] = src.tf(3);
+  if (!lc.prepare(b, q0, b.fxy(q0))) return 0;
+  int routed_clipped = 0;
+  struct Seg { int x0, y0, x1, y1; uint32_t meta; };
+  auto key = [](const Seg& s) { return std::make_tuple(s.x0, s.y0, s.x1, s.y1, s.meta); };
+  for (int piece = 0; piece < lc.nout; piece += 3) {
+    const Pt* pts = lc.spline + piece;
+    if (!piece_flattens_safe(pts, 3, lc.any, b)) continue;
+    Builder ba;
+    init_builder(ba, w, h, oa);
+    LaneCurve<3, CachedStack<3>> la;
+    bool busy = la.begin_piece(ba, pts, lc.any);
+    for (long guard = 0; busy; guard++) {
+      if (guard > 10000000) return -1;
+      la.step(ba);
+      if (la.state == kLsDone && !la.next_piece(ba, true)) busy = false;
+    }
+    ba.done(); ba.sink.flush();
+    std::vector<Seg> want, got;
+    for (uint32_t i = 0; i < oa.counter; i++)
+      want.push_back(Seg{oa.segs[i].x0, oa.segs[i].y0, oa.segs[i].x1, oa.segs[i].y1, oa.meta[i]});
+    uint32_t sign = 0;
+    std::vector<TreeNode<3>> pending{tree_root<3>(pts, sign)};
+    for (long guard = 0; !pending.empty(); guard++) {
+      if (guard > 10000000) return -1;
+      const size_t pick = size_t(rng() % pending.size());
+      const TreeNode<3> n = pending[pick];
+      pending[pick] = pending.back();
+      pending.pop_back();
+      TreeNode<3> l, r;
+      if (tree_step<3>(n, b.tol_sq, l, r)) {
+        const int x0 = trunc_i(n.p[0].x), y0 = trunc_i(n.p[0].y), x1 = trunc_i(n.p[3].x), y1 = trunc_i(n.p[3].y);
+        if (y0 != y1) got.push_back(Seg{x0, y0, x1, y1, (7u << 1) | sign});
+      }
+      else {
+        pending.push_back(l);
+        pending.push_back(r);
+      }
+    }
+    std::sort(want.begin(), want.end(), [&](const Seg& a, const Seg& c) { return key(a) < key(c); });
+    std::sort(got.begin(), got.end(), [&](const Seg& a, const Seg& c) { return key(a) < key(c); });
+    if (want.size() != got.size()) return -1;
+    for (size_t i = 0; i < want.size(); i++)
+      if (key(want[i]) != key(got[i])) return -1;
+    if (lc.any) routed_clipped++;
+  }
+  return routed_clipped;
+}
+
 int main(int argc, char** argv) {
   std::mt19937_64 rng(argc > 1 ? strtoull(argv[1], nullptr, 10) : 1);
   const int n = argc > 2 ? atoi(argv[2]) : 100000;
@@ -230,6 +292,28 @@ int main(int argc, char** argv) {
     if (r < 0 && ++fails <= 10) printf("mismatch: safe curve %d\n", it);
   }
   printf("safe curves %ld\n", safe_tested);
+  // cubic curves around and across the clip box: the pieces routed to the tree flattener
+  long routed = 0;
+  for (int it = 0; it < n; it++) {
+    const double w = 16 + std::floor(u(rng) * 200), h = 16 + std::floor(u(rng) * 200);
+    auto coord = [&](double lim) {
+      const double r = u(rng);
+      if (r < 0.08) return 0.0;
+      if (r < 0.16) return lim;
+      if (r < 0.22) return std::floor(u(rng) * lim);
+      if (r < 0.26) return -1e6 + 2e6 * u(rng);
+      if (r < 0.6) return std::floor(-0.25 * lim + 1.5 * lim * u(rng)) + (u(rng) < 0.5 ? 0.5 : 0.0);
+      return -0.5 * lim + 2.0 * lim * u(rng);
+    };
+    double xy[8];
+    for (int k = 0; k < 4; k++) { xy[2 * k] = coord(w); xy[2 * k + 1] = coord(h); }
+    if (u(rng) < 0.1) xy[2] = xy[0];
+    const uint8_t c[4] = {0, 4, 4, 4};
+    const int r = same_segments_routed(xy, c, w, h, rng);
+    if (r < 0 && ++fails <= 15) printf("mismatch: routed piece of curve %d\n", it);
+    if (r > 0) routed += r;
+  }
+  printf("routed pieces of clipped curves %ld\n", routed);
   printf("curves %d mismatches %ld\n", n, fails);
   return fails ? 1 : 0;
 }
