@@ -574,14 +574,16 @@ __global__ void __launch_bounds__(128) curve_split_kernel(FrameView f) {
   if (lane == 0 && rows) atomicAdd(f.totals + 1, rows);
 }
 
-// The cubic pieces inside the clip box, flattened as subdivision trees (eb::TreeNode) whose nodes
-// the lanes of a warp share. A lane splits its node, goes on with the left half and keeps the
+// The cubic pieces the safe loop flattens (those of curves inside the clip box, and the inside
+// pieces of clipped curves: eb::piece_flattens_safe), flattened as subdivision trees (eb::TreeNode)
+// whose nodes the lanes of a warp share. A lane splits its node, goes on with the left half and keeps the
 // right half on its own stack, unless a lane of the warp is out of work: then the right half goes
 // to that lane through shared memory. So lanes do not sit idle while other lanes' trees still have
 // nodes, and the FP64 instructions (whose cost to the pipe does not depend on the active lanes)
 // serve more of them. The segments are those of the loop flattener, in another order; they are
 // appended for the warp with one atomic per step, and each lane accumulates the command bounds
 // finish_curve would for the run of segments it emits for one command.
+
 // Idle lanes a warp of the tree flattener waits for before it takes new pieces, and its blocks per
 // SM: refills of 16, 24 and 32 lanes and 3, 4 and 6 blocks measured within 1 % of each other on the
 // batched workload (215.6-218.6 ms per step); 16 was the best on the curves frame (2.60 ms).
