@@ -806,13 +806,14 @@ __global__ void __launch_bounds__(kCurveThreads) edge_pieces_kernel(FrameView f)
 __global__ void __launch_bounds__(256) edge_items_kernel(FrameView f) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t rows = 0;
+  bool emitted = false;                        // the lane built an item whose segments count
+  eb::Builder b;
   const uint32_t n_items = min(f.work_counter[1], f.item_capacity);
   if (t < n_items) {
     const DevItem it = f.items[t];
     const DevCmd cmd = f.cmds[it.cmd];
     const DevCanvas cv = f.canvases[cmd.canvas];
     const DevXform xf = f.xforms[cmd.xform];
-    eb::Builder b;
     init_builder(b, cv);
     b.sink.init(f.segs, f.seg_meta, f.totals + 0, f.seg_capacity, it.cmd);
     eb::Src src;
@@ -839,26 +840,55 @@ __global__ void __launch_bounds__(256) edge_items_kernel(FrameView f) {
       if (it.kind == kItemCubic) eb::curve_to<3>(b, src, a, a_flags, false);
       else eb::curve_to<2>(b, src, a, a_flags, it.kind == kItemConic);
     }
-    uint32_t* status = &f.cmds_rw[it.cmd].status;
     if (rc) {
-      atomicOr(status, kCmdInvalid);
+      atomicOr(&f.cmds_rw[it.cmd].status, kCmdInvalid);
     }
     else {
       if (it.kind != kItemWhole) b.done();
-      b.sink.flush();
-      if (b.sink.n) {
-        int4* bb = f.cmd_bbox + it.cmd;
-        atomicMin(&bb->x, b.sink.xmin);
-        atomicMin(&bb->y, b.sink.ymin);
-        atomicMax(&bb->z, b.sink.xmax);
-        atomicMax(&bb->w, b.sink.ymax);
-        atomicOr(status, kCmdHasSegments);
-        rows = b.sink.rows;
+      emitted = true;
+    }
+  }
+  // What is left in the lanes' sinks (a line item's one segment, mostly) goes out with one atomic
+  // for the warp, and the command bounds with one set of atomics per command of the warp (the
+  // items of a polygon or path sit in consecutive lanes): Sink::flush and finish_curve's work.
+  const int lane = threadIdx.x & 31;
+  const uint32_t nb = emitted ? uint32_t(b.sink.nb) : 0u;
+  uint32_t incl = nb;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+  if (total) {
+    uint32_t base = 0;
+    if (lane == 31) base = atomicAdd(f.totals + 0, total);
+    base = __shfl_sync(0xFFFFFFFFu, base, 31) + incl - nb;
+    for (uint32_t k = 0; k < nb; k++) {
+      if (base + k < f.seg_capacity) {
+        f.segs[base + k] = b.sink.buf[k];
+        f.seg_meta[base + k] = (b.sink.cmd << 1) | b.sink.sbuf[k];
       }
     }
   }
+  const bool has = emitted && b.sink.n;
+  const uint32_t key = has ? b.sink.cmd : 0xFFFFFFFFu;
+  const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+  if (has) {
+    const int x0 = __reduce_min_sync(peers, b.sink.xmin), y0 = __reduce_min_sync(peers, b.sink.ymin);
+    const int x1 = __reduce_max_sync(peers, b.sink.xmax), y1 = __reduce_max_sync(peers, b.sink.ymax);
+    if (lane == __ffs(peers) - 1) {
+      int4* bb = f.cmd_bbox + key;
+      atomicMin(&bb->x, x0);
+      atomicMin(&bb->y, y0);
+      atomicMax(&bb->z, x1);
+      atomicMax(&bb->w, y1);
+      atomicOr(&f.cmds_rw[key].status, kCmdHasSegments);
+    }
+    rows = b.sink.rows;
+  }
   rows = __reduce_add_sync(0xFFFFFFFFu, rows);
-  if ((threadIdx.x & 31) == 0 && rows) atomicAdd(f.totals + 1, rows);
+  if (lane == 0 && rows) atomicAdd(f.totals + 1, rows);
 }
 
 // ---------------------------------------------------------------------------------------------
