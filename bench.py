@@ -501,7 +501,10 @@ def batch_record(args, dist, local, cpu: bool) -> dict:
         if errors:
             raise errors[0]
 
-    e2e_steps(max(args.warmup, 4))
+    # two warm-up steps per runtime at least: a runtime's first graph-frame call renders eagerly to
+    # size its arrays, and its second grows them to capacity and captures the graph (frees and
+    # allocations that wait for the whole device); neither belongs in the timed steps
+    e2e_steps(max(args.warmup, 2 * E2E_RUNTIMES))
     g0 = sum(int(r_.stats().graph_frames) for r_ in rts)
     dist.barrier()
     clocks = ClockSampler(local).start()
