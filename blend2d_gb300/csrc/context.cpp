@@ -1552,7 +1552,11 @@ BLGPU_API BLGpuResult blgpu_render_batch(BLGpuRuntime* rt, const void* const* st
   for (uint32_t i = 0; i < count; i++) total_bytes += sizes[i];
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
   const unsigned nt = std::max(1u, std::min({hw, 32u, (count + 7u) / 8u}));
-  while (rt->batch_parts.size() < nt) rt->batch_parts.emplace_back(new Frame(false));
+  // the parts' vertices in page-locked memory: the merged frame uploads them from there
+  while (rt->batch_parts.size() < nt) {
+    rt->batch_parts.emplace_back(new Frame(false));
+    rt->batch_parts.back()->verts.pinned = rt->batch_parts.back()->path_cmds.pinned = true;
+  }
   std::vector<uint32_t> first(nt + 1, count);
   first[0] = 0;
   {

@@ -79,6 +79,7 @@ void Frame::clear() {
   verts.clear(); path_cmds.clear(); lut_jobs.clear(); stops.clear(); images.clear();
   stroke_figs.clear(); stroke_params.clear(); stroke_xy.clear(); stroke_cmds.clear();
   image_words = 0; lut_words = 0; tiles = 0; rows = 0;
+  vert_parts.clear(); ext_verts = 0;
   generation = next_generation();
 }
 
@@ -151,9 +152,23 @@ void Frame::merge(Frame* const* parts, size_t count, unsigned threads) {
     acc.param += f.stroke_params.size(); acc.stroke_vert += f.stroke_cmds.size();
     acc.image_words += f.image_words; acc.lut_words += f.lut_words; acc.tiles += f.tiles; acc.rows += f.rows;
   }
+  // vertices recorded in page-locked memory stay where they are (uploaded part by part)
+  bool refer_verts = true;
+  for (size_t p = 0; p < count; p++) {
+    const Frame& f = *parts[p];
+    if (!f.path_cmds.empty() && !(f.verts.ptr_pinned && f.path_cmds.ptr_pinned)) refer_verts = false;
+  }
   clear();
   cmds.resize_uninit(acc.cmd); styles.resize_uninit(acc.style); xforms.resize_uninit(acc.xform);
-  verts.resize_uninit(2 * acc.vert); path_cmds.resize_uninit(acc.vert); lut_jobs.resize_uninit(acc.lut_job);
+  if (refer_verts) {
+    for (size_t p = 0; p < count; p++)
+      if (!parts[p]->path_cmds.empty()) vert_parts.push_back(parts[p]);
+    ext_verts = acc.vert;
+  }
+  else {
+    verts.resize_uninit(2 * acc.vert); path_cmds.resize_uninit(acc.vert);
+  }
+  lut_jobs.resize_uninit(acc.lut_job);
   stops.resize_uninit(acc.stop); stroke_figs.resize_uninit(acc.fig); stroke_params.resize_uninit(acc.param);
   stroke_xy.resize_uninit(2 * acc.stroke_vert); stroke_cmds.resize_uninit(acc.stroke_vert);
   canvases.resize(acc.canvas);
@@ -194,7 +209,7 @@ void Frame::merge(Frame* const* parts, size_t count, unsigned threads) {
       canvases[o.canvas + i] = cv;
       targets[o.canvas + i] = f.targets[i];
     }
-    if (f.path_cmds.size()) {
+    if (f.path_cmds.size() && !refer_verts) {
       memcpy(&verts[2 * o.vert], f.verts.data(), sizeof(double) * f.verts.size());
       memcpy(&path_cmds[o.vert], f.path_cmds.data(), f.path_cmds.size());
     }
@@ -349,7 +364,7 @@ BLGpuResult Runtime::prepare_strokes(const Frame& fr, FrameView& v, uint32_t& ou
   outline_verts = 0;
   const uint32_t nf = uint32_t(fr.stroke_figs.size());
   v.num_stroke_figs = nf;
-  v.stroke_vert_base = uint32_t(fr.verts.size() / 2);
+  v.stroke_vert_base = uint32_t(fr.vertex_count());
   if (!nf) return BLGPU_SUCCESS;
   // Thread order: a counting sort by vertex count (larger first), join and caps, so a warp's
   // figures run the same branches and loops of similar length (the stroker is FP64-bound and a
@@ -420,7 +435,7 @@ cudaError_t Runtime::put_counts(const Frame& fr, uint32_t* dev) {
   c[kCntRows] = fr.rows;
   c[kCntLutJobs] = uint32_t(fr.lut_jobs.size());
   c[kCntStrokeFigs] = uint32_t(fr.stroke_figs.size());
-  c[kCntStrokeVertBase] = uint32_t(fr.verts.size() / 2);
+  c[kCntStrokeVertBase] = uint32_t(fr.vertex_count());
   h2d_bytes += sizeof(uint32_t) * kCntWords;
   return cudaMemcpyAsync(dev, c, sizeof(uint32_t) * kCntWords, cudaMemcpyHostToDevice, stream);
 }
@@ -435,8 +450,8 @@ FrameSizes sizes_of(const Frame& fr, uint32_t outline_verts) {
   z.stops = uint32_t(fr.stops.size());
   z.tiles = fr.tiles;
   z.rows = fr.rows;
-  z.vert_words = fr.verts.size() + 2 * uint64_t(outline_verts);
-  z.cmd_bytes = fr.path_cmds.size() + uint64_t(outline_verts);
+  z.vert_words = 2 * fr.vertex_count() + 2 * uint64_t(outline_verts);
+  z.cmd_bytes = fr.vertex_count() + uint64_t(outline_verts);
   z.image_words = fr.image_words;
   z.lut_words = fr.lut_words;
   for (const FrameTarget& t : fr.targets)
@@ -552,7 +567,7 @@ BLGpuResult Runtime::upload_frame(const Frame& fr, const FrameSizes* caps) {
   needs_pack(fr.styles.ptr_pinned, sizeof(DevStyle) * fr.styles.size());
   needs_pack(fr.xforms.ptr_pinned, sizeof(DevXform) * fr.xforms.size());
   needs_pack(fr.verts.ptr_pinned, sizeof(double) * fr.verts.size());
-  needs_pack(fr.path_cmds.ptr_pinned, fr.path_cmds.size());
+  needs_pack(fr.path_cmds.ptr_pinned, fr.path_cmds.size());     // (a merged frame's vert_parts are page-locked)
   needs_pack(fr.lut_jobs.ptr_pinned, sizeof(DevLutJob) * fr.lut_jobs.size());
   needs_pack(fr.stops.ptr_pinned, sizeof(DevStop) * fr.stops.size());
   for (const FrameImage& im : fr.images)
@@ -592,6 +607,14 @@ BLGpuResult Runtime::upload_frame(const Frame& fr, const FrameSizes* caps) {
   BLGPU_CHECK(put(v.canvases, cvs.data(), sizeof(DevCanvas) * ncv, false));
   BLGPU_CHECK(put(v.verts, fr.verts.data(), sizeof(double) * fr.verts.size(), fr.verts.ptr_pinned));
   BLGPU_CHECK(put(v.path_cmds, fr.path_cmds.data(), fr.path_cmds.size(), fr.path_cmds.ptr_pinned));
+  {
+    size_t at = fr.verts.size() / 2;
+    for (const Frame* p : fr.vert_parts) {
+      BLGPU_CHECK(put(v.verts + 2 * at, p->verts.data(), sizeof(double) * p->verts.size(), true));
+      BLGPU_CHECK(put(v.path_cmds + at, p->path_cmds.data(), p->path_cmds.size(), true));
+      at += p->path_cmds.size();
+    }
+  }
   BLGPU_CHECK(put(v.lut_jobs, fr.lut_jobs.data(), sizeof(DevLutJob) * fr.lut_jobs.size(), fr.lut_jobs.ptr_pinned));
   BLGPU_CHECK(put(v.stops, fr.stops.data(), sizeof(DevStop) * fr.stops.size(), fr.stops.ptr_pinned));
   for (const FrameImage& im : fr.images) {
@@ -959,7 +982,7 @@ BLGpuResult Runtime::run_graph(const Frame& fr) {
   stats.fill_commands = fr.cmds.size();
   stats.segments = t.segs;
   stats.tiles = fr.tiles;
-  stats.input_vertices = uint64_t(fr.verts.size() / 2);
+  stats.input_vertices = fr.vertex_count();
   stats.h2d_bytes = h2d_bytes;
   stats.d2h_bytes = d2h_bytes;
   last_frame_bytes = in_bytes + measure.off + uint64_t(caps.dyn.segs) * (sizeof(DevSeg) + sizeof(uint32_t));
@@ -1028,7 +1051,7 @@ BLGpuResult Runtime::run_eager(const Frame& fr) {
   if (host_totals[20]) return BLGPU_ERROR_DATA_TOO_LARGE;   // a work array overflowed: pixels invalid
   has_frame = true;
   read_pixel_ops();
-  stats.input_vertices = uint64_t((fr.verts.size() + fr.stroke_xy.size()) / 2);
+  stats.input_vertices = fr.vertex_count() + uint64_t(fr.stroke_xy.size() / 2);
   stats.h2d_bytes = h2d_bytes;
   stats.d2h_bytes = d2h_bytes + 32;
 

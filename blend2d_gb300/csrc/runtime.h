@@ -125,6 +125,12 @@ struct Frame {
   uint32_t lut_words = 0;
   uint32_t tiles = 0, rows = 0;
   uint64_t generation = next_generation();   // renewed by clear(); per-frame registrations compare against it
+  // A merged frame's vertices stay in the parts it was made of when those hold them in page-locked
+  // memory: `vert_parts` lists them in order (uploaded by DMA from there) and `ext_verts` counts
+  // their vertices, which follow the frame's own `verts` (empty then).
+  std::vector<const Frame*> vert_parts;
+  uint64_t ext_verts = 0;
+  uint64_t vertex_count() const { return verts.size() / 2 + ext_verts; }
 
   static uint64_t next_generation();
   void clear();
@@ -134,7 +140,9 @@ struct Frame {
   uint64_t add_image(const BLGpuImage& image);
   // Replaces this frame's content with the concatenation of `parts` (frames recorded on their
   // own, e.g. by several threads), shifting every index a part holds by what the parts before it
-  // hold. The copies run on up to `threads` threads.
+  // hold. The copies run on up to `threads` threads. Vertices held in page-locked memory by every
+  // part are not copied but referenced (`vert_parts`): the parts must then stay unchanged until the
+  // frame has been uploaded.
   void merge(Frame* const* parts, size_t count, unsigned threads);
 };
 
