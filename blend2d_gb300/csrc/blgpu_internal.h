@@ -143,7 +143,7 @@ struct alignas(16) DevCmd {
   uint32_t seg_first;      // K1 output
   uint32_t seg_count;
   uint32_t status;         // after binning: 0 ok, 1 invalid geometry (NaN), 2 nothing to render
-  uint32_t pad;
+  uint32_t color;          // solid styles: the premultiplied colour (their style entry is shared and carries none)
 };
 
 struct alignas(16) DevCanvas {

@@ -236,7 +236,10 @@ struct BLGpuContext {
   // --- frame registration ---------------------------------------------------------------
 
   // The style's index in the frame; `xrgb_read`: the copy whose pattern fetches set the alpha byte.
+  // Solid styles take the context's one solid entry: their colour travels in the command
+  // (DevCmd::color, from Fill::color).
   uint32_t register_style(CtxStyle& cs, bool xrgb_read = false) {
+    if (cs.hs.dev.fetch == kFetchSolid) return register_solid_style();
     xrgb_read = xrgb_read && cs.hs.dev.fetch >= kFetchPatAlignedPad;
     if (!xrgb_read && cs.frame_gen == frame->generation) return cs.frame_index;
     if (xrgb_read && cs.frame_gen_x == frame->generation) return cs.frame_index_x;
@@ -269,7 +272,9 @@ struct BLGpuContext {
     return uint32_t(frame->styles.size() - 1);
   }
 
-  uint32_t register_clear_style() {
+  // The frame entry of every solid fill of this context (and of clear_all / clear_rect, whose
+  // colour is 0).
+  uint32_t register_solid_style() {
     if (clear_style_gen == frame->generation) return clear_style_index;
     DevStyle d{};
     d.fetch = kFetchSolid;
@@ -336,21 +341,26 @@ struct BLGpuContext {
     return uint32_t(frame->xforms.size() - 1);
   }
 
-  DevCmd& push_cmd(uint32_t kind, uint32_t style, bool src_copy, uint32_t alpha) {
+  // A resolved fill: the style's frame index, SrcCopy (else SrcOver), the fill alpha and, for a
+  // solid style, its premultiplied colour.
+  struct Fill { uint32_t style; bool src_copy; uint32_t alpha; uint32_t color = 0; };
+
+  static uint32_t style_color(const CtxStyle& cs) { return cs.hs.dev.fetch == kFetchSolid ? cs.hs.dev.solid : 0u; }
+
+  DevCmd& push_cmd(uint32_t kind, const Fill& f) {
     DevCmd c{};
     c.kind = kind;
     c.canvas = canvas;
-    c.style = style;
-    c.flags = src_copy ? 1u : 0u;
-    c.alpha = alpha;
+    c.style = f.style;
+    c.flags = f.src_copy ? 1u : 0u;
+    c.alpha = f.alpha;
+    c.color = f.color;
     frame->cmds.push_back(c);
     frame->canvases[canvas].cmd_count++;
     return frame->cmds.back();
   }
 
   // --- fill resolution --------------------------------------------------------------------
-
-  struct Fill { uint32_t style; bool src_copy; uint32_t alpha; };
 
   // Returns false for a NOP fill or stroke (no alpha, no style, or a comp-op that simplifies to
   // DstCopy) of the fill (slot 0) or stroke (slot 1) style.
@@ -362,11 +372,12 @@ struct BLGpuContext {
     if (!simplify_comp_op(target.format, s.comp_op, cs.hs.format, f.src_copy, xrgb_read)) return false;
     f.alpha = alpha;
     f.style = register_style(cs, xrgb_read);
+    f.color = style_color(cs);
     return true;
   }
 
   void fill_box_a(const Fill& f, int x0, int y0, int x1, int y1) {
-    DevCmd& c = push_cmd(kFillBoxA, f.style, f.src_copy, f.alpha);
+    DevCmd& c = push_cmd(kFillBoxA, f);
     c.box[0] = x0; c.box[1] = y0; c.box[2] = x1; c.box[3] = y1;
     c.fetch_y0 = y0;
   }
@@ -400,14 +411,14 @@ struct BLGpuContext {
       if (!m_last) row_y1--;
       if (!(row_y0 < row_y1) || (w == 1 && m_mid == 0)) return;
     }
-    DevCmd& c = push_cmd(kFillBoxU, f.style, f.src_copy, f.alpha);
+    DevCmd& c = push_cmd(kFillBoxU, f);
     c.box[0] = x0; c.box[1] = y0; c.box[2] = x1; c.box[3] = y1;
     c.fetch_y0 = int32_t(row_y0);
   }
 
   void fill_analytic(const Fill& f, const double* xy, const uint8_t* cmds, size_t n, uint32_t fill_rule,
                      uint32_t xform) {
-    DevCmd& c = push_cmd(kFillAnalytic, f.style, f.src_copy, f.alpha);
+    DevCmd& c = push_cmd(kFillAnalytic, f);
     c.flags |= fill_rule == 1 ? 2u : 0u;
     c.geom = cmds ? kGeomPath : kGeomPolygon;
     c.geom_first = uint32_t(frame->verts.size() / 2);
@@ -681,7 +692,7 @@ struct BLGpuContext {
 
   BLGpuResult clear_all() {
     if (!bound) return BLGPU_ERROR_INVALID_STATE;
-    Fill f{register_clear_style(), true, 255};
+    Fill f{register_solid_style(), true, 255};
     fill_box_a(f, 0, 0, w, h);
     return BLGPU_SUCCESS;
   }
@@ -791,7 +802,7 @@ struct BLGpuContext {
     else {
       xform = register_xform_at(origin, false);
     }
-    DevCmd& c = push_cmd(kFillAnalytic, f.style, f.src_copy, f.alpha);   // non-zero
+    DevCmd& c = push_cmd(kFillAnalytic, f);   // non-zero
     c.geom = kGeomPath;
     c.geom_first = 0;                  // the outline's range is set on the device
     c.geom_count = 0;
@@ -876,6 +887,7 @@ struct BLGpuContext {
     blit_style.frame_gen = 0;
     blit_style.frame_gen_x = 0;
     f.style = register_style(blit_style, xrgb_read);
+    f.color = style_color(blit_style);
     return true;
   }
 
@@ -978,7 +990,7 @@ struct BLGpuContext {
   void record_mask(const Fill& f, int x0, int y0, int x1, int y1, const BLGpuImage& mask, int mx, int my) {
     const uint64_t words = frame->add_image(mask);
     const uint64_t off = words * 4u + uint64_t(uint32_t(my)) * uint32_t(mask.width) + uint32_t(mx);
-    DevCmd& c = push_cmd(kFillMaskA, f.style, f.src_copy, f.alpha);
+    DevCmd& c = push_cmd(kFillMaskA, f);
     c.box[0] = x0; c.box[1] = y0; c.box[2] = x1; c.box[3] = y1;
     c.fetch_y0 = y0;
     c.geom_first = uint32_t(off);

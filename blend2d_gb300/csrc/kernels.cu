@@ -1219,7 +1219,7 @@ __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
       f.row_box[out + pos] = make_uint2(f.cmd_xr[c], f.cmd_yr[c]);
       rec[0] = make_uint4(c, f.cmd_xr[c], f.cmd_yr[c], meta);
       rec[1] = make_uint4(f.cmdrow_base[c], (ctx & 0xFFFFu) | (((ctx >> 16) - (ctx & 0xFFFFu) + 1u) << 16),
-                          cmd.style | (solid ? kRecSolid : 0u), solid ? f.styles[cmd.style].solid : f.rs_base[c]);
+                          cmd.style | (solid ? kRecSolid : 0u), solid ? cmd.color : f.rs_base[c]);
     }
     out += total;
   }
