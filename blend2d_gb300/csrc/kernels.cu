@@ -1209,8 +1209,9 @@ __global__ void row_fill_kernel(FrameView f, const uint32_t* row_canvas) {
     if (flag) {
       // everything the composite needs of the command to test it against a strip and find its
       // slot, gathered once here for every strip of the list row
-      // A solid style's colour takes the place of the row-state base it does not use, with bit 31
-      // of the style word saying so: the composite then loads neither the command nor the style.
+      // A solid fill's colour (DevCmd::color) takes the place of the row-state base it does not
+      // use, with bit 31 of the style word saying so: the composite then loads neither the command
+      // nor the style.
       const DevCmd& cmd = f.cmds[c];
       const uint32_t ctx = f.cmd_tile_x[c];
       const uint32_t meta = cmd.kind | (cmd.flags << 2) | (cmd.alpha << 4);
