@@ -1116,18 +1116,21 @@ __global__ void slot_compact_kernel(FrameView f) {
   if (i == n - 1) f.totals[5] = f.cmdrow_offsets[i] + (f.cmdrow_counts[i] ? 1u : 0u);
 }
 
-// Prefix of the backdrop deltas over the tile columns of every (command, strip row, row).
-__global__ void backdrop_prefix_kernel(FrameView f) {
+// Prefix of the backdrop deltas over the tile columns of every (command, strip row, row): one
+// warp per command (most commands are a few strip rows tall), nothing to do for one column.
+constexpr uint32_t kPrefixWarps = 8;
+__global__ void __launch_bounds__(32 * kPrefixWarps) backdrop_prefix_kernel(FrameView f) {
   if (frame_skipped(f)) return;
-  uint32_t c = blockIdx.x;
+  const uint32_t c = blockIdx.x * kPrefixWarps + (threadIdx.x >> 5);
   if (c >= f.counts[kCntCmds]) return;
-  uint32_t ctx = f.cmd_tile_x[c];
+  const uint32_t ctx = f.cmd_tile_x[c];
   if (ctx == 0xFFFFFFFFu || f.cmds[c].kind != kFillAnalytic) return;
   const uint32_t ntx = (ctx >> 16) - (ctx & 0xFFFFu) + 1u;
+  if (ntx == 1) return;
   const uint32_t yr = f.cmd_yr[c];
   const uint32_t nsr = ((yr >> 16) >> kStripShift) - ((yr & 0xFFFFu) >> kStripShift) + 1u;
   const uint32_t base = f.cmdrow_base[c];
-  for (uint32_t i = threadIdx.x; i < nsr * kStripRows; i += blockDim.x) {
+  for (uint32_t i = threadIdx.x & 31u; i < nsr * kStripRows; i += 32u) {
     uint32_t sr = i / kStripRows, row = i % kStripRows;
     uint32_t* bd = f.backdrop + size_t(base + sr * ntx) * kStripRows + row;
     uint32_t acc = 0;
@@ -1180,7 +1183,7 @@ int launch_frame_gate(const FrameView& f, cudaStream_t st) {
 
 int launch_backdrop_prefix(const FrameView& f, cudaStream_t st) {
   if (!f.num_cmds || !f.num_cmdrows) return 0;
-  backdrop_prefix_kernel<<<f.num_cmds, 64, 0, st>>>(f);
+  backdrop_prefix_kernel<<<(f.num_cmds + kPrefixWarps - 1) / kPrefixWarps, 32 * kPrefixWarps, 0, st>>>(f);
   return 1;
 }
 
